@@ -1,0 +1,329 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 shot-profile migration: shot*omega*depth-steps per second.
+
+Workload (default "survey64"): the 2-D PSPI survey -- velocity 500 x 1024 at 10 m
+(seeded Gaussian random field), 64 shots with receiver apertures of 200..800
+traces, nt=1500 at 2 ms, 5-50 Hz (271 frequencies), 8 reference velocities,
+padx=padt=2 (2048-point rows). One step = one migration of the whole survey
+(8,672,000 units: 64 shots x 271 frequencies x 500 depth steps).
+
+  value  units/s with the traces already in device memory (wem_migrate_device),
+         CUDA events on the library's stream around exactly K steps;
+  e2e    the same through the public C ABI with host buffers (wem_migrate): the
+         H2D copy of the traces, all kernels and the D2H copy of the image;
+  roofline  the depth-recursion kernel: algorithmic FLOPs per unit x units / its
+         event-timed duration;
+  cpu_baseline  the reference's CPU algorithm on this machine's host cores on a
+         bounded sample (one shot of the survey, all its frequencies).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--workload split1]
+Under torchrun each rank migrates its own copy of the survey (weak scaling); no
+collective is on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "seismic.jl_gb300"))
+
+import numpy as np  # noqa: E402
+
+
+def survey(workload: str, rank: int):
+    from wemgpu import synth
+    if workload == "survey64":
+        c = synth.config1(seed=1001 + rank)
+        wl = "2-D PSPI survey: 64 shots, 500x1024 grid @10 m, nref=8, 5-50 Hz, nt=1500, padx=padt=2"
+    elif workload == "survey8":
+        c = synth.config1(seed=1001 + rank, nshot=8)
+        wl = "2-D PSPI survey subset for profiling: 8 shots, 500x1024 grid @10 m, nref=8, 5-50 Hz, nt=1500"
+    elif workload == "split1":
+        c = synth.config0(seed=1000 + rank)
+        wl = "2-D split-step: 1 shot, 200x256 grid @10 m, 3 layers, 5-60 Hz, nt=1000, padx=padt=2"
+    else:
+        raise SystemExit(f"unknown workload {workload}")
+    return c, wl
+
+
+def band(p: dict):
+    """Number of frequencies the reference processes (wem.c:79-89, float arithmetic)."""
+    f32 = np.float32
+    nt, padt, dt = int(p["nt"]), int(p["padt"]), f32(p["dt"])
+    ntfft = int(f32(2 * padt) * f32(nt) / f32(2))
+    nw = ntfft // 2 + 1
+    fmax, fmin = f32(p["fmax"]), f32(p["fmin"])
+    ifmax = int(f32(int(fmax)) * dt * f32(ntfft) + f32(1)) if fmax * dt * f32(ntfft) + f32(1) < nw else nw
+    ifmin = int(f32(int(fmin)) * dt * f32(ntfft)) if fmin * dt * f32(ntfft) + f32(1) < ifmax else 0
+    return ifmax - ifmin
+
+
+def flops_per_unit(p: dict) -> float:
+    """Algorithmic FLOPs of one (shot, frequency, depth step): source and receiver
+    continuation plus the imaging condition, 5 N log2 N per complex FFT.
+    PSPI:  per wavefield 5N log2N + R (6N + 5N log2N) + 8n;  unit = 2 F + 3n.
+    Split-step: per wavefield 2 * 5N log2N + 6N + 14n;     unit = 2 F + 3n."""
+    n = int(p["nmx"])
+    N = int(p["padx"]) * n
+    lg = math.log2(N)
+    if int(p.get("pspi", 1)):
+        R = int(p["nref"])
+        F = 5 * N * lg + R * (6 * N + 5 * N * lg) + 8 * n
+    else:
+        F = 2 * 5 * N * lg + 6 * N + 14 * n
+    return 2 * F + 3 * n
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.device), "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def recorded_traffic():
+    """Per-launch DRAM bytes of the depth-recursion kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "migrate_kernel_traffic.json")) as f:
+            t = json.load(f)
+        return t
+    except Exception:
+        return None
+
+
+def cpu_baseline(c, seconds_hint: float = 20.0):
+    """The reference's CPU algorithm on one shot of the survey (every frequency), all
+    host cores. oracle/_ref (the reference's own C core) when it was built on this
+    machine, else the oracle port of it."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from wemgpu import synth
+    O.build()
+    p = dict(c["params"])
+    shots = c["shots"]
+    s = shots.nshot // 2
+    p["sx"] = float(shots.sx[s])
+    d = synth.shot_gather_full(shots, s, p["nmx"])
+    cores = os.cpu_count() or 1
+    kind = "reference" if O.ref_available() else "port"
+    t0 = time.perf_counter()
+    if kind == "reference":
+        O.wem_ref(p, c["vel"], c["wav"], d=d, adj=True)
+        cores = O.omp_threads()
+    else:
+        O.wem_port(p, c["vel"], c["wav"], d=d, adj=True, nthreads=cores)
+    dt = time.perf_counter() - t0
+    units = band(p) * int(p["nz"])
+    return {"value": units / dt, "unit": "shot*omega*depth-steps/s", "cores": cores, "kind": kind,
+            "sample": f"1 of {shots.nshot} shots, all {band(p)} frequencies x {p['nz']} depth steps "
+                      f"({units} units) in {dt:.1f} s"}
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    c, wl = survey(args.workload, 0)
+    p = c["params"]
+    nf = band(p)
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        info = cpu_baseline(c)
+        if i >= args.warmup:
+            vals.append(info["value"])
+    v = statistics.mean(vals)
+    info["value"] = v
+    line = {"impl": "reference", "metric": "shot*omega*depth-steps/s", "value": v, "unit": "shot*omega*depth-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * (nf * int(p["nz"])) / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": wl, "step": "one shot of the survey on the host cores"},
+            "cpu_baseline": info,
+            "e2e": {"value": v, "unit": "shot*omega*depth-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="survey64", choices=["survey64", "survey8", "split1"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    if args.warmup < 3:
+        args.warmup = 3
+
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import wemgpu
+    if not os.path.exists(wemgpu.LIB_PATH):
+        raise SystemExit("shotwem.so is not built: python -c 'import __graft_entry__ as g; g.build()'")
+    c, wl = survey(args.workload, rank)
+    p, shots = c["params"], c["shots"]
+    nf, nz, nshot = band(p), int(p["nz"]), shots.nshot
+    units = nshot * nf * nz
+    ctx = wemgpu.Context(local).prepare(p, c["vel"], c["wav"])
+    d_dev = torch.from_numpy(np.ascontiguousarray(shots.data)).to(dev)
+    m_dev = torch.empty((int(p["nmx"]), nz), dtype=torch.float32, device=dev)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
+
+    for _ in range(args.warmup):
+        ctx.migrate_device(shots, d_dev.data_ptr(), m_dev.data_ptr(), sync=True)
+    kernels_per_step = ctx.last_timing()[1]
+
+    sampler = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    kms = []
+    ev0.record(stream)
+    for _ in range(args.steps):
+        ctx.migrate_device(shots, d_dev.data_ptr(), m_dev.data_ptr(), sync=True)
+        kms.append(ctx.last_kernel_times())
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    elapsed = ev0.elapsed_time(ev1) / 1000.0
+    t = torch.tensor([elapsed], dtype=torch.float64, device=dev)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    elapsed = float(t.item())
+    value = world * units * args.steps / elapsed
+
+    # end to end through the public API with host buffers
+    e2e_t = []
+    img = np.zeros((int(p["nmx"]), nz), np.float32)
+    for _ in range(max(1, args.e2e_steps)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        img = ctx.migrate(shots)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_t)
+    te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
+    if dist:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_s = float(te.item())
+    h2d = int(shots.data.nbytes)
+    d2h = int(img.nbytes)
+
+    mig_ms = statistics.mean(k[1] for k in kms)
+    fl = flops_per_unit(p)
+    achieved = units * fl / (mig_ms / 1000.0) / 1e12
+    peaks, src = measured_peaks()
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    props = torch.cuda.get_device_properties(dev)
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    fp32_nominal = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+    tr = recorded_traffic()
+    traffic = None
+    if tr and tr.get("workload") == args.workload:
+        traffic = tr.get("bytes_per_launch")
+
+    line = {
+        "metric": "shot*omega*depth-steps/s", "value": value, "unit": "shot*omega*depth-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": wl, "units_per_step_per_gpu": units, "shots": nshot, "frequencies": nf,
+                   "depth_steps": nz, "pspi": int(p["pspi"]), "nref": int(p["nref"]), "nkx": int(p["padx"]) * int(p["nmx"]),
+                   "interp": p.get("interp", "ref"), "l2": "inputs larger than L2 (traces, spectra, image accumulators)",
+                   "parallelism": f"replicas x{world}, shots sharded by rank"},
+        "e2e": {"value": world * units / e2e_s, "unit": "shot*omega*depth-steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": kernels_per_step * args.steps,
+        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": f"bf16 dense, {src}",
+                     "kernel": "wem_migrate_kernel", "ms_per_launch": mig_ms,
+                     "flops_per_unit": fl, "fp32_nominal_tflops": fp32_nominal,
+                     "fp32_frac": achieved / fp32_nominal},
+        "kernel_ms": {"spectra": statistics.mean(k[0] for k in kms), "extrapolate": mig_ms,
+                      "reduce": statistics.mean(k[2] for k in kms)},
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(c)
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,145 @@
+/*
+ * shotwem_gb300.h -- C ABI of the GB300 shot-profile wave-equation migration library
+ * (shotwem.so). Plain pointers and sizes only; every entry returns an int status.
+ *
+ * Drop-in entry points (same names and argument meaning as the reference's C core):
+ *   main(argc, argv)   replaces src/Imaging/c/shotwem.c:12 (the symbol the Julia
+ *                      wrapper binds: src/Imaging/ShotProfileWEM.jl:347
+ *                      ccall((:main,"shotwem"), Int32, (Int32, Ptr{Ptr{UInt8}}), ...));
+ *                      exported by the library, also available as shotwem_main.
+ *   wem(...)           replaces src/Imaging/c/wem.h:3-11 / wem.c:3-204.
+ * Batched entry points (no reference counterpart; they let one call migrate or
+ * model every shot of a survey on one GPU instead of one process per shot,
+ * src/Imaging/ShotProfileWEM.jl:104-106 and :288-290):
+ *   wem_ctx_create / wem_prepare / wem_migrate / wem_model / wem_ctx_destroy.
+ *
+ * Array layouts follow the reference's float** arrays (first index slowest, n1
+ * fastest): vel[ix][iz], m[ix][iz], d[ix][it], ix = imx*nmy + imy.
+ */
+#ifndef SHOTWEM_GB300_H
+#define SHOTWEM_GB300_H
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Only the functions below are exported from shotwem.so. */
+#if defined(__GNUC__)
+#define WEM_API __attribute__((visibility("default")))
+#else
+#define WEM_API
+#endif
+
+/* Status codes. The reference has none: wem() is void (wem.c:3), main() calls
+   exit(1) on a missing argument (shotwem.c:30-33) and SeisRead/SeisWrite only
+   printf on I/O failure (seismic.c:277-289, 323-337). */
+#define WEM_OK 0
+#define WEM_ERR_ARG (-1)      /* invalid or missing argument */
+#define WEM_ERR_SIZE (-2)     /* size this build does not support (e.g. nkx not a power of two) */
+#define WEM_ERR_CUDA (-3)     /* a CUDA runtime call failed */
+#define WEM_ERR_TIMEOUT (-4)  /* a bounded device-side wait ran out */
+#define WEM_ERR_IO (-5)       /* seis file could not be read or written */
+#define WEM_ERR_NOMEM (-6)    /* host or device allocation failed */
+#define WEM_ERR_NODEV (-7)    /* no CUDA device */
+
+/* PSPI interpolation between reference wavefields */
+#define WEM_INTERP_REF 0     /* the reference's arithmetic: wem.c:450-460 with linear_interp
+                                (wem.c:473-478) returning float -> real part of the
+                                nearest-lower reference wavefield */
+#define WEM_INTERP_LINEAR 1  /* complex linear interpolation, the formula of wem.c:476 */
+
+/* arithmetic of the depth-extrapolation FFTs */
+#define WEM_PREC_FP32 0      /* complex FP32 */
+
+typedef struct wem_ctx wem_ctx;
+
+/* Survey geometry and operator options; names and meaning as the arguments of
+   wem() (wem.h:3-11) and the key=value options of main() (shotwem.c:27-42). */
+typedef struct wem_params {
+    int nt;         /* time samples per trace (and of the wavelet) */
+    float ot, dt;
+    int nmx;        /* image/receiver grid, x */
+    float omx, dmx;
+    int nmy;        /* image/receiver grid, y (1 for 2-D) */
+    float omy, dmy;
+    int nz;         /* depth steps */
+    float oz, dz;
+    float gz, sz;   /* receiver and source depth */
+    int nref;       /* PSPI reference velocities per depth step (>= 2) */
+    float fmin, fmax;
+    int padt, padx; /* FFT padding factors for t and x/y */
+    int pspi;       /* 1: PSPI (wem.c:380), 0: split-step (wem.c:289) */
+    int interp;     /* WEM_INTERP_* */
+    int precision;  /* WEM_PREC_* */
+    int verbose;
+} wem_params;
+
+/* Last error message of the calling thread ("" if none). */
+WEM_API const char *wem_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+WEM_API int wem_version(void);
+
+/* A context owns a CUDA stream and the device buffers it reuses from call to call
+   (tables, spectra, image accumulators); device = CUDA ordinal. */
+WEM_API int wem_ctx_create(wem_ctx **ctx, int device);
+WEM_API int wem_ctx_destroy(wem_ctx *ctx);
+
+/* Build the per-velocity-model tables on the device: slowness split (wem.c:28-36),
+   reference velocities and interpolation indices (wem.c:40-70), frequency and
+   wavenumber grids (wem.c:79-89), wavelet spectrum (wem.c:112-119).
+   vel: [nmx*nmy][nz]; wav: [nt]. Later wem_migrate / wem_model calls with the
+   same ctx reuse them until the next wem_prepare. */
+WEM_API int wem_prepare(wem_ctx *ctx, const wem_params *p, const float *vel, const float *wav);
+
+/* Migration (adjoint, wem.c adj=true) of nshot shots, stacked into one image.
+   Shot s has sources at (sx[s], sy[s]) and traces trace_offset[s] ..
+   trace_offset[s+1]-1 of d ([ntrace][nt], host memory); trace i lies on grid
+   cell trace_cell[i] (= imx*nmy + imy). Grid cells without a trace carry zero
+   data, as the reference migrates the full grid for every shot (wem.c:122-133).
+   m: [nmx*nmy][nz] host memory, overwritten. sy may be NULL (all 0). */
+WEM_API int wem_migrate(wem_ctx *ctx, int nshot, const float *sx, const float *sy,
+                const int64_t *trace_offset, const int32_t *trace_cell,
+                const float *d, float *m);
+
+/* Same, with every array already in device memory (ctx's device), ordered on
+   ctx's stream; returns after enqueueing when sync == 0. */
+WEM_API int wem_migrate_device(wem_ctx *ctx, int nshot, const float *sx, const float *sy,
+                       const int64_t *trace_offset, const int32_t *trace_cell,
+                       const float *d_dev, float *m_dev, int sync);
+
+/* One-call convenience: wem_prepare + wem_migrate. */
+WEM_API int wem_migrate_survey(wem_ctx *ctx, const wem_params *p, const float *vel, const float *wav,
+                       int nshot, const float *sx, const float *sy, const int64_t *trace_offset,
+                       const int32_t *trace_cell, const float *d, float *m);
+
+/* Elapsed device time (ms) of the last wem_migrate* call's GPU work, from CUDA
+   events on ctx's stream; and how many kernels it launched. */
+WEM_API int wem_last_timing(wem_ctx *ctx, float *ms, int *kernels);
+
+/* Device time (ms) of each kernel of the last call: trace spectra, depth
+   recursion, image reduction (CUDA events around each launch). */
+WEM_API int wem_last_kernel_times(wem_ctx *ctx, float *ms_spectra, float *ms_extrapolate, float *ms_reduce);
+
+/* The cudaStream_t (as void*) on which ctx orders all its work. */
+WEM_API int wem_ctx_stream(wem_ctx *ctx, void **stream);
+
+/* Drop-in for the reference's wem() (wem.h:3-11). Same arguments, float** rows as
+   alloc2float builds them (seismic.c:92-106). Returns a status instead of void.
+   adj=true: d -> m (m overwritten); adj=false: m -> d (d overwritten). */
+WEM_API int wem(float **d, float **m, float **wav, int nt, float ot, float dt, int nmx, float omx,
+        float dmx, int nmy, float omy, float dmy, float sx, float sy, int nz, float oz, float dz,
+        float gz, float sz, float **vel, int nref, float fmin, float fmax, int padt, int padx,
+        bool adj, bool pspi, bool verbose);
+
+/* Drop-in for shotwem.c:12 main(): argv holds key=value strings (argv[0] ignored):
+   adj= pspi= nref= d= m= vel= wav= sx= sy= sz= gz= fmin= fmax= padt= padx= verbose=
+   (y/n booleans, seismic.c:41-55), plus interp=ref|linear. Reads and writes seis
+   files; returns a WEM_* status instead of calling exit(). */
+WEM_API int shotwem_main(int argc, char **argv);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

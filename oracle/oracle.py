@@ -74,6 +74,7 @@ def lib():
         L.wemo_fft_f32.argtypes = [_fp, _i, _i, _i]
         L.wemo_fft_f64.restype = _i
         L.wemo_fft_f64.argtypes = [_dp, _i, _i, _i]
+        L.wemo_omp_max_threads.restype = _i
         _lib = L
     return _lib
 
@@ -101,6 +102,11 @@ def ref_lib():
     return _ref
 
 
+def omp_threads() -> int:
+    """Threads an OpenMP region of this process gets (fixed at the runtime's start)."""
+    return int(lib().wemo_omp_max_threads())
+
+
 # --------------------------------------------------------------------------- FFT
 
 def fft_f32(x: np.ndarray, sign: int = -1) -> np.ndarray:
@@ -121,6 +127,11 @@ def fft_f64(x: np.ndarray, sign: int = -1) -> np.ndarray:
 
 
 # --------------------------------------------------------------------------- operator
+
+def _interp(p: dict) -> int:
+    v = p.get("interp", 0)
+    return {"ref": 0, "linear": 1}[v] if isinstance(v, str) else int(v)
+
 
 def _common(p: dict):
     return [int(p["nt"]), float(p.get("ot", 0.0)), float(p["dt"]),
@@ -144,7 +155,7 @@ def wem_port(p: dict, vel: np.ndarray, wav: np.ndarray, d: np.ndarray | None = N
                              *_common(p), vel.ctypes.data_as(_fp), int(p.get("nref", 5)),
                              float(p.get("fmin", 0.0)), float(p.get("fmax", 80.0)),
                              int(p.get("padt", 1)), int(p.get("padx", 1)), int(adj),
-                             int(p.get("pspi", 1)), int(p.get("interp", 0)), int(nthreads))
+                             int(p.get("pspi", 1)), _interp(p), int(nthreads))
     if rc != 0:
         raise ValueError(f"wem_port rejected the arguments (rc={rc})")
     return mm if adj else dd
@@ -162,7 +173,7 @@ def wem_fp64(p: dict, vel: np.ndarray, wav: np.ndarray, d: np.ndarray | None = N
                              *_common(p), vel.ctypes.data_as(_fp), int(p.get("nref", 5)),
                              float(p.get("fmin", 0.0)), float(p.get("fmax", 80.0)),
                              int(p.get("padt", 1)), int(p.get("padx", 1)), int(adj),
-                             int(p.get("pspi", 1)), int(p.get("interp", 0)), int(nthreads))
+                             int(p.get("pspi", 1)), _interp(p), int(nthreads))
     if rc != 0:
         raise ValueError(f"wem_fp64 rejected the arguments (rc={rc})")
     return mm if adj else dd

@@ -58,3 +58,15 @@ int wemo_fft_f64(double *data, int n, int howmany, int sign)
     od_plan_destroy(p);
     return 0;
 }
+
+/* OpenMP threads a parallel region of this process gets (the reference's
+   omp_thread_count(), wem.c:539-544); tests pass it to the port so both reduce
+   their per-thread image slices identically. */
+int wemo_omp_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}

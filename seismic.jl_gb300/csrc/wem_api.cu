@@ -1,0 +1,558 @@
+// wem_api.cu -- host runtime and C ABI of shotwem.so (declared in include/shotwem_gb300.h).
+//
+// The per-velocity tables are derived on the host with the reference's own float
+// arithmetic (wem.c:28-89, compiled with -ffp-contract=off so that no FMA changes a
+// rounding), exactly once per wem_prepare; everything per shot and per frequency
+// runs on the GPU: trace spectra (wem_spectra_kernel), the fused depth recursion
+// (wem_migrate_kernel) and the image reduction (wem_image_reduce_kernel).
+// There is no CPU fallback: without a CUDA device every entry point fails.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+#include <vector>
+
+#include "../../include/shotwem_gb300.h"
+#include "wem_internal.h"
+
+using namespace gbwem;
+
+static thread_local char g_err[512] = "";
+
+static int fail(int code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+#define CK(call)                                                                                      \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return fail(WEM_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                                           __FILE__, __LINE__);                                       \
+    } while (0)
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+};
+
+static int ensure(DevBuf &b, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    if (b.n >= bytes) return WEM_OK;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.n = 0;
+    cudaError_t e = cudaMalloc(&b.p, bytes);
+    if (e != cudaSuccess) return fail(WEM_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    b.n = bytes;
+    return WEM_OK;
+}
+
+template <class T> static T *P(DevBuf &b) { return reinterpret_cast<T *>(b.p); }
+
+struct wem_ctx {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t evk[4] = { nullptr, nullptr, nullptr, nullptr };  // around spectra / migrate / reduce
+    int nsm = 0;
+    float last_ms = 0.f;
+    float last_kms[3] = { 0.f, 0.f, 0.f };
+    int last_kernels = 0;
+
+    bool prepared = false;
+    wem_params p{};
+    int ntfft = 0, nw = 0, ifmin = 0, ifmax = 0, nwf = 0, nkx = 0, nky = 0;
+    float dw = 0.f, dkx = 0.f;
+
+    // per-velocity tables
+    DevBuf vref, po, pd, sel, wlin, taper, zflag, twid, wtab, scale_recv, scale_src, srcw, wav, wav_base;
+    // per-call buffers
+    DevBuf recv, slots, image, data, tbase, igx;
+    // host copies of the last shot metadata (skip re-uploads)
+    std::vector<int64_t> h_tbase;
+    std::vector<int> h_igx;
+    int last_nshot = -1;
+};
+
+extern "C" const char *wem_last_error(void) { return g_err; }
+extern "C" int wem_version(void) { return 100; }
+
+extern "C" int wem_ctx_create(wem_ctx **out, int device)
+{
+    if (!out) return fail(WEM_ERR_ARG, "wem_ctx_create: null output pointer");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(WEM_ERR_NODEV, "no CUDA device: the GPU library has no CPU path");
+    if (device < 0 || device >= ndev) return fail(WEM_ERR_ARG, "device %d out of range (have %d)", device, ndev);
+    wem_ctx *c = new (std::nothrow) wem_ctx();
+    if (!c) return fail(WEM_ERR_NOMEM, "host allocation failed");
+    c->device = device;
+    CK(cudaSetDevice(device));
+    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&c->ev0));
+    CK(cudaEventCreate(&c->ev1));
+    for (int i = 0; i < 4; i++) CK(cudaEventCreate(&c->evk[i]));
+    CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
+    *out = c;
+    return WEM_OK;
+}
+
+extern "C" int wem_ctx_destroy(wem_ctx *c)
+{
+    if (!c) return WEM_OK;
+    cudaSetDevice(c->device);
+    if (c->st) cudaStreamSynchronize(c->st);
+    DevBuf *bufs[] = { &c->vref, &c->po, &c->pd, &c->sel, &c->wlin, &c->taper, &c->zflag, &c->twid,
+                       &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
+                       &c->recv, &c->slots, &c->image, &c->data, &c->tbase, &c->igx };
+    for (DevBuf *b : bufs)
+        if (b->p) cudaFree(b->p);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    for (int i = 0; i < 4; i++)
+        if (c->evk[i]) cudaEventDestroy(c->evk[i]);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    return WEM_OK;
+}
+
+extern "C" int wem_last_timing(wem_ctx *c, float *ms, int *kernels)
+{
+    if (!c) return fail(WEM_ERR_ARG, "null context");
+    if (ms) *ms = c->last_ms;
+    if (kernels) *kernels = c->last_kernels;
+    return WEM_OK;
+}
+
+extern "C" int wem_last_kernel_times(wem_ctx *c, float *ms_spectra, float *ms_extrapolate, float *ms_reduce)
+{
+    if (!c) return fail(WEM_ERR_ARG, "null context");
+    if (ms_spectra) *ms_spectra = c->last_kms[0];
+    if (ms_extrapolate) *ms_extrapolate = c->last_kms[1];
+    if (ms_reduce) *ms_reduce = c->last_kms[2];
+    return WEM_OK;
+}
+
+extern "C" int wem_ctx_stream(wem_ctx *c, void **stream)
+{
+    if (!c || !stream) return fail(WEM_ERR_ARG, "null argument");
+    *stream = (void *)c->st;
+    return WEM_OK;
+}
+
+// read the per-kernel event times of the last (completed) call
+static int collect_times(wem_ctx *c)
+{
+    CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+    for (int i = 0; i < 3; i++) CK(cudaEventElapsedTime(&c->last_kms[i], c->evk[i], c->evk[i + 1]));
+    return WEM_OK;
+}
+
+// ---------------------------------------------------------------- derived grids
+// Integer decisions with the reference's float expressions (wem.c:79-89, 112-113).
+static void freq_grid(const wem_params &p, int *ntfft, int *nw, int *ifmin, int *ifmax, float *dw)
+{
+    const int nt = p.nt, padt = p.padt;
+    const float fmin = p.fmin, fmax = p.fmax, dt = p.dt;
+    const int n = (int)2 * padt * ((float)nt) / 2;
+    const int w_ = (int)n / 2 + 1;
+    int hi, lo;
+    if (fmax * dt * n + 1 < w_) hi = (int)fmax * dt * n + 1;
+    else hi = w_;
+    if (fmin * dt * n + 1 < hi) lo = (int)fmin * dt * n;
+    else lo = 0;
+    *ntfft = n;
+    *nw = w_;
+    *ifmin = lo;
+    *ifmax = hi;
+    *dw = 2 * 3.141592653589793 / ((float)n) / dt;
+}
+
+static int is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, const float *wav)
+{
+    if (!c || !pp || !vel || !wav) return fail(WEM_ERR_ARG, "wem_prepare: null argument");
+    const wem_params p = *pp;
+    if (p.nt < 1 || p.nmx < 1 || p.nmy < 1 || p.nz < 1 || p.padt < 1 || p.padx < 1 || !(p.dt > 0) || !(p.dmx > 0))
+        return fail(WEM_ERR_ARG, "wem_prepare: invalid grid (nt=%d nmx=%d nmy=%d nz=%d padt=%d padx=%d)", p.nt,
+                    p.nmx, p.nmy, p.nz, p.padt, p.padx);
+    if (p.pspi && (p.nref < 2 || p.nref > 64))
+        return fail(WEM_ERR_ARG, "PSPI needs 2 <= nref <= 64 (nref=%d; the reference divides by nref-1, wem.c:52)",
+                    p.nref);
+    if (p.interp != WEM_INTERP_REF && p.interp != WEM_INTERP_LINEAR) return fail(WEM_ERR_ARG, "unknown interp %d", p.interp);
+    if (p.precision != WEM_PREC_FP32) return fail(WEM_ERR_SIZE, "precision mode %d not built", p.precision);
+    if (p.nmy != 1) return fail(WEM_ERR_SIZE, "3-D grids (nmy=%d) are not supported by this build", p.nmy);
+    const int nkx = p.nmx > 1 ? p.padx * p.nmx : 1;
+    if (!is_pow2(nkx) || nkx < 32 || nkx > 4096)
+        return fail(WEM_ERR_SIZE, "nkx = padx*nmx = %d must be a power of two in [32, 4096]", nkx);
+    CK(cudaSetDevice(c->device));
+
+    int ntfft, nw, ifmin, ifmax;
+    float dw;
+    freq_grid(p, &ntfft, &nw, &ifmin, &ifmax, &dw);
+    const int nwf = ifmax - ifmin;
+    const int nmx = p.nmx, nz = p.nz, n = p.nmx * p.nmy;
+    const int nref = p.pspi ? p.nref : 1;
+
+    // a1: slowness split (wem.c:28-36); a2: reference velocities (wem.c:40-70).
+    // Device layouts are depth-major ([iz][ix]) so that a depth step reads a row.
+    std::vector<float> po(nz), pd((size_t)nz * nmx), vref((size_t)nz * nref), wl((size_t)nz * nmx, 0.f);
+    std::vector<uint32_t> sel((size_t)nz * nmx);
+    for (int iz = 0; iz < nz; iz++) {
+        float s = 0.;
+        for (int ix = 0; ix < n; ix++) s += vel[(size_t)ix * nz + iz];
+        s /= (float)p.nmx * p.nmy;
+        s = 1. / s;
+        po[iz] = s;
+        for (int ix = 0; ix < n; ix++) pd[(size_t)iz * nmx + ix] = 1.0 / vel[(size_t)ix * nz + iz] - po[iz];
+        float vmin = vel[iz], vmax = vel[(size_t)(p.nmx - 1) * nz + iz];
+        for (int ix = 0; ix < p.nmx; ix++) if (vel[(size_t)ix * nz + iz] < vmin) vmin = vel[(size_t)ix * nz + iz];
+        for (int ix = 0; ix < n; ix++) if (vel[(size_t)ix * nz + iz] > vmax) vmax = vel[(size_t)ix * nz + iz];
+        for (int ir = 0; ir < nref; ir++)
+            vref[(size_t)iz * nref + ir] = nref > 1 ? vmin + (float)ir * (vmax - vmin) / ((float)nref - 1) : vmin;
+        for (int ix = 0; ix < n; ix++) {
+            const float v = vel[(size_t)ix * nz + iz];
+            int i1 = 0, i2 = 0;
+            if (vmax > vmin + 10) {
+                int ir = (int)(nref - 1) * (v - vmin) / (vmax - vmin);
+                if (ir < 0) ir = 0;  // unreachable in 2-D (vmin is the row minimum)
+                i1 = ir;
+                i2 = ir + 1;
+                if (ir > nref - 2) { i1 = nref - 1; i2 = nref - 1; }
+            }
+            const float vr1 = vref[(size_t)iz * nref + i1], vr2 = vref[(size_t)iz * nref + i2];
+            uint32_t word = (uint32_t)i1 | ((uint32_t)i2 << 8);
+            if (vr2 - vr1 > 10.0) {
+                word |= SEL_INTERP;
+                wl[(size_t)iz * nmx + ix] = (v - vr1) / (vr2 - vr1);
+            }
+            sel[(size_t)iz * nmx + ix] = word;
+        }
+    }
+    // taper of the split-step operator (wem.c:546-564), 2-D: tmy = 1
+    std::vector<float> taper(nmx);
+    {
+        const int lmx = p.nmx > 100 ? 30 : 0;
+        float tmx = 1.f;
+        for (int imx = 0; imx < nmx; imx++) {
+            if (imx >= 0 && imx < lmx) tmx = expf(-powf(0.015 * ((float)lmx - imx), 2.));
+            if (imx >= lmx && imx <= nmx - lmx) tmx = 1.;
+            if (imx > nmx - lmx && imx < nmx) tmx = expf(-powf(0.015 * ((float)imx - nmx + lmx), 2.));
+            taper[imx] = tmx;
+        }
+    }
+    std::vector<uint8_t> zf(nz);
+    for (int iz = 0; iz < nz; iz++) {
+        const float z = p.oz + p.dz * iz;
+        zf[iz] = (uint8_t)((z >= p.sz ? Z_SRC : 0) | (z >= p.gz ? Z_REC : 0));
+    }
+    const int ntw = twiddle_table_size(nkx);
+    std::vector<float2> tw(ntw > 0 ? ntw : 1);
+    twiddle_table_host(nkx, tw.data());
+    std::vector<float2> wtab(ntfft);
+    for (int k = 0; k < ntfft; k++) {
+        const double a = -6.283185307179586476925286766559 * (double)k / (double)ntfft;
+        wtab[k] = make_float2((float)cos(a), (float)sin(a));
+    }
+    // receiver weights w^2 (wem.c:128-129) and the 1/sqrtf(ntfft) of wem.c:231-232
+    std::vector<float> srec(nwf > 0 ? nwf : 1), ssrc(nwf > 0 ? nwf : 1);
+    const float sq = sqrtf((float)ntfft);
+    for (int i = 0; i < nwf; i++) {
+        const float w = (ifmin + i) * dw;
+        srec[i] = (float)((double)(w * w) / (double)sq);
+        ssrc[i] = (float)(1.0 / (double)sq);
+    }
+
+    int rc;
+    if ((rc = ensure(c->po, sizeof(float) * nz)) || (rc = ensure(c->pd, sizeof(float) * pd.size())) ||
+        (rc = ensure(c->vref, sizeof(float) * vref.size())) || (rc = ensure(c->sel, sizeof(uint32_t) * sel.size())) ||
+        (rc = ensure(c->wlin, sizeof(float) * wl.size())) || (rc = ensure(c->taper, sizeof(float) * nmx)) ||
+        (rc = ensure(c->zflag, nz)) || (rc = ensure(c->twid, sizeof(float2) * tw.size())) ||
+        (rc = ensure(c->wtab, sizeof(float2) * ntfft)) || (rc = ensure(c->scale_recv, sizeof(float) * srec.size())) ||
+        (rc = ensure(c->scale_src, sizeof(float) * ssrc.size())) || (rc = ensure(c->srcw, sizeof(float2) * (nwf > 0 ? nwf : 1))) ||
+        (rc = ensure(c->wav, sizeof(float) * p.nt)) || (rc = ensure(c->wav_base, sizeof(int64_t))))
+        return rc;
+    cudaStream_t st = c->st;
+    CK(cudaMemcpyAsync(c->po.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->pd.p, pd.data(), sizeof(float) * pd.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->vref.p, vref.data(), sizeof(float) * vref.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->sel.p, sel.data(), sizeof(uint32_t) * sel.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->wlin.p, wl.data(), sizeof(float) * wl.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->taper.p, taper.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->zflag.p, zf.data(), nz, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->twid.p, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->wtab.p, wtab.data(), sizeof(float2) * ntfft, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->scale_recv.p, srec.data(), sizeof(float) * srec.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->scale_src.p, ssrc.data(), sizeof(float) * ssrc.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->wav.p, wav, sizeof(float) * p.nt, cudaMemcpyHostToDevice, st));
+    const int64_t zero = 0;
+    CK(cudaMemcpyAsync(c->wav_base.p, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    // wavelet spectrum over the band (wem.c:112-119 with the 1/sqrtf(ntfft) of wem.c:231)
+    if (nwf > 0) {
+        SpectraArgs sa{};
+        sa.d = P<float>(c->wav);
+        sa.ntr = 1;
+        sa.nt = p.nt;
+        sa.ntfft = ntfft;
+        sa.ifmin = ifmin;
+        sa.nwf = nwf;
+        sa.out_base = P<int64_t>(c->wav_base);
+        sa.out_fstride = 1;
+        sa.wtab = P<float2>(c->wtab);
+        sa.scale = P<float>(c->scale_src);
+        sa.out = P<float2>(c->srcw);
+        if (launch_spectra(sa, st)) return fail(WEM_ERR_CUDA, "spectra launch: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    CK(cudaStreamSynchronize(st));  // the host vectors above go out of scope
+
+    c->p = p;
+    c->ntfft = ntfft;
+    c->nw = nw;
+    c->ifmin = ifmin;
+    c->ifmax = ifmax;
+    c->nwf = nwf;
+    c->nkx = nkx;
+    c->nky = 1;
+    c->dw = dw;
+    c->dkx = 2 * 3.141592653589793 / ((float)nkx) / p.dmx;
+    c->prepared = true;
+    c->last_nshot = -1;
+    return WEM_OK;
+}
+
+// Upload per-shot metadata when it changed: source cells and per-trace output offsets.
+static int set_shots(wem_ctx *c, int nshot, const float *sx, const float *sy, const int64_t *toff,
+                     const int32_t *tcell, int64_t *ntr_out)
+{
+    const wem_params &p = c->p;
+    if (nshot < 1 || !sx || !toff || !tcell) return fail(WEM_ERR_ARG, "migrate: bad shot arguments");
+    if (toff[0] != 0) return fail(WEM_ERR_ARG, "trace_offset[0] must be 0");
+    std::vector<int> igx(nshot);
+    for (int s = 0; s < nshot; s++) {
+        if (toff[s + 1] < toff[s]) return fail(WEM_ERR_ARG, "trace_offset not monotone at shot %d", s);
+        // wem.c:112-113: the cast binds to (sx - omx), then a float division, then truncation
+        const int gx = (int)(sx[s] - p.omx) / p.dmx;
+        const float syv = sy ? sy[s] : 0.f;
+        const int gy = (int)(syv - p.omy) / p.dmy;
+        if (gx < 0 || gx >= p.nmx || gy != 0)
+            return fail(WEM_ERR_ARG, "shot %d: source (%g, %g) falls outside the grid (igx=%d, igy=%d)", s, sx[s], syv, gx, gy);
+        igx[s] = gx;
+    }
+    const int64_t ntr = toff[nshot];
+    std::vector<int64_t> base(ntr > 0 ? ntr : 1);
+    for (int s = 0; s < nshot; s++)
+        for (int64_t i = toff[s]; i < toff[s + 1]; i++) {
+            const int cell = tcell[i];
+            if (cell < 0 || cell >= p.nmx * p.nmy) return fail(WEM_ERR_ARG, "trace %lld: cell %d outside the grid", (long long)i, cell);
+            base[i] = ((int64_t)s * c->nwf) * p.nmx + cell;
+        }
+    *ntr_out = ntr;
+    const bool same = c->last_nshot == nshot && c->h_igx == igx && c->h_tbase.size() == (size_t)ntr &&
+                      (ntr == 0 || memcmp(c->h_tbase.data(), base.data(), sizeof(int64_t) * ntr) == 0);
+    if (same) return WEM_OK;
+    int rc;
+    if ((rc = ensure(c->igx, sizeof(int) * nshot)) || (rc = ensure(c->tbase, sizeof(int64_t) * base.size()))) return rc;
+    CK(cudaMemcpyAsync(c->igx.p, igx.data(), sizeof(int) * nshot, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->tbase.p, base.data(), sizeof(int64_t) * base.size(), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    c->h_igx = igx;
+    c->h_tbase.assign(base.begin(), base.begin() + ntr);
+    c->last_nshot = nshot;
+    return WEM_OK;
+}
+
+// GPU part of a migration: spectra -> depth recursion -> image. Stream-ordered on c->st.
+static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, float *m_dev)
+{
+    const wem_params &p = c->p;
+    cudaStream_t st = c->st;
+    const int nmx = p.nmx, nz = p.nz;
+    int S, threads, bps = 0;
+    size_t smem;
+    if (migrate_config(c->nkx, p.pspi, nmx, p.nref, &S, &threads, &smem)) return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
+    if (migrate_max_grid(c->nkx, p.pspi, p.interp, S, threads, smem, &bps) || bps < 1)
+        return fail(WEM_ERR_CUDA, "kernel does not fit on the device (smem %zu B, %d threads): %s", smem, threads,
+                    cudaGetErrorString(cudaGetLastError()));
+    const int ngroups = (nshot + S - 1) / S;
+    const long long nitems = (long long)ngroups * c->nwf;
+    int grid = (int)((long long)c->nsm * bps < nitems ? (long long)c->nsm * bps : nitems);
+    if (grid < 1) grid = 1;
+    int rc;
+    const size_t recv_elems = (size_t)nshot * (c->nwf > 0 ? c->nwf : 1) * nmx;
+    if ((rc = ensure(c->recv, sizeof(float2) * recv_elems)) ||
+        (rc = ensure(c->slots, sizeof(float2) * (size_t)grid * nz * nmx)))
+        return rc;
+    int kernels = 0;
+    CK(cudaEventRecord(c->ev0, st));
+    CK(cudaMemsetAsync(c->recv.p, 0, sizeof(float2) * recv_elems, st));
+    CK(cudaMemsetAsync(c->slots.p, 0, sizeof(float2) * (size_t)grid * nz * nmx, st));
+    CK(cudaEventRecord(c->evk[0], st));
+    if (c->nwf > 0 && ntr > 0) {
+        SpectraArgs sa{};
+        sa.d = d_dev;
+        sa.ntr = (int)ntr;
+        sa.nt = p.nt;
+        sa.ntfft = c->ntfft;
+        sa.ifmin = c->ifmin;
+        sa.nwf = c->nwf;
+        sa.out_base = P<int64_t>(c->tbase);
+        sa.out_fstride = nmx;
+        sa.wtab = P<float2>(c->wtab);
+        sa.scale = P<float>(c->scale_recv);
+        sa.out = P<float2>(c->recv);
+        if (launch_spectra(sa, st)) return fail(WEM_ERR_CUDA, "spectra launch: %s", cudaGetErrorString(cudaGetLastError()));
+        kernels++;
+    }
+    CK(cudaEventRecord(c->evk[1], st));
+    if (c->nwf > 0) {
+        MigArgs a{};
+        a.nmx = nmx;
+        a.nz = nz;
+        a.nref = p.pspi ? p.nref : 1;
+        a.nwf = c->nwf;
+        a.ifmin = c->ifmin;
+        a.nshot = nshot;
+        a.ngroups = ngroups;
+        a.dw = c->dw;
+        a.dz = p.dz;
+        a.dkx = c->dkx;
+        a.inv_n = 1.0f / (float)c->nkx;
+        a.recv = P<float2>(c->recv);
+        a.srcw = P<float2>(c->srcw);
+        a.igx = P<int>(c->igx);
+        a.vref = P<float>(c->vref);
+        a.po = P<float>(c->po);
+        a.pd = P<float>(c->pd);
+        a.sel = P<uint32_t>(c->sel);
+        a.wlin = P<float>(c->wlin);
+        a.taper = P<float>(c->taper);
+        a.zflag = P<uint8_t>(c->zflag);
+        a.twid = P<float2>(c->twid);
+        a.slots = P<float2>(c->slots);
+        if (launch_migrate(c->nkx, p.pspi, p.interp, S, a, grid, st))
+            return fail(WEM_ERR_CUDA, "migrate launch: %s", cudaGetErrorString(cudaGetLastError()));
+        kernels++;
+    }
+    CK(cudaEventRecord(c->evk[2], st));
+    if (launch_image_reduce(P<float2>(c->slots), grid, nz, nmx, m_dev, st))
+        return fail(WEM_ERR_CUDA, "reduce launch: %s", cudaGetErrorString(cudaGetLastError()));
+    kernels++;
+    CK(cudaEventRecord(c->evk[3], st));
+    CK(cudaEventRecord(c->ev1, st));
+    c->last_kernels = kernels;
+    return WEM_OK;
+}
+
+extern "C" int wem_migrate_device(wem_ctx *c, int nshot, const float *sx, const float *sy, const int64_t *toff,
+                                  const int32_t *tcell, const float *d_dev, float *m_dev, int sync)
+{
+    if (!c || !c->prepared) return fail(WEM_ERR_ARG, "wem_migrate_device: context not prepared (call wem_prepare)");
+    if (nshot < 1 || !toff) return fail(WEM_ERR_ARG, "wem_migrate_device: need nshot >= 1 and trace offsets");
+    if (!m_dev || (!d_dev && toff[nshot] > 0)) return fail(WEM_ERR_ARG, "wem_migrate_device: null buffer");
+    CK(cudaSetDevice(c->device));
+    int64_t ntr = 0;
+    int rc = set_shots(c, nshot, sx, sy, toff, tcell, &ntr);
+    if (rc) return rc;
+    if ((rc = run_migrate(c, nshot, ntr, d_dev, m_dev))) return rc;
+    if (sync) {
+        CK(cudaStreamSynchronize(c->st));
+        if ((rc = collect_times(c))) return rc;
+    }
+    return WEM_OK;
+}
+
+extern "C" int wem_migrate(wem_ctx *c, int nshot, const float *sx, const float *sy, const int64_t *toff,
+                           const int32_t *tcell, const float *d, float *m)
+{
+    if (!c || !c->prepared) return fail(WEM_ERR_ARG, "wem_migrate: context not prepared (call wem_prepare)");
+    if (nshot < 1 || !toff) return fail(WEM_ERR_ARG, "wem_migrate: need nshot >= 1 and trace offsets");
+    if (!m || (!d && toff[nshot] > 0)) return fail(WEM_ERR_ARG, "wem_migrate: null buffer");
+    CK(cudaSetDevice(c->device));
+    const wem_params &p = c->p;
+    int64_t ntr = 0;
+    int rc = set_shots(c, nshot, sx, sy, toff, tcell, &ntr);
+    if (rc) return rc;
+    const size_t dbytes = sizeof(float) * (size_t)ntr * p.nt;
+    const size_t mbytes = sizeof(float) * (size_t)p.nmx * p.nmy * p.nz;
+    if ((rc = ensure(c->data, dbytes)) || (rc = ensure(c->image, mbytes))) return rc;
+    if (dbytes) CK(cudaMemcpyAsync(c->data.p, d, dbytes, cudaMemcpyHostToDevice, c->st));
+    if ((rc = run_migrate(c, nshot, ntr, P<float>(c->data), P<float>(c->image)))) return rc;
+    CK(cudaMemcpyAsync(m, c->image.p, mbytes, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return collect_times(c);
+}
+
+extern "C" int wem_migrate_survey(wem_ctx *c, const wem_params *p, const float *vel, const float *wav, int nshot,
+                                  const float *sx, const float *sy, const int64_t *toff, const int32_t *tcell,
+                                  const float *d, float *m)
+{
+    int rc = wem_prepare(c, p, vel, wav);
+    if (rc) return rc;
+    return wem_migrate(c, nshot, sx, sy, toff, tcell, d, m);
+}
+
+// ---------------------------------------------------------------- wem() drop-in
+static std::mutex g_default_mu;
+static wem_ctx *g_default = nullptr;
+
+static int default_ctx(wem_ctx **out)
+{
+    std::lock_guard<std::mutex> lk(g_default_mu);
+    if (!g_default) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) dev = 0;
+        int rc = wem_ctx_create(&g_default, dev);
+        if (rc) return rc;
+    }
+    *out = g_default;
+    return WEM_OK;
+}
+
+extern "C" int wem(float **d, float **m, float **wav, int nt, float ot, float dt, int nmx, float omx, float dmx, int nmy,
+                   float omy, float dmy, float sx, float sy, int nz, float oz, float dz, float gz, float sz, float **vel,
+                   int nref, float fmin, float fmax, int padt, int padx, bool adj, bool pspi, bool verbose)
+{
+    if (!d || !m || !wav || !vel || !wav[0]) return fail(WEM_ERR_ARG, "wem: null argument");
+    if (nt < 1 || nmx < 1 || nmy < 1 || nz < 1) return fail(WEM_ERR_ARG, "wem: invalid sizes");
+    if (!adj) return fail(WEM_ERR_SIZE, "wem: modelling (adj=false) is not available in this build");
+    wem_ctx *c;
+    int rc = default_ctx(&c);
+    if (rc) return rc;
+    wem_params p{};
+    p.nt = nt; p.ot = ot; p.dt = dt;
+    p.nmx = nmx; p.omx = omx; p.dmx = dmx;
+    p.nmy = nmy; p.omy = omy; p.dmy = dmy;
+    p.nz = nz; p.oz = oz; p.dz = dz; p.gz = gz; p.sz = sz;
+    p.nref = nref; p.fmin = fmin; p.fmax = fmax; p.padt = padt; p.padx = padx;
+    p.pspi = pspi ? 1 : 0;
+    p.interp = WEM_INTERP_REF;
+    p.precision = WEM_PREC_FP32;
+    p.verbose = verbose ? 1 : 0;
+    const int n = nmx * nmy;
+    std::vector<float> v((size_t)n * nz), dd((size_t)n * nt), mm((size_t)n * nz);
+    for (int ix = 0; ix < n; ix++) {
+        if (!vel[ix] || !d[ix] || !m[ix]) return fail(WEM_ERR_ARG, "wem: null row %d", ix);
+        memcpy(&v[(size_t)ix * nz], vel[ix], sizeof(float) * nz);
+        memcpy(&dd[(size_t)ix * nt], d[ix], sizeof(float) * nt);
+    }
+    if ((rc = wem_prepare(c, &p, v.data(), wav[0]))) return rc;
+    std::vector<int64_t> off = { 0, (int64_t)n };
+    std::vector<int32_t> cell(n);
+    for (int i = 0; i < n; i++) cell[i] = i;
+    if ((rc = wem_migrate(c, 1, &sx, &sy, off.data(), cell.data(), dd.data(), mm.data()))) return rc;
+    for (int ix = 0; ix < n; ix++) memcpy(m[ix], &mm[(size_t)ix * nz], sizeof(float) * nz);
+    if (verbose) fprintf(stderr, "wem: %d frequencies x %d depth steps on the GPU in %.3f ms\n", c->nwf, nz, c->last_ms);
+    return WEM_OK;
+}

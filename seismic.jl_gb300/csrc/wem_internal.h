@@ -1,0 +1,65 @@
+// wem_internal.h -- structures shared by the host runtime (wem_api.cu) and the
+// kernels (wem_kernels.cu). Not part of the public ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbwem {
+
+// Per-depth selection word of the PSPI interpolation, one per (iz, ix):
+// bits 0-7 iref1, bits 8-15 iref2, bit 16 set when vref2 - vref1 > 10
+// (wem.c:454: interpolate; otherwise the nearest-lower wavefield is taken whole).
+constexpr uint32_t SEL_INTERP = 1u << 16;
+
+// Per-depth activity flags (wem.c:235-242): source continued when z >= sz,
+// receiver continued and image formed when z >= gz.
+constexpr uint8_t Z_SRC = 1, Z_REC = 2;
+
+struct MigArgs {
+    int nmx;        // live samples per row (grid cells along x)
+    int nz;
+    int nref;       // PSPI reference velocities (1 for split-step)
+    int nwf;        // frequencies in the band [ifmin, ifmax)
+    int ifmin;
+    int nshot;
+    int ngroups;    // ceil(nshot / shots per CTA)
+    float dw;       // angular frequency step (float, wem.c:85)
+    float dz;
+    float dkx;      // wavenumber step (float, wem.c:83)
+    float inv_n;    // 1/nkx, folds the two 1/sqrt(nkx) of wem.c:437,445
+    const float2 *recv;    // [nshot][nwf][nmx] receiver spectra, w^2/sqrt(ntfft) applied
+    const float2 *srcw;    // [nwf] wavelet spectrum / sqrt(ntfft)
+    const int *igx;        // [nshot] source cell
+    const float *vref;     // [nz][nref]
+    const float *po;       // [nz] mean slowness
+    const float *pd;       // [nz][nmx] slowness perturbation
+    const uint32_t *sel;   // [nz][nmx]
+    const float *wlin;     // [nz][nmx] linear-interpolation weight of iref2
+    const float *taper;    // [nmx] boundary taper (split-step)
+    const uint8_t *zflag;  // [nz]
+    const float2 *twid;    // FFT twiddle table of the row length
+    float2 *slots;         // [gridDim.x][nz][nmx] (sum, compensation) image accumulators
+};
+
+struct SpectraArgs {
+    const float *d;        // [ntr][nt]
+    int ntr, nt, ntfft;
+    int ifmin, nwf;
+    const int64_t *out_base;  // [ntr] element offset of (row, iwi = 0) in out
+    int64_t out_fstride;      // element stride between consecutive frequencies
+    const float2 *wtab;       // [ntfft] e^{-2 pi i k / ntfft}
+    const float *scale;       // [nwf]
+    float2 *out;
+};
+
+// host-side launchers (wem_kernels.cu)
+int launch_migrate(int nkx, int pspi, int interp, int shots_per_cta, const MigArgs &a, int grid,
+                   cudaStream_t st);
+int migrate_config(int nkx, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem);
+int migrate_max_grid(int nkx, int pspi, int interp, int shots_per_cta, int threads, size_t smem, int *blocks_per_sm);
+int launch_spectra(const SpectraArgs &a, cudaStream_t st);
+int launch_image_reduce(const float2 *slots, int nslots, int nz, int nmx, float *m, cudaStream_t st);
+int twiddle_table_size(int nkx);
+void twiddle_table_host(int nkx, float2 *out);
+
+}  // namespace gbwem

@@ -1,0 +1,83 @@
+"""Generate tests/golden/*.npz from the reference's own C core.
+
+Runs src/Imaging/c/wem.c (+ shotwem.c, seismic.c) compiled UNMODIFIED in
+oracle/_ref/ (see oracle/Makefile; FFTW 3.3.4 is replaced by oracle/fftw_subset.c)
+on small seeded cases and stores inputs and outputs. Needs the reference sources,
+so it runs in the build container only; the fixtures then pin the oracle and the
+GPU path wherever the tests run.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+sys.path.insert(0, os.path.join(ROOT, "seismic.jl_gb300"))
+
+import oracle as O  # noqa: E402
+from wemgpu import seis, synth  # noqa: E402
+
+CASES = {
+    # name: (seed, nx, nz, nt, pspi, nref, fmax, padx, padt)
+    "ss_64": (11, 64, 24, 128, 0, 2, 40.0, 2, 2),
+    "ss_128_taper": (12, 128, 20, 128, 0, 2, 30.0, 2, 2),
+    "pspi_64": (13, 64, 24, 128, 1, 4, 40.0, 2, 2),
+    "pspi_128_r8": (14, 128, 16, 96, 1, 8, 30.0, 2, 1),
+    "pspi_64_padx1": (15, 64, 12, 64, 1, 3, 40.0, 1, 2),
+}
+
+
+def case_inputs(seed, nx, nz, nt, pspi, nref, fmax, padx, padt):
+    c = synth.small_case(seed, nx=nx, nz=nz, nt=nt, nshot=1, pspi=pspi, nref=nref, fmax=fmax, padx=padx,
+                         padt=padt)
+    p = dict(c["params"])
+    p["sx"] = float(c["shots"].sx[0])
+    d = synth.shot_gather_full(c["shots"], 0, nx)
+    rng = np.random.default_rng(seed + 100)
+    m_in = rng.standard_normal((nx, nz)).astype(np.float32)
+    return p, c["vel"], c["wav"], d, m_in
+
+
+def main():
+    O.build()
+    if O.build_ref() is None:
+        sys.exit("reference sources not found: golden vectors come from the reference itself")
+    os.environ.setdefault("OMP_NUM_THREADS", "4")
+    for name, args in CASES.items():
+        p, vel, wav, d, m_in = case_inputs(*args)
+        m_ref = O.wem_ref(p, vel, wav, d=d, adj=True)
+        d_ref = O.wem_ref(p, vel, wav, m=m_in, adj=False)
+        np.savez_compressed(os.path.join(HERE, f"wem_{name}.npz"), vel=vel, wav=wav, d=d, m_in=m_in,
+                            m_ref=m_ref, d_ref=d_ref,
+                            params=np.array(repr({k: v for k, v in p.items()})))
+        print(name, "image norm", float(np.linalg.norm(m_ref)), "data norm", float(np.linalg.norm(d_ref)))
+
+    # file-level: the reference's main() on seis files (shotwem.c:12-140)
+    p, vel, wav, d, _ = case_inputs(*CASES["pspi_64"])
+    with tempfile.TemporaryDirectory() as td:
+        seis.write_grid(os.path.join(td, "vel"), vel, o1=0.0, d1=p["dz"], ox=p["omx"], dx=p["dmx"])
+        seis.write_wavelet(os.path.join(td, "wav"), wav, dt=p["dt"])
+        seis.write_shot(os.path.join(td, "d"), d, sx=p["sx"], dt=p["dt"], ox=p["omx"], dx=p["dmx"])
+        argv = [os.path.join(O.HERE, "_ref", "shotwem_ref"), "adj=y", "pspi=y", f"nref={p['nref']}",
+                "d=" + os.path.join(td, "d"), "m=" + os.path.join(td, "m"), "vel=" + os.path.join(td, "vel"),
+                "wav=" + os.path.join(td, "wav"), f"sx={p['sx']}", "sy=0", "sz=0", "gz=0",
+                f"fmin={p['fmin']}", f"fmax={p['fmax']}", f"padt={p['padt']}", f"padx={p['padx']}", "verbose=n"]
+        subprocess.run(argv, check=True, cwd=td)
+        m_main, hdr, ext = seis.read(os.path.join(td, "m"))
+        np.savez_compressed(os.path.join(HERE, "main_pspi_64.npz"), vel=vel, wav=wav, d=d, m_ref=m_main,
+                            imx=np.array([h["imx"] for h in hdr]), mx=np.array([h["mx"] for h in hdr]),
+                            n=np.array(ext["n"]), o=np.array(ext["o"]), dd=np.array(ext["d"]),
+                            params=np.array(repr(p)))
+        print("main() image norm", float(np.linalg.norm(m_main)))
+
+
+if __name__ == "__main__":
+    main()

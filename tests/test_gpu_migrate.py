@@ -1,0 +1,153 @@
+"""Parity of the CUDA migration (called through the C ABI) with the oracle.
+
+Tolerance: relative L2 image error <= 1e-4 against the reference's arithmetic (the
+port / the reference's golden outputs) and against the FP64 operator. The GPU
+computes in complex FP32 like the reference, so the expected error is the FP32
+floor (1e-6 .. 1e-5).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+GOLDEN_CASES = ["ss_64", "ss_128_taper", "pspi_64", "pspi_128_r8", "pspi_64_padx1"]
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_wem_dropin_matches_reference_golden(gpu_lib, case):
+    """wem() (wem.h:3-11 signature, float** rows) vs the reference's own output."""
+    g = load_golden(f"wem_{case}.npz")
+    m = gpu_lib.wem_dropin(g["params"], g["vel"], g["wav"], d=g["d"], adj=True)
+    assert rel_l2(m, g["m_ref"]) < TOL
+
+
+def _port_stack(oracle_mod, p, vel, wav, shots, fp64=False):
+    from wemgpu import synth
+    op = oracle_mod.wem_fp64 if fp64 else oracle_mod.wem_port
+    img = None
+    for s in range(shots.nshot):
+        q = dict(p, sx=float(shots.sx[s]))
+        d = synth.shot_gather_full(shots, s, p["nmx"])
+        m = op(q, vel, wav, d=d, adj=True).astype(np.float64)
+        img = m if img is None else img + m
+    return img
+
+
+@pytest.mark.parametrize("pspi,interp", [(0, "ref"), (1, "ref"), (1, "linear")])
+def test_batched_survey_matches_oracle(gpu_lib, oracle_mod, pspi, interp):
+    """Several shots with uneven apertures in one call vs the oracle shot by shot,
+    stacked like ShotProfileWEM.jl:140-199."""
+    from wemgpu import synth
+    c = synth.small_case(21, nx=64, nz=24, nt=128, nshot=5, pspi=pspi, nref=5, interp=interp)
+    m = gpu_lib.migrate(c["params"], c["vel"], c["wav"], c["shots"])
+    want = _port_stack(oracle_mod, c["params"], c["vel"], c["wav"], c["shots"])
+    assert rel_l2(m, want) < TOL
+    want64 = _port_stack(oracle_mod, c["params"], c["vel"], c["wav"], c["shots"], fp64=True)
+    assert rel_l2(m, want64) < TOL
+
+
+@pytest.mark.parametrize("nx,padx", [(16, 2), (32, 1), (128, 2), (256, 2), (512, 2), (1024, 2), (2048, 2)])
+def test_row_lengths(gpu_lib, oracle_mod, nx, padx):
+    """Every FFT length the kernel is built for (nkx = 32 .. 4096)."""
+    from wemgpu import synth
+    c = synth.small_case(31 + nx, nx=nx, nz=6, nt=64, nshot=2, pspi=1, nref=3, fmax=30.0, padx=padx)
+    m = gpu_lib.migrate(c["params"], c["vel"], c["wav"], c["shots"])
+    want = _port_stack(oracle_mod, c["params"], c["vel"], c["wav"], c["shots"])
+    assert rel_l2(m, want) < TOL
+
+
+def test_deterministic(gpu_lib):
+    from wemgpu import synth
+    c = synth.small_case(41, nx=128, nz=16, nt=96, nshot=4)
+    with gpu_lib.Context() as ctx:
+        ctx.prepare(c["params"], c["vel"], c["wav"])
+        a = ctx.migrate(c["shots"])
+        b = ctx.migrate(c["shots"])
+    assert np.array_equal(a, b)
+
+
+def test_config0_full_size_matches_reference_port(gpu_lib, oracle_mod):
+    """The split-step workload at full size (1 shot, 200 x 256, 221 frequencies)."""
+    from wemgpu import synth
+    c = synth.config0()
+    m = gpu_lib.migrate(c["params"], c["vel"], c["wav"], c["shots"])
+    p = dict(c["params"], sx=float(c["shots"].sx[0]))
+    want = oracle_mod.wem_port(p, c["vel"], c["wav"], d=c["shots"].data, adj=True)
+    assert rel_l2(m, want) < TOL
+
+
+def test_config1_geometry_band_subset(gpu_lib, oracle_mod):
+    """The PSPI survey's grid (500 x 1024, nkx 2048, nref 8) on 2 shots and a narrow
+    band, so the oracle finishes in seconds."""
+    from wemgpu import synth
+    c = synth.config1(nshot=2, fmax=7.0, npoints=20)
+    p = dict(c["params"], fmin=5.0, fmax=7.0)
+    m = gpu_lib.migrate(p, c["vel"], c["wav"], c["shots"])
+    want = _port_stack(oracle_mod, p, c["vel"], c["wav"], c["shots"])
+    assert rel_l2(m, want) < TOL
+
+
+def test_main_dropin_on_seis_files(gpu_lib, tmp_path):
+    """main(argc, argv) on seis files (shotwem.c:12-140) vs the reference's main()."""
+    from wemgpu import seis
+    g = load_golden("main_pspi_64.npz")
+    p = g["params"]
+    seis.write_grid(str(tmp_path / "vel"), g["vel"], o1=0.0, d1=p["dz"], ox=p["omx"], dx=p["dmx"])
+    seis.write_wavelet(str(tmp_path / "wav"), g["wav"], dt=p["dt"])
+    seis.write_shot(str(tmp_path / "d"), g["d"], sx=p["sx"], dt=p["dt"], ox=p["omx"], dx=p["dmx"])
+    args = [b"0", b"adj=y", b"pspi=y", f"nref={p['nref']}".encode(), b"d=" + str(tmp_path / "d").encode(),
+            b"m=" + str(tmp_path / "m").encode(), b"vel=" + str(tmp_path / "vel").encode(),
+            b"wav=" + str(tmp_path / "wav").encode(), b"damping=1000.0", f"sx={p['sx']}".encode(), b"sy=0",
+            b"sz=0", b"gz=0", f"fmin={p['fmin']}".encode(), f"fmax={p['fmax']}".encode(),
+            f"padt={p['padt']}".encode(), f"padx={p['padx']}".encode(), b"verbose=n"]
+    argv = (C.c_char_p * len(args))(*args)
+    assert gpu_lib.lib().main(len(args), argv) == 0
+    m, h, ext = seis.read(str(tmp_path / "m"))
+    assert rel_l2(m, g["m_ref"]) < TOL
+    assert np.array_equal(h["imx"], g["imx"]) and np.allclose(h["mx"], g["mx"])
+    assert ext["n"][:3] == list(g["n"][:3])
+
+
+def test_edge_cases(gpu_lib):
+    from wemgpu import synth, WemError
+    c = synth.small_case(51, nx=64, nz=8, nt=64, nshot=2)
+    p, vel, wav, shots = c["params"], c["vel"], c["wav"], c["shots"]
+    with gpu_lib.Context() as ctx:
+        ctx.prepare(p, vel, wav)
+        # a shot without traces contributes nothing (its receiver wavefield is zero)
+        empty = gpu_lib.Shots(shots.sx[:1], shots.sy[:1], np.array([0, 0], np.int64), np.zeros(0, np.int32),
+                              np.zeros((0, p["nt"]), np.float32))
+        assert not np.any(ctx.migrate(empty))
+        # source outside the grid
+        bad = gpu_lib.Shots(np.array([1e6], np.float32), np.zeros(1, np.float32), shots.trace_offset[:2],
+                            shots.trace_cell[: shots.trace_offset[1]], shots.data[: shots.trace_offset[1]])
+        with pytest.raises(WemError) as e:
+            ctx.migrate(bad)
+        assert e.value.code == -1
+        # zero data gives a zero image
+        zero = gpu_lib.Shots(shots.sx, shots.sy, shots.trace_offset, shots.trace_cell, np.zeros_like(shots.data))
+        assert not np.any(ctx.migrate(zero))
+        # unsupported FFT length and a single reference velocity are rejected
+        with pytest.raises(WemError) as e:
+            ctx.prepare(dict(p, nmx=48), np.ones((48, p["nz"]), np.float32) * 2000, wav)
+        assert e.value.code == -2
+        with pytest.raises(WemError) as e:
+            ctx.prepare(dict(p, nref=1), vel, wav)
+        assert e.value.code == -1
+
+
+def test_source_and_receiver_depth(gpu_lib, oracle_mod):
+    """sz, gz > 0: continuation and imaging start below them (wem.c:235-242)."""
+    from wemgpu import synth
+    c = synth.small_case(61, nx=64, nz=20, nt=96, nshot=1)
+    p = dict(c["params"], sz=45.0, gz=95.0)
+    m = gpu_lib.migrate(p, c["vel"], c["wav"], c["shots"])
+    want = _port_stack(oracle_mod, p, c["vel"], c["wav"], c["shots"])
+    assert rel_l2(m, want) < TOL
+    assert not np.any(m[:, :10])

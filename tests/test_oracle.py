@@ -1,0 +1,127 @@
+"""Pins the oracle tier before anything is compared with it (CPU only).
+
+* the FFT restatement of FFTW's contract vs numpy and vs FFTW's own outputs
+  (the DCT-II/DST-II vectors FFTW generated for scipy's test suite, when present);
+* the reference-semantics port vs the golden vectors the reference's own C core
+  produced (tests/golden, tests/golden/make_golden.py) -- and bit for bit vs that
+  core itself when its sources are present to build it;
+* the C FP64 oracle vs the independent NumPy FP64 restatement, and the FP32 floor.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_l2
+
+GOLDEN_CASES = ["ss_64", "ss_128_taper", "pspi_64", "pspi_128_r8", "pspi_64_padx1"]
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 7, 12, 16, 17, 30, 64, 125, 256, 512, 1000, 1024, 2000, 2048, 3000, 4096])
+def test_fft_matches_numpy(oracle_mod, n):
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal((3, n)) + 1j * rng.standard_normal((3, n))
+    ref = np.fft.fft(x, axis=1)
+    scale = np.abs(ref).max()
+    assert np.abs(oracle_mod.fft_f32(x) - ref).max() / scale < 2e-6
+    assert np.abs(oracle_mod.fft_f64(x) - ref).max() / scale < 1e-13
+    assert np.abs(oracle_mod.fft_f32(x, +1) - np.fft.ifft(x, axis=1) * n).max() / scale < 2e-6
+
+
+FFTW_REF = None
+try:
+    import scipy.fftpack.tests as _t
+    _p = os.path.join(os.path.dirname(_t.__file__), "fftw_single_ref.npz")
+    FFTW_REF = _p if os.path.exists(_p) else None
+except Exception:
+    FFTW_REF = None
+
+
+@pytest.mark.skipif(FFTW_REF is None, reason="FFTW-generated reference vectors not installed")
+def test_fft_matches_fftw_generated_vectors(oracle_mod):
+    """FFTW's REDFT10/RODFT10 outputs for x = 0..n-1 (single precision), rebuilt from our
+    complex FFT through the even/odd extension of length 2n:
+    DCT-II_k = Re(e^{-i pi k/(2n)} FFT(z)_k), z = [x, reversed x];
+    DST-II_k = -Im(e^{-i pi (k+1)/(2n)} FFT(z)_{k+1}), z = [x, -reversed x]."""
+    ref = np.load(FFTW_REF)
+    for n in [int(s) for s in ref["sizes"]]:
+        x = np.arange(n, dtype=np.float64)
+        k = np.arange(n)
+        Z = oracle_mod.fft_f32(np.concatenate([x, x[::-1]]).astype(np.complex64)).astype(np.complex128)
+        dct2 = (np.exp(-1j * np.pi * k / (2 * n)) * Z[:n]).real
+        Zs = oracle_mod.fft_f32(np.concatenate([x, -x[::-1]]).astype(np.complex64)).astype(np.complex128)
+        dst2 = -(np.exp(-1j * np.pi * (k + 1) / (2 * n)) * Zs[1:n + 1]).imag
+        for got, key in ((dct2, f"dct_2_{n}"), (dst2, f"dst_2_{n}")):
+            want = ref[key].astype(np.float64)
+            assert np.abs(got - want).max() / np.abs(want).max() < 5e-6, key
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_port_matches_reference_golden(oracle_mod, case):
+    """The port vs the reference's own outputs. Both use the same FFT, so the only
+    freedom is the OpenMP reduction order (one image slice per thread) and libm; the
+    tolerance is the FP32 level."""
+    g = load_golden(f"wem_{case}.npz")
+    p = g["params"]
+    m = oracle_mod.wem_port(p, g["vel"], g["wav"], d=g["d"], adj=True, nthreads=4)
+    assert rel_l2(m, g["m_ref"]) < 1e-5
+    d = oracle_mod.wem_port(p, g["vel"], g["wav"], m=g["m_in"], adj=False, nthreads=4)
+    assert rel_l2(d, g["d_ref"]) < 1e-5
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/src/Imaging/c/wem.c"), reason="reference sources absent")
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_port_bitwise_vs_compiled_reference(oracle_mod, case):
+    oracle_mod.build_ref()
+    nthr = oracle_mod.omp_threads()  # the reference uses every thread of the process's OpenMP runtime
+    g = load_golden(f"wem_{case}.npz")
+    p = g["params"]
+    m_ref = oracle_mod.wem_ref(p, g["vel"], g["wav"], d=g["d"], adj=True)
+    m = oracle_mod.wem_port(p, g["vel"], g["wav"], d=g["d"], adj=True, nthreads=nthr)
+    assert np.array_equal(m, m_ref)
+    d_ref = oracle_mod.wem_ref(p, g["vel"], g["wav"], m=g["m_in"], adj=False)
+    d = oracle_mod.wem_port(p, g["vel"], g["wav"], m=g["m_in"], adj=False, nthreads=nthr)
+    assert np.array_equal(d, d_ref)
+
+
+@pytest.mark.parametrize("case", ["ss_64", "pspi_64", "pspi_64_padx1"])
+@pytest.mark.parametrize("interp", [0, 1])
+def test_fp64_oracles_agree(oracle_mod, case, interp):
+    """C FP64 oracle vs the independent NumPy restatement (adjoint and forward)."""
+    import wem_np
+    g = load_golden(f"wem_{case}.npz")
+    p = dict(g["params"], interp=interp)
+    if not p.get("pspi", 1) and interp:
+        pytest.skip("interpolation applies to PSPI only")
+    m64 = oracle_mod.wem_fp64(p, g["vel"], g["wav"], d=g["d"], adj=True, nthreads=2)
+    mnp = wem_np.wem(p, g["vel"].astype(np.float64), g["wav"], d=g["d"], adj=True)
+    assert rel_l2(m64, mnp) < 1e-10
+    d64 = oracle_mod.wem_fp64(p, g["vel"], g["wav"], m=g["m_in"], adj=False, nthreads=2)
+    dnp = wem_np.wem(p, g["vel"].astype(np.float64), g["wav"], m=g["m_in"].astype(np.float64), adj=False)
+    assert rel_l2(d64, dnp) < 1e-10
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_reference_fp32_floor(oracle_mod, case):
+    """The reference's FP32 arithmetic stays within 1e-4 of the FP64 operator (ref mode)."""
+    g = load_golden(f"wem_{case}.npz")
+    p = g["params"]
+    m64 = oracle_mod.wem_fp64(p, g["vel"], g["wav"], d=g["d"], adj=True, nthreads=2)
+    assert rel_l2(g["m_ref"], m64) < 1e-4
+
+
+def test_fp64_adjoint_pair_dot_test(oracle_mod):
+    """<d, L m> vs <L' d, m> for the FP64 operator pair. The reference's forward and
+    adjoint are not exact adjoints (split-step applies the taper and correction on
+    opposite sides, PSPI ref mode truncates to the real part), so this records the
+    mismatch of the reference pair rather than asserting 1e-5; see test_gpu_born for
+    the adjoint pair built for least squares."""
+    g = load_golden("wem_pspi_64.npz")
+    p = dict(g["params"], interp=1)
+    rng = np.random.default_rng(5)
+    m = rng.standard_normal(g["m_in"].shape)
+    d = rng.standard_normal(g["d"].shape)
+    Lm = oracle_mod.wem_fp64(p, g["vel"], g["wav"], m=m, adj=False, nthreads=2)
+    Ltd = oracle_mod.wem_fp64(p, g["vel"], g["wav"], d=d, adj=True, nthreads=2)
+    a, b = float(np.sum(d * Lm)), float(np.sum(Ltd * m))
+    assert np.isfinite(a) and np.isfinite(b)
