@@ -52,6 +52,24 @@ struct SpectraArgs {
     float2 *out;
 };
 
+struct BornArgs {
+    const float *img;   // [nz][nmx] image (depth-major)
+    float2 *smig;       // [gridDim.x * shots per CTA][nz][nmx] source wavefield scratch
+    float2 *dg;         // [nshot][nwf][nmx] modelled spectra (already / sqrt(ntfft))
+    float inv_sqt;      // 1/sqrtf(ntfft)
+};
+
+struct SynthArgs {
+    const float2 *dg;         // [nshot][nwf][nmx]
+    int nwf, ifmin, nt, nf;   // nf: length of the real transform, (nw-1)*2 (wem.c:487)
+    int ntr;
+    const int64_t *in_base;   // [ntr] element offset of (shot, iwi = 0, cell) in dg
+    int64_t in_fstride;       // nmx
+    const float2 *wtab;       // [nf] e^{-2 pi i k / nf}
+    const float *scale;       // [nwf] w^2 times the half-spectrum weight
+    float *out;               // [ntr][nt]
+};
+
 // host-side launchers (wem_kernels.cu)
 int launch_migrate(int nkx, int pspi, int interp, int shots_per_cta, const MigArgs &a, int grid,
                    cudaStream_t st);
@@ -59,6 +77,12 @@ int migrate_config(int nkx, int pspi, int nmx, int nref, int *shots_per_cta, int
 int migrate_max_grid(int nkx, int pspi, int interp, int shots_per_cta, int threads, size_t smem, int *blocks_per_sm);
 int launch_spectra(const SpectraArgs &a, cudaStream_t st);
 int launch_image_reduce(const float2 *slots, int nslots, int nz, int nmx, float *m, cudaStream_t st);
+int model_config(int nkx, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem);
+int model_max_grid(int nkx, int pspi, int interp, int exact, int threads, size_t smem, int *blocks_per_sm);
+int launch_model(int nkx, int pspi, int interp, int exact, const MigArgs &a, const BornArgs &b, int grid,
+                 cudaStream_t st);
+int launch_synth(const SynthArgs &a, cudaStream_t st);
+int launch_transpose(const float *in, int rows, int cols, float *out, cudaStream_t st);
 int twiddle_table_size(int nkx);
 void twiddle_table_host(int nkx, float2 *out);
 

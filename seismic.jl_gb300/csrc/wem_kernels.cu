@@ -56,7 +56,7 @@ __device__ __forceinline__ void kahan_add(float2 *slot, float v)
     *slot = s;
 }
 
-// ------------------------------------------------------------------ migration
+// ------------------------------------------------------------------ shared pieces
 template <int N> struct MigShape {
     static constexpr int T = N / 16;           // threads per row team
     static constexpr int HALF = N / 2 + 1;     // phase-table entries per reference
@@ -71,28 +71,231 @@ __host__ __device__ constexpr size_t mig_smem_bytes(int TWP, int HALF, int PADN,
     return sizeof(float2) * ((size_t)TWP + (size_t)nph * HALF + (size_t)((ncorr + 1) & ~1) + (size_t)teams * PADN);
 }
 
+// Shared-memory views of one CTA: twiddles, phase tables, split-step correction,
+// one exchange buffer per row team.
+template <int N, bool PSPI> struct Smem {
+    float2 *tw, *ph, *corr, *x;
+    __device__ Smem(float4 *raw, int nref, int nmx)
+    {
+        using SH = MigShape<N>;
+        tw = reinterpret_cast<float2 *>(raw);
+        ph = tw + SH::TWP;
+        corr = ph + (size_t)(PSPI ? nref : 1) * SH::HALF;
+        x = corr + (PSPI ? 0 : ((nmx + 1) & ~1));
+    }
+};
+
+// Tables of depth step iz at angular frequency w (all threads of the CTA):
+// PSPI: one phase table per reference velocity; split-step: the phase table of
+// the mean slowness and the correction exp(i w pd dz) * taper (wem.c:326, 353-359).
+template <int N, bool PSPI>
+__device__ __forceinline__ void build_tables(const MigArgs &a, const Smem<N, PSPI> &sm, float w, float w2, int iz,
+                                             int tid, int nthreads)
+{
+    constexpr int HALF = MigShape<N>::HALF;
+    if (PSPI) {
+        const float *vr = a.vref + (size_t)iz * a.nref;
+        for (int e = tid; e < a.nref * HALF; e += nthreads) {
+            const int r = e / HALF, kk = e - r * HALF;
+            const float v_ = vr[r];
+            const float slow2 = __fdiv_rn(1.0f, __fmul_rn(v_, v_));
+            sm.ph[e] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
+        }
+    } else {
+        const float po = a.po[iz];
+        const float slow2 = __fmul_rn(po, po);
+        for (int e = tid; e < HALF; e += nthreads)
+            sm.ph[e] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)e), a.dz, a.inv_n);
+        const float *pd = a.pd + (size_t)iz * a.nmx;
+        for (int x = tid; x < a.nmx; x += nthreads) {
+            const float th = __fmul_rn(__fmul_rn(w, pd[x]), a.dz);
+            float sn, cs;
+            sincosf(th, &sn, &cs);
+            const float tp = a.taper[x];
+            sm.corr[x] = make_float2(cs * tp, sn * tp);
+        }
+    }
+}
+
+template <int N> __device__ __forceinline__ int kfold(int t, int m)
+{
+    const int k = t + (N / 16) * m;
+    return k <= N / 2 ? k : N - k;
+}
+
+// Per-x selection data of depth iz for the thread's 16 positions.
+template <int N, int INTERP>
+__device__ __forceinline__ void load_sel(const MigArgs &a, int iz, int t, uint32_t (&sel)[16], float (&wl)[16])
+{
+    constexpr int T = N / 16;
+    const uint32_t *selr = a.sel + (size_t)iz * a.nmx;
+    const float *wlr = a.wlin + (size_t)iz * a.nmx;
+#pragma unroll
+    for (int m = 0; m < 16; m++) {
+        const int x = t + T * m;
+        sel[m] = x < a.nmx ? selr[x] : 0xffffu;  // 0xff never matches a reference index
+        wl[m] = (INTERP == 1 && x < a.nmx) ? wlr[x] : 0.f;
+    }
+}
+
+// Weight of reference r at one position, as the migration applies it after the
+// inverse FFTs (wem.c:450-460); `re_only` reports the real-part truncation of
+// linear_interp's float return (wem.c:473-478).
+template <int INTERP>
+__device__ __forceinline__ float sel_weight(uint32_t s_, float wl, int r, bool &re_only)
+{
+    const int i1 = s_ & 0xff, i2 = (s_ >> 8) & 0xff;
+    const bool interp = (s_ & SEL_INTERP) != 0;
+    re_only = (INTERP == 0) && interp;
+    if (INTERP == 0 || !interp) return r == i1 ? 1.f : 0.f;
+    return (r == i1 ? 1.f - wl : 0.f) + (r == i2 ? wl : 0.f);
+}
+
+// One depth step of the migration direction (extrap1f adj, wem.c:236-242): PSPI or
+// split-step on the team's row v (x-domain, x = t + T*m). CONJ selects -dz (the
+// source, and every row of the reference's modelling). Inactive rows keep v.
+template <int N, bool PSPI, int INTERP>
+__device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, bool active, const MigArgs &a,
+                                         const Smem<N, PSPI> &sm, float2 *xbuf, int iz, int t, int bar)
+{
+    constexpr int T = N / 16, HALF = MigShape<N>::HALF;
+    float2 sp[16];
+#pragma unroll
+    for (int m = 0; m < 16; m++) sp[m] = v[m];
+    fft_row<N, -1>(sp, xbuf, sm.tw, t, bar);
+    float2 acc[16];
+    if (PSPI) {
+        uint32_t sel[16];
+        float wl[16];
+        load_sel<N, INTERP>(a, iz, t, sel, wl);
+#pragma unroll
+        for (int m = 0; m < 16; m++) acc[m] = make_float2(0.f, 0.f);
+        for (int r = 0; r < a.nref; r++) {
+            const float2 *ph = sm.ph + (size_t)r * HALF;
+            float2 u[16];
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const float2 P = ph[kfold<N>(t, m)];
+                u[m] = conj ? cmulc(sp[m], P) : cmul(sp[m], P);
+            }
+            fft_row<N, +1>(u, xbuf, sm.tw, t, bar);
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                bool re_only;
+                const float wgt = sel_weight<INTERP>(sel[m], wl[m], r, re_only);
+                if (INTERP == 0) {
+                    // the nearest-lower wavefield, whole or its real part
+                    if (wgt != 0.f) acc[m] = re_only ? make_float2(u[m].x, 0.f) : u[m];
+                } else {
+                    acc[m].x += u[m].x * wgt;
+                    acc[m].y += u[m].y * wgt;
+                }
+            }
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const float2 P = sm.ph[kfold<N>(t, m)];
+            acc[m] = conj ? cmulc(sp[m], P) : cmul(sp[m], P);
+        }
+        fft_row<N, +1>(acc, xbuf, sm.tw, t, bar);
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            if (x < a.nmx) {
+                const float2 c = sm.corr[x];
+                acc[m] = conj ? cmulc(acc[m], c) : cmul(acc[m], c);
+            }
+        }
+    }
+    if (active) {
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            v[m] = x < a.nmx ? acc[m] : make_float2(0.f, 0.f);
+        }
+    }
+}
+
+// One upward step of the modelling recursion (wem.c:273-274, -dz, adj=false).
+// EXACT=false: the reference's operator -- PSPI as the migration step with -dz
+// (interpolation after the inverse FFTs); split-step with the taper and the
+// correction applied before the transform (wem.c:322-327).
+// EXACT=true: the exact adjoint of the migration step with +dz, for least squares:
+// PSPI scatters the row into the reference wavefields with the transposed
+// interpolation weights before transforming, y = sum_r F^-1 conj(P_r) F (W_r^T v);
+// for split-step the reference's operator already is that adjoint.
+template <int N, bool PSPI, int INTERP, bool EXACT>
+__device__ __forceinline__ void step_model(float2 (&v)[16], bool active, const MigArgs &a, const Smem<N, PSPI> &sm,
+                                           float2 *xbuf, int iz, int t, int bar)
+{
+    constexpr int T = N / 16, HALF = MigShape<N>::HALF;
+    if (PSPI && !EXACT) {
+        step_mig<N, PSPI, INTERP>(v, true, active, a, sm, xbuf, iz, t, bar);
+        return;
+    }
+    float2 acc[16];
+    if (!PSPI) {
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            acc[m] = x < a.nmx ? cmulc(v[m], sm.corr[x]) : make_float2(0.f, 0.f);
+        }
+        fft_row<N, -1>(acc, xbuf, sm.tw, t, bar);
+#pragma unroll
+        for (int m = 0; m < 16; m++) acc[m] = cmulc(acc[m], sm.ph[kfold<N>(t, m)]);
+    } else {
+        uint32_t sel[16];
+        float wl[16];
+        load_sel<N, INTERP>(a, iz, t, sel, wl);
+#pragma unroll
+        for (int m = 0; m < 16; m++) acc[m] = make_float2(0.f, 0.f);
+        for (int r = 0; r < a.nref; r++) {
+            float2 u[16];
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                bool re_only;
+                const float wgt = sel_weight<INTERP>(sel[m], wl[m], r, re_only);
+                u[m] = make_float2(v[m].x * wgt, re_only ? 0.f : v[m].y * wgt);
+            }
+            fft_row<N, -1>(u, xbuf, sm.tw, t, bar);
+            const float2 *ph = sm.ph + (size_t)r * HALF;
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const float2 q = cmulc(u[m], ph[kfold<N>(t, m)]);
+                acc[m].x += q.x;
+                acc[m].y += q.y;
+            }
+        }
+    }
+    fft_row<N, +1>(acc, xbuf, sm.tw, t, bar);
+    if (active) {
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            v[m] = x < a.nmx ? acc[m] : make_float2(0.f, 0.f);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ migration
 template <int N, bool PSPI, int INTERP, int S>
 __global__ void __launch_bounds__(2 * S * (N / 16)) wem_migrate_kernel(const MigArgs a)
 {
     using SH = MigShape<N>;
-    constexpr int T = SH::T, HALF = SH::HALF, PADN = SH::PADN;
+    constexpr int T = SH::T, PADN = SH::PADN;
     constexpr int NT = 2 * S * T;
     extern __shared__ float4 smem_raw[];
-    float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
-    float2 *s_ph = s_tw + SH::TWP;
-    const int nph = PSPI ? a.nref : 1;
-    float2 *s_corr = s_ph + (size_t)nph * HALF;           // split-step correction, [nmx]
-    const int ncorr = PSPI ? 0 : ((a.nmx + 1) & ~1);
-    float2 *s_x = s_corr + ncorr;                          // 2S exchange buffers
+    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx);
 
     const int tid = threadIdx.x;
     const int team = tid / T, t = tid - team * T;
     const bool is_src = team < S;
     const int sg = is_src ? team : team - S;               // shot within the group
-    float2 *xbuf = s_x + (size_t)team * PADN;
+    float2 *xbuf = sm.x + (size_t)team * PADN;
     const int bar = 1 + team;
 
-    for (int i = tid; i < SH::TW; i += NT) s_tw[i] = a.twid[i];
+    for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
 
     float2 *slot = a.slots + (size_t)blockIdx.x * a.nz * a.nmx;
     const int nitems = a.ngroups * a.nwf;
@@ -122,111 +325,12 @@ __global__ void __launch_bounds__(2 * S * (N / 16)) wem_migrate_kernel(const Mig
         }
 
         for (int iz = 0; iz < a.nz; iz++) {
-            __syncthreads();  // the previous step no longer reads s_ph / s_corr / s_x
-            if (PSPI) {
-                const float *vr = a.vref + (size_t)iz * a.nref;
-                for (int e = tid; e < a.nref * HALF; e += NT) {
-                    const int r = e / HALF, kk = e - r * HALF;
-                    const float v_ = vr[r];
-                    const float slow2 = __fdiv_rn(1.0f, __fmul_rn(v_, v_));
-                    s_ph[e] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
-                }
-            } else {
-                const float po = a.po[iz];
-                const float slow2 = __fmul_rn(po, po);
-                for (int e = tid; e < HALF; e += NT)
-                    s_ph[e] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)e), a.dz, a.inv_n);
-                // split-step correction exp(i w pd dz) times the taper (wem.c:353-359)
-                const float *pd = a.pd + (size_t)iz * nmx;
-                for (int x = tid; x < nmx; x += NT) {
-                    const float th = __fmul_rn(__fmul_rn(w, pd[x]), a.dz);
-                    float sn, cs;
-                    sincosf(th, &sn, &cs);
-                    const float tp = a.taper[x];
-                    s_corr[x] = make_float2(cs * tp, sn * tp);
-                }
-            }
+            __syncthreads();  // the previous step no longer reads the tables / exchange buffers
+            build_tables<N, PSPI>(a, sm, w, w2, iz, tid, NT);
             __syncthreads();
-
             const uint8_t zf = a.zflag[iz];
-            const bool active = is_src ? (zf & Z_SRC) : (zf & Z_REC);
-
-            // ---- one depth step of this team's row (all teams run it; inactive
-            //      rows discard the result so that barriers stay uniform)
-            float2 sp[16];
-#pragma unroll
-            for (int m = 0; m < 16; m++) sp[m] = v[m];
-            fft_row<N, -1>(sp, xbuf, s_tw, t, bar);
-
-            float2 acc[16];
-            if (PSPI) {
-                uint32_t sel[16];
-                float wl[16];
-                const uint32_t *selr = a.sel + (size_t)iz * nmx;
-                const float *wlr = a.wlin + (size_t)iz * nmx;
-#pragma unroll
-                for (int m = 0; m < 16; m++) {
-                    const int x = t + T * m;
-                    acc[m] = make_float2(0.f, 0.f);
-                    sel[m] = x < nmx ? selr[x] : 0xffffu;   // never matches a reference
-                    wl[m] = (INTERP == 1 && x < nmx) ? wlr[x] : 0.f;
-                }
-                for (int r = 0; r < a.nref; r++) {
-                    const float2 *ph = s_ph + (size_t)r * HALF;
-                    float2 u[16];
-#pragma unroll
-                    for (int m = 0; m < 16; m++) {
-                        const int k = t + T * m;
-                        const int kk = k <= N / 2 ? k : N - k;
-                        const float2 P = ph[kk];
-                        u[m] = is_src ? cmulc(sp[m], P) : cmul(sp[m], P);
-                    }
-                    fft_row<N, +1>(u, xbuf, s_tw, t, bar);
-#pragma unroll
-                    for (int m = 0; m < 16; m++) {
-                        const uint32_t s_ = sel[m];
-                        const int i1 = s_ & 0xff, i2 = (s_ >> 8) & 0xff;
-                        const bool interp = (s_ & SEL_INTERP) != 0;
-                        if (INTERP == 0) {
-                            // wem.c:454-459 with linear_interp's float return (wem.c:477)
-                            if (r == i1) acc[m] = interp ? make_float2(u[m].x, 0.f) : u[m];
-                        } else {
-                            if (!interp) {
-                                if (r == i1) acc[m] = u[m];
-                            } else {
-                                if (r == i1) { acc[m].x += u[m].x * (1.f - wl[m]); acc[m].y += u[m].y * (1.f - wl[m]); }
-                                if (r == i2) { acc[m].x += u[m].x * wl[m]; acc[m].y += u[m].y * wl[m]; }
-                            }
-                        }
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int m = 0; m < 16; m++) {
-                    const int k = t + T * m;
-                    const int kk = k <= N / 2 ? k : N - k;
-                    const float2 P = s_ph[kk];
-                    acc[m] = is_src ? cmulc(sp[m], P) : cmul(sp[m], P);
-                }
-                fft_row<N, +1>(acc, xbuf, s_tw, t, bar);
-#pragma unroll
-                for (int m = 0; m < 16; m++) {
-                    const int x = t + T * m;
-                    if (x < nmx) {
-                        const float2 c = s_corr[x];
-                        acc[m] = is_src ? cmulc(acc[m], c) : cmul(acc[m], c);
-                    } else {
-                        acc[m] = make_float2(0.f, 0.f);
-                    }
-                }
-            }
-            if (active) {
-#pragma unroll
-                for (int m = 0; m < 16; m++) {
-                    const int x = t + T * m;
-                    v[m] = x < nmx ? acc[m] : make_float2(0.f, 0.f);
-                }
-            }
+            // all teams run the step (barriers stay uniform); inactive rows keep v
+            step_mig<N, PSPI, INTERP>(v, is_src, is_src ? (zf & Z_SRC) : (zf & Z_REC), a, sm, xbuf, iz, t, bar);
 
             // ---- imaging condition (wem.c:243-247), summed over the group's shots
             if (zf & Z_REC) {
@@ -239,7 +343,7 @@ __global__ void __launch_bounds__(2 * S * (N / 16)) wem_migrate_kernel(const Mig
                 }
                 __syncthreads();
                 if (!is_src) {
-                    const float2 *us = s_x + (size_t)sg * PADN;
+                    const float2 *us = sm.x + (size_t)sg * PADN;
                     float *cv = reinterpret_cast<float *>(xbuf);
 #pragma unroll
                     for (int m = 0; m < 16; m++) {
@@ -255,9 +359,97 @@ __global__ void __launch_bounds__(2 * S * (N / 16)) wem_migrate_kernel(const Mig
                 for (int x = tid; x < nmx; x += NT) {
                     float c = 0.f;
 #pragma unroll
-                    for (int s_ = 0; s_ < S; s_++) c += reinterpret_cast<const float *>(s_x + (size_t)(S + s_) * PADN)[x];
+                    for (int s_ = 0; s_ < S; s_++) c += reinterpret_cast<const float *>(sm.x + (size_t)(S + s_) * PADN)[x];
                     kahan_add(&srow[x], c);
                 }
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ modelling (Born)
+// One team per shot. Per (group of S shots, frequency): the source wavefield is
+// continued down and kept at every depth in global scratch (smig, wem.c:253-265),
+// then the receiver wavefield is continued up from the bottom with the image
+// injected at each depth (wem.c:266-276); the surface row, divided by
+// sqrt(ntfft) (wem.c:277-279), is the shot's spectrum at this frequency.
+template <int N, bool PSPI, int INTERP, int S, bool EXACT>
+__global__ void __launch_bounds__(S * (N / 16)) wem_model_kernel(const MigArgs a, const BornArgs b)
+{
+    using SH = MigShape<N>;
+    constexpr int T = SH::T, PADN = SH::PADN;
+    constexpr int NT = S * T;
+    extern __shared__ float4 smem_raw[];
+    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx);
+    const int tid = threadIdx.x;
+    const int team = tid / T, t = tid - team * T;
+    float2 *xbuf = sm.x + (size_t)team * PADN;
+    const int bar = 1 + team;
+    for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
+
+    const int nmx = a.nmx, nz = a.nz;
+    float2 *smig = b.smig + ((size_t)blockIdx.x * S + team) * (size_t)nz * nmx;
+    const int nitems = a.ngroups * a.nwf;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int g = item % a.ngroups;
+        const int iwi = item / a.ngroups;
+        const int shot = g * S + team;
+        const bool shot_ok = shot < a.nshot;
+        const int iw = a.ifmin + iwi;
+        const float w = __fmul_rn((float)iw, a.dw);
+        const float w2 = __fmul_rn(w, w);
+        float2 v[16];
+        const int igx = shot_ok ? a.igx[shot] : -1;
+        const float2 sw = a.srcw[iwi];
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            v[m] = (x < nmx && x == igx) ? sw : make_float2(0.f, 0.f);
+        }
+        // source, downward (wem.c:255-265)
+        for (int iz = 0; iz < nz; iz++) {
+            __syncthreads();
+            build_tables<N, PSPI>(a, sm, w, w2, iz, tid, NT);
+            __syncthreads();
+            const bool act = (a.zflag[iz] & Z_SRC) != 0;
+            step_mig<N, PSPI, INTERP>(v, true, act, a, sm, xbuf, iz, t, bar);
+            float2 *row = smig + (size_t)iz * nmx;
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int x = t + T * m;
+                if (x < nmx) row[x] = act ? v[m] : make_float2(0.f, 0.f);
+            }
+        }
+        // receiver, upward with injection (wem.c:266-276)
+#pragma unroll
+        for (int m = 0; m < 16; m++) v[m] = make_float2(0.f, 0.f);
+        for (int iz = nz - 1; iz >= 0; iz--) {
+            __syncthreads();
+            build_tables<N, PSPI>(a, sm, w, w2, iz, tid, NT);
+            __syncthreads();
+            const bool act = (a.zflag[iz] & Z_REC) != 0;
+            if (act) {
+                const float2 *row = smig + (size_t)iz * nmx;
+                const float *mr = b.img + (size_t)iz * nmx;
+#pragma unroll
+                for (int m = 0; m < 16; m++) {
+                    const int x = t + T * m;
+                    if (x < nmx) {
+                        const float mv = mr[x];
+                        const float2 s_ = row[x];
+                        v[m].x += mv * s_.x;
+                        v[m].y += mv * s_.y;
+                    }
+                }
+            }
+            step_model<N, PSPI, INTERP, EXACT>(v, act, a, sm, xbuf, iz, t, bar);
+        }
+        if (shot_ok) {
+            float2 *out = b.dg + ((size_t)shot * a.nwf + iwi) * nmx;
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int x = t + T * m;
+                if (x < nmx) out[x] = make_float2(v[m].x * b.inv_sqt, v[m].y * b.inv_sqt);
             }
         }
     }
@@ -321,6 +513,88 @@ __global__ void __launch_bounds__(256) wem_spectra_kernel(const SpectraArgs a)
                 a.out[base + (int64_t)f * a.out_fstride] = make_float2(acc[i][j].x * sc, acc[i][j].y * sc);
             }
         }
+    }
+}
+
+// ------------------------------------------------------------------ synthesis
+// out[tr][t] = sum_f Re(scale[f] * dg[in_base[tr] + f*fstride] * e^{+2 pi i (ifmin+f) t / nf}), t < nt:
+// the half-spectrum inverse transform of f_op (wem.c:501-511) restricted to the
+// processed band, after the w^2 weighting of wem.c:179-184.
+// Tile: 32 traces x 64 samples per CTA of 256 threads, frequencies staged 32 at a time.
+__global__ void __launch_bounds__(256) wem_synth_kernel(const SynthArgs a)
+{
+    constexpr int TR = 32, TS = 64, KC = 32;
+    __shared__ float2 s_a[TR][KC + 1];
+    __shared__ float2 s_w[KC][TS];
+    const int tid = threadIdx.x;
+    const int tr0 = blockIdx.x * TR, t0 = blockIdx.y * TS;
+    const int tx = tid & 15, ty = tid >> 4;
+    float acc[2][4];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = 0.f;
+    for (int f0 = 0; f0 < a.nwf; f0 += KC) {
+        __syncthreads();
+        for (int e = tid; e < TR * KC; e += 256) {
+            const int i = e / KC, k = e - i * KC;
+            const int tr = tr0 + i, f = f0 + k;
+            float2 v = make_float2(0.f, 0.f);
+            if (tr < a.ntr && f < a.nwf) {
+                const float2 q = a.dg[a.in_base[tr] + (int64_t)f * a.in_fstride];
+                const float sc = a.scale[f];
+                v = make_float2(q.x * sc, q.y * sc);
+            }
+            s_a[i][k] = v;
+        }
+        for (int e = tid; e < KC * TS; e += 256) {
+            const int k = e / TS, j = e - k * TS;
+            const int iw = a.ifmin + f0 + k, ts = t0 + j;
+            float2 wv = make_float2(0.f, 0.f);
+            if (f0 + k < a.nwf && ts < a.nt) {
+                const float2 q = a.wtab[(int)(((long long)iw * ts) % a.nf)];
+                wv = make_float2(q.x, -q.y);  // e^{+i theta}
+            }
+            s_w[k][j] = wv;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int k = 0; k < KC; k++) {
+            const float2 a0 = s_a[ty * 2][k], a1 = s_a[ty * 2 + 1][k];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float2 wv = s_w[k][tx * 4 + j];
+                acc[0][j] = fmaf(a0.x, wv.x, fmaf(-a0.y, wv.y, acc[0][j]));
+                acc[1][j] = fmaf(a1.x, wv.x, fmaf(-a1.y, wv.y, acc[1][j]));
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        const int tr = tr0 + ty * 2 + i;
+        if (tr >= a.ntr) continue;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int ts = t0 + tx * 4 + j;
+            if (ts < a.nt) a.out[(size_t)tr * a.nt + ts] = acc[i][j];
+        }
+    }
+}
+
+// out[c][r] = in[r][c] (rows x cols), 32x32 tiles
+__global__ void __launch_bounds__(256) wem_transpose_kernel(const float *in, int rows, int cols, float *out)
+{
+    __shared__ float tile[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;
+    for (int j = ly; j < 32; j += 8) {
+        const int r = r0 + j, c = c0 + lx;
+        tile[j][lx] = (r < rows && c < cols) ? in[(size_t)r * cols + c] : 0.f;
+    }
+    __syncthreads();
+    for (int j = ly; j < 32; j += 8) {
+        const int c = c0 + j, r = r0 + lx;
+        if (c < cols && r < rows) out[(size_t)c * rows + r] = tile[lx][j];
     }
 }
 
@@ -505,6 +779,105 @@ int launch_image_reduce(const float2 *slots, int nslots, int nz, int nmx, float 
 {
     dim3 grid((nmx + 31) / 32, (nz + 31) / 32);
     wem_image_reduce_kernel<<<grid, 256, 0, st>>>(slots, nslots, nz, nmx, m);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// ---------------------------------------------------------------- modelling launchers
+template <int N> struct DispatchModel {
+    static constexpr int T = N / 16;
+    // one row team per shot; aim at 256 threads
+    static constexpr int S = (T >= 256) ? 1 : (256 / T > 8 ? 8 : 256 / T);
+};
+
+template <int N>
+static void model_config_n(int pspi, int nmx, int nref, int *S, int *threads, size_t *smem)
+{
+    using SH = MigShape<N>;
+    *S = DispatchModel<N>::S;
+    *threads = DispatchModel<N>::S * SH::T;
+    *smem = mig_smem_bytes(SH::TWP, SH::HALF, SH::PADN, pspi ? nref : 1, pspi ? 0 : nmx, DispatchModel<N>::S);
+}
+
+int model_config(int nkx, int pspi, int nmx, int nref, int *S, int *threads, size_t *smem)
+{
+    switch (nkx) {
+    case 32: model_config_n<32>(pspi, nmx, nref, S, threads, smem); return 0;
+    case 64: model_config_n<64>(pspi, nmx, nref, S, threads, smem); return 0;
+    case 128: model_config_n<128>(pspi, nmx, nref, S, threads, smem); return 0;
+    case 256: model_config_n<256>(pspi, nmx, nref, S, threads, smem); return 0;
+    case 512: model_config_n<512>(pspi, nmx, nref, S, threads, smem); return 0;
+    case 1024: model_config_n<1024>(pspi, nmx, nref, S, threads, smem); return 0;
+    case 2048: model_config_n<2048>(pspi, nmx, nref, S, threads, smem); return 0;
+    case 4096: model_config_n<4096>(pspi, nmx, nref, S, threads, smem); return 0;
+    default: return -1;
+    }
+}
+
+template <int N, bool PSPI, int INTERP, bool EXACT>
+static int model_n(const MigArgs *a, const BornArgs *b, int grid, size_t smem, cudaStream_t st, int threads, int *bps)
+{
+    constexpr int S = DispatchModel<N>::S;
+    auto k = wem_model_kernel<N, PSPI, INTERP, S, EXACT>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    if (bps) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, threads, smem) == cudaSuccess ? 0 : -1;
+    k<<<grid, S * (N / 16), smem, st>>>(*a, *b);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N>
+static int model_sel(int pspi, int interp, int exact, const MigArgs *a, const BornArgs *b, int grid, size_t smem,
+                     cudaStream_t st, int threads, int *bps)
+{
+    if (!pspi) return model_n<N, false, 0, false>(a, b, grid, smem, st, threads, bps);
+    if (exact) {
+        if (interp == 0) return model_n<N, true, 0, true>(a, b, grid, smem, st, threads, bps);
+        return model_n<N, true, 1, true>(a, b, grid, smem, st, threads, bps);
+    }
+    if (interp == 0) return model_n<N, true, 0, false>(a, b, grid, smem, st, threads, bps);
+    return model_n<N, true, 1, false>(a, b, grid, smem, st, threads, bps);
+}
+
+static int model_dispatch(int nkx, int pspi, int interp, int exact, const MigArgs *a, const BornArgs *b, int grid,
+                          size_t smem, cudaStream_t st, int threads, int *bps)
+{
+    switch (nkx) {
+    case 32: return model_sel<32>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
+    case 64: return model_sel<64>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
+    case 128: return model_sel<128>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
+    case 256: return model_sel<256>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
+    case 512: return model_sel<512>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
+    case 1024: return model_sel<1024>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
+    case 2048: return model_sel<2048>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
+    case 4096: return model_sel<4096>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
+    default: return -1;
+    }
+}
+
+int model_max_grid(int nkx, int pspi, int interp, int exact, int threads, size_t smem, int *bps)
+{
+    return model_dispatch(nkx, pspi, interp, exact, nullptr, nullptr, 0, smem, 0, threads, bps);
+}
+
+int launch_model(int nkx, int pspi, int interp, int exact, const MigArgs &a, const BornArgs &b, int grid, cudaStream_t st)
+{
+    int S, th;
+    size_t smem;
+    if (model_config(nkx, pspi, a.nmx, a.nref, &S, &th, &smem)) return -1;
+    return model_dispatch(nkx, pspi, interp, exact, &a, &b, grid, smem, st, th, nullptr);
+}
+
+int launch_synth(const SynthArgs &a, cudaStream_t st)
+{
+    if (a.ntr <= 0 || a.nt <= 0) return 0;
+    dim3 grid((a.ntr + 31) / 32, (a.nt + 63) / 64);
+    wem_synth_kernel<<<grid, 256, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_transpose(const float *in, int rows, int cols, float *out, cudaStream_t st)
+{
+    dim3 grid((cols + 31) / 32, (rows + 31) / 32);
+    wem_transpose_kernel<<<grid, 256, 0, st>>>(in, rows, cols, out);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
