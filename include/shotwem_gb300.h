@@ -125,6 +125,26 @@ WEM_API int wem_last_kernel_times(wem_ctx *ctx, float *ms_spectra, float *ms_ext
 /* The cudaStream_t (as void*) on which ctx orders all its work. */
 WEM_API int wem_ctx_stream(wem_ctx *ctx, void **stream);
 
+/* Migration of nshot shots that allocates nothing -- no counterpart in the reference.
+   For callers that cannot call cudaMalloc/cudaFree while they run (an application that
+   gives all device memory to its own pool at start-up, or a loop with a fixed memory
+   budget): the caller passes device buffers for every input and the output, and all
+   working memory comes from one fixed 24 MiB device array inside the library, which
+   every GPU that loads shotwem.so holds until the process exits.
+   vel_dev [nmx][nz], wav_dev [nt], d_dev [nshot][nmx][nt] (every shot on the full
+   grid), m_dev [nmx][nz] (overwritten); sx, sy: host arrays of nshot source
+   positions (sy may be NULL); stream: a cudaStream_t or NULL; the call returns when
+   the result is in m_dev. 2-D only; padx*nmx in {256, 512, 1024, 2048}; nmx, nz <= 1024;
+   nref <= 16; nshot <= 64; and the tables (12*nz*nmx bytes), trace spectra
+   (8*nshot*nfreq*nmx bytes) and image (4*nz*nmx bytes) must fit the 24 MiB together --
+   larger surveys return WEM_ERR_SIZE. The first call on a device (made current by the
+   caller) looks up the array's device address; make that first call before any stream
+   capture. Calls share the array: calls that overlap on the GPU (other streams, other
+   host threads) race and corrupt each other. The image is summed with atomic additions,
+   so its last bits can vary from run to run. */
+WEM_API int wem_migrate_noalloc(const wem_params *p, const float *vel_dev, const float *wav_dev, int nshot,
+                                const float *sx, const float *sy, const float *d_dev, float *m_dev, void *stream);
+
 /* Drop-in for the reference's wem() (wem.h:3-11). Same arguments, float** rows as
    alloc2float builds them (seismic.c:92-106). Returns a status instead of void.
    adj=true: d -> m (m overwritten); adj=false: m -> d (d overwritten). */

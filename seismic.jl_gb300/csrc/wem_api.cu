@@ -84,6 +84,11 @@ struct wem_ctx {
     int last_nshot = -1;
 };
 
+namespace gbwem {
+// lets other translation units of the library report through wem_last_error()
+int set_error(int code, const char *msg) { return fail(code, "%s", msg); }
+}  // namespace gbwem
+
 extern "C" const char *wem_last_error(void) { return g_err; }
 extern "C" int wem_version(void) { return 100; }
 
