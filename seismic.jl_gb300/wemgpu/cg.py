@@ -1,0 +1,67 @@
+"""Conjugate gradients for least-squares migration.
+
+Restates src/Solvers/ConjugateGradients.jl:1-39 (Algorithm 2 of Scales, 1987, "Tomographic
+inversion via the conjugate gradient method"): minimise ||L m - d||^2 + mu ||m||^2 given a
+forward operator L and its adjoint L'. Differences from the reference: inner products are
+accumulated in float64 (the reference's InnerProduct returns Float32, src/Tools/InnerProduct.jl:1-5,
+too coarse for a 1e-5 dot test), and the operator pair is two callables instead of a list of
+Julia operators chained by LinearOperator (src/Operators/LinearOperator.jl:1-22).
+
+The cost history is normalised by the initial residual <d, d> like the reference's.
+"""
+from __future__ import annotations
+
+from typing import Callable
+
+import numpy as np
+
+
+def inner(a: np.ndarray, b: np.ndarray) -> float:
+    """Re(sum(conj(a) * b)) in float64 (src/Tools/InnerProduct.jl:1-5 in FP32)."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    if np.iscomplexobj(a) or np.iscomplexobj(b):
+        return float(np.real(np.vdot(a.astype(np.complex128).ravel(), b.astype(np.complex128).ravel())))
+    return float(np.dot(a.astype(np.float64).ravel(), b.astype(np.float64).ravel()))
+
+
+def conjugate_gradients(d: np.ndarray, forward: Callable[[np.ndarray], np.ndarray],
+                        adjoint: Callable[[np.ndarray], np.ndarray], niter: int = 10, mu: float = 0.0,
+                        tol: float = 1.0e-15, callback: Callable | None = None):
+    """Returns (m, cost) with cost[0] = 1 and cost[i] = (||r||^2 + mu ||m||^2)/||d||^2."""
+    cost = [1.0]
+    r = np.array(d, copy=True)
+    g = adjoint(r)
+    m = np.zeros_like(g)
+    s = np.array(g, copy=True)
+    gamma = inner(g, g)
+    gamma00 = gamma
+    cost0 = inner(r, r)
+    for it in range(1, niter + 1):
+        t = forward(s)
+        delta = inner(t, t) + mu * inner(s, s)
+        if delta <= tol:
+            break
+        alpha = gamma / delta
+        m = m + alpha * s
+        r = r - alpha * t
+        g = adjoint(r)
+        g = g - mu * m
+        gamma0 = gamma
+        gamma = inner(g, g)
+        cost1 = inner(r, r) + mu * inner(m, m)
+        cost.append(cost1 / cost0 if cost0 > 0 else 0.0)
+        beta = gamma / gamma0
+        s = beta * s + g
+        if callback is not None:
+            callback(it, m, cost[-1])
+        if np.sqrt(gamma) <= np.sqrt(gamma00) * tol:
+            break
+    return m, np.asarray(cost)
+
+
+def dot_test(forward, adjoint, m_rand: np.ndarray, d_rand: np.ndarray):
+    """<d, L m> and <L' d, m> (src/Tools/DotTest.jl:1-12) in float64."""
+    d_fwd = forward(m_rand)
+    m_adj = adjoint(d_rand)
+    return inner(d_rand, d_fwd), inner(m_rand, m_adj)
