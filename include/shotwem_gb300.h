@@ -109,6 +109,23 @@ WEM_API int wem_migrate_device(wem_ctx *ctx, int nshot, const float *sx, const f
                        const int64_t *trace_offset, const int32_t *trace_cell,
                        const float *d_dev, float *m_dev, int sync);
 
+/* Modelling (wem.c adj=false, wem.c:252-281 and 177-188): the data the image m
+   ([nmx*nmy][nz], host) produces for each of nshot shots, at the traces given by
+   trace_offset / trace_cell (as in wem_migrate); d: [ntrace][nt] host, overwritten.
+   exact = 0: the reference's operator (its PSPI interpolation after the inverse FFTs,
+   the half-spectrum weights of its real inverse transform); exact = 1: the exact
+   adjoint of wem_migrate with the same parameters, for least-squares migration
+   (the two differ only for PSPI in laterally varying velocity and at the Nyquist
+   frequency). */
+WEM_API int wem_model(wem_ctx *ctx, int nshot, const float *sx, const float *sy,
+                      const int64_t *trace_offset, const int32_t *trace_cell,
+                      const float *m, float *d, int exact);
+
+/* Same, with m and d in device memory, ordered on ctx's stream. */
+WEM_API int wem_model_device(wem_ctx *ctx, int nshot, const float *sx, const float *sy,
+                             const int64_t *trace_offset, const int32_t *trace_cell,
+                             const float *m_dev, float *d_dev, int exact, int sync);
+
 /* One-call convenience: wem_prepare + wem_migrate. */
 WEM_API int wem_migrate_survey(wem_ctx *ctx, const wem_params *p, const float *vel, const float *wav,
                        int nshot, const float *sx, const float *sy, const int64_t *trace_offset,

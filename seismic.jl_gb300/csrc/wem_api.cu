@@ -71,13 +71,15 @@ struct wem_ctx {
 
     bool prepared = false;
     wem_params p{};
-    int ntfft = 0, nw = 0, ifmin = 0, ifmax = 0, nwf = 0, nkx = 0, nky = 0;
+    int ntfft = 0, nw = 0, nf = 0, ifmin = 0, ifmax = 0, nwf = 0, nkx = 0, nky = 0;
     float dw = 0.f, dkx = 0.f;
 
     // per-velocity tables
     DevBuf vref, po, pd, sel, wlin, taper, zflag, twid, wtab, scale_recv, scale_src, srcw, wav, wav_base;
+    DevBuf ssyn_ref, ssyn_exact;  // synthesis weights w^2 * (half-spectrum | image) factor
     // per-call buffers
-    DevBuf recv, slots, image, data, tbase, igx;
+    DevBuf recv, slots, image, data, tbase, igx, smig, mimg;
+    int max_smem = 0;
     // host copies of the last shot metadata (skip re-uploads)
     std::vector<int64_t> h_tbase;
     std::vector<int> h_igx;
@@ -109,6 +111,7 @@ extern "C" int wem_ctx_create(wem_ctx **out, int device)
     CK(cudaEventCreate(&c->ev1));
     for (int i = 0; i < 4; i++) CK(cudaEventCreate(&c->evk[i]));
     CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
+    CK(cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
     *out = c;
     return WEM_OK;
 }
@@ -120,7 +123,8 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
     if (c->st) cudaStreamSynchronize(c->st);
     DevBuf *bufs[] = { &c->vref, &c->po, &c->pd, &c->sel, &c->wlin, &c->taper, &c->zflag, &c->twid,
                        &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
-                       &c->recv, &c->slots, &c->image, &c->data, &c->tbase, &c->igx };
+                       &c->ssyn_ref, &c->ssyn_exact, &c->recv, &c->slots, &c->image, &c->data,
+                       &c->tbase, &c->igx, &c->smig, &c->mimg };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -214,7 +218,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     // a1: slowness split (wem.c:28-36); a2: reference velocities (wem.c:40-70).
     // Device layouts are depth-major ([iz][ix]) so that a depth step reads a row.
     std::vector<float> po(nz), pd((size_t)nz * nmx), vref((size_t)nz * nref), wl((size_t)nz * nmx, 0.f);
-    std::vector<uint32_t> sel((size_t)nz * nmx);
+    std::vector<uint8_t> sel((size_t)nz * nmx);
     for (int iz = 0; iz < nz; iz++) {
         float s = 0.;
         for (int ix = 0; ix < n; ix++) s += vel[(size_t)ix * nz + iz];
@@ -238,7 +242,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
                 if (ir > nref - 2) { i1 = nref - 1; i2 = nref - 1; }
             }
             const float vr1 = vref[(size_t)iz * nref + i1], vr2 = vref[(size_t)iz * nref + i2];
-            uint32_t word = (uint32_t)i1 | ((uint32_t)i2 << 8);
+            uint8_t word = (uint8_t)i1;  // where it interpolates, i2 = i1 + 1
             if (vr2 - vr1 > 10.0) {
                 word |= SEL_INTERP;
                 wl[(size_t)iz * nmx + ix] = (v - vr1) / (vr2 - vr1);
@@ -266,42 +270,57 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     const int ntw = twiddle_table_size(nkx);
     std::vector<float2> tw(ntw > 0 ? ntw : 1);
     twiddle_table_host(nkx, tw.data());
-    std::vector<float2> wtab(ntfft);
-    for (int k = 0; k < ntfft; k++) {
-        const double a = -6.283185307179586476925286766559 * (double)k / (double)ntfft;
+    // the real transform of f_op has length (nw-1)*2 (wem.c:487), which is ntfft - 1
+    // when padt*nt is odd
+    const int nf = (nw - 1) * 2;
+    if (nf < 2) return fail(WEM_ERR_ARG, "wem_prepare: trace too short (nt=%d, padt=%d)", p.nt, p.padt);
+    std::vector<float2> wtab(nf);
+    for (int k = 0; k < nf; k++) {
+        const double a = -6.283185307179586476925286766559 * (double)k / (double)nf;
         wtab[k] = make_float2((float)cos(a), (float)sin(a));
     }
     // receiver weights w^2 (wem.c:128-129) and the 1/sqrtf(ntfft) of wem.c:231-232
     std::vector<float> srec(nwf > 0 ? nwf : 1), ssrc(nwf > 0 ? nwf : 1);
+    // modelling: D = w^2 d_g (wem.c:179-184) and the weights of the half-spectrum
+    // inverse transform (c2r: 1 at DC and Nyquist, 2 elsewhere) -- or, for the exact
+    // adjoint of the migration, its image weights (1 at DC, 2 elsewhere, wem.c:226-227)
+    std::vector<float> syn_ref(nwf > 0 ? nwf : 1), syn_exact(nwf > 0 ? nwf : 1);
     const float sq = sqrtf((float)ntfft);
     for (int i = 0; i < nwf; i++) {
-        const float w = (ifmin + i) * dw;
+        const int iw = ifmin + i;
+        const float w = iw * dw;
         srec[i] = (float)((double)(w * w) / (double)sq);
         ssrc[i] = (float)(1.0 / (double)sq);
+        syn_ref[i] = (w * w) * ((iw == 0 || 2 * iw == (nw - 1) * 2) ? 1.f : 2.f);
+        syn_exact[i] = (w * w) * (iw == 0 ? 1.f : 2.f);
     }
 
     int rc;
     if ((rc = ensure(c->po, sizeof(float) * nz)) || (rc = ensure(c->pd, sizeof(float) * pd.size())) ||
-        (rc = ensure(c->vref, sizeof(float) * vref.size())) || (rc = ensure(c->sel, sizeof(uint32_t) * sel.size())) ||
+        (rc = ensure(c->vref, sizeof(float) * vref.size())) || (rc = ensure(c->sel, sel.size())) ||
         (rc = ensure(c->wlin, sizeof(float) * wl.size())) || (rc = ensure(c->taper, sizeof(float) * nmx)) ||
         (rc = ensure(c->zflag, nz)) || (rc = ensure(c->twid, sizeof(float2) * tw.size())) ||
-        (rc = ensure(c->wtab, sizeof(float2) * ntfft)) || (rc = ensure(c->scale_recv, sizeof(float) * srec.size())) ||
+        (rc = ensure(c->wtab, sizeof(float2) * nf)) || (rc = ensure(c->scale_recv, sizeof(float) * srec.size())) ||
         (rc = ensure(c->scale_src, sizeof(float) * ssrc.size())) || (rc = ensure(c->srcw, sizeof(float2) * (nwf > 0 ? nwf : 1))) ||
-        (rc = ensure(c->wav, sizeof(float) * p.nt)) || (rc = ensure(c->wav_base, sizeof(int64_t))))
+        (rc = ensure(c->wav, sizeof(float) * p.nt)) || (rc = ensure(c->wav_base, sizeof(int64_t))) ||
+        (rc = ensure(c->ssyn_ref, sizeof(float) * syn_ref.size())) ||
+        (rc = ensure(c->ssyn_exact, sizeof(float) * syn_exact.size())))
         return rc;
     cudaStream_t st = c->st;
     CK(cudaMemcpyAsync(c->po.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->pd.p, pd.data(), sizeof(float) * pd.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->vref.p, vref.data(), sizeof(float) * vref.size(), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(c->sel.p, sel.data(), sizeof(uint32_t) * sel.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->sel.p, sel.data(), sel.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->wlin.p, wl.data(), sizeof(float) * wl.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->taper.p, taper.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->zflag.p, zf.data(), nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->twid.p, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(c->wtab.p, wtab.data(), sizeof(float2) * ntfft, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->wtab.p, wtab.data(), sizeof(float2) * nf, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->scale_recv.p, srec.data(), sizeof(float) * srec.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->scale_src.p, ssrc.data(), sizeof(float) * ssrc.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->wav.p, wav, sizeof(float) * p.nt, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->ssyn_ref.p, syn_ref.data(), sizeof(float) * syn_ref.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->ssyn_exact.p, syn_exact.data(), sizeof(float) * syn_exact.size(), cudaMemcpyHostToDevice, st));
     const int64_t zero = 0;
     CK(cudaMemcpyAsync(c->wav_base.p, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, st));
     // wavelet spectrum over the band (wem.c:112-119 with the 1/sqrtf(ntfft) of wem.c:231)
@@ -310,7 +329,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         sa.d = P<float>(c->wav);
         sa.ntr = 1;
         sa.nt = p.nt;
-        sa.ntfft = ntfft;
+        sa.ntfft = nf;
         sa.ifmin = ifmin;
         sa.nwf = nwf;
         sa.out_base = P<int64_t>(c->wav_base);
@@ -325,6 +344,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     c->p = p;
     c->ntfft = ntfft;
     c->nw = nw;
+    c->nf = nf;
     c->ifmin = ifmin;
     c->ifmax = ifmax;
     c->nwf = nwf;
@@ -378,6 +398,17 @@ static int set_shots(wem_ctx *c, int nshot, const float *sx, const float *sy, co
     return WEM_OK;
 }
 
+static int cta_shape(wem_ctx *c, int pspi, int nmx, int nref)
+{
+    const char *e = getenv("WEM_CTA_SHAPE");
+    if (e && !strcmp(e, "narrow")) return 0;
+    int S, th;
+    size_t smem;
+    if (migrate_config(c->nkx, 1, pspi, nmx, nref, &S, &th, &smem)) return 0;
+    if (e && !strcmp(e, "wide")) return 1;
+    return (int)smem <= c->max_smem ? 1 : 0;
+}
+
 // GPU part of a migration: spectra -> depth recursion -> image. Stream-ordered on c->st.
 static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, float *m_dev)
 {
@@ -386,8 +417,15 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
     const int nmx = p.nmx, nz = p.nz;
     int S, threads, bps = 0;
     size_t smem;
-    if (migrate_config(c->nkx, p.pspi, nmx, p.nref, &S, &threads, &smem)) return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
-    if (migrate_max_grid(c->nkx, p.pspi, p.interp, S, threads, smem, &bps) || bps < 1)
+    // the 512-thread shape shares one set of phase tables among more rows; use it when
+    // its shared memory fits (WEM_CTA_SHAPE=narrow|wide overrides, for tuning)
+    const int wide = cta_shape(c, p.pspi, nmx, p.nref);
+    if (migrate_config(c->nkx, wide, p.pspi, nmx, p.nref, &S, &threads, &smem))
+        return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
+    if ((int)smem > c->max_smem)
+        return fail(WEM_ERR_SIZE, "nref=%d needs %zu B of shared memory per CTA (device limit %d B)", p.nref, smem,
+                    c->max_smem);
+    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, nmx, p.nref, &bps) || bps < 1)
         return fail(WEM_ERR_CUDA, "kernel does not fit on the device (smem %zu B, %d threads): %s", smem, threads,
                     cudaGetErrorString(cudaGetLastError()));
     const int ngroups = (nshot + S - 1) / S;
@@ -409,7 +447,7 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
         sa.d = d_dev;
         sa.ntr = (int)ntr;
         sa.nt = p.nt;
-        sa.ntfft = c->ntfft;
+        sa.ntfft = c->nf;
         sa.ifmin = c->ifmin;
         sa.nwf = c->nwf;
         sa.out_base = P<int64_t>(c->tbase);
@@ -440,13 +478,13 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
         a.vref = P<float>(c->vref);
         a.po = P<float>(c->po);
         a.pd = P<float>(c->pd);
-        a.sel = P<uint32_t>(c->sel);
+        a.selb = P<uint8_t>(c->sel);
         a.wlin = P<float>(c->wlin);
         a.taper = P<float>(c->taper);
         a.zflag = P<uint8_t>(c->zflag);
         a.twid = P<float2>(c->twid);
         a.slots = P<float2>(c->slots);
-        if (launch_migrate(c->nkx, p.pspi, p.interp, S, a, grid, st))
+        if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, grid, st))
             return fail(WEM_ERR_CUDA, "migrate launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;
     }
@@ -508,6 +546,111 @@ extern "C" int wem_migrate_survey(wem_ctx *c, const wem_params *p, const float *
     return wem_migrate(c, nshot, sx, sy, toff, tcell, d, m);
 }
 
+// GPU part of a modelling: image transpose -> Born recursion -> synthesis. On c->st.
+static int run_model(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, float *d_dev, int exact)
+{
+    const wem_params &p = c->p;
+    cudaStream_t st = c->st;
+    const int nmx = p.nmx, nz = p.nz;
+    int S, threads, bps = 0;
+    size_t smem;
+    if (model_config(c->nkx, p.pspi, nmx, p.nref, &S, &threads, &smem)) return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
+    if ((int)smem > c->max_smem)
+        return fail(WEM_ERR_SIZE, "nref=%d needs %zu B of shared memory per CTA (device limit %d B)", p.nref, smem,
+                    c->max_smem);
+    if (model_max_grid(c->nkx, p.pspi, p.interp, exact, nmx, p.nref, &bps) || bps < 1)
+        return fail(WEM_ERR_CUDA, "modelling kernel does not fit on the device: %s", cudaGetErrorString(cudaGetLastError()));
+    const int ngroups = (nshot + S - 1) / S;
+    const long long nitems = (long long)ngroups * c->nwf;
+    int grid = (int)((long long)c->nsm * bps < nitems ? (long long)c->nsm * bps : nitems);
+    if (grid < 1) grid = 1;
+    int rc;
+    const size_t dg_elems = (size_t)nshot * (c->nwf > 0 ? c->nwf : 1) * nmx;
+    if ((rc = ensure(c->recv, sizeof(float2) * dg_elems)) ||
+        (rc = ensure(c->smig, sizeof(float2) * (size_t)grid * S * nz * nmx)) ||
+        (rc = ensure(c->mimg, sizeof(float) * (size_t)nz * nmx)))
+        return rc;
+    int kernels = 0;
+    CK(cudaEventRecord(c->ev0, st));
+    CK(cudaMemsetAsync(c->recv.p, 0, sizeof(float2) * dg_elems, st));
+    if (launch_transpose(m_dev, nmx, nz, P<float>(c->mimg), st))
+        return fail(WEM_ERR_CUDA, "transpose launch: %s", cudaGetErrorString(cudaGetLastError()));
+    kernels++;
+    CK(cudaEventRecord(c->evk[0], st));
+    CK(cudaEventRecord(c->evk[1], st));
+    if (c->nwf > 0) {
+        MigArgs a{};
+        a.nmx = nmx; a.nz = nz; a.nref = p.pspi ? p.nref : 1; a.nwf = c->nwf; a.ifmin = c->ifmin;
+        a.nshot = nshot; a.ngroups = ngroups; a.dw = c->dw; a.dz = p.dz; a.dkx = c->dkx;
+        a.inv_n = 1.0f / (float)c->nkx;
+        a.recv = nullptr; a.srcw = P<float2>(c->srcw); a.igx = P<int>(c->igx); a.vref = P<float>(c->vref);
+        a.po = P<float>(c->po); a.pd = P<float>(c->pd); a.selb = P<uint8_t>(c->sel); a.wlin = P<float>(c->wlin);
+        a.taper = P<float>(c->taper); a.zflag = P<uint8_t>(c->zflag); a.twid = P<float2>(c->twid); a.slots = nullptr;
+        BornArgs b{};
+        b.img = P<float>(c->mimg);
+        b.smig = P<float2>(c->smig);
+        b.dg = P<float2>(c->recv);
+        b.inv_sqt = (float)(1.0 / (double)sqrtf((float)c->ntfft));
+        if (launch_model(c->nkx, p.pspi, p.interp, exact, a, b, grid, st))
+            return fail(WEM_ERR_CUDA, "modelling launch: %s", cudaGetErrorString(cudaGetLastError()));
+        kernels++;
+    }
+    CK(cudaEventRecord(c->evk[2], st));
+    if (ntr > 0) {
+        SynthArgs sy{};
+        sy.dg = P<float2>(c->recv);
+        sy.nwf = c->nwf; sy.ifmin = c->ifmin; sy.nt = p.nt; sy.nf = c->nf; sy.ntr = (int)ntr;
+        sy.in_base = P<int64_t>(c->tbase); sy.in_fstride = nmx; sy.wtab = P<float2>(c->wtab);
+        sy.scale = exact ? P<float>(c->ssyn_exact) : P<float>(c->ssyn_ref);
+        sy.out = d_dev;
+        if (launch_synth(sy, st)) return fail(WEM_ERR_CUDA, "synthesis launch: %s", cudaGetErrorString(cudaGetLastError()));
+        kernels++;
+    }
+    CK(cudaEventRecord(c->evk[3], st));
+    CK(cudaEventRecord(c->ev1, st));
+    c->last_kernels = kernels;
+    return WEM_OK;
+}
+
+extern "C" int wem_model_device(wem_ctx *c, int nshot, const float *sx, const float *sy, const int64_t *toff,
+                                const int32_t *tcell, const float *m_dev, float *d_dev, int exact, int sync)
+{
+    if (!c || !c->prepared) return fail(WEM_ERR_ARG, "wem_model_device: context not prepared (call wem_prepare)");
+    if (nshot < 1 || !toff) return fail(WEM_ERR_ARG, "wem_model_device: need nshot >= 1 and trace offsets");
+    if (!m_dev || (!d_dev && toff[nshot] > 0)) return fail(WEM_ERR_ARG, "wem_model_device: null buffer");
+    CK(cudaSetDevice(c->device));
+    int64_t ntr = 0;
+    int rc = set_shots(c, nshot, sx, sy, toff, tcell, &ntr);
+    if (rc) return rc;
+    if ((rc = run_model(c, nshot, ntr, m_dev, d_dev, exact ? 1 : 0))) return rc;
+    if (sync) {
+        CK(cudaStreamSynchronize(c->st));
+        if ((rc = collect_times(c))) return rc;
+    }
+    return WEM_OK;
+}
+
+extern "C" int wem_model(wem_ctx *c, int nshot, const float *sx, const float *sy, const int64_t *toff,
+                         const int32_t *tcell, const float *m, float *d, int exact)
+{
+    if (!c || !c->prepared) return fail(WEM_ERR_ARG, "wem_model: context not prepared (call wem_prepare)");
+    if (nshot < 1 || !toff) return fail(WEM_ERR_ARG, "wem_model: need nshot >= 1 and trace offsets");
+    if (!m || (!d && toff[nshot] > 0)) return fail(WEM_ERR_ARG, "wem_model: null buffer");
+    CK(cudaSetDevice(c->device));
+    const wem_params &p = c->p;
+    int64_t ntr = 0;
+    int rc = set_shots(c, nshot, sx, sy, toff, tcell, &ntr);
+    if (rc) return rc;
+    const size_t dbytes = sizeof(float) * (size_t)ntr * p.nt;
+    const size_t mbytes = sizeof(float) * (size_t)p.nmx * p.nmy * p.nz;
+    if ((rc = ensure(c->data, dbytes)) || (rc = ensure(c->image, mbytes))) return rc;
+    CK(cudaMemcpyAsync(c->image.p, m, mbytes, cudaMemcpyHostToDevice, c->st));
+    if ((rc = run_model(c, nshot, ntr, P<float>(c->image), P<float>(c->data), exact ? 1 : 0))) return rc;
+    if (dbytes) CK(cudaMemcpyAsync(d, c->data.p, dbytes, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return collect_times(c);
+}
+
 // ---------------------------------------------------------------- wem() drop-in
 static std::mutex g_default_mu;
 static wem_ctx *g_default = nullptr;
@@ -531,7 +674,6 @@ extern "C" int wem(float **d, float **m, float **wav, int nt, float ot, float dt
 {
     if (!d || !m || !wav || !vel || !wav[0]) return fail(WEM_ERR_ARG, "wem: null argument");
     if (nt < 1 || nmx < 1 || nmy < 1 || nz < 1) return fail(WEM_ERR_ARG, "wem: invalid sizes");
-    if (!adj) return fail(WEM_ERR_SIZE, "wem: modelling (adj=false) is not available in this build");
     wem_ctx *c;
     int rc = default_ctx(&c);
     if (rc) return rc;
@@ -550,14 +692,22 @@ extern "C" int wem(float **d, float **m, float **wav, int nt, float ot, float dt
     for (int ix = 0; ix < n; ix++) {
         if (!vel[ix] || !d[ix] || !m[ix]) return fail(WEM_ERR_ARG, "wem: null row %d", ix);
         memcpy(&v[(size_t)ix * nz], vel[ix], sizeof(float) * nz);
-        memcpy(&dd[(size_t)ix * nt], d[ix], sizeof(float) * nt);
+        if (adj) memcpy(&dd[(size_t)ix * nt], d[ix], sizeof(float) * nt);
+        else memcpy(&mm[(size_t)ix * nz], m[ix], sizeof(float) * nz);
     }
     if ((rc = wem_prepare(c, &p, v.data(), wav[0]))) return rc;
     std::vector<int64_t> off = { 0, (int64_t)n };
     std::vector<int32_t> cell(n);
     for (int i = 0; i < n; i++) cell[i] = i;
-    if ((rc = wem_migrate(c, 1, &sx, &sy, off.data(), cell.data(), dd.data(), mm.data()))) return rc;
-    for (int ix = 0; ix < n; ix++) memcpy(m[ix], &mm[(size_t)ix * nz], sizeof(float) * nz);
+    if (adj) {
+        // migration: d -> m, m overwritten (wem.c:73-74)
+        if ((rc = wem_migrate(c, 1, &sx, &sy, off.data(), cell.data(), dd.data(), mm.data()))) return rc;
+        for (int ix = 0; ix < n; ix++) memcpy(m[ix], &mm[(size_t)ix * nz], sizeof(float) * nz);
+    } else {
+        // modelling with the reference's operator: m -> d, d overwritten (wem.c:76-77)
+        if ((rc = wem_model(c, 1, &sx, &sy, off.data(), cell.data(), mm.data(), dd.data(), 0))) return rc;
+        for (int ix = 0; ix < n; ix++) memcpy(d[ix], &dd[(size_t)ix * nt], sizeof(float) * nt);
+    }
     if (verbose) fprintf(stderr, "wem: %d frequencies x %d depth steps on the GPU in %.3f ms\n", c->nwf, nz, c->last_ms);
     return WEM_OK;
 }

@@ -140,17 +140,18 @@ template <int N> __host__ __device__ constexpr int fft_tw_offset(int p)
 }
 template <int N> __host__ __device__ constexpr int fft_tw_size() { return fft_tw_offset<N>(fft_npass<N>()); }
 
-// Team barrier: a warp-sized team only needs __syncwarp; larger teams use a named
-// barrier (ids 1..15; id 0 is __syncthreads).
-template <int T> __device__ __forceinline__ void team_sync(int bar_id)
+// Team barrier. `sync` is the team's named-barrier id (1..15; 0 is __syncthreads) for
+// teams of 64 or more threads, and the team's lane mask within its warp for teams of
+// a warp or less, so that teams sharing a warp synchronise independently.
+template <int T> __device__ __forceinline__ void team_sync(unsigned sync)
 {
-    if constexpr (T <= 32) __syncwarp();
-    else asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "n"(T) : "memory");
+    if constexpr (T <= 32) __syncwarp(sync);
+    else asm volatile("bar.sync %0, %1;" ::"r"(sync), "n"(T) : "memory");
 }
 
 // One Stockham pass P of the team's row (compile-time radix and span).
 template <int N, int DIR, int P>
-__device__ __forceinline__ void fft_pass(float2 (&v)[16], float2 *xbuf, const float2 *tw, int t, int bar_id)
+__device__ __forceinline__ void fft_pass(float2 (&v)[16], float2 *xbuf, const float2 *tw, int t, unsigned bar_id)
 {
     constexpr int E = 16;
     constexpr int T = N / E;
@@ -208,7 +209,7 @@ __device__ __forceinline__ void fft_pass(float2 (&v)[16], float2 *xbuf, const fl
 // of pad16(N) float2. tw: the concatenated per-pass twiddle table (forward sign).
 // DIR = -1 forward (e^{-i...}), +1 inverse; unnormalised.
 template <int N, int DIR>
-__device__ __forceinline__ void fft_row(float2 (&v)[16], float2 *xbuf, const float2 *tw, int t, int bar_id)
+__device__ __forceinline__ void fft_row(float2 (&v)[16], float2 *xbuf, const float2 *tw, int t, unsigned bar_id)
 {
     fft_pass<N, DIR, 0>(v, xbuf, tw, t, bar_id);
 }

@@ -6,10 +6,10 @@
 
 namespace gbwem {
 
-// Per-depth selection word of the PSPI interpolation, one per (iz, ix):
-// bits 0-7 iref1, bits 8-15 iref2, bit 16 set when vref2 - vref1 > 10
-// (wem.c:454: interpolate; otherwise the nearest-lower wavefield is taken whole).
-constexpr uint32_t SEL_INTERP = 1u << 16;
+// Per-depth selection byte of the PSPI interpolation, one per (iz, ix): bits 0-6
+// iref1, bit 7 set when vref2 - vref1 > 10 (wem.c:454: interpolate between iref1
+// and iref2 = iref1 + 1; otherwise the nearest-lower wavefield is taken whole).
+constexpr uint8_t SEL_INTERP = 0x80;
 
 // Per-depth activity flags (wem.c:235-242): source continued when z >= sz,
 // receiver continued and image formed when z >= gz.
@@ -33,7 +33,7 @@ struct MigArgs {
     const float *vref;     // [nz][nref]
     const float *po;       // [nz] mean slowness
     const float *pd;       // [nz][nmx] slowness perturbation
-    const uint32_t *sel;   // [nz][nmx]
+    const uint8_t *selb;   // [nz][nmx] selection bytes
     const float *wlin;     // [nz][nmx] linear-interpolation weight of iref2
     const float *taper;    // [nmx] boundary taper (split-step)
     const uint8_t *zflag;  // [nz]
@@ -70,17 +70,17 @@ struct SynthArgs {
     float *out;               // [ntr][nt]
 };
 
-// host-side launchers (wem_kernels.cu)
-int launch_migrate(int nkx, int pspi, int interp, int shots_per_cta, const MigArgs &a, int grid,
-                   cudaStream_t st);
-int migrate_config(int nkx, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem);
-int migrate_max_grid(int nkx, int pspi, int interp, int shots_per_cta, int threads, size_t smem, int *blocks_per_sm);
-int launch_spectra(const SpectraArgs &a, cudaStream_t st);
-int launch_image_reduce(const float2 *slots, int nslots, int nz, int nmx, float *m, cudaStream_t st);
+// host-side launchers (wem_kernels.cu). `wide` selects the 512-thread CTA shape of
+// the migration kernel (2S rows sharing the phase tables) over the 256-thread one.
+int migrate_config(int nkx, int wide, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem);
+int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *blocks_per_sm);
+int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st);
 int model_config(int nkx, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem);
-int model_max_grid(int nkx, int pspi, int interp, int exact, int threads, size_t smem, int *blocks_per_sm);
+int model_max_grid(int nkx, int pspi, int interp, int exact, int nmx, int nref, int *blocks_per_sm);
 int launch_model(int nkx, int pspi, int interp, int exact, const MigArgs &a, const BornArgs &b, int grid,
                  cudaStream_t st);
+int launch_spectra(const SpectraArgs &a, cudaStream_t st);
+int launch_image_reduce(const float2 *slots, int nslots, int nz, int nmx, float *m, cudaStream_t st);
 int launch_synth(const SynthArgs &a, cudaStream_t st);
 int launch_transpose(const float *in, int rows, int cols, float *out, cudaStream_t st);
 int twiddle_table_size(int nkx);

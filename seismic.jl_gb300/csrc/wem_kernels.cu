@@ -19,188 +19,9 @@
 #include <stdio.h>
 #include <math.h>
 
-#include "wem_fft.cuh"
-#include "wem_internal.h"
-#include "wem_step.cuh"
+#include "wem_kernels.cuh"
 
 namespace gbwem {
-
-// ------------------------------------------------------------------ migration
-template <int N, bool PSPI, int INTERP, int S>
-__global__ void __launch_bounds__(2 * S * (N / 16)) wem_migrate_kernel(const MigArgs a)
-{
-    using SH = MigShape<N>;
-    constexpr int T = SH::T, PADN = SH::PADN;
-    constexpr int NT = 2 * S * T;
-    extern __shared__ float4 smem_raw[];
-    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx);
-
-    const int tid = threadIdx.x;
-    const int team = tid / T, t = tid - team * T;
-    const bool is_src = team < S;
-    const int sg = is_src ? team : team - S;               // shot within the group
-    float2 *xbuf = sm.x + (size_t)team * PADN;
-    const int bar = 1 + team;
-
-    for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
-
-    float2 *slot = a.slots + (size_t)blockIdx.x * a.nz * a.nmx;
-    const int nitems = a.ngroups * a.nwf;
-    const int nmx = a.nmx;
-
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int g = item % a.ngroups;
-        const int iwi = item / a.ngroups;
-        const int shot = g * S + sg;
-        const bool shot_ok = shot < a.nshot;
-        const int iw = a.ifmin + iwi;
-        const float w = __fmul_rn((float)iw, a.dw);        // w = iw*dw, wem.c:228
-        const float w2 = __fmul_rn(w, w);
-        const float factor = iw == 0 ? 1.f : 2.f;          // wem.c:226-227
-
-        // initial rows (wem.c:230-233): source spike at igx, receiver spectra
-        float2 v[16];
-        const int igx = shot_ok ? a.igx[shot] : -1;
-        const float2 sw = a.srcw[iwi];
-        const float2 *rrow = a.recv + ((size_t)(shot_ok ? shot : 0) * a.nwf + iwi) * nmx;
-#pragma unroll
-        for (int m = 0; m < 16; m++) {
-            const int x = t + T * m;
-            float2 u = make_float2(0.f, 0.f);
-            if (x < nmx && shot_ok) u = is_src ? (x == igx ? sw : u) : rrow[x];
-            v[m] = u;
-        }
-
-        for (int iz = 0; iz < a.nz; iz++) {
-            __syncthreads();  // the previous step no longer reads the tables / exchange buffers
-            build_tables<N, PSPI>(a, sm, w, w2, iz, tid, NT);
-            __syncthreads();
-            const uint8_t zf = a.zflag[iz];
-            // all teams run the step (barriers stay uniform); inactive rows keep v
-            step_mig<N, PSPI, INTERP>(v, is_src, is_src ? (zf & Z_SRC) : (zf & Z_REC), a, sm, xbuf, iz, t, bar);
-
-            // ---- imaging condition (wem.c:243-247), summed over the group's shots
-            if (zf & Z_REC) {
-                if (is_src) {
-#pragma unroll
-                    for (int m = 0; m < 16; m++) {
-                        const int x = t + T * m;
-                        if (x < nmx) xbuf[x] = v[m];
-                    }
-                }
-                __syncthreads();
-                if (!is_src) {
-                    const float2 *us = sm.x + (size_t)sg * PADN;
-                    float *cv = reinterpret_cast<float *>(xbuf);
-#pragma unroll
-                    for (int m = 0; m < 16; m++) {
-                        const int x = t + T * m;
-                        if (x < nmx) {
-                            const float2 s_ = us[x];
-                            cv[x] = factor * (v[m].x * s_.x + v[m].y * s_.y);
-                        }
-                    }
-                }
-                __syncthreads();
-                float2 *srow = slot + (size_t)iz * nmx;
-                for (int x = tid; x < nmx; x += NT) {
-                    float c = 0.f;
-#pragma unroll
-                    for (int s_ = 0; s_ < S; s_++) c += reinterpret_cast<const float *>(sm.x + (size_t)(S + s_) * PADN)[x];
-                    kahan_add(&srow[x], c);
-                }
-            }
-        }
-    }
-}
-
-// ------------------------------------------------------------------ modelling (Born)
-// One team per shot. Per (group of S shots, frequency): the source wavefield is
-// continued down and kept at every depth in global scratch (smig, wem.c:253-265),
-// then the receiver wavefield is continued up from the bottom with the image
-// injected at each depth (wem.c:266-276); the surface row, divided by
-// sqrt(ntfft) (wem.c:277-279), is the shot's spectrum at this frequency.
-template <int N, bool PSPI, int INTERP, int S, bool EXACT>
-__global__ void __launch_bounds__(S * (N / 16)) wem_model_kernel(const MigArgs a, const BornArgs b)
-{
-    using SH = MigShape<N>;
-    constexpr int T = SH::T, PADN = SH::PADN;
-    constexpr int NT = S * T;
-    extern __shared__ float4 smem_raw[];
-    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx);
-    const int tid = threadIdx.x;
-    const int team = tid / T, t = tid - team * T;
-    float2 *xbuf = sm.x + (size_t)team * PADN;
-    const int bar = 1 + team;
-    for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
-
-    const int nmx = a.nmx, nz = a.nz;
-    float2 *smig = b.smig + ((size_t)blockIdx.x * S + team) * (size_t)nz * nmx;
-    const int nitems = a.ngroups * a.nwf;
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int g = item % a.ngroups;
-        const int iwi = item / a.ngroups;
-        const int shot = g * S + team;
-        const bool shot_ok = shot < a.nshot;
-        const int iw = a.ifmin + iwi;
-        const float w = __fmul_rn((float)iw, a.dw);
-        const float w2 = __fmul_rn(w, w);
-        float2 v[16];
-        const int igx = shot_ok ? a.igx[shot] : -1;
-        const float2 sw = a.srcw[iwi];
-#pragma unroll
-        for (int m = 0; m < 16; m++) {
-            const int x = t + T * m;
-            v[m] = (x < nmx && x == igx) ? sw : make_float2(0.f, 0.f);
-        }
-        // source, downward (wem.c:255-265)
-        for (int iz = 0; iz < nz; iz++) {
-            __syncthreads();
-            build_tables<N, PSPI>(a, sm, w, w2, iz, tid, NT);
-            __syncthreads();
-            const bool act = (a.zflag[iz] & Z_SRC) != 0;
-            step_mig<N, PSPI, INTERP>(v, true, act, a, sm, xbuf, iz, t, bar);
-            float2 *row = smig + (size_t)iz * nmx;
-#pragma unroll
-            for (int m = 0; m < 16; m++) {
-                const int x = t + T * m;
-                if (x < nmx) row[x] = act ? v[m] : make_float2(0.f, 0.f);
-            }
-        }
-        // receiver, upward with injection (wem.c:266-276)
-#pragma unroll
-        for (int m = 0; m < 16; m++) v[m] = make_float2(0.f, 0.f);
-        for (int iz = nz - 1; iz >= 0; iz--) {
-            __syncthreads();
-            build_tables<N, PSPI>(a, sm, w, w2, iz, tid, NT);
-            __syncthreads();
-            const bool act = (a.zflag[iz] & Z_REC) != 0;
-            if (act) {
-                const float2 *row = smig + (size_t)iz * nmx;
-                const float *mr = b.img + (size_t)iz * nmx;
-#pragma unroll
-                for (int m = 0; m < 16; m++) {
-                    const int x = t + T * m;
-                    if (x < nmx) {
-                        const float mv = mr[x];
-                        const float2 s_ = row[x];
-                        v[m].x += mv * s_.x;
-                        v[m].y += mv * s_.y;
-                    }
-                }
-            }
-            step_model<N, PSPI, INTERP, EXACT>(v, act, a, sm, xbuf, iz, t, bar);
-        }
-        if (shot_ok) {
-            float2 *out = b.dg + ((size_t)shot * a.nwf + iwi) * nmx;
-#pragma unroll
-            for (int m = 0; m < 16; m++) {
-                const int x = t + T * m;
-                if (x < nmx) out[x] = make_float2(v[m].x * b.inv_sqt, v[m].y * b.inv_sqt);
-            }
-        }
-    }
-}
 
 // ------------------------------------------------------------------ spectra
 // out[out_base[tr] + iwi*fstride] = scale[iwi] * sum_t d[tr][t] e^{-2 pi i (ifmin+iwi) t / ntfft}
@@ -414,104 +235,69 @@ void twiddle_table_host(int nkx, float2 *out)
     }
 }
 
-template <int N> struct Dispatch {
-    static constexpr int T = N / 16;
-    // shots per CTA: the CTA holds 2S rows; aim at 256 threads
-    static constexpr int S = (2 * T >= 256) ? 1 : (256 / (2 * T) > 8 ? 8 : 256 / (2 * T));
-};
-
-template <int N, bool PSPI, int INTERP>
-static int launch_n(const MigArgs &a, int grid, size_t smem, cudaStream_t st)
-{
-    constexpr int S = Dispatch<N>::S;
-    auto k = wem_migrate_kernel<N, PSPI, INTERP, S>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
-    k<<<grid, 2 * S * (N / 16), smem, st>>>(a);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
-}
-
-template <int N>
-static int launch_sel(int pspi, int interp, const MigArgs &a, int grid, size_t smem, cudaStream_t st)
-{
-    if (!pspi) return launch_n<N, false, 0>(a, grid, smem, st);
-    if (interp == 0) return launch_n<N, true, 0>(a, grid, smem, st);
-    return launch_n<N, true, 1>(a, grid, smem, st);
-}
-
-template <int N>
-static void config_n(int pspi, int nmx, int nref, int *S, int *threads, size_t *smem)
-{
-    using SH = MigShape<N>;
-    *S = Dispatch<N>::S;
-    *threads = 2 * Dispatch<N>::S * SH::T;
-    *smem = mig_smem_bytes(SH::TWP, SH::HALF, SH::PADN, pspi ? nref : 1, pspi ? 0 : nmx, 2 * Dispatch<N>::S);
-}
-
-int migrate_config(int nkx, int pspi, int nmx, int nref, int *S, int *threads, size_t *smem)
-{
-    switch (nkx) {
-    case 32: config_n<32>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 64: config_n<64>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 128: config_n<128>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 256: config_n<256>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 512: config_n<512>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 1024: config_n<1024>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 2048: config_n<2048>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 4096: config_n<4096>(pspi, nmx, nref, S, threads, smem); return 0;
-    default: return -1;
+// ---------------------------------------------------------------- dispatch over the row length
+#define WEM_SWITCH_N(nkx, CALL)            \
+    switch (nkx) {                         \
+    case 32: return CALL(32);              \
+    case 64: return CALL(64);              \
+    case 128: return CALL(128);            \
+    case 256: return CALL(256);            \
+    case 512: return CALL(512);            \
+    case 1024: return CALL(1024);          \
+    case 2048: return CALL(2048);          \
+    case 4096: return CALL(4096);          \
+    default: return -1;                    \
     }
+
+int migrate_config(int nkx, int wide, int pspi, int nmx, int nref, int *S, int *threads, size_t *smem)
+{
+#define CALL(N) mig_launch<N>(wide, pspi, 0, nref, nmx, nullptr, 0, 0, S, threads, smem, nullptr)
+    WEM_SWITCH_N(nkx, CALL)
+#undef CALL
 }
 
-template <int N, bool PSPI, int INTERP>
-static int occ_n(int threads, size_t smem, int *bps)
+int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *bps)
 {
-    constexpr int S = Dispatch<N>::S;
-    auto k = wem_migrate_kernel<N, PSPI, INTERP, S>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, threads, smem) == cudaSuccess ? 0 : -1;
-}
-
-template <int N>
-static int occ_sel(int pspi, int interp, int threads, size_t smem, int *bps)
-{
-    if (!pspi) return occ_n<N, false, 0>(threads, smem, bps);
-    if (interp == 0) return occ_n<N, true, 0>(threads, smem, bps);
-    return occ_n<N, true, 1>(threads, smem, bps);
-}
-
-int migrate_max_grid(int nkx, int pspi, int interp, int S, int threads, size_t smem, int *bps)
-{
-    (void)S;
-    switch (nkx) {
-    case 32: return occ_sel<32>(pspi, interp, threads, smem, bps);
-    case 64: return occ_sel<64>(pspi, interp, threads, smem, bps);
-    case 128: return occ_sel<128>(pspi, interp, threads, smem, bps);
-    case 256: return occ_sel<256>(pspi, interp, threads, smem, bps);
-    case 512: return occ_sel<512>(pspi, interp, threads, smem, bps);
-    case 1024: return occ_sel<1024>(pspi, interp, threads, smem, bps);
-    case 2048: return occ_sel<2048>(pspi, interp, threads, smem, bps);
-    case 4096: return occ_sel<4096>(pspi, interp, threads, smem, bps);
-    default: return -1;
-    }
-}
-
-int launch_migrate(int nkx, int pspi, int interp, int S, const MigArgs &a, int grid, cudaStream_t st)
-{
-    int s_, th;
+    int S, th;
     size_t smem;
-    if (migrate_config(nkx, pspi, a.nmx, a.nref, &s_, &th, &smem)) return -1;
-    (void)S;
-    switch (nkx) {
-    case 32: return launch_sel<32>(pspi, interp, a, grid, smem, st);
-    case 64: return launch_sel<64>(pspi, interp, a, grid, smem, st);
-    case 128: return launch_sel<128>(pspi, interp, a, grid, smem, st);
-    case 256: return launch_sel<256>(pspi, interp, a, grid, smem, st);
-    case 512: return launch_sel<512>(pspi, interp, a, grid, smem, st);
-    case 1024: return launch_sel<1024>(pspi, interp, a, grid, smem, st);
-    case 2048: return launch_sel<2048>(pspi, interp, a, grid, smem, st);
-    case 4096: return launch_sel<4096>(pspi, interp, a, grid, smem, st);
-    default: return -1;
-    }
+#define CALL(N) mig_launch<N>(wide, pspi, interp, nref, nmx, nullptr, 0, 0, &S, &th, &smem, bps)
+    WEM_SWITCH_N(nkx, CALL)
+#undef CALL
+}
+
+int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st)
+{
+    int S, th;
+    size_t smem;
+#define CALL(N) mig_launch<N>(wide, pspi, interp, a.nref, a.nmx, &a, grid, st, &S, &th, &smem, nullptr)
+    WEM_SWITCH_N(nkx, CALL)
+#undef CALL
+}
+
+int model_config(int nkx, int pspi, int nmx, int nref, int *S, int *threads, size_t *smem)
+{
+#define CALL(N) model_launch<N>(pspi, 0, 0, nref, nmx, nullptr, nullptr, 0, 0, S, threads, smem, nullptr)
+    WEM_SWITCH_N(nkx, CALL)
+#undef CALL
+}
+
+int model_max_grid(int nkx, int pspi, int interp, int exact, int nmx, int nref, int *bps)
+{
+    int S, th;
+    size_t smem;
+#define CALL(N) model_launch<N>(pspi, interp, exact, nref, nmx, nullptr, nullptr, 0, 0, &S, &th, &smem, bps)
+    WEM_SWITCH_N(nkx, CALL)
+#undef CALL
+}
+
+int launch_model(int nkx, int pspi, int interp, int exact, const MigArgs &a, const BornArgs &b, int grid,
+                 cudaStream_t st)
+{
+    int S, th;
+    size_t smem;
+#define CALL(N) model_launch<N>(pspi, interp, exact, a.nref, a.nmx, &a, &b, grid, st, &S, &th, &smem, nullptr)
+    WEM_SWITCH_N(nkx, CALL)
+#undef CALL
 }
 
 int launch_spectra(const SpectraArgs &a, cudaStream_t st)
@@ -527,90 +313,6 @@ int launch_image_reduce(const float2 *slots, int nslots, int nz, int nmx, float 
     dim3 grid((nmx + 31) / 32, (nz + 31) / 32);
     wem_image_reduce_kernel<<<grid, 256, 0, st>>>(slots, nslots, nz, nmx, m);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
-}
-
-// ---------------------------------------------------------------- modelling launchers
-template <int N> struct DispatchModel {
-    static constexpr int T = N / 16;
-    // one row team per shot; aim at 256 threads
-    static constexpr int S = (T >= 256) ? 1 : (256 / T > 8 ? 8 : 256 / T);
-};
-
-template <int N>
-static void model_config_n(int pspi, int nmx, int nref, int *S, int *threads, size_t *smem)
-{
-    using SH = MigShape<N>;
-    *S = DispatchModel<N>::S;
-    *threads = DispatchModel<N>::S * SH::T;
-    *smem = mig_smem_bytes(SH::TWP, SH::HALF, SH::PADN, pspi ? nref : 1, pspi ? 0 : nmx, DispatchModel<N>::S);
-}
-
-int model_config(int nkx, int pspi, int nmx, int nref, int *S, int *threads, size_t *smem)
-{
-    switch (nkx) {
-    case 32: model_config_n<32>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 64: model_config_n<64>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 128: model_config_n<128>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 256: model_config_n<256>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 512: model_config_n<512>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 1024: model_config_n<1024>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 2048: model_config_n<2048>(pspi, nmx, nref, S, threads, smem); return 0;
-    case 4096: model_config_n<4096>(pspi, nmx, nref, S, threads, smem); return 0;
-    default: return -1;
-    }
-}
-
-template <int N, bool PSPI, int INTERP, bool EXACT>
-static int model_n(const MigArgs *a, const BornArgs *b, int grid, size_t smem, cudaStream_t st, int threads, int *bps)
-{
-    constexpr int S = DispatchModel<N>::S;
-    auto k = wem_model_kernel<N, PSPI, INTERP, S, EXACT>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
-    if (bps) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, threads, smem) == cudaSuccess ? 0 : -1;
-    k<<<grid, S * (N / 16), smem, st>>>(*a, *b);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
-}
-
-template <int N>
-static int model_sel(int pspi, int interp, int exact, const MigArgs *a, const BornArgs *b, int grid, size_t smem,
-                     cudaStream_t st, int threads, int *bps)
-{
-    if (!pspi) return model_n<N, false, 0, false>(a, b, grid, smem, st, threads, bps);
-    if (exact) {
-        if (interp == 0) return model_n<N, true, 0, true>(a, b, grid, smem, st, threads, bps);
-        return model_n<N, true, 1, true>(a, b, grid, smem, st, threads, bps);
-    }
-    if (interp == 0) return model_n<N, true, 0, false>(a, b, grid, smem, st, threads, bps);
-    return model_n<N, true, 1, false>(a, b, grid, smem, st, threads, bps);
-}
-
-static int model_dispatch(int nkx, int pspi, int interp, int exact, const MigArgs *a, const BornArgs *b, int grid,
-                          size_t smem, cudaStream_t st, int threads, int *bps)
-{
-    switch (nkx) {
-    case 32: return model_sel<32>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
-    case 64: return model_sel<64>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
-    case 128: return model_sel<128>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
-    case 256: return model_sel<256>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
-    case 512: return model_sel<512>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
-    case 1024: return model_sel<1024>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
-    case 2048: return model_sel<2048>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
-    case 4096: return model_sel<4096>(pspi, interp, exact, a, b, grid, smem, st, threads, bps);
-    default: return -1;
-    }
-}
-
-int model_max_grid(int nkx, int pspi, int interp, int exact, int threads, size_t smem, int *bps)
-{
-    return model_dispatch(nkx, pspi, interp, exact, nullptr, nullptr, 0, smem, 0, threads, bps);
-}
-
-int launch_model(int nkx, int pspi, int interp, int exact, const MigArgs &a, const BornArgs &b, int grid, cudaStream_t st)
-{
-    int S, th;
-    size_t smem;
-    if (model_config(nkx, pspi, a.nmx, a.nref, &S, &th, &smem)) return -1;
-    return model_dispatch(nkx, pspi, interp, exact, &a, &b, grid, smem, st, th, nullptr);
 }
 
 int launch_synth(const SynthArgs &a, cudaStream_t st)

@@ -1,0 +1,287 @@
+// wem_kernels.cuh -- the depth-recursion kernels as templates over the row length N
+// (migration and Born modelling) and their per-N launch helpers. Each N is
+// instantiated in its own translation unit (wem_n<N>.cu) so that the build
+// compiles them in parallel.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "wem_fft.cuh"
+#include "wem_internal.h"
+#include "wem_step.cuh"
+
+namespace gbwem {
+
+// ------------------------------------------------------------------ migration
+template <int N, bool PSPI, int INTERP, int S>
+__global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const MigArgs a)
+{
+    using SH = MigShape<N>;
+    constexpr int T = SH::T, PADN = SH::PADN;
+    constexpr int NT = 2 * S * T;
+    extern __shared__ float4 smem_raw[];
+    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx, 2 * S);
+
+    const int tid = threadIdx.x;
+    const int team = tid / T, t = tid - team * T;
+    const bool is_src = team < S;
+    const int sg = is_src ? team : team - S;               // shot within the group
+    float2 *xbuf = sm.x + (size_t)team * PADN;
+    float2 *sacc = sm.acc + (size_t)team * N;
+    const unsigned sync = team_sync_handle<N>(tid);
+
+    for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
+
+    float2 *slot = a.slots + (size_t)blockIdx.x * a.nz * a.nmx;
+    const int nitems = a.ngroups * a.nwf;
+    const int nmx = a.nmx;
+    bool tables_free = true;  // no thread still reads the tables of the previous step
+
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int g = item % a.ngroups;
+        const int iwi = item / a.ngroups;
+        const int shot = g * S + sg;
+        const bool shot_ok = shot < a.nshot;
+        const int iw = a.ifmin + iwi;
+        const float w = __fmul_rn((float)iw, a.dw);        // w = iw*dw, wem.c:228
+        const float w2 = __fmul_rn(w, w);
+        const float factor = iw == 0 ? 1.f : 2.f;          // wem.c:226-227
+
+        // initial rows (wem.c:230-233): source spike at igx, receiver spectra
+        float2 v[16];
+        const int igx = shot_ok ? a.igx[shot] : -1;
+        const float2 sw = a.srcw[iwi];
+        const float2 *rrow = a.recv + ((size_t)(shot_ok ? shot : 0) * a.nwf + iwi) * nmx;
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            float2 u = make_float2(0.f, 0.f);
+            if (x < nmx && shot_ok) u = is_src ? (x == igx ? sw : u) : rrow[x];
+            v[m] = u;
+        }
+
+        for (int iz = 0; iz < a.nz; iz++) {
+            if (!tables_free) __syncthreads();
+            build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
+            __syncthreads();
+            const uint8_t zf = a.zflag[iz];
+            const bool active = is_src ? (zf & Z_SRC) : (zf & Z_REC);
+            if (active) step_mig<N, PSPI, INTERP>(v, is_src, a, sm, xbuf, sacc, t, sync);
+
+            // ---- imaging condition (wem.c:243-247), summed over the group's shots
+            if (zf & Z_REC) {
+                if (is_src) {
+#pragma unroll
+                    for (int m = 0; m < 16; m++) {
+                        const int x = t + T * m;
+                        if (x < nmx) xbuf[x] = v[m];
+                    }
+                }
+                __syncthreads();  // every step done: the tables are free from here on
+                if (!is_src) {
+                    const float2 *us = sm.x + (size_t)sg * PADN;
+                    float *cv = reinterpret_cast<float *>(xbuf);
+#pragma unroll
+                    for (int m = 0; m < 16; m++) {
+                        const int x = t + T * m;
+                        if (x < nmx) {
+                            const float2 s_ = us[x];
+                            cv[x] = factor * (v[m].x * s_.x + v[m].y * s_.y);
+                        }
+                    }
+                }
+                __syncthreads();
+                float2 *srow = slot + (size_t)iz * nmx;
+                for (int x = tid; x < nmx; x += NT) {
+                    float c = 0.f;
+#pragma unroll
+                    for (int s_ = 0; s_ < S; s_++) c += reinterpret_cast<const float *>(sm.x + (size_t)(S + s_) * PADN)[x];
+                    kahan_add(&srow[x], c);
+                }
+                tables_free = true;
+            } else {
+                tables_free = false;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ modelling (Born)
+// One team per shot. Per (group of S shots, frequency): the source wavefield is
+// continued down and kept at every depth in global scratch (smig, wem.c:253-265),
+// then the receiver wavefield is continued up from the bottom with the image
+// injected at each depth (wem.c:266-276); the surface row, divided by
+// sqrt(ntfft) (wem.c:277-279), is the shot's spectrum at this frequency.
+template <int N, bool PSPI, int INTERP, int S, bool EXACT>
+__global__ void __launch_bounds__(S * (N / 16), 1) wem_model_kernel(const MigArgs a, const BornArgs b)
+{
+    using SH = MigShape<N>;
+    constexpr int T = SH::T, PADN = SH::PADN;
+    constexpr int NT = S * T;
+    extern __shared__ float4 smem_raw[];
+    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx, S);
+    const int tid = threadIdx.x;
+    const int team = tid / T, t = tid - team * T;
+    float2 *xbuf = sm.x + (size_t)team * PADN;
+    float2 *sacc = sm.acc + (size_t)team * N;
+    const unsigned sync = team_sync_handle<N>(tid);
+    for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
+
+    const int nmx = a.nmx, nz = a.nz;
+    float2 *smig = b.smig + ((size_t)blockIdx.x * S + team) * (size_t)nz * nmx;
+    const int nitems = a.ngroups * a.nwf;
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int g = item % a.ngroups;
+        const int iwi = item / a.ngroups;
+        const int shot = g * S + team;
+        const bool shot_ok = shot < a.nshot;
+        const int iw = a.ifmin + iwi;
+        const float w = __fmul_rn((float)iw, a.dw);
+        const float w2 = __fmul_rn(w, w);
+        float2 v[16];
+        const int igx = shot_ok ? a.igx[shot] : -1;
+        const float2 sw = a.srcw[iwi];
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            v[m] = (x < nmx && x == igx) ? sw : make_float2(0.f, 0.f);
+        }
+        // source, downward (wem.c:255-265)
+        for (int iz = 0; iz < nz; iz++) {
+            __syncthreads();
+            build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
+            __syncthreads();
+            const bool act = (a.zflag[iz] & Z_SRC) != 0;
+            if (act) step_mig<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync);
+            float2 *row = smig + (size_t)iz * nmx;
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int x = t + T * m;
+                if (x < nmx) row[x] = act ? v[m] : make_float2(0.f, 0.f);
+            }
+        }
+        // receiver, upward with injection (wem.c:266-276)
+#pragma unroll
+        for (int m = 0; m < 16; m++) v[m] = make_float2(0.f, 0.f);
+        for (int iz = nz - 1; iz >= 0; iz--) {
+            __syncthreads();
+            build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
+            __syncthreads();
+            if (a.zflag[iz] & Z_REC) {
+                const float2 *row = smig + (size_t)iz * nmx;
+                const float *mr = b.img + (size_t)iz * nmx;
+#pragma unroll
+                for (int m = 0; m < 16; m++) {
+                    const int x = t + T * m;
+                    if (x < nmx) {
+                        const float mv = mr[x];
+                        const float2 s_ = row[x];
+                        v[m].x += mv * s_.x;
+                        v[m].y += mv * s_.y;
+                    }
+                }
+                step_model<N, PSPI, INTERP, EXACT>(v, a, sm, xbuf, sacc, t, sync);
+            }
+        }
+        if (shot_ok) {
+            float2 *out = b.dg + ((size_t)shot * a.nwf + iwi) * nmx;
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int x = t + T * m;
+                if (x < nmx) out[x] = make_float2(v[m].x * b.inv_sqt, v[m].y * b.inv_sqt);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ per-N launch helpers
+// Two CTA shapes per row length: "wide" (512 threads, 2S rows sharing one set of phase
+// tables) and "narrow" (256 threads); wide is used whenever its shared memory fits.
+template <int N> struct Shapes {
+    static constexpr int T = N / 16;
+    static constexpr int S_WIDE = (2 * T >= 512) ? 1 : (512 / (2 * T) > 16 ? 16 : 512 / (2 * T));
+    static constexpr int S_NARROW = (2 * T >= 256) ? 1 : (256 / (2 * T) > 16 ? 16 : 256 / (2 * T));
+    // modelling: one team per shot, 256 threads
+    static constexpr int S_MODEL = (T >= 256) ? 1 : (256 / T > 16 ? 16 : 256 / T);
+};
+
+template <int N, bool PSPI, int INTERP, int S>
+int mig_run(const MigArgs *a, int grid, size_t smem, cudaStream_t st, int *bps)
+{
+    auto k = wem_migrate_kernel<N, PSPI, INTERP, S>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    if (bps) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, 2 * S * (N / 16), smem) == cudaSuccess ? 0 : -1;
+    k<<<grid, 2 * S * (N / 16), smem, st>>>(*a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N, int S>
+int mig_sel(int pspi, int interp, const MigArgs *a, int grid, size_t smem, cudaStream_t st, int *bps)
+{
+    if (!pspi) return mig_run<N, false, 0, S>(a, grid, smem, st, bps);
+    if (interp == 0) return mig_run<N, true, 0, S>(a, grid, smem, st, bps);
+    return mig_run<N, true, 1, S>(a, grid, smem, st, bps);
+}
+
+// wide = 1 selects the 512-thread shape. Fills *S/*threads/*smem; launches when
+// a != nullptr and bps == nullptr, queries occupancy when bps != nullptr.
+template <int N>
+int mig_launch(int wide, int pspi, int interp, int nref, int nmx, const MigArgs *a, int grid, cudaStream_t st,
+               int *S, int *threads, size_t *smem, int *bps)
+{
+    using SH = Shapes<N>;
+    const int s_ = wide ? SH::S_WIDE : SH::S_NARROW;
+    *S = s_;
+    *threads = 2 * s_ * SH::T;
+    *smem = mig_smem_bytes<N>(pspi != 0, nref, nmx, 2 * s_);
+    if (!a && !bps) return 0;
+    if (wide) return mig_sel<N, SH::S_WIDE>(pspi, interp, a, grid, *smem, st, bps);
+    return mig_sel<N, SH::S_NARROW>(pspi, interp, a, grid, *smem, st, bps);
+}
+
+template <int N, bool PSPI, int INTERP, bool EXACT>
+int model_run(const MigArgs *a, const BornArgs *b, int grid, size_t smem, cudaStream_t st, int *bps)
+{
+    constexpr int S = Shapes<N>::S_MODEL;
+    auto k = wem_model_kernel<N, PSPI, INTERP, S, EXACT>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    if (bps) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, S * (N / 16), smem) == cudaSuccess ? 0 : -1;
+    k<<<grid, S * (N / 16), smem, st>>>(*a, *b);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N>
+int model_launch(int pspi, int interp, int exact, int nref, int nmx, const MigArgs *a, const BornArgs *b, int grid,
+                 cudaStream_t st, int *S, int *threads, size_t *smem, int *bps)
+{
+    using SH = Shapes<N>;
+    *S = SH::S_MODEL;
+    *threads = SH::S_MODEL * SH::T;
+    *smem = mig_smem_bytes<N>(pspi != 0, nref, nmx, SH::S_MODEL);
+    if (!a && !bps) return 0;
+    if (!pspi) return model_run<N, false, 0, false>(a, b, grid, *smem, st, bps);
+    if (exact) {
+        if (interp == 0) return model_run<N, true, 0, true>(a, b, grid, *smem, st, bps);
+        return model_run<N, true, 1, true>(a, b, grid, *smem, st, bps);
+    }
+    if (interp == 0) return model_run<N, true, 0, false>(a, b, grid, *smem, st, bps);
+    return model_run<N, true, 1, false>(a, b, grid, *smem, st, bps);
+}
+
+// defined in wem_n<N>.cu
+#define WEM_DECLARE_N(N)                                                                                          \
+    extern template int mig_launch<N>(int, int, int, int, int, const MigArgs *, int, cudaStream_t, int *, int *, \
+                                      size_t *, int *);                                                           \
+    extern template int model_launch<N>(int, int, int, int, int, const MigArgs *, const BornArgs *, int,         \
+                                        cudaStream_t, int *, int *, size_t *, int *);
+WEM_DECLARE_N(32)
+WEM_DECLARE_N(64)
+WEM_DECLARE_N(128)
+WEM_DECLARE_N(256)
+WEM_DECLARE_N(512)
+WEM_DECLARE_N(1024)
+WEM_DECLARE_N(2048)
+WEM_DECLARE_N(4096)
+#undef WEM_DECLARE_N
+
+}  // namespace gbwem

@@ -1,0 +1,8 @@
+// wem_n512.cu -- instantiates the depth-recursion kernels for rows of 512 samples.
+#include "wem_kernels.cuh"
+
+namespace gbwem {
+template int mig_launch<512>(int, int, int, int, int, const MigArgs *, int, cudaStream_t, int *, int *, size_t *, int *);
+template int model_launch<512>(int, int, int, int, int, const MigArgs *, const BornArgs *, int, cudaStream_t, int *,
+                               int *, size_t *, int *);
+}  // namespace gbwem

@@ -53,7 +53,7 @@ Layout noalloc_layout(int nmx, int nz, int nref, int ntw, int nf, int nwf, int n
     L.po = take(sizeof(float) * nz);
     L.pd = take(sizeof(float) * (size_t)nz * nmx);
     L.vref = take(sizeof(float) * (size_t)nz * nref);
-    L.sel = take(sizeof(uint32_t) * (size_t)nz * nmx);
+    L.sel = take((size_t)nz * nmx);
     L.wlin = take(sizeof(float) * (size_t)nz * nmx);
     L.taper = take(sizeof(float) * nmx);
     L.zflag = take((size_t)nz);
@@ -100,7 +100,7 @@ struct TableArgs {
     int nmx, nz, nref, ntw, nkx, nf, nwf, ifmin, ntfft, nshot, lmx;
     float oz, dz, sz, gz, dw;
     float *po, *pd, *vref, *wlin, *taper, *srec, *ssrc;
-    uint32_t *sel;
+    uint8_t *sel;
     uint8_t *zflag;
     float2 *twid, *wtab;
     int *igx;
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(256) noalloc_tables_kernel(const TableArgs a)
             }
             const float vr1 = nr > 1 ? __fadd_rn(vmin, __fdiv_rn(__fmul_rn((float)i1, __fsub_rn(vmax, vmin)), __fsub_rn((float)nr, 1.f))) : vmin;
             const float vr2 = nr > 1 ? __fadd_rn(vmin, __fdiv_rn(__fmul_rn((float)i2, __fsub_rn(vmax, vmin)), __fsub_rn((float)nr, 1.f))) : vmin;
-            uint32_t word = (uint32_t)i1 | ((uint32_t)i2 << 8);
+            uint8_t word = (uint8_t)i1;  // where it interpolates, i2 = i1 + 1
             float wl = 0.f;
             if (__fsub_rn(vr2, vr1) > 10.f) {
                 word |= SEL_INTERP;
@@ -229,13 +229,14 @@ __global__ void __launch_bounds__(2 * S * (N / 16)) wem_migrate_atomic_kernel(co
     constexpr int T = SH::T, PADN = SH::PADN;
     constexpr int NT = 2 * S * T;
     extern __shared__ float4 smem_raw[];
-    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx);
+    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx, 2 * S);
     const int tid = threadIdx.x;
     const int team = tid / T, t = tid - team * T;
     const bool is_src = team < S;
     const int sg = is_src ? team : team - S;
     float2 *xbuf = sm.x + (size_t)team * PADN;
-    const int bar = 1 + team;
+    float2 *sacc = sm.acc + (size_t)team * N;
+    const unsigned sync = team_sync_handle<N>(tid);
     for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
     const int nitems = a.ngroups * a.nwf;
     const int nmx = a.nmx;
@@ -261,10 +262,10 @@ __global__ void __launch_bounds__(2 * S * (N / 16)) wem_migrate_atomic_kernel(co
         }
         for (int iz = 0; iz < a.nz; iz++) {
             __syncthreads();
-            build_tables<N, PSPI>(a, sm, w, w2, iz, tid, NT);
+            build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
             __syncthreads();
             const uint8_t zf = a.zflag[iz];
-            step_mig<N, PSPI, INTERP>(v, is_src, is_src ? (zf & Z_SRC) : (zf & Z_REC), a, sm, xbuf, iz, t, bar);
+            if (is_src ? (zf & Z_SRC) : (zf & Z_REC)) step_mig<N, PSPI, INTERP>(v, is_src, a, sm, xbuf, sacc, t, sync);
             if (zf & Z_REC) {
                 if (is_src) {
 #pragma unroll
@@ -309,7 +310,7 @@ int launch_atomic(const MigArgs &a, float *img, int nsm, cudaStream_t st)
     using SH = MigShape<N>;
     constexpr int S = NaDispatch<N>::S;
     const int threads = 2 * S * SH::T;
-    const size_t smem = mig_smem_bytes(SH::TWP, SH::HALF, SH::PADN, PSPI ? a.nref : 1, PSPI ? 0 : a.nmx, 2 * S);
+    const size_t smem = mig_smem_bytes<N>(PSPI, a.nref, a.nmx, 2 * S);
     auto k = wem_migrate_atomic_kernel<N, PSPI, INTERP, S>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
     int bps = 0;
@@ -402,7 +403,7 @@ extern "C" WEM_API int wem_migrate_noalloc(const wem_params *pp, const float *ve
     ta.oz = p.oz; ta.dz = p.dz; ta.sz = p.sz; ta.gz = p.gz; ta.dw = dw;
     ta.po = NA(float, po); ta.pd = NA(float, pd); ta.vref = NA(float, vref); ta.wlin = NA(float, wlin);
     ta.taper = NA(float, taper); ta.srec = NA(float, srec); ta.ssrc = NA(float, ssrc);
-    ta.sel = NA(uint32_t, sel); ta.zflag = NA(uint8_t, zflag); ta.twid = NA(float2, twid); ta.wtab = NA(float2, wtab);
+    ta.sel = NA(uint8_t, sel); ta.zflag = NA(uint8_t, zflag); ta.twid = NA(float2, twid); ta.wtab = NA(float2, wtab);
     ta.igx = NA(int, igx); ta.tbase = NA(int64_t, tbase); ta.wbase = NA(int64_t, wbase);
     noalloc_tables_kernel<<<p.nz + 64, 256, 0, st>>>(ta);
     if (cudaGetLastError() != cudaSuccess) return set_error(WEM_ERR_CUDA, "table kernel launch failed");
@@ -419,7 +420,7 @@ extern "C" WEM_API int wem_migrate_noalloc(const wem_params *pp, const float *ve
         a.nmx = p.nmx; a.nz = p.nz; a.nref = nref; a.nwf = nwf; a.ifmin = ifmin; a.nshot = nshot;
         a.dw = dw; a.dz = p.dz; a.dkx = dkx; a.inv_n = 1.0f / (float)nkx;
         a.recv = NA(float2, recv); a.srcw = NA(float2, srcw); a.igx = NA(int, igx); a.vref = NA(float, vref);
-        a.po = NA(float, po); a.pd = NA(float, pd); a.sel = NA(uint32_t, sel); a.wlin = NA(float, wlin);
+        a.po = NA(float, po); a.pd = NA(float, pd); a.selb = NA(uint8_t, sel); a.wlin = NA(float, wlin);
         a.taper = NA(float, taper); a.zflag = NA(uint8_t, zflag); a.twid = NA(float2, twid); a.slots = nullptr;
         int r2 = -1;
         switch (nkx) {

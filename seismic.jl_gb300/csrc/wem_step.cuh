@@ -52,30 +52,42 @@ template <int N> struct MigShape {
     static constexpr int TWP = (TW + 1) & ~1;  // keep 16-byte alignment of what follows
 };
 
-// shared-memory footprint (bytes) of one CTA
-__host__ __device__ constexpr size_t mig_smem_bytes(int TWP, int HALF, int PADN, int nph, int ncorr, int teams)
-{
-    return sizeof(float2) * ((size_t)TWP + (size_t)nph * HALF + (size_t)((ncorr + 1) & ~1) + (size_t)teams * PADN);
-}
-
-// Shared-memory views of one CTA: twiddles, phase tables, split-step correction,
-// one exchange buffer per row team.
+// Shared-memory views of one CTA: twiddles, phase tables, split-step correction, one
+// exchange buffer per team; PSPI CTAs also hold one N-sample selection accumulator per
+// team (each thread owning its 16 positions), the depth's selection bytes and
+// interpolation weights.
 template <int N, bool PSPI> struct Smem {
-    float2 *tw, *ph, *corr, *x;
-    __device__ Smem(float4 *raw, int nref, int nmx)
+    float2 *tw, *ph, *corr, *x, *acc;
+    uint8_t *selb;
+    float *wl;
+    __device__ Smem(float4 *raw, int nref, int nmx, int teams)
     {
         using SH = MigShape<N>;
         tw = reinterpret_cast<float2 *>(raw);
         ph = tw + SH::TWP;
         corr = ph + (size_t)(PSPI ? nref : 1) * SH::HALF;
         x = corr + (PSPI ? 0 : ((nmx + 1) & ~1));
+        acc = x + (size_t)teams * SH::PADN;
+        wl = reinterpret_cast<float *>(acc + (PSPI ? (size_t)teams * N : 0));
+        selb = reinterpret_cast<uint8_t *>(wl + (PSPI ? ((nmx + 3) & ~3) : 0));
     }
 };
 
+// shared-memory footprint (bytes) of one CTA with `teams` row teams
+template <int N>
+__host__ __device__ constexpr size_t mig_smem_bytes(bool pspi, int nref, int nmx, int teams)
+{
+    using SH = MigShape<N>;
+    return sizeof(float2) * ((size_t)SH::TWP + (size_t)(pspi ? nref : 1) * SH::HALF + (size_t)(pspi ? 0 : ((nmx + 1) & ~1)) +
+                             (size_t)teams * SH::PADN + (pspi ? (size_t)teams * N : 0)) +
+           (pspi ? sizeof(float) * (size_t)((nmx + 3) & ~3) + (size_t)((nmx + 15) & ~15) : 0);
+}
+
 // Tables of depth step iz at angular frequency w (all threads of the CTA):
-// PSPI: one phase table per reference velocity; split-step: the phase table of
-// the mean slowness and the correction exp(i w pd dz) * taper (wem.c:326, 353-359).
-template <int N, bool PSPI>
+// PSPI: one phase table per reference velocity and the depth's selection row;
+// split-step: the phase table of the mean slowness and the correction
+// exp(i w pd dz) * taper (wem.c:326, 353-359).
+template <int N, bool PSPI, int INTERP>
 __device__ __forceinline__ void build_tables(const MigArgs &a, const Smem<N, PSPI> &sm, float w, float w2, int iz,
                                              int tid, int nthreads)
 {
@@ -87,6 +99,12 @@ __device__ __forceinline__ void build_tables(const MigArgs &a, const Smem<N, PSP
             const float v_ = vr[r];
             const float slow2 = __fdiv_rn(1.0f, __fmul_rn(v_, v_));
             sm.ph[e] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
+        }
+        const uint8_t *sr = a.selb + (size_t)iz * a.nmx;
+        for (int x = tid; x < a.nmx; x += nthreads) sm.selb[x] = sr[x];
+        if (INTERP == 1) {
+            const float *wr = a.wlin + (size_t)iz * a.nmx;
+            for (int x = tid; x < a.nmx; x += nthreads) sm.wl[x] = wr[x];
         }
     } else {
         const float po = a.po[iz];
@@ -110,101 +128,112 @@ template <int N> __device__ __forceinline__ int kfold(int t, int m)
     return k <= N / 2 ? k : N - k;
 }
 
-// Per-x selection data of depth iz for the thread's 16 positions.
-template <int N, int INTERP>
-__device__ __forceinline__ void load_sel(const MigArgs &a, int iz, int t, uint32_t (&sel)[16], float (&wl)[16])
+// The thread's selection bytes of the current depth (from shared memory), four per
+// register: bits 0-6 iref1, bit 7 set where the reference interpolates
+// (vref2 - vref1 > 10, wem.c:454); positions beyond nmx get 0x7f, which matches no
+// reference. Linear mode also loads the weight of iref2 (= iref1 + 1 there).
+template <int N, int INTERP, bool PSPI>
+__device__ __forceinline__ void load_sel(const Smem<N, PSPI> &sm, int nmx, int t, uint32_t (&selp)[4], float (&wl)[16])
 {
     constexpr int T = N / 16;
-    const uint32_t *selr = a.sel + (size_t)iz * a.nmx;
-    const float *wlr = a.wlin + (size_t)iz * a.nmx;
+#pragma unroll
+    for (int q = 0; q < 4; q++) selp[q] = 0;
 #pragma unroll
     for (int m = 0; m < 16; m++) {
         const int x = t + T * m;
-        sel[m] = x < a.nmx ? selr[x] : 0xffffu;  // 0xff never matches a reference index
-        wl[m] = (INTERP == 1 && x < a.nmx) ? wlr[x] : 0.f;
+        const uint32_t b = x < nmx ? sm.selb[x] : 0x7fu;
+        selp[m >> 2] |= b << (8 * (m & 3));
+        wl[m] = (INTERP == 1 && x < nmx) ? sm.wl[x] : 0.f;
     }
 }
 
-// Weight of reference r at one position, as the migration applies it after the
+// Weight of reference r at position m, as the migration applies it after the
 // inverse FFTs (wem.c:450-460); `re_only` reports the real-part truncation of
 // linear_interp's float return (wem.c:473-478).
 template <int INTERP>
-__device__ __forceinline__ float sel_weight(uint32_t s_, float wl, int r, bool &re_only)
+__device__ __forceinline__ float sel_weight(const uint32_t (&selp)[4], const float (&wl)[16], int m, int r, bool &re_only)
 {
-    const int i1 = s_ & 0xff, i2 = (s_ >> 8) & 0xff;
-    const bool interp = (s_ & SEL_INTERP) != 0;
+    const uint32_t b = (selp[m >> 2] >> (8 * (m & 3))) & 0xffu;
+    const int i1 = (int)(b & 0x7fu);
+    const bool interp = (b & 0x80u) != 0;
     re_only = (INTERP == 0) && interp;
     if (INTERP == 0 || !interp) return r == i1 ? 1.f : 0.f;
-    return (r == i1 ? 1.f - wl : 0.f) + (r == i2 ? wl : 0.f);
+    return r == i1 ? 1.f - wl[m] : (r == i1 + 1 ? wl[m] : 0.f);
 }
 
 // One depth step of the migration direction (extrap1f adj, wem.c:236-242): PSPI or
-// split-step on the team's row v (x-domain, x = t + T*m). CONJ selects -dz (the
-// source, and every row of the reference's modelling). Inactive rows keep v.
+// split-step on the team's row v (x-domain, x = t + T*m), in place. CONJ selects
+// -dz (the source, and every row of the reference's modelling). Called by active
+// teams only; `sync` is the team's barrier id (teams of 64+ threads) or warp mask.
 template <int N, bool PSPI, int INTERP>
-__device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, bool active, const MigArgs &a,
-                                         const Smem<N, PSPI> &sm, float2 *xbuf, int iz, int t, int bar)
+__device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, PSPI> &sm,
+                                         float2 *xbuf, float2 *sacc, int t, unsigned sync)
 {
     constexpr int T = N / 16, HALF = MigShape<N>::HALF;
-    float2 sp[16];
-#pragma unroll
-    for (int m = 0; m < 16; m++) sp[m] = v[m];
-    fft_row<N, -1>(sp, xbuf, sm.tw, t, bar);
-    float2 acc[16];
+    fft_row<N, -1>(v, xbuf, sm.tw, t, sync);  // v now holds the spectrum at k = t + T*m
     if (PSPI) {
-        uint32_t sel[16];
-        float wl[16];
-        load_sel<N, INTERP>(a, iz, t, sel, wl);
+        // sacc: this team's selection accumulator; thread t owns entries m*T + t
+        uint32_t selp[4];
 #pragma unroll
-        for (int m = 0; m < 16; m++) acc[m] = make_float2(0.f, 0.f);
+        for (int q = 0; q < 4; q++) selp[q] = 0;
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            selp[m >> 2] |= (x < a.nmx ? (uint32_t)sm.selb[x] : 0x7fu) << (8 * (m & 3));
+        }
         for (int r = 0; r < a.nref; r++) {
             const float2 *ph = sm.ph + (size_t)r * HALF;
             float2 u[16];
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const float2 P = ph[kfold<N>(t, m)];
-                u[m] = conj ? cmulc(sp[m], P) : cmul(sp[m], P);
+                u[m] = conj ? cmulc(v[m], P) : cmul(v[m], P);
             }
-            fft_row<N, +1>(u, xbuf, sm.tw, t, bar);
+            fft_row<N, +1>(u, xbuf, sm.tw, t, sync);
 #pragma unroll
             for (int m = 0; m < 16; m++) {
-                bool re_only;
-                const float wgt = sel_weight<INTERP>(sel[m], wl[m], r, re_only);
+                const uint32_t b = (selp[m >> 2] >> (8 * (m & 3))) & 0xffu;
+                const int i1 = (int)(b & 0x7fu);
+                const bool interp = (b & 0x80u) != 0;
+                float2 *dst = sacc + m * T + t;
                 if (INTERP == 0) {
-                    // the nearest-lower wavefield, whole or its real part
-                    if (wgt != 0.f) acc[m] = re_only ? make_float2(u[m].x, 0.f) : u[m];
-                } else {
-                    acc[m].x += u[m].x * wgt;
-                    acc[m].y += u[m].y * wgt;
+                    // the nearest-lower wavefield, whole or its real part (wem.c:454-459, 477)
+                    if (r == i1) *dst = interp ? make_float2(u[m].x, 0.f) : u[m];
+                } else if (!interp) {
+                    if (r == i1) *dst = u[m];
+                } else if (r == i1) {
+                    const float w1 = 1.f - sm.wl[t + T * m];
+                    *dst = make_float2(u[m].x * w1, u[m].y * w1);
+                } else if (r == i1 + 1) {
+                    const float w2 = sm.wl[t + T * m];
+                    const float2 q = *dst;
+                    *dst = make_float2(q.x + u[m].x * w2, q.y + u[m].y * w2);
                 }
             }
         }
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            v[m] = x < a.nmx ? sacc[m * T + t] : make_float2(0.f, 0.f);
+        }
     } else {
+        float2 acc[16];
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             const float2 P = sm.ph[kfold<N>(t, m)];
-            acc[m] = conj ? cmulc(sp[m], P) : cmul(sp[m], P);
+            acc[m] = conj ? cmulc(v[m], P) : cmul(v[m], P);
         }
-        fft_row<N, +1>(acc, xbuf, sm.tw, t, bar);
+        fft_row<N, +1>(acc, xbuf, sm.tw, t, sync);
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             const int x = t + T * m;
-            if (x < a.nmx) {
-                const float2 c = sm.corr[x];
-                acc[m] = conj ? cmulc(acc[m], c) : cmul(acc[m], c);
-            }
-        }
-    }
-    if (active) {
-#pragma unroll
-        for (int m = 0; m < 16; m++) {
-            const int x = t + T * m;
-            v[m] = x < a.nmx ? acc[m] : make_float2(0.f, 0.f);
+            v[m] = x < a.nmx ? (conj ? cmulc(acc[m], sm.corr[x]) : cmul(acc[m], sm.corr[x])) : make_float2(0.f, 0.f);
         }
     }
 }
 
-// One upward step of the modelling recursion (wem.c:273-274, -dz, adj=false).
+// One upward step of the modelling recursion (wem.c:273-274, -dz, adj=false), in
+// place, active teams only.
 // EXACT=false: the reference's operator -- PSPI as the migration step with -dz
 // (interpolation after the inverse FFTs); split-step with the taper and the
 // correction applied before the transform (wem.c:322-327).
@@ -213,12 +242,12 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, bool active
 // interpolation weights before transforming, y = sum_r F^-1 conj(P_r) F (W_r^T v);
 // for split-step the reference's operator already is that adjoint.
 template <int N, bool PSPI, int INTERP, bool EXACT>
-__device__ __forceinline__ void step_model(float2 (&v)[16], bool active, const MigArgs &a, const Smem<N, PSPI> &sm,
-                                           float2 *xbuf, int iz, int t, int bar)
+__device__ __forceinline__ void step_model(float2 (&v)[16], const MigArgs &a, const Smem<N, PSPI> &sm, float2 *xbuf,
+                                           float2 *sacc, int t, unsigned sync)
 {
     constexpr int T = N / 16, HALF = MigShape<N>::HALF;
     if (PSPI && !EXACT) {
-        step_mig<N, PSPI, INTERP>(v, true, active, a, sm, xbuf, iz, t, bar);
+        step_mig<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync);
         return;
     }
     float2 acc[16];
@@ -228,13 +257,13 @@ __device__ __forceinline__ void step_model(float2 (&v)[16], bool active, const M
             const int x = t + T * m;
             acc[m] = x < a.nmx ? cmulc(v[m], sm.corr[x]) : make_float2(0.f, 0.f);
         }
-        fft_row<N, -1>(acc, xbuf, sm.tw, t, bar);
+        fft_row<N, -1>(acc, xbuf, sm.tw, t, sync);
 #pragma unroll
         for (int m = 0; m < 16; m++) acc[m] = cmulc(acc[m], sm.ph[kfold<N>(t, m)]);
     } else {
-        uint32_t sel[16];
+        uint32_t selp[4];
         float wl[16];
-        load_sel<N, INTERP>(a, iz, t, sel, wl);
+        load_sel<N, INTERP, PSPI>(sm, a.nmx, t, selp, wl);
 #pragma unroll
         for (int m = 0; m < 16; m++) acc[m] = make_float2(0.f, 0.f);
         for (int r = 0; r < a.nref; r++) {
@@ -242,10 +271,10 @@ __device__ __forceinline__ void step_model(float2 (&v)[16], bool active, const M
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 bool re_only;
-                const float wgt = sel_weight<INTERP>(sel[m], wl[m], r, re_only);
+                const float wgt = sel_weight<INTERP>(selp, wl, m, r, re_only);
                 u[m] = make_float2(v[m].x * wgt, re_only ? 0.f : v[m].y * wgt);
             }
-            fft_row<N, -1>(u, xbuf, sm.tw, t, bar);
+            fft_row<N, -1>(u, xbuf, sm.tw, t, sync);
             const float2 *ph = sm.ph + (size_t)r * HALF;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
@@ -255,14 +284,22 @@ __device__ __forceinline__ void step_model(float2 (&v)[16], bool active, const M
             }
         }
     }
-    fft_row<N, +1>(acc, xbuf, sm.tw, t, bar);
-    if (active) {
+    fft_row<N, +1>(acc, xbuf, sm.tw, t, sync);
 #pragma unroll
-        for (int m = 0; m < 16; m++) {
-            const int x = t + T * m;
-            v[m] = x < a.nmx ? acc[m] : make_float2(0.f, 0.f);
-        }
+    for (int m = 0; m < 16; m++) {
+        const int x = t + T * m;
+        v[m] = x < a.nmx ? acc[m] : make_float2(0.f, 0.f);
     }
+}
+
+// Barrier handle of a row team: a named-barrier id for teams of 64 or more threads,
+// the team's lane mask within its warp otherwise.
+template <int N> __device__ __forceinline__ unsigned team_sync_handle(int tid)
+{
+    constexpr int T = N / 16;
+    if constexpr (T >= 64) return 1u + (unsigned)(tid / T);
+    else if constexpr (T == 32) return 0xffffffffu;
+    else return ((1u << T) - 1u) << ((tid & 31) / T * T);
 }
 
 }  // namespace gbwem

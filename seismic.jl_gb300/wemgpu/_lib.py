@@ -27,7 +27,8 @@ PRECISION = {"fp32": 0}
 # every symbol the public header declares
 EXPORTS = ["wem_last_error", "wem_version", "wem_ctx_create", "wem_ctx_destroy", "wem_prepare",
            "wem_migrate", "wem_migrate_device", "wem_migrate_survey", "wem_last_timing",
-           "wem_last_kernel_times", "wem_ctx_stream", "wem_migrate_noalloc", "wem",
+           "wem_last_kernel_times", "wem_ctx_stream", "wem_migrate_noalloc", "wem_model",
+           "wem_model_device", "wem",
            "shotwem_main", "main"]
 
 
@@ -78,6 +79,8 @@ def lib():
         L.wem_prepare.argtypes = [vp, C.POINTER(Params), fp, fp]
         L.wem_migrate.argtypes = [vp, C.c_int, fp, fp, i64p, i32p, fp, fp]
         L.wem_migrate_device.argtypes = [vp, C.c_int, fp, fp, i64p, i32p, vp, vp, C.c_int]
+        L.wem_model.argtypes = [vp, C.c_int, fp, fp, i64p, i32p, fp, fp, C.c_int]
+        L.wem_model_device.argtypes = [vp, C.c_int, fp, fp, i64p, i32p, vp, vp, C.c_int, C.c_int]
         L.wem_migrate_survey.argtypes = [vp, C.POINTER(Params), fp, fp, C.c_int, fp, fp, i64p, i32p, fp, fp]
         L.wem_last_timing.argtypes = [vp, C.POINTER(C.c_float), C.POINTER(C.c_int)]
         f_p = C.POINTER(C.c_float)

@@ -115,6 +115,26 @@ class Context:
                                     d.ctypes.data_as(_f32p), m.ctypes.data_as(_f32p)))
         return m
 
+    def model(self, shots: Shots, m: np.ndarray, exact: bool = False) -> np.ndarray:
+        """Born modelling of the image m [nmx*nmy, nz] at the traces of `shots` (their
+        data is ignored); returns [ntrace, nt]. exact=False: the reference's operator;
+        exact=True: the exact adjoint of migrate()."""
+        p = self.params
+        if p is None:
+            raise RuntimeError("prepare() first")
+        m = np.ascontiguousarray(m, dtype=np.float32)
+        if m.shape != (p.nmx * p.nmy, p.nz):
+            raise ValueError(f"m must be [nmx*nmy, nz] = {(p.nmx * p.nmy, p.nz)}")
+        sx = np.ascontiguousarray(shots.sx, dtype=np.float32)
+        sy = np.ascontiguousarray(shots.sy, dtype=np.float32)
+        off = np.ascontiguousarray(shots.trace_offset, dtype=np.int64)
+        cell = np.ascontiguousarray(shots.trace_cell, dtype=np.int32)
+        d = np.empty((int(off[-1]), p.nt), np.float32)
+        L.check(L.lib().wem_model(self._h, len(sx), sx.ctypes.data_as(_f32p), sy.ctypes.data_as(_f32p),
+                                  off.ctypes.data_as(_i64p), cell.ctypes.data_as(_i32p),
+                                  m.ctypes.data_as(_f32p), d.ctypes.data_as(_f32p), int(bool(exact))))
+        return d
+
     def migrate_device(self, shots: Shots, d_dev_ptr: int, m_dev_ptr: int, sync: bool = True):
         """Same, with the trace data and the image already in device memory (raw pointers)."""
         sx = np.ascontiguousarray(shots.sx, dtype=np.float32)
