@@ -45,6 +45,9 @@ def survey(workload: str, rank: int):
     elif workload == "survey8":
         c = synth.config1(seed=1001 + rank, nshot=8)
         wl = "2-D PSPI survey subset for profiling: 8 shots, 500x1024 grid @10 m, nref=8, 5-50 Hz, nt=1500"
+    elif workload == "survey3d":
+        c = synth.config3(seed=1003 + rank)
+        wl = "3-D PSPI: 1 shot, 300x256x256 grid @12.5 m, nref=6, 3-60 Hz, nt=2000, padx=padt=2 (512x512 planes)"
     elif workload == "split1":
         c = synth.config0(seed=1000 + rank)
         wl = "2-D split-step: 1 shot, 200x256 grid @10 m, 3 layers, 5-60 Hz, nt=1000, padx=padt=2"
@@ -160,6 +163,10 @@ def cpu_baseline(c, seconds_hint: float = 20.0):
     d = synth.shot_gather_full(shots, s, p["nmx"])
     cores = os.cpu_count() or 1
     kind = "reference" if O.ref_available() else "port"
+    if int(p.get("nmy", 1)) > 1:
+        # a 3-D depth step costs ~1000x a 2-D one: the sample is the lowest 17 frequencies
+        # (the band edge is (int)fmax, wem.c:86), about one per host core
+        p["fmax"] = float(p["fmin"]) + 2.0
     t0 = time.perf_counter()
     if kind == "reference":
         O.wem_ref(p, c["vel"], c["wav"], d=d, adj=True)
@@ -205,7 +212,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="survey64", choices=["survey64", "survey8", "split1"])
+    ap.add_argument("--workload", default="survey64", choices=["survey64", "survey8", "survey3d", "split1"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
     args = ap.parse_args()

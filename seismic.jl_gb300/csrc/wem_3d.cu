@@ -1,0 +1,410 @@
+// wem_3d.cu -- the 3-D depth recursion (nmy > 1): the x-y plane of a wavefield
+// (padx*nmx by padx*nmy complex samples, 2 MB at 512 x 512) does not fit in shared
+// memory, so one depth step of every (shot, frequency) in flight is three batched
+// passes over device memory (the planes stay L2/HBM resident between them):
+//
+//   pass A  rows:    U[x][y]  --FFT_y-->  Y[x][ky]                          (x < nmx)
+//   pass B  columns: Y[:, ky] --FFT_x--> A[kx][ky]; for every reference r:
+//                    A * P_r(kx, ky) --IFFT_x--> C_r[x][ky]                 (x < nmx)
+//   pass C  rows:    C_r[x][:] --IFFT_y--> select/interpolate over r (or the
+//                    split-step correction) --> U[x][y]; imaging condition
+//
+// which is the 2-D transform pair of pspiop/ssop (wem.c:380-471, 289-378: p1/p2 are
+// rank-2 FFTW plans over (nkx, nky), wem.c:100-104) split by axis. The source and the
+// receiver wavefield of an item are processed by the same CTA in every pass: pass B
+// shares the phase values between them (the source uses their conjugates) and pass C
+// forms the image. Pass C sums the image over a chunk of items in registers and
+// writes one partial image per chunk; wem_image_reduce_kernel adds the chunks.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "wem_fft.cuh"
+#include "wem_internal.h"
+#include "wem_step.cuh"
+
+namespace gbwem {
+
+// ---------------------------------------------------------------- pass A
+template <int NY>
+__global__ void __launch_bounds__(256) wem3d_rows_fwd_kernel(const Mig3dArgs a)
+{
+    constexpr int TY = NY / 16, TEAMS = 256 / TY;
+    constexpr int TW = fft_tw_size<NY>(), TWP = (TW + 1) & ~1;
+    extern __shared__ float4 smem_raw[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *s_x = s_tw + TWP;
+    const int tid = threadIdx.x, team = tid / TY, t = tid - team * TY;
+    float2 *xbuf = s_x + (size_t)team * pad16(NY);
+    const unsigned sync = team_sync_handle<NY>(tid);
+    for (int i = tid; i < TW; i += 256) s_tw[i] = a.twy[i];
+    __syncthreads();
+    const uint8_t zf = a.zflag[a.iz];
+    const int n = a.nmx * a.nmy;
+    const long long njobs = (long long)a.nitems * 2 * a.nmx;
+    for (long long job = (long long)blockIdx.x * TEAMS + team; job < njobs; job += (long long)gridDim.x * TEAMS) {
+        const int item = (int)(job / (2 * a.nmx));
+        const int rem = (int)(job - (long long)item * 2 * a.nmx);
+        const int w = rem / a.nmx, x = rem - w * a.nmx;
+        if (!(zf & (w == 0 ? Z_SRC : Z_REC))) continue;  // team-uniform
+        const float2 *urow = a.U + ((size_t)item * 2 + w) * n + (size_t)x * a.nmy;
+        float2 v[16];
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int y = t + TY * m;
+            v[m] = y < a.nmy ? urow[y] : make_float2(0.f, 0.f);
+        }
+        fft_row<NY, -1>(v, xbuf, s_tw, t, sync);
+        float2 *yrow = a.Y + (((size_t)item * 2 + w) * a.nmx + x) * NY;
+#pragma unroll
+        for (int m = 0; m < 16; m++) yrow[t + TY * m] = v[m];
+    }
+}
+
+// ---------------------------------------------------------------- pass B
+// CTA: 2*CW teams of TX = NX/16 threads -- the CW columns ky0..ky0+CW-1 of the source
+// (teams 0..CW-1) and of the receiver (teams CW..2CW-1) of one item.
+template <int NX> struct ColShape {
+    static constexpr int TX = NX / 16;
+    static constexpr int CW = (2 * TX >= 512) ? 1 : (512 / (2 * TX) > 16 ? 16 : 512 / (2 * TX));
+    static constexpr int NT = 2 * CW * TX;
+    static constexpr int HALF = NX / 2 + 1;
+    static constexpr int TW = fft_tw_size<NX>(), TWP = (TW + 1) & ~1;
+};
+
+__host__ __device__ constexpr size_t col_smem_bytes(int twp, int half, int cw, int teams, int padn, int nmx)
+{
+    return sizeof(float2) * ((size_t)twp + (size_t)cw * half + (size_t)teams * padn + (size_t)2 * nmx * cw);
+}
+
+template <int NX, bool PSPI>
+__global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3dArgs a)
+{
+    using CS = ColShape<NX>;
+    constexpr int TX = CS::TX, CW = CS::CW, NT = CS::NT, HALF = CS::HALF;
+    extern __shared__ float4 smem_raw[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *s_ph = s_tw + CS::TWP;                 // [CW][HALF] phase of one reference
+    float2 *s_x = s_ph + (size_t)CW * HALF;       // exchange buffers
+    float2 *s_tile = s_x + (size_t)2 * CW * pad16(NX);  // [2][nmx][CW] column tile
+    const int tid = threadIdx.x, team = tid / TX, t = tid - team * TX;
+    const int w = team / CW, c = team - w * CW;
+    float2 *xbuf = s_x + (size_t)team * pad16(NX);
+    const unsigned sync = team_sync_handle<NX>(tid);
+    for (int i = tid; i < CS::TW; i += NT) s_tw[i] = a.twx[i];
+    const uint8_t zf = a.zflag[a.iz];
+    const bool active = (zf & (w == 0 ? Z_SRC : Z_REC)) != 0;
+    const int nmx = a.nmx, nky = a.nky, nref = PSPI ? a.nref : 1;
+    const int nblk = nky / CW;
+    const int iz = a.iz;
+    for (int job = blockIdx.x; job < a.nitems * nblk; job += gridDim.x) {
+        const int item = job / nblk, ky0 = (job - item * nblk) * CW;
+        const int iw = a.ifmin + a.item_iwi[item];
+        const float wv = __fmul_rn((float)iw, a.dw);
+        const float w2 = __fmul_rn(wv, wv);
+        __syncthreads();  // the previous job no longer uses the tile or the tables
+        for (int e = tid; e < 2 * nmx * CW; e += NT) {
+            const int ww = e / (nmx * CW), r_ = e - ww * nmx * CW, x = r_ / CW, cc = r_ - x * CW;
+            s_tile[e] = a.Y[(((size_t)item * 2 + ww) * nmx + x) * nky + ky0 + cc];
+        }
+        __syncthreads();
+        float2 v[16];
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + TX * m;
+            v[m] = x < nmx ? s_tile[((size_t)w * nmx + x) * CW + c] : make_float2(0.f, 0.f);
+        }
+        if (active) fft_row<NX, -1>(v, xbuf, s_tw, t, sync);
+        const float slow_po = PSPI ? 0.f : __fmul_rn(a.po[iz], a.po[iz]);
+        for (int r = 0; r < nref; r++) {
+            __syncthreads();  // tile and table free
+            // phase of reference r for the CW columns: entry [cc][kk], |kx| = kk
+            const float slow2 = PSPI ? __fdiv_rn(1.0f, __fmul_rn(a.vref[(size_t)iz * a.nref + r], a.vref[(size_t)iz * a.nref + r]))
+                                     : slow_po;
+            for (int e = tid; e < CW * HALF; e += NT) {
+                const int cc = e / HALF, kk = e - cc * HALF;
+                const int kyi = ky0 + cc;
+                const float ky = kyi <= nky / 2 ? __fmul_rn(a.dky, (float)kyi) : -__fsub_rn(__fmul_rn(a.dky, (float)nky), __fmul_rn(a.dky, (float)kyi));
+                const float kx = __fmul_rn(a.dkx, (float)kk);
+                const float s = __fsub_rn(__fsub_rn(__fmul_rn(w2, slow2), __fmul_rn(kx, kx)), __fmul_rn(ky, ky));
+                float2 P;
+                if (s >= 0.f) {
+                    float sn, cs;
+                    sincosf(__fmul_rn(__fsqrt_rn(s), a.dz), &sn, &cs);
+                    P = make_float2(cs, sn);
+                } else {
+                    P = make_float2(expf(-__fmul_rn(__fmul_rn(0.2f, __fsqrt_rn(-s)), fabsf(a.dz))), 0.f);
+                }
+                s_ph[e] = make_float2(P.x * a.inv_n, P.y * a.inv_n);
+            }
+            __syncthreads();
+            if (active) {
+                float2 u[16];
+#pragma unroll
+                for (int m = 0; m < 16; m++) {
+                    const int k = t + TX * m;
+                    const float2 P = s_ph[(size_t)c * HALF + (k <= NX / 2 ? k : NX - k)];
+                    u[m] = w == 0 ? cmulc(v[m], P) : cmul(v[m], P);
+                }
+                fft_row<NX, +1>(u, xbuf, s_tw, t, sync);
+#pragma unroll
+                for (int m = 0; m < 16; m++) {
+                    const int x = t + TX * m;
+                    if (x < nmx) s_tile[((size_t)w * nmx + x) * CW + c] = u[m];
+                }
+            }
+            __syncthreads();
+            for (int e = tid; e < 2 * nmx * CW; e += NT) {
+                const int ww = e / (nmx * CW), r_ = e - ww * nmx * CW, x = r_ / CW, cc = r_ - x * CW;
+                if (zf & (ww == 0 ? Z_SRC : Z_REC))
+                    a.C[((((size_t)item * 2 + ww) * nref + r) * nmx + x) * nky + ky0 + cc] = s_tile[e];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- pass C
+// CTA of 256 threads: pairs of teams (source, receiver) of TY = NY/16 threads, one
+// pair per row x; each pair runs the items of one chunk in turn and keeps the
+// chunk's image row in registers.
+template <int NY, bool PSPI, int INTERP>
+__global__ void __launch_bounds__(256) wem3d_rows_inv_kernel(const Mig3dArgs a)
+{
+    constexpr int TY = NY / 16, TEAMS = 256 / TY, PAIRS = TEAMS / 2;
+    constexpr int TW = fft_tw_size<NY>(), TWP = (TW + 1) & ~1;
+    extern __shared__ float4 smem_raw[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *s_x = s_tw + TWP;
+    const int tid = threadIdx.x, team = tid / TY, t = tid - team * TY;
+    const int pair = team >> 1, w = team & 1;
+    float2 *xbuf = s_x + (size_t)team * pad16(NY);
+    const unsigned sync = team_sync_handle<NY>(tid);
+    for (int i = tid; i < TW; i += 256) s_tw[i] = a.twy[i];
+    __syncthreads();
+    const int iz = a.iz, nmx = a.nmx, nmy = a.nmy, nky = a.nky, n = nmx * nmy;
+    const int nref = PSPI ? a.nref : 1;
+    const uint8_t zf = a.zflag[iz];
+    const bool active = (zf & (w == 0 ? Z_SRC : Z_REC)) != 0;
+    const int nchunk = (a.nitems + a.chunk - 1) / a.chunk;
+    const long long njobs = (long long)nchunk * nmx;
+    // the pair's partner buffer for the imaging condition: the source team's xbuf
+    float2 *src_buf = s_x + (size_t)(pair * 2) * pad16(NY);
+    for (long long job = (long long)blockIdx.x * PAIRS + pair; job < njobs; job += (long long)gridDim.x * PAIRS) {
+        const int ch = (int)(job / nmx), x = (int)(job - (long long)ch * nmx);
+        const int it0 = ch * a.chunk, it1 = min(a.nitems, it0 + a.chunk);
+        float img[16];
+#pragma unroll
+        for (int m = 0; m < 16; m++) img[m] = 0.f;
+        // per-position selection of this depth and row
+        uint32_t selp[4] = { 0, 0, 0, 0 };
+        if (PSPI) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int y = t + TY * m;
+                const uint32_t b = y < nmy ? a.selb[(size_t)iz * n + (size_t)x * nmy + y] : 0x7fu;
+                selp[m >> 2] |= b << (8 * (m & 3));
+            }
+        }
+        for (int item = it0; item < it1; item++) {
+            const int iwi = a.item_iwi[item];
+            const int iw = a.ifmin + iwi;
+            const float wv = __fmul_rn((float)iw, a.dw);
+            const float factor = iw == 0 ? 1.f : 2.f;
+            float2 *urow = a.U + ((size_t)item * 2 + w) * n + (size_t)x * nmy;
+            float2 unew[16];
+            if (active) {
+                float2 acc[16];
+#pragma unroll
+                for (int m = 0; m < 16; m++) acc[m] = make_float2(0.f, 0.f);
+                for (int r = 0; r < nref; r++) {
+                    const float2 *crow = a.C + ((((size_t)item * 2 + w) * nref + r) * nmx + x) * nky;
+                    float2 u[16];
+#pragma unroll
+                    for (int m = 0; m < 16; m++) u[m] = crow[t + TY * m];
+                    fft_row<NY, +1>(u, xbuf, s_tw, t, sync);
+#pragma unroll
+                    for (int m = 0; m < 16; m++) {
+                        if (PSPI) {
+                            const uint32_t b = (selp[m >> 2] >> (8 * (m & 3))) & 0xffu;
+                            const int i1 = (int)(b & 0x7fu);
+                            const bool interp = (b & 0x80u) != 0;
+                            if (INTERP == 0) {
+                                if (r == i1) acc[m] = interp ? make_float2(u[m].x, 0.f) : u[m];
+                            } else if (!interp) {
+                                if (r == i1) acc[m] = u[m];
+                            } else if (r == i1 || r == i1 + 1) {
+                                const int y = t + TY * m;
+                                const float wl = a.wlin[(size_t)iz * n + (size_t)x * nmy + y];
+                                const float g = r == i1 ? 1.f - wl : wl;
+                                acc[m].x += u[m].x * g;
+                                acc[m].y += u[m].y * g;
+                            }
+                        } else {
+                            acc[m] = u[m];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int m = 0; m < 16; m++) {
+                    const int y = t + TY * m;
+                    float2 q = make_float2(0.f, 0.f);
+                    if (y < nmy) {
+                        q = acc[m];
+                        if (!PSPI) {
+                            // split-step correction and taper (wem.c:349-359), -dz for the source
+                            const float th = __fmul_rn(__fmul_rn(wv, a.pd[(size_t)iz * n + (size_t)x * nmy + y]), a.dz);
+                            float sn, cs;
+                            sincosf(th, &sn, &cs);
+                            const float tp = a.taper[x] * a.tapery[y];
+                            const float2 cr = make_float2(cs * tp, sn * tp);
+                            q = w == 0 ? cmulc(q, cr) : cmul(q, cr);
+                        }
+                        urow[y] = q;
+                    }
+                    unew[m] = q;
+                }
+            } else {
+#pragma unroll
+                for (int m = 0; m < 16; m++) {
+                    const int y = t + TY * m;
+                    unew[m] = y < nmy ? urow[y] : make_float2(0.f, 0.f);
+                }
+            }
+            if (zf & Z_REC) {
+                // imaging condition (wem.c:243-247): the pair meets in the source team's buffer
+                team_pair_sync<NY>(pair, tid);
+                if (w == 0) {
+#pragma unroll
+                    for (int m = 0; m < 16; m++) {
+                        const int y = t + TY * m;
+                        if (y < nmy) src_buf[y] = unew[m];
+                    }
+                }
+                team_pair_sync<NY>(pair, tid);
+                if (w == 1) {
+#pragma unroll
+                    for (int m = 0; m < 16; m++) {
+                        const int y = t + TY * m;
+                        if (y < nmy) {
+                            const float2 s_ = src_buf[y];
+                            img[m] += factor * (unew[m].x * s_.x + unew[m].y * s_.y);
+                        }
+                    }
+                }
+                team_pair_sync<NY>(pair, tid);
+            }
+        }
+        if (w == 1) {
+            float2 *part = a.img_parts + ((size_t)ch * a.nz + iz) * n + (size_t)x * nmy;
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int y = t + TY * m;
+                if (y < nmy) part[y] = make_float2(img[m], 0.f);
+            }
+        }
+    }
+}
+
+// initial planes: source spike at (igx, igy), receiver spectra (wem.c:230-233)
+__global__ void wem3d_init_kernel(const Mig3dArgs a)
+{
+    const int n = a.nmx * a.nmy;
+    const long long total = (long long)a.nitems * 2 * n;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int item = (int)(e / (2 * n));
+        const int rem = (int)(e - (long long)item * 2 * n);
+        const int w = rem / n, cell = rem - w * n;
+        const int shot = a.item_shot[item], iwi = a.item_iwi[item];
+        float2 v;
+        if (w == 0) v = cell == a.src_cell[shot] ? a.srcw[iwi] : make_float2(0.f, 0.f);
+        else v = a.recv[((size_t)shot * a.nwf + iwi) * n + cell];
+        a.U[e] = v;
+    }
+}
+
+// ---------------------------------------------------------------- host side
+template <int NY> static int rows_fwd(const Mig3dArgs &a, int grid, cudaStream_t st)
+{
+    constexpr int TW = fft_tw_size<NY>(), TWP = (TW + 1) & ~1;
+    const size_t smem = sizeof(float2) * ((size_t)TWP + (size_t)(256 / (NY / 16)) * pad16(NY));
+    auto k = wem3d_rows_fwd_kernel<NY>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    k<<<grid, 256, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int NY, bool PSPI, int INTERP> static int rows_inv(const Mig3dArgs &a, int grid, cudaStream_t st)
+{
+    constexpr int TW = fft_tw_size<NY>(), TWP = (TW + 1) & ~1;
+    const size_t smem = sizeof(float2) * ((size_t)TWP + (size_t)(256 / (NY / 16)) * pad16(NY));
+    auto k = wem3d_rows_inv_kernel<NY, PSPI, INTERP>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    k<<<grid, 256, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int NX, bool PSPI> static int cols(const Mig3dArgs &a, int grid, cudaStream_t st, size_t *smem_out)
+{
+    using CS = ColShape<NX>;
+    const size_t smem = col_smem_bytes(CS::TWP, CS::HALF, CS::CW, 2 * CS::CW, pad16(NX), a.nmx);
+    if (smem_out) { *smem_out = smem; return 0; }
+    auto k = wem3d_cols_kernel<NX, PSPI>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    k<<<grid, CS::NT, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+#define W3_SWITCH(n, CALL)              \
+    switch (n) {                        \
+    case 64: return CALL(64);           \
+    case 128: return CALL(128);         \
+    case 256: return CALL(256);         \
+    case 512: return CALL(512);         \
+    case 1024: return CALL(1024);       \
+    default: return -1;                 \
+    }
+
+int m3d_supported(int nkx, int nky)
+{
+    auto ok = [](int n) { return n == 64 || n == 128 || n == 256 || n == 512 || n == 1024; };
+    return ok(nkx) && ok(nky);
+}
+
+int m3d_cols_block(int nkx)
+{
+#define CALL(N) ColShape<N>::CW
+    W3_SWITCH(nkx, CALL)
+#undef CALL
+}
+
+int m3d_cols_smem(int nkx, int pspi, const Mig3dArgs &a, size_t *smem)
+{
+#define CALL(N) (pspi ? cols<N, true>(a, 0, 0, smem) : cols<N, false>(a, 0, 0, smem))
+    W3_SWITCH(nkx, CALL)
+#undef CALL
+}
+
+int m3d_launch_step(int nkx, int nky, int pspi, int interp, const Mig3dArgs &a, int nsm, cudaStream_t st)
+{
+    int rc;
+#define CALL(N) rows_fwd<N>(a, nsm * 4, st)
+    rc = [&]() { W3_SWITCH(nky, CALL) }();
+#undef CALL
+    if (rc) return rc;
+#define CALL(N) (pspi ? cols<N, true>(a, nsm * 2, st, nullptr) : cols<N, false>(a, nsm * 2, st, nullptr))
+    rc = [&]() { W3_SWITCH(nkx, CALL) }();
+#undef CALL
+    if (rc) return rc;
+#define CALL(N) (!pspi ? rows_inv<N, false, 0>(a, nsm * 4, st) : interp == 0 ? rows_inv<N, true, 0>(a, nsm * 4, st) : rows_inv<N, true, 1>(a, nsm * 4, st))
+    rc = [&]() { W3_SWITCH(nky, CALL) }();
+#undef CALL
+    return rc;
+}
+
+int m3d_launch_init(const Mig3dArgs &a, cudaStream_t st)
+{
+    wem3d_init_kernel<<<1024, 256, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace gbwem

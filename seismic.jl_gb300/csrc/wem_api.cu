@@ -13,6 +13,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -72,11 +73,13 @@ struct wem_ctx {
     bool prepared = false;
     wem_params p{};
     int ntfft = 0, nw = 0, nf = 0, ifmin = 0, ifmax = 0, nwf = 0, nkx = 0, nky = 0;
-    float dw = 0.f, dkx = 0.f;
+    float dw = 0.f, dkx = 0.f, dky = 0.f;
 
     // per-velocity tables
     DevBuf vref, po, pd, sel, wlin, taper, zflag, twid, wtab, scale_recv, scale_src, srcw, wav, wav_base;
     DevBuf ssyn_ref, ssyn_exact;  // synthesis weights w^2 * (half-spectrum | image) factor
+    DevBuf tapery, twy;           // 3-D: y taper and y-FFT twiddles
+    DevBuf m3_items, m3_U, m3_Y, m3_C, m3_parts;
     // per-call buffers
     DevBuf recv, slots, image, data, tbase, igx, smig, mimg;
     int max_smem = 0;
@@ -124,7 +127,8 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
     DevBuf *bufs[] = { &c->vref, &c->po, &c->pd, &c->sel, &c->wlin, &c->taper, &c->zflag, &c->twid,
                        &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
                        &c->ssyn_ref, &c->ssyn_exact, &c->recv, &c->slots, &c->image, &c->data,
-                       &c->tbase, &c->igx, &c->smig, &c->mimg };
+                       &c->tbase, &c->igx, &c->smig, &c->mimg, &c->tapery, &c->twy, &c->m3_items,
+                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -202,10 +206,16 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
                     p.nref);
     if (p.interp != WEM_INTERP_REF && p.interp != WEM_INTERP_LINEAR) return fail(WEM_ERR_ARG, "unknown interp %d", p.interp);
     if (p.precision != WEM_PREC_FP32) return fail(WEM_ERR_SIZE, "precision mode %d not built", p.precision);
-    if (p.nmy != 1) return fail(WEM_ERR_SIZE, "3-D grids (nmy=%d) are not supported by this build", p.nmy);
     const int nkx = p.nmx > 1 ? p.padx * p.nmx : 1;
-    if (!is_pow2(nkx) || nkx < 32 || nkx > 4096)
-        return fail(WEM_ERR_SIZE, "nkx = padx*nmx = %d must be a power of two in [32, 4096]", nkx);
+    const int nky = p.nmy > 1 ? p.padx * p.nmy : 1;
+    if (p.nmy == 1) {
+        if (!is_pow2(nkx) || nkx < 32 || nkx > 4096)
+            return fail(WEM_ERR_SIZE, "nkx = padx*nmx = %d must be a power of two in [32, 4096]", nkx);
+    } else if (!m3d_supported(nkx, nky)) {
+        return fail(WEM_ERR_SIZE, "3-D: padx*nmx = %d and padx*nmy = %d must be powers of two in [64, 1024]", nkx, nky);
+    } else if (!(p.dmy > 0)) {
+        return fail(WEM_ERR_ARG, "3-D: dmy must be positive");
+    }
     CK(cudaSetDevice(c->device));
 
     int ntfft, nw, ifmin, ifmax;
@@ -217,15 +227,15 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
 
     // a1: slowness split (wem.c:28-36); a2: reference velocities (wem.c:40-70).
     // Device layouts are depth-major ([iz][ix]) so that a depth step reads a row.
-    std::vector<float> po(nz), pd((size_t)nz * nmx), vref((size_t)nz * nref), wl((size_t)nz * nmx, 0.f);
-    std::vector<uint8_t> sel((size_t)nz * nmx);
+    std::vector<float> po(nz), pd((size_t)nz * n), vref((size_t)nz * nref), wl((size_t)nz * n, 0.f);
+    std::vector<uint8_t> sel((size_t)nz * n);
     for (int iz = 0; iz < nz; iz++) {
         float s = 0.;
         for (int ix = 0; ix < n; ix++) s += vel[(size_t)ix * nz + iz];
         s /= (float)p.nmx * p.nmy;
         s = 1. / s;
         po[iz] = s;
-        for (int ix = 0; ix < n; ix++) pd[(size_t)iz * nmx + ix] = 1.0 / vel[(size_t)ix * nz + iz] - po[iz];
+        for (int ix = 0; ix < n; ix++) pd[(size_t)iz * n + ix] = 1.0 / vel[(size_t)ix * nz + iz] - po[iz];
         float vmin = vel[iz], vmax = vel[(size_t)(p.nmx - 1) * nz + iz];
         for (int ix = 0; ix < p.nmx; ix++) if (vel[(size_t)ix * nz + iz] < vmin) vmin = vel[(size_t)ix * nz + iz];
         for (int ix = 0; ix < n; ix++) if (vel[(size_t)ix * nz + iz] > vmax) vmax = vel[(size_t)ix * nz + iz];
@@ -245,23 +255,25 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
             uint8_t word = (uint8_t)i1;  // where it interpolates, i2 = i1 + 1
             if (vr2 - vr1 > 10.0) {
                 word |= SEL_INTERP;
-                wl[(size_t)iz * nmx + ix] = (v - vr1) / (vr2 - vr1);
+                wl[(size_t)iz * n + ix] = (v - vr1) / (vr2 - vr1);
             }
-            sel[(size_t)iz * nmx + ix] = word;
+            sel[(size_t)iz * n + ix] = word;
         }
     }
-    // taper of the split-step operator (wem.c:546-564), 2-D: tmy = 1
-    std::vector<float> taper(nmx);
-    {
-        const int lmx = p.nmx > 100 ? 30 : 0;
-        float tmx = 1.f;
-        for (int imx = 0; imx < nmx; imx++) {
-            if (imx >= 0 && imx < lmx) tmx = expf(-powf(0.015 * ((float)lmx - imx), 2.));
-            if (imx >= lmx && imx <= nmx - lmx) tmx = 1.;
-            if (imx > nmx - lmx && imx < nmx) tmx = expf(-powf(0.015 * ((float)imx - nmx + lmx), 2.));
-            taper[imx] = tmx;
+    // taper of the split-step operator (wem.c:546-564): tmx(imx) * tmy(imy)
+    auto taper_of = [](int nm) {
+        std::vector<float> tp(nm);
+        const int lm = nm > 100 ? 30 : 0;
+        float tm = 1.f;
+        for (int im = 0; im < nm; im++) {
+            if (im >= 0 && im < lm) tm = expf(-powf(0.015 * ((float)lm - im), 2.));
+            if (im >= lm && im <= nm - lm) tm = 1.;
+            if (im > nm - lm && im < nm) tm = expf(-powf(0.015 * ((float)im - nm + lm), 2.));
+            tp[im] = tm;
         }
-    }
+        return tp;
+    };
+    std::vector<float> taper = taper_of(nmx), tapery = taper_of(p.nmy);
     std::vector<uint8_t> zf(nz);
     for (int iz = 0; iz < nz; iz++) {
         const float z = p.oz + p.dz * iz;
@@ -270,6 +282,9 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     const int ntw = twiddle_table_size(nkx);
     std::vector<float2> tw(ntw > 0 ? ntw : 1);
     twiddle_table_host(nkx, tw.data());
+    const int ntwy = p.nmy > 1 ? twiddle_table_size(nky) : 1;
+    std::vector<float2> twy(ntwy > 0 ? ntwy : 1);
+    if (p.nmy > 1) twiddle_table_host(nky, twy.data());
     // the real transform of f_op has length (nw-1)*2 (wem.c:487), which is ntfft - 1
     // when padt*nt is odd
     const int nf = (nw - 1) * 2;
@@ -304,7 +319,8 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         (rc = ensure(c->scale_src, sizeof(float) * ssrc.size())) || (rc = ensure(c->srcw, sizeof(float2) * (nwf > 0 ? nwf : 1))) ||
         (rc = ensure(c->wav, sizeof(float) * p.nt)) || (rc = ensure(c->wav_base, sizeof(int64_t))) ||
         (rc = ensure(c->ssyn_ref, sizeof(float) * syn_ref.size())) ||
-        (rc = ensure(c->ssyn_exact, sizeof(float) * syn_exact.size())))
+        (rc = ensure(c->ssyn_exact, sizeof(float) * syn_exact.size())) ||
+        (rc = ensure(c->tapery, sizeof(float) * tapery.size())) || (rc = ensure(c->twy, sizeof(float2) * twy.size())))
         return rc;
     cudaStream_t st = c->st;
     CK(cudaMemcpyAsync(c->po.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
@@ -313,6 +329,8 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     CK(cudaMemcpyAsync(c->sel.p, sel.data(), sel.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->wlin.p, wl.data(), sizeof(float) * wl.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->taper.p, taper.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->tapery.p, tapery.data(), sizeof(float) * tapery.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->twy.p, twy.data(), sizeof(float2) * twy.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->zflag.p, zf.data(), nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->twid.p, tw.data(), sizeof(float2) * tw.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->wtab.p, wtab.data(), sizeof(float2) * nf, cudaMemcpyHostToDevice, st));
@@ -349,9 +367,10 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     c->ifmax = ifmax;
     c->nwf = nwf;
     c->nkx = nkx;
-    c->nky = 1;
+    c->nky = nky;
     c->dw = dw;
     c->dkx = 2 * 3.141592653589793 / ((float)nkx) / p.dmx;
+    c->dky = 2 * 3.141592653589793 / ((float)nky) / p.dmy;
     c->prepared = true;
     c->last_nshot = -1;
     return WEM_OK;
@@ -371,9 +390,9 @@ static int set_shots(wem_ctx *c, int nshot, const float *sx, const float *sy, co
         const int gx = (int)(sx[s] - p.omx) / p.dmx;
         const float syv = sy ? sy[s] : 0.f;
         const int gy = (int)(syv - p.omy) / p.dmy;
-        if (gx < 0 || gx >= p.nmx || gy != 0)
+        if (gx < 0 || gx >= p.nmx || gy < 0 || gy >= p.nmy)
             return fail(WEM_ERR_ARG, "shot %d: source (%g, %g) falls outside the grid (igx=%d, igy=%d)", s, sx[s], syv, gx, gy);
-        igx[s] = gx;
+        igx[s] = gx * p.nmy + gy;  // source cell (= igx in 2-D)
     }
     const int64_t ntr = toff[nshot];
     std::vector<int64_t> base(ntr > 0 ? ntr : 1);
@@ -381,7 +400,7 @@ static int set_shots(wem_ctx *c, int nshot, const float *sx, const float *sy, co
         for (int64_t i = toff[s]; i < toff[s + 1]; i++) {
             const int cell = tcell[i];
             if (cell < 0 || cell >= p.nmx * p.nmy) return fail(WEM_ERR_ARG, "trace %lld: cell %d outside the grid", (long long)i, cell);
-            base[i] = ((int64_t)s * c->nwf) * p.nmx + cell;
+            base[i] = ((int64_t)s * c->nwf) * ((int64_t)p.nmx * p.nmy) + cell;
         }
     *ntr_out = ntr;
     const bool same = c->last_nshot == nshot && c->h_igx == igx && c->h_tbase.size() == (size_t)ntr &&
@@ -409,10 +428,89 @@ static int cta_shape(wem_ctx *c, int pspi, int nmx, int nref)
     return (int)smem <= c->max_smem ? 1 : 0;
 }
 
+// 3-D migration: spectra -> per depth step the three plane passes of wem_3d.cu for
+// every (shot, frequency) of a batch -> image chunks -> image.
+static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, float *m_dev)
+{
+    const wem_params &p = c->p;
+    cudaStream_t st = c->st;
+    const int nmx = p.nmx, nmy = p.nmy, nz = p.nz, n = nmx * nmy;
+    const int nref = p.pspi ? p.nref : 1;
+    const int nitems = nshot * c->nwf;
+    const int chunk = std::max(32, (nitems + 15) / 16);
+    const int nchunk = (nitems + chunk - 1) / chunk;
+    // items per batch: whole chunks, within half of the free device memory
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const size_t per_item = sizeof(float2) * ((size_t)2 * n + (size_t)2 * nmx * c->nky * (1 + nref));
+    const size_t parts_b = sizeof(float2) * (size_t)nchunk * nz * n;
+    const size_t recv_b = sizeof(float2) * (size_t)nshot * c->nwf * n;
+    if (parts_b + recv_b + per_item * chunk > free_b)
+        return fail(WEM_ERR_NOMEM, "3-D survey needs %zu MB of device memory at least", (parts_b + recv_b + per_item * chunk) >> 20);
+    long long fit = (long long)((free_b - parts_b - recv_b) / 2 / per_item);
+    int batch = (int)std::min<long long>(nitems, std::max<long long>(chunk, fit / chunk * chunk));
+    int rc;
+    if ((rc = ensure(c->recv, recv_b)) || (rc = ensure(c->m3_parts, parts_b)) ||
+        (rc = ensure(c->m3_U, sizeof(float2) * (size_t)batch * 2 * n)) ||
+        (rc = ensure(c->m3_Y, sizeof(float2) * (size_t)batch * 2 * nmx * c->nky)) ||
+        (rc = ensure(c->m3_C, sizeof(float2) * (size_t)batch * 2 * nref * nmx * c->nky)) ||
+        (rc = ensure(c->m3_items, sizeof(int) * 2 * (size_t)nitems)))
+        return rc;
+    std::vector<int> items(2 * (size_t)nitems);
+    for (int it = 0; it < nitems; it++) { items[it] = it % c->nwf; items[nitems + it] = it / c->nwf; }
+    CK(cudaMemcpyAsync(c->m3_items.p, items.data(), sizeof(int) * items.size(), cudaMemcpyHostToDevice, st));
+    int kernels = 0;
+    CK(cudaEventRecord(c->ev0, st));
+    CK(cudaMemsetAsync(c->recv.p, 0, recv_b, st));
+    CK(cudaMemsetAsync(c->m3_parts.p, 0, parts_b, st));
+    CK(cudaEventRecord(c->evk[0], st));
+    if (c->nwf > 0 && ntr > 0) {
+        SpectraArgs sa{};
+        sa.d = d_dev; sa.ntr = (int)ntr; sa.nt = p.nt; sa.ntfft = c->nf; sa.ifmin = c->ifmin; sa.nwf = c->nwf;
+        sa.out_base = P<int64_t>(c->tbase); sa.out_fstride = n; sa.wtab = P<float2>(c->wtab);
+        sa.scale = P<float>(c->scale_recv); sa.out = P<float2>(c->recv);
+        if (launch_spectra(sa, st)) return fail(WEM_ERR_CUDA, "spectra launch: %s", cudaGetErrorString(cudaGetLastError()));
+        kernels++;
+    }
+    CK(cudaEventRecord(c->evk[1], st));
+    for (int b0 = 0; b0 < nitems; b0 += batch) {
+        const int nb = std::min(batch, nitems - b0);
+        Mig3dArgs a{};
+        a.nmx = nmx; a.nmy = nmy; a.nkx = c->nkx; a.nky = c->nky; a.nz = nz; a.nref = nref; a.nwf = c->nwf;
+        a.ifmin = c->ifmin; a.nitems = nb; a.chunk = chunk;
+        a.dw = c->dw; a.dz = p.dz; a.dkx = c->dkx; a.dky = c->dky; a.inv_n = 1.0f / ((float)c->nkx * c->nky);
+        a.vref = P<float>(c->vref); a.po = P<float>(c->po); a.pd = P<float>(c->pd); a.wlin = P<float>(c->wlin);
+        a.taper = P<float>(c->taper); a.tapery = P<float>(c->tapery); a.selb = P<uint8_t>(c->sel);
+        a.zflag = P<uint8_t>(c->zflag); a.twx = P<float2>(c->twid); a.twy = P<float2>(c->twy);
+        a.item_iwi = P<int>(c->m3_items) + b0; a.item_shot = P<int>(c->m3_items) + nitems + b0;
+        a.src_cell = P<int>(c->igx); a.srcw = P<float2>(c->srcw); a.recv = P<float2>(c->recv);
+        a.U = P<float2>(c->m3_U); a.Y = P<float2>(c->m3_Y); a.C = P<float2>(c->m3_C);
+        // batches start on chunk boundaries, so the chunk index of local item i is (b0+i)/chunk
+        a.img_parts = P<float2>(c->m3_parts) + (size_t)(b0 / chunk) * nz * n;
+        if (m3d_launch_init(a, st)) return fail(WEM_ERR_CUDA, "3-D init launch: %s", cudaGetErrorString(cudaGetLastError()));
+        kernels++;
+        for (int iz = 0; iz < nz; iz++) {
+            a.iz = iz;
+            if (m3d_launch_step(c->nkx, c->nky, p.pspi, p.interp, a, c->nsm, st))
+                return fail(WEM_ERR_CUDA, "3-D depth step launch: %s", cudaGetErrorString(cudaGetLastError()));
+            kernels += 3;
+        }
+    }
+    CK(cudaEventRecord(c->evk[2], st));
+    if (launch_image_reduce(P<float2>(c->m3_parts), nchunk, nz, n, m_dev, st))
+        return fail(WEM_ERR_CUDA, "reduce launch: %s", cudaGetErrorString(cudaGetLastError()));
+    kernels++;
+    CK(cudaEventRecord(c->evk[3], st));
+    CK(cudaEventRecord(c->ev1, st));
+    c->last_kernels = kernels;
+    return WEM_OK;
+}
+
 // GPU part of a migration: spectra -> depth recursion -> image. Stream-ordered on c->st.
 static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, float *m_dev)
 {
     const wem_params &p = c->p;
+    if (p.nmy > 1) return run_migrate3d(c, nshot, ntr, d_dev, m_dev);
     cudaStream_t st = c->st;
     const int nmx = p.nmx, nz = p.nz;
     int S, threads, bps = 0;
@@ -550,6 +648,7 @@ extern "C" int wem_migrate_survey(wem_ctx *c, const wem_params *p, const float *
 static int run_model(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, float *d_dev, int exact)
 {
     const wem_params &p = c->p;
+    if (p.nmy > 1) return fail(WEM_ERR_SIZE, "modelling of 3-D grids is not built (migration is)");
     cudaStream_t st = c->st;
     const int nmx = p.nmx, nz = p.nz;
     int S, threads, bps = 0;

@@ -70,6 +70,26 @@ struct SynthArgs {
     float *out;               // [ntr][nt]
 };
 
+// 3-D depth recursion (wem_3d.cu): state of every item (shot, frequency) in flight.
+struct Mig3dArgs {
+    int nmx, nmy, nkx, nky, nz, nref, nwf, ifmin, nitems, chunk, iz;
+    float dw, dz, dkx, dky, inv_n;
+    const float *vref, *po, *pd, *wlin, *taper, *tapery;
+    const uint8_t *selb, *zflag;
+    const float2 *twx, *twy;
+    const int *item_iwi, *item_shot, *src_cell;
+    const float2 *srcw, *recv;
+    float2 *U;          // [item][2][nmx][nmy]
+    float2 *Y;          // [item][2][nmx][nky]
+    float2 *C;          // [item][2][nref][nmx][nky]
+    float2 *img_parts;  // [chunk][nz][nmx*nmy] (sum, 0)
+};
+int m3d_supported(int nkx, int nky);
+int m3d_cols_block(int nkx);
+int m3d_cols_smem(int nkx, int pspi, const Mig3dArgs &a, size_t *smem);
+int m3d_launch_step(int nkx, int nky, int pspi, int interp, const Mig3dArgs &a, int nsm, cudaStream_t st);
+int m3d_launch_init(const Mig3dArgs &a, cudaStream_t st);
+
 // host-side launchers (wem_kernels.cu). `wide` selects the 512-thread CTA shape of
 // the migration kernel (2S rows sharing the phase tables) over the 256-thread one.
 int migrate_config(int nkx, int wide, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem);

@@ -302,4 +302,18 @@ template <int N> __device__ __forceinline__ unsigned team_sync_handle(int tid)
     else return ((1u << T) - 1u) << ((tid & 31) / T * T);
 }
 
+// Barrier of a pair of row teams (2T threads starting at team 2*pair): the pair's warp
+// lanes when it fits in a warp, else a named barrier (ids 8..15, above the ids
+// team_sync_handle hands out to CTAs of up to 512 threads).
+template <int N> __device__ __forceinline__ void team_pair_sync(int pair, int tid)
+{
+    constexpr int T = N / 16;
+    if constexpr (2 * T <= 32) {
+        constexpr unsigned lanes = (2 * T == 32) ? 0xffffffffu : ((1u << (2 * T)) - 1u);
+        __syncwarp(2 * T == 32 ? lanes : lanes << ((tid & 31) / (2 * T) * (2 * T)));
+    } else {
+        asm volatile("bar.sync %0, %1;" ::"r"(8 + pair), "n"(2 * T) : "memory");
+    }
+}
+
 }  // namespace gbwem

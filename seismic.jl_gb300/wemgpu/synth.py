@@ -12,6 +12,8 @@ Workloads (seed = 1000 + index):
   1  PSPI, Gaussian random-field velocity (sigma 200 m, mean 3000, std 400 m/s,
      clipped to [1500, 4500]) nz=500 x nx=1024, 10 m; 64 shots, apertures
      U{200..800} traces centred on the source; nt=1500; 5-50 Hz; nref=8
+  3  3-D PSPI, smooth random field in [1500, 4000] m/s, nz=300 x 256 x 256 at 12.5 m;
+     one shot at the centre, 256 x 256 receivers; nt=2000; 3-60 Hz; nref=6
   4  PSPI, dipping layers 1500..3500 m/s, nz=300 x nx=512, 10 m; 32 shots with
      256..512 receivers; nt=1500; 5-45 Hz; nref=8
 """
@@ -191,6 +193,76 @@ def small_case(seed: int, nx: int = 64, nz: int = 24, nt: int = 128, nshot: int 
     params = dict(nt=nt, ot=0.0, dt=dt, nmx=nx, omx=0.0, dmx=dx, nz=nz, oz=0.0, dz=dz,
                   fmin=3.0, fmax=fmax, padt=padt, padx=padx, pspi=pspi, nref=nref, interp=interp)
     return dict(name=f"small seed={seed}", params=params, vel=vel, wav=wav, shots=shots)
+
+
+def diffraction_gather_3d(xr, yr, sx, sy, points, amps, nt, dt, wav, vmean):
+    """Like diffraction_gather for receivers at (xr[i], yr[i]), constant-velocity times."""
+    nr = len(xr)
+    spikes = np.zeros((nr, nt), np.float64)
+    for (px, py, pz), a in zip(points, amps):
+        tau = (np.sqrt((px - sx) ** 2 + (py - sy) ** 2 + pz ** 2) +
+               np.sqrt((xr - px) ** 2 + (yr - py) ** 2 + pz ** 2)) / vmean
+        f = tau / dt
+        i0 = np.floor(f).astype(np.int64)
+        w1 = f - i0
+        ok = (i0 >= 0) & (i0 + 1 < nt)
+        r = np.nonzero(ok)[0]
+        np.add.at(spikes, (r, i0[ok]), a * (1 - w1[ok]))
+        np.add.at(spikes, (r, i0[ok] + 1), a * w1[ok])
+    n = 1 << int(np.ceil(np.log2(nt + len(wav))))
+    W = np.fft.rfft(wav.astype(np.float64), n)
+    return np.fft.irfft(np.fft.rfft(spikes, n, axis=1) * W[None, :], n, axis=1)[:, :nt].astype(np.float32)
+
+
+def smooth_field_3d(rng, nx, ny, nz, sigma, lo, hi):
+    g = gaussian_filter(rng.standard_normal((nx, ny, nz)), sigma, mode="reflect")
+    g = (g - g.min()) / (g.max() - g.min())
+    return (lo + (hi - lo) * g).astype(np.float32)
+
+
+def config3(seed: int = 1003, nx: int = 256, ny: int = 256, nz: int = 300, nt: int = 2000, fmax: float = 60.0,
+            npoints: int = 50, d: float = 12.5):
+    rng = np.random.default_rng(seed)
+    dt = 0.002
+    vel = smooth_field_3d(rng, nx, ny, nz, 8.0, 1500.0, 4000.0).reshape(nx * ny, nz)
+    wav = wavelet_trace(nt, dt)
+    sx, sy = (nx // 2) * d, (ny // 2) * d
+    pts = np.stack([rng.uniform(0, (nx - 1) * d, npoints), rng.uniform(0, (ny - 1) * d, npoints),
+                    rng.uniform(10 * d, (nz - 1) * d, npoints)], 1)
+    amps = rng.uniform(0.5, 1.0, npoints)
+    gx, gy = np.meshgrid(np.arange(nx) * d, np.arange(ny) * d, indexing="ij")
+    data = diffraction_gather_3d(gx.ravel(), gy.ravel(), sx, sy, pts, amps, nt, dt, wav, float(vel.mean()))
+    shots = Shots(np.array([sx], np.float32), np.array([sy], np.float32), np.array([0, nx * ny], np.int64),
+                  np.arange(nx * ny, dtype=np.int32), data)
+    params = dict(nt=nt, ot=0.0, dt=dt, nmx=nx, omx=0.0, dmx=d, nmy=ny, omy=0.0, dmy=d, nz=nz, oz=0.0, dz=d,
+                  fmin=3.0, fmax=fmax, padt=2, padx=2, pspi=1, nref=6)
+    return dict(name=f"3-D PSPI, 1 shot, nz={nz} x {nx} x {ny}, nref=6", params=params, vel=vel, wav=wav,
+                shots=shots)
+
+
+def small_case3d(seed: int, nx: int = 32, ny: int = 32, nz: int = 10, nt: int = 64, nshot: int = 1, pspi: int = 1,
+                 nref: int = 3, interp: str = "ref", fmax: float = 40.0, padx: int = 2):
+    """Seeded small 3-D survey; the velocity's minimum of every depth lies on the first
+    x-plane (the reference takes vmin over the first nmx traces, wem.c:48-49)."""
+    rng = np.random.default_rng(seed)
+    d = 10.0
+    dt = 0.004
+    vel = smooth_field_3d(rng, nx, ny, nz, 2.0, 1800.0, 3200.0)
+    vel[0, 0, :] = vel.min(axis=(0, 1)) - 1.0
+    vel = vel.reshape(nx * ny, nz)
+    wav = wavelet_trace(nt, dt, f0=15.0)
+    srcs = [((nx // 2 + 3 * s) * d, (ny // 2 - 2 * s) * d) for s in range(nshot)]
+    pts = np.stack([rng.uniform(0, (nx - 1) * d, 4), rng.uniform(0, (ny - 1) * d, 4),
+                    rng.uniform(3 * d, (nz - 1) * d, 4)], 1)
+    amps = rng.uniform(0.5, 1.0, 4)
+    gx, gy = np.meshgrid(np.arange(nx) * d, np.arange(ny) * d, indexing="ij")
+    datas = [diffraction_gather_3d(gx.ravel(), gy.ravel(), sx, sy, pts, amps, nt, dt, wav, 2500.0) for sx, sy in srcs]
+    shots = Shots(np.array([q[0] for q in srcs], np.float32), np.array([q[1] for q in srcs], np.float32),
+                  np.arange(nshot + 1, dtype=np.int64) * nx * ny, np.tile(np.arange(nx * ny, dtype=np.int32), nshot),
+                  np.concatenate(datas))
+    params = dict(nt=nt, ot=0.0, dt=dt, nmx=nx, omx=0.0, dmx=d, nmy=ny, omy=0.0, dmy=d, nz=nz, oz=0.0, dz=d,
+                  fmin=3.0, fmax=fmax, padt=2, padx=padx, pspi=pspi, nref=nref, interp=interp)
+    return dict(name=f"small 3-D seed={seed}", params=params, vel=vel, wav=wav, shots=shots)
 
 
 def shot_gather_full(shots: Shots, s: int, ncell: int) -> np.ndarray:

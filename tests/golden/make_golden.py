@@ -60,6 +60,19 @@ def main():
                             params=np.array(repr({k: v for k, v in p.items()})))
         print(name, "image norm", float(np.linalg.norm(m_ref)), "data norm", float(np.linalg.norm(d_ref)))
 
+    # 3-D (nmy > 1): rank-2 transforms over (nkx, nky), wem.c:100-104
+    for name, (seed, pspi) in {"ss3d_32": (21, 0), "pspi3d_32": (22, 1)}.items():
+        c = synth.small_case3d(seed, nx=32, ny=32, nz=8, nt=64, pspi=pspi, nref=3)
+        p = dict(c["params"], sx=float(c["shots"].sx[0]), sy=float(c["shots"].sy[0]))
+        d = c["shots"].data
+        rng = np.random.default_rng(seed + 100)
+        m_in = rng.standard_normal((32 * 32, 8)).astype(np.float32)
+        m_ref = O.wem_ref(p, c["vel"], c["wav"], d=d, adj=True)
+        d_ref = O.wem_ref(p, c["vel"], c["wav"], m=m_in, adj=False)
+        np.savez_compressed(os.path.join(HERE, f"wem_{name}.npz"), vel=c["vel"], wav=c["wav"], d=d, m_in=m_in,
+                            m_ref=m_ref, d_ref=d_ref, params=np.array(repr(p)))
+        print(name, "image norm", float(np.linalg.norm(m_ref)))
+
     # file-level: the reference's main() on seis files (shotwem.c:12-140)
     p, vel, wav, d, _ = case_inputs(*CASES["pspi_64"])
     with tempfile.TemporaryDirectory() as td:
