@@ -1,0 +1,78 @@
+"""The file-level operator ShotProfileWEM(m, d, adj; ...) over seis files
+(src/Imaging/ShotProfileWEM.jl:39-310)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+
+def _write_survey(tmp, c):
+    """vel, wav and one data file holding every shot (headers sx, gx, ...), as SeisWindow
+    expects to find them."""
+    from wemgpu import seis, synth
+    p, shots = c["params"], c["shots"]
+    seis.write_grid(os.path.join(tmp, "vel"), c["vel"], o1=0.0, d1=p["dz"], ox=p["omx"], dx=p["dmx"])
+    seis.write_wavelet(os.path.join(tmp, "wav"), c["wav"], dt=p["dt"])
+    nx, nt = p["nmx"], p["nt"]
+    datas, hs = [], []
+    for s in range(shots.nshot):
+        g = synth.shot_gather_full(shots, s, nx)
+        h = seis.empty_headers(nx)
+        h["n1"], h["d1"], h["sx"] = nt, p["dt"], shots.sx[s]
+        h["gx"] = p["omx"] + p["dmx"] * np.arange(nx)
+        h["imx"] = np.arange(nx)
+        datas.append(g)
+        hs.append(h)
+    seis.write(os.path.join(tmp, "d"), np.concatenate(datas), np.concatenate(hs), [nt, nx, 1, shots.nshot, 1],
+               [0.0, p["omx"], 0.0, float(shots.sx[0]), 0.0], [p["dt"], p["dmx"], 1.0, 1.0, 1.0])
+
+
+def test_window_shots_selects_by_source_and_places_by_receiver(tmp_path):
+    from wemgpu import seis, shotprofile
+    h = seis.empty_headers(6)
+    h["sx"] = [100, 100, 200, 200, 200, 300]
+    h["gx"] = [0, 20, 10, 30, 40, 0]
+    d = np.arange(6 * 4, dtype=np.float32).reshape(6, 4)
+    g = dict(nmx=5, omx=0.0, dmx=10.0, nmy=1, omy=0.0, dmy=10.0)
+    s = shotprofile.window_shots(d, h, [200.0, 100.0], [0.0, 0.0], g)
+    assert list(s.trace_offset) == [0, 3, 5]
+    assert list(s.trace_cell) == [1, 3, 4, 0, 2]
+    assert np.array_equal(s.data[0], d[2]) and np.array_equal(s.data[3], d[0])
+
+
+def test_image_headers_follow_the_reference():
+    from wemgpu import shotprofile
+    g = dict(nmx=3, nmy=2, dmx=10.0, dmy=5.0, nz=7, min_imx=4, min_imy=1)
+    h = shotprofile.image_headers(g, 2.5)
+    assert list(h["imx"]) == [4, 4, 5, 5, 6, 6] and list(h["imy"]) == [1, 2, 1, 2, 1, 2]
+    assert list(h["mx"]) == [40, 40, 50, 50, 60, 60] and h["n1"][0] == 7 and h["tracenum"][0] == 2
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pspi", [0, 1])
+def test_shotprofile_migration_and_demigration_on_files(gpu_lib, oracle_mod, tmp_path, pspi):
+    from wemgpu import seis, synth, shotprofile
+    c = synth.small_case(121, nx=64, nz=16, nt=128, nshot=3, pspi=pspi, nref=4)
+    p = c["params"]
+    _write_survey(str(tmp_path), c)
+    sx = [float(v) for v in c["shots"].sx]
+    kw = dict(pspi=bool(pspi), nref=p["nref"], vel=str(tmp_path / "vel"), wav=str(tmp_path / "wav"),
+              fmin=p["fmin"], fmax=p["fmax"], padt=p["padt"], padx=p["padx"], sx=sx, sy=[0.0] * len(sx))
+    shotprofile.ShotProfileWEM(str(tmp_path / "m"), str(tmp_path / "d"), True, **kw)
+    m, hm, em = seis.read(str(tmp_path / "m"))
+    want = None
+    for s, x0 in enumerate(sx):
+        g = synth.shot_gather_full(c["shots"], s, p["nmx"])
+        w = oracle_mod.wem_port(dict(p, sx=x0), c["vel"], c["wav"], d=g, adj=True).astype(np.float64)
+        want = w if want is None else want + w
+    assert rel_l2(m, want) < 1e-4
+    assert em["n"][:3] == [p["nz"], p["nmx"], 1]
+    # demigration of that image back to data
+    shotprofile.ShotProfileWEM(str(tmp_path / "m"), str(tmp_path / "dm"), False, **kw)
+    dm, hd, ed = seis.read(str(tmp_path / "dm"))
+    for s, x0 in enumerate(sx):
+        w = oracle_mod.wem_port(dict(p, sx=x0), c["vel"], c["wav"], m=m, adj=False)
+        assert rel_l2(dm[s * p["nmx"]:(s + 1) * p["nmx"]], w) < 1e-4
+        assert np.all(hd["sx"][s * p["nmx"]:(s + 1) * p["nmx"]] == np.float32(x0))
