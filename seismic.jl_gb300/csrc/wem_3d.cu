@@ -119,8 +119,7 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
         for (int r = 0; r < nref; r++) {
             __syncthreads();  // tile and table free
             // phase of reference r for the CW columns: entry [cc][kk], |kx| = kk
-            const float slow2 = PSPI ? __fdiv_rn(1.0f, __fmul_rn(a.vref[(size_t)iz * a.nref + r], a.vref[(size_t)iz * a.nref + r]))
-                                     : slow_po;
+            const float slow2 = PSPI ? a.slow2[(size_t)iz * a.nref + r] : slow_po;
             for (int e = tid; e < CW * HALF; e += NT) {
                 const int cc = e / HALF, kk = e - cc * HALF;
                 const int kyi = ky0 + cc;

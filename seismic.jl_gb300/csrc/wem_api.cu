@@ -76,7 +76,7 @@ struct wem_ctx {
     float dw = 0.f, dkx = 0.f, dky = 0.f;
 
     // per-velocity tables
-    DevBuf vref, po, pd, sel, wlin, taper, zflag, twid, wtab, scale_recv, scale_src, srcw, wav, wav_base;
+    DevBuf vref, slow2, po, pd, sel, wlin, taper, zflag, twid, wtab, scale_recv, scale_src, srcw, wav, wav_base;
     DevBuf ssyn_ref, ssyn_exact;  // synthesis weights w^2 * (half-spectrum | image) factor
     DevBuf tapery, twy;           // 3-D: y taper and y-FFT twiddles
     DevBuf m3_items, m3_U, m3_Y, m3_C, m3_parts;
@@ -124,7 +124,7 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
     if (!c) return WEM_OK;
     cudaSetDevice(c->device);
     if (c->st) cudaStreamSynchronize(c->st);
-    DevBuf *bufs[] = { &c->vref, &c->po, &c->pd, &c->sel, &c->wlin, &c->taper, &c->zflag, &c->twid,
+    DevBuf *bufs[] = { &c->vref, &c->slow2, &c->po, &c->pd, &c->sel, &c->wlin, &c->taper, &c->zflag, &c->twid,
                        &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
                        &c->ssyn_ref, &c->ssyn_exact, &c->recv, &c->slots, &c->image, &c->data,
                        &c->tbase, &c->igx, &c->smig, &c->mimg, &c->tapery, &c->twy, &c->m3_items,
@@ -228,6 +228,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     // a1: slowness split (wem.c:28-36); a2: reference velocities (wem.c:40-70).
     // Device layouts are depth-major ([iz][ix]) so that a depth step reads a row.
     std::vector<float> po(nz), pd((size_t)nz * n), vref((size_t)nz * nref), wl((size_t)nz * n, 0.f);
+    std::vector<float> slow2((size_t)nz * nref);
     std::vector<uint8_t> sel((size_t)nz * n);
     for (int iz = 0; iz < nz; iz++) {
         float s = 0.;
@@ -239,8 +240,11 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         float vmin = vel[iz], vmax = vel[(size_t)(p.nmx - 1) * nz + iz];
         for (int ix = 0; ix < p.nmx; ix++) if (vel[(size_t)ix * nz + iz] < vmin) vmin = vel[(size_t)ix * nz + iz];
         for (int ix = 0; ix < n; ix++) if (vel[(size_t)ix * nz + iz] > vmax) vmax = vel[(size_t)ix * nz + iz];
-        for (int ir = 0; ir < nref; ir++)
-            vref[(size_t)iz * nref + ir] = nref > 1 ? vmin + (float)ir * (vmax - vmin) / ((float)nref - 1) : vmin;
+        for (int ir = 0; ir < nref; ir++) {
+            const float vr = nref > 1 ? vmin + (float)ir * (vmax - vmin) / ((float)nref - 1) : vmin;
+            vref[(size_t)iz * nref + ir] = vr;
+            slow2[(size_t)iz * nref + ir] = 1 / (vr * vr);  // the float expression of wem.c:434
+        }
         for (int ix = 0; ix < n; ix++) {
             const float v = vel[(size_t)ix * nz + iz];
             int i1 = 0, i2 = 0;
@@ -312,7 +316,8 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
 
     int rc;
     if ((rc = ensure(c->po, sizeof(float) * nz)) || (rc = ensure(c->pd, sizeof(float) * pd.size())) ||
-        (rc = ensure(c->vref, sizeof(float) * vref.size())) || (rc = ensure(c->sel, sel.size())) ||
+        (rc = ensure(c->vref, sizeof(float) * vref.size())) ||
+        (rc = ensure(c->slow2, sizeof(float) * slow2.size())) || (rc = ensure(c->sel, sel.size())) ||
         (rc = ensure(c->wlin, sizeof(float) * wl.size())) || (rc = ensure(c->taper, sizeof(float) * nmx)) ||
         (rc = ensure(c->zflag, nz)) || (rc = ensure(c->twid, sizeof(float2) * tw.size())) ||
         (rc = ensure(c->wtab, sizeof(float2) * nf)) || (rc = ensure(c->scale_recv, sizeof(float) * srec.size())) ||
@@ -326,6 +331,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     CK(cudaMemcpyAsync(c->po.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->pd.p, pd.data(), sizeof(float) * pd.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->vref.p, vref.data(), sizeof(float) * vref.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->slow2.p, slow2.data(), sizeof(float) * slow2.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->sel.p, sel.data(), sel.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->wlin.p, wl.data(), sizeof(float) * wl.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->taper.p, taper.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
@@ -479,7 +485,7 @@ static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev,
         a.nmx = nmx; a.nmy = nmy; a.nkx = c->nkx; a.nky = c->nky; a.nz = nz; a.nref = nref; a.nwf = c->nwf;
         a.ifmin = c->ifmin; a.nitems = nb; a.chunk = chunk;
         a.dw = c->dw; a.dz = p.dz; a.dkx = c->dkx; a.dky = c->dky; a.inv_n = 1.0f / ((float)c->nkx * c->nky);
-        a.vref = P<float>(c->vref); a.po = P<float>(c->po); a.pd = P<float>(c->pd); a.wlin = P<float>(c->wlin);
+        a.vref = P<float>(c->vref); a.slow2 = P<float>(c->slow2); a.po = P<float>(c->po); a.pd = P<float>(c->pd); a.wlin = P<float>(c->wlin);
         a.taper = P<float>(c->taper); a.tapery = P<float>(c->tapery); a.selb = P<uint8_t>(c->sel);
         a.zflag = P<uint8_t>(c->zflag); a.twx = P<float2>(c->twid); a.twy = P<float2>(c->twy);
         a.item_iwi = P<int>(c->m3_items) + b0; a.item_shot = P<int>(c->m3_items) + nitems + b0;
@@ -573,7 +579,7 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
         a.recv = P<float2>(c->recv);
         a.srcw = P<float2>(c->srcw);
         a.igx = P<int>(c->igx);
-        a.vref = P<float>(c->vref);
+        a.vref = P<float>(c->vref); a.slow2 = P<float>(c->slow2);
         a.po = P<float>(c->po);
         a.pd = P<float>(c->pd);
         a.selb = P<uint8_t>(c->sel);
@@ -682,7 +688,7 @@ static int run_model(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, flo
         a.nmx = nmx; a.nz = nz; a.nref = p.pspi ? p.nref : 1; a.nwf = c->nwf; a.ifmin = c->ifmin;
         a.nshot = nshot; a.ngroups = ngroups; a.dw = c->dw; a.dz = p.dz; a.dkx = c->dkx;
         a.inv_n = 1.0f / (float)c->nkx;
-        a.recv = nullptr; a.srcw = P<float2>(c->srcw); a.igx = P<int>(c->igx); a.vref = P<float>(c->vref);
+        a.recv = nullptr; a.srcw = P<float2>(c->srcw); a.igx = P<int>(c->igx); a.vref = P<float>(c->vref); a.slow2 = P<float>(c->slow2);
         a.po = P<float>(c->po); a.pd = P<float>(c->pd); a.selb = P<uint8_t>(c->sel); a.wlin = P<float>(c->wlin);
         a.taper = P<float>(c->taper); a.zflag = P<uint8_t>(c->zflag); a.twid = P<float2>(c->twid); a.slots = nullptr;
         BornArgs b{};

@@ -160,6 +160,11 @@ __device__ __forceinline__ void fft_pass(float2 (&v)[16], float2 *xbuf, const fl
     constexpr int NS = fft_span<N>(P);
     constexpr int B = E / R;
     constexpr int TWO = fft_tw_offset<N>(P);
+    // For T >= 16 every exchange offset added to t (or to a pass base) is a multiple of
+    // 16, and pad16(base + 16q) = pad16(base) + 17q: shared addresses are a per-thread
+    // base plus a compile-time constant.
+    constexpr bool FAST = T >= 16;
+    const int pt = t + (t >> 4);  // pad16(t)
     float2 u[E];
     if constexpr (P == 0) {
 #pragma unroll
@@ -171,7 +176,8 @@ __device__ __forceinline__ void fft_pass(float2 (&v)[16], float2 *xbuf, const fl
         for (int b = 0; b < B; b++) {
             const int j = t + T * b;
 #pragma unroll
-            for (int r = 0; r < R; r++) u[b * R + r] = xbuf[pad16(j + r * (N / R))];
+            for (int r = 0; r < R; r++)
+                u[b * R + r] = FAST ? xbuf[pt + (T * b + r * (N / R)) / 16 * 17] : xbuf[pad16(j + r * (N / R))];
         }
         team_sync<T>(bar_id);  // every thread has read xbuf before it is rewritten
 #pragma unroll
@@ -197,8 +203,17 @@ __device__ __forceinline__ void fft_pass(float2 (&v)[16], float2 *xbuf, const fl
         for (int b = 0; b < B; b++) {
             const int j = t + T * b;
             const int base = (j / NS) * NS * R + (j % NS);
+            if constexpr (FAST && NS == 1 && R == 16) {
 #pragma unroll
-            for (int r = 0; r < R; r++) xbuf[pad16(base + r * NS)] = u[b * R + r];
+                for (int r = 0; r < R; r++) xbuf[17 * t + r] = u[b * R + r];  // B == 1: j == t
+            } else if constexpr (FAST && NS >= 16) {
+                const int pb = base + (base >> 4);
+#pragma unroll
+                for (int r = 0; r < R; r++) xbuf[pb + r * (NS / 16) * 17] = u[b * R + r];
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; r++) xbuf[pad16(base + r * NS)] = u[b * R + r];
+            }
         }
         team_sync<T>(bar_id);  // writes visible before the next pass reads
         fft_pass<N, DIR, P + 1>(v, xbuf, tw, t, bar_id);

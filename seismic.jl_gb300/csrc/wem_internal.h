@@ -31,6 +31,7 @@ struct MigArgs {
     const float2 *srcw;    // [nwf] wavelet spectrum / sqrt(ntfft)
     const int *igx;        // [nshot] source cell
     const float *vref;     // [nz][nref]
+    const float *slow2;    // [nz][nref] 1/(vref*vref) in float (wem.c:434)
     const float *po;       // [nz] mean slowness
     const float *pd;       // [nz][nmx] slowness perturbation
     const uint8_t *selb;   // [nz][nmx] selection bytes
@@ -74,7 +75,7 @@ struct SynthArgs {
 struct Mig3dArgs {
     int nmx, nmy, nkx, nky, nz, nref, nwf, ifmin, nitems, chunk, iz;
     float dw, dz, dkx, dky, inv_n;
-    const float *vref, *po, *pd, *wlin, *taper, *tapery;
+    const float *vref, *slow2, *po, *pd, *wlin, *taper, *tapery;
     const uint8_t *selb, *zflag;
     const float2 *twx, *twy;
     const int *item_iwi, *item_shot, *src_cell;

@@ -40,7 +40,7 @@ static __device__ __align__(256) unsigned char g_wem_scratch[WEM_NOALLOC_SCRATCH
 namespace {
 
 struct Layout {
-    size_t po, pd, vref, sel, wlin, taper, zflag, twid, wtab, srec, ssrc, srcw, igx, tbase, wbase, recv, img, total;
+    size_t po, pd, vref, slow2, sel, wlin, taper, zflag, twid, wtab, srec, ssrc, srcw, igx, tbase, wbase, recv, img, total;
 };
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -53,6 +53,7 @@ Layout noalloc_layout(int nmx, int nz, int nref, int ntw, int nf, int nwf, int n
     L.po = take(sizeof(float) * nz);
     L.pd = take(sizeof(float) * (size_t)nz * nmx);
     L.vref = take(sizeof(float) * (size_t)nz * nref);
+    L.slow2 = take(sizeof(float) * (size_t)nz * nref);
     L.sel = take((size_t)nz * nmx);
     L.wlin = take(sizeof(float) * (size_t)nz * nmx);
     L.taper = take(sizeof(float) * nmx);
@@ -99,7 +100,7 @@ struct TableArgs {
     const float *vel;  // [nmx][nz] (the reference's layout)
     int nmx, nz, nref, ntw, nkx, nf, nwf, ifmin, ntfft, nshot, lmx;
     float oz, dz, sz, gz, dw;
-    float *po, *pd, *vref, *wlin, *taper, *srec, *ssrc;
+    float *po, *pd, *vref, *slow2, *wlin, *taper, *srec, *ssrc;
     uint8_t *sel;
     uint8_t *zflag;
     float2 *twid, *wtab;
@@ -138,10 +139,13 @@ __global__ void __launch_bounds__(256) noalloc_tables_kernel(const TableArgs a)
         __syncthreads();
         const float po = s_po, vmin = s_vmin, vmax = s_vmax;
         const int nr = a.nref;
-        for (int r = tid; r < nr; r += blockDim.x)
-            a.vref[(size_t)iz * nr + r] =
+        for (int r = tid; r < nr; r += blockDim.x) {
+            const float vr =
                 nr > 1 ? __fadd_rn(vmin, __fdiv_rn(__fmul_rn((float)r, __fsub_rn(vmax, vmin)), __fsub_rn((float)nr, 1.f)))
                        : vmin;
+            a.vref[(size_t)iz * nr + r] = vr;
+            a.slow2[(size_t)iz * nr + r] = __fdiv_rn(1.f, __fmul_rn(vr, vr));
+        }
         for (int ix = tid; ix < a.nmx; ix += blockDim.x) {
             const float v = a.vel[(size_t)ix * a.nz + iz];
             a.pd[(size_t)iz * a.nmx + ix] = __double2float_rn(__dsub_rn(__ddiv_rn(1.0, (double)v), (double)po));
@@ -401,7 +405,7 @@ extern "C" WEM_API int wem_migrate_noalloc(const wem_params *pp, const float *ve
     ta.nmx = p.nmx; ta.nz = p.nz; ta.nref = nref; ta.ntw = ntw; ta.nkx = nkx; ta.nf = nf; ta.nwf = nwf;
     ta.ifmin = ifmin; ta.ntfft = ntfft; ta.nshot = nshot; ta.lmx = p.nmx > 100 ? 30 : 0;
     ta.oz = p.oz; ta.dz = p.dz; ta.sz = p.sz; ta.gz = p.gz; ta.dw = dw;
-    ta.po = NA(float, po); ta.pd = NA(float, pd); ta.vref = NA(float, vref); ta.wlin = NA(float, wlin);
+    ta.po = NA(float, po); ta.pd = NA(float, pd); ta.vref = NA(float, vref); ta.slow2 = NA(float, slow2); ta.wlin = NA(float, wlin);
     ta.taper = NA(float, taper); ta.srec = NA(float, srec); ta.ssrc = NA(float, ssrc);
     ta.sel = NA(uint8_t, sel); ta.zflag = NA(uint8_t, zflag); ta.twid = NA(float2, twid); ta.wtab = NA(float2, wtab);
     ta.igx = NA(int, igx); ta.tbase = NA(int64_t, tbase); ta.wbase = NA(int64_t, wbase);
@@ -420,6 +424,7 @@ extern "C" WEM_API int wem_migrate_noalloc(const wem_params *pp, const float *ve
         a.nmx = p.nmx; a.nz = p.nz; a.nref = nref; a.nwf = nwf; a.ifmin = ifmin; a.nshot = nshot;
         a.dw = dw; a.dz = p.dz; a.dkx = dkx; a.inv_n = 1.0f / (float)nkx;
         a.recv = NA(float2, recv); a.srcw = NA(float2, srcw); a.igx = NA(int, igx); a.vref = NA(float, vref);
+        a.slow2 = NA(float, slow2);
         a.po = NA(float, po); a.pd = NA(float, pd); a.selb = NA(uint8_t, sel); a.wlin = NA(float, wlin);
         a.taper = NA(float, taper); a.zflag = NA(uint8_t, zflag); a.twid = NA(float2, twid); a.slots = nullptr;
         int r2 = -1;

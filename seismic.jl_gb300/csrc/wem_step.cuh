@@ -93,12 +93,12 @@ __device__ __forceinline__ void build_tables(const MigArgs &a, const Smem<N, PSP
 {
     constexpr int HALF = MigShape<N>::HALF;
     if (PSPI) {
-        const float *vr = a.vref + (size_t)iz * a.nref;
-        for (int e = tid; e < a.nref * HALF; e += nthreads) {
-            const int r = e / HALF, kk = e - r * HALF;
-            const float v_ = vr[r];
-            const float slow2 = __fdiv_rn(1.0f, __fmul_rn(v_, v_));
-            sm.ph[e] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
+        const float *sl = a.slow2 + (size_t)iz * a.nref;
+        for (int r = 0; r < a.nref; r++) {
+            const float slow2 = sl[r];
+            float2 *ph = sm.ph + (size_t)r * HALF;
+            for (int kk = tid; kk < HALF; kk += nthreads)
+                ph[kk] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
         }
         const uint8_t *sr = a.selb + (size_t)iz * a.nmx;
         for (int x = tid; x < a.nmx; x += nthreads) sm.selb[x] = sr[x];
@@ -122,10 +122,12 @@ __device__ __forceinline__ void build_tables(const MigArgs &a, const Smem<N, PSP
     }
 }
 
+// |k| of position m of thread t: k = t + T*m is at most N/2 exactly for m < 8 (or
+// m == 8, t == 0, where both forms give N/2), and the folded index N - k is T*(16-m) - t.
 template <int N> __device__ __forceinline__ int kfold(int t, int m)
 {
-    const int k = t + (N / 16) * m;
-    return k <= N / 2 ? k : N - k;
+    constexpr int T = N / 16;
+    return m < 8 ? t + T * m : T * (16 - m) - t;
 }
 
 // The thread's selection bytes of the current depth (from shared memory), four per
