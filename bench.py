@@ -48,6 +48,11 @@ def survey(workload: str, rank: int):
     elif workload == "survey3d":
         c = synth.config3(seed=1003 + rank)
         wl = "3-D PSPI: 1 shot, 300x256x256 grid @12.5 m, nref=6, 3-60 Hz, nt=2000, padx=padt=2 (512x512 planes)"
+    elif workload == "lsm32":
+        c = synth.config4(seed=1004 + rank)
+        c["params"] = dict(c["params"], interp="linear")
+        wl = ("2-D least-squares PSPI migration: 32 shots, 300x512 grid @10 m, nref=8, 5-45 Hz, nt=1500, "
+              "20 CG iterations over the exact modelling/migration pair")
     elif workload == "split1":
         c = synth.config0(seed=1000 + rank)
         wl = "2-D split-step: 1 shot, 200x256 grid @10 m, 3 layers, 5-60 Hz, nt=1000, padx=padt=2"
@@ -206,13 +211,60 @@ def run_reference_arm(args):
     return 0
 
 
+def run_lsm(args, ctx, c, wl, units, dev, rank, world, dist):
+    """configs[4]: Born data of a seeded reflectivity (1 % of the cells, N(0,1)), then CG
+    (Scales 1987) from zero over wem_model(exact) / wem_migrate. One step = one CG solve."""
+    import torch
+    from wemgpu import Shots
+    from wemgpu.cg import conjugate_gradients, dot_test
+    p, shots = c["params"], c["shots"]
+    rng = np.random.default_rng(2004)
+    m_true = np.zeros((int(p["nmx"]), int(p["nz"])), np.float32)
+    k = m_true.size // 100
+    m_true.flat[rng.choice(m_true.size, k, replace=False)] = rng.standard_normal(k).astype(np.float32)
+    d_obs = ctx.model(shots, m_true, exact=True)
+    geo = lambda d: Shots(shots.sx, shots.sy, shots.trace_offset, shots.trace_cell, np.ascontiguousarray(d, np.float32))
+    fwd = lambda m: ctx.model(shots, np.asarray(m, np.float32), exact=True)
+    adj = lambda r: ctx.migrate(geo(r))
+    a, b = dot_test(fwd, adj, rng.standard_normal(m_true.shape).astype(np.float32),
+                    rng.standard_normal(d_obs.shape).astype(np.float32))
+    for _ in range(args.warmup):
+        conjugate_gradients(d_obs, fwd, adj, niter=2)
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.synchronize()
+    sampler.start()
+    t0 = time.perf_counter()
+    costs = None
+    for _ in range(args.steps):
+        m_est, costs = conjugate_gradients(d_obs, fwd, adj, niter=20)
+    el = (time.perf_counter() - t0) / args.steps
+    clocks = sampler.stop()
+    napply = 2 * 20 + 1
+    err = float(np.linalg.norm(m_est - m_true) / np.linalg.norm(m_true))
+    line = {"metric": "shot*omega*depth-steps/s", "value": world * napply * units / el, "unit": "shot*omega*depth-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * el,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": wl, "units_per_operator": units, "operator_applications_per_step": napply,
+                       "l2": "inputs larger than L2"},
+            "e2e": {"value": world * napply * units / el, "unit": "shot*omega*depth-steps/s",
+                    "h2d_bytes_per_step": int(napply * (shots.data.nbytes + m_true.nbytes) // 2),
+                    "d2h_bytes_per_step": int(napply * (shots.data.nbytes + m_true.nbytes) // 2)},
+            "cg": {"misfit": [float(x) for x in costs], "dot_test": [a, b], "dot_rel": abs(a - b) / abs(a),
+                   "model_rel_err": err},
+            "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="survey64", choices=["survey64", "survey8", "survey3d", "split1"])
+    ap.add_argument("--workload", default="survey64", choices=["survey64", "survey8", "survey3d", "split1", "lsm32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
     args = ap.parse_args()
@@ -241,9 +293,11 @@ def main():
     units = nshot * nf * nz
     ctx = wemgpu.Context(local).prepare(p, c["vel"], c["wav"])
     d_dev = torch.from_numpy(np.ascontiguousarray(shots.data)).to(dev)
-    m_dev = torch.empty((int(p["nmx"]), nz), dtype=torch.float32, device=dev)
+    m_dev = torch.empty((int(p["nmx"]) * int(p.get("nmy", 1)), nz), dtype=torch.float32, device=dev)  # [nmx*nmy][nz]
     stream = torch.cuda.ExternalStream(ctx.stream(), device=dev)
 
+    if args.workload == "lsm32":
+        return run_lsm(args, ctx, c, wl, units, dev, rank, world, dist)
     for _ in range(args.warmup):
         ctx.migrate_device(shots, d_dev.data_ptr(), m_dev.data_ptr(), sync=True)
     kernels_per_step = ctx.last_timing()[1]
@@ -274,7 +328,7 @@ def main():
 
     # end to end through the public API with host buffers
     e2e_t = []
-    img = np.zeros((int(p["nmx"]), nz), np.float32)
+    img = np.zeros((int(p["nmx"]) * int(p.get("nmy", 1)), nz), np.float32)
     for _ in range(max(1, args.e2e_steps)):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
