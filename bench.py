@@ -165,9 +165,10 @@ def cpu_baseline(c, seconds_hint: float = 20.0):
     shots = c["shots"]
     s = shots.nshot // 2
     p["sx"] = float(shots.sx[s])
-    d = synth.shot_gather_full(shots, s, p["nmx"])
+    d = synth.shot_gather_full(shots, s, int(p["nmx"]) * int(p.get("nmy", 1)))
     cores = os.cpu_count() or 1
     kind = "reference" if O.ref_available() else "port"
+    nf_all = band(p)
     if int(p.get("nmy", 1)) > 1:
         # a 3-D depth step costs ~1000x a 2-D one: the sample is the lowest 17 frequencies
         # (the band edge is (int)fmax, wem.c:86), about one per host core
@@ -181,7 +182,7 @@ def cpu_baseline(c, seconds_hint: float = 20.0):
     dt = time.perf_counter() - t0
     units = band(p) * int(p["nz"])
     return {"value": units / dt, "unit": "shot*omega*depth-steps/s", "cores": cores, "kind": kind,
-            "sample": f"1 of {shots.nshot} shots, all {band(p)} frequencies x {p['nz']} depth steps "
+            "sample": f"1 of {shots.nshot} shots, {band(p)} of {nf_all} frequencies x {p['nz']} depth steps "
                       f"({units} units) in {dt:.1f} s"}
 
 
