@@ -75,11 +75,13 @@ def band(p: dict):
 
 def flops_per_unit(p: dict) -> float:
     """Algorithmic FLOPs of one (shot, frequency, depth step): source and receiver
-    continuation plus the imaging condition, 5 N log2 N per complex FFT.
+    continuation plus the imaging condition, 5 N log2 N per complex FFT, with
+    N = nkx (2-D) or nkx*nky (3-D) and n = nmx*nmy.
     PSPI:  per wavefield 5N log2N + R (6N + 5N log2N) + 8n;  unit = 2 F + 3n.
     Split-step: per wavefield 2 * 5N log2N + 6N + 14n;     unit = 2 F + 3n."""
-    n = int(p["nmx"])
-    N = int(p["padx"]) * n
+    nmy = int(p.get("nmy", 1))
+    n = int(p["nmx"]) * nmy
+    N = int(p["padx"]) * int(p["nmx"]) * (int(p["padx"]) * nmy if nmy > 1 else 1)
     lg = math.log2(N)
     if int(p.get("pspi", 1)):
         R = int(p["nref"])
@@ -87,6 +89,19 @@ def flops_per_unit(p: dict) -> float:
     else:
         F = 2 * 5 * N * lg + 6 * N + 14 * n
     return 2 * F + 3 * n
+
+
+def bytes_per_unit_3d(p: dict) -> float:
+    """Device-memory bytes of one 3-D (shot, frequency, depth step) in the three-pass
+    design (the padded x-y plane does not fit in shared memory): with n = nmx*nmy,
+    M = nmx*nky rows kept after the y transform and R references, both wavefields:
+    pass A reads U (2n) and writes Y (2M); pass B reads Y (2M) and writes C (2RM);
+    pass C reads C (2RM) and writes U (2n); 8 bytes per complex sample."""
+    nmy = int(p["nmy"])
+    n = int(p["nmx"]) * nmy
+    M = int(p["nmx"]) * int(p["padx"]) * nmy
+    R = int(p["nref"]) if int(p.get("pspi", 1)) else 1
+    return 8.0 * (4 * n + 4 * M + 4 * R * M)
 
 
 class ClockSampler:
@@ -320,6 +335,7 @@ def main():
     if dist:
         dist.barrier()
     clocks = sampler.stop()
+    launch = ctx.last_launch() if int(p.get("nmy", 1)) == 1 else None
     elapsed = ev0.elapsed_time(ev1) / 1000.0
     t = torch.tensor([elapsed], dtype=torch.float64, device=dev)
     if dist:
@@ -356,6 +372,22 @@ def main():
     if tr and tr.get("workload") == args.workload:
         traffic = tr.get("bytes_per_launch")
 
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_source": f"bf16 dense, {src}",
+            "kernel": "wem_migrate_kernel", "ms_per_launch": mig_ms,
+            "flops_per_unit": fl, "fp32_nominal_tflops": fp32_nominal,
+            "fp32_frac": achieved / fp32_nominal}
+    if int(p.get("nmy", 1)) > 1:
+        # 3-D: three passes over device memory per depth step; their bytes bound it
+        bu = bytes_per_unit_3d(p)
+        hbm = float(peaks.get("hbm_gbs", 6800.0))
+        gbs = units * bu / (mig_ms / 1000.0) / 1e9
+        roof = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                "traffic": traffic, "peak_source": f"HBM copy, {src}",
+                "kernel": "wem3d_rows_fwd + wem3d_cols + wem3d_rows_inv (all depth steps)",
+                "ms_per_launch": mig_ms, "bytes_per_unit": bu, "flops_per_unit": fl,
+                "fp32_tflops": achieved, "fp32_nominal_tflops": fp32_nominal,
+                "fp32_frac": achieved / fp32_nominal}
     line = {
         "metric": "shot*omega*depth-steps/s", "value": value, "unit": "shot*omega*depth-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -364,15 +396,12 @@ def main():
         "config": {"workload": wl, "units_per_step_per_gpu": units, "shots": nshot, "frequencies": nf,
                    "depth_steps": nz, "pspi": int(p["pspi"]), "nref": int(p["nref"]), "nkx": int(p["padx"]) * int(p["nmx"]),
                    "interp": p.get("interp", "ref"), "l2": "inputs larger than L2 (traces, spectra, image accumulators)",
-                   "parallelism": f"replicas x{world}, shots sharded by rank"},
+                   "parallelism": f"replicas x{world}, shots sharded by rank",
+                   "depth_kernel_launch": launch},
         "e2e": {"value": world * units / e2e_s, "unit": "shot*omega*depth-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": kernels_per_step * args.steps,
-        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_source": f"bf16 dense, {src}",
-                     "kernel": "wem_migrate_kernel", "ms_per_launch": mig_ms,
-                     "flops_per_unit": fl, "fp32_nominal_tflops": fp32_nominal,
-                     "fp32_frac": achieved / fp32_nominal},
+        "roofline": roof,
         "kernel_ms": {"spectra": statistics.mean(k[0] for k in kms), "extrapolate": mig_ms,
                       "reduce": statistics.mean(k[2] for k in kms)},
         "clocks": clocks,

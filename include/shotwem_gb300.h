@@ -139,6 +139,13 @@ WEM_API int wem_last_timing(wem_ctx *ctx, float *ms, int *kernels);
    recursion, image reduction (CUDA events around each launch). */
 WEM_API int wem_last_kernel_times(wem_ctx *ctx, float *ms_spectra, float *ms_extrapolate, float *ms_reduce);
 
+/* How the last 2-D wem_migrate* call ran its depth recursion (no counterpart in the
+   reference): threads per CTA, shots sharing one CTA's phase tables, CTAs launched,
+   whether the call replayed a captured CUDA graph of the whole launch sequence (1) or
+   launched it (0), and whether it timed the CTA shapes on this geometry first (1). */
+WEM_API int wem_last_launch(wem_ctx *ctx, int *threads, int *shots_per_cta, int *grid, int *replayed,
+                            int *tuned);
+
 /* The cudaStream_t (as void*) on which ctx orders all its work. */
 WEM_API int wem_ctx_stream(wem_ctx *ctx, void **stream);
 

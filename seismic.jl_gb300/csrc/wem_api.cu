@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -45,6 +46,10 @@ struct DevBuf {
     size_t n = 0;
 };
 
+// bumped on every device (re)allocation: a captured launch sequence that was recorded
+// before the bump may hold a freed pointer and is re-captured
+static std::atomic<unsigned long long> g_alloc_gen{ 0 };
+
 static int ensure(DevBuf &b, size_t bytes)
 {
     if (bytes == 0) bytes = 16;
@@ -55,6 +60,7 @@ static int ensure(DevBuf &b, size_t bytes)
     cudaError_t e = cudaMalloc(&b.p, bytes);
     if (e != cudaSuccess) return fail(WEM_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
     b.n = bytes;
+    g_alloc_gen++;
     return WEM_OK;
 }
 
@@ -87,6 +93,26 @@ struct wem_ctx {
     std::vector<int64_t> h_tbase;
     std::vector<int> h_igx;
     int last_nshot = -1;
+    unsigned long long prep_gen = 0;  // bumped by every wem_prepare
+
+    // the launch sequence of the last 2-D migration, captured as a CUDA graph and
+    // replayed while nothing it depends on has changed
+    bool use_graph = true;
+    cudaGraphExec_t gexec = nullptr;
+    struct GraphKey {
+        int nshot, wide, grid;
+        int64_t ntr;
+        const float *d;
+        float *m;
+        unsigned long long alloc_gen, prep_gen;
+        bool operator==(const GraphKey &o) const
+        {
+            return nshot == o.nshot && wide == o.wide && grid == o.grid && ntr == o.ntr && d == o.d && m == o.m &&
+                   alloc_gen == o.alloc_gen && prep_gen == o.prep_gen;
+        }
+    } gkey{};
+    // what the last migration launched
+    int last_threads = 0, last_S = 0, last_grid = 0, last_replayed = 0, last_tuned = 0;
 };
 
 namespace gbwem {
@@ -115,6 +141,8 @@ extern "C" int wem_ctx_create(wem_ctx **out, int device)
     for (int i = 0; i < 4; i++) CK(cudaEventCreate(&c->evk[i]));
     CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
     CK(cudaDeviceGetAttribute(&c->max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    const char *g = getenv("WEM_GRAPH");
+    c->use_graph = !(g && !strcmp(g, "0"));
     *out = c;
     return WEM_OK;
 }
@@ -131,6 +159,7 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
                        &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (int i = 0; i < 4; i++)
@@ -154,6 +183,17 @@ extern "C" int wem_last_kernel_times(wem_ctx *c, float *ms_spectra, float *ms_ex
     if (ms_spectra) *ms_spectra = c->last_kms[0];
     if (ms_extrapolate) *ms_extrapolate = c->last_kms[1];
     if (ms_reduce) *ms_reduce = c->last_kms[2];
+    return WEM_OK;
+}
+
+extern "C" int wem_last_launch(wem_ctx *c, int *threads, int *shots_per_cta, int *grid, int *replayed, int *tuned)
+{
+    if (!c) return fail(WEM_ERR_ARG, "null context");
+    if (threads) *threads = c->last_threads;
+    if (shots_per_cta) *shots_per_cta = c->last_S;
+    if (grid) *grid = c->last_grid;
+    if (replayed) *replayed = c->last_replayed;
+    if (tuned) *tuned = c->last_tuned;
     return WEM_OK;
 }
 
@@ -378,6 +418,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     c->dkx = 2 * 3.141592653589793 / ((float)nkx) / p.dmx;
     c->dky = 2 * 3.141592653589793 / ((float)nky) / p.dmy;
     c->prepared = true;
+    c->prep_gen++;
     c->last_nshot = -1;
     return WEM_OK;
 }
@@ -423,15 +464,118 @@ static int set_shots(wem_ctx *c, int nshot, const float *sx, const float *sy, co
     return WEM_OK;
 }
 
-static int cta_shape(wem_ctx *c, int pspi, int nmx, int nref)
+// ---------------------------------------------------------------- CTA shape autotuner
+// The depth-recursion kernel comes in two shapes: "wide" (512 threads; S shots of an item
+// share one set of per-depth phase tables) and "narrow" (256 threads; S = 1, more CTAs per
+// SM where the shared memory allows). Which one is faster depends on nkx, nref, nmx and the
+// device, so the first migration of a geometry times both on a slice of its own work (one
+// wave of items over the first 48 depth steps, after a warm-up launch) and the process
+// keeps the faster one for that geometry. WEM_CTA_SHAPE=wide|narrow forces a shape;
+// WEM_AUTOTUNE=0 takes the wide shape whenever its shared memory fits.
+struct TuneEntry {
+    int device, nkx, pspi, interp, nmx, nref, wide;
+};
+static std::mutex g_tune_mu;
+static std::vector<TuneEntry> g_tune;
+
+static MigArgs mig_args(wem_ctx *c, int nshot, int ngroups)
 {
+    const wem_params &p = c->p;
+    MigArgs a{};
+    a.nmx = p.nmx;
+    a.nz = p.nz;
+    a.nref = p.pspi ? p.nref : 1;
+    a.nwf = c->nwf;
+    a.ifmin = c->ifmin;
+    a.nshot = nshot;
+    a.ngroups = ngroups;
+    a.dw = c->dw;
+    a.dz = p.dz;
+    a.dkx = c->dkx;
+    a.inv_n = 1.0f / (float)c->nkx;
+    a.recv = P<float2>(c->recv);
+    a.srcw = P<float2>(c->srcw);
+    a.igx = P<int>(c->igx);
+    a.vref = P<float>(c->vref);
+    a.slow2 = P<float>(c->slow2);
+    a.po = P<float>(c->po);
+    a.pd = P<float>(c->pd);
+    a.selb = P<uint8_t>(c->sel);
+    a.wlin = P<float>(c->wlin);
+    a.taper = P<float>(c->taper);
+    a.zflag = P<uint8_t>(c->zflag);
+    a.twid = P<float2>(c->twid);
+    a.slots = P<float2>(c->slots);
+    return a;
+}
+
+// shots*frequencies per ms of one shape on a slice of the survey; 0 when the shape
+// does not fit. c->recv must hold nshot*nwf rows (contents do not matter for timing).
+static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
+{
+    const wem_params &p = c->p;
+    *rate = 0.0;
+    int S, threads, bps = 0;
+    size_t smem;
+    if (migrate_config(c->nkx, wide, p.pspi, p.nmx, p.nref, &S, &threads, &smem) || (int)smem > c->max_smem)
+        return WEM_OK;
+    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, p.nmx, p.nref, &bps) || bps < 1) {
+        cudaGetLastError();
+        return WEM_OK;
+    }
+    const int cap = c->nsm * bps;
+    const int ngroups = (nshot + S - 1) / S;
+    const int ngroups_t = std::min(ngroups, cap);
+    const int nwf_t = std::max(1, std::min(c->nwf, cap / ngroups_t));
+    const int items = ngroups_t * nwf_t;  // <= cap: one wave
+    int rc;
+    MigArgs a = mig_args(c, nshot, ngroups_t);
+    a.nwf = nwf_t;  // frequency rows iwi < nwf_t <= nwf stay inside recv
+    a.nz = std::min(p.nz, 48);
+    if ((rc = ensure(c->slots, sizeof(float2) * (size_t)items * a.nz * p.nmx))) return rc;
+    a.slots = P<float2>(c->slots);
+    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st))
+        return fail(WEM_ERR_CUDA, "migrate launch (tuning): %s", cudaGetErrorString(cudaGetLastError()));
+    CK(cudaEventRecord(c->ev0, c->st));
+    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st))
+        return fail(WEM_ERR_CUDA, "migrate launch (tuning): %s", cudaGetErrorString(cudaGetLastError()));
+    CK(cudaEventRecord(c->ev1, c->st));
+    CK(cudaEventSynchronize(c->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    const int shots = std::min(nshot, ngroups_t * S);
+    *rate = ms > 0.f ? (double)shots * nwf_t / ms : 0.0;
+    return WEM_OK;
+}
+
+static int choose_shape(wem_ctx *c, int nshot, int *wide)
+{
+    const wem_params &p = c->p;
     const char *e = getenv("WEM_CTA_SHAPE");
-    if (e && !strcmp(e, "narrow")) return 0;
     int S, th;
     size_t smem;
-    if (migrate_config(c->nkx, 1, pspi, nmx, nref, &S, &th, &smem)) return 0;
-    if (e && !strcmp(e, "wide")) return 1;
-    return (int)smem <= c->max_smem ? 1 : 0;
+    const bool wide_fits = !migrate_config(c->nkx, 1, p.pspi, p.nmx, p.nref, &S, &th, &smem) && (int)smem <= c->max_smem;
+    c->last_tuned = 0;
+    if (e && !strcmp(e, "narrow")) return *wide = 0, WEM_OK;
+    if (e && !strcmp(e, "wide")) return *wide = wide_fits ? 1 : 0, WEM_OK;
+    const char *t = getenv("WEM_AUTOTUNE");
+    if (!wide_fits || (t && !strcmp(t, "0")) || c->nwf < 1) return *wide = wide_fits ? 1 : 0, WEM_OK;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        for (const TuneEntry &te : g_tune)
+            if (te.device == c->device && te.nkx == c->nkx && te.pspi == p.pspi && te.interp == p.interp &&
+                te.nmx == p.nmx && te.nref == p.nref)
+                return *wide = te.wide, WEM_OK;
+    }
+    int rc;
+    if ((rc = ensure(c->recv, sizeof(float2) * (size_t)nshot * std::max(c->nwf, 1) * p.nmx))) return rc;
+    double rw = 0.0, rn = 0.0;
+    if ((rc = trial_rate(c, nshot, 1, &rw)) || (rc = trial_rate(c, nshot, 0, &rn))) return rc;
+    *wide = rw >= rn ? 1 : 0;
+    c->last_tuned = 1;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.push_back({ c->device, c->nkx, p.pspi, p.interp, p.nmx, p.nref, *wide });
+    return WEM_OK;
 }
 
 // 3-D migration: spectra -> per depth step the three plane passes of wem_3d.cu for
@@ -512,40 +656,26 @@ static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev,
     return WEM_OK;
 }
 
-// GPU part of a migration: spectra -> depth recursion -> image. Stream-ordered on c->st.
-static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, float *m_dev)
+// record an event on c->st; inside a stream capture as a graph node (so that the
+// per-kernel times stay readable after every replay)
+static cudaError_t rec(cudaEvent_t ev, cudaStream_t st, bool capture)
+{
+    return capture ? cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal) : cudaEventRecord(ev, st);
+}
+
+// the launch sequence of a 2-D migration: zero the spectra and accumulators -> trace
+// spectra -> depth recursion -> image reduction, with events between the kernels
+static int enqueue_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, float *m_dev, int wide, int grid,
+                           int ngroups, size_t recv_elems, bool capture)
 {
     const wem_params &p = c->p;
-    if (p.nmy > 1) return run_migrate3d(c, nshot, ntr, d_dev, m_dev);
     cudaStream_t st = c->st;
     const int nmx = p.nmx, nz = p.nz;
-    int S, threads, bps = 0;
-    size_t smem;
-    // the 512-thread shape shares one set of phase tables among more rows; use it when
-    // its shared memory fits (WEM_CTA_SHAPE=narrow|wide overrides, for tuning)
-    const int wide = cta_shape(c, p.pspi, nmx, p.nref);
-    if (migrate_config(c->nkx, wide, p.pspi, nmx, p.nref, &S, &threads, &smem))
-        return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
-    if ((int)smem > c->max_smem)
-        return fail(WEM_ERR_SIZE, "nref=%d needs %zu B of shared memory per CTA (device limit %d B)", p.nref, smem,
-                    c->max_smem);
-    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, nmx, p.nref, &bps) || bps < 1)
-        return fail(WEM_ERR_CUDA, "kernel does not fit on the device (smem %zu B, %d threads): %s", smem, threads,
-                    cudaGetErrorString(cudaGetLastError()));
-    const int ngroups = (nshot + S - 1) / S;
-    const long long nitems = (long long)ngroups * c->nwf;
-    int grid = (int)((long long)c->nsm * bps < nitems ? (long long)c->nsm * bps : nitems);
-    if (grid < 1) grid = 1;
-    int rc;
-    const size_t recv_elems = (size_t)nshot * (c->nwf > 0 ? c->nwf : 1) * nmx;
-    if ((rc = ensure(c->recv, sizeof(float2) * recv_elems)) ||
-        (rc = ensure(c->slots, sizeof(float2) * (size_t)grid * nz * nmx)))
-        return rc;
     int kernels = 0;
-    CK(cudaEventRecord(c->ev0, st));
+    CK(rec(c->ev0, st, capture));
     CK(cudaMemsetAsync(c->recv.p, 0, sizeof(float2) * recv_elems, st));
     CK(cudaMemsetAsync(c->slots.p, 0, sizeof(float2) * (size_t)grid * nz * nmx, st));
-    CK(cudaEventRecord(c->evk[0], st));
+    CK(rec(c->evk[0], st, capture));
     if (c->nwf > 0 && ntr > 0) {
         SpectraArgs sa{};
         sa.d = d_dev;
@@ -562,43 +692,89 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
         if (launch_spectra(sa, st)) return fail(WEM_ERR_CUDA, "spectra launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;
     }
-    CK(cudaEventRecord(c->evk[1], st));
+    CK(rec(c->evk[1], st, capture));
     if (c->nwf > 0) {
-        MigArgs a{};
-        a.nmx = nmx;
-        a.nz = nz;
-        a.nref = p.pspi ? p.nref : 1;
-        a.nwf = c->nwf;
-        a.ifmin = c->ifmin;
-        a.nshot = nshot;
-        a.ngroups = ngroups;
-        a.dw = c->dw;
-        a.dz = p.dz;
-        a.dkx = c->dkx;
-        a.inv_n = 1.0f / (float)c->nkx;
-        a.recv = P<float2>(c->recv);
-        a.srcw = P<float2>(c->srcw);
-        a.igx = P<int>(c->igx);
-        a.vref = P<float>(c->vref); a.slow2 = P<float>(c->slow2);
-        a.po = P<float>(c->po);
-        a.pd = P<float>(c->pd);
-        a.selb = P<uint8_t>(c->sel);
-        a.wlin = P<float>(c->wlin);
-        a.taper = P<float>(c->taper);
-        a.zflag = P<uint8_t>(c->zflag);
-        a.twid = P<float2>(c->twid);
-        a.slots = P<float2>(c->slots);
+        MigArgs a = mig_args(c, nshot, ngroups);
         if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, grid, st))
             return fail(WEM_ERR_CUDA, "migrate launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;
     }
-    CK(cudaEventRecord(c->evk[2], st));
+    CK(rec(c->evk[2], st, capture));
     if (launch_image_reduce(P<float2>(c->slots), grid, nz, nmx, m_dev, st))
         return fail(WEM_ERR_CUDA, "reduce launch: %s", cudaGetErrorString(cudaGetLastError()));
     kernels++;
-    CK(cudaEventRecord(c->evk[3], st));
-    CK(cudaEventRecord(c->ev1, st));
+    CK(rec(c->evk[3], st, capture));
+    CK(rec(c->ev1, st, capture));
     c->last_kernels = kernels;
+    return WEM_OK;
+}
+
+// GPU part of a migration: spectra -> depth recursion -> image. Stream-ordered on c->st.
+// The whole sequence is captured once as a CUDA graph and replayed by later calls with
+// the same shots, buffers and tables (WEM_GRAPH=0 launches it directly every time).
+static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, float *m_dev)
+{
+    const wem_params &p = c->p;
+    if (p.nmy > 1) return run_migrate3d(c, nshot, ntr, d_dev, m_dev);
+    cudaStream_t st = c->st;
+    const int nmx = p.nmx, nz = p.nz;
+    int S, threads, bps = 0, wide = 0;
+    size_t smem;
+    int rc;
+    if ((rc = choose_shape(c, nshot, &wide))) return rc;
+    if (migrate_config(c->nkx, wide, p.pspi, nmx, p.nref, &S, &threads, &smem))
+        return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
+    if ((int)smem > c->max_smem)
+        return fail(WEM_ERR_SIZE, "nref=%d needs %zu B of shared memory per CTA (device limit %d B)", p.nref, smem,
+                    c->max_smem);
+    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, nmx, p.nref, &bps) || bps < 1)
+        return fail(WEM_ERR_CUDA, "kernel does not fit on the device (smem %zu B, %d threads): %s", smem, threads,
+                    cudaGetErrorString(cudaGetLastError()));
+    const int ngroups = (nshot + S - 1) / S;
+    const long long nitems = (long long)ngroups * c->nwf;
+    int grid = (int)((long long)c->nsm * bps < nitems ? (long long)c->nsm * bps : nitems);
+    if (grid < 1) grid = 1;
+    const size_t recv_elems = (size_t)nshot * (c->nwf > 0 ? c->nwf : 1) * nmx;
+    if ((rc = ensure(c->recv, sizeof(float2) * recv_elems)) ||
+        (rc = ensure(c->slots, sizeof(float2) * (size_t)grid * nz * nmx)))
+        return rc;
+    c->last_threads = threads;
+    c->last_S = S;
+    c->last_grid = grid;
+    c->last_replayed = 0;
+    if (!c->use_graph) return enqueue_migrate(c, nshot, ntr, d_dev, m_dev, wide, grid, ngroups, recv_elems, false);
+
+    const wem_ctx::GraphKey key{ nshot, wide, grid, ntr, d_dev, m_dev, g_alloc_gen.load(), c->prep_gen };
+    if (c->gexec && key == c->gkey) {
+        CK(cudaGraphLaunch(c->gexec, st));
+        c->last_replayed = 1;
+        return WEM_OK;
+    }
+    if (c->gexec) {
+        cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+    }
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue_migrate(c, nshot, ntr, d_dev, m_dev, wide, grid, ngroups, recv_elems, true);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(st, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc;
+    }
+    cudaGraphExec_t ex = nullptr;
+    if (ee != cudaSuccess || !g || cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) {
+        // this driver cannot capture the sequence: launch directly from now on
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        c->use_graph = false;
+        return enqueue_migrate(c, nshot, ntr, d_dev, m_dev, wide, grid, ngroups, recv_elems, false);
+    }
+    cudaGraphDestroy(g);
+    c->gexec = ex;
+    c->gkey = key;
+    CK(cudaGraphLaunch(ex, st));
     return WEM_OK;
 }
 

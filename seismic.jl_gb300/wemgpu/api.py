@@ -158,6 +158,13 @@ class Context:
         L.check(L.lib().wem_last_kernel_times(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
 
+    def last_launch(self) -> dict:
+        """How the last 2-D migration ran: threads per CTA, shots per CTA, grid, whether
+        it replayed the captured CUDA graph and whether it timed the CTA shapes first."""
+        v = [C.c_int() for _ in range(5)]
+        L.check(L.lib().wem_last_launch(self._h, *[C.byref(x) for x in v]))
+        return dict(zip(["threads", "shots_per_cta", "grid", "graph_replayed", "tuned"], [x.value for x in v]))
+
     def stream(self) -> int:
         """cudaStream_t of this context, as an integer handle."""
         s = C.c_void_p()

@@ -72,6 +72,64 @@ def test_deterministic(gpu_lib):
     assert np.array_equal(a, b)
 
 
+def test_graph_replay_matches_direct_launch(gpu_lib, monkeypatch):
+    """A second call with the same shots replays the captured CUDA graph of the whole
+    launch sequence. Its image equals the directly launched one bit for bit, and new data
+    in the same buffers is migrated afresh: data x2 gives exactly image x2 (scaling by a
+    power of two commutes with every FP32 rounding)."""
+    from wemgpu import synth
+    from wemgpu.api import Shots
+    c = synth.small_case(43, nx=128, nz=16, nt=96, nshot=4, pspi=1, nref=4)
+    s = c["shots"]
+    s2 = Shots(s.sx, s.sy, s.trace_offset, s.trace_cell, s.data * np.float32(2))
+    with gpu_lib.Context() as ctx:
+        ctx.prepare(c["params"], c["vel"], c["wav"])
+        a = ctx.migrate(s)
+        la = ctx.last_launch()
+        b = ctx.migrate(s)
+        lb = ctx.last_launch()
+        d2 = ctx.migrate(s2)
+        lc = ctx.last_launch()
+    monkeypatch.setenv("WEM_GRAPH", "0")
+    with gpu_lib.Context() as ctx:
+        ctx.prepare(c["params"], c["vel"], c["wav"])
+        direct = ctx.migrate(s)
+        ld = ctx.last_launch()
+    assert (la["graph_replayed"], lb["graph_replayed"], lc["graph_replayed"], ld["graph_replayed"]) == (0, 1, 1, 0)
+    assert la["threads"] == ld["threads"] and la["grid"] == ld["grid"]
+    assert np.array_equal(a, b) and np.array_equal(a, direct)
+    assert np.array_equal(d2, a * np.float32(2))
+
+
+def test_autotuned_cta_shape(gpu_lib, oracle_mod, monkeypatch):
+    """The first migration of a geometry times both CTA shapes and keeps the faster one
+    for the process; both shapes, forced, match the oracle."""
+    from wemgpu import synth
+    monkeypatch.delenv("WEM_CTA_SHAPE", raising=False)
+    monkeypatch.delenv("WEM_AUTOTUNE", raising=False)
+    c = synth.small_case(45, nx=256, nz=12, nt=96, nshot=3, pspi=1, nref=7)  # nref=7: a geometry no other test uses
+    want = _port_stack(oracle_mod, c["params"], c["vel"], c["wav"], c["shots"])
+    with gpu_lib.Context() as ctx:
+        ctx.prepare(c["params"], c["vel"], c["wav"])
+        m1 = ctx.migrate(c["shots"])
+        l1 = ctx.last_launch()
+    with gpu_lib.Context() as ctx:
+        ctx.prepare(c["params"], c["vel"], c["wav"])
+        ctx.migrate(c["shots"])
+        l2 = ctx.last_launch()
+    assert l1["tuned"] == 1 and l2["tuned"] == 0 and l1["threads"] == l2["threads"]
+    assert rel_l2(m1, want) < TOL
+    threads = set()
+    for shape in ("wide", "narrow"):
+        monkeypatch.setenv("WEM_CTA_SHAPE", shape)
+        with gpu_lib.Context() as ctx:
+            ctx.prepare(c["params"], c["vel"], c["wav"])
+            m = ctx.migrate(c["shots"])
+            threads.add(ctx.last_launch()["threads"])
+        assert rel_l2(m, want) < TOL
+    assert len(threads) == 2 and l1["threads"] in threads
+
+
 def test_config0_full_size_matches_reference_port(gpu_lib, oracle_mod):
     """The split-step workload at full size (1 shot, 200 x 256, 221 frequencies)."""
     from wemgpu import synth
