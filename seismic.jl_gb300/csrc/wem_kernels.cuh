@@ -27,7 +27,7 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
     const bool is_src = team < S;
     const int sg = is_src ? team : team - S;               // shot within the group
     float2 *xbuf = sm.x + (size_t)team * PADN;
-    float2 *sacc = sm.acc + (size_t)team * N;
+    float2 *sacc = sm.acc + (size_t)team * sm.acc_stride;
     const unsigned sync = team_sync_handle<N>(tid);
 
     for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(S * (N / 16), 1) wem_model_kernel(const MigArg
     const int tid = threadIdx.x;
     const int team = tid / T, t = tid - team * T;
     float2 *xbuf = sm.x + (size_t)team * PADN;
-    float2 *sacc = sm.acc + (size_t)team * N;
+    float2 *sacc = sm.acc + (size_t)team * sm.acc_stride;
     const unsigned sync = team_sync_handle<N>(tid);
     for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
 

@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(2 * S * (N / 16)) wem_migrate_atomic_kernel(co
     const bool is_src = team < S;
     const int sg = is_src ? team : team - S;
     float2 *xbuf = sm.x + (size_t)team * PADN;
-    float2 *sacc = sm.acc + (size_t)team * N;
+    float2 *sacc = sm.acc + (size_t)team * sm.acc_stride;
     const unsigned sync = team_sync_handle<N>(tid);
     for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
     const int nitems = a.ngroups * a.nwf;

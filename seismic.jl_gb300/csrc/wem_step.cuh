@@ -56,10 +56,18 @@ template <int N> struct MigShape {
 // exchange buffer per team; PSPI CTAs also hold one N-sample selection accumulator per
 // team (each thread owning its 16 positions), the depth's selection bytes and
 // interpolation weights.
+// entries of a team's PSPI selection accumulator: thread t owns entries m*T + t for the
+// live positions x = t + T*m < nmx only (the padding is never selected)
+template <int N> __host__ __device__ constexpr int sel_entries(int nmx)
+{
+    return (nmx + N / 16 - 1) / (N / 16) * (N / 16);
+}
+
 template <int N, bool PSPI> struct Smem {
     float2 *tw, *ph, *corr, *x, *acc;
     uint8_t *selb;
     float *wl;
+    int acc_stride;  // float2 per team in acc
     __device__ Smem(float4 *raw, int nref, int nmx, int teams)
     {
         using SH = MigShape<N>;
@@ -68,7 +76,8 @@ template <int N, bool PSPI> struct Smem {
         corr = ph + (size_t)(PSPI ? nref : 1) * SH::HALF;
         x = corr + (PSPI ? 0 : ((nmx + 1) & ~1));
         acc = x + (size_t)teams * SH::PADN;
-        wl = reinterpret_cast<float *>(acc + (PSPI ? (size_t)teams * N : 0));
+        acc_stride = PSPI ? sel_entries<N>(nmx) : 0;
+        wl = reinterpret_cast<float *>(acc + (size_t)teams * acc_stride);
         selb = reinterpret_cast<uint8_t *>(wl + (PSPI ? ((nmx + 3) & ~3) : 0));
     }
 };
@@ -79,7 +88,7 @@ __host__ __device__ constexpr size_t mig_smem_bytes(bool pspi, int nref, int nmx
 {
     using SH = MigShape<N>;
     return sizeof(float2) * ((size_t)SH::TWP + (size_t)(pspi ? nref : 1) * SH::HALF + (size_t)(pspi ? 0 : ((nmx + 1) & ~1)) +
-                             (size_t)teams * SH::PADN + (pspi ? (size_t)teams * N : 0)) +
+                             (size_t)teams * SH::PADN + (pspi ? (size_t)teams * sel_entries<N>(nmx) : 0)) +
            (pspi ? sizeof(float) * (size_t)((nmx + 3) & ~3) + (size_t)((nmx + 15) & ~15) : 0);
 }
 
