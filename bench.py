@@ -91,6 +91,48 @@ def flops_per_unit(p: dict) -> float:
     return 2 * F + 3 * n
 
 
+def tensor_flops_per_unit(p: dict) -> float:
+    """Tensor-core FLOPs one (shot, frequency, depth step) executes in split16 mode: every
+    radix-16 pass of a 2048-sample row is M=128 x N=32 x K=32 per product and the radix-8
+    pass two M=128 x N=16 x K=16 products, with 3 products (hi*hi, lo*hi, hi*lo) each;
+    (1 + R) transforms per wavefield (PSPI) or 2 (split-step), 2 wavefields."""
+    per_fft = 3 * (2 * (2 * 128 * 32 * 32) + 2 * (2 * 128 * 16 * 16))
+    nfft = 1 + int(p["nref"]) if int(p.get("pspi", 1)) else 2
+    return 2.0 * nfft * per_fft
+
+
+def accuracy(c: dict, ctx_factory) -> dict:
+    """Relative L2 image error of one shot of the survey (the middle one, a 10 Hz band from
+    fmin, every depth step) against the oracle's FP64 operator, for the precision of the
+    run and for FP32 beside it."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from wemgpu import synth
+    from wemgpu.api import Shots
+    O.build()
+    p = dict(c["params"])
+    p["fmax"] = float(p["fmin"]) + 10.0
+    shots = c["shots"]
+    s = shots.nshot // 2
+    lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
+    one = Shots(shots.sx[s:s + 1], shots.sy[s:s + 1], np.array([0, hi - lo], np.int64),
+                shots.trace_cell[lo:hi], shots.data[lo:hi])
+    q = {k: v for k, v in p.items() if k != "precision"}
+    d = synth.shot_gather_full(shots, s, int(p["nmx"]) * int(p.get("nmy", 1)))
+    want = O.wem_fp64(dict(q, sx=float(shots.sx[s])), c["vel"], c["wav"], d=d, adj=True,
+                      nthreads=os.cpu_count() or 1).astype(np.float64)
+    out = {"sample": f"shot {s}, {band(p)} frequencies ({p['fmin']:g}-{p['fmax']:g} Hz) x {p['nz']} depth steps",
+           "oracle": "FP64 restatement of wem.c"}
+    for prec in sorted({"fp32", p.get("precision", "fp32")}):
+        ctx = ctx_factory()
+        try:
+            m = ctx.prepare(dict(q, precision=prec), c["vel"], c["wav"]).migrate(one)
+        finally:
+            ctx.close()
+        out[f"rel_l2_{prec}"] = float(np.linalg.norm(m - want) / np.linalg.norm(want))
+    return out
+
+
 def bytes_per_unit_3d(p: dict) -> float:
     """Device-memory bytes of one 3-D (shot, frequency, depth step) in the three-pass
     design (the padded x-y plane does not fit in shared memory): with n = nmx*nmy,
@@ -283,6 +325,9 @@ def main():
     ap.add_argument("--workload", default="survey64", choices=["survey64", "survey8", "survey3d", "split1", "lsm32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "split16"],
+                    help="split16: the FFTs' DFT stages on the tensor cores (split fp16 operands)")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the image-error check against the FP64 oracle")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -304,6 +349,9 @@ def main():
     if not os.path.exists(wemgpu.LIB_PATH):
         raise SystemExit("shotwem.so is not built: python -c 'import __graft_entry__ as g; g.build()'")
     c, wl = survey(args.workload, rank)
+    if args.precision != "fp32":
+        c["params"] = dict(c["params"], precision=args.precision)
+        wl += f" [{args.precision}: DFT stages on the tensor cores, split fp16 hi+lo operands, fp32 accumulation]"
     p, shots = c["params"], c["shots"]
     nf, nz, nshot = band(p), int(p["nz"]), shots.nshot
     units = nshot * nf * nz
@@ -377,6 +425,14 @@ def main():
             "kernel": "wem_migrate_kernel", "ms_per_launch": mig_ms,
             "flops_per_unit": fl, "fp32_nominal_tflops": fp32_nominal,
             "fp32_frac": achieved / fp32_nominal}
+    if p.get("precision", "fp32") == "split16":
+        tf = tensor_flops_per_unit(p)
+        tach = units * tf / (mig_ms / 1000.0) / 1e12
+        roof = {"bound": "tensor", "achieved": tach, "peak": peak, "unit": "TFLOP/s", "frac": tach / peak,
+                "traffic": traffic, "peak_source": f"bf16 dense, {src}",
+                "kernel": "wem_migrate_kernel (split16: DFT stages on tcgen05)", "ms_per_launch": mig_ms,
+                "tensor_flops_per_unit": tf, "flops_per_unit": fl, "algorithmic_tflops": achieved,
+                "fp32_nominal_tflops": fp32_nominal, "fp32_frac": achieved / fp32_nominal}
     if int(p.get("nmy", 1)) > 1:
         # 3-D: three passes over device memory per depth step; their bytes bound it
         bu = bytes_per_unit_3d(p)
@@ -392,7 +448,8 @@ def main():
         "metric": "shot*omega*depth-steps/s", "value": value, "unit": "shot*omega*depth-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "vs_baseline": None, "dtype": "f32" if p.get("precision", "fp32") == "fp32" else "f16x2-split/f32",
+        "data": "synthetic (seeded)",
         "config": {"workload": wl, "units_per_step_per_gpu": units, "shots": nshot, "frequencies": nf,
                    "depth_steps": nz, "pspi": int(p["pspi"]), "nref": int(p["nref"]), "nkx": int(p["padx"]) * int(p["nmx"]),
                    "interp": p.get("interp", "ref"), "l2": "inputs larger than L2 (traces, spectra, image accumulators)",
@@ -407,7 +464,11 @@ def main():
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # the CPU leg: the reference's algorithm timed on the host cores, and the FP64
+        # oracle as the checker of the image error
         line["cpu_baseline"] = cpu_baseline(c)
+        if not args.no_accuracy and int(p.get("nmy", 1)) == 1:
+            line["accuracy"] = accuracy(c, lambda: wemgpu.Context(local))
     if rank == 0:
         print(json.dumps(line))
     ctx.close()

@@ -52,6 +52,11 @@ extern "C" {
 
 /* arithmetic of the depth-extrapolation FFTs */
 #define WEM_PREC_FP32 0      /* complex FP32 */
+#define WEM_PREC_SPLIT16 1   /* no counterpart in the reference: the DFT stages of the migration's
+                                FFTs on the tensor cores with split fp16 (hi + lo) operands and
+                                FP32 accumulation; 2-D rows of padx*nmx = 2048 only (other
+                                geometries return WEM_ERR_SIZE). Modelling (wem_model*) computes
+                                in FP32 in this mode. */
 
 typedef struct wem_ctx wem_ctx;
 

@@ -85,6 +85,7 @@ struct wem_ctx {
     DevBuf vref, slow2, po, pd, sel, wlin, taper, zflag, twid, wtab, scale_recv, scale_src, srcw, wav, wav_base;
     DevBuf ssyn_ref, ssyn_exact;  // synthesis weights w^2 * (half-spectrum | image) factor
     DevBuf tapery, twy;           // 3-D: y taper and y-FFT twiddles
+    DevBuf tcw, tcerr;            // split16: W operands of the tensor-core DFT stages, timeout word
     DevBuf m3_items, m3_U, m3_Y, m3_C, m3_parts;
     // per-call buffers
     DevBuf recv, slots, image, data, tbase, igx, smig, mimg;
@@ -156,7 +157,7 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
                        &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
                        &c->ssyn_ref, &c->ssyn_exact, &c->recv, &c->slots, &c->image, &c->data,
                        &c->tbase, &c->igx, &c->smig, &c->mimg, &c->tapery, &c->twy, &c->m3_items,
-                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts };
+                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -204,9 +205,15 @@ extern "C" int wem_ctx_stream(wem_ctx *c, void **stream)
     return WEM_OK;
 }
 
-// read the per-kernel event times of the last (completed) call
+// read the per-kernel event times of the last (completed) call; in split16 mode also
+// the tensor-core timeout word of the depth kernel
 static int collect_times(wem_ctx *c)
 {
+    if (c->prepared && c->p.precision == WEM_PREC_SPLIT16 && c->p.nmy == 1 && c->tcerr.p) {
+        int e = 0;
+        CK(cudaMemcpy(&e, c->tcerr.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e) return fail(WEM_ERR_TIMEOUT, "a tensor-core wait of the depth kernel ran out (split16 mode)");
+    }
     CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
     for (int i = 0; i < 3; i++) CK(cudaEventElapsedTime(&c->last_kms[i], c->evk[i], c->evk[i + 1]));
     return WEM_OK;
@@ -245,9 +252,13 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         return fail(WEM_ERR_ARG, "PSPI needs 2 <= nref <= 64 (nref=%d; the reference divides by nref-1, wem.c:52)",
                     p.nref);
     if (p.interp != WEM_INTERP_REF && p.interp != WEM_INTERP_LINEAR) return fail(WEM_ERR_ARG, "unknown interp %d", p.interp);
-    if (p.precision != WEM_PREC_FP32) return fail(WEM_ERR_SIZE, "precision mode %d not built", p.precision);
     const int nkx = p.nmx > 1 ? p.padx * p.nmx : 1;
     const int nky = p.nmy > 1 ? p.padx * p.nmy : 1;
+    if (p.precision != WEM_PREC_FP32 && p.precision != WEM_PREC_SPLIT16)
+        return fail(WEM_ERR_ARG, "unknown precision mode %d", p.precision);
+    if (p.precision == WEM_PREC_SPLIT16 && (p.nmy != 1 || nkx != 2048))
+        return fail(WEM_ERR_SIZE, "split16 (tensor-core) migration is built for 2-D rows of nkx = padx*nmx = 2048 "
+                                  "(have nmy=%d, nkx=%d)", p.nmy, nkx);
     if (p.nmy == 1) {
         if (!is_pow2(nkx) || nkx < 32 || nkx > 4096)
             return fail(WEM_ERR_SIZE, "nkx = padx*nmx = %d must be a power of two in [32, 4096]", nkx);
@@ -365,9 +376,14 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         (rc = ensure(c->wav, sizeof(float) * p.nt)) || (rc = ensure(c->wav_base, sizeof(int64_t))) ||
         (rc = ensure(c->ssyn_ref, sizeof(float) * syn_ref.size())) ||
         (rc = ensure(c->ssyn_exact, sizeof(float) * syn_exact.size())) ||
-        (rc = ensure(c->tapery, sizeof(float) * tapery.size())) || (rc = ensure(c->twy, sizeof(float2) * twy.size())))
+        (rc = ensure(c->tapery, sizeof(float) * tapery.size())) || (rc = ensure(c->twy, sizeof(float2) * twy.size())) ||
+        (rc = ensure(c->tcw, 10240)) || (rc = ensure(c->tcerr, sizeof(int))))
         return rc;
     cudaStream_t st = c->st;
+    std::vector<uint16_t> tcw(5120);
+    tc_w_table_host(tcw.data());
+    CK(cudaMemcpyAsync(c->tcw.p, tcw.data(), 10240, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(c->tcerr.p, 0, sizeof(int), st));
     CK(cudaMemcpyAsync(c->po.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->pd.p, pd.data(), sizeof(float) * pd.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->vref.p, vref.data(), sizeof(float) * vref.size(), cudaMemcpyHostToDevice, st));
@@ -473,8 +489,10 @@ static int set_shots(wem_ctx *c, int nshot, const float *sx, const float *sy, co
 // keeps the faster one for that geometry. WEM_CTA_SHAPE=wide|narrow forces a shape;
 // WEM_AUTOTUNE=0 takes the wide shape whenever its shared memory fits.
 struct TuneEntry {
-    int device, nkx, pspi, interp, nmx, nref, wide;
+    int device, nkx, pspi, interp, nmx, nref, prec, wide;
 };
+
+static int tcmode(const wem_ctx *c) { return c->p.precision == WEM_PREC_SPLIT16 ? 1 : 0; }
 static std::mutex g_tune_mu;
 static std::vector<TuneEntry> g_tune;
 
@@ -506,6 +524,8 @@ static MigArgs mig_args(wem_ctx *c, int nshot, int ngroups)
     a.zflag = P<uint8_t>(c->zflag);
     a.twid = P<float2>(c->twid);
     a.slots = P<float2>(c->slots);
+    a.tcw = P<uint4>(c->tcw);
+    a.err = P<int>(c->tcerr);
     return a;
 }
 
@@ -517,9 +537,9 @@ static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
     *rate = 0.0;
     int S, threads, bps = 0;
     size_t smem;
-    if (migrate_config(c->nkx, wide, p.pspi, p.nmx, p.nref, &S, &threads, &smem) || (int)smem > c->max_smem)
+    if (migrate_config(c->nkx, wide, p.pspi, p.nmx, p.nref, &S, &threads, &smem, tcmode(c)) || (int)smem > c->max_smem)
         return WEM_OK;
-    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, p.nmx, p.nref, &bps) || bps < 1) {
+    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, p.nmx, p.nref, &bps, tcmode(c)) || bps < 1) {
         cudaGetLastError();
         return WEM_OK;
     }
@@ -534,10 +554,10 @@ static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
     a.nz = std::min(p.nz, 48);
     if ((rc = ensure(c->slots, sizeof(float2) * (size_t)items * a.nz * p.nmx))) return rc;
     a.slots = P<float2>(c->slots);
-    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st))
+    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st, tcmode(c)))
         return fail(WEM_ERR_CUDA, "migrate launch (tuning): %s", cudaGetErrorString(cudaGetLastError()));
     CK(cudaEventRecord(c->ev0, c->st));
-    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st))
+    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st, tcmode(c)))
         return fail(WEM_ERR_CUDA, "migrate launch (tuning): %s", cudaGetErrorString(cudaGetLastError()));
     CK(cudaEventRecord(c->ev1, c->st));
     CK(cudaEventSynchronize(c->ev1));
@@ -554,7 +574,7 @@ static int choose_shape(wem_ctx *c, int nshot, int *wide)
     const char *e = getenv("WEM_CTA_SHAPE");
     int S, th;
     size_t smem;
-    const bool wide_fits = !migrate_config(c->nkx, 1, p.pspi, p.nmx, p.nref, &S, &th, &smem) && (int)smem <= c->max_smem;
+    const bool wide_fits = !migrate_config(c->nkx, 1, p.pspi, p.nmx, p.nref, &S, &th, &smem, tcmode(c)) && (int)smem <= c->max_smem;
     c->last_tuned = 0;
     if (e && !strcmp(e, "narrow")) return *wide = 0, WEM_OK;
     if (e && !strcmp(e, "wide")) return *wide = wide_fits ? 1 : 0, WEM_OK;
@@ -564,7 +584,7 @@ static int choose_shape(wem_ctx *c, int nshot, int *wide)
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (const TuneEntry &te : g_tune)
             if (te.device == c->device && te.nkx == c->nkx && te.pspi == p.pspi && te.interp == p.interp &&
-                te.nmx == p.nmx && te.nref == p.nref)
+                te.nmx == p.nmx && te.nref == p.nref && te.prec == p.precision)
                 return *wide = te.wide, WEM_OK;
     }
     int rc;
@@ -574,7 +594,7 @@ static int choose_shape(wem_ctx *c, int nshot, int *wide)
     *wide = rw >= rn ? 1 : 0;
     c->last_tuned = 1;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune.push_back({ c->device, c->nkx, p.pspi, p.interp, p.nmx, p.nref, *wide });
+    g_tune.push_back({ c->device, c->nkx, p.pspi, p.interp, p.nmx, p.nref, p.precision, *wide });
     return WEM_OK;
 }
 
@@ -675,6 +695,7 @@ static int enqueue_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_de
     CK(rec(c->ev0, st, capture));
     CK(cudaMemsetAsync(c->recv.p, 0, sizeof(float2) * recv_elems, st));
     CK(cudaMemsetAsync(c->slots.p, 0, sizeof(float2) * (size_t)grid * nz * nmx, st));
+    if (tcmode(c)) CK(cudaMemsetAsync(c->tcerr.p, 0, sizeof(int), st));
     CK(rec(c->evk[0], st, capture));
     if (c->nwf > 0 && ntr > 0) {
         SpectraArgs sa{};
@@ -695,7 +716,7 @@ static int enqueue_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_de
     CK(rec(c->evk[1], st, capture));
     if (c->nwf > 0) {
         MigArgs a = mig_args(c, nshot, ngroups);
-        if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, grid, st))
+        if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, grid, st, tcmode(c)))
             return fail(WEM_ERR_CUDA, "migrate launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;
     }
@@ -722,12 +743,12 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
     size_t smem;
     int rc;
     if ((rc = choose_shape(c, nshot, &wide))) return rc;
-    if (migrate_config(c->nkx, wide, p.pspi, nmx, p.nref, &S, &threads, &smem))
+    if (migrate_config(c->nkx, wide, p.pspi, nmx, p.nref, &S, &threads, &smem, tcmode(c)))
         return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
     if ((int)smem > c->max_smem)
         return fail(WEM_ERR_SIZE, "nref=%d needs %zu B of shared memory per CTA (device limit %d B)", p.nref, smem,
                     c->max_smem);
-    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, nmx, p.nref, &bps) || bps < 1)
+    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, nmx, p.nref, &bps, tcmode(c)) || bps < 1)
         return fail(WEM_ERR_CUDA, "kernel does not fit on the device (smem %zu B, %d threads): %s", smem, threads,
                     cudaGetErrorString(cudaGetLastError()));
     const int ngroups = (nshot + S - 1) / S;

@@ -149,9 +149,16 @@ template <int T> __device__ __forceinline__ void team_sync(unsigned sync)
     else asm volatile("bar.sync %0, %1;" ::"r"(sync), "n"(T) : "memory");
 }
 
-// One Stockham pass P of the team's row (compile-time radix and span).
-template <int N, int DIR, int P>
-__device__ __forceinline__ void fft_pass(float2 (&v)[16], float2 *xbuf, const float2 *tw, int t, unsigned bar_id)
+// The tensor-core DFT stage (wem_tc.cuh): split16 mode, teams of one warpgroup.
+struct TcTeam;
+template <int R, int DIR, int T>
+__device__ __forceinline__ void tc_dft(float2 (&u)[16], TcTeam &tc, char *a_gen, int t, unsigned bar_id);
+
+// One Stockham pass P of the team's row (compile-time radix and span). TC: the DFTs of
+// the pass run on the tensor cores (tc describes the team's operands).
+template <int N, int DIR, int P, bool TC = false>
+__device__ __forceinline__ void fft_pass(float2 (&v)[16], float2 *xbuf, const float2 *tw, int t, unsigned bar_id,
+                                         TcTeam *tc = nullptr)
 {
     constexpr int E = 16;
     constexpr int T = N / E;
@@ -191,8 +198,12 @@ __device__ __forceinline__ void fft_pass(float2 (&v)[16], float2 *xbuf, const fl
             }
         }
     }
+    if constexpr (TC) {
+        tc_dft<R, DIR, T>(u, *tc, reinterpret_cast<char *>(xbuf), t, bar_id);
+    } else {
 #pragma unroll
-    for (int b = 0; b < B; b++) dft<R, DIR>(&u[b * R]);
+        for (int b = 0; b < B; b++) dft<R, DIR>(&u[b * R]);
+    }
     if constexpr (P == NP - 1) {
 #pragma unroll
         for (int b = 0; b < B; b++)
@@ -216,17 +227,18 @@ __device__ __forceinline__ void fft_pass(float2 (&v)[16], float2 *xbuf, const fl
             }
         }
         team_sync<T>(bar_id);  // writes visible before the next pass reads
-        fft_pass<N, DIR, P + 1>(v, xbuf, tw, t, bar_id);
+        fft_pass<N, DIR, P + 1, TC>(v, xbuf, tw, t, bar_id, tc);
     }
 }
 
 // One transform of the team's row, in registers. xbuf: the team's exchange buffer
 // of pad16(N) float2. tw: the concatenated per-pass twiddle table (forward sign).
 // DIR = -1 forward (e^{-i...}), +1 inverse; unnormalised.
-template <int N, int DIR>
-__device__ __forceinline__ void fft_row(float2 (&v)[16], float2 *xbuf, const float2 *tw, int t, unsigned bar_id)
+template <int N, int DIR, bool TC = false>
+__device__ __forceinline__ void fft_row(float2 (&v)[16], float2 *xbuf, const float2 *tw, int t, unsigned bar_id,
+                                        TcTeam *tc = nullptr)
 {
-    fft_pass<N, DIR, 0>(v, xbuf, tw, t, bar_id);
+    fft_pass<N, DIR, 0, TC>(v, xbuf, tw, t, bar_id, tc);
 }
 
 }  // namespace gbwem

@@ -40,6 +40,8 @@ struct MigArgs {
     const uint8_t *zflag;  // [nz]
     const float2 *twid;    // FFT twiddle table of the row length
     float2 *slots;         // [gridDim.x][nz][nmx] (sum, compensation) image accumulators
+    const uint4 *tcw;      // split16 mode: the W operands of the tensor-core DFT stages (10240 B)
+    int *err;              // split16 mode: set when a tensor-core wait ran out
 };
 
 struct SpectraArgs {
@@ -93,9 +95,13 @@ int m3d_launch_init(const Mig3dArgs &a, cudaStream_t st);
 
 // host-side launchers (wem_kernels.cu). `wide` selects the 512-thread CTA shape of
 // the migration kernel (2S rows sharing the phase tables) over the 256-thread one.
-int migrate_config(int nkx, int wide, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem);
-int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *blocks_per_sm);
-int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st);
+// tc = 1: the split16 (tensor-core) form of the depth kernel, built for nkx = 2048 only
+int migrate_config(int nkx, int wide, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem,
+                   int tc = 0);
+int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *blocks_per_sm, int tc = 0);
+int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st, int tc = 0);
+// the 10240-byte W operand image of the split16 DFT stages
+void tc_w_table_host(uint16_t *out);
 int model_config(int nkx, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem);
 int model_max_grid(int nkx, int pspi, int interp, int exact, int nmx, int nref, int *blocks_per_sm);
 int launch_model(int nkx, int pspi, int interp, int exact, const MigArgs &a, const BornArgs &b, int grid,

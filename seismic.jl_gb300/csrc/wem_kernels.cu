@@ -18,6 +18,7 @@
 #include <stdint.h>
 #include <stdio.h>
 #include <math.h>
+#include <string.h>
 
 #include "wem_kernels.cuh"
 
@@ -249,29 +250,88 @@ void twiddle_table_host(int nkx, float2 *out)
     default: return -1;                    \
     }
 
-int migrate_config(int nkx, int wide, int pspi, int nmx, int nref, int *S, int *threads, size_t *smem)
+int migrate_config(int nkx, int wide, int pspi, int nmx, int nref, int *S, int *threads, size_t *smem, int tc)
 {
-#define CALL(N) mig_launch<N>(wide, pspi, 0, nref, nmx, nullptr, 0, 0, S, threads, smem, nullptr)
+#define CALL(N) mig_launch<N>(wide, pspi, 0, nref, nmx, nullptr, 0, 0, S, threads, smem, nullptr, tc)
     WEM_SWITCH_N(nkx, CALL)
 #undef CALL
 }
 
-int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *bps)
+int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *bps, int tc)
 {
     int S, th;
     size_t smem;
-#define CALL(N) mig_launch<N>(wide, pspi, interp, nref, nmx, nullptr, 0, 0, &S, &th, &smem, bps)
+#define CALL(N) mig_launch<N>(wide, pspi, interp, nref, nmx, nullptr, 0, 0, &S, &th, &smem, bps, tc)
     WEM_SWITCH_N(nkx, CALL)
 #undef CALL
 }
 
-int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st)
+int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st, int tc)
 {
     int S, th;
     size_t smem;
-#define CALL(N) mig_launch<N>(wide, pspi, interp, a.nref, a.nmx, &a, grid, st, &S, &th, &smem, nullptr)
+#define CALL(N) mig_launch<N>(wide, pspi, interp, a.nref, a.nmx, &a, grid, st, &S, &th, &smem, nullptr, tc)
     WEM_SWITCH_N(nkx, CALL)
 #undef CALL
+}
+
+// IEEE binary16 bits of x, round to nearest even (|x| < 65504; subnormals kept)
+static uint16_t half_bits(double x)
+{
+    const uint16_t sign = x < 0 ? 0x8000u : 0u;
+    x = fabs(x);
+    if (x == 0.0) return sign;
+    int e;
+    const double m = frexp(x, &e);  // x = m 2^e, m in [0.5, 1)
+    if (e - 1 >= -14) {
+        double q = nearbyint(ldexp(m, 11));  // 11 significant bits
+        if (q == 2048.0) {
+            q = 1024.0;
+            e++;
+        }
+        return (uint16_t)(sign | ((e - 1 + 15) << 10) | ((int)q - 1024));
+    }
+    return (uint16_t)(sign | (int)nearbyint(ldexp(x, 24)));  // multiples of 2^-24 (1024 -> smallest normal)
+}
+
+static double half_value(uint16_t h)
+{
+    const int ex = (h >> 10) & 0x1f, mant = h & 0x3ff;
+    const double v = ex == 0 ? ldexp((double)mant, -24) : ldexp(1024.0 + mant, ex - 25);
+    return (h & 0x8000u) ? -v : v;
+}
+
+// The W operands of the split16 DFT stages as they sit in shared memory (layout of
+// wem_tc.cuh): real form of the radix-16 and radix-8 DFT matrices for both signs,
+// each split into fp16 hi = rn(w) and lo = rn(w - hi) from double precision values,
+// stored K-major (row n = output component, K = input component) in 8x8 core matrices.
+void tc_w_table_host(uint16_t *out)
+{
+    memset(out, 0, 10240);
+    int off = 0;
+    for (int R : { 16, 8 }) {
+        const int K = 2 * R;  // fp16 per row, also the number of rows
+        for (int dir = 0; dir < 2; dir++) {
+            const double sgn = dir == 0 ? -1.0 : 1.0;
+            uint16_t *hi = out + off / 2, *lo = out + (off + 2 * K * K) / 2;  // off in bytes
+            for (int q = 0; q < R; q++)
+                for (int r = 0; r < R; r++) {
+                    const double ang = sgn * 6.283185307179586476925286766559 * (double)((r * q) % R) / R;
+                    const double c = cos(ang), sn = sin(ang);
+                    // W[k][n]: k = 2r + (0 re, 1 im) input, n = 2q + (0 re, 1 im) output
+                    const double wv[2][2] = { { c, sn }, { -sn, c } };  // [k parity][n parity]
+                    for (int kp = 0; kp < 2; kp++)
+                        for (int np = 0; np < 2; np++) {
+                            const int k = 2 * r + kp, n = 2 * q + np;
+                            const int e = (n / 8) * (8 * K) + (k / 8) * 64 + (n % 8) * 8 + (k % 8);  // fp16 index
+                            const uint16_t h = half_bits(wv[kp][np]);
+                            hi[e] = h;
+                            lo[e] = half_bits(wv[kp][np] - half_value(h));
+                        }
+                }
+            off += 4 * K * K;  // hi and lo, K*K fp16 each
+        }
+    }
 }
 
 int model_config(int nkx, int pspi, int nmx, int nref, int *S, int *threads, size_t *smem)

@@ -13,7 +13,9 @@
 namespace gbwem {
 
 // ------------------------------------------------------------------ migration
-template <int N, bool PSPI, int INTERP, int S>
+// TC (split16 mode, N = 2048): the FFTs' DFT stages run on the tensor cores; each
+// team gets 32 TMEM columns for its accumulators and an mbarrier.
+template <int N, bool PSPI, int INTERP, int S, bool TC = false>
 __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const MigArgs a)
 {
     using SH = MigShape<N>;
@@ -31,6 +33,37 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
     const unsigned sync = team_sync_handle<N>(tid);
 
     for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
+
+    TcTeam tc{};
+    constexpr uint32_t TCOLS = 2 * S * 32 < 32 ? 32 : 2 * S * 32;  // power of two for 2S in {1, 2, 4}
+    uint32_t *tslot = nullptr;
+    if constexpr (TC) {
+        uint4 *w = reinterpret_cast<uint4 *>(sm.tcx);
+        for (int i = tid; i < TC_W_BYTES / 16; i += NT) w[i] = a.tcw[i];
+        fence_async_smem();  // the W operands become visible to the tensor core
+        uint64_t *mb = reinterpret_cast<uint64_t *>(sm.tcx + TC_W_BYTES);
+        float *red = reinterpret_cast<float *>(mb + 2 * S);
+        tslot = reinterpret_cast<uint32_t *>(red + 4 * 2 * S);
+        int *abort = reinterpret_cast<int *>(tslot + 1);
+        if (tid == 0) {
+            for (int i = 0; i < 2 * S; i++) mbar_init(smem_u32(&mb[i]), 1);
+            *abort = 0;
+            mbar_init_fence();
+        }
+        if (tid < 32) tmem_alloc(tslot, TCOLS);
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        tc.red = red + 4 * team;
+        tc.a = smem_u32(xbuf);
+        tc.w = smem_u32(w);
+        tc.d = *tslot + 32u * team;
+        tc.dw = tc.d + ((uint32_t)(32 * ((t >> 5) & 3)) << 16);
+        tc.mbar = smem_u32(&mb[team]);
+        tc.phase = 0;
+        tc.abort = abort;
+        tc.err = a.err;
+    }
 
     float2 *slot = a.slots + (size_t)blockIdx.x * a.nz * a.nmx;
     const int nitems = a.ngroups * a.nwf;
@@ -66,7 +99,7 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
             __syncthreads();
             const uint8_t zf = a.zflag[iz];
             const bool active = is_src ? (zf & Z_SRC) : (zf & Z_REC);
-            if (active) step_mig<N, PSPI, INTERP>(v, is_src, a, sm, xbuf, sacc, t, sync);
+            if (active) step_mig<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc);
 
             // ---- imaging condition (wem.c:243-247), summed over the group's shots
             if (zf & Z_REC) {
@@ -103,6 +136,17 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                 tables_free = false;
             }
         }
+    }
+    if constexpr (TC) {
+        // every MMA was waited for, unless a wait ran out: then drain before freeing TMEM
+        if (t == 0 && *tc.abort) {
+            tc_commit(tc.mbar);
+            mbar_wait_bounded(tc.mbar, tc.phase);
+        }
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (tid < 32) tmem_dealloc(*tslot, TCOLS);
     }
 }
 
@@ -205,38 +249,48 @@ template <int N> struct Shapes {
     static constexpr int S_MODEL = (T >= 256) ? 1 : (256 / T > 16 ? 16 : 256 / T);
 };
 
-template <int N, bool PSPI, int INTERP, int S>
+template <int N, bool PSPI, int INTERP, int S, bool TC>
 int mig_run(const MigArgs *a, int grid, size_t smem, cudaStream_t st, int *bps)
 {
-    auto k = wem_migrate_kernel<N, PSPI, INTERP, S>;
+    auto k = wem_migrate_kernel<N, PSPI, INTERP, S, TC>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
     if (bps) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, 2 * S * (N / 16), smem) == cudaSuccess ? 0 : -1;
     k<<<grid, 2 * S * (N / 16), smem, st>>>(*a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <int N, int S>
+template <int N, int S, bool TC>
 int mig_sel(int pspi, int interp, const MigArgs *a, int grid, size_t smem, cudaStream_t st, int *bps)
 {
-    if (!pspi) return mig_run<N, false, 0, S>(a, grid, smem, st, bps);
-    if (interp == 0) return mig_run<N, true, 0, S>(a, grid, smem, st, bps);
-    return mig_run<N, true, 1, S>(a, grid, smem, st, bps);
+    if (!pspi) return mig_run<N, false, 0, S, TC>(a, grid, smem, st, bps);
+    if (interp == 0) return mig_run<N, true, 0, S, TC>(a, grid, smem, st, bps);
+    return mig_run<N, true, 1, S, TC>(a, grid, smem, st, bps);
 }
 
-// wide = 1 selects the 512-thread shape. Fills *S/*threads/*smem; launches when
+// wide = 1 selects the 512-thread shape; tc = 1 the split16 (tensor-core) form, built
+// for N = 2048 only (-2 otherwise). Fills *S/*threads/*smem; launches when
 // a != nullptr and bps == nullptr, queries occupancy when bps != nullptr.
 template <int N>
 int mig_launch(int wide, int pspi, int interp, int nref, int nmx, const MigArgs *a, int grid, cudaStream_t st,
-               int *S, int *threads, size_t *smem, int *bps)
+               int *S, int *threads, size_t *smem, int *bps, int tc)
 {
     using SH = Shapes<N>;
     const int s_ = wide ? SH::S_WIDE : SH::S_NARROW;
     *S = s_;
     *threads = 2 * s_ * SH::T;
-    *smem = mig_smem_bytes<N>(pspi != 0, nref, nmx, 2 * s_);
+    *smem = mig_smem_bytes<N>(pspi != 0, nref, nmx, 2 * s_, tc != 0);
+    if (tc) {
+        if constexpr (N == 2048) {
+            if (!a && !bps) return 0;
+            if (wide) return mig_sel<N, SH::S_WIDE, true>(pspi, interp, a, grid, *smem, st, bps);
+            return mig_sel<N, SH::S_NARROW, true>(pspi, interp, a, grid, *smem, st, bps);
+        } else {
+            return -2;
+        }
+    }
     if (!a && !bps) return 0;
-    if (wide) return mig_sel<N, SH::S_WIDE>(pspi, interp, a, grid, *smem, st, bps);
-    return mig_sel<N, SH::S_NARROW>(pspi, interp, a, grid, *smem, st, bps);
+    if (wide) return mig_sel<N, SH::S_WIDE, false>(pspi, interp, a, grid, *smem, st, bps);
+    return mig_sel<N, SH::S_NARROW, false>(pspi, interp, a, grid, *smem, st, bps);
 }
 
 template <int N, bool PSPI, int INTERP, bool EXACT>
@@ -271,7 +325,7 @@ int model_launch(int pspi, int interp, int exact, int nref, int nmx, const MigAr
 // defined in wem_n<N>.cu
 #define WEM_DECLARE_N(N)                                                                                          \
     extern template int mig_launch<N>(int, int, int, int, int, const MigArgs *, int, cudaStream_t, int *, int *, \
-                                      size_t *, int *);                                                           \
+                                      size_t *, int *, int);                                                      \
     extern template int model_launch<N>(int, int, int, int, int, const MigArgs *, const BornArgs *, int,         \
                                         cudaStream_t, int *, int *, size_t *, int *);
 WEM_DECLARE_N(32)

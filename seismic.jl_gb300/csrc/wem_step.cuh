@@ -8,6 +8,7 @@
 
 #include "wem_fft.cuh"
 #include "wem_internal.h"
+#include "wem_tc.cuh"
 
 namespace gbwem {
 
@@ -63,33 +64,49 @@ template <int N> __host__ __device__ constexpr int sel_entries(int nmx)
     return (nmx + N / 16 - 1) / (N / 16) * (N / 16);
 }
 
+// float2 entries of the phase tables, kept even so that what follows stays 16-byte aligned
+template <int N> __host__ __device__ constexpr int ph_entries(bool pspi, int nref)
+{
+    return ((pspi ? nref : 1) * MigShape<N>::HALF + 1) & ~1;
+}
+
+// bytes after the selection rows that the tensor-core stages use (split16 mode):
+// the W operands, one mbarrier and 4 floats of reduction scratch per team, the TMEM
+// base address and the abort flag
+__host__ __device__ constexpr int tc_extra_bytes(int teams) { return 10240 + 8 * teams + 16 * teams + 16; }
+
 template <int N, bool PSPI> struct Smem {
     float2 *tw, *ph, *corr, *x, *acc;
     uint8_t *selb;
     float *wl;
+    char *tcx;       // split16 mode: the tensor-core region (128-byte aligned)
     int acc_stride;  // float2 per team in acc
     __device__ Smem(float4 *raw, int nref, int nmx, int teams)
     {
         using SH = MigShape<N>;
         tw = reinterpret_cast<float2 *>(raw);
         ph = tw + SH::TWP;
-        corr = ph + (size_t)(PSPI ? nref : 1) * SH::HALF;
+        corr = ph + ph_entries<N>(PSPI, nref);
         x = corr + (PSPI ? 0 : ((nmx + 1) & ~1));
         acc = x + (size_t)teams * SH::PADN;
         acc_stride = PSPI ? sel_entries<N>(nmx) : 0;
         wl = reinterpret_cast<float *>(acc + (size_t)teams * acc_stride);
         selb = reinterpret_cast<uint8_t *>(wl + (PSPI ? ((nmx + 3) & ~3) : 0));
+        const size_t off = (size_t)(selb + (PSPI ? ((nmx + 15) & ~15) : 0) - reinterpret_cast<uint8_t *>(raw));
+        tcx = reinterpret_cast<char *>(raw) + ((off + 127) & ~(size_t)127);
     }
 };
 
 // shared-memory footprint (bytes) of one CTA with `teams` row teams
 template <int N>
-__host__ __device__ constexpr size_t mig_smem_bytes(bool pspi, int nref, int nmx, int teams)
+__host__ __device__ constexpr size_t mig_smem_bytes(bool pspi, int nref, int nmx, int teams, bool tc = false)
 {
     using SH = MigShape<N>;
-    return sizeof(float2) * ((size_t)SH::TWP + (size_t)(pspi ? nref : 1) * SH::HALF + (size_t)(pspi ? 0 : ((nmx + 1) & ~1)) +
-                             (size_t)teams * SH::PADN + (pspi ? (size_t)teams * sel_entries<N>(nmx) : 0)) +
-           (pspi ? sizeof(float) * (size_t)((nmx + 3) & ~3) + (size_t)((nmx + 15) & ~15) : 0);
+    const size_t base =
+        sizeof(float2) * ((size_t)SH::TWP + (size_t)ph_entries<N>(pspi, nref) + (size_t)(pspi ? 0 : ((nmx + 1) & ~1)) +
+                          (size_t)teams * SH::PADN + (pspi ? (size_t)teams * sel_entries<N>(nmx) : 0)) +
+        (pspi ? sizeof(float) * (size_t)((nmx + 3) & ~3) + (size_t)((nmx + 15) & ~15) : 0);
+    return tc ? ((base + 127) & ~(size_t)127) + (size_t)tc_extra_bytes(teams) : base;
 }
 
 // Tables of depth step iz at angular frequency w (all threads of the CTA):
@@ -176,12 +193,21 @@ __device__ __forceinline__ float sel_weight(const uint32_t (&selp)[4], const flo
 // split-step on the team's row v (x-domain, x = t + T*m), in place. CONJ selects
 // -dz (the source, and every row of the reference's modelling). Called by active
 // teams only; `sync` is the team's barrier id (teams of 64+ threads) or warp mask.
-template <int N, bool PSPI, int INTERP>
+// TC (split16 mode): the FFTs run their DFT stages on the tensor cores; the row is
+// scaled by a power of two into the operands' range first and back at the end.
+template <int N, bool PSPI, int INTERP, bool TC = false>
 __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, PSPI> &sm,
-                                         float2 *xbuf, float2 *sacc, int t, unsigned sync)
+                                         float2 *xbuf, float2 *sacc, int t, unsigned sync, TcTeam *tc = nullptr)
 {
     constexpr int T = N / 16, HALF = MigShape<N>::HALF;
-    fft_row<N, -1>(v, xbuf, sm.tw, t, sync);  // v now holds the spectrum at k = t + T*m
+    float inv_s = 1.f;
+    if constexpr (TC) {
+        float s;
+        row_scale<T>(v, tc->red, t, sync, s, inv_s);
+#pragma unroll
+        for (int m = 0; m < 16; m++) v[m] = cscale(v[m], s);
+    }
+    fft_row<N, -1, TC>(v, xbuf, sm.tw, t, sync, tc);  // v now holds the spectrum at k = t + T*m
     if (PSPI) {
         // sacc: this team's selection accumulator; thread t owns entries m*T + t
         uint32_t selp[4];
@@ -200,7 +226,7 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
                 const float2 P = ph[kfold<N>(t, m)];
                 u[m] = conj ? cmulc(v[m], P) : cmul(v[m], P);
             }
-            fft_row<N, +1>(u, xbuf, sm.tw, t, sync);
+            fft_row<N, +1, TC>(u, xbuf, sm.tw, t, sync, tc);
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const uint32_t b = (selp[m >> 2] >> (8 * (m & 3))) & 0xffu;
@@ -225,7 +251,7 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             const int x = t + T * m;
-            v[m] = x < a.nmx ? sacc[m * T + t] : make_float2(0.f, 0.f);
+            v[m] = x < a.nmx ? (TC ? cscale(sacc[m * T + t], inv_s) : sacc[m * T + t]) : make_float2(0.f, 0.f);
         }
     } else {
         float2 acc[16];
@@ -234,10 +260,11 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
             const float2 P = sm.ph[kfold<N>(t, m)];
             acc[m] = conj ? cmulc(v[m], P) : cmul(v[m], P);
         }
-        fft_row<N, +1>(acc, xbuf, sm.tw, t, sync);
+        fft_row<N, +1, TC>(acc, xbuf, sm.tw, t, sync, tc);
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             const int x = t + T * m;
+            if constexpr (TC) acc[m] = cscale(acc[m], inv_s);
             v[m] = x < a.nmx ? (conj ? cmulc(acc[m], sm.corr[x]) : cmul(acc[m], sm.corr[x])) : make_float2(0.f, 0.f);
         }
     }

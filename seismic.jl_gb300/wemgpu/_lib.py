@@ -22,7 +22,7 @@ WEM_ERR_NOMEM = -6
 WEM_ERR_NODEV = -7
 
 INTERP = {"ref": 0, "linear": 1}
-PRECISION = {"fp32": 0}
+PRECISION = {"fp32": 0, "split16": 1}
 
 # every symbol the public header declares
 EXPORTS = ["wem_last_error", "wem_version", "wem_ctx_create", "wem_ctx_destroy", "wem_prepare",
