@@ -86,6 +86,7 @@ struct wem_ctx {
     DevBuf ssyn_ref, ssyn_exact;  // synthesis weights w^2 * (half-spectrum | image) factor
     DevBuf tapery, twy;           // 3-D: y taper and y-FFT twiddles
     DevBuf tcw, tcerr;            // split16: W operands of the tensor-core DFT stages, timeout word
+    DevBuf refmask;               // [nz] bit r: some grid point takes its wavefield from reference r
     DevBuf m3_items, m3_U, m3_Y, m3_C, m3_parts;
     // per-call buffers
     DevBuf recv, slots, image, data, tbase, igx, smig, mimg;
@@ -157,7 +158,7 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
                        &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
                        &c->ssyn_ref, &c->ssyn_exact, &c->recv, &c->slots, &c->image, &c->data,
                        &c->tbase, &c->igx, &c->smig, &c->mimg, &c->tapery, &c->twy, &c->m3_items,
-                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr };
+                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -281,6 +282,9 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     std::vector<float> po(nz), pd((size_t)nz * n), vref((size_t)nz * nref), wl((size_t)nz * n, 0.f);
     std::vector<float> slow2((size_t)nz * nref);
     std::vector<uint8_t> sel((size_t)nz * n);
+    // reference velocities some grid point of the depth takes its wavefield from: the
+    // others' inverse transforms are skipped (their results would not be used)
+    std::vector<unsigned long long> used(nz, 0ull);
     for (int iz = 0; iz < nz; iz++) {
         float s = 0.;
         for (int ix = 0; ix < n; ix++) s += vel[(size_t)ix * nz + iz];
@@ -313,7 +317,10 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
                 wl[(size_t)iz * n + ix] = (v - vr1) / (vr2 - vr1);
             }
             sel[(size_t)iz * n + ix] = word;
+            used[iz] |= 1ull << i1;
+            if ((word & SEL_INTERP) && p.interp == WEM_INTERP_LINEAR) used[iz] |= 1ull << (i1 + 1);
         }
+        if (!p.pspi) used[iz] = 1ull;
     }
     // taper of the split-step operator (wem.c:546-564): tmx(imx) * tmy(imy)
     auto taper_of = [](int nm) {
@@ -377,13 +384,15 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         (rc = ensure(c->ssyn_ref, sizeof(float) * syn_ref.size())) ||
         (rc = ensure(c->ssyn_exact, sizeof(float) * syn_exact.size())) ||
         (rc = ensure(c->tapery, sizeof(float) * tapery.size())) || (rc = ensure(c->twy, sizeof(float2) * twy.size())) ||
-        (rc = ensure(c->tcw, 10240)) || (rc = ensure(c->tcerr, sizeof(int))))
+        (rc = ensure(c->tcw, 10240)) || (rc = ensure(c->tcerr, sizeof(int))) ||
+        (rc = ensure(c->refmask, sizeof(unsigned long long) * nz)))
         return rc;
     cudaStream_t st = c->st;
     std::vector<uint16_t> tcw(5120);
     tc_w_table_host(tcw.data());
     CK(cudaMemcpyAsync(c->tcw.p, tcw.data(), 10240, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(c->tcerr.p, 0, sizeof(int), st));
+    CK(cudaMemcpyAsync(c->refmask.p, used.data(), sizeof(unsigned long long) * nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->po.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->pd.p, pd.data(), sizeof(float) * pd.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->vref.p, vref.data(), sizeof(float) * vref.size(), cudaMemcpyHostToDevice, st));
@@ -526,6 +535,7 @@ static MigArgs mig_args(wem_ctx *c, int nshot, int ngroups)
     a.slots = P<float2>(c->slots);
     a.tcw = P<uint4>(c->tcw);
     a.err = P<int>(c->tcerr);
+    a.refmask = P<unsigned long long>(c->refmask);
     return a;
 }
 
@@ -888,6 +898,7 @@ static int run_model(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, flo
         a.recv = nullptr; a.srcw = P<float2>(c->srcw); a.igx = P<int>(c->igx); a.vref = P<float>(c->vref); a.slow2 = P<float>(c->slow2);
         a.po = P<float>(c->po); a.pd = P<float>(c->pd); a.selb = P<uint8_t>(c->sel); a.wlin = P<float>(c->wlin);
         a.taper = P<float>(c->taper); a.zflag = P<uint8_t>(c->zflag); a.twid = P<float2>(c->twid); a.slots = nullptr;
+        a.refmask = P<unsigned long long>(c->refmask);
         BornArgs b{};
         b.img = P<float>(c->mimg);
         b.smig = P<float2>(c->smig);

@@ -42,6 +42,7 @@ struct MigArgs {
     float2 *slots;         // [gridDim.x][nz][nmx] (sum, compensation) image accumulators
     const uint4 *tcw;      // split16 mode: the W operands of the tensor-core DFT stages (10240 B)
     int *err;              // split16 mode: set when a tensor-core wait ran out
+    const unsigned long long *refmask;  // [nz] references in use at each depth (nullptr: all)
 };
 
 struct SpectraArgs {

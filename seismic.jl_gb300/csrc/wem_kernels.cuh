@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
             __syncthreads();
             const uint8_t zf = a.zflag[iz];
             const bool active = is_src ? (zf & Z_SRC) : (zf & Z_REC);
-            if (active) step_mig<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc);
+            if (active) step_mig<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc, ref_mask(a, iz));
 
             // ---- imaging condition (wem.c:243-247), summed over the group's shots
             if (zf & Z_REC) {
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(S * (N / 16), 1) wem_model_kernel(const MigArg
             build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
             __syncthreads();
             const bool act = (a.zflag[iz] & Z_SRC) != 0;
-            if (act) step_mig<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync);
+            if (act) step_mig<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync, nullptr, ref_mask(a, iz));
             float2 *row = smig + (size_t)iz * nmx;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(S * (N / 16), 1) wem_model_kernel(const MigArg
                         v[m].y += mv * s_.y;
                     }
                 }
-                step_model<N, PSPI, INTERP, EXACT>(v, a, sm, xbuf, sacc, t, sync);
+                step_model<N, PSPI, INTERP, EXACT>(v, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz));
             }
         }
         if (shot_ok) {

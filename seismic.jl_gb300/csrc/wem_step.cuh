@@ -109,6 +109,12 @@ __host__ __device__ constexpr size_t mig_smem_bytes(bool pspi, int nref, int nmx
     return tc ? ((base + 127) & ~(size_t)127) + (size_t)tc_extra_bytes(teams) : base;
 }
 
+// references some grid point of depth iz takes its wavefield from (bit r)
+__device__ __forceinline__ unsigned long long ref_mask(const MigArgs &a, int iz)
+{
+    return a.refmask ? a.refmask[iz] : ~0ull;
+}
+
 // Tables of depth step iz at angular frequency w (all threads of the CTA):
 // PSPI: one phase table per reference velocity and the depth's selection row;
 // split-step: the phase table of the mean slowness and the correction
@@ -120,7 +126,9 @@ __device__ __forceinline__ void build_tables(const MigArgs &a, const Smem<N, PSP
     constexpr int HALF = MigShape<N>::HALF;
     if (PSPI) {
         const float *sl = a.slow2 + (size_t)iz * a.nref;
+        const unsigned long long used = ref_mask(a, iz);
         for (int r = 0; r < a.nref; r++) {
+            if (!((used >> r) & 1ull)) continue;  // no grid point takes this reference
             const float slow2 = sl[r];
             float2 *ph = sm.ph + (size_t)r * HALF;
             for (int kk = tid; kk < HALF; kk += nthreads)
@@ -195,9 +203,11 @@ __device__ __forceinline__ float sel_weight(const uint32_t (&selp)[4], const flo
 // teams only; `sync` is the team's barrier id (teams of 64+ threads) or warp mask.
 // TC (split16 mode): the FFTs run their DFT stages on the tensor cores; the row is
 // scaled by a power of two into the operands' range first and back at the end.
+// used: the references in use at this depth (ref_mask); the others are skipped.
 template <int N, bool PSPI, int INTERP, bool TC = false>
 __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, PSPI> &sm,
-                                         float2 *xbuf, float2 *sacc, int t, unsigned sync, TcTeam *tc = nullptr)
+                                         float2 *xbuf, float2 *sacc, int t, unsigned sync, TcTeam *tc = nullptr,
+                                         unsigned long long used = ~0ull)
 {
     constexpr int T = N / 16, HALF = MigShape<N>::HALF;
     float inv_s = 1.f;
@@ -219,6 +229,7 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
             selp[m >> 2] |= (x < a.nmx ? (uint32_t)sm.selb[x] : 0x7fu) << (8 * (m & 3));
         }
         for (int r = 0; r < a.nref; r++) {
+            if (!((used >> r) & 1ull)) continue;  // CTA-uniform
             const float2 *ph = sm.ph + (size_t)r * HALF;
             float2 u[16];
 #pragma unroll
@@ -281,11 +292,11 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
 // for split-step the reference's operator already is that adjoint.
 template <int N, bool PSPI, int INTERP, bool EXACT>
 __device__ __forceinline__ void step_model(float2 (&v)[16], const MigArgs &a, const Smem<N, PSPI> &sm, float2 *xbuf,
-                                           float2 *sacc, int t, unsigned sync)
+                                           float2 *sacc, int t, unsigned sync, unsigned long long used = ~0ull)
 {
     constexpr int T = N / 16, HALF = MigShape<N>::HALF;
     if (PSPI && !EXACT) {
-        step_mig<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync);
+        step_mig<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync, nullptr, used);
         return;
     }
     float2 acc[16];
@@ -305,6 +316,7 @@ __device__ __forceinline__ void step_model(float2 (&v)[16], const MigArgs &a, co
 #pragma unroll
         for (int m = 0; m < 16; m++) acc[m] = make_float2(0.f, 0.f);
         for (int r = 0; r < a.nref; r++) {
+            if (!((used >> r) & 1ull)) continue;  // every weight of this reference is zero
             float2 u[16];
 #pragma unroll
             for (int m = 0; m < 16; m++) {

@@ -30,9 +30,10 @@
 // core matrices adjacent along K are 128 B apart (leading byte offset) and groups
 // of 8 rows are 16*K bytes apart (stride byte offset, K in fp16 elements).
 //
-// Every wait on an mbarrier is bounded (about a second of clock cycles); a wait that
-// runs out sets the CTA's abort flag and the launch's error word, after which the
-// CTA issues no more tensor-core work and waits no more, so it runs to its end
+// The issuing thread alone waits on the mbarrier, the rest of the team at a named
+// barrier behind it. Every mbarrier wait is bounded (about a second of clock cycles); a
+// wait that runs out sets the CTA's abort flag and the launch's error word, after which
+// the CTA issues no more tensor-core work and waits no more, so it runs to its end
 // (results are garbage, the host reports WEM_ERR_TIMEOUT).
 #pragma once
 #include <cuda_fp16.h>
@@ -225,14 +226,14 @@ __device__ __forceinline__ void tc_dft(float2 (&u)[16], TcTeam &tc, char *a_gen,
             }
         }
         tc_commit(tc.mbar);
-    }
-    if (live && *tc.abort == 0) {
+        // the issuing thread alone polls the mbarrier; the team waits at the barrier below
         if (!mbar_wait_bounded(tc.mbar, tc.phase)) {
             *tc.abort = 1;
             atomicExch(tc.err, 1);
         }
     }
     tc.phase ^= 1u;
+    team_sync<T>(bar_id);  // the team's MMAs have completed
     tc_fence_after();
     float r[32];
     tmem_ld32(tc.dw, r);
