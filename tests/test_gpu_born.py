@@ -101,3 +101,51 @@ def test_least_squares_migration_reduces_misfit(gpu_lib):
     m, cost = conjugate_gradients(d, fwd, lambda r: adj(r.astype(np.float32)), niter=10)
     ctx.close()
     assert np.all(np.diff(cost) <= 1e-6) and cost[-1] < 0.2
+
+
+def test_misfit_curve_matches_reference_operator_pair(gpu_lib, oracle_mod):
+    """CG over the GPU's reference operator pair (wem_model with exact=0, wem_migrate)
+    against CG over the oracle's restatement of the reference's own pair (wem.c adj and
+    fwd, shot by shot), same data and start: the normalised misfit curves agree."""
+    from wemgpu import synth
+    from wemgpu.cg import conjugate_gradients
+    c = synth.small_case(112, nx=64, nz=16, nt=96, nshot=2, pspi=1, nref=4, interp="linear")
+    p, shots = c["params"], c["shots"]
+    ctx = gpu_lib.Context()
+    ctx.prepare(p, c["vel"], c["wav"])
+
+    def fwd_gpu(m):
+        return ctx.model(shots, m, exact=False)
+
+    def adj_gpu(d):
+        return ctx.migrate(gpu_lib.Shots(shots.sx, shots.sy, shots.trace_offset, shots.trace_cell,
+                                         np.ascontiguousarray(d, np.float32)))
+
+    def fwd_ref(m):
+        out = []
+        for s in range(shots.nshot):
+            lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
+            full = oracle_mod.wem_port(dict(p, sx=float(shots.sx[s])), c["vel"], c["wav"], m=m, adj=False)
+            out.append(full[shots.trace_cell[lo:hi]])
+        return np.concatenate(out).astype(np.float64)
+
+    def adj_ref(d):
+        img = np.zeros((p["nmx"], p["nz"]))
+        for s in range(shots.nshot):
+            lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
+            g = np.zeros((p["nmx"], p["nt"]), np.float32)
+            g[shots.trace_cell[lo:hi]] = d[lo:hi]
+            img += oracle_mod.wem_port(dict(p, sx=float(shots.sx[s])), c["vel"], c["wav"], d=g, adj=True)
+        return img
+
+    rng = np.random.default_rng(14)
+    m_true = np.zeros((p["nmx"], p["nz"]), np.float32)
+    m_true[rng.integers(0, p["nmx"], 20), rng.integers(2, p["nz"], 20)] = rng.standard_normal(20)
+    d = fwd_ref(m_true)
+    _, cost_gpu = conjugate_gradients(d, lambda m: fwd_gpu(np.asarray(m, np.float32)),
+                                      lambda r: adj_gpu(r.astype(np.float32)), niter=6)
+    _, cost_ref = conjugate_gradients(d, lambda m: fwd_ref(np.asarray(m, np.float32)),
+                                      lambda r: adj_ref(r.astype(np.float32)), niter=6)
+    ctx.close()
+    cost_gpu, cost_ref = np.array(cost_gpu), np.array(cost_ref)
+    assert np.all(np.abs(cost_gpu - cost_ref) <= 1e-3 * np.maximum(cost_ref, 1e-3)), (cost_gpu, cost_ref)
