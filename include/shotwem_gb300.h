@@ -136,6 +136,18 @@ WEM_API int wem_migrate_survey(wem_ctx *ctx, const wem_params *p, const float *v
                        int nshot, const float *sx, const float *sy, const int64_t *trace_offset,
                        const int32_t *trace_cell, const float *d, float *m);
 
+/* Source-side incidence angles of nshot shots: compute_angles (wem.c:566-684, and its
+   file-level main in compute_angles.c), the operator behind Seismic.jl's ComputeAngles.
+   For each shot the source wavefield of every frequency in [fmin, fmax] of the unpadded
+   time axis is continued down with ssop_source's split-step operator on the unpadded
+   grid, and angx = mean over frequency of (180/pi) atan(|du/dx| / (|du/dz| + 1e-10)),
+   signed by the side the energy arrives from. Uses nt, dt, the grid, sz, fmin and fmax of
+   p (padt, padx, pspi, nref, interp are not used; any nmx and nz). vel [nmx][nz], wav [nt];
+   angx, angy: host [nshot][nmx][nz] (angy may be NULL; it is 0 in 2-D). Needs a context
+   (wem_ctx_create), not wem_prepare. 2-D grids only (WEM_ERR_SIZE otherwise), nmx <= 4096. */
+WEM_API int wem_angles(wem_ctx *ctx, const wem_params *p, const float *vel, const float *wav, int nshot,
+                       const float *sx, const float *sy, float *angx, float *angy);
+
 /* Elapsed device time (ms) of the last wem_migrate* call's GPU work, from CUDA
    events on ctx's stream; and how many kernels it launched. */
 WEM_API int wem_last_timing(wem_ctx *ctx, float *ms, int *kernels);

@@ -98,8 +98,32 @@ def ref_lib():
             fpp, _i, _f, _f, _i, _i, C.c_bool, C.c_bool, C.c_bool]
         L.main.restype = _i
         L.main.argtypes = [_i, C.POINTER(C.c_char_p)]
+        # wem.h:44-50
+        L.compute_angles.restype = None
+        L.compute_angles.argtypes = [fpp, fpp, fpp, _i, _f, _f, _i, _f, _f, _i, _f, _f, _f, _f, _i, _f, _f, _f,
+                                     fpp, _f, _f, C.c_bool]
         _ref = L
     return _ref
+
+
+def angles_ref(p: dict, vel: np.ndarray, wav: np.ndarray):
+    """The reference's own compute_angles() (oracle/_ref, src/Imaging/c/wem.c:566-684):
+    angx, angy [nx*ny, nz] of the shot at (p["sx"], p["sy"]). Its frequency loop adds
+    into shared arrays from every OpenMP thread without synchronisation, so only a
+    process started with OMP_NUM_THREADS=1 gives a well-defined result."""
+    L = ref_lib()
+    n = int(p["nmx"]) * int(p.get("nmy", 1))
+    nz = int(p["nz"])
+    vel = np.ascontiguousarray(vel, dtype=np.float32).copy()
+    wav2 = np.ascontiguousarray(np.asarray(wav, np.float32).reshape(1, -1)).copy()
+    ax = np.zeros((n, nz), np.float32)
+    ay = np.zeros((n, nz), np.float32)
+    L.compute_angles(_rows(ax), _rows(ay), _rows(wav2), int(p["nt"]), float(p.get("ot", 0.0)), float(p["dt"]),
+                     int(p["nmx"]), float(p.get("omx", 0.0)), float(p["dmx"]), int(p.get("nmy", 1)),
+                     float(p.get("omy", 0.0)), float(p.get("dmy", p["dmx"])), float(p["sx"]), float(p.get("sy", 0.0)),
+                     nz, float(p.get("oz", 0.0)), float(p["dz"]), float(p.get("sz", 0.0)), _rows(vel),
+                     float(p.get("fmin", 0.0)), float(p.get("fmax", 80.0)), False)
+    return ax, ay
 
 
 def omp_threads() -> int:

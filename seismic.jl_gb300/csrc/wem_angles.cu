@@ -1,0 +1,243 @@
+// wem_angles.cu -- source-side incidence angles on the GPU: the reference's
+// compute_angles / extrapolate_source / ssop_source / calculate_derivatives
+// (src/Imaging/c/wem.c:566-992), 2-D grids.
+//
+// Per frequency of the band (no time or space padding: ntfft = nt, nkx = nmx, nkz = nz):
+//   1. wem_angles_extrap_kernel: the source wavefield continued down with the split-step
+//      operator of ssop_source (taper, then exp(i w pd dz), FFT_x, phase with the mean
+//      slowness, IFFT_x, wem.c:763-820), one CTA per frequency, the row in shared memory,
+//      every depth stored: u[f][z][x].
+//   2. wem_axis_dft_kernel: the derivatives. The reference takes 3-D FFTs of u and
+//      inverse FFTs of i k_x A, i k_z A, i k_x^left A, i k_x^right A (wem.c:822-985).
+//      The transform is separable and each factor i k acts on one axis only, so
+//      IDFT3(i k_x DFT3(u)) = IDFT_x(i k_x DFT_x(u)) exactly: two forward and four inverse
+//      one-axis transforms per frequency instead of one forward and seven inverse 3-D ones.
+//      The axes have any length (nz is rarely a power of two), so each transform is a
+//      tiled direct DFT (a complex matrix product against W^{ik}, the table built in FP64).
+//   3. wem_angles_accum_kernel: per grid point, in frequency order,
+//      ang += (180/pi) atan(|u_x| / (|u_z| + 1e-10)) and sign += +-|u| / nw, then
+//      ang *= sign(sign) / (ifmax - ifmin + 1) (wem.c:675-676, 735-754).
+// In 2-D the y terms vanish: u_y = 0 gives angy = 0 (the reference's value).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "wem_internal.h"
+
+namespace gbwem {
+
+__device__ __forceinline__ float2 c_mul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+// wavenumber of index i on an axis of n samples: dk*i up to n/2, then -(dk*n - dk*i),
+// in float without contraction (wem.c:802-803, 866-867, 905-906)
+__device__ __forceinline__ float axis_k(int i, int n, float dk)
+{
+    return i <= n / 2 ? __fmul_rn(dk, (float)i) : -__fsub_rn(__fmul_rn(dk, (float)n), __fmul_rn(dk, (float)i));
+}
+
+// ------------------------------------------------------------------ 1. extrapolation
+__global__ void __launch_bounds__(512) wem_angles_extrap_kernel(const AngleArgs a)
+{
+    extern __shared__ float2 sh[];
+    const int nmx = a.nmx, tid = threadIdx.x, nth = blockDim.x;
+    float2 *d = sh, *x = sh + nmx;
+    const float2 *tw = sh + 2 * nmx;
+    float2 *tws = sh + 2 * nmx;
+    const int f = blockIdx.x;
+    const float w = __fmul_rn((float)(a.ifmin + f), a.dw);  // w = iw*dw
+    const float dzs = -a.dz;                                 // extrapolate_source passes -dz
+    for (int i = tid; i < nmx; i += nth) {
+        tws[i] = a.twx[i];
+        d[i] = i == a.igx ? a.srcw[f] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int iz = 0; iz < a.nz; iz++) {
+        float2 *urow = a.u + ((size_t)f * a.nz + iz) * nmx;
+        const float z = __fadd_rn(a.oz, __fmul_rn(a.dz, (float)iz));
+        if (!(z >= a.sz)) {  // CTA-uniform: nothing above the source
+            for (int i = tid; i < nmx; i += nth) urow[i] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const float *pdr = a.pd + (size_t)iz * nmx;
+        for (int i = tid; i < nmx; i += nth) {
+            const float2 v = make_float2(d[i].x * a.taper[i], d[i].y * a.taper[i]);  // boundary_condition
+            float sn, cs;
+            sincosf(__fmul_rn(__fmul_rn(w, pdr[i]), dzs), &sn, &cs);              // cexpf(I*w*pd*dz)
+            x[i] = c_mul(v, make_float2(cs, sn));
+        }
+        __syncthreads();
+        const float po = a.po[iz];
+        const float wp = __fmul_rn(__fmul_rn(w, w), __fmul_rn(po, po));
+        for (int k = tid; k < nmx; k += nth) {  // forward DFT, phase shift
+            float2 acc = make_float2(0.f, 0.f);
+            int idx = 0;
+            for (int j = 0; j < nmx; j++) {
+                const float2 xv = x[j], wv = tw[idx];
+                acc.x = fmaf(xv.x, wv.x, fmaf(-xv.y, wv.y, acc.x));
+                acc.y = fmaf(xv.x, wv.y, fmaf(xv.y, wv.x, acc.y));
+                idx += k;
+                if (idx >= nmx) idx -= nmx;
+            }
+            const float kx = axis_k(k, nmx, a.dkx);
+            const float s = __fsub_rn(__fsub_rn(wp, __fmul_rn(kx, kx)), 0.f);
+            float2 L;
+            if (s >= 0.f) {
+                float sn, cs;
+                sincosf(__fmul_rn(__fsqrt_rn(s), dzs), &sn, &cs);
+                L = make_float2(cs, sn);
+            } else {
+                // cexpf(-0.2*sqrtf(fabs(s))*fabs(dz)): the argument is a double expression
+                L = make_float2(expf((float)(-0.2 * (double)__fsqrt_rn(fabsf(s)) * (double)fabsf(dzs))), 0.f);
+            }
+            const float2 q = c_mul(acc, L);
+            d[k] = make_float2(q.x * a.inv_sqrt_n, q.y * a.inv_sqrt_n);
+        }
+        __syncthreads();
+        for (int i = tid; i < nmx; i += nth) {  // inverse DFT
+            float2 acc = make_float2(0.f, 0.f);
+            int idx = 0;
+            for (int k = 0; k < nmx; k++) {
+                const float2 dv = d[k], wv = tw[idx];  // conj(W^{ik})
+                acc.x = fmaf(dv.x, wv.x, fmaf(dv.y, wv.y, acc.x));
+                acc.y = fmaf(dv.y, wv.x, fmaf(-dv.x, wv.y, acc.y));
+                idx += i;
+                if (idx >= nmx) idx -= nmx;
+            }
+            const float2 v = make_float2(acc.x * a.inv_sqrt_n, acc.y * a.inv_sqrt_n);
+            x[i] = v;
+            urow[i] = v;
+        }
+        __syncthreads();
+        float2 *t = d;  // the new row is in x
+        d = x;
+        x = t;
+    }
+}
+
+// ------------------------------------------------------------------ 2. one-axis DFTs
+// out[base(l) + k*se] = scale * sum_i mult(i) in[base(l) + i*se] W^{+-ik},
+// base(l) = (l / nb) * sa + (l % nb) * sb. Tile: 32 lines x 64 outputs per CTA of
+// 256 threads, input staged 32 samples at a time; each thread 2 lines x 4 outputs.
+__global__ void __launch_bounds__(256) wem_axis_dft_kernel(const AxisDftArgs a)
+{
+    constexpr int LN = 32, KO = 64, KC = 32;
+    __shared__ float2 s_in[LN][KC + 1];
+    __shared__ float2 s_w[KC][KO];
+    const int tid = threadIdx.x;
+    const long long l0 = (long long)blockIdx.x * LN;
+    const int k0 = blockIdx.y * KO;
+    const int tx = tid & 15, ty = tid >> 4;
+    float2 acc[2][4];
+#pragma unroll
+    for (int i = 0; i < 2; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = make_float2(0.f, 0.f);
+    const bool contiguous = a.se == 1;
+    for (int i0 = 0; i0 < a.L; i0 += KC) {
+        __syncthreads();
+        for (int e = tid; e < LN * KC; e += 256) {
+            // contiguous lines: consecutive threads walk one line; strided: across lines
+            const int li = contiguous ? e / KC : e % LN, ii = contiguous ? e % KC : e / LN;
+            const long long l = l0 + li;
+            const int i = i0 + ii;
+            float2 v = make_float2(0.f, 0.f);
+            if (l < a.nlines && i < a.L) {
+                const long long base = (l / a.nb) * a.sa + (l % a.nb) * a.sb;
+                v = a.in[base + (long long)i * a.se];
+                if (a.mode) {  // i k(i) for the derivative of the axis (left / right halves)
+                    float k = axis_k(i, a.L, a.dk);
+                    if (a.mode == 2) k = i <= a.L / 2 ? 0.f : k;
+                    if (a.mode == 3) k = i <= a.L / 2 ? k : 0.f;
+                    v = make_float2(-k * v.y, k * v.x);
+                }
+            }
+            s_in[li][ii] = v;
+        }
+        for (int e = tid; e < KC * KO; e += 256) {
+            const int ii = e / KO, kk = e - ii * KO;
+            const int i = i0 + ii, k = k0 + kk;
+            float2 wv = make_float2(0.f, 0.f);
+            if (i < a.L && k < a.L) {
+                wv = a.tw[(int)(((long long)i * k) % a.L)];
+                if (a.sign > 0) wv.y = -wv.y;
+            }
+            s_w[ii][kk] = wv;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int ii = 0; ii < KC; ii++) {
+            const float2 v0 = s_in[ty * 2][ii], v1 = s_in[ty * 2 + 1][ii];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const float2 wv = s_w[ii][tx * 4 + j];
+                acc[0][j].x = fmaf(v0.x, wv.x, fmaf(-v0.y, wv.y, acc[0][j].x));
+                acc[0][j].y = fmaf(v0.x, wv.y, fmaf(v0.y, wv.x, acc[0][j].y));
+                acc[1][j].x = fmaf(v1.x, wv.x, fmaf(-v1.y, wv.y, acc[1][j].x));
+                acc[1][j].y = fmaf(v1.x, wv.y, fmaf(v1.y, wv.x, acc[1][j].y));
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; i++) {
+        const long long l = l0 + ty * 2 + i;
+        if (l >= a.nlines) continue;
+        const long long base = (l / a.nb) * a.sa + (l % a.nb) * a.sb;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int k = k0 + tx * 4 + j;
+            if (k < a.L) a.out[base + (long long)k * a.se] = make_float2(acc[i][j].x * a.scale, acc[i][j].y * a.scale);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ 3. accumulation
+// One thread per grid point (x, z), frequencies in order; out [nmx][nz].
+__global__ void __launch_bounds__(256) wem_angles_accum_kernel(const AngleAccumArgs a)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= (long long)a.nmx * a.nz) return;
+    const int z = (int)(p / a.nmx), x = (int)(p - (long long)z * a.nmx);
+    const size_t plane = (size_t)a.nmx * a.nz, off = (size_t)z * a.nmx + x;
+    float ang = 0.f, sgn = 0.f;
+    for (int f = 0; f < a.nwf; f++) {
+        const size_t q = (size_t)f * plane + off;
+        const float2 u = a.u[q], sx = a.ux[q], sz = a.uz[q], ul = a.ul[q], ur = a.ur[q];
+        const float au = hypotf(u.x, u.y);
+        const float ratio = hypotf(sx.x, sx.y) / (hypotf(sz.x, sz.y) + 1e-10f);
+        ang += (float)(57.295779513082323 * (double)atanf(ratio));  // (180/PI)*atanf(...) in double
+        const float s = hypotf(ul.x, ul.y) >= hypotf(ur.x, ur.y) ? au : -au;
+        sgn += s / (float)a.nw;
+    }
+    a.angx[(size_t)x * a.nz + z] = ang * ((sgn >= 0.f ? 1.f : -1.f) / (float)a.nfreq_div);
+    if (a.angy) a.angy[(size_t)x * a.nz + z] = 0.f;  // 2-D: u_y = 0
+}
+
+int launch_angles_extrap(const AngleArgs &a, cudaStream_t st)
+{
+    const size_t smem = sizeof(float2) * 3 * (size_t)a.nmx;
+    if (cudaFuncSetAttribute(wem_angles_extrap_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return -1;
+    wem_angles_extrap_kernel<<<a.nwf, 512, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_axis_dft(const AxisDftArgs &a, cudaStream_t st)
+{
+    if (a.nlines <= 0 || a.L <= 0) return 0;
+    dim3 grid((unsigned)((a.nlines + 31) / 32), (unsigned)((a.L + 63) / 64));
+    wem_axis_dft_kernel<<<grid, 256, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_angles_accum(const AngleAccumArgs &a, cudaStream_t st)
+{
+    const long long n = (long long)a.nmx * a.nz;
+    wem_angles_accum_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace gbwem

@@ -242,6 +242,22 @@ static void freq_grid(const wem_params &p, int *ntfft, int *nw, int *ifmin, int 
 
 static int is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
+// boundary_condition weights along one axis (wem.c:546-564), in the reference's float
+// expressions (lm = 30 points from each edge when the axis has more than 100)
+static std::vector<float> taper_of(int nm)
+{
+    std::vector<float> tp(nm);
+    const int lm = nm > 100 ? 30 : 0;
+    float tm = 1.f;
+    for (int im = 0; im < nm; im++) {
+        if (im >= 0 && im < lm) tm = expf(-powf(0.015 * ((float)lm - im), 2.));
+        if (im >= lm && im <= nm - lm) tm = 1.;
+        if (im > nm - lm && im < nm) tm = expf(-powf(0.015 * ((float)im - nm + lm), 2.));
+        tp[im] = tm;
+    }
+    return tp;
+}
+
 extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, const float *wav)
 {
     if (!c || !pp || !vel || !wav) return fail(WEM_ERR_ARG, "wem_prepare: null argument");
@@ -323,18 +339,6 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         if (!p.pspi) used[iz] = 1ull;
     }
     // taper of the split-step operator (wem.c:546-564): tmx(imx) * tmy(imy)
-    auto taper_of = [](int nm) {
-        std::vector<float> tp(nm);
-        const int lm = nm > 100 ? 30 : 0;
-        float tm = 1.f;
-        for (int im = 0; im < nm; im++) {
-            if (im >= 0 && im < lm) tm = expf(-powf(0.015 * ((float)lm - im), 2.));
-            if (im >= lm && im <= nm - lm) tm = 1.;
-            if (im > nm - lm && im < nm) tm = expf(-powf(0.015 * ((float)im - nm + lm), 2.));
-            tp[im] = tm;
-        }
-        return tp;
-    };
     std::vector<float> taper = taper_of(nmx), tapery = taper_of(p.nmy);
     std::vector<uint8_t> zf(nz);
     for (int iz = 0; iz < nz; iz++) {
@@ -846,6 +850,183 @@ extern "C" int wem_migrate(wem_ctx *c, int nshot, const float *sx, const float *
     CK(cudaMemcpyAsync(m, c->image.p, mbytes, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     return collect_times(c);
+}
+
+// ---------------------------------------------------------------- incidence angles
+// compute_angles (wem.c:566-684) for each shot: the band [fmin, fmax] of the unpadded
+// time axis (ntfft = nt), no spatial padding; any grid length (direct transforms).
+extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, const float *wav, int nshot,
+                          const float *sx, const float *sy, float *angx, float *angy)
+{
+    if (!c || !pp || !vel || !wav) return fail(WEM_ERR_ARG, "wem_angles: null argument");
+    if (nshot < 1 || !sx || !angx) return fail(WEM_ERR_ARG, "wem_angles: need nshot >= 1, sx and angx");
+    const wem_params &p = *pp;
+    if (p.nt < 2 || p.nmx < 1 || p.nz < 1 || !(p.dt > 0) || !(p.dmx > 0) || !(p.dz > 0))
+        return fail(WEM_ERR_ARG, "wem_angles: invalid grid (nt=%d nmx=%d nz=%d)", p.nt, p.nmx, p.nz);
+    if (p.nmy != 1) return fail(WEM_ERR_SIZE, "wem_angles: incidence angles are built for 2-D grids (nmy = 1)");
+    const int nmx = p.nmx, nz = p.nz;
+    if (nmx > 4096) return fail(WEM_ERR_SIZE, "wem_angles: nmx = %d above 4096", nmx);
+    CK(cudaSetDevice(c->device));
+    cudaStream_t st = c->st;
+    // slowness split of compute_angles (wem.c:609-618), depth-major on the device
+    std::vector<float> po(nz), pd((size_t)nz * nmx);
+    for (int iz = 0; iz < nz; iz++) {
+        float s = 0.;
+        for (int ix = 0; ix < nmx; ix++) s += vel[(size_t)ix * nz + iz];
+        s /= (float)nmx * p.nmy;
+        s = 1. / s;
+        po[iz] = s;
+        for (int ix = 0; ix < nmx; ix++) pd[(size_t)iz * nmx + ix] = 1.0 / vel[(size_t)ix * nz + iz] - po[iz];
+    }
+    const std::vector<float> taper = taper_of(nmx);
+    wem_params q = p;
+    q.padt = 1;  // compute_angles does not pad the time axis (wem.c:589)
+    int ntfft, nw, ifmin, ifmax;
+    float dw;
+    freq_grid(q, &ntfft, &nw, &ifmin, &ifmax, &dw);
+    const int nwf = ifmax - ifmin;
+    const size_t n = (size_t)nmx * nz;
+    if (nwf < 1) {
+        memset(angx, 0, sizeof(float) * n * nshot);
+        if (angy) memset(angy, 0, sizeof(float) * n * nshot);
+        return WEM_OK;
+    }
+    const float dkx = 2 * 3.141592653589793 / ((float)nmx) / p.dmx;
+    const float dkz = 2 * 3.141592653589793 / ((float)nz) / p.dz;
+    // source spectrum: f_op of the wavelet on (nw - 1) * 2 samples, / sqrtf(ntfft)
+    const int lop = (nw - 1) * 2;
+    std::vector<float2> wt(lop), twx(nmx), twz(nz);
+    for (int k = 0; k < lop; k++) {
+        const double a = -6.283185307179586476925286766559 * k / lop;
+        wt[k] = make_float2((float)cos(a), (float)sin(a));
+    }
+    for (int k = 0; k < nmx; k++) {
+        const double a = -6.283185307179586476925286766559 * k / nmx;
+        twx[k] = make_float2((float)cos(a), (float)sin(a));
+    }
+    for (int k = 0; k < nz; k++) {
+        const double a = -6.283185307179586476925286766559 * k / nz;
+        twz[k] = make_float2((float)cos(a), (float)sin(a));
+    }
+    std::vector<float> sc(nwf, 1.f / sqrtf((float)ntfft));
+    const int64_t zero = 0;
+    const size_t plane = sizeof(float2) * (size_t)nwf * n;
+    DevBuf bwt, btwx, btwz, bsc, bsrc, bbase, bU, bT, bX, bL, bR, bZ, bang, bpo, bpd, btap, bwav;
+    auto release = [&]() {
+        DevBuf *bs[] = { &bwt, &btwx, &btwz, &bsc, &bsrc, &bbase, &bU, &bT, &bX, &bL, &bR, &bZ, &bang,
+                         &bpo, &bpd, &btap, &bwav };
+        for (DevBuf *b : bs)
+            if (b->p) cudaFree(b->p);
+    };
+    int rc;
+    if ((rc = ensure(bwt, sizeof(float2) * lop)) || (rc = ensure(btwx, sizeof(float2) * nmx)) ||
+        (rc = ensure(btwz, sizeof(float2) * nz)) || (rc = ensure(bsc, sizeof(float) * nwf)) ||
+        (rc = ensure(bsrc, sizeof(float2) * nwf)) || (rc = ensure(bbase, sizeof(int64_t))) || (rc = ensure(bU, plane)) ||
+        (rc = ensure(bT, plane)) || (rc = ensure(bX, plane)) || (rc = ensure(bL, plane)) || (rc = ensure(bR, plane)) ||
+        (rc = ensure(bZ, plane)) || (rc = ensure(bang, sizeof(float) * 2 * n)) ||
+        (rc = ensure(bpo, sizeof(float) * nz)) || (rc = ensure(bpd, sizeof(float) * n)) ||
+        (rc = ensure(btap, sizeof(float) * nmx)) || (rc = ensure(bwav, sizeof(float) * p.nt))) {
+        release();
+        return rc;
+    }
+#define CKR(call)                                                                                                 \
+    do {                                                                                                          \
+        cudaError_t e_ = (call);                                                                                  \
+        if (e_ != cudaSuccess) {                                                                                  \
+            release();                                                                                            \
+            return fail(WEM_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);     \
+        }                                                                                                         \
+    } while (0)
+    CKR(cudaMemcpyAsync(bwt.p, wt.data(), sizeof(float2) * lop, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(btwx.p, twx.data(), sizeof(float2) * nmx, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(btwz.p, twz.data(), sizeof(float2) * nz, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bsc.p, sc.data(), sizeof(float) * nwf, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bbase.p, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bpo.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bpd.p, pd.data(), sizeof(float) * n, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(btap.p, taper.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bwav.p, wav, sizeof(float) * p.nt, cudaMemcpyHostToDevice, st));
+    SpectraArgs sa{};
+    sa.d = P<float>(bwav);
+    sa.ntr = 1;
+    sa.nt = p.nt < lop ? p.nt : lop;
+    sa.ntfft = lop;
+    sa.ifmin = ifmin;
+    sa.nwf = nwf;
+    sa.out_base = P<int64_t>(bbase);
+    sa.out_fstride = 1;
+    sa.wtab = P<float2>(bwt);
+    sa.scale = P<float>(bsc);
+    sa.out = P<float2>(bsrc);
+    if (launch_spectra(sa, st)) {
+        release();
+        return fail(WEM_ERR_CUDA, "angles: spectra launch: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    int kernels = 1;
+    CK(cudaEventRecord(c->ev0, st));
+    for (int s = 0; s < nshot; s++) {
+        const float xs = sx[s];
+        const int igx = (int)((float)(int)(xs - p.omx) / p.dmx);  // (int) (sx - omx)/dmx, wem.c:654
+        if (igx < 0 || igx >= nmx) {
+            release();
+            return fail(WEM_ERR_ARG, "wem_angles: shot %d at sx=%g is outside the grid", s, (double)xs);
+        }
+        AngleArgs a{};
+        a.nmx = nmx; a.nz = nz; a.nwf = nwf; a.ifmin = ifmin; a.igx = igx;
+        a.dw = dw; a.dz = p.dz; a.oz = p.oz; a.sz = p.sz; a.dkx = dkx; a.inv_sqrt_n = 1.f / sqrtf((float)nmx);
+        a.po = P<float>(bpo); a.pd = P<float>(bpd); a.taper = P<float>(btap); a.srcw = P<float2>(bsrc);
+        a.twx = P<float2>(btwx); a.u = P<float2>(bU);
+        if (launch_angles_extrap(a, st)) {
+            release();
+            return fail(WEM_ERR_CUDA, "angles: extrapolation launch: %s", cudaGetErrorString(cudaGetLastError()));
+        }
+        // one-axis transforms: x lines are contiguous, z lines are nmx apart
+        AxisDftArgs xa{};
+        xa.nlines = (long long)nwf * nz; xa.nb = 1; xa.sa = nmx; xa.sb = 0; xa.se = 1; xa.L = nmx;
+        xa.dk = dkx; xa.tw = P<float2>(btwx);
+        AxisDftArgs za{};
+        za.nlines = (long long)nwf * nmx; za.nb = nmx; za.sa = (long long)nz * nmx; za.sb = 1; za.se = nmx; za.L = nz;
+        za.dk = dkz; za.tw = P<float2>(btwz);
+        struct Step { AxisDftArgs base; const DevBuf *in; DevBuf *out; int sign, mode; float scale; };
+        const Step steps[] = {
+            { xa, &bU, &bT, -1, 0, 1.f },                    // DFT_x(u)
+            { xa, &bT, &bX, +1, 1, 1.f / (float)nmx },       // u_x = IDFT_x(i kx .) / nkx
+            { xa, &bT, &bL, +1, 2, 1.f },                    // u_left  (wem.c:932-945)
+            { xa, &bT, &bR, +1, 3, 1.f },                    // u_right
+            { za, &bU, &bT, -1, 0, 1.f },                    // DFT_z(u)
+            { za, &bT, &bZ, +1, 1, 1.f / (float)nz },        // u_z = IDFT_z(i kz .) / nkz
+        };
+        for (const Step &sp : steps) {
+            AxisDftArgs d = sp.base;
+            d.in = reinterpret_cast<const float2 *>(sp.in->p);
+            d.out = reinterpret_cast<float2 *>(sp.out->p);
+            d.sign = sp.sign; d.mode = sp.mode; d.scale = sp.scale;
+            if (launch_axis_dft(d, st)) {
+                release();
+                return fail(WEM_ERR_CUDA, "angles: axis transform launch: %s", cudaGetErrorString(cudaGetLastError()));
+            }
+        }
+        AngleAccumArgs ac{};
+        ac.nmx = nmx; ac.nz = nz; ac.nwf = nwf; ac.nw = nw; ac.nfreq_div = ifmax - ifmin + 1;
+        ac.u = P<float2>(bU); ac.ux = P<float2>(bX); ac.uz = P<float2>(bZ); ac.ul = P<float2>(bL); ac.ur = P<float2>(bR);
+        ac.angx = P<float>(bang); ac.angy = P<float>(bang) + n;
+        if (launch_angles_accum(ac, st)) {
+            release();
+            return fail(WEM_ERR_CUDA, "angles: accumulation launch: %s", cudaGetErrorString(cudaGetLastError()));
+        }
+        kernels += 8;
+        CKR(cudaMemcpyAsync(angx + (size_t)s * n, bang.p, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+        if (angy)
+            CKR(cudaMemcpyAsync(angy + (size_t)s * n, P<float>(bang) + n, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+        CKR(cudaStreamSynchronize(st));  // bang is reused by the next shot
+    }
+    CKR(cudaEventRecord(c->ev1, st));
+    CKR(cudaStreamSynchronize(st));
+#undef CKR
+    release();
+    cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
+    c->last_kernels = kernels;
+    return WEM_OK;
 }
 
 extern "C" int wem_migrate_survey(wem_ctx *c, const wem_params *p, const float *vel, const float *wav, int nshot,

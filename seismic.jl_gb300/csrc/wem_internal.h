@@ -96,6 +96,34 @@ int m3d_launch_init(const Mig3dArgs &a, cudaStream_t st);
 
 // host-side launchers (wem_kernels.cu). `wide` selects the 512-thread CTA shape of
 // the migration kernel (2S rows sharing the phase tables) over the 256-thread one.
+// source-side incidence angles (wem_angles.cu), 2-D
+struct AngleArgs {
+    int nmx, nz, nwf, ifmin, igx;
+    float dw, dz, oz, sz, dkx, inv_sqrt_n;  // inv_sqrt_n = 1/sqrtf(nkx)
+    const float *po;       // [nz] mean slowness
+    const float *pd;       // [nz][nmx] slowness perturbation
+    const float *taper;    // [nmx] boundary_condition weights
+    const float2 *srcw;    // [nwf] source spectrum / sqrt(ntfft) over the band
+    const float2 *twx;     // [nmx] e^{-2 pi i k / nmx}
+    float2 *u;             // [nwf][nz][nmx] source wavefield
+};
+struct AxisDftArgs {
+    const float2 *in;
+    float2 *out;
+    long long nlines, nb, sa, sb, se;  // line l starts at (l / nb) * sa + (l % nb) * sb, elements se apart
+    int L, sign, mode;                 // mode: 0 none, 1 i k, 2 i k (upper half), 3 i k (lower half)
+    float dk, scale;
+    const float2 *tw;                  // [L] e^{-2 pi i m / L}
+};
+struct AngleAccumArgs {
+    int nmx, nz, nwf, nw, nfreq_div;
+    const float2 *u, *ux, *uz, *ul, *ur;  // [nwf][nz][nmx]
+    float *angx, *angy;                   // [nmx][nz]
+};
+int launch_angles_extrap(const AngleArgs &a, cudaStream_t st);
+int launch_axis_dft(const AxisDftArgs &a, cudaStream_t st);
+int launch_angles_accum(const AngleAccumArgs &a, cudaStream_t st);
+
 // tc = 1: the split16 (tensor-core) form of the depth kernel, built for nkx = 2048 only
 int migrate_config(int nkx, int wide, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem,
                    int tc = 0);

@@ -158,6 +158,22 @@ class Context:
         L.check(L.lib().wem_last_kernel_times(self._h, C.byref(a), C.byref(b), C.byref(c)))
         return a.value, b.value, c.value
 
+    def angles(self, params, vel: np.ndarray, wav: np.ndarray, sx, sy=None):
+        """Source-side incidence angles of the shots at sx (compute_angles, wem.c:566-684)
+        on the grid of params (no prepare needed; any nmx, nz): (angx, angy), each
+        [nshot, nmx*nmy, nz] float32."""
+        p = params if isinstance(params, L.Params) else make_params(**params)
+        vel = np.ascontiguousarray(vel, dtype=np.float32)
+        wav = np.ascontiguousarray(np.asarray(wav, np.float32).reshape(-1))
+        sx = np.ascontiguousarray(np.atleast_1d(sx), dtype=np.float32)
+        sy = np.ascontiguousarray(np.zeros_like(sx) if sy is None else np.atleast_1d(sy), dtype=np.float32)
+        ax = np.empty((len(sx), p.nmx * p.nmy, p.nz), np.float32)
+        ay = np.empty_like(ax)
+        L.check(L.lib().wem_angles(self._h, C.byref(p), vel.ctypes.data_as(_f32p), wav.ctypes.data_as(_f32p),
+                                   len(sx), sx.ctypes.data_as(_f32p), sy.ctypes.data_as(_f32p),
+                                   ax.ctypes.data_as(_f32p), ay.ctypes.data_as(_f32p)))
+        return ax, ay
+
     def last_launch(self) -> dict:
         """How the last 2-D migration ran: threads per CTA, shots per CTA, grid, whether
         it replayed the captured CUDA graph and whether it timed the CTA shapes first."""

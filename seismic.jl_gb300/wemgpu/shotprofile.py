@@ -76,6 +76,134 @@ def image_headers(g: dict, dz: float):
     return h
 
 
+# --------------------------------------------------------------------------- angles
+
+def ComputeAngles(angx: str, angy: str, dip_flag=False, vel="vel", wav="wav", sz=0.0, fmin=0, fmax=80,
+                  verbose=False, sx=(0.0,), sy=(0.0,), dipx="dipx", dipy="dipy", device=0,
+                  ctx: Context | None = None):
+    """Source-side incidence angles of every shot into the seis files angx and angy:
+    Seismic.jl's ComputeAngles (src/Imaging/ComputeAngles.jl:55-100) over the GPU's
+    wem_angles (compute_angles, src/Imaging/c/wem.c:566-684). Each shot's section has the
+    velocity's trace headers with sx set (compute_angles.c:66-69); sections follow each
+    other in shot order. dip_flag adds the dip sections of dipx/dipy
+    (compute_angles.c:83-96)."""
+    velv, hv, g = grid_from_velocity(vel)
+    w, hw, ew = seis.read(wav)
+    nt, dt, ot = int(hw[0]["n1"]), float(hw[0]["d1"]), float(hw[0]["o1"])
+    sx = [float(v) for v in np.atleast_1d(sx)]
+    sy = [float(v) for v in np.atleast_1d(sy)]
+    if len(sy) == 1 and len(sx) > 1:
+        sy = sy * len(sx)
+    params = dict(nt=nt, ot=ot, dt=dt, nmx=g["nmx"], omx=g["omx"], dmx=g["dmx"], nmy=g["nmy"], omy=g["omy"],
+                  dmy=g["dmy"], nz=g["nz"], oz=g["oz"], dz=g["dz"], sz=sz, fmin=fmin, fmax=fmax,
+                  verbose=int(bool(verbose)))
+    own = ctx is None
+    ctx = ctx or Context(device)
+    try:
+        ax, ay = ctx.angles(params, velv, w[0], sx, sy)
+    finally:
+        if own:
+            ctx.close()
+    if dip_flag:
+        ax = ax + seis.read(dipx)[0][None]
+        ay = ay + seis.read(dipy)[0][None]
+    n = g["nmx"] * g["nmy"]
+    hs = []
+    for i, x0 in enumerate(sx):
+        h = hv.copy()
+        h["sx"] = x0
+        h["tracenum"] = np.arange(1, n + 1) + i * n
+        hs.append(h)
+    hh = np.concatenate(hs)
+    ext = ([g["nz"], g["nmx"], g["nmy"], 1, 1], [g["oz"], g["omx"], g["omy"], 0.0, 0.0],
+           [g["dz"], g["dmx"], g["dmy"], 1.0, 1.0])
+    seis.write(angx, ax.reshape(len(sx) * n, g["nz"]), hh, *ext)
+    seis.write(angy, ay.reshape(len(sx) * n, g["nz"]), hh, *ext)
+    return ax, ay
+
+
+def angle_bins(ax, ay, nangx, oangx, dangx, nangy, oangy, dangy):
+    """Bins and bilinear weights of every sample's angles (ShotProfileWEM.jl:161-176)."""
+    ax = np.asarray(ax, np.float64)
+    ay = np.asarray(ay, np.float64)
+    iangx = np.floor((ax - oangx) / dangx).astype(np.int64) + 1
+    iangy = np.floor((ay - oangy) / dangy).astype(np.int64) + 1
+    angx1 = (iangx - 1) * dangx + oangx
+    angx2 = angx1 + dangx
+    angy1 = (iangy - 1) * dangy + oangy
+    angy2 = angy1 + dangy
+    den = (angx2 - angx1) * (angy2 - angy1)
+    w1 = (angx2 - ax) * (angy2 - ay) / den
+    w2 = (ax - angx1) * (angy2 - ay) / den
+    w3 = (angx2 - ax) * (ay - angy1) / den
+    w4 = (ax - angx1) * (ay - angy1) / den
+    valid = (iangx >= 1) & (iangx <= nangx) & (iangy >= 1) & (iangy <= nangy)
+    return iangx, iangy, (w1, w2, w3, w4), valid
+
+
+def _bin_terms(iangx, iangy, w, valid, nangx, nangy):
+    """(weight, bin index, mask) of the four bilinear terms; the last term's guard is
+    iangx < nangx (ShotProfileWEM.jl:264-266; the adjoint side's `iang < nang` names no
+    defined variable, :183, and is read as the same guard)."""
+    b1 = (iangx - 1) * nangy + (iangy - 1)
+    terms = [(w[0], b1, valid), (w[1], b1 + nangy, valid & (iangx < nangx))]
+    if nangy > 1:
+        terms += [(w[2], b1 + 1, valid), (w[3], b1 + nangy + 1, valid & (iangx < nangx))]
+    return terms
+
+
+def bin_shot(img, ax, ay, out, nangx, oangx, dangx, nangy, oangy, dangy):
+    """Adds one shot's image [n, nz] into the angle gathers out [n, nangx*nangy, nz]
+    (ShotProfileWEM.jl:155-188)."""
+    iangx, iangy, w, valid = angle_bins(ax, ay, nangx, oangx, dangx, nangy, oangy, dangy)
+    n, nz = img.shape
+    cell = np.repeat(np.arange(n), nz).reshape(n, nz)
+    z = np.tile(np.arange(nz), n).reshape(n, nz)
+    for wk, b, ok in _bin_terms(iangx, iangy, w, valid, nangx, nangy):
+        np.add.at(out, (cell[ok], b[ok], z[ok]), wk[ok] * img[ok])
+    return out
+
+
+def unbin_shot(gath, ax, ay, nangx, oangx, dangx, nangy, oangy, dangy):
+    """One shot's image [n, nz] from the angle gathers gath [n, nangx*nangy, nz] at its
+    own incidence angles (ShotProfileWEM.jl:246-270)."""
+    iangx, iangy, w, valid = angle_bins(ax, ay, nangx, oangx, dangx, nangy, oangy, dangy)
+    n, nb, nz = gath.shape
+    cell = np.repeat(np.arange(n), nz).reshape(n, nz)
+    z = np.tile(np.arange(nz), n).reshape(n, nz)
+    img = np.zeros((n, nz))
+    for wk, b, ok in _bin_terms(iangx, iangy, w, valid, nangx, nangy):
+        bb = np.clip(b, 0, nb - 1)
+        img += np.where(ok, wk * gath[cell, bb, z], 0.0)
+    return img
+
+
+def _shot_angles(name: str, x0: float, y0: float, n: int, nz: int) -> np.ndarray:
+    """The section of the shot at (x0, y0) in an angle file written by ComputeAngles
+    (SeisWindow by sx, sy: ShotProfileWEM.jl:93-97)."""
+    a, h, e = seis.read(name)
+    sel = np.nonzero((h["sx"] == np.float32(x0)) & (h["sy"] == np.float32(y0)))[0]
+    if len(sel) != n:
+        raise ValueError(f"{name}: {len(sel)} traces for the shot at sx={x0}, sy={y0}, need {n}")
+    return a[sel].reshape(n, nz)
+
+
+def gather_headers(g: dict, dz: float, nangx, oangx, dangx, nangy, oangy, dangy):
+    """Trace headers of the angle-gather image (ShotProfileWEM.jl:115-137): one trace per
+    (imx, imy, iangx, iangy), angles fastest."""
+    nb = nangx * nangy
+    base = image_headers(g, dz)
+    h = np.repeat(base, nb)
+    ia = np.tile(np.repeat(np.arange(nangx), nangy), len(base))
+    iz = np.tile(np.tile(np.arange(nangy), nangx), len(base))
+    h["tracenum"] = np.arange(1, len(h) + 1) + 1
+    h["iang"] = ia
+    h["ang"] = ia * dangx + oangx
+    h["iaz"] = iz
+    h["az"] = iz * dangy + oangy
+    return h
+
+
 def ShotProfileWEM(m: str, d: str, adj: bool = True, *, pspi=True, nref=5, damping=1000.0, vel="vel",
                    angx="angx", angy="angy", wav="wav", sz=0.0, gz=0.0, nangx=1, oangx=0, dangx=1, nangy=1,
                    oangy=0, dangy=1, fmin=0, fmax=80, padt=2, padx=2, verbose=False, sx=(0.0,), sy=(0.0,),
@@ -84,8 +212,8 @@ def ShotProfileWEM(m: str, d: str, adj: bool = True, *, pspi=True, nref=5, dampi
     image file m -> data file d) of the shots at (sx[i], sy[i]). Keyword names and
     defaults of ShotProfileWEM.jl:39; `damping` is accepted and unused, as there
     (shotwem.c never reads it)."""
-    if nangx != 1 or nangy != 1:
-        raise NotImplementedError("angle gathers (nangx, nangy > 1) are outside this path")
+    gathers = nangx != 1 or nangy != 1
+    abin = (nangx, float(oangx), float(dangx), nangy, float(oangy), float(dangy))
     velv, hv, g = grid_from_velocity(vel)
     w, hw, ew = seis.read(wav)
     nt, dt, ot = int(hw[0]["n1"]), float(hw[0]["d1"]), float(hw[0]["o1"])
@@ -101,6 +229,22 @@ def ShotProfileWEM(m: str, d: str, adj: bool = True, *, pspi=True, nref=5, dampi
     ctx = ctx or Context(device)
     try:
         ctx.prepare(params, velv, w[0])
+        n = g["nmx"] * g["nmy"]
+        if adj and gathers:
+            # angle gathers: every shot's image binned by its own incidence angles
+            data, hd, ed = seis.read(d)
+            out = np.zeros((n, nangx * nangy, g["nz"]))
+            for x0, y0 in zip(sx, sy):
+                img = ctx.migrate(window_shots(data, hd, [x0], [y0], g)).astype(np.float64)
+                ax = _shot_angles(angx, x0, y0, n, g["nz"])
+                ay = _shot_angles(angy, x0, y0, n, g["nz"])
+                bin_shot(img, ax, ay, out, *abin)
+            h = gather_headers(g, g["dz"], *abin)
+            seis.write(m, out.reshape(n * nangx * nangy, g["nz"]).astype(np.float32), h,
+                       [g["nz"], g["nmx"], g["nmy"], nangx, nangy], [g["oz"], g["omx"], g["omy"], oangx, oangy],
+                       [g["dz"], g["dmx"], g["dmy"], dangx, dangy],
+                       labels=["Depth", "mx", "my", "angx", "angy"], units=["m", "m", "m", "degrees", "degrees"])
+            return out
         if adj:
             data, hd, ed = seis.read(d)
             shots = window_shots(data, hd, sx, sy, g)
@@ -113,10 +257,22 @@ def ShotProfileWEM(m: str, d: str, adj: bool = True, *, pspi=True, nref=5, dampi
             return image
         # demigration: every shot recorded on every grid cell (ShotProfileWEM.jl:210-309)
         img, hm, em = seis.read(m)
-        n = g["nmx"] * g["nmy"]
         shots = Shots(np.asarray(sx, np.float32), np.asarray(sy, np.float32), np.arange(len(sx) + 1, dtype=np.int64) * n,
                       np.tile(np.arange(n, dtype=np.int32), len(sx)), np.zeros((0, nt), np.float32))
-        data = ctx.model(shots, img[:n], exact=False)
+        if gathers:
+            # each shot sees the gathers at its own incidence angles (ShotProfileWEM.jl:228-270)
+            gath = img.reshape(n, nangx * nangy, g["nz"]).astype(np.float64)
+            parts = []
+            for i, (x0, y0) in enumerate(zip(sx, sy)):
+                ax = _shot_angles(angx, x0, y0, n, g["nz"])
+                ay = _shot_angles(angy, x0, y0, n, g["nz"])
+                im = unbin_shot(gath, ax, ay, *abin).astype(np.float32)
+                one = Shots(shots.sx[i:i + 1], shots.sy[i:i + 1], np.array([0, n], np.int64),
+                            np.arange(n, dtype=np.int32), np.zeros((0, nt), np.float32))
+                parts.append(ctx.model(one, im, exact=False))
+            data = np.concatenate(parts)
+        else:
+            data = ctx.model(shots, img[:n], exact=False)
         hd = seis.empty_headers(len(sx) * n)
         mx = g["omx"] + g["dmx"] * np.repeat(np.arange(g["nmx"]), g["nmy"])
         my = g["omy"] + g["dmy"] * np.tile(np.arange(g["nmy"]), g["nmx"])

@@ -92,5 +92,30 @@ def main():
         print("main() image norm", float(np.linalg.norm(m_main)))
 
 
+ANGLE_CASES = {
+    # name: (seed, nx, nz, nt, fmax); nx > 100 switches the reference's taper on
+    "angles_64": (31, 64, 24, 64, 40.0),
+    "angles_128": (32, 128, 16, 64, 30.0),
+}
+
+
+def angles_main():
+    """compute_angles() of the reference (wem.c:566-684), one shot per case. Run in a
+    process with OMP_NUM_THREADS=1: the reference's frequency loop adds into shared
+    arrays from every thread without synchronisation."""
+    for name, (seed, nx, nz, nt, fmax) in ANGLE_CASES.items():
+        c = synth.small_case(seed, nx=nx, nz=nz, nt=nt, nshot=1, pspi=0, fmax=fmax)
+        p = dict(c["params"], sx=float(c["shots"].sx[0]))
+        ax, ay = O.angles_ref(p, c["vel"], c["wav"])
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), vel=c["vel"], wav=c["wav"], angx=ax, angy=ay,
+                            params=np.array(repr(p)))
+        print(name, "angx range", float(ax.min()), float(ax.max()), "angy max", float(np.abs(ay).max()))
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["angles"]:
+        angles_main()
+    else:
+        main()
+        subprocess.run([sys.executable, os.path.abspath(__file__), "angles"], check=True,
+                       env=dict(os.environ, OMP_NUM_THREADS="1"))

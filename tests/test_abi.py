@@ -17,8 +17,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "shotwem_gb300.h")
 
 
-def declared_functions():
-    src = open(HEADER).read()
+def declared_functions(header=HEADER):
+    src = open(header).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     names = re.findall(r"^\s*(?:WEM_API\s+)?(?:const\s+)?\w+\s*\*?\s*(\w+)\s*\(", src, flags=re.M)
     return sorted(set(n for n in names if n not in ("if", "while")))
@@ -34,6 +34,21 @@ def test_library_exports_every_declared_symbol(gpu_lib):
     lib = C.CDLL(gpu_lib.LIB_PATH)
     for name in declared_functions() + ["main"]:
         assert hasattr(lib, name), f"shotwem.so does not export {name}"
+
+
+def test_compute_angles_library_exports_its_entry_points(gpu_lib):
+    """compute_angles.so (the drop-in for the reference's compute_angles library) exports
+    main and what include/compute_angles_gb300.h declares, and reports a missing key as
+    a status (compute_angles.c:27-33 calls exit(1))."""
+    path = os.path.join(os.path.dirname(gpu_lib.LIB_PATH), "compute_angles.so")
+    lib = C.CDLL(path)
+    names = declared_functions(os.path.join(ROOT, "include", "compute_angles_gb300.h"))
+    assert names == ["compute_angles_main"]
+    for name in names + ["main"]:
+        assert hasattr(lib, name)
+    lib.main.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+    argv = (C.c_char_p * 2)(b"0", b"angx=a")
+    assert lib.main(2, argv) == gpu_lib._lib.WEM_ERR_ARG
 
 
 def _has_gpu():

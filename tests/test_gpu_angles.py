@@ -1,0 +1,78 @@
+"""Source-side incidence angles on the GPU (wem_angles, the reference's compute_angles,
+src/Imaging/c/wem.c:566-992) against the reference's own output (golden vectors) and
+the oracle's FP64 restatement (oracle/angles_np.py).
+
+Tolerance: relative L2 <= 1e-4 over the angle section, and no grid point whose sign
+(the side the source energy arrives from) differs.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+def _angles(gpu_lib, p, vel, wav, sx):
+    with gpu_lib.Context() as ctx:
+        return ctx.angles(p, vel, wav, sx)
+
+
+@pytest.mark.parametrize("case", ["angles_64", "angles_128"])
+def test_angles_match_reference_golden(gpu_lib, case):
+    g = load_golden(f"{case}.npz")
+    p = g["params"]
+    ax, ay = _angles(gpu_lib, p, g["vel"], g["wav"], [p["sx"]])
+    ref = g["angx"]
+    assert rel_l2(ax[0], ref) < TOL, rel_l2(ax[0], ref)
+    assert np.count_nonzero(np.sign(ax[0]) != np.sign(ref)) == 0
+    assert np.all(ay == 0) and np.all(g["angy"] == 0)
+
+
+def test_angles_any_depth_count_matches_fp64_oracle(gpu_lib):
+    """nz = 100 and nmx = 250 (direct transforms of any length), source off centre, a
+    source depth below the surface, several shots in one call."""
+    import angles_np as A
+    from wemgpu import synth
+    c = synth.small_case(33, nx=250, nz=100, nt=128, nshot=1, pspi=0, fmax=25.0)
+    p = dict(c["params"], sz=50.0)
+    sxs = [600.0, 1800.0]
+    ax, _ = _angles(gpu_lib, p, c["vel"], c["wav"], sxs)
+    for i, s in enumerate(sxs):
+        want, _ = A.compute_angles(dict(p, sx=s), c["vel"], c["wav"])
+        assert rel_l2(ax[i], want) < TOL, rel_l2(ax[i], want)
+        assert np.count_nonzero(np.sign(ax[i]) != np.sign(want)) == 0
+        assert np.all(ax[i][:, :5] == 0)  # above the source depth (sz = 50 m, dz = 10 m)
+
+
+def test_angles_reject_3d(gpu_lib):
+    from wemgpu import synth
+    from wemgpu._lib import WemError
+    c = synth.small_case3d(34, nx=32, ny=32, nz=8, nt=64, pspi=0)
+    with gpu_lib.Context() as ctx:
+        with pytest.raises(WemError) as e:
+            ctx.angles(c["params"], c["vel"], c["wav"], [float(c["shots"].sx[0])])
+    assert e.value.code == -2
+
+
+def test_compute_angles_main_on_seis_files(gpu_lib, tmp_path):
+    """main of compute_angles.so (compute_angles.c:12-120) on seis files against the
+    reference's compute_angles() output."""
+    import ctypes as C
+    import os
+    from wemgpu import seis
+    g = load_golden("angles_64.npz")
+    p = g["params"]
+    t = str(tmp_path)
+    seis.write_grid(t + "/vel", g["vel"], o1=0.0, d1=p["dz"], ox=p["omx"], dx=p["dmx"])
+    seis.write_wavelet(t + "/wav", g["wav"], dt=p["dt"])
+    lib = C.CDLL(os.path.join(os.path.dirname(gpu_lib.LIB_PATH), "compute_angles.so"))
+    lib.main.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+    args = ["0", f"angx={t}/ax", f"angy={t}/ay", f"vel={t}/vel", f"wav={t}/wav", f"dipx={t}/none",
+            f"dipy={t}/none", f"sx={p['sx']}", "sy=0", "sz=0", f"fmin={p['fmin']}", f"fmax={p['fmax']}"]
+    argv = (C.c_char_p * len(args))(*[a.encode() for a in args])
+    assert lib.main(len(args), argv) == 0
+    ax, hx, ex = seis.read(t + "/ax")
+    assert rel_l2(ax, g["angx"]) < TOL
+    assert np.all(hx["sx"] == np.float32(p["sx"])) and ex["n"][:2] == [p["nz"], p["nmx"]]

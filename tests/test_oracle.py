@@ -125,3 +125,16 @@ def test_fp64_adjoint_pair_dot_test(oracle_mod):
     Ltd = oracle_mod.wem_fp64(p, g["vel"], g["wav"], d=d, adj=True, nthreads=2)
     a, b = float(np.sum(d * Lm)), float(np.sum(Ltd * m))
     assert np.isfinite(a) and np.isfinite(b)
+
+
+@pytest.mark.parametrize("case", ["angles_64", "angles_128"])
+def test_angle_oracle_matches_reference_golden(case):
+    """The FP64 restatement of compute_angles (oracle/angles_np.py) against the
+    reference's own compute_angles() output (wem.c:566-992, run single-threaded)."""
+    import angles_np as A
+    g = load_golden(f"{case}.npz")
+    ax, ay = A.compute_angles(g["params"], g["vel"], g["wav"])
+    assert rel_l2(ax, g["angx"]) < 1e-4
+    assert np.count_nonzero(np.sign(ax) != np.sign(g["angx"])) == 0
+    assert np.all(ay == 0) and np.all(g["angy"] == 0)
+    assert np.abs(g["angx"]).max() > 30.0  # a real angle section, not zeros

@@ -76,3 +76,53 @@ def test_shotprofile_migration_and_demigration_on_files(gpu_lib, oracle_mod, tmp
         w = oracle_mod.wem_port(dict(p, sx=x0), c["vel"], c["wav"], m=m, adj=False)
         assert rel_l2(dm[s * p["nmx"]:(s + 1) * p["nmx"]], w) < 1e-4
         assert np.all(hd["sx"][s * p["nmx"]:(s + 1) * p["nmx"]] == np.float32(x0))
+
+
+def test_angle_binning_weights_and_adjoint():
+    """Bilinear binning of ShotProfileWEM.jl:155-188 and its forward counterpart
+    (:246-270) are adjoint to each other, and the weights of one sample add up to 1
+    where both neighbouring bins exist."""
+    from wemgpu import shotprofile as S
+    rng = np.random.default_rng(5)
+    n, nz = 7, 9
+    spec = (6, -60.0, 20.0, 1, 0.0, 1.0)
+    ax = rng.uniform(-59.0, 39.0, (n, nz))  # bins 1..5: the upper neighbour always exists
+    ay = np.zeros((n, nz))
+    img = rng.standard_normal((n, nz))
+    out = S.bin_shot(img, ax, ay, np.zeros((n, 6, nz)), *spec)
+    assert np.allclose(out.sum(axis=1), img)  # every sample lands in bins iangx < nangx
+    g = rng.standard_normal((n, 6, nz))
+    assert np.isclose(np.vdot(out, g), np.vdot(img, S.unbin_shot(g, ax, ay, *spec)))
+    # one sample by hand: angle 5 deg, bins of 20 from -60: bin 4 (-0..) gets 0.75, bin 5 0.25
+    one = S.bin_shot(np.ones((1, 1)), np.array([[5.0]]), np.zeros((1, 1)), np.zeros((1, 6, 1)), *spec)
+    assert np.allclose(one[0, :, 0], [0, 0, 0, 0.75, 0.25, 0])
+
+
+@pytest.mark.gpu
+def test_compute_angles_and_angle_gathers_on_files(gpu_lib, tmp_path):
+    """ComputeAngles on seis files (one section per shot, headers with sx), then
+    ShotProfileWEM with angle bins: the gathers summed over the bins give the stacked
+    image, and demigration from the gathers runs shot by shot."""
+    import angles_np as A
+    from wemgpu import seis, synth, shotprofile
+    c = synth.small_case(123, nx=64, nz=16, nt=128, nshot=2, pspi=1, nref=3)
+    p = c["params"]
+    _write_survey(str(tmp_path), c)
+    sx = [float(v) for v in c["shots"].sx]
+    t = str(tmp_path)
+    shotprofile.ComputeAngles(t + "/angx", t + "/angy", vel=t + "/vel", wav=t + "/wav", fmin=p["fmin"],
+                              fmax=p["fmax"], sx=sx, sy=[0.0] * len(sx))
+    a, ha, ea = seis.read(t + "/angx")
+    assert a.shape == (2 * p["nmx"], p["nz"]) and list(np.unique(ha["sx"])) == sorted(np.float32(sx))
+    want, _ = A.compute_angles(dict(p, sx=sx[1]), c["vel"], c["wav"])
+    assert rel_l2(a[p["nmx"]:], want) < 1e-4
+    kw = dict(pspi=True, nref=p["nref"], vel=t + "/vel", wav=t + "/wav", angx=t + "/angx", angy=t + "/angy",
+              fmin=p["fmin"], fmax=p["fmax"], padt=p["padt"], padx=p["padx"], sx=sx, sy=[0.0] * len(sx))
+    spec = dict(nangx=7, oangx=-90.0, dangx=30.0)
+    gath = shotprofile.ShotProfileWEM(t + "/mg", t + "/d", True, **kw, **spec)
+    stack = shotprofile.ShotProfileWEM(t + "/m", t + "/d", True, **kw)
+    assert rel_l2(gath.sum(axis=1), stack) < 1e-5
+    mg, hg, eg = seis.read(t + "/mg")
+    assert eg["n"][:4] == [p["nz"], p["nmx"], 1, 7] and list(hg["ang"][:7]) == [-90, -60, -30, 0, 30, 60, 90]
+    dd = shotprofile.ShotProfileWEM(t + "/mg", t + "/dg", False, **kw, **spec)
+    assert dd.shape == (2 * p["nmx"], p["nt"]) and np.all(np.isfinite(dd)) and np.any(dd)
