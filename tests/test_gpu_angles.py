@@ -42,8 +42,11 @@ def test_angles_any_depth_count_matches_fp64_oracle(gpu_lib):
     for i, s in enumerate(sxs):
         want, _ = A.compute_angles(dict(p, sx=s), c["vel"], c["wav"])
         assert rel_l2(ax[i], want) < TOL, rel_l2(ax[i], want)
-        assert np.count_nonzero(np.sign(ax[i]) != np.sign(want)) == 0
-        assert np.all(ax[i][:, :5] == 0)  # above the source depth (sz = 50 m, dz = 10 m)
+        # signs wherever the angle is not zero (above the source the oracle's 3-D transforms
+        # leave round-off of 1e-13 degrees where the separable ones give exact zeros)
+        live = np.abs(want) > 1e-6
+        assert np.count_nonzero(np.sign(ax[i][live]) != np.sign(want[live])) == 0
+        assert np.all(ax[i][:, :5] == 0) and np.abs(want[:, :5]).max() < 1e-9  # above sz = 50 m
 
 
 def test_angles_reject_3d(gpu_lib):
