@@ -115,8 +115,10 @@ def ComputeAngles(angx: str, angy: str, dip_flag=False, vel="vel", wav="wav", sz
         h["tracenum"] = np.arange(1, n + 1) + i * n
         hs.append(h)
     hh = np.concatenate(hs)
-    ext = ([g["nz"], g["nmx"], g["nmy"], 1, 1], [g["oz"], g["omx"], g["omy"], 0.0, 0.0],
-           [g["dz"], g["dmx"], g["dmy"], 1.0, 1.0])
+    # one section per shot along the 4th axis, so that the file's extent counts every trace
+    ns = len(sx)
+    ext = ([g["nz"], g["nmx"], g["nmy"], ns, 1], [g["oz"], g["omx"], g["omy"], sx[0], 0.0],
+           [g["dz"], g["dmx"], g["dmy"], (sx[1] - sx[0]) if ns > 1 else 1.0, 1.0])
     seis.write(angx, ax.reshape(len(sx) * n, g["nz"]), hh, *ext)
     seis.write(angy, ay.reshape(len(sx) * n, g["nz"]), hh, *ext)
     return ax, ay
