@@ -53,6 +53,10 @@ def survey(workload: str, rank: int):
         c["params"] = dict(c["params"], interp="linear")
         wl = ("2-D least-squares PSPI migration: 32 shots, 300x512 grid @10 m, nref=8, 5-45 Hz, nt=1500, "
               "20 CG iterations over the exact modelling/migration pair")
+    elif workload == "angles8":
+        c = synth.config1(seed=1001 + rank, nshot=8)
+        wl = ("2-D source incidence angles (compute_angles): 8 shots, 500x1024 grid @10 m, 5-50 Hz of the "
+              "unpadded 1500-sample axis")
     elif workload == "split1":
         c = synth.config0(seed=1000 + rank)
         wl = "2-D split-step: 1 shot, 200x256 grid @10 m, 3 layers, 5-60 Hz, nt=1000, padx=padt=2"
@@ -269,6 +273,62 @@ def run_reference_arm(args):
     return 0
 
 
+def run_angles(args, c, wl, rank, world, local):
+    """Source-side incidence angles of every shot (wem_angles; the reference's
+    compute_angles, wem.c:566-992). A unit is one shot * frequency * depth step of the
+    angle computation (frequencies of the unpadded time axis). One step = all shots."""
+    import torch
+    import wemgpu
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    p, shots = c["params"], c["shots"]
+    ctx = wemgpu.Context(local)
+    sx = np.asarray(shots.sx, np.float32)
+    nt, dt = int(p["nt"]), float(p["dt"])
+    nf = band(dict(p, padt=1))
+    units = len(sx) * nf * int(p["nz"])
+    for _ in range(args.warmup):
+        ctx.angles(p, c["vel"], c["wav"], sx)
+    sampler = ClockSampler(local)
+    torch.cuda.synchronize()
+    sampler.start()
+    dev_ms, wall = [], []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        ax, ay = ctx.angles(p, c["vel"], c["wav"], sx)
+        wall.append(time.perf_counter() - t0)
+        dev_ms.append(ctx.last_timing()[0])
+    clocks = sampler.stop()
+    ms = statistics.mean(dev_ms)
+    line = {"metric": "shot*omega*depth-steps/s", "value": world * units / (ms / 1000.0),
+            "unit": "shot*omega*depth-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": {"workload": wl, "units_per_step_per_gpu": units, "shots": len(sx), "frequencies": nf,
+                       "depth_steps": int(p["nz"]), "l2": "inputs larger than L2 (wavefields of every frequency)"},
+            "e2e": {"value": world * units / statistics.mean(wall), "unit": "shot*omega*depth-steps/s",
+                    "h2d_bytes_per_step": int(c["vel"].nbytes + c["wav"].nbytes),
+                    "d2h_bytes_per_step": int(ax.nbytes + ay.nbytes)},
+            "clocks": clocks}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # the CPU leg: the oracle's FP64 restatement of compute_angles on one shot, 2 Hz of the band
+        import angles_np as A
+        q = dict(p, sx=float(sx[len(sx) // 2]), fmax=float(p["fmin"]) + 2.0)
+        nq = band(dict(q, padt=1))
+        t0 = time.perf_counter()
+        want, _ = A.compute_angles(q, c["vel"], c["wav"])
+        el = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": nq * int(p["nz"]) / el, "unit": "shot*omega*depth-steps/s", "cores": 1,
+                                "kind": "port", "sample": f"1 shot, {nq} frequencies x {p['nz']} depth steps in {el:.1f} s "
+                                                          "(NumPy FP64 restatement, one thread)"}
+        got, _ = ctx.angles(q, c["vel"], c["wav"], [q["sx"]])
+        line["accuracy"] = {"rel_l2_vs_fp64": float(np.linalg.norm(got[0] - want) / np.linalg.norm(want)),
+                            "sample": "the CPU leg's shot and band"}
+    if rank == 0:
+        print(json.dumps(line))
+    ctx.close()
+    return 0
+
+
 def run_lsm(args, ctx, c, wl, units, dev, rank, world, dist):
     """configs[4]: Born data of a seeded reflectivity (1 % of the cells, N(0,1)), then CG
     (Scales 1987) from zero over wem_model(exact) / wem_migrate. One step = one CG solve."""
@@ -322,7 +382,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="survey64", choices=["survey64", "survey8", "survey3d", "split1", "lsm32"])
+    ap.add_argument("--workload", default="survey64",
+                    choices=["survey64", "survey8", "survey3d", "split1", "lsm32", "angles8"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split16"],
@@ -349,6 +410,8 @@ def main():
     if not os.path.exists(wemgpu.LIB_PATH):
         raise SystemExit("shotwem.so is not built: python -c 'import __graft_entry__ as g; g.build()'")
     c, wl = survey(args.workload, rank)
+    if args.workload == "angles8":
+        return run_angles(args, c, wl, rank, world, local)
     if args.precision != "fp32":
         c["params"] = dict(c["params"], precision=args.precision)
         wl += f" [{args.precision}: DFT stages on the tensor cores, split fp16 hi+lo operands, fp32 accumulation]"

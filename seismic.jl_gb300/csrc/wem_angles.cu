@@ -14,6 +14,9 @@
 //      one-axis transforms per frequency instead of one forward and seven inverse 3-D ones.
 //      The axes have any length (nz is rarely a power of two), so each transform is a
 //      tiled direct DFT (a complex matrix product against W^{ik}, the table built in FP64).
+//   When nmx is a power of two in [32, 2048] steps 1 and the x transforms of 2 run on the
+//   register-resident row FFT of wem_fft.cuh instead (wem_angles_extrap_fft_kernel,
+//   wem_angles_xderiv_fft_kernel); the z transforms stay direct (nz is any length).
 //   3. wem_angles_accum_kernel: per grid point, in frequency order,
 //      ang += (180/pi) atan(|u_x| / (|u_z| + 1e-10)) and sign += +-|u| / nw, then
 //      ang *= sign(sign) / (ifmax - ifmin + 1) (wem.c:675-676, 735-754).
@@ -22,7 +25,9 @@
 #include <math.h>
 #include <stdint.h>
 
+#include "wem_fft.cuh"
 #include "wem_internal.h"
+#include "wem_step.cuh"
 
 namespace gbwem {
 
@@ -114,6 +119,112 @@ __global__ void __launch_bounds__(512) wem_angles_extrap_kernel(const AngleArgs 
         float2 *t = d;  // the new row is in x
         d = x;
         x = t;
+    }
+}
+
+// ------------------------------------------------------------------ 1'. FFT rows
+// One team of N/16 threads per frequency: the same recursion with the row in registers.
+template <int N>
+__global__ void __launch_bounds__(N / 16 < 32 ? 32 : N / 16) wem_angles_extrap_fft_kernel(const AngleArgs a)
+{
+    constexpr int T = N / 16, TW = fft_tw_size<N>(), TWP = (TW + 1) & ~1;
+    __shared__ float2 s_tw[TWP > 0 ? TWP : 2];
+    __shared__ float2 s_x[pad16(N)];
+    const int t = threadIdx.x;
+    if (t >= T) return;  // T < 32: the rest of the warp idles
+    const unsigned sync = team_sync_handle<N>(t);
+    for (int i = t; i < TW; i += T) s_tw[i] = a.twx[i];
+    team_sync<T>(sync);
+    const int f = blockIdx.x;
+    const float w = __fmul_rn((float)(a.ifmin + f), a.dw);
+    const float dzs = -a.dz;
+    float2 v[16];
+#pragma unroll
+    for (int m = 0; m < 16; m++) v[m] = (t + T * m) == a.igx ? a.srcw[f] : make_float2(0.f, 0.f);
+    for (int iz = 0; iz < a.nz; iz++) {
+        float2 *urow = a.u + ((size_t)f * a.nz + iz) * N;
+        const float z = __fadd_rn(a.oz, __fmul_rn(a.dz, (float)iz));
+        if (!(z >= a.sz)) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) urow[t + T * m] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const float *pdr = a.pd + (size_t)iz * N;
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            const float tp = a.taper[x];
+            float sn, cs;
+            sincosf(__fmul_rn(__fmul_rn(w, pdr[x]), dzs), &sn, &cs);
+            v[m] = c_mul(make_float2(v[m].x * tp, v[m].y * tp), make_float2(cs, sn));
+        }
+        fft_row<N, -1>(v, s_x, s_tw, t, sync);
+        const float po = a.po[iz];
+        const float wp = __fmul_rn(__fmul_rn(w, w), __fmul_rn(po, po));
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int k = t + T * m;
+            const float kx = axis_k(k, N, a.dkx);
+            const float s = __fsub_rn(wp, __fmul_rn(kx, kx));
+            float2 L;
+            if (s >= 0.f) {
+                float sn, cs;
+                sincosf(__fmul_rn(__fsqrt_rn(s), dzs), &sn, &cs);
+                L = make_float2(cs, sn);
+            } else {
+                L = make_float2(expf((float)(-0.2 * (double)__fsqrt_rn(fabsf(s)) * (double)fabsf(dzs))), 0.f);
+            }
+            const float2 q = c_mul(v[m], L);
+            v[m] = make_float2(q.x * a.inv_sqrt_n, q.y * a.inv_sqrt_n);
+        }
+        fft_row<N, +1>(v, s_x, s_tw, t, sync);
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            v[m] = make_float2(v[m].x * a.inv_sqrt_n, v[m].y * a.inv_sqrt_n);
+            urow[t + T * m] = v[m];
+        }
+    }
+}
+
+// The x derivatives of one row per team: X = FFT_x(u), then u_x = IFFT_x(i kx X) / N and
+// the unnormalised u_left, u_right (wem.c:838-856, 932-950). CTA of 256 threads.
+template <int N>
+__global__ void __launch_bounds__(256) wem_angles_xderiv_fft_kernel(const AngleXArgs a)
+{
+    constexpr int T = N / 16, TEAMS = 256 / T < 1 ? 1 : 256 / T, NT = TEAMS * T;
+    constexpr int TW = fft_tw_size<N>(), TWP = (TW + 1) & ~1;
+    extern __shared__ float4 smem_raw[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *s_x = s_tw + TWP;
+    const int tid = threadIdx.x, team = tid / T, t = tid - team * T;
+    float2 *xbuf = s_x + (size_t)team * pad16(N);
+    const unsigned sync = team_sync_handle<N>(tid);
+    for (int i = tid; i < TW; i += NT) s_tw[i] = a.twx[i];
+    __syncthreads();
+    for (long long l = (long long)blockIdx.x * TEAMS + team; l < a.nlines; l += (long long)gridDim.x * TEAMS) {
+        const float2 *in = a.u + (size_t)l * N;
+        float2 X[16];
+#pragma unroll
+        for (int m = 0; m < 16; m++) X[m] = in[t + T * m];
+        fft_row<N, -1>(X, xbuf, s_tw, t, sync);
+        float2 *outs[3] = { a.ux + (size_t)l * N, a.ul + (size_t)l * N, a.ur + (size_t)l * N };
+#pragma unroll 1
+        for (int mode = 1; mode <= 3; mode++) {
+            float2 u[16];
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int k = t + T * m;
+                float kx = axis_k(k, N, a.dkx);
+                if (mode == 2) kx = k <= N / 2 ? 0.f : kx;
+                if (mode == 3) kx = k <= N / 2 ? kx : 0.f;
+                u[m] = make_float2(-kx * X[m].y, kx * X[m].x);
+            }
+            fft_row<N, +1>(u, xbuf, s_tw, t, sync);
+            const float sc = mode == 1 ? 1.f / (float)N : 1.f;
+            float2 *o = outs[mode - 1];
+#pragma unroll
+            for (int m = 0; m < 16; m++) o[t + T * m] = make_float2(u[m].x * sc, u[m].y * sc);
+        }
     }
 }
 
@@ -223,6 +334,42 @@ int launch_angles_extrap(const AngleArgs &a, cudaStream_t st)
         return -1;
     wem_angles_extrap_kernel<<<a.nwf, 512, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N> static int launch_fft_paths(const AngleArgs &a, const AngleXArgs &x, int which, cudaStream_t st)
+{
+    constexpr int T = N / 16, TEAMS = 256 / T < 1 ? 1 : 256 / T;
+    constexpr int TWP = (fft_tw_size<N>() + 1) & ~1;
+    if (which == 0) {
+        wem_angles_extrap_fft_kernel<N><<<a.nwf, T < 32 ? 32 : T, 0, st>>>(a);
+    } else {
+        const size_t smem = sizeof(float2) * ((size_t)TWP + (size_t)TEAMS * pad16(N));
+        if (cudaFuncSetAttribute(wem_angles_xderiv_fft_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return -1;
+        long long blocks = (x.nlines + TEAMS - 1) / TEAMS;
+        if (blocks > 65535LL * 16) blocks = 65535LL * 16;
+        wem_angles_xderiv_fft_kernel<N><<<(unsigned)blocks, 256, smem, st>>>(x);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// up to 2048: the extrapolation kernel keeps its row buffers in static shared memory
+bool angles_fft_supported(int nmx) { return nmx >= 32 && nmx <= 2048 && (nmx & (nmx - 1)) == 0; }
+
+// which = 0: the extrapolation, 1: the x derivatives
+int launch_angles_fft(const AngleArgs &a, const AngleXArgs &x, int which, cudaStream_t st)
+{
+    switch (a.nmx) {
+    case 32: return launch_fft_paths<32>(a, x, which, st);
+    case 64: return launch_fft_paths<64>(a, x, which, st);
+    case 128: return launch_fft_paths<128>(a, x, which, st);
+    case 256: return launch_fft_paths<256>(a, x, which, st);
+    case 512: return launch_fft_paths<512>(a, x, which, st);
+    case 1024: return launch_fft_paths<1024>(a, x, which, st);
+    case 2048: return launch_fft_paths<2048>(a, x, which, st);
+    default: return -2;
+    }
 }
 
 int launch_axis_dft(const AxisDftArgs &a, cudaStream_t st)

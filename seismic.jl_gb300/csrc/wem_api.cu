@@ -909,12 +909,16 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
         twz[k] = make_float2((float)cos(a), (float)sin(a));
     }
     std::vector<float> sc(nwf, 1.f / sqrtf((float)ntfft));
+    // power-of-two widths: the row FFT's per-pass twiddles instead of the direct table
+    const bool fftx = angles_fft_supported(nmx);
+    std::vector<float2> twf(fftx ? twiddle_table_size(nmx) : 0);
+    if (fftx) twiddle_table_host(nmx, twf.data());
     const int64_t zero = 0;
     const size_t plane = sizeof(float2) * (size_t)nwf * n;
-    DevBuf bwt, btwx, btwz, bsc, bsrc, bbase, bU, bT, bX, bL, bR, bZ, bang, bpo, bpd, btap, bwav;
+    DevBuf bwt, btwx, btwz, bsc, bsrc, bbase, bU, bT, bX, bL, bR, bZ, bang, bpo, bpd, btap, bwav, btwf;
     auto release = [&]() {
         DevBuf *bs[] = { &bwt, &btwx, &btwz, &bsc, &bsrc, &bbase, &bU, &bT, &bX, &bL, &bR, &bZ, &bang,
-                         &bpo, &bpd, &btap, &bwav };
+                         &bpo, &bpd, &btap, &bwav, &btwf };
         for (DevBuf *b : bs)
             if (b->p) cudaFree(b->p);
     };
@@ -925,7 +929,8 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
         (rc = ensure(bT, plane)) || (rc = ensure(bX, plane)) || (rc = ensure(bL, plane)) || (rc = ensure(bR, plane)) ||
         (rc = ensure(bZ, plane)) || (rc = ensure(bang, sizeof(float) * 2 * n)) ||
         (rc = ensure(bpo, sizeof(float) * nz)) || (rc = ensure(bpd, sizeof(float) * n)) ||
-        (rc = ensure(btap, sizeof(float) * nmx)) || (rc = ensure(bwav, sizeof(float) * p.nt))) {
+        (rc = ensure(btap, sizeof(float) * nmx)) || (rc = ensure(bwav, sizeof(float) * p.nt)) ||
+        (rc = ensure(btwf, sizeof(float2) * (twf.size() + 1)))) {
         release();
         return rc;
     }
@@ -946,6 +951,7 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     CKR(cudaMemcpyAsync(bpd.p, pd.data(), sizeof(float) * n, cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(btap.p, taper.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bwav.p, wav, sizeof(float) * p.nt, cudaMemcpyHostToDevice, st));
+    if (fftx) CKR(cudaMemcpyAsync(btwf.p, twf.data(), sizeof(float2) * twf.size(), cudaMemcpyHostToDevice, st));
     SpectraArgs sa{};
     sa.d = P<float>(bwav);
     sa.ntr = 1;
@@ -976,7 +982,17 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
         a.dw = dw; a.dz = p.dz; a.oz = p.oz; a.sz = p.sz; a.dkx = dkx; a.inv_sqrt_n = 1.f / sqrtf((float)nmx);
         a.po = P<float>(bpo); a.pd = P<float>(bpd); a.taper = P<float>(btap); a.srcw = P<float2>(bsrc);
         a.twx = P<float2>(btwx); a.u = P<float2>(bU);
-        if (launch_angles_extrap(a, st)) {
+        AngleXArgs xf{};
+        xf.nlines = (long long)nwf * nz; xf.dkx = dkx; xf.twx = P<float2>(btwf); xf.u = P<float2>(bU);
+        xf.ux = P<float2>(bX); xf.ul = P<float2>(bL); xf.ur = P<float2>(bR);
+        if (fftx) {
+            AngleArgs af = a;
+            af.twx = P<float2>(btwf);
+            if (launch_angles_fft(af, xf, 0, st)) {
+                release();
+                return fail(WEM_ERR_CUDA, "angles: extrapolation launch: %s", cudaGetErrorString(cudaGetLastError()));
+            }
+        } else if (launch_angles_extrap(a, st)) {
             release();
             return fail(WEM_ERR_CUDA, "angles: extrapolation launch: %s", cudaGetErrorString(cudaGetLastError()));
         }
@@ -996,7 +1012,12 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
             { za, &bU, &bT, -1, 0, 1.f },                    // DFT_z(u)
             { za, &bT, &bZ, +1, 1, 1.f / (float)nz },        // u_z = IDFT_z(i kz .) / nkz
         };
+        if (fftx && launch_angles_fft(a, xf, 1, st)) {
+            release();
+            return fail(WEM_ERR_CUDA, "angles: x-derivative launch: %s", cudaGetErrorString(cudaGetLastError()));
+        }
         for (const Step &sp : steps) {
+            if (fftx && sp.base.se == 1) continue;  // the x transforms ran on the row FFT
             AxisDftArgs d = sp.base;
             d.in = reinterpret_cast<const float2 *>(sp.in->p);
             d.out = reinterpret_cast<float2 *>(sp.out->p);

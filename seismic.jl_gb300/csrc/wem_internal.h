@@ -120,7 +120,17 @@ struct AngleAccumArgs {
     const float2 *u, *ux, *uz, *ul, *ur;  // [nwf][nz][nmx]
     float *angx, *angy;                   // [nmx][nz]
 };
+struct AngleXArgs {
+    long long nlines;                  // rows of nmx samples (frequency, depth)
+    float dkx;
+    const float2 *twx;                 // FFT twiddle table of the row length
+    const float2 *u;                   // [nlines][nmx]
+    float2 *ux, *ul, *ur;              // [nlines][nmx]
+};
 int launch_angles_extrap(const AngleArgs &a, cudaStream_t st);
+// power-of-two nmx in [32, 2048]: which = 0 extrapolation, 1 x derivatives on the row FFT
+bool angles_fft_supported(int nmx);
+int launch_angles_fft(const AngleArgs &a, const AngleXArgs &x, int which, cudaStream_t st);
 int launch_axis_dft(const AxisDftArgs &a, cudaStream_t st);
 int launch_angles_accum(const AngleAccumArgs &a, cudaStream_t st);
 
