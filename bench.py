@@ -321,8 +321,15 @@ def run_angles(args, c, wl, rank, world, local):
                                 "kind": "port", "sample": f"1 shot, {nq} frequencies x {p['nz']} depth steps in {el:.1f} s "
                                                           "(NumPy FP64 restatement, one thread)"}
         got, _ = ctx.angles(q, c["vel"], c["wav"], [q["sx"]])
-        line["accuracy"] = {"rel_l2_vs_fp64": float(np.linalg.norm(got[0] - want) / np.linalg.norm(want)),
-                            "sample": "the CPU leg's shot and band"}
+        g0 = got[0].astype(np.float64)
+        live = np.abs(want) > 1e-3
+        # the sign (side of arrival) is ill-conditioned where the two sides carry equal energy;
+        # the reference's own FP32 result flips a few such points against FP64 too
+        line["accuracy"] = {"rel_l2_vs_fp64": float(np.linalg.norm(g0 - want) / np.linalg.norm(want)),
+                            "rel_l2_of_magnitude_vs_fp64": float(np.linalg.norm(np.abs(g0) - np.abs(want))
+                                                                 / np.linalg.norm(want)),
+                            "sign_flips": int(np.count_nonzero(np.sign(g0[live]) != np.sign(want[live]))),
+                            "points": int(live.sum()), "sample": "the CPU leg's shot and band"}
     if rank == 0:
         print(json.dumps(line))
     ctx.close()
