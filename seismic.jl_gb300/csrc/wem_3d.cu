@@ -72,9 +72,13 @@ template <int NX> struct ColShape {
     static constexpr int TW = fft_tw_size<NX>(), TWP = (TW + 1) & ~1;
 };
 
+// the column tile is [2][CW][P] with P = tile_pitch(nmx): a team (one column) walks x with
+// unit stride, and P = 2 mod 16 puts the 8 columns x 2 rows a half-warp touches in the
+// global copies on 16 different 8-byte banks
+__host__ __device__ constexpr int tile_pitch(int nmx) { return ((nmx + 15) & ~15) + 2; }
 __host__ __device__ constexpr size_t col_smem_bytes(int twp, int half, int cw, int teams, int padn, int nmx)
 {
-    return sizeof(float2) * ((size_t)twp + (size_t)cw * half + (size_t)teams * padn + (size_t)2 * nmx * cw);
+    return sizeof(float2) * ((size_t)twp + (size_t)cw * half + (size_t)teams * padn + (size_t)2 * tile_pitch(nmx) * cw);
 }
 
 template <int NX, bool PSPI>
@@ -86,7 +90,8 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
     float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
     float2 *s_ph = s_tw + CS::TWP;                 // [CW][HALF] phase of one reference
     float2 *s_x = s_ph + (size_t)CW * HALF;       // exchange buffers
-    float2 *s_tile = s_x + (size_t)2 * CW * pad16(NX);  // [2][nmx][CW] column tile
+    float2 *s_tile = s_x + (size_t)2 * CW * pad16(NX);  // [2][CW][pitch] column tile
+    const int pitch = tile_pitch(a.nmx);
     const int tid = threadIdx.x, team = tid / TX, t = tid - team * TX;
     const int w = team / CW, c = team - w * CW;
     float2 *xbuf = s_x + (size_t)team * pad16(NX);
@@ -105,14 +110,14 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
         __syncthreads();  // the previous job no longer uses the tile or the tables
         for (int e = tid; e < 2 * nmx * CW; e += NT) {
             const int ww = e / (nmx * CW), r_ = e - ww * nmx * CW, x = r_ / CW, cc = r_ - x * CW;
-            s_tile[e] = a.Y[(((size_t)item * 2 + ww) * nmx + x) * nky + ky0 + cc];
+            s_tile[((size_t)ww * CW + cc) * pitch + x] = a.Y[(((size_t)item * 2 + ww) * nmx + x) * nky + ky0 + cc];
         }
         __syncthreads();
         float2 v[16];
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             const int x = t + TX * m;
-            v[m] = x < nmx ? s_tile[((size_t)w * nmx + x) * CW + c] : make_float2(0.f, 0.f);
+            v[m] = x < nmx ? s_tile[((size_t)w * CW + c) * pitch + x] : make_float2(0.f, 0.f);
         }
         if (active) fft_row<NX, -1>(v, xbuf, s_tw, t, sync);
         const float slow_po = PSPI ? 0.f : __fmul_rn(a.po[iz], a.po[iz]);
@@ -149,14 +154,15 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
 #pragma unroll
                 for (int m = 0; m < 16; m++) {
                     const int x = t + TX * m;
-                    if (x < nmx) s_tile[((size_t)w * nmx + x) * CW + c] = u[m];
+                    if (x < nmx) s_tile[((size_t)w * CW + c) * pitch + x] = u[m];
                 }
             }
             __syncthreads();
             for (int e = tid; e < 2 * nmx * CW; e += NT) {
                 const int ww = e / (nmx * CW), r_ = e - ww * nmx * CW, x = r_ / CW, cc = r_ - x * CW;
                 if (zf & (ww == 0 ? Z_SRC : Z_REC))
-                    a.C[((((size_t)item * 2 + ww) * nref + r) * nmx + x) * nky + ky0 + cc] = s_tile[e];
+                    a.C[((((size_t)item * 2 + ww) * nref + r) * nmx + x) * nky + ky0 + cc] =
+                        s_tile[((size_t)ww * CW + cc) * pitch + x];
             }
         }
     }
