@@ -48,6 +48,11 @@ def survey(workload: str, rank: int):
     elif workload == "survey3d":
         c = synth.config3(seed=1003 + rank)
         wl = "3-D PSPI: 1 shot, 300x256x256 grid @12.5 m, nref=6, 3-60 Hz, nt=2000, padx=padt=2 (512x512 planes)"
+    elif workload == "survey3d_band":
+        c = synth.config3(seed=1003 + rank)
+        c["params"] = dict(c["params"], fmax=float(c["params"]["fmin"]) + 12.0)
+        wl = ("3-D PSPI for profiling: 1 shot, 300x256x256 grid @12.5 m, nref=6, 3-15 Hz, nt=2000, padx=padt=2 "
+              "(512x512 planes)")
     elif workload == "lsm32":
         c = synth.config4(seed=1004 + rank)
         c["params"] = dict(c["params"], interp="linear")
@@ -390,7 +395,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="survey64",
-                    choices=["survey64", "survey8", "survey3d", "split1", "lsm32", "angles8"])
+                    choices=["survey64", "survey8", "survey3d", "survey3d_band", "split1", "lsm32", "angles8"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split16"],

@@ -62,15 +62,28 @@ __global__ void __launch_bounds__(256) wem3d_rows_fwd_kernel(const Mig3dArgs a)
 }
 
 // ---------------------------------------------------------------- pass B
-// CTA: 2*CW teams of TX = NX/16 threads -- the CW columns ky0..ky0+CW-1 of the source
-// (teams 0..CW-1) and of the receiver (teams CW..2CW-1) of one item.
+// CTA: 2*CW teams of TX = NX/16 threads -- CW columns of the source (teams 0..CW-1) and of
+// the receiver (teams CW..2CW-1) of one item. A job's columns are CW/2 columns ky of the
+// first half (1..nky/2) and their mirrors nky - ky, which share the phase table (it
+// depends on ky^2); the mirror of the Nyquist column nky/2 is itself, so the last job
+// takes column 0 in its place, with a table row of its own.
 template <int NX> struct ColShape {
     static constexpr int TX = NX / 16;
     static constexpr int CW = (2 * TX >= 512) ? 1 : (512 / (2 * TX) > 16 ? 16 : 512 / (2 * TX));
     static constexpr int NT = 2 * CW * TX;
     static constexpr int HALF = NX / 2 + 1;
+    static constexpr int ROWS = CW / 2 + 1;  // phase-table rows of a job
     static constexpr int TW = fft_tw_size<NX>(), TWP = (TW + 1) & ~1;
 };
+
+// ky index of column cc of job block b (see pass B)
+__device__ __forceinline__ int col_ky(int b, int cc, int half_cols, int nky)
+{
+    const int base = 1 + b * half_cols;
+    if (cc < half_cols) return base + cc;
+    const int kym = nky - (base + cc - half_cols);
+    return kym == nky / 2 ? 0 : kym;
+}
 
 // the column tile is [2][CW][P] with P = tile_pitch(nmx): a team (one column) walks x with
 // unit stride, and P = 2 mod 16 puts the 8 columns x 2 rows a half-warp touches in the
@@ -78,7 +91,8 @@ template <int NX> struct ColShape {
 __host__ __device__ constexpr int tile_pitch(int nmx) { return ((nmx + 15) & ~15) + 2; }
 __host__ __device__ constexpr size_t col_smem_bytes(int twp, int half, int cw, int teams, int padn, int nmx)
 {
-    return sizeof(float2) * ((size_t)twp + (size_t)cw * half + (size_t)teams * padn + (size_t)2 * tile_pitch(nmx) * cw);
+    return sizeof(float2) * ((size_t)twp + (size_t)(cw / 2 + 1) * half + (size_t)teams * padn +
+                             (size_t)2 * tile_pitch(nmx) * cw);
 }
 
 template <int NX, bool PSPI>
@@ -88,8 +102,8 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
     constexpr int TX = CS::TX, CW = CS::CW, NT = CS::NT, HALF = CS::HALF;
     extern __shared__ float4 smem_raw[];
     float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
-    float2 *s_ph = s_tw + CS::TWP;                 // [CW][HALF] phase of one reference
-    float2 *s_x = s_ph + (size_t)CW * HALF;       // exchange buffers
+    float2 *s_ph = s_tw + CS::TWP;                 // [ROWS][HALF] phase of one reference
+    float2 *s_x = s_ph + (size_t)CS::ROWS * HALF;  // exchange buffers
     float2 *s_tile = s_x + (size_t)2 * CW * pad16(NX);  // [2][CW][pitch] column tile
     const int pitch = tile_pitch(a.nmx);
     const int tid = threadIdx.x, team = tid / TX, t = tid - team * TX;
@@ -103,14 +117,19 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
     const int nblk = nky / CW;
     const int iz = a.iz;
     for (int job = blockIdx.x; job < a.nitems * nblk; job += gridDim.x) {
-        const int item = job / nblk, ky0 = (job - item * nblk) * CW;
+        const int item = job / nblk, blk = job - item * nblk;
+        constexpr int H = CW / 2;
+        const int ky_c = col_ky(blk, c, H, nky);
+        const int row_c = c < H ? c : (ky_c == 0 ? H : c - H);
+        const bool zero_col = col_ky(blk, CW - 1, H, nky) == 0;  // this job holds column 0
         const int iw = a.ifmin + a.item_iwi[item];
         const float wv = __fmul_rn((float)iw, a.dw);
         const float w2 = __fmul_rn(wv, wv);
         __syncthreads();  // the previous job no longer uses the tile or the tables
         for (int e = tid; e < 2 * nmx * CW; e += NT) {
             const int ww = e / (nmx * CW), r_ = e - ww * nmx * CW, x = r_ / CW, cc = r_ - x * CW;
-            s_tile[((size_t)ww * CW + cc) * pitch + x] = a.Y[(((size_t)item * 2 + ww) * nmx + x) * nky + ky0 + cc];
+            s_tile[((size_t)ww * CW + cc) * pitch + x] =
+                a.Y[(((size_t)item * 2 + ww) * nmx + x) * nky + col_ky(blk, cc, H, nky)];
         }
         __syncthreads();
         float2 v[16];
@@ -123,12 +142,13 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
         const float slow_po = PSPI ? 0.f : __fmul_rn(a.po[iz], a.po[iz]);
         for (int r = 0; r < nref; r++) {
             __syncthreads();  // tile and table free
-            // phase of reference r for the CW columns: entry [cc][kk], |kx| = kk
+            // phase of reference r: row rr < H for first-half column rr (and its mirror),
+            // row H for column 0 when the job holds it; entry [rr][kk], |kx| = kk
             const float slow2 = PSPI ? a.slow2[(size_t)iz * a.nref + r] : slow_po;
-            for (int e = tid; e < CW * HALF; e += NT) {
-                const int cc = e / HALF, kk = e - cc * HALF;
-                const int kyi = ky0 + cc;
-                const float ky = kyi <= nky / 2 ? __fmul_rn(a.dky, (float)kyi) : -__fsub_rn(__fmul_rn(a.dky, (float)nky), __fmul_rn(a.dky, (float)kyi));
+            for (int e = tid; e < (zero_col ? H + 1 : H) * HALF; e += NT) {
+                const int rr = e / HALF, kk = e - rr * HALF;
+                const int kyi = rr < H ? col_ky(blk, rr, H, nky) : 0;  // first half: 1..nky/2
+                const float ky = __fmul_rn(a.dky, (float)kyi);
                 const float kx = __fmul_rn(a.dkx, (float)kk);
                 const float s = __fsub_rn(__fsub_rn(__fmul_rn(w2, slow2), __fmul_rn(kx, kx)), __fmul_rn(ky, ky));
                 float2 P;
@@ -147,7 +167,7 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
 #pragma unroll
                 for (int m = 0; m < 16; m++) {
                     const int k = t + TX * m;
-                    const float2 P = s_ph[(size_t)c * HALF + (k <= NX / 2 ? k : NX - k)];
+                    const float2 P = s_ph[(size_t)row_c * HALF + (k <= NX / 2 ? k : NX - k)];
                     u[m] = w == 0 ? cmulc(v[m], P) : cmul(v[m], P);
                 }
                 fft_row<NX, +1>(u, xbuf, s_tw, t, sync);
@@ -161,7 +181,7 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
             for (int e = tid; e < 2 * nmx * CW; e += NT) {
                 const int ww = e / (nmx * CW), r_ = e - ww * nmx * CW, x = r_ / CW, cc = r_ - x * CW;
                 if (zf & (ww == 0 ? Z_SRC : Z_REC))
-                    a.C[((((size_t)item * 2 + ww) * nref + r) * nmx + x) * nky + ky0 + cc] =
+                    a.C[((((size_t)item * 2 + ww) * nref + r) * nmx + x) * nky + col_ky(blk, cc, H, nky)] =
                         s_tile[((size_t)ww * CW + cc) * pitch + x];
             }
         }
