@@ -89,10 +89,12 @@ __device__ __forceinline__ int col_ky(int b, int cc, int half_cols, int nky)
 // unit stride, and P = 2 mod 16 puts the 8 columns x 2 rows a half-warp touches in the
 // global copies on 16 different 8-byte banks
 __host__ __device__ constexpr int tile_pitch(int nmx) { return ((nmx + 15) & ~15) + 2; }
+// two phase tables and two column tiles: reference r works in buffer r % 2 while the
+// result of reference r - 1 is copied out of the other
 __host__ __device__ constexpr size_t col_smem_bytes(int twp, int half, int cw, int teams, int padn, int nmx)
 {
-    return sizeof(float2) * ((size_t)twp + (size_t)(cw / 2 + 1) * half + (size_t)teams * padn +
-                             (size_t)2 * tile_pitch(nmx) * cw);
+    return sizeof(float2) * ((size_t)twp + (size_t)2 * (cw / 2 + 1) * half + (size_t)teams * padn +
+                             (size_t)2 * 2 * tile_pitch(nmx) * cw);
 }
 
 template <int NX, bool PSPI>
@@ -102,10 +104,11 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
     constexpr int TX = CS::TX, CW = CS::CW, NT = CS::NT, HALF = CS::HALF;
     extern __shared__ float4 smem_raw[];
     float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
-    float2 *s_ph = s_tw + CS::TWP;                 // [ROWS][HALF] phase of one reference
-    float2 *s_x = s_ph + (size_t)CS::ROWS * HALF;  // exchange buffers
-    float2 *s_tile = s_x + (size_t)2 * CW * pad16(NX);  // [2][CW][pitch] column tile
+    float2 *s_ph0 = s_tw + CS::TWP;                    // [2][ROWS][HALF] phase tables
+    float2 *s_x = s_ph0 + (size_t)2 * CS::ROWS * HALF;  // exchange buffers
     const int pitch = tile_pitch(a.nmx);
+    float2 *s_tile0 = s_x + (size_t)2 * CW * pad16(NX);  // [2][2][CW][pitch] column tiles
+    const size_t tile_sz = (size_t)2 * CW * pitch;
     const int tid = threadIdx.x, team = tid / TX, t = tid - team * TX;
     const int w = team / CW, c = team - w * CW;
     float2 *xbuf = s_x + (size_t)team * pad16(NX);
@@ -125,23 +128,38 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
         const int iw = a.ifmin + a.item_iwi[item];
         const float wv = __fmul_rn((float)iw, a.dw);
         const float w2 = __fmul_rn(wv, wv);
-        __syncthreads();  // the previous job no longer uses the tile or the tables
-        for (int e = tid; e < 2 * nmx * CW; e += NT) {
-            const int ww = e / (nmx * CW), r_ = e - ww * nmx * CW, x = r_ / CW, cc = r_ - x * CW;
-            s_tile[((size_t)ww * CW + cc) * pitch + x] =
-                a.Y[(((size_t)item * 2 + ww) * nmx + x) * nky + col_ky(blk, cc, H, nky)];
+        // columns of tile b to C for reference rr (the wavefields active at this depth)
+        // (element e of a wavefield's tile: column cc = e % CW fastest, then x = e / CW)
+        auto copy_out = [&](const float2 *tile, int rr) {
+            for (int ww = 0; ww < 2; ww++) {
+                if (!(zf & (ww == 0 ? Z_SRC : Z_REC))) continue;
+                float2 *dst = a.C + (((size_t)item * 2 + ww) * nref + rr) * nmx * nky;
+                for (int e = tid; e < nmx * CW; e += NT) {
+                    const int x = e / CW, cc = e - x * CW;
+                    dst[(size_t)x * nky + col_ky(blk, cc, H, nky)] = tile[((size_t)ww * CW + cc) * pitch + x];
+                }
+            }
+        };
+        __syncthreads();  // the previous job no longer uses the tiles or the tables
+        for (int ww = 0; ww < 2; ww++) {
+            const float2 *src = a.Y + ((size_t)item * 2 + ww) * nmx * nky;
+            for (int e = tid; e < nmx * CW; e += NT) {
+                const int x = e / CW, cc = e - x * CW;
+                s_tile0[((size_t)ww * CW + cc) * pitch + x] = src[(size_t)x * nky + col_ky(blk, cc, H, nky)];
+            }
         }
         __syncthreads();
         float2 v[16];
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             const int x = t + TX * m;
-            v[m] = x < nmx ? s_tile[((size_t)w * CW + c) * pitch + x] : make_float2(0.f, 0.f);
+            v[m] = x < nmx ? s_tile0[((size_t)w * CW + c) * pitch + x] : make_float2(0.f, 0.f);
         }
         if (active) fft_row<NX, -1>(v, xbuf, s_tw, t, sync);
         const float slow_po = PSPI ? 0.f : __fmul_rn(a.po[iz], a.po[iz]);
         for (int r = 0; r < nref; r++) {
-            __syncthreads();  // tile and table free
+            float2 *s_ph = s_ph0 + (size_t)(r & 1) * CS::ROWS * HALF;
+            float2 *s_tile = s_tile0 + (size_t)(r & 1) * tile_sz;
             // phase of reference r: row rr < H for first-half column rr (and its mirror),
             // row H for column 0 when the job holds it; entry [rr][kk], |kx| = kk
             const float slow2 = PSPI ? a.slow2[(size_t)iz * a.nref + r] : slow_po;
@@ -161,6 +179,8 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
                 }
                 s_ph[e] = make_float2(P.x * a.inv_n, P.y * a.inv_n);
             }
+            // table r is complete; tile r % 2 is free (its copy-out of reference r - 2 and
+            // every read of the input tile came before this barrier in each thread)
             __syncthreads();
             if (active) {
                 float2 u[16];
@@ -177,14 +197,11 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
                     if (x < nmx) s_tile[((size_t)w * CW + c) * pitch + x] = u[m];
                 }
             }
-            __syncthreads();
-            for (int e = tid; e < 2 * nmx * CW; e += NT) {
-                const int ww = e / (nmx * CW), r_ = e - ww * nmx * CW, x = r_ / CW, cc = r_ - x * CW;
-                if (zf & (ww == 0 ? Z_SRC : Z_REC))
-                    a.C[((((size_t)item * 2 + ww) * nref + r) * nmx + x) * nky + col_ky(blk, cc, H, nky)] =
-                        s_tile[((size_t)ww * CW + cc) * pitch + x];
-            }
+            // reference r - 1 finished before the barrier above: copy it out meanwhile
+            if (r > 0) copy_out(s_tile0 + (size_t)((r - 1) & 1) * tile_sz, r - 1);
         }
+        __syncthreads();
+        copy_out(s_tile0 + (size_t)((nref - 1) & 1) * tile_sz, nref - 1);
     }
 }
 
