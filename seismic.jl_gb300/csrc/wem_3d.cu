@@ -25,6 +25,15 @@
 
 namespace gbwem {
 
+// wavefield w (0 source, 1 receiver) steps at this depth: its zflag bit, and in the
+// modelling modes only the wavefield being continued (1: source, 2: receiver)
+__device__ __forceinline__ bool m3_active(const Mig3dArgs &a, uint8_t zf, int w)
+{
+    if (a.mode == 1 && w != 0) return false;
+    if (a.mode == 2 && w != 1) return false;
+    return (zf & (w == 0 ? Z_SRC : Z_REC)) != 0;
+}
+
 // ---------------------------------------------------------------- pass A
 template <int NY>
 __global__ void __launch_bounds__(256) wem3d_rows_fwd_kernel(const Mig3dArgs a)
@@ -46,13 +55,36 @@ __global__ void __launch_bounds__(256) wem3d_rows_fwd_kernel(const Mig3dArgs a)
         const int item = (int)(job / (2 * a.nmx));
         const int rem = (int)(job - (long long)item * 2 * a.nmx);
         const int w = rem / a.nmx, x = rem - w * a.nmx;
-        if (!(zf & (w == 0 ? Z_SRC : Z_REC))) continue;  // team-uniform
+        if (!m3_active(a, zf, w)) continue;  // team-uniform
         const float2 *urow = a.U + ((size_t)item * 2 + w) * n + (size_t)x * a.nmy;
         float2 v[16];
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             const int y = t + TY * m;
             v[m] = y < a.nmy ? urow[y] : make_float2(0.f, 0.f);
+        }
+        if (a.mode == 2) {
+            // receiver going up: inject m * smig (wem.c:270-272), then for split-step the
+            // taper and the correction come before the transform (ssop adj=false, wem.c:321-330)
+            const size_t zrow = (size_t)a.iz * n + (size_t)x * a.nmy;
+            const float2 *sm = a.smig + ((size_t)item * a.nz + a.iz) * n + (size_t)x * a.nmy;
+            const float wv = __fmul_rn((float)(a.ifmin + a.item_iwi[item]), a.dw);
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int y = t + TY * m;
+                if (y < a.nmy) {
+                    const float mv = a.mimg[zrow + y];
+                    const float2 s_ = sm[y];
+                    v[m].x += mv * s_.x;
+                    v[m].y += mv * s_.y;
+                    if (!a.pspi) {
+                        const float tp = a.taper[x] * a.tapery[y];
+                        float sn, cs;
+                        sincosf(__fmul_rn(__fmul_rn(wv, a.pd[zrow + y]), -a.dz), &sn, &cs);
+                        v[m] = cmul(make_float2(v[m].x * tp, v[m].y * tp), make_float2(cs, sn));
+                    }
+                }
+            }
         }
         fft_row<NY, -1>(v, xbuf, s_tw, t, sync);
         float2 *yrow = a.Y + (((size_t)item * 2 + w) * a.nmx + x) * NY;
@@ -115,7 +147,8 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
     const unsigned sync = team_sync_handle<NX>(tid);
     for (int i = tid; i < CS::TW; i += NT) s_tw[i] = a.twx[i];
     const uint8_t zf = a.zflag[a.iz];
-    const bool active = (zf & (w == 0 ? Z_SRC : Z_REC)) != 0;
+    const bool active = m3_active(a, zf, w);
+    const bool conj = w == 0 || a.mode == 2;  // -dz: the source, and the modelling receiver
     const int nmx = a.nmx, nky = a.nky, nref = PSPI ? a.nref : 1;
     const int nblk = nky / CW;
     const int iz = a.iz;
@@ -132,7 +165,7 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
         // (element e of a wavefield's tile: column cc = e % CW fastest, then x = e / CW)
         auto copy_out = [&](const float2 *tile, int rr) {
             for (int ww = 0; ww < 2; ww++) {
-                if (!(zf & (ww == 0 ? Z_SRC : Z_REC))) continue;
+                if (!m3_active(a, zf, ww)) continue;
                 float2 *dst = a.C + (((size_t)item * 2 + ww) * nref + rr) * nmx * nky;
                 for (int e = tid; e < nmx * CW; e += NT) {
                     const int x = e / CW, cc = e - x * CW;
@@ -188,7 +221,7 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
                 for (int m = 0; m < 16; m++) {
                     const int k = t + TX * m;
                     const float2 P = s_ph[(size_t)row_c * HALF + (k <= NX / 2 ? k : NX - k)];
-                    u[m] = w == 0 ? cmulc(v[m], P) : cmul(v[m], P);
+                    u[m] = conj ? cmulc(v[m], P) : cmul(v[m], P);
                 }
                 fft_row<NX, +1>(u, xbuf, s_tw, t, sync);
 #pragma unroll
@@ -226,7 +259,7 @@ __global__ void __launch_bounds__(256) wem3d_rows_inv_kernel(const Mig3dArgs a)
     const int iz = a.iz, nmx = a.nmx, nmy = a.nmy, nky = a.nky, n = nmx * nmy;
     const int nref = PSPI ? a.nref : 1;
     const uint8_t zf = a.zflag[iz];
-    const bool active = (zf & (w == 0 ? Z_SRC : Z_REC)) != 0;
+    const bool active = m3_active(a, zf, w);
     const int nchunk = (a.nitems + a.chunk - 1) / a.chunk;
     const long long njobs = (long long)nchunk * nmx;
     // the pair's partner buffer for the imaging condition: the source team's xbuf
@@ -292,7 +325,7 @@ __global__ void __launch_bounds__(256) wem3d_rows_inv_kernel(const Mig3dArgs a)
                     float2 q = make_float2(0.f, 0.f);
                     if (y < nmy) {
                         q = acc[m];
-                        if (!PSPI) {
+                        if (!PSPI && a.mode != 2) {
                             // split-step correction and taper (wem.c:349-359), -dz for the source
                             const float th = __fmul_rn(__fmul_rn(wv, a.pd[(size_t)iz * n + (size_t)x * nmy + y]), a.dz);
                             float sn, cs;
@@ -305,6 +338,14 @@ __global__ void __launch_bounds__(256) wem3d_rows_inv_kernel(const Mig3dArgs a)
                     }
                     unew[m] = q;
                 }
+                if (a.mode == 1) {  // keep the source of this depth (wem.c:260)
+                    float2 *sm = a.smig + ((size_t)item * a.nz + iz) * n + (size_t)x * nmy;
+#pragma unroll
+                    for (int m = 0; m < 16; m++) {
+                        const int y = t + TY * m;
+                        if (y < nmy) sm[y] = unew[m];
+                    }
+                }
             } else {
 #pragma unroll
                 for (int m = 0; m < 16; m++) {
@@ -312,7 +353,15 @@ __global__ void __launch_bounds__(256) wem3d_rows_inv_kernel(const Mig3dArgs a)
                     unew[m] = y < nmy ? urow[y] : make_float2(0.f, 0.f);
                 }
             }
-            if (zf & Z_REC) {
+            if (a.mode == 1 && w == 0 && !active) {  // no source above its depth (wem.c:262-264)
+                float2 *sm = a.smig + ((size_t)item * a.nz + iz) * n + (size_t)x * nmy;
+#pragma unroll
+                for (int m = 0; m < 16; m++) {
+                    const int y = t + TY * m;
+                    if (y < nmy) sm[y] = make_float2(0.f, 0.f);
+                }
+            }
+            if (a.mode == 0 && (zf & Z_REC)) {
                 // imaging condition (wem.c:243-247): the pair meets in the source team's buffer
                 team_pair_sync<NY>(pair, tid);
                 if (w == 0) {
@@ -336,7 +385,7 @@ __global__ void __launch_bounds__(256) wem3d_rows_inv_kernel(const Mig3dArgs a)
                 team_pair_sync<NY>(pair, tid);
             }
         }
-        if (w == 1) {
+        if (w == 1 && a.mode == 0) {
             float2 *part = a.img_parts + ((size_t)ch * a.nz + iz) * n + (size_t)x * nmy;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
@@ -359,7 +408,7 @@ __global__ void wem3d_init_kernel(const Mig3dArgs a)
         const int shot = a.item_shot[item], iwi = a.item_iwi[item];
         float2 v;
         if (w == 0) v = cell == a.src_cell[shot] ? a.srcw[iwi] : make_float2(0.f, 0.f);
-        else v = a.recv[((size_t)shot * a.nwf + iwi) * n + cell];
+        else v = a.mode == 0 ? a.recv[((size_t)shot * a.nwf + iwi) * n + cell] : make_float2(0.f, 0.f);
         a.U[e] = v;
     }
 }
@@ -446,6 +495,24 @@ int m3d_launch_step(int nkx, int nky, int pspi, int interp, const Mig3dArgs &a, 
 int m3d_launch_init(const Mig3dArgs &a, cudaStream_t st)
 {
     wem3d_init_kernel<<<1024, 256, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+// the modelled receiver planes at the surface (wem.c:278-280)
+__global__ void wem3d_collect_kernel(const Mig3dArgs a, float2 *dg, float scale)
+{
+    const int n = a.nmx * a.nmy;
+    const long long total = (long long)a.nitems * n;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const int item = (int)(e / n), cell = (int)(e - (long long)item * n);
+        const float2 u = a.U[((size_t)item * 2 + 1) * n + cell];
+        dg[((size_t)a.item_shot[item] * a.nwf + a.item_iwi[item]) * n + cell] = make_float2(u.x * scale, u.y * scale);
+    }
+}
+
+int m3d_launch_collect(const Mig3dArgs &a, float2 *dg, float scale, cudaStream_t st)
+{
+    wem3d_collect_kernel<<<1024, 256, 0, st>>>(a, dg, scale);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -1060,10 +1060,101 @@ extern "C" int wem_migrate_survey(wem_ctx *c, const wem_params *p, const float *
 }
 
 // GPU part of a modelling: image transpose -> Born recursion -> synthesis. On c->st.
+// 3-D modelling with the reference's operator (wem.c:252-281): per batch of items, the
+// source continued down with every depth kept (pass C writes smig), then the receiver
+// continued up from the bottom with m * smig injected before each step (pass A), then
+// the surface planes collected; the synthesis is the 2-D path's.
+static int run_model3d(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, float *d_dev, int exact)
+{
+    const wem_params &p = c->p;
+    if (exact) return fail(WEM_ERR_SIZE, "the exact adjoint of the 3-D migration is not built (the reference's "
+                                         "modelling operator is: exact = 0)");
+    cudaStream_t st = c->st;
+    const int nmx = p.nmx, nmy = p.nmy, nz = p.nz, n = nmx * nmy;
+    const int nref = p.pspi ? p.nref : 1;
+    const int nitems = nshot * c->nwf;
+    const size_t dg_elems = (size_t)nshot * (c->nwf > 0 ? c->nwf : 1) * n;
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const size_t per_item = sizeof(float2) * ((size_t)2 * n + (size_t)2 * nmx * c->nky * (1 + nref) + (size_t)nz * n);
+    const size_t fixed = sizeof(float2) * dg_elems + sizeof(float) * (size_t)nz * n;
+    if (fixed + per_item > free_b)
+        return fail(WEM_ERR_NOMEM, "3-D modelling needs %zu MB of device memory at least", (fixed + per_item) >> 20);
+    int batch = (int)std::min<long long>(nitems, std::max<long long>(1, (long long)((free_b - fixed) / 2 / per_item)));
+    int rc;
+    if ((rc = ensure(c->recv, sizeof(float2) * dg_elems)) || (rc = ensure(c->mimg, sizeof(float) * (size_t)nz * n)) ||
+        (rc = ensure(c->m3_U, sizeof(float2) * (size_t)batch * 2 * n)) ||
+        (rc = ensure(c->m3_Y, sizeof(float2) * (size_t)batch * 2 * nmx * c->nky)) ||
+        (rc = ensure(c->m3_C, sizeof(float2) * (size_t)batch * 2 * nref * nmx * c->nky)) ||
+        (rc = ensure(c->smig, sizeof(float2) * (size_t)batch * nz * n)) ||
+        (rc = ensure(c->m3_items, sizeof(int) * 2 * (size_t)std::max(nitems, 1))))
+        return rc;
+    std::vector<int> items(2 * (size_t)std::max(nitems, 1));
+    for (int it = 0; it < nitems; it++) { items[it] = it % c->nwf; items[nitems + it] = it / c->nwf; }
+    if (nitems > 0) CK(cudaMemcpyAsync(c->m3_items.p, items.data(), sizeof(int) * 2 * nitems, cudaMemcpyHostToDevice, st));
+    int kernels = 0;
+    CK(cudaEventRecord(c->ev0, st));
+    CK(cudaMemsetAsync(c->recv.p, 0, sizeof(float2) * dg_elems, st));
+    if (launch_transpose(m_dev, n, nz, P<float>(c->mimg), st))
+        return fail(WEM_ERR_CUDA, "transpose launch: %s", cudaGetErrorString(cudaGetLastError()));
+    kernels++;
+    CK(cudaEventRecord(c->evk[0], st));
+    CK(cudaEventRecord(c->evk[1], st));
+    const float inv_sqt = (float)(1.0 / (double)sqrtf((float)c->ntfft));
+    for (int b0 = 0; b0 < nitems; b0 += batch) {
+        const int nb = std::min(batch, nitems - b0);
+        Mig3dArgs a{};
+        a.nmx = nmx; a.nmy = nmy; a.nkx = c->nkx; a.nky = c->nky; a.nz = nz; a.nref = nref; a.nwf = c->nwf;
+        a.ifmin = c->ifmin; a.nitems = nb; a.chunk = 32;  // pass C runs 32 items per job
+        a.dw = c->dw; a.dz = p.dz; a.dkx = c->dkx; a.dky = c->dky; a.inv_n = 1.0f / ((float)c->nkx * c->nky);
+        a.vref = P<float>(c->vref); a.slow2 = P<float>(c->slow2); a.po = P<float>(c->po); a.pd = P<float>(c->pd);
+        a.wlin = P<float>(c->wlin); a.taper = P<float>(c->taper); a.tapery = P<float>(c->tapery);
+        a.selb = P<uint8_t>(c->sel); a.zflag = P<uint8_t>(c->zflag); a.twx = P<float2>(c->twid); a.twy = P<float2>(c->twy);
+        a.item_iwi = P<int>(c->m3_items) + b0; a.item_shot = P<int>(c->m3_items) + nitems + b0;
+        a.src_cell = P<int>(c->igx); a.srcw = P<float2>(c->srcw); a.recv = nullptr;
+        a.U = P<float2>(c->m3_U); a.Y = P<float2>(c->m3_Y); a.C = P<float2>(c->m3_C); a.img_parts = nullptr;
+        a.pspi = p.pspi; a.smig = P<float2>(c->smig); a.mimg = P<float>(c->mimg);
+        a.mode = 1;
+        if (m3d_launch_init(a, st)) return fail(WEM_ERR_CUDA, "3-D init launch: %s", cudaGetErrorString(cudaGetLastError()));
+        kernels++;
+        for (int iz = 0; iz < nz; iz++) {  // source down (wem.c:255-265)
+            a.iz = iz;
+            if (m3d_launch_step(c->nkx, c->nky, p.pspi, p.interp, a, c->nsm, st))
+                return fail(WEM_ERR_CUDA, "3-D modelling step launch: %s", cudaGetErrorString(cudaGetLastError()));
+            kernels += 3;
+        }
+        a.mode = 2;
+        for (int iz = nz - 1; iz >= 0; iz--) {  // receiver up (wem.c:266-276)
+            a.iz = iz;
+            if (m3d_launch_step(c->nkx, c->nky, p.pspi, p.interp, a, c->nsm, st))
+                return fail(WEM_ERR_CUDA, "3-D modelling step launch: %s", cudaGetErrorString(cudaGetLastError()));
+            kernels += 3;
+        }
+        if (m3d_launch_collect(a, P<float2>(c->recv), inv_sqt, st))
+            return fail(WEM_ERR_CUDA, "3-D collect launch: %s", cudaGetErrorString(cudaGetLastError()));
+        kernels++;
+    }
+    CK(cudaEventRecord(c->evk[2], st));
+    if (ntr > 0) {
+        SynthArgs sy{};
+        sy.dg = P<float2>(c->recv);
+        sy.nwf = c->nwf; sy.ifmin = c->ifmin; sy.nt = p.nt; sy.nf = c->nf; sy.ntr = (int)ntr;
+        sy.in_base = P<int64_t>(c->tbase); sy.in_fstride = n; sy.wtab = P<float2>(c->wtab);
+        sy.scale = P<float>(c->ssyn_ref);
+        sy.out = d_dev;
+        if (launch_synth(sy, st)) return fail(WEM_ERR_CUDA, "synthesis launch: %s", cudaGetErrorString(cudaGetLastError()));
+        kernels++;
+    }
+    CK(cudaEventRecord(c->evk[3], st));
+    CK(cudaEventRecord(c->ev1, st));
+    c->last_kernels = kernels;
+    return WEM_OK;
+}
+
 static int run_model(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, float *d_dev, int exact)
 {
     const wem_params &p = c->p;
-    if (p.nmy > 1) return fail(WEM_ERR_SIZE, "modelling of 3-D grids is not built (migration is)");
+    if (p.nmy > 1) return run_model3d(c, nshot, ntr, m_dev, d_dev, exact);
     cudaStream_t st = c->st;
     const int nmx = p.nmx, nz = p.nz;
     int S, threads, bps = 0;

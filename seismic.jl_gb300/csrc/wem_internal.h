@@ -87,12 +87,19 @@ struct Mig3dArgs {
     float2 *Y;          // [item][2][nmx][nky]
     float2 *C;          // [item][2][nref][nmx][nky]
     float2 *img_parts;  // [chunk][nz][nmx*nmy] (sum, 0)
+    // modelling (wem.c:252-281): mode 1 continues the source down and keeps it in smig;
+    // mode 2 continues the receiver up (-dz, adj=false) with m * smig injected first
+    int mode, pspi;     // mode 0: migration
+    float2 *smig;       // [item][nz][nmx*nmy]
+    const float *mimg;  // [nz][nmx*nmy] image, depth-major
 };
 int m3d_supported(int nkx, int nky);
 int m3d_cols_block(int nkx);
 int m3d_cols_smem(int nkx, int pspi, const Mig3dArgs &a, size_t *smem);
 int m3d_launch_step(int nkx, int nky, int pspi, int interp, const Mig3dArgs &a, int nsm, cudaStream_t st);
 int m3d_launch_init(const Mig3dArgs &a, cudaStream_t st);
+// dg[(shot * nwf + iwi) * n + cell] = receiver plane of each item * scale
+int m3d_launch_collect(const Mig3dArgs &a, float2 *dg, float scale, cudaStream_t st);
 
 // host-side launchers (wem_kernels.cu). `wide` selects the 512-thread CTA shape of
 // the migration kernel (2S rows sharing the phase tables) over the 256-thread one.
