@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
 // pair per row x; each pair runs the items of one chunk in turn and keeps the
 // chunk's image row in registers.
 template <int NY, bool PSPI, int INTERP>
-__global__ void __launch_bounds__(256) wem3d_rows_inv_kernel(const Mig3dArgs a)
+__global__ void __launch_bounds__(256, 2) wem3d_rows_inv_kernel(const Mig3dArgs a)
 {
     constexpr int TY = NY / 16, TEAMS = 256 / TY, PAIRS = TEAMS / 2;
     constexpr int TW = fft_tw_size<NY>(), TWP = (TW + 1) & ~1;
