@@ -156,8 +156,10 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
 // then the receiver wavefield is continued up from the bottom with the image
 // injected at each depth (wem.c:266-276); the surface row, divided by
 // sqrt(ntfft) (wem.c:277-279), is the shot's spectrum at this frequency.
+// Rows of up to 1024 samples: two CTAs per SM (their shared memory fits twice), so the
+// registers are capped at 128 per thread.
 template <int N, bool PSPI, int INTERP, int S, bool EXACT>
-__global__ void __launch_bounds__(S * (N / 16), 1) wem_model_kernel(const MigArgs a, const BornArgs b)
+__global__ void __launch_bounds__(S * (N / 16), N <= 1024 ? 2 : 1) wem_model_kernel(const MigArgs a, const BornArgs b)
 {
     using SH = MigShape<N>;
     constexpr int T = SH::T, PADN = SH::PADN;
