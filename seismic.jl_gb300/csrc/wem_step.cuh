@@ -228,6 +228,9 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
             const int x = t + T * m;
             selp[m >> 2] |= (x < a.nmx ? (uint32_t)sm.selb[x] : 0x7fu) << (8 * (m & 3));
         }
+        uint32_t i1p[4];  // the 16 positions' lower reference, four per word
+#pragma unroll
+        for (int q = 0; q < 4; q++) i1p[q] = selp[q] & 0x7f7f7f7fu;
         for (int r = 0; r < a.nref; r++) {
             if (!((used >> r) & 1ull)) continue;  // CTA-uniform
             const float2 *ph = sm.ph + (size_t)r * HALF;
@@ -238,16 +241,32 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
                 u[m] = conj ? cmulc(v[m], P) : cmul(v[m], P);
             }
             fft_row<N, +1, TC>(u, xbuf, sm.tw, t, sync, tc);
+            if (INTERP == 0) {
+                // the nearest-lower wavefield, whole or its real part (wem.c:454-459, 477):
+                // the positions that take reference r, found four at a time
+                const uint32_t rr = (uint32_t)r * 0x01010101u;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const uint32_t eq = __vcmpeq4(i1p[q], rr);
+                    if (eq == 0u) continue;
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const int m = 4 * q + j;
+                        if ((eq >> (8 * j)) & 1u) {
+                            const bool interp = ((selp[q] >> (8 * j + 7)) & 1u) != 0;
+                            sacc[m * T + t] = interp ? make_float2(u[m].x, 0.f) : u[m];
+                        }
+                    }
+                }
+                continue;
+            }
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const uint32_t b = (selp[m >> 2] >> (8 * (m & 3))) & 0xffu;
                 const int i1 = (int)(b & 0x7fu);
                 const bool interp = (b & 0x80u) != 0;
                 float2 *dst = sacc + m * T + t;
-                if (INTERP == 0) {
-                    // the nearest-lower wavefield, whole or its real part (wem.c:454-459, 477)
-                    if (r == i1) *dst = interp ? make_float2(u[m].x, 0.f) : u[m];
-                } else if (!interp) {
+                if (!interp) {
                     if (r == i1) *dst = u[m];
                 } else if (r == i1) {
                     const float w1 = 1.f - sm.wl[t + T * m];
