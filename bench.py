@@ -342,7 +342,7 @@ def run_angles(args, c, wl, rank, world, local):
 
 
 def run_lsm(args, ctx, c, wl, units, dev, rank, world, dist):
-    """configs[4]: Born data of a seeded reflectivity (1 % of the cells, N(0,1)), then CG
+    """The least-squares workload: Born data of a seeded reflectivity (1 % of the cells, N(0,1)), then CG
     (Scales 1987) from zero over wem_model(exact) / wem_migrate. One step = one CG solve."""
     import torch
     from wemgpu import Shots

@@ -50,10 +50,18 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
+# where the reference's sources lie in the build container (the recipe reads them there)
+REF_ROOT = os.environ.get("WEM_REFERENCE_ROOT", "/root/reference")
+
+
+def ref_sources_available() -> bool:
+    return os.path.exists(os.path.join(REF_ROOT, "src", "Imaging", "c", "wem.c"))
+
+
 def build_ref() -> str | None:
     """Compile the reference C core into oracle/_ref when its sources exist."""
-    ref_root = os.environ.get("WEM_REFERENCE_ROOT", "/root/reference")
-    if not os.path.exists(os.path.join(ref_root, "src", "Imaging", "c", "wem.c")):
+    ref_root = REF_ROOT
+    if not ref_sources_available():
         return None
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
     return REF_LIB_PATH

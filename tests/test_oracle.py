@@ -69,7 +69,7 @@ def test_port_matches_reference_golden(oracle_mod, case):
     assert rel_l2(d, g["d_ref"]) < 1e-5
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/src/Imaging/c/wem.c"), reason="reference sources absent")
+@pytest.mark.skipif(not __import__("oracle").ref_sources_available(), reason="reference sources absent")
 @pytest.mark.parametrize("case", GOLDEN_CASES)
 def test_port_bitwise_vs_compiled_reference(oracle_mod, case):
     oracle_mod.build_ref()
