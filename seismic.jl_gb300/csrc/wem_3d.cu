@@ -26,10 +26,10 @@
 namespace gbwem {
 
 // wavefield w (0 source, 1 receiver) steps at this depth: its zflag bit, and in the
-// modelling modes only the wavefield being continued (1: source, 2: receiver)
+// modelling and angle modes only the wavefield being continued (1, 3: source; 2: receiver)
 __device__ __forceinline__ bool m3_active(const Mig3dArgs &a, uint8_t zf, int w)
 {
-    if (a.mode == 1 && w != 0) return false;
+    if ((a.mode == 1 || a.mode == 3) && w != 0) return false;
     if (a.mode == 2 && w != 1) return false;
     return (zf & (w == 0 ? Z_SRC : Z_REC)) != 0;
 }
@@ -63,8 +63,9 @@ __global__ void __launch_bounds__(256) wem3d_rows_fwd_kernel(const Mig3dArgs a)
             const int y = t + TY * m;
             v[m] = y < a.nmy ? urow[y] : make_float2(0.f, 0.f);
         }
-        if (a.mode == 2) {
-            // receiver going up: inject m * smig (wem.c:270-272), then for split-step the
+        if (a.mode == 2 || a.mode == 3) {
+            // mode 2, receiver going up: inject m * smig (wem.c:270-272); modes 2 and 3 (the
+            // angle computation's source, ssop_source wem.c:763-776): for split-step the
             // taper and the correction come before the transform (ssop adj=false, wem.c:321-330)
             const size_t zrow = (size_t)a.iz * n + (size_t)x * a.nmy;
             const float2 *sm = a.smig + ((size_t)item * a.nz + a.iz) * n + (size_t)x * a.nmy;
@@ -73,10 +74,12 @@ __global__ void __launch_bounds__(256) wem3d_rows_fwd_kernel(const Mig3dArgs a)
             for (int m = 0; m < 16; m++) {
                 const int y = t + TY * m;
                 if (y < a.nmy) {
-                    const float mv = a.mimg[zrow + y];
-                    const float2 s_ = sm[y];
-                    v[m].x += mv * s_.x;
-                    v[m].y += mv * s_.y;
+                    if (a.mode == 2) {
+                        const float mv = a.mimg[zrow + y];
+                        const float2 s_ = sm[y];
+                        v[m].x += mv * s_.x;
+                        v[m].y += mv * s_.y;
+                    }
                     if (!a.pspi) {
                         const float tp = a.taper[x] * a.tapery[y];
                         float sn, cs;
@@ -325,7 +328,7 @@ __global__ void __launch_bounds__(256, 2) wem3d_rows_inv_kernel(const Mig3dArgs 
                     float2 q = make_float2(0.f, 0.f);
                     if (y < nmy) {
                         q = acc[m];
-                        if (!PSPI && a.mode != 2) {
+                        if (!PSPI && a.mode != 2 && a.mode != 3) {
                             // split-step correction and taper (wem.c:349-359), -dz for the source
                             const float th = __fmul_rn(__fmul_rn(wv, a.pd[(size_t)iz * n + (size_t)x * nmy + y]), a.dz);
                             float sn, cs;
@@ -338,7 +341,7 @@ __global__ void __launch_bounds__(256, 2) wem3d_rows_inv_kernel(const Mig3dArgs 
                     }
                     unew[m] = q;
                 }
-                if (a.mode == 1) {  // keep the source of this depth (wem.c:260)
+                if (a.mode == 1 || a.mode == 3) {  // keep the source of this depth (wem.c:260, 720)
                     float2 *sm = a.smig + ((size_t)item * a.nz + iz) * n + (size_t)x * nmy;
 #pragma unroll
                     for (int m = 0; m < 16; m++) {
@@ -353,7 +356,7 @@ __global__ void __launch_bounds__(256, 2) wem3d_rows_inv_kernel(const Mig3dArgs 
                     unew[m] = y < nmy ? urow[y] : make_float2(0.f, 0.f);
                 }
             }
-            if (a.mode == 1 && w == 0 && !active) {  // no source above its depth (wem.c:262-264)
+            if ((a.mode == 1 || a.mode == 3) && w == 0 && !active) {  // none above its depth (wem.c:262-264)
                 float2 *sm = a.smig + ((size_t)item * a.nz + iz) * n + (size_t)x * nmy;
 #pragma unroll
                 for (int m = 0; m < 16; m++) {

@@ -20,7 +20,10 @@
 //   3. wem_angles_accum_kernel: per grid point, in frequency order,
 //      ang += (180/pi) atan(|u_x| / (|u_z| + 1e-10)) and sign += +-|u| / nw, then
 //      ang *= sign(sign) / (ifmax - ifmin + 1) (wem.c:675-676, 735-754).
-// In 2-D the y terms vanish: u_y = 0 gives angy = 0 (the reference's value).
+// In 2-D the y terms vanish: u_y = 0 gives angy = 0 (the reference's value). 3-D grids
+// (power-of-two nmx, nmy) continue the source with the plane passes of wem_3d.cu (mode 3)
+// and take x, y and z transforms of every depth volume (wem_axis_dft_kernel, any stride);
+// wem_angles_accum3_kernel sums over batches of frequencies.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -324,6 +327,43 @@ __global__ void __launch_bounds__(256) wem_angles_accum_kernel(const AngleAccumA
     }
     a.angx[(size_t)x * a.nz + z] = ang * ((sgn >= 0.f ? 1.f : -1.f) / (float)a.nfreq_div);
     if (a.angy) a.angy[(size_t)x * a.nz + z] = 0.f;  // 2-D: u_y = 0
+}
+
+// 3-D (wem.c:735-754 with both lateral axes): per grid point (cell, z), the frequencies of
+// a batch in order, added to the running sums of the earlier batches.
+__global__ void __launch_bounds__(256) wem_angles_accum3_kernel(const AngleAccum3Args a)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long np = (long long)a.n * a.nz;
+    if (p >= np) return;
+    const int z = (int)(p / a.n), cell = (int)(p - (long long)z * a.n);
+    const size_t vol = (size_t)a.nz * a.n, off = (size_t)z * a.n + cell, o = (size_t)cell * a.nz + z;
+    float ax = a.sum[o], sx = a.sum[np + o], ay = a.sum[2 * np + o], sy = a.sum[3 * np + o];
+    for (int f = 0; f < a.nwf; f++) {
+        const size_t q = (size_t)f * vol + off;
+        const float au = hypotf(a.u[q].x, a.u[q].y);
+        const float az = hypotf(a.uz[q].x, a.uz[q].y) + 1e-10f;
+        ax += (float)(57.295779513082323 * (double)atanf(hypotf(a.ux[q].x, a.ux[q].y) / az));
+        ay += (float)(57.295779513082323 * (double)atanf(hypotf(a.uy[q].x, a.uy[q].y) / az));
+        sx += (hypotf(a.lx[q].x, a.lx[q].y) >= hypotf(a.rx[q].x, a.rx[q].y) ? au : -au) / (float)a.nw;
+        sy += (hypotf(a.ly[q].x, a.ly[q].y) >= hypotf(a.ry[q].x, a.ry[q].y) ? au : -au) / (float)a.nw;
+    }
+    if (a.last) {
+        a.angx[o] = ax * ((sx >= 0.f ? 1.f : -1.f) / (float)a.nfreq_div);
+        a.angy[o] = ay * ((sy >= 0.f ? 1.f : -1.f) / (float)a.nfreq_div);
+    } else {
+        a.sum[o] = ax;
+        a.sum[np + o] = sx;
+        a.sum[2 * np + o] = ay;
+        a.sum[3 * np + o] = sy;
+    }
+}
+
+int launch_angles_accum3(const AngleAccum3Args &a, cudaStream_t st)
+{
+    const long long n = (long long)a.n * a.nz;
+    wem_angles_accum3_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_angles_extrap(const AngleArgs &a, cudaStream_t st)

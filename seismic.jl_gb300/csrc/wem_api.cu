@@ -853,6 +853,215 @@ extern "C" int wem_migrate(wem_ctx *c, int nshot, const float *sx, const float *
 }
 
 // ---------------------------------------------------------------- incidence angles
+// 3-D (nmy > 1), compute_angles with both lateral axes: per shot and batch of frequencies
+// the source is continued down with the plane passes of wem_3d.cu (mode 3, ssop_source's
+// split-step step on the unpadded plane, every depth kept), then one-axis transforms
+// give u_x, u_y, u_z and the left/right parts along x and y of every depth volume, and
+// wem_angles_accum3_kernel adds the batch to the running sums. nmx and nmy must be powers
+// of two in [64, 1024] (the plane FFTs of wem_3d.cu).
+static int angles3d(wem_ctx *c, const wem_params &p, const float *vel, const float *wav, int nshot, const float *sx,
+                    const float *sy, float *angx, float *angy)
+{
+    const int nmx = p.nmx, nmy = p.nmy, nz = p.nz, n = nmx * nmy;
+    if (!m3d_supported(nmx, nmy))
+        return fail(WEM_ERR_SIZE, "wem_angles: 3-D needs nmx = %d and nmy = %d to be powers of two in [64, 1024]", nmx,
+                    nmy);
+    if (!(p.dmy > 0)) return fail(WEM_ERR_ARG, "wem_angles: 3-D needs dmy > 0");
+    CK(cudaSetDevice(c->device));
+    cudaStream_t st = c->st;
+    wem_params q = p;
+    q.padt = 1;
+    int ntfft, nw, ifmin, ifmax;
+    float dw;
+    freq_grid(q, &ntfft, &nw, &ifmin, &ifmax, &dw);
+    const int nwf = ifmax - ifmin;
+    const size_t nn = (size_t)n * nz;
+    if (nwf < 1) {
+        memset(angx, 0, sizeof(float) * nn * nshot);
+        if (angy) memset(angy, 0, sizeof(float) * nn * nshot);
+        return WEM_OK;
+    }
+    // slowness split of compute_angles (wem.c:609-618), depth-major; taper; depth flags
+    std::vector<float> po(nz), pd(nn);
+    std::vector<uint8_t> zf(nz);
+    for (int iz = 0; iz < nz; iz++) {
+        float s = 0.;
+        for (int ix = 0; ix < n; ix++) s += vel[(size_t)ix * nz + iz];
+        s /= (float)nmx * nmy;
+        s = 1. / s;
+        po[iz] = s;
+        for (int ix = 0; ix < n; ix++) pd[(size_t)iz * n + ix] = 1.0 / vel[(size_t)ix * nz + iz] - po[iz];
+        const float z = p.oz + p.dz * iz;
+        zf[iz] = z >= p.sz ? Z_SRC : 0;
+    }
+    const std::vector<float> tx = taper_of(nmx), ty = taper_of(nmy);
+    std::vector<float2> fx(twiddle_table_size(nmx)), fy(twiddle_table_size(nmy));
+    twiddle_table_host(nmx, fx.data());
+    twiddle_table_host(nmy, fy.data());
+    auto dft_table = [](int L) {
+        std::vector<float2> w(L);
+        for (int k = 0; k < L; k++) {
+            const double a = -6.283185307179586476925286766559 * k / L;
+            w[k] = make_float2((float)cos(a), (float)sin(a));
+        }
+        return w;
+    };
+    const int lop = (nw - 1) * 2;
+    const std::vector<float2> wt = dft_table(lop), wx = dft_table(nmx), wy = dft_table(nmy), wz = dft_table(nz);
+    const float dkx = 2 * 3.141592653589793 / ((float)nmx) / p.dmx;
+    const float dky = 2 * 3.141592653589793 / ((float)nmy) / p.dmy;
+    const float dkz = 2 * 3.141592653589793 / ((float)nz) / p.dz;
+    std::vector<float> sc(nwf, 1.f / sqrtf((float)ntfft));
+    // frequencies per batch: 9 depth volumes each, within half of the free memory
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const size_t per_f = sizeof(float2) * ((size_t)9 * nn + (size_t)6 * n);
+    const int batch = (int)std::max<long long>(1, std::min<long long>(nwf, (long long)(free_b / 2 / per_f)));
+    const size_t vol = sizeof(float2) * (size_t)batch * nn;
+    DevBuf bpo, bpd, btx, bty, bfx, bfy, bwt, bwx, bwy, bwz, bsc, bsrc, bbase, bwav, bzf, bitems, bcell, bU, bY, bC, bS,
+        bT, bSX, bLX, bRX, bSY, bLY, bRY, bSZ, bsum, bang;
+    auto release = [&]() {
+        DevBuf *bs[] = { &bpo, &bpd, &btx, &bty, &bfx, &bfy, &bwt, &bwx, &bwy, &bwz, &bsc, &bsrc, &bbase, &bwav, &bzf,
+                         &bitems, &bcell, &bU, &bY, &bC, &bS, &bT, &bSX, &bLX, &bRX, &bSY, &bLY, &bRY, &bSZ, &bsum,
+                         &bang };
+        for (DevBuf *b : bs)
+            if (b->p) cudaFree(b->p);
+    };
+    int rc;
+    if ((rc = ensure(bpo, sizeof(float) * nz)) || (rc = ensure(bpd, sizeof(float) * nn)) ||
+        (rc = ensure(btx, sizeof(float) * nmx)) || (rc = ensure(bty, sizeof(float) * nmy)) ||
+        (rc = ensure(bfx, sizeof(float2) * fx.size())) || (rc = ensure(bfy, sizeof(float2) * fy.size())) ||
+        (rc = ensure(bwt, sizeof(float2) * lop)) || (rc = ensure(bwx, sizeof(float2) * nmx)) ||
+        (rc = ensure(bwy, sizeof(float2) * nmy)) || (rc = ensure(bwz, sizeof(float2) * nz)) ||
+        (rc = ensure(bsc, sizeof(float) * nwf)) || (rc = ensure(bsrc, sizeof(float2) * nwf)) ||
+        (rc = ensure(bbase, sizeof(int64_t))) || (rc = ensure(bwav, sizeof(float) * p.nt)) || (rc = ensure(bzf, nz)) ||
+        (rc = ensure(bitems, sizeof(int) * 2 * (size_t)nwf)) || (rc = ensure(bcell, sizeof(int))) ||
+        (rc = ensure(bU, sizeof(float2) * (size_t)batch * 2 * n)) || (rc = ensure(bY, sizeof(float2) * (size_t)batch * 2 * n)) ||
+        (rc = ensure(bC, sizeof(float2) * (size_t)batch * 2 * n)) || (rc = ensure(bS, vol)) || (rc = ensure(bT, vol)) ||
+        (rc = ensure(bSX, vol)) || (rc = ensure(bLX, vol)) || (rc = ensure(bRX, vol)) || (rc = ensure(bSY, vol)) ||
+        (rc = ensure(bLY, vol)) || (rc = ensure(bRY, vol)) || (rc = ensure(bSZ, vol)) ||
+        (rc = ensure(bsum, sizeof(float) * 4 * nn)) || (rc = ensure(bang, sizeof(float) * 2 * nn))) {
+        release();
+        return rc;
+    }
+#define CKR(call)                                                                                                 \
+    do {                                                                                                          \
+        cudaError_t e_ = (call);                                                                                  \
+        if (e_ != cudaSuccess) {                                                                                  \
+            release();                                                                                            \
+            return fail(WEM_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);     \
+        }                                                                                                         \
+    } while (0)
+#define LCHK(expr, what)                                                                                          \
+    do {                                                                                                          \
+        if (expr) {                                                                                               \
+            release();                                                                                            \
+            return fail(WEM_ERR_CUDA, "angles: %s launch: %s", what, cudaGetErrorString(cudaGetLastError()));    \
+        }                                                                                                         \
+    } while (0)
+    std::vector<int> items(2 * (size_t)nwf, 0);  // [iwi][shot = 0]
+    for (int f = 0; f < nwf; f++) items[f] = f;
+    const int64_t zero = 0;
+    CKR(cudaMemcpyAsync(bpo.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bpd.p, pd.data(), sizeof(float) * nn, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(btx.p, tx.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bty.p, ty.data(), sizeof(float) * nmy, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bfx.p, fx.data(), sizeof(float2) * fx.size(), cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bfy.p, fy.data(), sizeof(float2) * fy.size(), cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bwt.p, wt.data(), sizeof(float2) * lop, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bwx.p, wx.data(), sizeof(float2) * nmx, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bwy.p, wy.data(), sizeof(float2) * nmy, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bwz.p, wz.data(), sizeof(float2) * nz, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bsc.p, sc.data(), sizeof(float) * nwf, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bbase.p, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bwav.p, wav, sizeof(float) * p.nt, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bzf.p, zf.data(), nz, cudaMemcpyHostToDevice, st));
+    CKR(cudaMemcpyAsync(bitems.p, items.data(), sizeof(int) * items.size(), cudaMemcpyHostToDevice, st));
+    SpectraArgs sa{};
+    sa.d = P<float>(bwav); sa.ntr = 1; sa.nt = p.nt < lop ? p.nt : lop; sa.ntfft = lop; sa.ifmin = ifmin; sa.nwf = nwf;
+    sa.out_base = P<int64_t>(bbase); sa.out_fstride = 1; sa.wtab = P<float2>(bwt); sa.scale = P<float>(bsc);
+    sa.out = P<float2>(bsrc);
+    LCHK(launch_spectra(sa, st), "spectra");
+    int kernels = 1;
+    CKR(cudaEventRecord(c->ev0, st));
+    for (int s = 0; s < nshot; s++) {
+        const float ys = sy ? sy[s] : 0.f;
+        const int igx = (int)((float)(int)(sx[s] - p.omx) / p.dmx);  // wem.c:654-655
+        const int igy = (int)((float)(int)(ys - p.omy) / p.dmy);
+        if (igx < 0 || igx >= nmx || igy < 0 || igy >= nmy) {
+            release();
+            return fail(WEM_ERR_ARG, "wem_angles: shot %d at (%g, %g) is outside the grid", s, (double)sx[s], (double)ys);
+        }
+        const int cell = igx * nmy + igy;
+        CKR(cudaMemcpyAsync(bcell.p, &cell, sizeof(int), cudaMemcpyHostToDevice, st));
+        CKR(cudaMemsetAsync(bsum.p, 0, sizeof(float) * 4 * nn, st));
+        for (int b0 = 0; b0 < nwf; b0 += batch) {
+            const int nb = std::min(batch, nwf - b0);
+            Mig3dArgs a{};
+            a.nmx = nmx; a.nmy = nmy; a.nkx = nmx; a.nky = nmy; a.nz = nz; a.nref = 1; a.nwf = nwf;
+            a.ifmin = ifmin; a.nitems = nb; a.chunk = 32; a.dw = dw; a.dz = p.dz; a.dkx = dkx; a.dky = dky;
+            a.inv_n = 1.0f / ((float)nmx * nmy);
+            a.po = P<float>(bpo); a.pd = P<float>(bpd); a.taper = P<float>(btx); a.tapery = P<float>(bty);
+            a.zflag = P<uint8_t>(bzf); a.twx = P<float2>(bfx); a.twy = P<float2>(bfy);
+            a.item_iwi = P<int>(bitems) + b0; a.item_shot = P<int>(bitems) + nwf;  // shot 0 for every item
+            a.src_cell = P<int>(bcell); a.srcw = P<float2>(bsrc);
+            a.U = P<float2>(bU); a.Y = P<float2>(bY); a.C = P<float2>(bC); a.smig = P<float2>(bS);
+            a.mode = 3; a.pspi = 0;
+            LCHK(m3d_launch_init(a, st), "3-D init");
+            for (int iz = 0; iz < nz; iz++) {
+                a.iz = iz;
+                LCHK(m3d_launch_step(nmx, nmy, 0, 0, a, c->nsm, st), "3-D source step");
+            }
+            kernels += 1 + 3 * nz;
+            // one-axis transforms of the depth volumes [f][z][x][y]
+            const long long nbl = nb;
+            AxisDftArgs ax{};  // x lines: stride nmy
+            ax.nlines = nbl * nz * nmy; ax.nb = nmy; ax.sa = n; ax.sb = 1; ax.se = nmy; ax.L = nmx; ax.dk = dkx;
+            ax.tw = P<float2>(bwx);
+            AxisDftArgs ay{};  // y lines: contiguous
+            ay.nlines = nbl * nz * nmx; ay.nb = 1; ay.sa = nmy; ay.sb = 0; ay.se = 1; ay.L = nmy; ay.dk = dky;
+            ay.tw = P<float2>(bwy);
+            AxisDftArgs az{};  // z lines: stride n
+            az.nlines = nbl * n; az.nb = n; az.sa = (long long)nz * n; az.sb = 1; az.se = n; az.L = nz; az.dk = dkz;
+            az.tw = P<float2>(bwz);
+            struct Step { AxisDftArgs base; const DevBuf *in; DevBuf *out; int sign, mode; float scale; };
+            const Step steps[] = {
+                { ax, &bS, &bT, -1, 0, 1.f }, { ax, &bT, &bSX, +1, 1, 1.f / (float)nmx },
+                { ax, &bT, &bLX, +1, 2, 1.f }, { ax, &bT, &bRX, +1, 3, 1.f },
+                { ay, &bS, &bT, -1, 0, 1.f }, { ay, &bT, &bSY, +1, 1, 1.f / (float)nmy },
+                { ay, &bT, &bLY, +1, 2, 1.f }, { ay, &bT, &bRY, +1, 3, 1.f },
+                { az, &bS, &bT, -1, 0, 1.f }, { az, &bT, &bSZ, +1, 1, 1.f / (float)nz },
+            };
+            for (const Step &sp : steps) {
+                AxisDftArgs d = sp.base;
+                d.in = reinterpret_cast<const float2 *>(sp.in->p);
+                d.out = reinterpret_cast<float2 *>(sp.out->p);
+                d.sign = sp.sign; d.mode = sp.mode; d.scale = sp.scale;
+                LCHK(launch_axis_dft(d, st), "axis transform");
+            }
+            AngleAccum3Args ac{};
+            ac.n = n; ac.nz = nz; ac.nwf = nb; ac.nw = nw; ac.nfreq_div = ifmax - ifmin + 1;
+            ac.last = b0 + nb >= nwf;
+            ac.u = P<float2>(bS); ac.ux = P<float2>(bSX); ac.uy = P<float2>(bSY); ac.uz = P<float2>(bSZ);
+            ac.lx = P<float2>(bLX); ac.rx = P<float2>(bRX); ac.ly = P<float2>(bLY); ac.ry = P<float2>(bRY);
+            ac.sum = P<float>(bsum); ac.angx = P<float>(bang); ac.angy = P<float>(bang) + nn;
+            LCHK(launch_angles_accum3(ac, st), "accumulation");
+            kernels += 11;
+        }
+        CKR(cudaMemcpyAsync(angx + (size_t)s * nn, bang.p, sizeof(float) * nn, cudaMemcpyDeviceToHost, st));
+        if (angy) CKR(cudaMemcpyAsync(angy + (size_t)s * nn, P<float>(bang) + nn, sizeof(float) * nn, cudaMemcpyDeviceToHost, st));
+        CKR(cudaStreamSynchronize(st));
+    }
+    CKR(cudaEventRecord(c->ev1, st));
+    CKR(cudaStreamSynchronize(st));
+#undef CKR
+#undef LCHK
+    release();
+    cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1);
+    c->last_kernels = kernels;
+    return WEM_OK;
+}
+
 // compute_angles (wem.c:566-684) for each shot: the band [fmin, fmax] of the unpadded
 // time axis (ntfft = nt), no spatial padding; any grid length (direct transforms).
 extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, const float *wav, int nshot,
@@ -863,7 +1072,7 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     const wem_params &p = *pp;
     if (p.nt < 2 || p.nmx < 1 || p.nz < 1 || !(p.dt > 0) || !(p.dmx > 0) || !(p.dz > 0))
         return fail(WEM_ERR_ARG, "wem_angles: invalid grid (nt=%d nmx=%d nz=%d)", p.nt, p.nmx, p.nz);
-    if (p.nmy != 1) return fail(WEM_ERR_SIZE, "wem_angles: incidence angles are built for 2-D grids (nmy = 1)");
+    if (p.nmy != 1) return angles3d(c, p, vel, wav, nshot, sx, sy, angx, angy);
     const int nmx = p.nmx, nz = p.nz;
     if (nmx > 4096) return fail(WEM_ERR_SIZE, "wem_angles: nmx = %d above 4096", nmx);
     CK(cudaSetDevice(c->device));

@@ -88,7 +88,9 @@ struct Mig3dArgs {
     float2 *C;          // [item][2][nref][nmx][nky]
     float2 *img_parts;  // [chunk][nz][nmx*nmy] (sum, 0)
     // modelling (wem.c:252-281): mode 1 continues the source down and keeps it in smig;
-    // mode 2 continues the receiver up (-dz, adj=false) with m * smig injected first
+    // mode 2 continues the receiver up (-dz, adj=false) with m * smig injected first;
+    // mode 3 continues the source down as the angle computation does (ssop_source: the
+    // split-step correction before the transform) and keeps it in smig
     int mode, pspi;     // mode 0: migration
     float2 *smig;       // [item][nz][nmx*nmy]
     const float *mimg;  // [nz][nmx*nmy] image, depth-major
@@ -127,6 +129,14 @@ struct AngleAccumArgs {
     const float2 *u, *ux, *uz, *ul, *ur;  // [nwf][nz][nmx]
     float *angx, *angy;                   // [nmx][nz]
 };
+// 3-D: running sums over batches of frequencies, one point per thread
+struct AngleAccum3Args {
+    int n, nz, nwf, nw, nfreq_div, last;  // n = nmx*nmy; last: write the angles after this batch
+    const float2 *u, *ux, *uy, *uz, *lx, *rx, *ly, *ry;  // [nwf][nz][n]
+    float *sum;                                          // [4][n][nz]: ang x, sign x, ang y, sign y
+    float *angx, *angy;                                  // [n][nz]
+};
+int launch_angles_accum3(const AngleAccum3Args &a, cudaStream_t st);
 struct AngleXArgs {
     long long nlines;                  // rows of nmx samples (frequency, depth)
     float dkx;

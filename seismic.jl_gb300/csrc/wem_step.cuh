@@ -241,7 +241,7 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
                 u[m] = conj ? cmulc(v[m], P) : cmul(v[m], P);
             }
             fft_row<N, +1, TC>(u, xbuf, sm.tw, t, sync, tc);
-            if (INTERP == 0) {
+            if constexpr (INTERP == 0) {
                 // the nearest-lower wavefield, whole or its real part (wem.c:454-459, 477):
                 // the positions that take reference r, found four at a time
                 const uint32_t rr = (uint32_t)r * 0x01010101u;
@@ -258,23 +258,23 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
                         }
                     }
                 }
-                continue;
-            }
+            } else {
 #pragma unroll
-            for (int m = 0; m < 16; m++) {
-                const uint32_t b = (selp[m >> 2] >> (8 * (m & 3))) & 0xffu;
-                const int i1 = (int)(b & 0x7fu);
-                const bool interp = (b & 0x80u) != 0;
-                float2 *dst = sacc + m * T + t;
-                if (!interp) {
-                    if (r == i1) *dst = u[m];
-                } else if (r == i1) {
-                    const float w1 = 1.f - sm.wl[t + T * m];
-                    *dst = make_float2(u[m].x * w1, u[m].y * w1);
-                } else if (r == i1 + 1) {
-                    const float w2 = sm.wl[t + T * m];
-                    const float2 q = *dst;
-                    *dst = make_float2(q.x + u[m].x * w2, q.y + u[m].y * w2);
+                for (int m = 0; m < 16; m++) {
+                    const uint32_t b = (selp[m >> 2] >> (8 * (m & 3))) & 0xffu;
+                    const int i1 = (int)(b & 0x7fu);
+                    const bool interp = (b & 0x80u) != 0;
+                    float2 *dst = sacc + m * T + t;
+                    if (!interp) {
+                        if (r == i1) *dst = u[m];
+                    } else if (r == i1) {
+                        const float w1 = 1.f - sm.wl[t + T * m];
+                        *dst = make_float2(u[m].x * w1, u[m].y * w1);
+                    } else if (r == i1 + 1) {
+                        const float w2 = sm.wl[t + T * m];
+                        const float2 q = *dst;
+                        *dst = make_float2(q.x + u[m].x * w2, q.y + u[m].y * w2);
+                    }
                 }
             }
         }

@@ -110,6 +110,13 @@ def angles_main():
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), vel=c["vel"], wav=c["wav"], angx=ax, angy=ay,
                             params=np.array(repr(p)))
         print(name, "angx range", float(ax.min()), float(ax.max()), "angy max", float(np.abs(ay).max()))
+    # 3-D: both lateral axes (rank-3 transforms over nkx, nky, nkz, wem.c:630-641)
+    c = synth.small_case3d(35, nx=64, ny=64, nz=8, nt=64, nshot=1, pspi=0, fmax=30.0)
+    p = dict(c["params"], sx=float(c["shots"].sx[0]), sy=float(c["shots"].sy[0]))
+    ax, ay = O.angles_ref(p, c["vel"], c["wav"])
+    np.savez_compressed(os.path.join(HERE, "angles3d_64.npz"), vel=c["vel"], wav=c["wav"], angx=ax, angy=ay,
+                        params=np.array(repr(p)))
+    print("angles3d_64 angx range", float(ax.min()), float(ax.max()), "angy range", float(ay.min()), float(ay.max()))
 
 
 if __name__ == "__main__":

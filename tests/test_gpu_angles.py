@@ -49,7 +49,38 @@ def test_angles_any_depth_count_matches_fp64_oracle(gpu_lib):
         assert np.all(ax[i][:, :5] == 0) and np.abs(want[:, :5]).max() < 1e-9  # above sz = 50 m
 
 
-def test_angles_reject_3d(gpu_lib):
+def test_angles_3d_match_reference_golden(gpu_lib):
+    """Both lateral axes (nmy > 1): angx and angy against the reference's compute_angles."""
+    g = load_golden("angles3d_64.npz")
+    p = g["params"]
+    with gpu_lib.Context() as ctx:
+        ax, ay = ctx.angles(p, g["vel"], g["wav"], [p["sx"]], [p["sy"]])
+    for got, ref in ((ax[0], g["angx"]), (ay[0], g["angy"])):
+        assert rel_l2(got, ref) < TOL, rel_l2(got, ref)
+        live = np.abs(ref) > 1e-3
+        assert np.count_nonzero(np.sign(got[live]) != np.sign(ref[live])) == 0
+
+
+def test_angles_3d_matches_fp64_oracle(gpu_lib):
+    """A 64 x 128 plane, 12 depth steps (a z axis of any length), a source depth below the
+    surface, two shots in one call."""
+    import angles_np as A
+    from wemgpu import synth
+    c = synth.small_case3d(36, nx=64, ny=128, nz=12, nt=64, nshot=1, pspi=0, fmax=25.0)
+    p = dict(c["params"], sz=15.0)
+    xs, ys = [200.0, 450.0], [300.0, 900.0]
+    with gpu_lib.Context() as ctx:
+        ax, ay = ctx.angles(p, c["vel"], c["wav"], xs, ys)
+    for i in range(2):
+        wx, wy = A.compute_angles(dict(p, sx=xs[i], sy=ys[i]), c["vel"], c["wav"])
+        for got, want in ((ax[i], wx), (ay[i], wy)):
+            assert rel_l2(got, want) < TOL, rel_l2(got, want)
+            live = np.abs(want) > 1e-3
+            assert np.count_nonzero(np.sign(got[live]) != np.sign(want[live])) == 0
+
+
+def test_angles_reject_unsupported_3d_planes(gpu_lib):
+    """3-D planes must be powers of two in [64, 1024] along x and y."""
     from wemgpu import synth
     from wemgpu._lib import WemError
     c = synth.small_case3d(34, nx=32, ny=32, nz=8, nt=64, pspi=0)

@@ -138,3 +138,16 @@ def test_angle_oracle_matches_reference_golden(case):
     assert np.count_nonzero(np.sign(ax) != np.sign(g["angx"])) == 0
     assert np.all(ay == 0) and np.all(g["angy"] == 0)
     assert np.abs(g["angx"]).max() > 30.0  # a real angle section, not zeros
+
+
+def test_angle_oracle_matches_reference_golden_3d():
+    """Both lateral axes: angx and angy of the reference's compute_angles on a 64 x 64 x 8
+    grid (rank-3 transforms, wem.c:630-641)."""
+    import angles_np as A
+    g = load_golden("angles3d_64.npz")
+    ax, ay = A.compute_angles(g["params"], g["vel"], g["wav"])
+    for got, ref in ((ax, g["angx"]), (ay, g["angy"])):
+        assert rel_l2(got, ref) < 1e-4
+        live = np.abs(ref) > 1e-3
+        assert np.count_nonzero(np.sign(got[live]) != np.sign(ref[live])) == 0
+        assert np.abs(ref).max() > 30.0
