@@ -100,6 +100,43 @@ def flops_per_unit(p: dict) -> float:
     return 2 * F + 3 * n
 
 
+def inverse_transforms_per_step(p: dict, vel: np.ndarray, paired: bool) -> float:
+    """Mean inverse transforms per wavefield step of the 2-D PSPI depth kernel over the
+    depth steps: one per reference some point takes its wavefield from; in the paired
+    form of the nearest-lower mode (interp=ref) one per two references whose every taker
+    keeps the real part only, and one per reference taken whole somewhere. The selection
+    restates the float arithmetic of wem.c:40-70."""
+    f32 = np.float32
+    nref, nmx = int(p["nref"]), int(p["nmx"])
+    vel = np.asarray(vel, f32).reshape(-1, int(p["nz"]))
+    total = 0
+    for iz in range(vel.shape[1]):
+        v = vel[:, iz]
+        vmin = f32(v[:nmx].min())
+        vmax = f32(max(v[nmx - 1], v.max()))
+        ir = np.arange(nref, dtype=f32)
+        vref = vmin + ir * (vmax - vmin) / (f32(nref) - f32(1))
+        if vmax > vmin + f32(10):
+            i = ((f32(nref - 1) * (v - vmin)) / (vmax - vmin)).astype(np.int64)
+            i1 = np.where(i > nref - 2, nref - 1, i)
+            i2 = np.where(i > nref - 2, nref - 1, i + 1)
+        else:
+            i1 = i2 = np.zeros(v.shape, np.int64)
+        interp = (vref[i2] - vref[i1]).astype(np.float64) > 10.0
+        used = set(i1.tolist())
+        if p.get("interp", "ref") == "linear":
+            used |= set((i1[interp] + 1).tolist())
+            total += len(used)
+            continue
+        if not paired:
+            total += len(used)
+            continue
+        whole = set(i1[~interp].tolist())
+        ro = len(used - whole)
+        total += len(whole) + ro // 2 + ro % 2
+    return total / vel.shape[1]
+
+
 def tensor_flops_per_unit(p: dict) -> float:
     """Tensor-core FLOPs one (shot, frequency, depth step) executes in split16 mode: every
     radix-16 pass of a 2048-sample row is M=128 x N=32 x K=32 per product and the radix-8
@@ -500,6 +537,10 @@ def main():
             "kernel": "wem_migrate_kernel", "ms_per_launch": mig_ms,
             "flops_per_unit": fl, "fp32_nominal_tflops": fp32_nominal,
             "fp32_frac": achieved / fp32_nominal}
+    if int(p.get("pspi", 1)) and int(p.get("nmy", 1)) == 1:
+        paired = p.get("interp", "ref") == "ref" and os.environ.get("WEM_PAIRED", "1") != "0" and \
+            p.get("precision", "fp32") == "fp32"
+        roof["inverse_transforms_per_wavefield_step"] = inverse_transforms_per_step(p, c["vel"], paired)
     if p.get("precision", "fp32") == "split16":
         tf = tensor_flops_per_unit(p)
         tach = units * tf / (mig_ms / 1000.0) / 1e12

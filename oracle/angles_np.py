@@ -53,9 +53,11 @@ def taper(nm: int) -> np.ndarray:
     return t
 
 
-def compute_angles(p: dict, vel: np.ndarray, wav: np.ndarray):
+def compute_angles(p: dict, vel: np.ndarray, wav: np.ndarray, sign_margin: bool = False):
     """angx, angy [nmx*nmy, nz] (float64) of one shot at (p["sx"], p["sy"]).
-    vel [nmx*nmy, nz]; wav [nt]."""
+    vel [nmx*nmy, nz]; wav [nt].
+    sign_margin: also return, per point and axis, |sign sum| / (sum of |u|/nw), the
+    margin by which the side the energy arrives from is decided (0: undecided)."""
     nt, dt = int(p["nt"]), float(p["dt"])
     nmx, nmy, nz = int(p["nmx"]), int(p.get("nmy", 1)), int(p["nz"])
     dmx, dmy, dz = float(p["dmx"]), float(p.get("dmy", p["dmx"])), float(p["dz"])
@@ -82,6 +84,7 @@ def compute_angles(p: dict, vel: np.ndarray, wav: np.ndarray):
     angy = np.zeros((nmx, nmy, nz))
     sgx = np.zeros((nmx, nmy, nz))
     sgy = np.zeros((nmx, nmy, nz))
+    sgw = np.zeros((nmx, nmy, nz))
     KX, KY = np.meshgrid(kx, ky, indexing="ij")
     nk = nmx * nmy
     dzs = -dz  # extrapolate_source passes -dz to ssop_source (wem.c:719)
@@ -118,9 +121,16 @@ def compute_angles(p: dict, vel: np.ndarray, wav: np.ndarray):
         sgx += np.where(ul >= ur, 1.0, -1.0) * np.abs(us) / nw
         ul, ur = np.abs(np.fft.ifftn(1j * kyl * A)), np.abs(np.fft.ifftn(1j * kyr * A))
         sgy += np.where(ul >= ur, 1.0, -1.0) * np.abs(us) / nw
+        sgw += np.abs(us) / nw
         angx += (180 / PI) * np.arctan(np.abs(usx) / (np.abs(usz) + 1e-10))
         angy += (180 / PI) * np.arctan(np.abs(usy) / (np.abs(usz) + 1e-10))
     nfreq = ifmax - ifmin + 1  # wem.c:676 divides by ifmax - ifmin + 1
     angx *= np.where(sgx >= 0, 1.0, -1.0) / nfreq
     angy *= np.where(sgy >= 0, 1.0, -1.0) / nfreq
+    if sign_margin:
+        with np.errstate(invalid="ignore", divide="ignore"):
+            mx = np.where(sgw > 0, np.abs(sgx) / sgw, 0.0)
+            my = np.where(sgw > 0, np.abs(sgy) / sgw, 0.0)
+        return (angx.reshape(nmx * nmy, nz), angy.reshape(nmx * nmy, nz),
+                mx.reshape(nmx * nmy, nz), my.reshape(nmx * nmy, nz))
     return angx.reshape(nmx * nmy, nz), angy.reshape(nmx * nmy, nz)

@@ -86,7 +86,8 @@ struct wem_ctx {
     DevBuf ssyn_ref, ssyn_exact;  // synthesis weights w^2 * (half-spectrum | image) factor
     DevBuf tapery, twy;           // 3-D: y taper and y-FFT twiddles
     DevBuf tcw, tcerr;            // split16: W operands of the tensor-core DFT stages, timeout word
-    DevBuf refmask;               // [nz] bit r: some grid point takes its wavefield from reference r
+    DevBuf refmask;               // [2][nz] bit r: some grid point takes its wavefield from reference r
+                                  // (all of it, in the second row)
     DevBuf m3_items, m3_U, m3_Y, m3_C, m3_parts;
     // per-call buffers
     DevBuf recv, slots, image, data, tbase, igx, smig, mimg;
@@ -100,6 +101,7 @@ struct wem_ctx {
     // the launch sequence of the last 2-D migration, captured as a CUDA graph and
     // replayed while nothing it depends on has changed
     bool use_graph = true;
+    bool paired = true;  // PSPI nearest-lower mode: the paired inverse transforms (WEM_PAIRED=0: off)
     cudaGraphExec_t gexec = nullptr;
     struct GraphKey {
         int nshot, wide, grid;
@@ -299,8 +301,10 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     std::vector<float> slow2((size_t)nz * nref);
     std::vector<uint8_t> sel((size_t)nz * n);
     // reference velocities some grid point of the depth takes its wavefield from: the
-    // others' inverse transforms are skipped (their results would not be used)
-    std::vector<unsigned long long> used(nz, 0ull);
+    // others' inverse transforms are skipped (their results would not be used); then
+    // (from nz on) those some point takes whole in the nearest-lower mode, where the
+    // others give real parts only (wem.c:454-458, 473-478)
+    std::vector<unsigned long long> used(2 * (size_t)nz, 0ull);
     for (int iz = 0; iz < nz; iz++) {
         float s = 0.;
         for (int ix = 0; ix < n; ix++) s += vel[(size_t)ix * nz + iz];
@@ -335,8 +339,9 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
             sel[(size_t)iz * n + ix] = word;
             used[iz] |= 1ull << i1;
             if ((word & SEL_INTERP) && p.interp == WEM_INTERP_LINEAR) used[iz] |= 1ull << (i1 + 1);
+            if (!(word & SEL_INTERP)) used[(size_t)nz + iz] |= 1ull << i1;
         }
-        if (!p.pspi) used[iz] = 1ull;
+        if (!p.pspi) used[iz] = used[(size_t)nz + iz] = 1ull;
     }
     // taper of the split-step operator (wem.c:546-564): tmx(imx) * tmy(imy)
     std::vector<float> taper = taper_of(nmx), tapery = taper_of(p.nmy);
@@ -389,14 +394,14 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         (rc = ensure(c->ssyn_exact, sizeof(float) * syn_exact.size())) ||
         (rc = ensure(c->tapery, sizeof(float) * tapery.size())) || (rc = ensure(c->twy, sizeof(float2) * twy.size())) ||
         (rc = ensure(c->tcw, 10240)) || (rc = ensure(c->tcerr, sizeof(int))) ||
-        (rc = ensure(c->refmask, sizeof(unsigned long long) * nz)))
+        (rc = ensure(c->refmask, sizeof(unsigned long long) * 2 * nz)))
         return rc;
     cudaStream_t st = c->st;
     std::vector<uint16_t> tcw(5120);
     tc_w_table_host(tcw.data());
     CK(cudaMemcpyAsync(c->tcw.p, tcw.data(), 10240, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(c->tcerr.p, 0, sizeof(int), st));
-    CK(cudaMemcpyAsync(c->refmask.p, used.data(), sizeof(unsigned long long) * nz, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->refmask.p, used.data(), sizeof(unsigned long long) * 2 * nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->po.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->pd.p, pd.data(), sizeof(float) * pd.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->vref.p, vref.data(), sizeof(float) * vref.size(), cudaMemcpyHostToDevice, st));
@@ -448,6 +453,10 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     c->dky = 2 * 3.141592653589793 / ((float)nky) / p.dmy;
     c->prepared = true;
     c->prep_gen++;
+    {
+        const char *e = getenv("WEM_PAIRED");
+        c->paired = !(e && !strcmp(e, "0"));
+    }
     c->last_nshot = -1;
     return WEM_OK;
 }
@@ -502,10 +511,26 @@ static int set_shots(wem_ctx *c, int nshot, const float *sx, const float *sy, co
 // keeps the faster one for that geometry. WEM_CTA_SHAPE=wide|narrow forces a shape;
 // WEM_AUTOTUNE=0 takes the wide shape whenever its shared memory fits.
 struct TuneEntry {
-    int device, nkx, pspi, interp, nmx, nref, prec, wide;
+    int device, nkx, pspi, interp, nmx, nref, prec, paired, wide;
 };
 
 static int tcmode(const wem_ctx *c) { return c->p.precision == WEM_PREC_SPLIT16 ? 1 : 0; }
+
+// the form of the 2-D depth kernel for a CTA shape: split16 when asked for; in the PSPI
+// nearest-lower mode the paired inverse transforms when their shared memory fits; FP32
+static int mig_form(const wem_ctx *c, int wide)
+{
+    const wem_params &p = c->p;
+    if (tcmode(c)) return MIG_FORM_SPLIT16;
+    if (c->paired && p.pspi && p.interp == WEM_INTERP_REF) {
+        int S, th;
+        size_t smem;
+        if (!migrate_config(c->nkx, wide, p.pspi, p.interp, p.nmx, p.nref, &S, &th, &smem, MIG_FORM_PAIRED) &&
+            (int)smem <= c->max_smem)
+            return MIG_FORM_PAIRED;
+    }
+    return MIG_FORM_FP32;
+}
 static std::mutex g_tune_mu;
 static std::vector<TuneEntry> g_tune;
 
@@ -540,6 +565,7 @@ static MigArgs mig_args(wem_ctx *c, int nshot, int ngroups)
     a.tcw = P<uint4>(c->tcw);
     a.err = P<int>(c->tcerr);
     a.refmask = P<unsigned long long>(c->refmask);
+    a.cxmask = P<unsigned long long>(c->refmask) + c->p.nz;
     return a;
 }
 
@@ -551,9 +577,11 @@ static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
     *rate = 0.0;
     int S, threads, bps = 0;
     size_t smem;
-    if (migrate_config(c->nkx, wide, p.pspi, p.nmx, p.nref, &S, &threads, &smem, tcmode(c)) || (int)smem > c->max_smem)
+    const int form = mig_form(c, wide);
+    if (migrate_config(c->nkx, wide, p.pspi, p.interp, p.nmx, p.nref, &S, &threads, &smem, form) ||
+        (int)smem > c->max_smem)
         return WEM_OK;
-    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, p.nmx, p.nref, &bps, tcmode(c)) || bps < 1) {
+    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, p.nmx, p.nref, &bps, form) || bps < 1) {
         cudaGetLastError();
         return WEM_OK;
     }
@@ -568,10 +596,10 @@ static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
     a.nz = std::min(p.nz, 48);
     if ((rc = ensure(c->slots, sizeof(float2) * (size_t)items * a.nz * p.nmx))) return rc;
     a.slots = P<float2>(c->slots);
-    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st, tcmode(c)))
+    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st, form))
         return fail(WEM_ERR_CUDA, "migrate launch (tuning): %s", cudaGetErrorString(cudaGetLastError()));
     CK(cudaEventRecord(c->ev0, c->st));
-    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st, tcmode(c)))
+    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st, form))
         return fail(WEM_ERR_CUDA, "migrate launch (tuning): %s", cudaGetErrorString(cudaGetLastError()));
     CK(cudaEventRecord(c->ev1, c->st));
     CK(cudaEventSynchronize(c->ev1));
@@ -588,7 +616,8 @@ static int choose_shape(wem_ctx *c, int nshot, int *wide)
     const char *e = getenv("WEM_CTA_SHAPE");
     int S, th;
     size_t smem;
-    const bool wide_fits = !migrate_config(c->nkx, 1, p.pspi, p.nmx, p.nref, &S, &th, &smem, tcmode(c)) && (int)smem <= c->max_smem;
+    const bool wide_fits = !migrate_config(c->nkx, 1, p.pspi, p.interp, p.nmx, p.nref, &S, &th, &smem, mig_form(c, 1)) &&
+                           (int)smem <= c->max_smem;
     c->last_tuned = 0;
     if (e && !strcmp(e, "narrow")) return *wide = 0, WEM_OK;
     if (e && !strcmp(e, "wide")) return *wide = wide_fits ? 1 : 0, WEM_OK;
@@ -598,7 +627,7 @@ static int choose_shape(wem_ctx *c, int nshot, int *wide)
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (const TuneEntry &te : g_tune)
             if (te.device == c->device && te.nkx == c->nkx && te.pspi == p.pspi && te.interp == p.interp &&
-                te.nmx == p.nmx && te.nref == p.nref && te.prec == p.precision)
+                te.nmx == p.nmx && te.nref == p.nref && te.prec == p.precision && te.paired == (int)c->paired)
                 return *wide = te.wide, WEM_OK;
     }
     int rc;
@@ -608,7 +637,7 @@ static int choose_shape(wem_ctx *c, int nshot, int *wide)
     *wide = rw >= rn ? 1 : 0;
     c->last_tuned = 1;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune.push_back({ c->device, c->nkx, p.pspi, p.interp, p.nmx, p.nref, p.precision, *wide });
+    g_tune.push_back({ c->device, c->nkx, p.pspi, p.interp, p.nmx, p.nref, p.precision, (int)c->paired, *wide });
     return WEM_OK;
 }
 
@@ -730,7 +759,7 @@ static int enqueue_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_de
     CK(rec(c->evk[1], st, capture));
     if (c->nwf > 0) {
         MigArgs a = mig_args(c, nshot, ngroups);
-        if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, grid, st, tcmode(c)))
+        if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, grid, st, mig_form(c, wide)))
             return fail(WEM_ERR_CUDA, "migrate launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;
     }
@@ -757,12 +786,13 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
     size_t smem;
     int rc;
     if ((rc = choose_shape(c, nshot, &wide))) return rc;
-    if (migrate_config(c->nkx, wide, p.pspi, nmx, p.nref, &S, &threads, &smem, tcmode(c)))
+    const int form = mig_form(c, wide);
+    if (migrate_config(c->nkx, wide, p.pspi, p.interp, nmx, p.nref, &S, &threads, &smem, form))
         return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
     if ((int)smem > c->max_smem)
         return fail(WEM_ERR_SIZE, "nref=%d needs %zu B of shared memory per CTA (device limit %d B)", p.nref, smem,
                     c->max_smem);
-    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, nmx, p.nref, &bps, tcmode(c)) || bps < 1)
+    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, nmx, p.nref, &bps, form) || bps < 1)
         return fail(WEM_ERR_CUDA, "kernel does not fit on the device (smem %zu B, %d threads): %s", smem, threads,
                     cudaGetErrorString(cudaGetLastError()));
     const int ngroups = (nshot + S - 1) / S;

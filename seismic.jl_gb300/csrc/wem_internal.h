@@ -43,6 +43,7 @@ struct MigArgs {
     const uint4 *tcw;      // split16 mode: the W operands of the tensor-core DFT stages (10240 B)
     int *err;              // split16 mode: set when a tensor-core wait ran out
     const unsigned long long *refmask;  // [nz] references in use at each depth (nullptr: all)
+    const unsigned long long *cxmask;   // [nz] references some point takes whole (nullptr: all)
 };
 
 struct SpectraArgs {
@@ -151,11 +152,15 @@ int launch_angles_fft(const AngleArgs &a, const AngleXArgs &x, int which, cudaSt
 int launch_axis_dft(const AxisDftArgs &a, cudaStream_t st);
 int launch_angles_accum(const AngleAccumArgs &a, cudaStream_t st);
 
-// tc = 1: the split16 (tensor-core) form of the depth kernel, built for nkx = 2048 only
-int migrate_config(int nkx, int wide, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem,
-                   int tc = 0);
-int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *blocks_per_sm, int tc = 0);
-int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st, int tc = 0);
+// Forms of the 2-D depth kernel: FP32; split16 (tensor-core DFT stages, nkx = 2048 only);
+// paired (FP32, PSPI nearest-lower mode: two references' real parts per inverse transform).
+constexpr int MIG_FORM_FP32 = 0, MIG_FORM_SPLIT16 = 1, MIG_FORM_PAIRED = 2;
+int migrate_config(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *shots_per_cta, int *threads,
+                   size_t *smem, int form = MIG_FORM_FP32);
+int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *blocks_per_sm,
+                     int form = MIG_FORM_FP32);
+int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st,
+                   int form = MIG_FORM_FP32);
 // the 10240-byte W operand image of the split16 DFT stages
 void tc_w_table_host(uint16_t *out);
 int model_config(int nkx, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem);

@@ -250,27 +250,28 @@ void twiddle_table_host(int nkx, float2 *out)
     default: return -1;                    \
     }
 
-int migrate_config(int nkx, int wide, int pspi, int nmx, int nref, int *S, int *threads, size_t *smem, int tc)
+int migrate_config(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *S, int *threads, size_t *smem,
+                   int form)
 {
-#define CALL(N) mig_launch<N>(wide, pspi, 0, nref, nmx, nullptr, 0, 0, S, threads, smem, nullptr, tc)
+#define CALL(N) mig_launch<N>(wide, pspi, interp, nref, nmx, nullptr, 0, 0, S, threads, smem, nullptr, form)
     WEM_SWITCH_N(nkx, CALL)
 #undef CALL
 }
 
-int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *bps, int tc)
+int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *bps, int form)
 {
     int S, th;
     size_t smem;
-#define CALL(N) mig_launch<N>(wide, pspi, interp, nref, nmx, nullptr, 0, 0, &S, &th, &smem, bps, tc)
+#define CALL(N) mig_launch<N>(wide, pspi, interp, nref, nmx, nullptr, 0, 0, &S, &th, &smem, bps, form)
     WEM_SWITCH_N(nkx, CALL)
 #undef CALL
 }
 
-int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st, int tc)
+int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st, int form)
 {
     int S, th;
     size_t smem;
-#define CALL(N) mig_launch<N>(wide, pspi, interp, a.nref, a.nmx, &a, grid, st, &S, &th, &smem, nullptr, tc)
+#define CALL(N) mig_launch<N>(wide, pspi, interp, a.nref, a.nmx, &a, grid, st, &S, &th, &smem, nullptr, form)
     WEM_SWITCH_N(nkx, CALL)
 #undef CALL
 }

@@ -15,14 +15,17 @@ namespace gbwem {
 // ------------------------------------------------------------------ migration
 // TC (split16 mode, N = 2048): the FFTs' DFT stages run on the tensor cores; each
 // team gets 32 TMEM columns for its accumulators and an mbarrier.
-template <int N, bool PSPI, int INTERP, int S, bool TC = false>
+// PAIR (PSPI nearest-lower mode, FP32): the step of step_mig_paired, with an N-sample
+// spectrum buffer per team in place of the selection accumulator.
+template <int N, bool PSPI, int INTERP, int S, bool TC = false, bool PAIR = false>
 __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const MigArgs a)
 {
+    static_assert(!PAIR || (PSPI && INTERP == 0 && !TC), "paired transforms: PSPI nearest-lower mode, FP32");
     using SH = MigShape<N>;
     constexpr int T = SH::T, PADN = SH::PADN;
     constexpr int NT = 2 * S * T;
     extern __shared__ float4 smem_raw[];
-    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx, 2 * S);
+    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx, 2 * S, PAIR);
 
     const int tid = threadIdx.x;
     const int team = tid / T, t = tid - team * T;
@@ -99,7 +102,12 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
             __syncthreads();
             const uint8_t zf = a.zflag[iz];
             const bool active = is_src ? (zf & Z_SRC) : (zf & Z_REC);
-            if (active) step_mig<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc, ref_mask(a, iz));
+            if (active) {
+                if constexpr (PAIR)
+                    step_mig_paired<N>(v, is_src, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz), cx_mask(a, iz));
+                else
+                    step_mig<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc, ref_mask(a, iz));
+            }
 
             // ---- imaging condition (wem.c:243-247), summed over the group's shots
             if (zf & Z_REC) {
@@ -251,10 +259,10 @@ template <int N> struct Shapes {
     static constexpr int S_MODEL = (T >= 256) ? 1 : (256 / T > 16 ? 16 : 256 / T);
 };
 
-template <int N, bool PSPI, int INTERP, int S, bool TC>
+template <int N, bool PSPI, int INTERP, int S, bool TC, bool PAIR = false>
 int mig_run(const MigArgs *a, int grid, size_t smem, cudaStream_t st, int *bps)
 {
-    auto k = wem_migrate_kernel<N, PSPI, INTERP, S, TC>;
+    auto k = wem_migrate_kernel<N, PSPI, INTERP, S, TC, PAIR>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
     if (bps) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, 2 * S * (N / 16), smem) == cudaSuccess ? 0 : -1;
     k<<<grid, 2 * S * (N / 16), smem, st>>>(*a);
@@ -269,18 +277,27 @@ int mig_sel(int pspi, int interp, const MigArgs *a, int grid, size_t smem, cudaS
     return mig_run<N, true, 1, S, TC>(a, grid, smem, st, bps);
 }
 
-// wide = 1 selects the 512-thread shape; tc = 1 the split16 (tensor-core) form, built
-// for N = 2048 only (-2 otherwise). Fills *S/*threads/*smem; launches when
-// a != nullptr and bps == nullptr, queries occupancy when bps != nullptr.
+// wide = 1 selects the 512-thread shape. form: MIG_FORM_FP32; MIG_FORM_SPLIT16, the
+// tensor-core form, built for N = 2048 only (-2 otherwise); MIG_FORM_PAIRED, the paired
+// inverse transforms of the PSPI nearest-lower mode (-2 for other modes). Fills
+// *S/*threads/*smem; launches when a != nullptr and bps == nullptr, queries occupancy
+// when bps != nullptr.
 template <int N>
 int mig_launch(int wide, int pspi, int interp, int nref, int nmx, const MigArgs *a, int grid, cudaStream_t st,
-               int *S, int *threads, size_t *smem, int *bps, int tc)
+               int *S, int *threads, size_t *smem, int *bps, int form)
 {
     using SH = Shapes<N>;
     const int s_ = wide ? SH::S_WIDE : SH::S_NARROW;
+    const int tc = form == MIG_FORM_SPLIT16;
     *S = s_;
     *threads = 2 * s_ * SH::T;
-    *smem = mig_smem_bytes<N>(pspi != 0, nref, nmx, 2 * s_, tc != 0);
+    *smem = mig_smem_bytes<N>(pspi != 0, nref, nmx, 2 * s_, tc != 0, form == MIG_FORM_PAIRED);
+    if (form == MIG_FORM_PAIRED) {
+        if (!pspi || interp != 0) return -2;
+        if (!a && !bps) return 0;
+        if (wide) return mig_run<N, true, 0, SH::S_WIDE, false, true>(a, grid, *smem, st, bps);
+        return mig_run<N, true, 0, SH::S_NARROW, false, true>(a, grid, *smem, st, bps);
+    }
     if (tc) {
         if constexpr (N == 2048) {
             if (!a && !bps) return 0;

@@ -75,13 +75,15 @@ template <int N> __host__ __device__ constexpr int ph_entries(bool pspi, int nre
 // base address and the abort flag
 __host__ __device__ constexpr int tc_extra_bytes(int teams) { return 10240 + 8 * teams + 16 * teams + 16; }
 
+// paired: the teams' acc rows are N-sample spectrum buffers (step_mig_paired) instead
+// of selection accumulators.
 template <int N, bool PSPI> struct Smem {
     float2 *tw, *ph, *corr, *x, *acc;
     uint8_t *selb;
     float *wl;
     char *tcx;       // split16 mode: the tensor-core region (128-byte aligned)
     int acc_stride;  // float2 per team in acc
-    __device__ Smem(float4 *raw, int nref, int nmx, int teams)
+    __device__ Smem(float4 *raw, int nref, int nmx, int teams, bool paired = false)
     {
         using SH = MigShape<N>;
         tw = reinterpret_cast<float2 *>(raw);
@@ -89,7 +91,7 @@ template <int N, bool PSPI> struct Smem {
         corr = ph + ph_entries<N>(PSPI, nref);
         x = corr + (PSPI ? 0 : ((nmx + 1) & ~1));
         acc = x + (size_t)teams * SH::PADN;
-        acc_stride = PSPI ? sel_entries<N>(nmx) : 0;
+        acc_stride = PSPI ? (paired ? N : sel_entries<N>(nmx)) : 0;
         wl = reinterpret_cast<float *>(acc + (size_t)teams * acc_stride);
         selb = reinterpret_cast<uint8_t *>(wl + (PSPI ? ((nmx + 3) & ~3) : 0));
         const size_t off = (size_t)(selb + (PSPI ? ((nmx + 15) & ~15) : 0) - reinterpret_cast<uint8_t *>(raw));
@@ -99,12 +101,14 @@ template <int N, bool PSPI> struct Smem {
 
 // shared-memory footprint (bytes) of one CTA with `teams` row teams
 template <int N>
-__host__ __device__ constexpr size_t mig_smem_bytes(bool pspi, int nref, int nmx, int teams, bool tc = false)
+__host__ __device__ constexpr size_t mig_smem_bytes(bool pspi, int nref, int nmx, int teams, bool tc = false,
+                                                    bool paired = false)
 {
     using SH = MigShape<N>;
     const size_t base =
         sizeof(float2) * ((size_t)SH::TWP + (size_t)ph_entries<N>(pspi, nref) + (size_t)(pspi ? 0 : ((nmx + 1) & ~1)) +
-                          (size_t)teams * SH::PADN + (pspi ? (size_t)teams * sel_entries<N>(nmx) : 0)) +
+                          (size_t)teams * SH::PADN +
+                          (pspi ? (size_t)teams * (paired ? (size_t)N : (size_t)sel_entries<N>(nmx)) : 0)) +
         (pspi ? sizeof(float) * (size_t)((nmx + 3) & ~3) + (size_t)((nmx + 15) & ~15) : 0);
     return tc ? ((base + 127) & ~(size_t)127) + (size_t)tc_extra_bytes(teams) : base;
 }
@@ -113,6 +117,13 @@ __host__ __device__ constexpr size_t mig_smem_bytes(bool pspi, int nref, int nmx
 __device__ __forceinline__ unsigned long long ref_mask(const MigArgs &a, int iz)
 {
     return a.refmask ? a.refmask[iz] : ~0ull;
+}
+
+// references some grid point of depth iz takes whole (complex) in the nearest-lower mode
+// (vref2 - vref1 <= 10 there, wem.c:457-458); the others give real parts only
+__device__ __forceinline__ unsigned long long cx_mask(const MigArgs &a, int iz)
+{
+    return a.cxmask ? a.cxmask[iz] : ~0ull;
 }
 
 // Tables of depth step iz at angular frequency w (all threads of the CTA):
@@ -296,6 +307,114 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
             const int x = t + T * m;
             if constexpr (TC) acc[m] = cscale(acc[m], inv_s);
             v[m] = x < a.nmx ? (conj ? cmulc(acc[m], sm.corr[x]) : cmul(acc[m], sm.corr[x])) : make_float2(0.f, 0.f);
+        }
+    }
+}
+
+// The PSPI migration step of the nearest-lower mode (INTERP = 0, FP32) with the real
+// parts of two reference wavefields taken from one inverse transform.
+// Where vref2 - vref1 > 10 a grid point keeps Re(dref[iref1]) only (wem.c:454-455 through
+// linear_interp's float return, wem.c:473-478), so a reference r whose every taker is such
+// a point needs only Re(IFFT(a Q_r)) = IFFT(X_r), X_r[k] = (a[k] Q_r[k] + conj(a[-k] Q_r[-k]))/2
+// (a the row's spectrum, Q_r the phase, which depends on |k| only). X_r is Hermitian, so
+// IFFT(X_r1 + i X_r2) = Re(dref[r1]) + i Re(dref[r2]): with p = a[k], q = conj(a[-k]),
+//     z[k] = (p (Q1 + i Q2) + q (conj Q1 + i conj Q2)) / 2.
+// References taken whole somewhere (cx) and an odd one left over get a transform of their
+// own, as in step_mig. The spectrum is kept in the team's buffer spec (N samples) so that
+// every thread can read a[-k]; the selected row builds up in v.
+template <int N>
+__device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, true> &sm,
+                                                float2 *xbuf, float2 *spec, int t, unsigned sync,
+                                                unsigned long long used, unsigned long long cx)
+{
+    constexpr int T = N / 16, HALF = MigShape<N>::HALF;
+    fft_row<N, -1>(v, xbuf, sm.tw, t, sync);  // v: the spectrum at k = t + T*m
+#pragma unroll
+    for (int m = 0; m < 16; m++) spec[t + T * m] = v[m];
+    uint32_t selp[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) selp[q] = 0;
+#pragma unroll
+    for (int m = 0; m < 16; m++) {
+        const int x = t + T * m;
+        selp[m >> 2] |= (x < a.nmx ? (uint32_t)sm.selb[x] : 0x7fu) << (8 * (m & 3));
+    }
+    uint32_t i1p[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) i1p[q] = selp[q] & 0x7f7f7f7fu;
+#pragma unroll
+    for (int m = 0; m < 16; m++) v[m] = make_float2(0.f, 0.f);  // positions >= nmx stay 0
+    team_sync<T>(sync);  // the whole spectrum is in spec
+    used &= a.nref >= 64 ? ~0ull : ((1ull << a.nref) - 1ull);
+    unsigned long long ro = used & ~cx, whole = used & cx;  // CTA-uniform
+    while (ro | whole) {
+        int r1, r2 = -1;
+        if (ro) {
+            r1 = __ffsll((long long)ro) - 1;
+            ro &= ro - 1ull;
+            if (ro) {
+                r2 = __ffsll((long long)ro) - 1;
+                ro &= ro - 1ull;
+            }
+        } else {
+            r1 = __ffsll((long long)whole) - 1;
+            whole &= whole - 1ull;
+        }
+        const float2 *ph1 = sm.ph + (size_t)r1 * HALF;
+        float2 u[16];
+        if (r2 < 0) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const float2 P = ph1[kfold<N>(t, m)];
+                const float2 p = spec[t + T * m];
+                u[m] = conj ? cmulc(p, P) : cmul(p, P);
+            }
+        } else {
+            const float2 *ph2 = sm.ph + (size_t)r2 * HALF;
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int kf = kfold<N>(t, m);
+                float2 Q1 = ph1[kf], Q2 = ph2[kf];
+                if (conj) {
+                    Q1.y = -Q1.y;
+                    Q2.y = -Q2.y;
+                }
+                const float2 p = spec[t + T * m];
+                const float2 qm = spec[(N - t - T * m) & (N - 1)];
+                const float2 q = make_float2(qm.x, -qm.y);
+                const float2 M = make_float2(Q1.x - Q2.y, Q1.y + Q2.x);   // Q1 + i Q2
+                const float2 Pc = make_float2(Q1.x + Q2.y, Q2.x - Q1.y);  // conj Q1 + i conj Q2
+                const float2 z = cadd(cmul(p, M), cmul(q, Pc));
+                u[m] = make_float2(0.5f * z.x, 0.5f * z.y);
+            }
+        }
+        fft_row<N, +1>(u, xbuf, sm.tw, t, sync);
+        const uint32_t rr1 = (uint32_t)r1 * 0x01010101u;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const uint32_t eq = __vcmpeq4(i1p[q], rr1);
+            if (eq == 0u) continue;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int m = 4 * q + j;
+                if ((eq >> (8 * j)) & 1u) {
+                    const bool re = r2 >= 0 || ((selp[q] >> (8 * j + 7)) & 1u) != 0;
+                    v[m] = re ? make_float2(u[m].x, 0.f) : u[m];
+                }
+            }
+        }
+        if (r2 >= 0) {
+            const uint32_t rr2 = (uint32_t)r2 * 0x01010101u;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint32_t eq = __vcmpeq4(i1p[q], rr2);
+                if (eq == 0u) continue;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int m = 4 * q + j;
+                    if ((eq >> (8 * j)) & 1u) v[m] = make_float2(u[m].y, 0.f);
+                }
+            }
         }
     }
 }

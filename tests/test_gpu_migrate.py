@@ -130,6 +130,32 @@ def test_autotuned_cta_shape(gpu_lib, oracle_mod, monkeypatch):
     assert len(threads) == 2 and l1["threads"] in threads
 
 
+@pytest.mark.parametrize("nref", [3, 8])
+def test_paired_inverse_transforms(gpu_lib, oracle_mod, monkeypatch, nref):
+    """The nearest-lower PSPI mode takes the real parts of two reference wavefields from
+    one inverse transform wherever every point that takes them keeps the real part only
+    (wem.c:454-455, 473-478). Depth levels of three kinds: random velocities (real parts;
+    the reference of the row maximum taken whole), a velocity range of 40 m/s (reference
+    spacing <= 10 m/s: every reference taken whole, wem.c:457-458) and constant velocity
+    (vmax <= vmin + 10: reference 0 taken whole, wem.c:55-67). Against the port and
+    against one transform per reference (WEM_PAIRED=0)."""
+    from wemgpu import synth
+    c = synth.small_case(47, nx=256, nz=18, nt=96, nshot=3, pspi=1, nref=nref, interp="ref")
+    rng = np.random.default_rng(48)
+    vel = c["vel"].copy()
+    vel[:, 6:9] = 2500.0
+    vel[:, 9:12] = 2500.0 + 40.0 * rng.random((vel.shape[0], 3))
+    want = _port_stack(oracle_mod, c["params"], vel, c["wav"], c["shots"])
+    images = []
+    for paired in ("1", "0"):
+        monkeypatch.setenv("WEM_PAIRED", paired)
+        with gpu_lib.Context() as ctx:
+            ctx.prepare(c["params"], vel, c["wav"])
+            images.append(ctx.migrate(c["shots"]))
+        assert rel_l2(images[-1], want) < TOL, (paired, rel_l2(images[-1], want))
+    assert rel_l2(images[0], images[1]) < 1e-5
+
+
 def test_config0_full_size_matches_reference_port(gpu_lib, oracle_mod):
     """The split-step workload at full size (1 shot, 200 x 256, 221 frequencies)."""
     from wemgpu import synth
