@@ -131,6 +131,9 @@ def inverse_transforms_per_step(p: dict, vel: np.ndarray, paired: bool) -> float
         if not paired:
             total += len(used)
             continue
+        if 1 <= np.count_nonzero(~interp) <= 4:  # whole points by direct sums, every reference paired
+            total += (len(used) + 1) // 2
+            continue
         whole = set(i1[~interp].tolist())
         ro = len(used - whole)
         total += len(whole) + ro // 2 + ro % 2

@@ -86,6 +86,8 @@ struct wem_ctx {
     DevBuf ssyn_ref, ssyn_exact;  // synthesis weights w^2 * (half-spectrum | image) factor
     DevBuf tapery, twy;           // 3-D: y taper and y-FFT twiddles
     DevBuf tcw, tcerr;            // split16: W operands of the tensor-core DFT stages, timeout word
+    DevBuf wposb;                 // [nz][1 + WHOLE_MAX] points taking their wavefield whole (paired form)
+    int wdot_off = 0;             // offset of the direct-sum table in twid
     DevBuf refmask;               // [2][nz] bit r: some grid point takes its wavefield from reference r
                                   // (all of it, in the second row)
     DevBuf m3_items, m3_U, m3_Y, m3_C, m3_parts;
@@ -160,7 +162,7 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
                        &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
                        &c->ssyn_ref, &c->ssyn_exact, &c->recv, &c->slots, &c->image, &c->data,
                        &c->tbase, &c->igx, &c->smig, &c->mimg, &c->tapery, &c->twy, &c->m3_items,
-                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask };
+                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -300,6 +302,11 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     std::vector<float> po(nz), pd((size_t)nz * n), vref((size_t)nz * nref), wl((size_t)nz * n, 0.f);
     std::vector<float> slow2((size_t)nz * nref);
     std::vector<uint8_t> sel((size_t)nz * n);
+    // points taking their wavefield whole, listed where a depth has at most WHOLE_MAX (their
+    // references then pair like the others, and the imaginary parts come from direct sums)
+    std::vector<int> wpos((size_t)nz * (1 + WHOLE_MAX), 0);
+    const char *ds_env = getenv("WEM_DIRECT_SUMS");  // 0: no direct sums
+    const bool direct_sums = !(ds_env && !strcmp(ds_env, "0"));
     // reference velocities some grid point of the depth takes its wavefield from: the
     // others' inverse transforms are skipped (their results would not be used); then
     // (from nz on) those some point takes whole in the nearest-lower mode, where the
@@ -339,9 +346,23 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
             sel[(size_t)iz * n + ix] = word;
             used[iz] |= 1ull << i1;
             if ((word & SEL_INTERP) && p.interp == WEM_INTERP_LINEAR) used[iz] |= 1ull << (i1 + 1);
-            if (!(word & SEL_INTERP)) used[(size_t)nz + iz] |= 1ull << i1;
+            if (!(word & SEL_INTERP)) {
+                used[(size_t)nz + iz] |= 1ull << i1;
+                int &cnt = wpos[(size_t)iz * (1 + WHOLE_MAX)];
+                if (cnt <= WHOLE_MAX) {
+                    if (cnt < WHOLE_MAX) wpos[(size_t)iz * (1 + WHOLE_MAX) + 1 + cnt] = ix;
+                    cnt++;
+                }
+            }
         }
-        if (!p.pspi) used[iz] = used[(size_t)nz + iz] = 1ull;
+        int &cnt = wpos[(size_t)iz * (1 + WHOLE_MAX)];
+        if (cnt > WHOLE_MAX || p.nmy > 1 || p.interp != WEM_INTERP_REF || !direct_sums)
+            cnt = 0;  // the whole references keep transforms of their own
+        else used[(size_t)nz + iz] = 0ull;
+        if (!p.pspi) {
+            used[iz] = used[(size_t)nz + iz] = 1ull;
+            cnt = 0;
+        }
     }
     // taper of the split-step operator (wem.c:546-564): tmx(imx) * tmy(imy)
     std::vector<float> taper = taper_of(nmx), tapery = taper_of(p.nmy);
@@ -353,6 +374,13 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     const int ntw = twiddle_table_size(nkx);
     std::vector<float2> tw(ntw > 0 ? ntw : 1);
     twiddle_table_host(nkx, tw.data());
+    // then e^{+2 pi i e / nkx}, e = 0 .. nkx/2 (FP64-built): the direct sums of the paired form
+    c->wdot_off = (int)tw.size();
+    tw.resize(tw.size() + nkx / 2 + 1);
+    for (int e = 0; e <= nkx / 2; e++) {
+        const double ang = 6.283185307179586476925 * (double)e / (double)nkx;
+        tw[(size_t)c->wdot_off + e] = make_float2((float)cos(ang), (float)sin(ang));
+    }
     const int ntwy = p.nmy > 1 ? twiddle_table_size(nky) : 1;
     std::vector<float2> twy(ntwy > 0 ? ntwy : 1);
     if (p.nmy > 1) twiddle_table_host(nky, twy.data());
@@ -394,7 +422,8 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         (rc = ensure(c->ssyn_exact, sizeof(float) * syn_exact.size())) ||
         (rc = ensure(c->tapery, sizeof(float) * tapery.size())) || (rc = ensure(c->twy, sizeof(float2) * twy.size())) ||
         (rc = ensure(c->tcw, 10240)) || (rc = ensure(c->tcerr, sizeof(int))) ||
-        (rc = ensure(c->refmask, sizeof(unsigned long long) * 2 * nz)))
+        (rc = ensure(c->refmask, sizeof(unsigned long long) * 2 * nz)) ||
+        (rc = ensure(c->wposb, sizeof(int) * wpos.size())))
         return rc;
     cudaStream_t st = c->st;
     std::vector<uint16_t> tcw(5120);
@@ -402,6 +431,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     CK(cudaMemcpyAsync(c->tcw.p, tcw.data(), 10240, cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(c->tcerr.p, 0, sizeof(int), st));
     CK(cudaMemcpyAsync(c->refmask.p, used.data(), sizeof(unsigned long long) * 2 * nz, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->wposb.p, wpos.data(), sizeof(int) * wpos.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->po.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->pd.p, pd.data(), sizeof(float) * pd.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->vref.p, vref.data(), sizeof(float) * vref.size(), cudaMemcpyHostToDevice, st));
@@ -566,6 +596,8 @@ static MigArgs mig_args(wem_ctx *c, int nshot, int ngroups)
     a.err = P<int>(c->tcerr);
     a.refmask = P<unsigned long long>(c->refmask);
     a.cxmask = P<unsigned long long>(c->refmask) + c->p.nz;
+    a.wpos = P<int>(c->wposb);
+    a.wdot = P<float2>(c->twid) + c->wdot_off;
     return a;
 }
 

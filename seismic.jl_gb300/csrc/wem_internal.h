@@ -44,7 +44,13 @@ struct MigArgs {
     int *err;              // split16 mode: set when a tensor-core wait ran out
     const unsigned long long *refmask;  // [nz] references in use at each depth (nullptr: all)
     const unsigned long long *cxmask;   // [nz] references some point takes whole (nullptr: all)
+    // paired form: per depth the count (0 .. WHOLE_MAX) and positions of the points that take
+    // their wavefield whole when they are that few ([nz][1 + WHOLE_MAX]; nullptr: none)
+    const int *wpos;
+    const float2 *wdot;    // paired form: e^{+2 pi i e / nkx}, e = 0 .. nkx/2
 };
+// points per depth whose imaginary part the paired form takes from a direct sum
+constexpr int WHOLE_MAX = 4;
 
 struct SpectraArgs {
     const float *d;        // [ntr][nt]

@@ -36,6 +36,8 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
     const unsigned sync = team_sync_handle<N>(tid);
 
     for (int i = tid; i < SH::TW; i += NT) sm.tw[i] = a.twid[i];
+    if constexpr (PAIR)
+        for (int i = tid; i <= N / 2; i += NT) sm.wd[i] = a.wdot[i];
 
     TcTeam tc{};
     constexpr uint32_t TCOLS = 2 * S * 32 < 32 ? 32 : 2 * S * 32;  // power of two for 2S in {1, 2, 4}
@@ -99,6 +101,8 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
         for (int iz = 0; iz < a.nz; iz++) {
             if (!tables_free) __syncthreads();
             build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
+            if constexpr (PAIR)
+                if (tid <= WHOLE_MAX) sm.wpos[tid] = a.wpos ? a.wpos[(size_t)iz * (1 + WHOLE_MAX) + tid] : 0;
             __syncthreads();
             const uint8_t zf = a.zflag[iz];
             const bool active = is_src ? (zf & Z_SRC) : (zf & Z_REC);

@@ -75,12 +75,17 @@ template <int N> __host__ __device__ constexpr int ph_entries(bool pspi, int nre
 // base address and the abort flag
 __host__ __device__ constexpr int tc_extra_bytes(int teams) { return 10240 + 8 * teams + 16 * teams + 16; }
 
-// paired: the teams' acc rows are N-sample spectrum buffers (step_mig_paired) instead
-// of selection accumulators.
+// paired: the teams' acc rows are N-sample spectrum buffers (step_mig_paired) instead of
+// selection accumulators, and the direct-sum table (N/2 + 1 entries) and the depth's list
+// of points taken whole follow the selection bytes.
+template <int N> __host__ __device__ constexpr int wdot_entries() { return (N / 2 + 2) & ~1; }
+
 template <int N, bool PSPI> struct Smem {
     float2 *tw, *ph, *corr, *x, *acc;
     uint8_t *selb;
     float *wl;
+    float2 *wd;      // paired form: e^{+2 pi i e / N}, e = 0 .. N/2
+    int *wpos;       // paired form: count and positions of the points taken whole
     char *tcx;       // split16 mode: the tensor-core region (128-byte aligned)
     int acc_stride;  // float2 per team in acc
     __device__ Smem(float4 *raw, int nref, int nmx, int teams, bool paired = false)
@@ -95,6 +100,8 @@ template <int N, bool PSPI> struct Smem {
         wl = reinterpret_cast<float *>(acc + (size_t)teams * acc_stride);
         selb = reinterpret_cast<uint8_t *>(wl + (PSPI ? ((nmx + 3) & ~3) : 0));
         const size_t off = (size_t)(selb + (PSPI ? ((nmx + 15) & ~15) : 0) - reinterpret_cast<uint8_t *>(raw));
+        wd = reinterpret_cast<float2 *>(reinterpret_cast<char *>(raw) + off);
+        wpos = reinterpret_cast<int *>(wd + wdot_entries<N>());
         tcx = reinterpret_cast<char *>(raw) + ((off + 127) & ~(size_t)127);
     }
 };
@@ -110,6 +117,7 @@ __host__ __device__ constexpr size_t mig_smem_bytes(bool pspi, int nref, int nmx
                           (size_t)teams * SH::PADN +
                           (pspi ? (size_t)teams * (paired ? (size_t)N : (size_t)sel_entries<N>(nmx)) : 0)) +
         (pspi ? sizeof(float) * (size_t)((nmx + 3) & ~3) + (size_t)((nmx + 15) & ~15) : 0);
+    if (paired) return base + sizeof(float2) * (size_t)wdot_entries<N>() + sizeof(int) * 8;
     return tc ? ((base + 127) & ~(size_t)127) + (size_t)tc_extra_bytes(teams) : base;
 }
 
@@ -311,6 +319,14 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
     }
 }
 
+// e^{+2 pi i e / N}, e in [0, N), from the table of e in [0, N/2]
+template <int N> __device__ __forceinline__ float2 wpow(const float2 *wd, int e)
+{
+    if (e <= N / 2) return wd[e];
+    const float2 w = wd[N - e];
+    return make_float2(w.x, -w.y);
+}
+
 // The PSPI migration step of the nearest-lower mode (INTERP = 0, FP32) with the real
 // parts of two reference wavefields taken from one inverse transform.
 // Where vref2 - vref1 > 10 a grid point keeps Re(dref[iref1]) only (wem.c:454-455 through
@@ -322,6 +338,8 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
 // References taken whole somewhere (cx) and an odd one left over get a transform of their
 // own, as in step_mig. The spectrum is kept in the team's buffer spec (N samples) so that
 // every thread can read a[-k]; the selected row builds up in v.
+// At a depth with at most WHOLE_MAX points taken whole (wpos) every reference is paired,
+// and the imaginary parts at those points are direct sums.
 template <int N>
 __device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, true> &sm,
                                                 float2 *xbuf, float2 *spec, int t, unsigned sync,
@@ -416,6 +434,48 @@ __device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, cons
                 }
             }
         }
+    }
+    // Points taken whole at a depth that has at most WHOLE_MAX of them: their references were
+    // paired like the others (real parts), and the imaginary part is the direct sum
+    // Im dref_r[x] = Im sum_k a[k] Q_r[k] e^{+2 pi i k x / N} over the team, in a fixed order.
+    const int nj = sm.wpos[0];  // CTA-uniform
+    if (nj > 0) {
+        constexpr int NW = T >= 32 ? T / 32 : 1;  // partial sums per team
+        const unsigned lanes = T >= 32 ? 0xffffffffu : sync;
+        float *scr = reinterpret_cast<float *>(xbuf);  // free after the last inverse transform
+        for (int j = 0; j < nj; j++) {
+            const int xj = sm.wpos[1 + j];
+            const float2 *ph = sm.ph + (size_t)(sm.selb[xj] & 0x7f) * HALF;
+            // sum_m b_m W^(e0 + m c) = W^e0 (...((b_15 z + b_14) z + ...) z + b_0), z = W^c:
+            // e0 = t xj, c = T xj (mod N); W^e = e^{+2 pi i e / N} from the half table
+            const float2 z = wpow<N>(sm.wd, (T * xj) & (N - 1));
+            float2 h = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int m = 15; m >= 0; m--) {
+                const int kf = kfold<N>(t, m);
+                const float2 P = ph[kf];
+                const float2 b = conj ? cmulc(spec[t + T * m], P) : cmul(spec[t + T * m], P);
+                h = cadd(cmul(h, z), b);
+            }
+            const float2 w0 = wpow<N>(sm.wd, (t * xj) & (N - 1));
+            float acc = h.x * w0.y + h.y * w0.x;  // Im(h W^e0)
+#pragma unroll
+            for (int off = (T >= 32 ? 16 : T / 2); off > 0; off >>= 1) acc += __shfl_xor_sync(lanes, acc, off);
+            if ((t & 31) == 0) scr[j * NW + (t >> 5)] = acc;
+        }
+        team_sync<T>(sync);
+        for (int j = 0; j < nj; j++) {
+            const int xj = sm.wpos[1 + j];
+            if (xj % T == t) {
+                float im = 0.f;
+                for (int w = 0; w < NW; w++) im += scr[j * NW + w];
+                const int mj = xj / T;
+#pragma unroll
+                for (int m = 0; m < 16; m++)
+                    if (m == mj) v[m].y = im;
+            }
+        }
+        team_sync<T>(sync);  // the sums are read before the exchange buffer is reused
     }
 }
 

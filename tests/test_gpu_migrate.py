@@ -137,14 +137,18 @@ def test_paired_inverse_transforms(gpu_lib, oracle_mod, monkeypatch, nref):
     (wem.c:454-455, 473-478). Depth levels of three kinds: random velocities (real parts;
     the reference of the row maximum taken whole), a velocity range of 40 m/s (reference
     spacing <= 10 m/s: every reference taken whole, wem.c:457-458) and constant velocity
-    (vmax <= vmin + 10: reference 0 taken whole, wem.c:55-67). Against the port and
-    against one transform per reference (WEM_PAIRED=0)."""
+    (vmax <= vmin + 10: reference 0 taken whole, wem.c:55-67); random levels whose maximum
+    is taken by 3 points (their imaginary parts by direct sums) and by 5 points (the
+    reference keeps a transform of its own). Against the port and against one transform
+    per reference (WEM_PAIRED=0)."""
     from wemgpu import synth
     c = synth.small_case(47, nx=256, nz=18, nt=96, nshot=3, pspi=1, nref=nref, interp="ref")
     rng = np.random.default_rng(48)
     vel = c["vel"].copy()
     vel[:, 6:9] = 2500.0
     vel[:, 9:12] = 2500.0 + 40.0 * rng.random((vel.shape[0], 3))
+    for iz, pts in ((12, [3, 100, 200]), (13, [7, 8, 9, 150, 250])):
+        vel[pts, iz] = vel[:, iz].max()
     want = _port_stack(oracle_mod, c["params"], vel, c["wav"], c["shots"])
     images = []
     for paired in ("1", "0"):
