@@ -86,7 +86,11 @@ struct wem_ctx {
     DevBuf ssyn_ref, ssyn_exact;  // synthesis weights w^2 * (half-spectrum | image) factor
     DevBuf tapery, twy;           // 3-D: y taper and y-FFT twiddles
     DevBuf tcw, tcerr;            // split16: W operands of the tensor-core DFT stages, timeout word
-    DevBuf wposb;                 // [nz][1 + WHOLE_MAX] points taking their wavefield whole (paired form)
+    DevBuf wposb;                 // [nz][WPOS_STRIDE] points taking their wavefield whole (paired form)
+    DevBuf selbp;                 // [nz][nmx rounded up to 16] selection rows (paired form)
+    DevBuf ptab;                  // [nwf][nz][nref][nkx/2 + 2] phase tables (paired form)
+    bool use_ptab = true;         // WEM_PHASE_TABLES=0: every CTA builds its own tables
+    bool ptab_ok = false;         // the current migration uses ptab
     int wdot_off = 0;             // offset of the direct-sum table in twid
     DevBuf refmask;               // [2][nz] bit r: some grid point takes its wavefield from reference r
                                   // (all of it, in the second row)
@@ -162,7 +166,7 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
                        &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
                        &c->ssyn_ref, &c->ssyn_exact, &c->recv, &c->slots, &c->image, &c->data,
                        &c->tbase, &c->igx, &c->smig, &c->mimg, &c->tapery, &c->twy, &c->m3_items,
-                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb };
+                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb, &c->selbp, &c->ptab };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -304,7 +308,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     std::vector<uint8_t> sel((size_t)nz * n);
     // points taking their wavefield whole, listed where a depth has at most WHOLE_MAX (their
     // references then pair like the others, and the imaginary parts come from direct sums)
-    std::vector<int> wpos((size_t)nz * (1 + WHOLE_MAX), 0);
+    std::vector<int> wpos((size_t)nz * WPOS_STRIDE, 0);
     const char *ds_env = getenv("WEM_DIRECT_SUMS");  // 0: no direct sums
     const bool direct_sums = !(ds_env && !strcmp(ds_env, "0"));
     // reference velocities some grid point of the depth takes its wavefield from: the
@@ -348,14 +352,14 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
             if ((word & SEL_INTERP) && p.interp == WEM_INTERP_LINEAR) used[iz] |= 1ull << (i1 + 1);
             if (!(word & SEL_INTERP)) {
                 used[(size_t)nz + iz] |= 1ull << i1;
-                int &cnt = wpos[(size_t)iz * (1 + WHOLE_MAX)];
+                int &cnt = wpos[(size_t)iz * WPOS_STRIDE];
                 if (cnt <= WHOLE_MAX) {
-                    if (cnt < WHOLE_MAX) wpos[(size_t)iz * (1 + WHOLE_MAX) + 1 + cnt] = ix;
+                    if (cnt < WHOLE_MAX) wpos[(size_t)iz * WPOS_STRIDE + 1 + cnt] = ix;
                     cnt++;
                 }
             }
         }
-        int &cnt = wpos[(size_t)iz * (1 + WHOLE_MAX)];
+        int &cnt = wpos[(size_t)iz * WPOS_STRIDE];
         if (cnt > WHOLE_MAX || p.nmy > 1 || p.interp != WEM_INTERP_REF || !direct_sums)
             cnt = 0;  // the whole references keep transforms of their own
         else used[(size_t)nz + iz] = 0ull;
@@ -423,7 +427,8 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         (rc = ensure(c->tapery, sizeof(float) * tapery.size())) || (rc = ensure(c->twy, sizeof(float2) * twy.size())) ||
         (rc = ensure(c->tcw, 10240)) || (rc = ensure(c->tcerr, sizeof(int))) ||
         (rc = ensure(c->refmask, sizeof(unsigned long long) * 2 * nz)) ||
-        (rc = ensure(c->wposb, sizeof(int) * wpos.size())))
+        (rc = ensure(c->wposb, sizeof(int) * wpos.size())) ||
+        (rc = ensure(c->selbp, (size_t)nz * ((nmx + 15) / 16 * 16))))
         return rc;
     cudaStream_t st = c->st;
     std::vector<uint16_t> tcw(5120);
@@ -437,6 +442,13 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     CK(cudaMemcpyAsync(c->vref.p, vref.data(), sizeof(float) * vref.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->slow2.p, slow2.data(), sizeof(float) * slow2.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->sel.p, sel.data(), sel.size(), cudaMemcpyHostToDevice, st));
+    if (p.nmy == 1) {  // the selection rows padded to 16 bytes (the paired form's asynchronous copies)
+        const size_t nsp = (size_t)(nmx + 15) / 16 * 16;
+        std::vector<uint8_t> selp(nz * nsp, 0x7f);
+        for (int iz = 0; iz < nz; iz++) memcpy(&selp[iz * nsp], &sel[(size_t)iz * nmx], nmx);
+        CK(cudaMemcpyAsync(c->selbp.p, selp.data(), selp.size(), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));  // selp is a local
+    }
     CK(cudaMemcpyAsync(c->wlin.p, wl.data(), sizeof(float) * wl.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->taper.p, taper.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->tapery.p, tapery.data(), sizeof(float) * tapery.size(), cudaMemcpyHostToDevice, st));
@@ -486,6 +498,8 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     {
         const char *e = getenv("WEM_PAIRED");
         c->paired = !(e && !strcmp(e, "0"));
+        const char *pt = getenv("WEM_PHASE_TABLES");
+        c->use_ptab = !(pt && !strcmp(pt, "0"));
     }
     c->last_nshot = -1;
     return WEM_OK;
@@ -598,6 +612,8 @@ static MigArgs mig_args(wem_ctx *c, int nshot, int ngroups)
     a.cxmask = P<unsigned long long>(c->refmask) + c->p.nz;
     a.wpos = P<int>(c->wposb);
     a.wdot = P<float2>(c->twid) + c->wdot_off;
+    a.selbp = P<uint8_t>(c->selbp);
+    a.ptab = nullptr;
     return a;
 }
 
@@ -791,6 +807,12 @@ static int enqueue_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_de
     CK(rec(c->evk[1], st, capture));
     if (c->nwf > 0) {
         MigArgs a = mig_args(c, nshot, ngroups);
+        if (c->ptab_ok) {
+            a.ptab = P<float2>(c->ptab);
+            if (launch_phase_tables(c->nkx, a, P<float2>(c->ptab), st))
+                return fail(WEM_ERR_CUDA, "phase-table launch: %s", cudaGetErrorString(cudaGetLastError()));
+            kernels++;
+        }
         if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, grid, st, mig_form(c, wide)))
             return fail(WEM_ERR_CUDA, "migrate launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;
@@ -835,6 +857,19 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
     if ((rc = ensure(c->recv, sizeof(float2) * recv_elems)) ||
         (rc = ensure(c->slots, sizeof(float2) * (size_t)grid * nz * nmx)))
         return rc;
+    // the paired form reads the phase tables of every (frequency, depth) from one array that a
+    // kernel fills first, when it fits (at most 32 GiB and half the free device memory)
+    c->ptab_ok = false;
+    if (c->use_ptab && c->nwf > 0 && form == MIG_FORM_PAIRED) {
+        const size_t bytes = sizeof(float2) * (size_t)c->nwf * nz * p.nref * (size_t)(c->nkx / 2 + 2);
+        size_t fr = 0, tot = 0;
+        if (c->ptab.n >= bytes) {
+            c->ptab_ok = true;
+        } else if (bytes <= (32ull << 30) && cudaMemGetInfo(&fr, &tot) == cudaSuccess && bytes <= fr / 2) {
+            c->ptab_ok = ensure(c->ptab, bytes) == WEM_OK;
+        }
+        cudaGetLastError();
+    }
     c->last_threads = threads;
     c->last_S = S;
     c->last_grid = grid;

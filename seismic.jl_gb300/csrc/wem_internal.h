@@ -45,12 +45,17 @@ struct MigArgs {
     const unsigned long long *refmask;  // [nz] references in use at each depth (nullptr: all)
     const unsigned long long *cxmask;   // [nz] references some point takes whole (nullptr: all)
     // paired form: per depth the count (0 .. WHOLE_MAX) and positions of the points that take
-    // their wavefield whole when they are that few ([nz][1 + WHOLE_MAX]; nullptr: none)
+    // their wavefield whole when they are that few ([nz][WPOS_STRIDE]; nullptr: none)
     const int *wpos;
     const float2 *wdot;    // paired form: e^{+2 pi i e / nkx}, e = 0 .. nkx/2
+    // paired form: the phase tables of every (frequency, depth), [nwf][nz][nref][nkx/2 + 2]
+    // (nullptr: each CTA builds its own), and the selection rows padded to 16 bytes
+    const float2 *ptab;
+    const uint8_t *selbp;  // [nz][(nmx + 15) / 16 * 16]
 };
 // points per depth whose imaginary part the paired form takes from a direct sum
 constexpr int WHOLE_MAX = 4;
+constexpr int WPOS_STRIDE = 8;  // ints per depth in wpos (count, positions, padding to 32 bytes)
 
 struct SpectraArgs {
     const float *d;        // [ntr][nt]
@@ -167,6 +172,8 @@ int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref,
                      int form = MIG_FORM_FP32);
 int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st,
                    int form = MIG_FORM_FP32);
+// the precomputed phase tables of the paired form (a.ptab layout) into out
+int launch_phase_tables(int nkx, const MigArgs &a, float2 *out, cudaStream_t st);
 // the 10240-byte W operand image of the split16 DFT stages
 void tc_w_table_host(uint16_t *out);
 int model_config(int nkx, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem);

@@ -250,6 +250,32 @@ void twiddle_table_host(int nkx, float2 *out)
     default: return -1;                    \
     }
 
+// The phase tables of the paired form for every (frequency, depth): one CTA per (depth,
+// frequency), entries as build_tables makes them (phase_entry, the same FP32 operations),
+// references some point of the depth takes only. out: [nwf][nz][nref][phs].
+__global__ void __launch_bounds__(256) wem_phase_tables_kernel(const MigArgs a, int half, int phs, float2 *out)
+{
+    const int iz = blockIdx.x, iwi = blockIdx.y;
+    const float w = __fmul_rn((float)(a.ifmin + iwi), a.dw);
+    const float w2 = __fmul_rn(w, w);
+    const unsigned long long used = ref_mask(a, iz);
+    const float *sl = a.slow2 + (size_t)iz * a.nref;
+    for (int r = 0; r < a.nref; r++) {
+        if (!((used >> r) & 1ull)) continue;
+        const float slow2 = sl[r];
+        float2 *o = out + (((size_t)iwi * a.nz + iz) * a.nref + r) * phs;
+        for (int kk = threadIdx.x; kk < half; kk += blockDim.x)
+            o[kk] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
+    }
+}
+
+int launch_phase_tables(int nkx, const MigArgs &a, float2 *out, cudaStream_t st)
+{
+    if (a.nz < 1 || a.nwf < 1) return 0;
+    wem_phase_tables_kernel<<<dim3(a.nz, a.nwf), 256, 0, st>>>(a, nkx / 2 + 1, nkx / 2 + 2, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 int migrate_config(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *S, int *threads, size_t *smem,
                    int form)
 {

@@ -99,18 +99,32 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
         }
 
         for (int iz = 0; iz < a.nz; iz++) {
-            if (!tables_free) __syncthreads();
-            build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
-            if constexpr (PAIR)
-                if (tid <= WHOLE_MAX) sm.wpos[tid] = a.wpos ? a.wpos[(size_t)iz * (1 + WHOLE_MAX) + tid] : 0;
-            __syncthreads();
             const uint8_t zf = a.zflag[iz];
             const bool active = is_src ? (zf & Z_SRC) : (zf & Z_REC);
-            if (active) {
+            if (PAIR && a.ptab) {
+                // precomputed tables: copied while the rows go through their forward
+                // transforms (the barrier first: the previous depth's tables and exchange
+                // buffers are no longer read)
+                __syncthreads();
+                if constexpr (PAIR) {
+                    copy_tables_async<N>(a, sm, iwi, iz, tid, NT);
+                    if (active) paired_forward<N>(v, xbuf, sacc, sm.tw, t, sync);
+                    cp_async_wait_all();
+                    __syncthreads();
+                    if (active) paired_inverse<N>(v, is_src, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz), cx_mask(a, iz));
+                }
+            } else {
+                if (!tables_free) __syncthreads();
+                build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
                 if constexpr (PAIR)
-                    step_mig_paired<N>(v, is_src, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz), cx_mask(a, iz));
-                else
-                    step_mig<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc, ref_mask(a, iz));
+                    if (tid < WPOS_STRIDE) sm.wpos[tid] = a.wpos ? a.wpos[(size_t)iz * WPOS_STRIDE + tid] : 0;
+                __syncthreads();
+                if (active) {
+                    if constexpr (PAIR)
+                        step_mig_paired<N>(v, is_src, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz), cx_mask(a, iz));
+                    else
+                        step_mig<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc, ref_mask(a, iz));
+                }
             }
 
             // ---- imaging condition (wem.c:243-247), summed over the group's shots

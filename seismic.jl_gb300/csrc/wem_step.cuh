@@ -48,6 +48,7 @@ __device__ __forceinline__ void kahan_add(float2 *slot, float v)
 template <int N> struct MigShape {
     static constexpr int T = N / 16;           // threads per row team
     static constexpr int HALF = N / 2 + 1;     // phase-table entries per reference
+    static constexpr int PHS = N / 2 + 2;      // phase-table stride: a multiple of 16 bytes
     static constexpr int PADN = pad16(N);      // exchange buffer length (float2)
     static constexpr int TW = fft_tw_size<N>();
     static constexpr int TWP = (TW + 1) & ~1;  // keep 16-byte alignment of what follows
@@ -67,7 +68,7 @@ template <int N> __host__ __device__ constexpr int sel_entries(int nmx)
 // float2 entries of the phase tables, kept even so that what follows stays 16-byte aligned
 template <int N> __host__ __device__ constexpr int ph_entries(bool pspi, int nref)
 {
-    return ((pspi ? nref : 1) * MigShape<N>::HALF + 1) & ~1;
+    return (pspi ? nref : 1) * MigShape<N>::PHS;
 }
 
 // bytes after the selection rows that the tensor-core stages use (split16 mode):
@@ -149,7 +150,7 @@ __device__ __forceinline__ void build_tables(const MigArgs &a, const Smem<N, PSP
         for (int r = 0; r < a.nref; r++) {
             if (!((used >> r) & 1ull)) continue;  // no grid point takes this reference
             const float slow2 = sl[r];
-            float2 *ph = sm.ph + (size_t)r * HALF;
+            float2 *ph = sm.ph + (size_t)r * MigShape<N>::PHS;
             for (int kk = tid; kk < HALF; kk += nthreads)
                 ph[kk] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
         }
@@ -228,7 +229,7 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
                                          float2 *xbuf, float2 *sacc, int t, unsigned sync, TcTeam *tc = nullptr,
                                          unsigned long long used = ~0ull)
 {
-    constexpr int T = N / 16, HALF = MigShape<N>::HALF;
+    constexpr int T = N / 16;
     float inv_s = 1.f;
     if constexpr (TC) {
         float s;
@@ -252,7 +253,7 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
         for (int q = 0; q < 4; q++) i1p[q] = selp[q] & 0x7f7f7f7fu;
         for (int r = 0; r < a.nref; r++) {
             if (!((used >> r) & 1ull)) continue;  // CTA-uniform
-            const float2 *ph = sm.ph + (size_t)r * HALF;
+            const float2 *ph = sm.ph + (size_t)r * MigShape<N>::PHS;
             float2 u[16];
 #pragma unroll
             for (int m = 0; m < 16; m++) {
@@ -340,15 +341,24 @@ template <int N> __device__ __forceinline__ float2 wpow(const float2 *wd, int e)
 // every thread can read a[-k]; the selected row builds up in v.
 // At a depth with at most WHOLE_MAX points taken whole (wpos) every reference is paired,
 // and the imaginary parts at those points are direct sums.
+// First part: the forward transform, its spectrum to spec. The second part
+// (paired_inverse) follows a barrier that makes spec and the depth's tables visible.
 template <int N>
-__device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, true> &sm,
-                                                float2 *xbuf, float2 *spec, int t, unsigned sync,
-                                                unsigned long long used, unsigned long long cx)
+__device__ __forceinline__ void paired_forward(float2 (&v)[16], float2 *xbuf, float2 *spec, const float2 *tw, int t,
+                                               unsigned sync)
 {
-    constexpr int T = N / 16, HALF = MigShape<N>::HALF;
-    fft_row<N, -1>(v, xbuf, sm.tw, t, sync);  // v: the spectrum at k = t + T*m
+    constexpr int T = N / 16;
+    fft_row<N, -1>(v, xbuf, tw, t, sync);  // v: the spectrum at k = t + T*m
 #pragma unroll
     for (int m = 0; m < 16; m++) spec[t + T * m] = v[m];
+}
+
+template <int N>
+__device__ __forceinline__ void paired_inverse(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, true> &sm,
+                                               float2 *xbuf, const float2 *spec, int t, unsigned sync,
+                                               unsigned long long used, unsigned long long cx)
+{
+    constexpr int T = N / 16;
     uint32_t selp[4];
 #pragma unroll
     for (int q = 0; q < 4; q++) selp[q] = 0;
@@ -362,7 +372,6 @@ __device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, cons
     for (int q = 0; q < 4; q++) i1p[q] = selp[q] & 0x7f7f7f7fu;
 #pragma unroll
     for (int m = 0; m < 16; m++) v[m] = make_float2(0.f, 0.f);  // positions >= nmx stay 0
-    team_sync<T>(sync);  // the whole spectrum is in spec
     used &= a.nref >= 64 ? ~0ull : ((1ull << a.nref) - 1ull);
     unsigned long long ro = used & ~cx, whole = used & cx;  // CTA-uniform
     while (ro | whole) {
@@ -378,7 +387,7 @@ __device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, cons
             r1 = __ffsll((long long)whole) - 1;
             whole &= whole - 1ull;
         }
-        const float2 *ph1 = sm.ph + (size_t)r1 * HALF;
+        const float2 *ph1 = sm.ph + (size_t)r1 * MigShape<N>::PHS;
         float2 u[16];
         if (r2 < 0) {
 #pragma unroll
@@ -388,7 +397,7 @@ __device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, cons
                 u[m] = conj ? cmulc(p, P) : cmul(p, P);
             }
         } else {
-            const float2 *ph2 = sm.ph + (size_t)r2 * HALF;
+            const float2 *ph2 = sm.ph + (size_t)r2 * MigShape<N>::PHS;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const int kf = kfold<N>(t, m);
@@ -445,7 +454,7 @@ __device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, cons
         float *scr = reinterpret_cast<float *>(xbuf);  // free after the last inverse transform
         for (int j = 0; j < nj; j++) {
             const int xj = sm.wpos[1 + j];
-            const float2 *ph = sm.ph + (size_t)(sm.selb[xj] & 0x7f) * HALF;
+            const float2 *ph = sm.ph + (size_t)(sm.selb[xj] & 0x7f) * MigShape<N>::PHS;
             // sum_m b_m W^(e0 + m c) = W^e0 (...((b_15 z + b_14) z + ...) z + b_0), z = W^c:
             // e0 = t xj, c = T xj (mod N); W^e = e^{+2 pi i e / N} from the half table
             const float2 z = wpow<N>(sm.wd, (T * xj) & (N - 1));
@@ -479,6 +488,48 @@ __device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, cons
     }
 }
 
+template <int N>
+__device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, true> &sm,
+                                                float2 *xbuf, float2 *spec, int t, unsigned sync,
+                                                unsigned long long used, unsigned long long cx)
+{
+    paired_forward<N>(v, xbuf, spec, sm.tw, t, sync);
+    team_sync<N / 16>(sync);  // the whole spectrum is in spec
+    paired_inverse<N>(v, conj, a, sm, xbuf, spec, t, sync, used, cx);
+}
+
+// The depth's tables of the paired form from the precomputed phase tables (a.ptab
+// [nwf][nz][nref][PHS]), the padded selection row and the list of points taken whole,
+// copied by every thread of the CTA with 16-byte asynchronous copies (cp.async); the
+// caller waits (cp_async_wait_all) and synchronises the CTA before reading them.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N, true> &sm, int iwi, int iz, int tid,
+                                                  int nthreads)
+{
+    constexpr int PHS = MigShape<N>::PHS, CH = PHS / 2;  // 16-byte chunks per table
+    const float4 *src = reinterpret_cast<const float4 *>(a.ptab + ((size_t)iwi * a.nz + iz) * a.nref * PHS);
+    float4 *dst = reinterpret_cast<float4 *>(sm.ph);
+    unsigned long long used = ref_mask(a, iz) & (a.nref >= 64 ? ~0ull : ((1ull << a.nref) - 1ull));
+    while (used) {
+        const int r = __ffsll((long long)used) - 1;
+        used &= used - 1ull;
+        for (int c = tid; c < CH; c += nthreads) cp_async16(dst + (size_t)r * CH + c, src + (size_t)r * CH + c);
+    }
+    const int nsel = (a.nmx + 15) / 16;
+    const float4 *ss = reinterpret_cast<const float4 *>(a.selbp + (size_t)iz * nsel * 16);
+    for (int c = tid; c < nsel; c += nthreads) cp_async16(reinterpret_cast<float4 *>(sm.selb) + c, ss + c);
+    if (tid < 2) cp_async16(reinterpret_cast<float4 *>(sm.wpos) + tid, reinterpret_cast<const float4 *>(a.wpos + (size_t)iz * WPOS_STRIDE) + tid);
+    cp_async_commit();
+}
+
 // One upward step of the modelling recursion (wem.c:273-274, -dz, adj=false), in
 // place, active teams only.
 // EXACT=false: the reference's operator -- PSPI as the migration step with -dz
@@ -492,7 +543,7 @@ template <int N, bool PSPI, int INTERP, bool EXACT>
 __device__ __forceinline__ void step_model(float2 (&v)[16], const MigArgs &a, const Smem<N, PSPI> &sm, float2 *xbuf,
                                            float2 *sacc, int t, unsigned sync, unsigned long long used = ~0ull)
 {
-    constexpr int T = N / 16, HALF = MigShape<N>::HALF;
+    constexpr int T = N / 16;
     if (PSPI && !EXACT) {
         step_mig<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync, nullptr, used);
         return;
@@ -523,7 +574,7 @@ __device__ __forceinline__ void step_model(float2 (&v)[16], const MigArgs &a, co
                 u[m] = make_float2(v[m].x * wgt, re_only ? 0.f : v[m].y * wgt);
             }
             fft_row<N, -1>(u, xbuf, sm.tw, t, sync);
-            const float2 *ph = sm.ph + (size_t)r * HALF;
+            const float2 *ph = sm.ph + (size_t)r * MigShape<N>::PHS;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const float2 q = cmulc(u[m], ph[kfold<N>(t, m)]);

@@ -140,7 +140,9 @@ def test_paired_inverse_transforms(gpu_lib, oracle_mod, monkeypatch, nref):
     (vmax <= vmin + 10: reference 0 taken whole, wem.c:55-67); random levels whose maximum
     is taken by 3 points (their imaginary parts by direct sums) and by 5 points (the
     reference keeps a transform of its own). Against the port and against one transform
-    per reference (WEM_PAIRED=0)."""
+    per reference (WEM_PAIRED=0); the phase tables precomputed for every (frequency,
+    depth) give the image bit for bit that tables built in each CTA give
+    (WEM_PHASE_TABLES=0)."""
     from wemgpu import synth
     c = synth.small_case(47, nx=256, nz=18, nt=96, nshot=3, pspi=1, nref=nref, interp="ref")
     rng = np.random.default_rng(48)
@@ -158,6 +160,11 @@ def test_paired_inverse_transforms(gpu_lib, oracle_mod, monkeypatch, nref):
             images.append(ctx.migrate(c["shots"]))
         assert rel_l2(images[-1], want) < TOL, (paired, rel_l2(images[-1], want))
     assert rel_l2(images[0], images[1]) < 1e-5
+    monkeypatch.setenv("WEM_PAIRED", "1")
+    monkeypatch.setenv("WEM_PHASE_TABLES", "0")
+    with gpu_lib.Context() as ctx:
+        ctx.prepare(c["params"], vel, c["wav"])
+        assert np.array_equal(ctx.migrate(c["shots"]), images[0])
 
 
 def test_config0_full_size_matches_reference_port(gpu_lib, oracle_mod):
