@@ -87,7 +87,8 @@ struct wem_ctx {
     DevBuf tapery, twy;           // 3-D: y taper and y-FFT twiddles
     DevBuf tcw, tcerr;            // split16: W operands of the tensor-core DFT stages, timeout word
     DevBuf wposb;                 // [nz][WPOS_STRIDE] points taking their wavefield whole (paired form)
-    DevBuf selbp;                 // [nz][nmx rounded up to 16] selection rows (paired form)
+    DevBuf selbp;                 // [nz][nmx rounded up to 16] selection rows (precomputed-table path)
+    DevBuf wlinp;                 // [nz][nmx rounded up to 4] linear weights (precomputed-table path)
     DevBuf ptab;                  // [nwf][nz][nref][nkx/2 + 2] phase tables (paired form)
     bool use_ptab = true;         // WEM_PHASE_TABLES=0: every CTA builds its own tables
     bool ptab_ok = false;         // the current migration uses ptab
@@ -166,7 +167,7 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
                        &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
                        &c->ssyn_ref, &c->ssyn_exact, &c->recv, &c->slots, &c->image, &c->data,
                        &c->tbase, &c->igx, &c->smig, &c->mimg, &c->tapery, &c->twy, &c->m3_items,
-                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb, &c->selbp, &c->ptab };
+                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb, &c->selbp, &c->wlinp, &c->ptab };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -428,7 +429,8 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         (rc = ensure(c->tcw, 10240)) || (rc = ensure(c->tcerr, sizeof(int))) ||
         (rc = ensure(c->refmask, sizeof(unsigned long long) * 2 * nz)) ||
         (rc = ensure(c->wposb, sizeof(int) * wpos.size())) ||
-        (rc = ensure(c->selbp, (size_t)nz * ((nmx + 15) / 16 * 16))))
+        (rc = ensure(c->selbp, (size_t)nz * ((nmx + 15) / 16 * 16))) ||
+        (rc = ensure(c->wlinp, sizeof(float) * (size_t)nz * ((nmx + 3) / 4 * 4))))
         return rc;
     cudaStream_t st = c->st;
     std::vector<uint16_t> tcw(5120);
@@ -442,12 +444,17 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     CK(cudaMemcpyAsync(c->vref.p, vref.data(), sizeof(float) * vref.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->slow2.p, slow2.data(), sizeof(float) * slow2.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->sel.p, sel.data(), sel.size(), cudaMemcpyHostToDevice, st));
-    if (p.nmy == 1) {  // the selection rows padded to 16 bytes (the paired form's asynchronous copies)
-        const size_t nsp = (size_t)(nmx + 15) / 16 * 16;
+    if (p.nmy == 1) {  // selection rows and weights padded to 16 bytes (asynchronous table copies)
+        const size_t nsp = (size_t)(nmx + 15) / 16 * 16, nwp = (size_t)(nmx + 3) / 4 * 4;
         std::vector<uint8_t> selp(nz * nsp, 0x7f);
-        for (int iz = 0; iz < nz; iz++) memcpy(&selp[iz * nsp], &sel[(size_t)iz * nmx], nmx);
+        std::vector<float> wlp(nz * nwp, 0.f);
+        for (int iz = 0; iz < nz; iz++) {
+            memcpy(&selp[iz * nsp], &sel[(size_t)iz * nmx], nmx);
+            memcpy(&wlp[iz * nwp], &wl[(size_t)iz * nmx], sizeof(float) * nmx);
+        }
         CK(cudaMemcpyAsync(c->selbp.p, selp.data(), selp.size(), cudaMemcpyHostToDevice, st));
-        CK(cudaStreamSynchronize(st));  // selp is a local
+        CK(cudaMemcpyAsync(c->wlinp.p, wlp.data(), sizeof(float) * wlp.size(), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st));  // selp and wlp are locals
     }
     CK(cudaMemcpyAsync(c->wlin.p, wl.data(), sizeof(float) * wl.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->taper.p, taper.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
@@ -613,6 +620,7 @@ static MigArgs mig_args(wem_ctx *c, int nshot, int ngroups)
     a.wpos = P<int>(c->wposb);
     a.wdot = P<float2>(c->twid) + c->wdot_off;
     a.selbp = P<uint8_t>(c->selbp);
+    a.wlinp = P<float>(c->wlinp);
     a.ptab = nullptr;
     return a;
 }
@@ -767,6 +775,23 @@ static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev,
     return WEM_OK;
 }
 
+// The FP32 PSPI kernels read the phase tables of every (frequency, depth) from one array
+// that wem_phase_tables_kernel fills first, when it fits (at most 32 GiB and half the free
+// device memory); otherwise each CTA builds its own. True when c->ptab holds them.
+static bool alloc_phase_tables(wem_ctx *c)
+{
+    const wem_params &p = c->p;
+    if (!c->use_ptab || c->nwf < 1 || !p.pspi || p.nmy > 1) return false;
+    const size_t bytes = sizeof(float2) * (size_t)c->nwf * p.nz * p.nref * (size_t)(c->nkx / 2 + 2);
+    if (c->ptab.n >= bytes) return true;
+    size_t fr = 0, tot = 0;
+    bool ok = false;
+    if (bytes <= (32ull << 30) && cudaMemGetInfo(&fr, &tot) == cudaSuccess && bytes <= fr / 2)
+        ok = ensure(c->ptab, bytes) == WEM_OK;
+    cudaGetLastError();
+    return ok;
+}
+
 // record an event on c->st; inside a stream capture as a graph node (so that the
 // per-kernel times stay readable after every replay)
 static cudaError_t rec(cudaEvent_t ev, cudaStream_t st, bool capture)
@@ -857,19 +882,7 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
     if ((rc = ensure(c->recv, sizeof(float2) * recv_elems)) ||
         (rc = ensure(c->slots, sizeof(float2) * (size_t)grid * nz * nmx)))
         return rc;
-    // the paired form reads the phase tables of every (frequency, depth) from one array that a
-    // kernel fills first, when it fits (at most 32 GiB and half the free device memory)
-    c->ptab_ok = false;
-    if (c->use_ptab && c->nwf > 0 && form == MIG_FORM_PAIRED) {
-        const size_t bytes = sizeof(float2) * (size_t)c->nwf * nz * p.nref * (size_t)(c->nkx / 2 + 2);
-        size_t fr = 0, tot = 0;
-        if (c->ptab.n >= bytes) {
-            c->ptab_ok = true;
-        } else if (bytes <= (32ull << 30) && cudaMemGetInfo(&fr, &tot) == cudaSuccess && bytes <= fr / 2) {
-            c->ptab_ok = ensure(c->ptab, bytes) == WEM_OK;
-        }
-        cudaGetLastError();
-    }
+    c->ptab_ok = form != MIG_FORM_SPLIT16 && alloc_phase_tables(c);
     c->last_threads = threads;
     c->last_S = S;
     c->last_grid = grid;
@@ -1498,6 +1511,14 @@ static int run_model(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, flo
         a.po = P<float>(c->po); a.pd = P<float>(c->pd); a.selb = P<uint8_t>(c->sel); a.wlin = P<float>(c->wlin);
         a.taper = P<float>(c->taper); a.zflag = P<uint8_t>(c->zflag); a.twid = P<float2>(c->twid); a.slots = nullptr;
         a.refmask = P<unsigned long long>(c->refmask);
+        a.selbp = P<uint8_t>(c->selbp);
+        a.wlinp = P<float>(c->wlinp);
+        if (alloc_phase_tables(c)) {
+            a.ptab = P<float2>(c->ptab);
+            if (launch_phase_tables(c->nkx, a, P<float2>(c->ptab), st))
+                return fail(WEM_ERR_CUDA, "phase-table launch: %s", cudaGetErrorString(cudaGetLastError()));
+            kernels++;
+        }
         BornArgs b{};
         b.img = P<float>(c->mimg);
         b.smig = P<float2>(c->smig);

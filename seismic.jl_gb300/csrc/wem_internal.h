@@ -52,6 +52,7 @@ struct MigArgs {
     // (nullptr: each CTA builds its own), and the selection rows padded to 16 bytes
     const float2 *ptab;
     const uint8_t *selbp;  // [nz][(nmx + 15) / 16 * 16]
+    const float *wlinp;    // [nz][(nmx + 3) / 4 * 4] linear weights, rows padded to 16 bytes
 };
 // points per depth whose imaginary part the paired form takes from a direct sum
 constexpr int WHOLE_MAX = 4;

@@ -101,17 +101,31 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
         for (int iz = 0; iz < a.nz; iz++) {
             const uint8_t zf = a.zflag[iz];
             const bool active = is_src ? (zf & Z_SRC) : (zf & Z_REC);
-            if (PAIR && a.ptab) {
+            if (zf & Z_REC) {
+                // the CTA's image row of this depth to L2 now; it is read and rewritten at the
+                // end of the step
+                const float2 *srow = slot + (size_t)iz * nmx;
+                for (int x = tid * 16; x < nmx; x += NT * 16) asm volatile("prefetch.global.L2 [%0];" ::"l"(srow + x));
+            }
+            if (PSPI && !TC && a.ptab) {
                 // precomputed tables: copied while the rows go through their forward
                 // transforms (the barrier first: the previous depth's tables and exchange
                 // buffers are no longer read)
                 __syncthreads();
-                if constexpr (PAIR) {
-                    copy_tables_async<N>(a, sm, iwi, iz, tid, NT);
-                    if (active) paired_forward<N>(v, xbuf, sacc, sm.tw, t, sync);
+                if constexpr (PSPI && !TC) {
+                    copy_tables_async<N, INTERP, PAIR>(a, sm, iwi, iz, tid, NT);
+                    if (active) {
+                        if constexpr (PAIR) paired_forward<N>(v, xbuf, sacc, sm.tw, t, sync);
+                        else fft_row<N, -1>(v, xbuf, sm.tw, t, sync);
+                    }
                     cp_async_wait_all();
                     __syncthreads();
-                    if (active) paired_inverse<N>(v, is_src, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz), cx_mask(a, iz));
+                    if (active) {
+                        if constexpr (PAIR)
+                            paired_inverse<N>(v, is_src, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz), cx_mask(a, iz));
+                        else
+                            step_mig_tail<N, PSPI, INTERP>(v, is_src, a, sm, xbuf, sacc, t, sync, nullptr, ref_mask(a, iz), 1.f);
+                    }
                 }
             } else {
                 if (!tables_free) __syncthreads();
@@ -220,11 +234,22 @@ __global__ void __launch_bounds__(S * (N / 16), N <= 1024 ? 2 : 1) wem_model_ker
         }
         // source, downward (wem.c:255-265)
         for (int iz = 0; iz < nz; iz++) {
-            __syncthreads();
-            build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
-            __syncthreads();
             const bool act = (a.zflag[iz] & Z_SRC) != 0;
-            if (act) step_mig<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync, nullptr, ref_mask(a, iz));
+            __syncthreads();
+            if (PSPI && a.ptab) {
+                // precomputed tables, copied behind the forward transform
+                if constexpr (PSPI) {
+                    copy_tables_async<N, INTERP, false>(a, sm, iwi, iz, tid, NT);
+                    if (act) fft_row<N, -1>(v, xbuf, sm.tw, t, sync);
+                    cp_async_wait_all();
+                    __syncthreads();
+                    if (act) step_mig_tail<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync, nullptr, ref_mask(a, iz), 1.f);
+                }
+            } else {
+                build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
+                __syncthreads();
+                if (act) step_mig<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync, nullptr, ref_mask(a, iz));
+            }
             float2 *row = smig + (size_t)iz * nmx;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
@@ -237,7 +262,14 @@ __global__ void __launch_bounds__(S * (N / 16), N <= 1024 ? 2 : 1) wem_model_ker
         for (int m = 0; m < 16; m++) v[m] = make_float2(0.f, 0.f);
         for (int iz = nz - 1; iz >= 0; iz--) {
             __syncthreads();
-            build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
+            if (PSPI && a.ptab) {
+                if constexpr (PSPI) {
+                    copy_tables_async<N, INTERP, false>(a, sm, iwi, iz, tid, NT);
+                    cp_async_wait_all();
+                }
+            } else {
+                build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
+            }
             __syncthreads();
             if (a.zflag[iz] & Z_REC) {
                 const float2 *row = smig + (size_t)iz * nmx;

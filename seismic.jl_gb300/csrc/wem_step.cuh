@@ -224,20 +224,14 @@ __device__ __forceinline__ float sel_weight(const uint32_t (&selp)[4], const flo
 // TC (split16 mode): the FFTs run their DFT stages on the tensor cores; the row is
 // scaled by a power of two into the operands' range first and back at the end.
 // used: the references in use at this depth (ref_mask); the others are skipped.
+// step_mig_tail is everything after the forward transform (v holds the spectrum at
+// k = t + T*m; inv_s undoes the split16 row scaling), step_mig the whole step.
 template <int N, bool PSPI, int INTERP, bool TC = false>
-__device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, PSPI> &sm,
-                                         float2 *xbuf, float2 *sacc, int t, unsigned sync, TcTeam *tc = nullptr,
-                                         unsigned long long used = ~0ull)
+__device__ __forceinline__ void step_mig_tail(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, PSPI> &sm,
+                                              float2 *xbuf, float2 *sacc, int t, unsigned sync, TcTeam *tc,
+                                              unsigned long long used, float inv_s)
 {
     constexpr int T = N / 16;
-    float inv_s = 1.f;
-    if constexpr (TC) {
-        float s;
-        row_scale<T>(v, tc->red, t, sync, s, inv_s);
-#pragma unroll
-        for (int m = 0; m < 16; m++) v[m] = cscale(v[m], s);
-    }
-    fft_row<N, -1, TC>(v, xbuf, sm.tw, t, sync, tc);  // v now holds the spectrum at k = t + T*m
     if (PSPI) {
         // sacc: this team's selection accumulator; thread t owns entries m*T + t
         uint32_t selp[4];
@@ -318,6 +312,23 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
             v[m] = x < a.nmx ? (conj ? cmulc(acc[m], sm.corr[x]) : cmul(acc[m], sm.corr[x])) : make_float2(0.f, 0.f);
         }
     }
+}
+
+template <int N, bool PSPI, int INTERP, bool TC = false>
+__device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, PSPI> &sm,
+                                         float2 *xbuf, float2 *sacc, int t, unsigned sync, TcTeam *tc = nullptr,
+                                         unsigned long long used = ~0ull)
+{
+    constexpr int T = N / 16;
+    float inv_s = 1.f;
+    if constexpr (TC) {
+        float s;
+        row_scale<T>(v, tc->red, t, sync, s, inv_s);
+#pragma unroll
+        for (int m = 0; m < 16; m++) v[m] = cscale(v[m], s);
+    }
+    fft_row<N, -1, TC>(v, xbuf, sm.tw, t, sync, tc);  // v now holds the spectrum at k = t + T*m
+    step_mig_tail<N, PSPI, INTERP, TC>(v, conj, a, sm, xbuf, sacc, t, sync, tc, used, inv_s);
 }
 
 // e^{+2 pi i e / N}, e in [0, N), from the table of e in [0, N/2]
@@ -498,10 +509,11 @@ __device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, cons
     paired_inverse<N>(v, conj, a, sm, xbuf, spec, t, sync, used, cx);
 }
 
-// The depth's tables of the paired form from the precomputed phase tables (a.ptab
-// [nwf][nz][nref][PHS]), the padded selection row and the list of points taken whole,
-// copied by every thread of the CTA with 16-byte asynchronous copies (cp.async); the
-// caller waits (cp_async_wait_all) and synchronises the CTA before reading them.
+// The depth's PSPI tables from the precomputed phase tables (a.ptab [nwf][nz][nref][PHS]):
+// the phase tables of the references in use, the padded selection row, the linear weights
+// (INTERP = 1) and the list of points taken whole (PAIR), copied by every thread of the
+// CTA with 16-byte asynchronous copies (cp.async); the caller waits (cp_async_wait_all) and
+// synchronises the CTA before reading them.
 __device__ __forceinline__ void cp_async16(void *dst, const void *src)
 {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
@@ -510,7 +522,7 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-template <int N>
+template <int N, int INTERP, bool PAIR>
 __device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N, true> &sm, int iwi, int iz, int tid,
                                                   int nthreads)
 {
@@ -526,7 +538,13 @@ __device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N
     const int nsel = (a.nmx + 15) / 16;
     const float4 *ss = reinterpret_cast<const float4 *>(a.selbp + (size_t)iz * nsel * 16);
     for (int c = tid; c < nsel; c += nthreads) cp_async16(reinterpret_cast<float4 *>(sm.selb) + c, ss + c);
-    if (tid < 2) cp_async16(reinterpret_cast<float4 *>(sm.wpos) + tid, reinterpret_cast<const float4 *>(a.wpos + (size_t)iz * WPOS_STRIDE) + tid);
+    if (INTERP == 1) {
+        const int nwl = (a.nmx + 3) / 4;
+        const float4 *ws = reinterpret_cast<const float4 *>(a.wlinp + (size_t)iz * nwl * 4);
+        for (int c = tid; c < nwl; c += nthreads) cp_async16(reinterpret_cast<float4 *>(sm.wl) + c, ws + c);
+    }
+    if (PAIR && tid < 2)
+        cp_async16(reinterpret_cast<float4 *>(sm.wpos) + tid, reinterpret_cast<const float4 *>(a.wpos + (size_t)iz * WPOS_STRIDE) + tid);
     cp_async_commit();
 }
 
