@@ -249,12 +249,12 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
-def recorded_traffic():
-    """Per-launch DRAM bytes of the depth-recursion kernel from the committed ncu summary."""
+def recorded_traffic(workload: str):
+    """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the depth
+    kernel for a workload, from the committed ncu summary (profiles/dram_traffic.json)."""
     try:
-        with open(os.path.join(ROOT, "profiles", "migrate_kernel_traffic.json")) as f:
-            t = json.load(f)
-        return t
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            return json.load(f).get(workload)
     except Exception:
         return None
 
@@ -530,10 +530,8 @@ def main():
     props = torch.cuda.get_device_properties(dev)
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     fp32_nominal = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
-    tr = recorded_traffic()
-    traffic = None
-    if tr and tr.get("workload") == args.workload:
-        traffic = tr.get("bytes_per_launch")
+    tr = recorded_traffic(args.workload)
+    traffic = tr.get("bytes_per_launch") if tr else None
 
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "traffic": traffic, "peak_source": f"bf16 dense, {src}",
