@@ -76,7 +76,7 @@ template <int N> __host__ __device__ constexpr int ph_entries(bool pspi, int nre
 // base address and the abort flag
 __host__ __device__ constexpr int tc_extra_bytes(int teams) { return 10240 + 8 * teams + 16 * teams + 16; }
 
-// paired: the teams' acc rows are N-sample spectrum buffers (step_mig_paired) instead of
+// paired: the teams' acc rows are N + 2-sample spectrum buffers (step_mig_paired) instead of
 // selection accumulators, and the direct-sum table (N/2 + 1 entries) and the depth's list
 // of points taken whole follow the selection bytes.
 template <int N> __host__ __device__ constexpr int wdot_entries() { return (N / 2 + 2) & ~1; }
@@ -97,7 +97,7 @@ template <int N, bool PSPI> struct Smem {
         corr = ph + ph_entries<N>(PSPI, nref);
         x = corr + (PSPI ? 0 : ((nmx + 1) & ~1));
         acc = x + (size_t)teams * SH::PADN;
-        acc_stride = PSPI ? (paired ? N : sel_entries<N>(nmx)) : 0;
+        acc_stride = PSPI ? (paired ? N + 2 : sel_entries<N>(nmx)) : 0;
         wl = reinterpret_cast<float *>(acc + (size_t)teams * acc_stride);
         selb = reinterpret_cast<uint8_t *>(wl + (PSPI ? ((nmx + 3) & ~3) : 0));
         const size_t off = (size_t)(selb + (PSPI ? ((nmx + 15) & ~15) : 0) - reinterpret_cast<uint8_t *>(raw));
@@ -116,7 +116,7 @@ __host__ __device__ constexpr size_t mig_smem_bytes(bool pspi, int nref, int nmx
     const size_t base =
         sizeof(float2) * ((size_t)SH::TWP + (size_t)ph_entries<N>(pspi, nref) + (size_t)(pspi ? 0 : ((nmx + 1) & ~1)) +
                           (size_t)teams * SH::PADN +
-                          (pspi ? (size_t)teams * (paired ? (size_t)N : (size_t)sel_entries<N>(nmx)) : 0)) +
+                          (pspi ? (size_t)teams * (paired ? (size_t)N + 2 : (size_t)sel_entries<N>(nmx)) : 0)) +
         (pspi ? sizeof(float) * (size_t)((nmx + 3) & ~3) + (size_t)((nmx + 15) & ~15) : 0);
     if (paired) return base + sizeof(float2) * (size_t)wdot_entries<N>() + sizeof(int) * 8;
     return tc ? ((base + 127) & ~(size_t)127) + (size_t)tc_extra_bytes(teams) : base;
@@ -348,20 +348,32 @@ template <int N> __device__ __forceinline__ float2 wpow(const float2 *wd, int e)
 // IFFT(X_r1 + i X_r2) = Re(dref[r1]) + i Re(dref[r2]): with p = a[k], q = conj(a[-k]),
 //     z[k] = (p (Q1 + i Q2) + q (conj Q1 + i conj Q2)) / 2.
 // References taken whole somewhere (cx) and an odd one left over get a transform of their
-// own, as in step_mig. The spectrum is kept in the team's buffer spec (N samples) so that
+// own, as in step_mig. The spectrum is kept in the team's buffer spec (N + 1 samples) so that
 // every thread can read a[-k]; the selected row builds up in v.
 // At a depth with at most WHOLE_MAX points taken whole (wpos) every reference is paired,
 // and the imaginary parts at those points are direct sums.
 // First part: the forward transform, its spectrum to spec. The second part
 // (paired_inverse) follows a barrier that makes spec and the depth's tables visible.
+// spec holds a'[k], k = 0 .. N (a'[N] = a'[0], so that a'[-k] = a'[N - k] needs no wrap), with
+// a' = a for the receiver and a'[k] = conj(a[-k]) for the source row (conj): with P
+// symmetric in k, IFFT(a conj(P)) = conj(IFFT(a' P)), so the source's phase conj(P) becomes
+// P and the transforms of both rows run the same arithmetic.
 template <int N>
-__device__ __forceinline__ void paired_forward(float2 (&v)[16], float2 *xbuf, float2 *spec, const float2 *tw, int t,
-                                               unsigned sync)
+__device__ __forceinline__ void paired_forward(float2 (&v)[16], bool conj, float2 *xbuf, float2 *spec,
+                                               const float2 *tw, int t, unsigned sync)
 {
     constexpr int T = N / 16;
     fft_row<N, -1>(v, xbuf, tw, t, sync);  // v: the spectrum at k = t + T*m
+    if (!conj) {
 #pragma unroll
-    for (int m = 0; m < 16; m++) spec[t + T * m] = v[m];
+        for (int m = 0; m < 16; m++) spec[t + T * m] = v[m];
+        if (t == 0) spec[N] = v[0];
+    } else {
+        float2 *sm_ = spec + N - t;  // a'[N - k] = conj(a[k]), k = t + T*m
+#pragma unroll
+        for (int m = 0; m < 16; m++) sm_[-T * m] = make_float2(v[m].x, -v[m].y);
+        if (t == 0) spec[0] = make_float2(v[0].x, -v[0].y);
+    }
 }
 
 template <int N>
@@ -402,28 +414,22 @@ __device__ __forceinline__ void paired_inverse(float2 (&v)[16], bool conj, const
         float2 u[16];
         if (r2 < 0) {
 #pragma unroll
-            for (int m = 0; m < 16; m++) {
-                const float2 P = ph1[kfold<N>(t, m)];
-                const float2 p = spec[t + T * m];
-                u[m] = conj ? cmulc(p, P) : cmul(p, P);
-            }
+            for (int m = 0; m < 16; m++) u[m] = cmul(spec[t + T * m], ph1[kfold<N>(t, m)]);
         } else {
+            // 2 z = p (Q1 + i Q2) + q (conj Q1 + i conj Q2); the factor 1/2 is applied to the
+            // selected values
             const float2 *ph2 = sm.ph + (size_t)r2 * MigShape<N>::PHS;
+            const float2 *sq = spec + N - t;  // a'[-k] = sq[-T*m], k = t + T*m
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const int kf = kfold<N>(t, m);
-                float2 Q1 = ph1[kf], Q2 = ph2[kf];
-                if (conj) {
-                    Q1.y = -Q1.y;
-                    Q2.y = -Q2.y;
-                }
+                const float2 Q1 = ph1[kf], Q2 = ph2[kf];
                 const float2 p = spec[t + T * m];
-                const float2 qm = spec[(N - t - T * m) & (N - 1)];
+                const float2 qm = sq[-T * m];
                 const float2 q = make_float2(qm.x, -qm.y);
                 const float2 M = make_float2(Q1.x - Q2.y, Q1.y + Q2.x);   // Q1 + i Q2
                 const float2 Pc = make_float2(Q1.x + Q2.y, Q2.x - Q1.y);  // conj Q1 + i conj Q2
-                const float2 z = cadd(cmul(p, M), cmul(q, Pc));
-                u[m] = make_float2(0.5f * z.x, 0.5f * z.y);
+                u[m] = cadd(cmul(p, M), cmul(q, Pc));
             }
         }
         fft_row<N, +1>(u, xbuf, sm.tw, t, sync);
@@ -436,8 +442,9 @@ __device__ __forceinline__ void paired_inverse(float2 (&v)[16], bool conj, const
             for (int j = 0; j < 4; j++) {
                 const int m = 4 * q + j;
                 if ((eq >> (8 * j)) & 1u) {
-                    const bool re = r2 >= 0 || ((selp[q] >> (8 * j + 7)) & 1u) != 0;
-                    v[m] = re ? make_float2(u[m].x, 0.f) : u[m];
+                    if (r2 >= 0) v[m] = make_float2(0.5f * u[m].x, 0.f);
+                    else if ((selp[q] >> (8 * j + 7)) & 1u) v[m] = make_float2(u[m].x, 0.f);
+                    else v[m] = make_float2(u[m].x, conj ? -u[m].y : u[m].y);  // dref = conj(u) for the source
                 }
             }
         }
@@ -450,7 +457,7 @@ __device__ __forceinline__ void paired_inverse(float2 (&v)[16], bool conj, const
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const int m = 4 * q + j;
-                    if ((eq >> (8 * j)) & 1u) v[m] = make_float2(u[m].y, 0.f);
+                    if ((eq >> (8 * j)) & 1u) v[m] = make_float2(0.5f * u[m].y, 0.f);
                 }
             }
         }
@@ -467,18 +474,15 @@ __device__ __forceinline__ void paired_inverse(float2 (&v)[16], bool conj, const
             const int xj = sm.wpos[1 + j];
             const float2 *ph = sm.ph + (size_t)(sm.selb[xj] & 0x7f) * MigShape<N>::PHS;
             // sum_m b_m W^(e0 + m c) = W^e0 (...((b_15 z + b_14) z + ...) z + b_0), z = W^c:
-            // e0 = t xj, c = T xj (mod N); W^e = e^{+2 pi i e / N} from the half table
+            // e0 = t xj, c = T xj (mod N); W^e = e^{+2 pi i e / N} from the half table. For the
+            // source dref = conj(IFFT(a' P)): the imaginary part changes sign.
             const float2 z = wpow<N>(sm.wd, (T * xj) & (N - 1));
+            const float2 w0 = wpow<N>(sm.wd, (t * xj) & (N - 1));
             float2 h = make_float2(0.f, 0.f);
 #pragma unroll
-            for (int m = 15; m >= 0; m--) {
-                const int kf = kfold<N>(t, m);
-                const float2 P = ph[kf];
-                const float2 b = conj ? cmulc(spec[t + T * m], P) : cmul(spec[t + T * m], P);
-                h = cadd(cmul(h, z), b);
-            }
-            const float2 w0 = wpow<N>(sm.wd, (t * xj) & (N - 1));
+            for (int m = 15; m >= 0; m--) h = cadd(cmul(h, z), cmul(spec[t + T * m], ph[kfold<N>(t, m)]));
             float acc = h.x * w0.y + h.y * w0.x;  // Im(h W^e0)
+            if (conj) acc = -acc;
 #pragma unroll
             for (int off = (T >= 32 ? 16 : T / 2); off > 0; off >>= 1) acc += __shfl_xor_sync(lanes, acc, off);
             if ((t & 31) == 0) scr[j * NW + (t >> 5)] = acc;
@@ -504,7 +508,7 @@ __device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, cons
                                                 float2 *xbuf, float2 *spec, int t, unsigned sync,
                                                 unsigned long long used, unsigned long long cx)
 {
-    paired_forward<N>(v, xbuf, spec, sm.tw, t, sync);
+    paired_forward<N>(v, conj, xbuf, spec, sm.tw, t, sync);
     team_sync<N / 16>(sync);  // the whole spectrum is in spec
     paired_inverse<N>(v, conj, a, sm, xbuf, spec, t, sync, used, cx);
 }
