@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                 if constexpr (PSPI && !TC) {
                     copy_tables_async<N, INTERP, PAIR>(a, sm, iwi, iz, tid, NT);
                     if (active) {
-                        if constexpr (PAIR) paired_forward<N>(v, is_src, xbuf, sacc, sm.tw, t, sync);
+                        if constexpr (PAIR) paired_forward<N>(v, xbuf, sacc, sm.tw, t, sync);
                         else fft_row<N, -1>(v, xbuf, sm.tw, t, sync);
                     }
                     cp_async_wait_all();

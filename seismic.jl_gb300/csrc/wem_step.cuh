@@ -348,32 +348,21 @@ template <int N> __device__ __forceinline__ float2 wpow(const float2 *wd, int e)
 // IFFT(X_r1 + i X_r2) = Re(dref[r1]) + i Re(dref[r2]): with p = a[k], q = conj(a[-k]),
 //     z[k] = (p (Q1 + i Q2) + q (conj Q1 + i conj Q2)) / 2.
 // References taken whole somewhere (cx) and an odd one left over get a transform of their
-// own, as in step_mig. The spectrum is kept in the team's buffer spec (N + 1 samples) so that
+// own, as in step_mig. The spectrum is kept in the team's buffer spec (N samples) so that
 // every thread can read a[-k]; the selected row builds up in v.
 // At a depth with at most WHOLE_MAX points taken whole (wpos) every reference is paired,
 // and the imaginary parts at those points are direct sums.
 // First part: the forward transform, its spectrum to spec. The second part
 // (paired_inverse) follows a barrier that makes spec and the depth's tables visible.
-// spec holds a'[k], k = 0 .. N (a'[N] = a'[0], so that a'[-k] = a'[N - k] needs no wrap), with
-// a' = a for the receiver and a'[k] = conj(a[-k]) for the source row (conj): with P
-// symmetric in k, IFFT(a conj(P)) = conj(IFFT(a' P)), so the source's phase conj(P) becomes
-// P and the transforms of both rows run the same arithmetic.
 template <int N>
-__device__ __forceinline__ void paired_forward(float2 (&v)[16], bool conj, float2 *xbuf, float2 *spec,
-                                               const float2 *tw, int t, unsigned sync)
+__device__ __forceinline__ void paired_forward(float2 (&v)[16], float2 *xbuf, float2 *spec, const float2 *tw, int t,
+                                               unsigned sync)
 {
     constexpr int T = N / 16;
     fft_row<N, -1>(v, xbuf, tw, t, sync);  // v: the spectrum at k = t + T*m
-    if (!conj) {
 #pragma unroll
-        for (int m = 0; m < 16; m++) spec[t + T * m] = v[m];
-        if (t == 0) spec[N] = v[0];
-    } else {
-        float2 *sm_ = spec + N - t;  // a'[N - k] = conj(a[k]), k = t + T*m
-#pragma unroll
-        for (int m = 0; m < 16; m++) sm_[-T * m] = make_float2(v[m].x, -v[m].y);
-        if (t == 0) spec[0] = make_float2(v[0].x, -v[0].y);
-    }
+    for (int m = 0; m < 16; m++) spec[t + T * m] = v[m];
+    if (t == 0) spec[N] = v[0];  // a[N] = a[0]: a[-k] = spec[N - k] needs no wrap
 }
 
 template <int N>
@@ -414,16 +403,23 @@ __device__ __forceinline__ void paired_inverse(float2 (&v)[16], bool conj, const
         float2 u[16];
         if (r2 < 0) {
 #pragma unroll
-            for (int m = 0; m < 16; m++) u[m] = cmul(spec[t + T * m], ph1[kfold<N>(t, m)]);
+            for (int m = 0; m < 16; m++) {
+                const float2 P = ph1[kfold<N>(t, m)];
+                const float2 p = spec[t + T * m];
+                u[m] = conj ? cmulc(p, P) : cmul(p, P);
+            }
         } else {
-            // 2 z = p (Q1 + i Q2) + q (conj Q1 + i conj Q2); the factor 1/2 is applied to the
-            // selected values
+            // 2 z: the factor 1/2 is applied to the selected values
             const float2 *ph2 = sm.ph + (size_t)r2 * MigShape<N>::PHS;
-            const float2 *sq = spec + N - t;  // a'[-k] = sq[-T*m], k = t + T*m
+            const float2 *sq = spec + N - t;  // a[-k] = sq[-T*m], k = t + T*m
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const int kf = kfold<N>(t, m);
-                const float2 Q1 = ph1[kf], Q2 = ph2[kf];
+                float2 Q1 = ph1[kf], Q2 = ph2[kf];
+                if (conj) {
+                    Q1.y = -Q1.y;
+                    Q2.y = -Q2.y;
+                }
                 const float2 p = spec[t + T * m];
                 const float2 qm = sq[-T * m];
                 const float2 q = make_float2(qm.x, -qm.y);
@@ -442,9 +438,8 @@ __device__ __forceinline__ void paired_inverse(float2 (&v)[16], bool conj, const
             for (int j = 0; j < 4; j++) {
                 const int m = 4 * q + j;
                 if ((eq >> (8 * j)) & 1u) {
-                    if (r2 >= 0) v[m] = make_float2(0.5f * u[m].x, 0.f);
-                    else if ((selp[q] >> (8 * j + 7)) & 1u) v[m] = make_float2(u[m].x, 0.f);
-                    else v[m] = make_float2(u[m].x, conj ? -u[m].y : u[m].y);  // dref = conj(u) for the source
+                    const bool re = r2 >= 0 || ((selp[q] >> (8 * j + 7)) & 1u) != 0;
+                    v[m] = re ? make_float2(r2 >= 0 ? 0.5f * u[m].x : u[m].x, 0.f) : u[m];
                 }
             }
         }
@@ -474,15 +469,18 @@ __device__ __forceinline__ void paired_inverse(float2 (&v)[16], bool conj, const
             const int xj = sm.wpos[1 + j];
             const float2 *ph = sm.ph + (size_t)(sm.selb[xj] & 0x7f) * MigShape<N>::PHS;
             // sum_m b_m W^(e0 + m c) = W^e0 (...((b_15 z + b_14) z + ...) z + b_0), z = W^c:
-            // e0 = t xj, c = T xj (mod N); W^e = e^{+2 pi i e / N} from the half table. For the
-            // source dref = conj(IFFT(a' P)): the imaginary part changes sign.
+            // e0 = t xj, c = T xj (mod N); W^e = e^{+2 pi i e / N} from the half table
             const float2 z = wpow<N>(sm.wd, (T * xj) & (N - 1));
-            const float2 w0 = wpow<N>(sm.wd, (t * xj) & (N - 1));
             float2 h = make_float2(0.f, 0.f);
 #pragma unroll
-            for (int m = 15; m >= 0; m--) h = cadd(cmul(h, z), cmul(spec[t + T * m], ph[kfold<N>(t, m)]));
+            for (int m = 15; m >= 0; m--) {
+                const int kf = kfold<N>(t, m);
+                const float2 P = ph[kf];
+                const float2 b = conj ? cmulc(spec[t + T * m], P) : cmul(spec[t + T * m], P);
+                h = cadd(cmul(h, z), b);
+            }
+            const float2 w0 = wpow<N>(sm.wd, (t * xj) & (N - 1));
             float acc = h.x * w0.y + h.y * w0.x;  // Im(h W^e0)
-            if (conj) acc = -acc;
 #pragma unroll
             for (int off = (T >= 32 ? 16 : T / 2); off > 0; off >>= 1) acc += __shfl_xor_sync(lanes, acc, off);
             if ((t & 31) == 0) scr[j * NW + (t >> 5)] = acc;
@@ -508,7 +506,7 @@ __device__ __forceinline__ void step_mig_paired(float2 (&v)[16], bool conj, cons
                                                 float2 *xbuf, float2 *spec, int t, unsigned sync,
                                                 unsigned long long used, unsigned long long cx)
 {
-    paired_forward<N>(v, conj, xbuf, spec, sm.tw, t, sync);
+    paired_forward<N>(v, xbuf, spec, sm.tw, t, sync);
     team_sync<N / 16>(sync);  // the whole spectrum is in spec
     paired_inverse<N>(v, conj, a, sm, xbuf, spec, t, sync, used, cx);
 }
