@@ -145,6 +145,17 @@ class Context:
                                            off.ctypes.data_as(_i64p), cell.ctypes.data_as(_i32p),
                                            C.c_void_p(d_dev_ptr), C.c_void_p(m_dev_ptr), int(sync)))
 
+    def model_device(self, shots: Shots, m_dev_ptr: int, d_dev_ptr: int, exact: bool = False, sync: bool = True):
+        """model() with the image [nmx*nmy, nz] and the traces [ntrace, nt] in device memory
+        (raw pointers); the traces of `shots` give the geometry only."""
+        sx = np.ascontiguousarray(shots.sx, dtype=np.float32)
+        sy = np.ascontiguousarray(shots.sy, dtype=np.float32)
+        off = np.ascontiguousarray(shots.trace_offset, dtype=np.int64)
+        cell = np.ascontiguousarray(shots.trace_cell, dtype=np.int32)
+        L.check(L.lib().wem_model_device(self._h, len(sx), sx.ctypes.data_as(_f32p), sy.ctypes.data_as(_f32p),
+                                         off.ctypes.data_as(_i64p), cell.ctypes.data_as(_i32p),
+                                         C.c_void_p(m_dev_ptr), C.c_void_p(d_dev_ptr), int(bool(exact)), int(sync)))
+
     def last_timing(self):
         """(device ms of the last call, kernels it launched)"""
         ms = C.c_float()

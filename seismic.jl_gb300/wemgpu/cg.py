@@ -25,21 +25,27 @@ def inner(a: np.ndarray, b: np.ndarray) -> float:
     return float(np.dot(a.astype(np.float64).ravel(), b.astype(np.float64).ravel()))
 
 
-def conjugate_gradients(d: np.ndarray, forward: Callable[[np.ndarray], np.ndarray],
-                        adjoint: Callable[[np.ndarray], np.ndarray], niter: int = 10, mu: float = 0.0,
-                        tol: float = 1.0e-15, callback: Callable | None = None):
-    """Returns (m, cost) with cost[0] = 1 and cost[i] = (||r||^2 + mu ||m||^2)/||d||^2."""
+def _copy(x):
+    return x.clone() if hasattr(x, "clone") else np.array(x, copy=True)
+
+
+def conjugate_gradients(d, forward: Callable, adjoint: Callable, niter: int = 10, mu: float = 0.0,
+                        tol: float = 1.0e-15, callback: Callable | None = None, inner_fn: Callable = inner):
+    """Returns (m, cost) with cost[0] = 1 and cost[i] = (||r||^2 + mu ||m||^2)/||d||^2.
+    d, and what forward/adjoint return, are NumPy arrays, or device tensors with inner_fn a
+    float64 inner product of them."""
+    inner_ = inner_fn
     cost = [1.0]
-    r = np.array(d, copy=True)
+    r = _copy(d)
     g = adjoint(r)
-    m = np.zeros_like(g)
-    s = np.array(g, copy=True)
-    gamma = inner(g, g)
+    m = g * 0  # zeros of g's kind
+    s = _copy(g)
+    gamma = inner_(g, g)
     gamma00 = gamma
-    cost0 = inner(r, r)
+    cost0 = inner_(r, r)
     for it in range(1, niter + 1):
         t = forward(s)
-        delta = inner(t, t) + mu * inner(s, s)
+        delta = inner_(t, t) + mu * inner_(s, s)
         if delta <= tol:
             break
         alpha = gamma / delta
@@ -48,8 +54,8 @@ def conjugate_gradients(d: np.ndarray, forward: Callable[[np.ndarray], np.ndarra
         g = adjoint(r)
         g = g - mu * m
         gamma0 = gamma
-        gamma = inner(g, g)
-        cost1 = inner(r, r) + mu * inner(m, m)
+        gamma = inner_(g, g)
+        cost1 = inner_(r, r) + mu * inner_(m, m)
         cost.append(cost1 / cost0 if cost0 > 0 else 0.0)
         beta = gamma / gamma0
         s = beta * s + g

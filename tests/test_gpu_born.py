@@ -149,3 +149,52 @@ def test_misfit_curve_matches_reference_operator_pair(gpu_lib, oracle_mod):
     ctx.close()
     cost_gpu, cost_ref = np.array(cost_gpu), np.array(cost_ref)
     assert np.all(np.abs(cost_gpu - cost_ref) <= 1e-3 * np.maximum(cost_ref, 1e-3)), (cost_gpu, cost_ref)
+
+
+def test_device_buffer_calls_match_host_calls(gpu_lib):
+    """wem_model_device / wem_migrate_device on device tensors give the host-buffer calls'
+    results bit for bit, and CG over them (device vectors, float64 inner products) follows
+    the same misfit curve."""
+    torch = pytest.importorskip("torch")
+    from wemgpu import synth
+    from wemgpu.api import Shots
+    from wemgpu.cg import conjugate_gradients
+    c = synth.small_case(71, nx=128, nz=20, nt=96, nshot=3, pspi=1, nref=4, interp="linear")
+    p, s = c["params"], c["shots"]
+    rng = np.random.default_rng(72)
+    m = rng.standard_normal((p["nmx"], p["nz"])).astype(np.float32)
+    dev = torch.device("cuda", 0)
+    with gpu_lib.Context() as ctx:
+        ctx.prepare(p, c["vel"], c["wav"])
+        d_host = ctx.model(s, m, exact=True)
+        m_host = ctx.migrate(s)
+        m_t = torch.from_numpy(m).to(dev)
+        d_t = torch.empty(d_host.shape, dtype=torch.float32, device=dev)
+        torch.cuda.synchronize()
+        ctx.model_device(s, m_t.data_ptr(), d_t.data_ptr(), exact=True)
+        assert np.array_equal(d_t.cpu().numpy(), d_host)
+        dd_t = torch.from_numpy(np.ascontiguousarray(s.data, np.float32)).to(dev)
+        mm_t = torch.empty(m.shape, dtype=torch.float32, device=dev)
+        torch.cuda.synchronize()
+        ctx.migrate_device(s, dd_t.data_ptr(), mm_t.data_ptr())
+        assert np.array_equal(mm_t.cpu().numpy(), m_host)
+
+        geo = lambda d: Shots(s.sx, s.sy, s.trace_offset, s.trace_cell, np.ascontiguousarray(d, np.float32))
+
+        def fwd_t(x):
+            y = torch.empty(d_host.shape, dtype=torch.float32, device=dev)
+            torch.cuda.synchronize()
+            ctx.model_device(s, x.data_ptr(), y.data_ptr(), exact=True)
+            return y
+
+        def adj_t(r):
+            y = torch.empty(m.shape, dtype=torch.float32, device=dev)
+            torch.cuda.synchronize()
+            ctx.migrate_device(s, r.data_ptr(), y.data_ptr())
+            return y
+
+        inner_t = lambda a, b: float(torch.dot(a.reshape(-1).double(), b.reshape(-1).double()))
+        _, cost_t = conjugate_gradients(torch.from_numpy(d_host).to(dev), fwd_t, adj_t, niter=5, inner_fn=inner_t)
+        _, cost_h = conjugate_gradients(d_host, lambda x: ctx.model(s, np.asarray(x, np.float32), exact=True),
+                                        lambda r: ctx.migrate(geo(r)), niter=5)
+    assert np.allclose(cost_t, cost_h, rtol=1e-4, atol=1e-7)
