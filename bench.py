@@ -100,7 +100,7 @@ def flops_per_unit(p: dict) -> float:
     return 2 * F + 3 * n
 
 
-def inverse_transforms_per_step(p: dict, vel: np.ndarray, paired: bool) -> float:
+def inverse_transforms_per_step(p: dict, vel: np.ndarray, paired: bool, direct_sums: bool = True) -> float:
     """Mean inverse transforms per wavefield step of the 2-D PSPI depth kernel over the
     depth steps: one per reference some point takes its wavefield from; in the paired
     form of the nearest-lower mode (interp=ref) one per two references whose every taker
@@ -117,7 +117,7 @@ def inverse_transforms_per_step(p: dict, vel: np.ndarray, paired: bool) -> float
         ir = np.arange(nref, dtype=f32)
         vref = vmin + ir * (vmax - vmin) / (f32(nref) - f32(1))
         if vmax > vmin + f32(10):
-            i = ((f32(nref - 1) * (v - vmin)) / (vmax - vmin)).astype(np.int64)
+            i = np.maximum(((f32(nref - 1) * (v - vmin)) / (vmax - vmin)).astype(np.int64), 0)  # 3-D: v < vmin
             i1 = np.where(i > nref - 2, nref - 1, i)
             i2 = np.where(i > nref - 2, nref - 1, i + 1)
         else:
@@ -131,7 +131,7 @@ def inverse_transforms_per_step(p: dict, vel: np.ndarray, paired: bool) -> float
         if not paired:
             total += len(used)
             continue
-        if 1 <= np.count_nonzero(~interp) <= 4:  # whole points by direct sums, every reference paired
+        if direct_sums and 1 <= np.count_nonzero(~interp) <= 4:  # whole points by direct sums, every reference paired
             total += (len(used) + 1) // 2
             continue
         whole = set(i1[~interp].tolist())
@@ -182,16 +182,17 @@ def accuracy(c: dict, ctx_factory) -> dict:
     return out
 
 
-def bytes_per_unit_3d(p: dict) -> float:
+def bytes_per_unit_3d(p: dict, planes: float | None = None) -> float:
     """Device-memory bytes of one 3-D (shot, frequency, depth step) in the three-pass
     design (the padded x-y plane does not fit in shared memory): with n = nmx*nmy,
-    M = nmx*nky rows kept after the y transform and R references, both wavefields:
-    pass A reads U (2n) and writes Y (2M); pass B reads Y (2M) and writes C (2RM);
-    pass C reads C (2RM) and writes U (2n); 8 bytes per complex sample."""
+    M = nmx*nky rows kept after the y transform and R planes per wavefield (one per
+    reference, or fewer with paired planes), both wavefields: pass A reads U (2n) and
+    writes Y (2M); pass B reads Y (2M) and writes C (2RM); pass C reads C (2RM) and
+    writes U (2n); 8 bytes per complex sample."""
     nmy = int(p["nmy"])
     n = int(p["nmx"]) * nmy
     M = int(p["nmx"]) * int(p["padx"]) * nmy
-    R = int(p["nref"]) if int(p.get("pspi", 1)) else 1
+    R = planes if planes is not None else (int(p["nref"]) if int(p.get("pspi", 1)) else 1)
     return 8.0 * (4 * n + 4 * M + 4 * R * M)
 
 
@@ -584,8 +585,13 @@ def main():
                 "tensor_flops_per_unit": tf, "flops_per_unit": fl, "algorithmic_tflops": achieved,
                 "fp32_nominal_tflops": fp32_nominal, "fp32_frac": achieved / fp32_nominal}
     if int(p.get("nmy", 1)) > 1:
-        # 3-D: three passes over device memory per depth step; their bytes bound it
-        bu = bytes_per_unit_3d(p)
+        # 3-D: three passes over device memory per depth step; their bytes bound it (the
+        # planes per wavefield the run uses: paired planes in the nearest-lower mode)
+        paired3 = int(p.get("pspi", 1)) and p.get("interp", "ref") == "ref" and \
+            os.environ.get("WEM_PAIRED", "1") != "0" and int(p["nref"]) <= 16
+        planes = inverse_transforms_per_step(p, c["vel"], bool(paired3), direct_sums=False) \
+            if int(p.get("pspi", 1)) else 1.0
+        bu = bytes_per_unit_3d(p, planes)
         hbm = float(peaks.get("hbm_gbs", 6800.0))
         gbs = units * bu / (mig_ms / 1000.0) / 1e9
         roof = {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,

@@ -125,11 +125,13 @@ __device__ __forceinline__ int col_ky(int b, int cc, int half_cols, int nky)
 // global copies on 16 different 8-byte banks
 __host__ __device__ constexpr int tile_pitch(int nmx) { return ((nmx + 15) & ~15) + 2; }
 // two phase tables and two column tiles: reference r works in buffer r % 2 while the
-// result of reference r - 1 is copied out of the other
-__host__ __device__ constexpr size_t col_smem_bytes(int twp, int half, int cw, int teams, int padn, int nmx)
+// result of reference r - 1 is copied out of the other; with paired planes (a.plan) the
+// two tables hold the pair's references and the columns' spectra follow ([2][CW][NX + 2])
+__host__ __device__ constexpr size_t col_smem_bytes(int twp, int half, int cw, int teams, int padn, int nmx,
+                                                    int nx = 0, bool paired = false)
 {
     return sizeof(float2) * ((size_t)twp + (size_t)2 * (cw / 2 + 1) * half + (size_t)teams * padn +
-                             (size_t)2 * 2 * tile_pitch(nmx) * cw);
+                             (size_t)2 * 2 * tile_pitch(nmx) * cw + (paired ? (size_t)2 * cw * (nx + 2) : 0));
 }
 
 template <int NX, bool PSPI>
@@ -144,6 +146,8 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
     const int pitch = tile_pitch(a.nmx);
     float2 *s_tile0 = s_x + (size_t)2 * CW * pad16(NX);  // [2][2][CW][pitch] column tiles
     const size_t tile_sz = (size_t)2 * CW * pitch;
+    float2 *s_spec = s_tile0 + 2 * tile_sz;                // paired planes: [2][CW][NX + 2] spectra
+    const int *plan = PSPI && a.plan ? a.plan + (size_t)a.iz * PLAN3_STRIDE : nullptr;
     const int tid = threadIdx.x, team = tid / TX, t = tid - team * TX;
     const int w = team / CW, c = team - w * CW;
     float2 *xbuf = s_x + (size_t)team * pad16(NX);
@@ -193,6 +197,86 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
         }
         if (active) fft_row<NX, -1>(v, xbuf, s_tw, t, sync);
         const float slow_po = PSPI ? 0.f : __fmul_rn(a.po[iz], a.po[iz]);
+        if (plan) {
+            if (active) {
+                // the column's spectrum for the pairs' a(-kx, -ky) reads; entry NX = entry 0
+                float2 *sp = s_spec + ((size_t)w * CW + c) * (NX + 2);
+#pragma unroll
+                for (int m = 0; m < 16; m++) sp[t + TX * m] = v[m];
+                if (t == 0) sp[NX] = v[0];
+            }
+            // the column holding -ky: the mirror half, or itself for ky = 0 and nky/2
+            const int pc = (ky_c == 0 || ky_c == nky / 2) ? c : (c < H ? c + H : c - H);
+            const float2 *sq = s_spec + ((size_t)w * CW + pc) * (NX + 2) + NX - t;  // a(-k) = sq[-TX*m]
+            const int np = plan[0];
+            for (int sl = 0; sl < np; sl++) {
+                const int r1 = plan[1 + 2 * sl], r2 = plan[2 + 2 * sl];
+                float2 *s_tile = s_tile0 + (size_t)(sl & 1) * tile_sz;
+                // every thread is past the previous slot's products before its tables change
+                __syncthreads();
+                for (int e = tid; e < 2 * (zero_col ? H + 1 : H) * HALF; e += NT) {
+                    const int half_e = (zero_col ? H + 1 : H) * HALF;
+                    const int which = e >= half_e ? 1 : 0, ee = e - which * half_e;
+                    const int rr = ee / HALF, kk = ee - rr * HALF;
+                    const int r = which ? r2 : r1;
+                    if (r < 0) continue;
+                    const int kyi = rr < H ? col_ky(blk, rr, H, nky) : 0;
+                    const float ky = __fmul_rn(a.dky, (float)kyi);
+                    const float kx = __fmul_rn(a.dkx, (float)kk);
+                    const float slow2 = a.slow2[(size_t)iz * a.nref + r];
+                    const float s2 = __fsub_rn(__fsub_rn(__fmul_rn(w2, slow2), __fmul_rn(kx, kx)), __fmul_rn(ky, ky));
+                    float2 P;
+                    if (s2 >= 0.f) {
+                        float sn, cs;
+                        sincosf(__fmul_rn(__fsqrt_rn(s2), a.dz), &sn, &cs);
+                        P = make_float2(cs, sn);
+                    } else {
+                        P = make_float2(expf(-__fmul_rn(__fmul_rn(0.2f, __fsqrt_rn(-s2)), fabsf(a.dz))), 0.f);
+                    }
+                    s_ph0[(size_t)which * CS::ROWS * HALF + ee] = make_float2(P.x * a.inv_n, P.y * a.inv_n);
+                }
+                __syncthreads();  // tables complete; tile sl % 2 free
+                if (active) {
+                    const float2 *ph1 = s_ph0 + (size_t)row_c * HALF;
+                    const float2 *ph2 = s_ph0 + (size_t)CS::ROWS * HALF + (size_t)row_c * HALF;
+                    float2 u[16];
+                    if (r2 < 0) {
+#pragma unroll
+                        for (int m = 0; m < 16; m++) {
+                            const int k = t + TX * m;
+                            const float2 P = ph1[k <= NX / 2 ? k : NX - k];
+                            u[m] = conj ? cmulc(v[m], P) : cmul(v[m], P);
+                        }
+                    } else {
+                        // 2 z = p (Q1 + i Q2) + conj(a(-k)) (conj Q1 + i conj Q2); the 1/2 is
+                        // applied where pass C selects the real parts
+#pragma unroll
+                        for (int m = 0; m < 16; m++) {
+                            const int k = t + TX * m, kf = k <= NX / 2 ? k : NX - k;
+                            float2 Q1 = ph1[kf], Q2 = ph2[kf];
+                            if (conj) {
+                                Q1.y = -Q1.y;
+                                Q2.y = -Q2.y;
+                            }
+                            const float2 qm = sq[-TX * m];
+                            const float2 M = make_float2(Q1.x - Q2.y, Q1.y + Q2.x);
+                            const float2 Pc = make_float2(Q1.x + Q2.y, Q2.x - Q1.y);
+                            u[m] = cadd(cmul(v[m], M), cmulc(Pc, qm));
+                        }
+                    }
+                    fft_row<NX, +1>(u, xbuf, s_tw, t, sync);
+#pragma unroll
+                    for (int m = 0; m < 16; m++) {
+                        const int x = t + TX * m;
+                        if (x < nmx) s_tile[((size_t)w * CW + c) * pitch + x] = u[m];
+                    }
+                }
+                if (sl > 0) copy_out(s_tile0 + (size_t)((sl - 1) & 1) * tile_sz, sl - 1);
+            }
+            __syncthreads();
+            if (np > 0) copy_out(s_tile0 + (size_t)((np - 1) & 1) * tile_sz, np - 1);
+            continue;
+        }
         for (int r = 0; r < nref; r++) {
             float2 *s_ph = s_ph0 + (size_t)(r & 1) * CS::ROWS * HALF;
             float2 *s_tile = s_tile0 + (size_t)(r & 1) * tile_sz;
@@ -294,12 +378,32 @@ __global__ void __launch_bounds__(256, 2) wem3d_rows_inv_kernel(const Mig3dArgs 
                 float2 acc[16];
 #pragma unroll
                 for (int m = 0; m < 16; m++) acc[m] = make_float2(0.f, 0.f);
-                for (int r = 0; r < nref; r++) {
-                    const float2 *crow = a.C + ((((size_t)item * 2 + w) * nref + r) * nmx + x) * nky;
+                // planes: one per reference, or (paired planes, a.plan) the real parts of two
+                // references in one plane and one plane per reference taken whole
+                const int *plan = (PSPI && INTERP == 0 && a.plan) ? a.plan + (size_t)iz * PLAN3_STRIDE : nullptr;
+                const int np = plan ? plan[0] : nref;
+                for (int pl = 0; pl < np; pl++) {
+                    const float2 *crow = a.C + ((((size_t)item * 2 + w) * nref + pl) * nmx + x) * nky;
                     float2 u[16];
 #pragma unroll
                     for (int m = 0; m < 16; m++) u[m] = crow[t + TY * m];
                     fft_row<NY, +1>(u, xbuf, s_tw, t, sync);
+                    if (plan) {
+                        const int r1 = plan[1 + 2 * pl], r2 = plan[2 + 2 * pl];
+#pragma unroll
+                        for (int m = 0; m < 16; m++) {
+                            const uint32_t b = (selp[m >> 2] >> (8 * (m & 3))) & 0xffu;
+                            const int i1 = (int)(b & 0x7fu);
+                            if (i1 == r1) {
+                                if (r2 >= 0) acc[m] = make_float2(0.5f * u[m].x, 0.f);
+                                else acc[m] = (b & 0x80u) ? make_float2(u[m].x, 0.f) : u[m];
+                            } else if (r2 >= 0 && i1 == r2) {
+                                acc[m] = make_float2(0.5f * u[m].y, 0.f);
+                            }
+                        }
+                        continue;
+                    }
+                    const int r = pl;
 #pragma unroll
                     for (int m = 0; m < 16; m++) {
                         if (PSPI) {
@@ -440,7 +544,7 @@ template <int NY, bool PSPI, int INTERP> static int rows_inv(const Mig3dArgs &a,
 template <int NX, bool PSPI> static int cols(const Mig3dArgs &a, int grid, cudaStream_t st, size_t *smem_out)
 {
     using CS = ColShape<NX>;
-    const size_t smem = col_smem_bytes(CS::TWP, CS::HALF, CS::CW, 2 * CS::CW, pad16(NX), a.nmx);
+    const size_t smem = col_smem_bytes(CS::TWP, CS::HALF, CS::CW, 2 * CS::CW, pad16(NX), a.nmx, NX, PSPI && a.plan);
     if (smem_out) { *smem_out = smem; return 0; }
     auto k = wem3d_cols_kernel<NX, PSPI>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;

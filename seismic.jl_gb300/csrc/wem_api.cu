@@ -87,6 +87,8 @@ struct wem_ctx {
     DevBuf tapery, twy;           // 3-D: y taper and y-FFT twiddles
     DevBuf tcw, tcerr;            // split16: W operands of the tensor-core DFT stages, timeout word
     DevBuf wposb;                 // [nz][WPOS_STRIDE] points taking their wavefield whole (paired form)
+    DevBuf plan3;                 // [nz][PLAN3_STRIDE] 3-D paired planes (empty: one plane per reference)
+    bool plan3_ok = false;
     DevBuf selbp;                 // [nz][nmx rounded up to 16] selection rows (precomputed-table path)
     DevBuf wlinp;                 // [nz][nmx rounded up to 4] linear weights (precomputed-table path)
     DevBuf ptab;                  // [nwf][nz][nref][nkx/2 + 2] phase tables (paired form)
@@ -167,7 +169,7 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
                        &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
                        &c->ssyn_ref, &c->ssyn_exact, &c->recv, &c->slots, &c->image, &c->data,
                        &c->tbase, &c->igx, &c->smig, &c->mimg, &c->tapery, &c->twy, &c->m3_items,
-                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb, &c->selbp, &c->wlinp, &c->ptab };
+                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb, &c->selbp, &c->wlinp, &c->ptab, &c->plan3 };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -439,6 +441,48 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     CK(cudaMemsetAsync(c->tcerr.p, 0, sizeof(int), st));
     CK(cudaMemcpyAsync(c->refmask.p, used.data(), sizeof(unsigned long long) * 2 * nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->wposb.p, wpos.data(), sizeof(int) * wpos.size(), cudaMemcpyHostToDevice, st));
+    // 3-D nearest-lower PSPI: the planes of pass B/C per depth -- pairs of references whose
+    // every taker keeps the real part, then an odd one and those taken whole, one plane each
+    c->plan3_ok = false;
+    if (p.nmy > 1 && p.pspi && p.interp == WEM_INTERP_REF && nref <= PLAN3_MAX) {
+        const char *pe = getenv("WEM_PAIRED");
+        if (!(pe && !strcmp(pe, "0"))) {
+            std::vector<int> plan((size_t)nz * PLAN3_STRIDE, 0);
+            for (int iz = 0; iz < nz; iz++) {
+                int *pr = &plan[(size_t)iz * PLAN3_STRIDE];
+                const unsigned long long u = used[iz], cxm = used[(size_t)nz + iz];
+                int np = 0, pend = -1;
+                for (int r = 0; r < nref; r++) {
+                    if (!((u >> r) & 1ull) || ((cxm >> r) & 1ull)) continue;
+                    if (pend < 0) {
+                        pend = r;
+                    } else {
+                        pr[1 + 2 * np] = pend;
+                        pr[2 + 2 * np] = r;
+                        np++;
+                        pend = -1;
+                    }
+                }
+                if (pend >= 0) {
+                    pr[1 + 2 * np] = pend;
+                    pr[2 + 2 * np] = -1;
+                    np++;
+                }
+                for (int r = 0; r < nref; r++) {
+                    if (!((u >> r) & 1ull) || !((cxm >> r) & 1ull)) continue;
+                    pr[1 + 2 * np] = r;
+                    pr[2 + 2 * np] = -1;
+                    np++;
+                }
+                pr[0] = np;
+            }
+            int rc3;
+            if ((rc3 = ensure(c->plan3, sizeof(int) * plan.size()))) return rc3;
+            CK(cudaMemcpyAsync(c->plan3.p, plan.data(), sizeof(int) * plan.size(), cudaMemcpyHostToDevice, st));
+            CK(cudaStreamSynchronize(st));  // plan is a local
+            c->plan3_ok = true;
+        }
+    }
     CK(cudaMemcpyAsync(c->po.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->pd.p, pd.data(), sizeof(float) * pd.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->vref.p, vref.data(), sizeof(float) * vref.size(), cudaMemcpyHostToDevice, st));
@@ -697,6 +741,17 @@ static int choose_shape(wem_ctx *c, int nshot, int *wide)
     return WEM_OK;
 }
 
+// the paired-plane plan of the 3-D passes when it was built and pass B's shared memory
+// (with the columns' spectra) fits the device
+static const int *plan3_for(wem_ctx *c, Mig3dArgs a)
+{
+    if (!c->plan3_ok) return nullptr;
+    a.plan = P<int>(c->plan3);
+    size_t smem = 0;
+    if (m3d_cols_smem(c->nkx, c->p.pspi, a, &smem) || (int)smem > c->max_smem) return nullptr;
+    return P<int>(c->plan3);
+}
+
 // 3-D migration: spectra -> per depth step the three plane passes of wem_3d.cu for
 // every (shot, frequency) of a batch -> image chunks -> image.
 static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, float *m_dev)
@@ -756,6 +811,7 @@ static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev,
         a.U = P<float2>(c->m3_U); a.Y = P<float2>(c->m3_Y); a.C = P<float2>(c->m3_C);
         // batches start on chunk boundaries, so the chunk index of local item i is (b0+i)/chunk
         a.img_parts = P<float2>(c->m3_parts) + (size_t)(b0 / chunk) * nz * n;
+        a.plan = plan3_for(c, a);
         if (m3d_launch_init(a, st)) return fail(WEM_ERR_CUDA, "3-D init launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;
         for (int iz = 0; iz < nz; iz++) {
@@ -1433,6 +1489,7 @@ static int run_model3d(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, f
         a.src_cell = P<int>(c->igx); a.srcw = P<float2>(c->srcw); a.recv = nullptr;
         a.U = P<float2>(c->m3_U); a.Y = P<float2>(c->m3_Y); a.C = P<float2>(c->m3_C); a.img_parts = nullptr;
         a.pspi = p.pspi; a.smig = P<float2>(c->smig); a.mimg = P<float>(c->mimg);
+        a.plan = plan3_for(c, a);
         a.mode = 1;
         if (m3d_launch_init(a, st)) return fail(WEM_ERR_CUDA, "3-D init launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;

@@ -107,7 +107,12 @@ struct Mig3dArgs {
     int mode, pspi;     // mode 0: migration
     float2 *smig;       // [item][nz][nmx*nmy]
     const float *mimg;  // [nz][nmx*nmy] image, depth-major
+    // PSPI nearest-lower mode: per depth the planes of pass B/C, [nz][PLAN3_STRIDE] = count,
+    // then (r1, r2) per plane: the real parts of r1 and r2 in one plane, or r2 = -1 for a
+    // reference of its own (nullptr: one plane per reference)
+    const int *plan;
 };
+constexpr int PLAN3_MAX = 16, PLAN3_STRIDE = 1 + 2 * PLAN3_MAX;
 int m3d_supported(int nkx, int nky);
 int m3d_cols_block(int nkx);
 int m3d_cols_smem(int nkx, int pspi, const Mig3dArgs &a, size_t *smem);

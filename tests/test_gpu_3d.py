@@ -51,6 +51,32 @@ def test_3d_plane_shapes(gpu_lib, oracle_mod, nx, ny, padx):
     assert rel_l2(m, want) < TOL
 
 
+@pytest.mark.parametrize("nref", [3, 6])
+def test_3d_paired_planes(gpu_lib, oracle_mod, monkeypatch, nref):
+    """The nearest-lower mode in 3-D: the real parts of two reference wavefields come from
+    one plane of passes B and C (Hermitian projection over (kx, ky): a(-kx, -ky) from the
+    mirror column), references taken whole somewhere keep a plane of their own. Depth
+    levels: random, a velocity range of 40 m/s (reference spacing <= 10 m/s at nref 6:
+    every reference taken whole) and constant velocity. Against the port and against one
+    plane per reference (WEM_PAIRED=0)."""
+    from wemgpu import synth
+    c = synth.small_case3d(81, nx=64, ny=32, nz=9, nt=64, nshot=2, pspi=1, nref=nref, fmax=30.0)
+    rng = np.random.default_rng(82)
+    vel = c["vel"].copy()
+    vel[:, 3:5] = 2500.0
+    vel[:, 5:7] = 2500.0 + 40.0 * rng.random((vel.shape[0], 2))
+    vel[0, 5:7] = vel[:, 5:7].min(axis=0) - 1.0  # the depth's minimum on the first x-plane
+    want = _port_stack(oracle_mod, c["params"], vel, c["wav"], c["shots"])
+    images = []
+    for paired in ("1", "0"):
+        monkeypatch.setenv("WEM_PAIRED", paired)
+        with gpu_lib.Context() as ctx:
+            ctx.prepare(c["params"], vel, c["wav"])
+            images.append(ctx.migrate(c["shots"]))
+        assert rel_l2(images[-1], want) < TOL, (paired, rel_l2(images[-1], want))
+    assert rel_l2(images[0], images[1]) < 1e-5
+
+
 def test_3d_deterministic_and_depths(gpu_lib, oracle_mod):
     from wemgpu import synth
     c = synth.small_case3d(51, nx=32, ny=32, nz=10, nt=64, nshot=1, pspi=1, nref=3)
@@ -73,7 +99,7 @@ def test_3d_modelling_matches_reference_golden(gpu_lib, case):
     assert rel_l2(d, g["d_ref"]) < TOL, rel_l2(d, g["d_ref"])
 
 
-@pytest.mark.parametrize("pspi,interp", [(0, "ref"), (1, "linear")])
+@pytest.mark.parametrize("pspi,interp", [(0, "ref"), (1, "ref"), (1, "linear")])
 def test_3d_batched_modelling_matches_port(gpu_lib, oracle_mod, pspi, interp):
     """Several shots with source depth and receiver depth below the surface in one call,
     against the oracle's port shot by shot at the shots' receiver cells; the exact
