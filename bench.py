@@ -589,7 +589,9 @@ def main():
         # planes per wavefield the run uses: paired planes in the nearest-lower mode)
         paired3 = int(p.get("pspi", 1)) and p.get("interp", "ref") == "ref" and \
             os.environ.get("WEM_PAIRED", "1") != "0" and int(p["nref"]) <= 16
-        planes = inverse_transforms_per_step(p, c["vel"], bool(paired3), direct_sums=False) \
+        sums3 = int(p["padx"]) * int(p["nmx"]) <= 512 and int(p["padx"]) * int(p["nmy"]) <= 512 and \
+            os.environ.get("WEM_DIRECT_SUMS", "1") != "0"
+        planes = inverse_transforms_per_step(p, c["vel"], bool(paired3), direct_sums=sums3) \
             if int(p.get("pspi", 1)) else 1.0
         bu = bytes_per_unit_3d(p, planes)
         hbm = float(peaks.get("hbm_gbs", 6800.0))

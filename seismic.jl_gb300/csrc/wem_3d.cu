@@ -96,6 +96,26 @@ __global__ void __launch_bounds__(256) wem3d_rows_fwd_kernel(const Mig3dArgs a)
     }
 }
 
+// e^{+2 pi i e / n}, e in [0, n) (n a power of two): sincospif of the exact fraction 2e/n
+__device__ __forceinline__ float2 expi_frac(int e, int n)
+{
+    float sn, cs;
+    sincospif(__fdiv_rn(2.f * (float)e, (float)n), &sn, &cs);
+    return make_float2(cs, sn);
+}
+
+// sum over the team (T <= 32 threads, aligned lanes): every thread gets the total
+template <int T> __device__ __forceinline__ float2 team_sum2(float2 v, unsigned lanes)
+{
+    static_assert(T <= 32, "team within a warp");
+#pragma unroll
+    for (int off = T / 2; off > 0; off >>= 1) {
+        v.x += __shfl_xor_sync(lanes, v.x, off);
+        v.y += __shfl_xor_sync(lanes, v.y, off);
+    }
+    return v;
+}
+
 // ---------------------------------------------------------------- pass B
 // CTA: 2*CW teams of TX = NX/16 threads -- CW columns of the source (teams 0..CW-1) and of
 // the receiver (teams CW..2CW-1) of one item. A job's columns are CW/2 columns ky of the
@@ -148,6 +168,7 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
     const size_t tile_sz = (size_t)2 * CW * pitch;
     float2 *s_spec = s_tile0 + 2 * tile_sz;                // paired planes: [2][CW][NX + 2] spectra
     const int *plan = PSPI && a.plan ? a.plan + (size_t)a.iz * PLAN3_STRIDE : nullptr;
+    const int *wp = plan && a.wpos ? a.wpos + (size_t)a.iz * WPOS_STRIDE : nullptr;  // points taken whole
     const int tid = threadIdx.x, team = tid / TX, t = tid - team * TX;
     const int w = team / CW, c = team - w * CW;
     float2 *xbuf = s_x + (size_t)team * pad16(NX);
@@ -239,6 +260,29 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
                 if (active) {
                     const float2 *ph1 = s_ph0 + (size_t)row_c * HALF;
                     const float2 *ph2 = s_ph0 + (size_t)CS::ROWS * HALF + (size_t)row_c * HALF;
+                    if constexpr (TX <= 32) {
+                        // points taken whole whose reference is in this plane: the column's
+                        // sum over kx, S(ky) = sum a(kx) Q(kx, ky) e^{+2 pi i kx x0 / NX}, by
+                        // Horner's rule over the thread's wavenumbers, for pass C's sum over ky
+                        const int nj = wp ? wp[0] : 0;
+                        for (int j = 0; j < nj; j++) {
+                            const int cell = wp[1 + j];
+                            const int rj = a.selb[(size_t)iz * a.nmx * a.nmy + cell] & 0x7f;
+                            if (rj != r1 && rj != r2) continue;
+                            const int x0 = cell / a.nmy;
+                            const float2 *ph = rj == r1 ? ph1 : ph2;
+                            const float2 zz = expi_frac((TX * x0) & (NX - 1), NX);
+                            float2 h = make_float2(0.f, 0.f);
+#pragma unroll
+                            for (int m = 15; m >= 0; m--) {
+                                const int k = t + TX * m;
+                                const float2 P = ph[k <= NX / 2 ? k : NX - k];
+                                h = cadd(cmul(h, zz), conj ? cmulc(v[m], P) : cmul(v[m], P));
+                            }
+                            const float2 sj = team_sum2<TX>(cmul(h, expi_frac((t * x0) & (NX - 1), NX)), sync);
+                            if (t == 0) a.dsum[(((size_t)item * 2 + w) * WHOLE_MAX + j) * nky + ky_c] = sj;
+                        }
+                    }
                     float2 u[16];
                     if (r2 < 0) {
 #pragma unroll
@@ -403,7 +447,7 @@ __global__ void __launch_bounds__(256, 2) wem3d_rows_inv_kernel(const Mig3dArgs 
                         }
                         continue;
                     }
-                    const int r = pl;
+                    const int r = pl;  // one plane per reference
 #pragma unroll
                     for (int m = 0; m < 16; m++) {
                         if (PSPI) {
@@ -423,6 +467,29 @@ __global__ void __launch_bounds__(256, 2) wem3d_rows_inv_kernel(const Mig3dArgs 
                             }
                         } else {
                             acc[m] = u[m];
+                        }
+                    }
+                }
+                if constexpr (PSPI && INTERP == 0 && TY <= 32) {
+                    // points of this row taken whole: Im dref(x0, y0) = Im sum_ky S(ky)
+                    // e^{+2 pi i ky y0 / NY} over pass B's column sums (Horner, team sum)
+                    const int *wp = (a.plan && a.wpos) ? a.wpos + (size_t)iz * WPOS_STRIDE : nullptr;
+                    const int nj = wp ? wp[0] : 0;
+                    for (int j = 0; j < nj; j++) {
+                        const int cell = wp[1 + j];
+                        if (cell / nmy != x) continue;
+                        const int y0 = cell - x * nmy;
+                        const float2 *ds = a.dsum + (((size_t)item * 2 + w) * WHOLE_MAX + j) * nky;
+                        const float2 zz = expi_frac((TY * y0) & (NY - 1), NY);
+                        float2 h = make_float2(0.f, 0.f);
+#pragma unroll
+                        for (int m = 15; m >= 0; m--) h = cadd(cmul(h, zz), ds[t + TY * m]);
+                        const float2 tot = team_sum2<TY>(cmul(h, expi_frac((t * y0) & (NY - 1), NY)), sync);
+                        if (t == y0 % TY) {
+                            const int mj = y0 / TY;
+#pragma unroll
+                            for (int m = 0; m < 16; m++)
+                                if (m == mj) acc[m].y = tot.y;
                         }
                     }
                 }

@@ -88,6 +88,7 @@ struct wem_ctx {
     DevBuf tcw, tcerr;            // split16: W operands of the tensor-core DFT stages, timeout word
     DevBuf wposb;                 // [nz][WPOS_STRIDE] points taking their wavefield whole (paired form)
     DevBuf plan3;                 // [nz][PLAN3_STRIDE] 3-D paired planes (empty: one plane per reference)
+    DevBuf dsum3;                 // 3-D direct sums: [item][2][WHOLE_MAX][nky] column sums
     bool plan3_ok = false;
     DevBuf selbp;                 // [nz][nmx rounded up to 16] selection rows (precomputed-table path)
     DevBuf wlinp;                 // [nz][nmx rounded up to 4] linear weights (precomputed-table path)
@@ -169,7 +170,7 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
                        &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
                        &c->ssyn_ref, &c->ssyn_exact, &c->recv, &c->slots, &c->image, &c->data,
                        &c->tbase, &c->igx, &c->smig, &c->mimg, &c->tapery, &c->twy, &c->m3_items,
-                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb, &c->selbp, &c->wlinp, &c->ptab, &c->plan3 };
+                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb, &c->selbp, &c->wlinp, &c->ptab, &c->plan3, &c->dsum3 };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -363,7 +364,9 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
             }
         }
         int &cnt = wpos[(size_t)iz * WPOS_STRIDE];
-        if (cnt > WHOLE_MAX || p.nmy > 1 || p.interp != WEM_INTERP_REF || !direct_sums)
+        // 3-D: direct sums where the paired planes' passes reduce within a warp (nkx, nky <= 512)
+        const bool sums_here = p.nmy == 1 || (nkx <= 512 && nky <= 512);
+        if (cnt > WHOLE_MAX || !sums_here || p.interp != WEM_INTERP_REF || !direct_sums)
             cnt = 0;  // the whole references keep transforms of their own
         else used[(size_t)nz + iz] = 0ull;
         if (!p.pspi) {
@@ -778,6 +781,7 @@ static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev,
         (rc = ensure(c->m3_U, sizeof(float2) * (size_t)batch * 2 * n)) ||
         (rc = ensure(c->m3_Y, sizeof(float2) * (size_t)batch * 2 * nmx * c->nky)) ||
         (rc = ensure(c->m3_C, sizeof(float2) * (size_t)batch * 2 * nref * nmx * c->nky)) ||
+        (rc = ensure(c->dsum3, sizeof(float2) * (size_t)batch * 2 * WHOLE_MAX * c->nky)) ||
         (rc = ensure(c->m3_items, sizeof(int) * 2 * (size_t)nitems)))
         return rc;
     std::vector<int> items(2 * (size_t)nitems);
@@ -812,6 +816,10 @@ static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev,
         // batches start on chunk boundaries, so the chunk index of local item i is (b0+i)/chunk
         a.img_parts = P<float2>(c->m3_parts) + (size_t)(b0 / chunk) * nz * n;
         a.plan = plan3_for(c, a);
+        if (a.plan) {
+            a.wpos = P<int>(c->wposb);
+            a.dsum = P<float2>(c->dsum3);
+        }
         if (m3d_launch_init(a, st)) return fail(WEM_ERR_CUDA, "3-D init launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;
         for (int iz = 0; iz < nz; iz++) {
@@ -1461,6 +1469,7 @@ static int run_model3d(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, f
         (rc = ensure(c->m3_U, sizeof(float2) * (size_t)batch * 2 * n)) ||
         (rc = ensure(c->m3_Y, sizeof(float2) * (size_t)batch * 2 * nmx * c->nky)) ||
         (rc = ensure(c->m3_C, sizeof(float2) * (size_t)batch * 2 * nref * nmx * c->nky)) ||
+        (rc = ensure(c->dsum3, sizeof(float2) * (size_t)batch * 2 * WHOLE_MAX * c->nky)) ||
         (rc = ensure(c->smig, sizeof(float2) * (size_t)batch * nz * n)) ||
         (rc = ensure(c->m3_items, sizeof(int) * 2 * (size_t)std::max(nitems, 1))))
         return rc;
@@ -1490,6 +1499,10 @@ static int run_model3d(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, f
         a.U = P<float2>(c->m3_U); a.Y = P<float2>(c->m3_Y); a.C = P<float2>(c->m3_C); a.img_parts = nullptr;
         a.pspi = p.pspi; a.smig = P<float2>(c->smig); a.mimg = P<float>(c->mimg);
         a.plan = plan3_for(c, a);
+        if (a.plan) {
+            a.wpos = P<int>(c->wposb);
+            a.dsum = P<float2>(c->dsum3);
+        }
         a.mode = 1;
         if (m3d_launch_init(a, st)) return fail(WEM_ERR_CUDA, "3-D init launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;

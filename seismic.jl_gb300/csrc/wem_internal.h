@@ -111,6 +111,11 @@ struct Mig3dArgs {
     // then (r1, r2) per plane: the real parts of r1 and r2 in one plane, or r2 = -1 for a
     // reference of its own (nullptr: one plane per reference)
     const int *plan;
+    // with a plan: per depth the count (<= WHOLE_MAX) and cells (x * nmy + y) of the points
+    // that take their wavefield whole (their references are paired; the imaginary parts are
+    // direct sums: pass B sums each column over kx into dsum, pass C sums over ky)
+    const int *wpos;    // [nz][WPOS_STRIDE]
+    float2 *dsum;       // [item][2][WHOLE_MAX][nky]
 };
 constexpr int PLAN3_MAX = 16, PLAN3_STRIDE = 1 + 2 * PLAN3_MAX;
 int m3d_supported(int nkx, int nky);

@@ -57,8 +57,10 @@ def test_3d_paired_planes(gpu_lib, oracle_mod, monkeypatch, nref):
     one plane of passes B and C (Hermitian projection over (kx, ky): a(-kx, -ky) from the
     mirror column), references taken whole somewhere keep a plane of their own. Depth
     levels: random, a velocity range of 40 m/s (reference spacing <= 10 m/s at nref 6:
-    every reference taken whole) and constant velocity. Against the port and against one
-    plane per reference (WEM_PAIRED=0)."""
+    every reference taken whole) and constant velocity; random levels whose maximum one or
+    three points take (their references paired, the imaginary parts there from direct sums
+    over kx in pass B and over ky in pass C). Against the port and against one plane per
+    reference (WEM_PAIRED=0)."""
     from wemgpu import synth
     c = synth.small_case3d(81, nx=64, ny=32, nz=9, nt=64, nshot=2, pspi=1, nref=nref, fmax=30.0)
     rng = np.random.default_rng(82)
@@ -66,6 +68,7 @@ def test_3d_paired_planes(gpu_lib, oracle_mod, monkeypatch, nref):
     vel[:, 3:5] = 2500.0
     vel[:, 5:7] = 2500.0 + 40.0 * rng.random((vel.shape[0], 2))
     vel[0, 5:7] = vel[:, 5:7].min(axis=0) - 1.0  # the depth's minimum on the first x-plane
+    vel[[3, 700, 1500], 7] = vel[:, 7].max()  # a maximum taken by 3 points (direct sums)
     want = _port_stack(oracle_mod, c["params"], vel, c["wav"], c["shots"])
     images = []
     for paired in ("1", "0"):
