@@ -7,22 +7,22 @@
 //      operator of ssop_source (taper, then exp(i w pd dz), FFT_x, phase with the mean
 //      slowness, IFFT_x, wem.c:763-820), one CTA per frequency, the row in shared memory,
 //      every depth stored: u[f][z][x].
-//   2. wem_axis_dft_kernel: the derivatives. The reference takes 3-D FFTs of u and
-//      inverse FFTs of i k_x A, i k_z A, i k_x^left A, i k_x^right A (wem.c:822-985).
-//      The transform is separable and each factor i k acts on one axis only, so
-//      IDFT3(i k_x DFT3(u)) = IDFT_x(i k_x DFT_x(u)) exactly: two forward and four inverse
-//      one-axis transforms per frequency instead of one forward and seven inverse 3-D ones.
-//      The axes have any length (nz is rarely a power of two), so each transform is a
-//      tiled direct DFT (a complex matrix product against W^{ik}, the table built in FP64).
-//   When nmx is a power of two in [32, 2048] steps 1 and the x transforms of 2 run on the
+//   2. the derivatives. The reference takes 3-D FFTs of u and inverse FFTs of i k_x A,
+//      i k_z A, i k_x^left A, i k_x^right A (wem.c:822-985). The transform is separable
+//      and each factor i k acts on one axis only, so IDFT3(i k_x DFT3(u)) =
+//      IDFT_x(i k_x DFT_x(u)) exactly; along its axis that is a circular convolution, so
+//      the host runtime (wem_api.cu, deriv_gemm) applies each derivative to all lines at
+//      once as one complex GEMM against an L x L matrix built in FP64 (cuBLAS; the axes
+//      have any length: nz is rarely a power of two).
+//   When nmx is a power of two in [32, 2048] steps 1 and the x derivatives run on the
 //   register-resident row FFT of wem_fft.cuh instead (wem_angles_extrap_fft_kernel,
-//   wem_angles_xderiv_fft_kernel); the z transforms stay direct (nz is any length).
+//   wem_angles_xderiv_fft_kernel).
 //   3. wem_angles_accum_kernel: per grid point, in frequency order,
 //      ang += (180/pi) atan(|u_x| / (|u_z| + 1e-10)) and sign += +-|u| / nw, then
 //      ang *= sign(sign) / (ifmax - ifmin + 1) (wem.c:675-676, 735-754).
 // In 2-D the y terms vanish: u_y = 0 gives angy = 0 (the reference's value). 3-D grids
 // (power-of-two nmx, nmy) continue the source with the plane passes of wem_3d.cu (mode 3)
-// and take x, y and z transforms of every depth volume (wem_axis_dft_kernel, any stride);
+// and take the x, y and z derivatives of every depth volume with the same GEMMs;
 // wem_angles_accum3_kernel sums over batches of frequencies.
 #include <cuda_runtime.h>
 #include <math.h>
@@ -231,82 +231,6 @@ __global__ void __launch_bounds__(256) wem_angles_xderiv_fft_kernel(const AngleX
     }
 }
 
-// ------------------------------------------------------------------ 2. one-axis DFTs
-// out[base(l) + k*se] = scale * sum_i mult(i) in[base(l) + i*se] W^{+-ik},
-// base(l) = (l / nb) * sa + (l % nb) * sb. Tile: 32 lines x 64 outputs per CTA of
-// 256 threads, input staged 32 samples at a time; each thread 2 lines x 4 outputs.
-__global__ void __launch_bounds__(256) wem_axis_dft_kernel(const AxisDftArgs a)
-{
-    constexpr int LN = 32, KO = 64, KC = 32;
-    __shared__ float2 s_in[LN][KC + 1];
-    __shared__ float2 s_w[KC][KO];
-    const int tid = threadIdx.x;
-    const long long l0 = (long long)blockIdx.x * LN;
-    const int k0 = blockIdx.y * KO;
-    const int tx = tid & 15, ty = tid >> 4;
-    float2 acc[2][4];
-#pragma unroll
-    for (int i = 0; i < 2; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) acc[i][j] = make_float2(0.f, 0.f);
-    const bool contiguous = a.se == 1;
-    for (int i0 = 0; i0 < a.L; i0 += KC) {
-        __syncthreads();
-        for (int e = tid; e < LN * KC; e += 256) {
-            // contiguous lines: consecutive threads walk one line; strided: across lines
-            const int li = contiguous ? e / KC : e % LN, ii = contiguous ? e % KC : e / LN;
-            const long long l = l0 + li;
-            const int i = i0 + ii;
-            float2 v = make_float2(0.f, 0.f);
-            if (l < a.nlines && i < a.L) {
-                const long long base = (l / a.nb) * a.sa + (l % a.nb) * a.sb;
-                v = a.in[base + (long long)i * a.se];
-                if (a.mode) {  // i k(i) for the derivative of the axis (left / right halves)
-                    float k = axis_k(i, a.L, a.dk);
-                    if (a.mode == 2) k = i <= a.L / 2 ? 0.f : k;
-                    if (a.mode == 3) k = i <= a.L / 2 ? k : 0.f;
-                    v = make_float2(-k * v.y, k * v.x);
-                }
-            }
-            s_in[li][ii] = v;
-        }
-        for (int e = tid; e < KC * KO; e += 256) {
-            const int ii = e / KO, kk = e - ii * KO;
-            const int i = i0 + ii, k = k0 + kk;
-            float2 wv = make_float2(0.f, 0.f);
-            if (i < a.L && k < a.L) {
-                wv = a.tw[(int)(((long long)i * k) % a.L)];
-                if (a.sign > 0) wv.y = -wv.y;
-            }
-            s_w[ii][kk] = wv;
-        }
-        __syncthreads();
-#pragma unroll 4
-        for (int ii = 0; ii < KC; ii++) {
-            const float2 v0 = s_in[ty * 2][ii], v1 = s_in[ty * 2 + 1][ii];
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const float2 wv = s_w[ii][tx * 4 + j];
-                acc[0][j].x = fmaf(v0.x, wv.x, fmaf(-v0.y, wv.y, acc[0][j].x));
-                acc[0][j].y = fmaf(v0.x, wv.y, fmaf(v0.y, wv.x, acc[0][j].y));
-                acc[1][j].x = fmaf(v1.x, wv.x, fmaf(-v1.y, wv.y, acc[1][j].x));
-                acc[1][j].y = fmaf(v1.x, wv.y, fmaf(v1.y, wv.x, acc[1][j].y));
-            }
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 2; i++) {
-        const long long l = l0 + ty * 2 + i;
-        if (l >= a.nlines) continue;
-        const long long base = (l / a.nb) * a.sa + (l % a.nb) * a.sb;
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            const int k = k0 + tx * 4 + j;
-            if (k < a.L) a.out[base + (long long)k * a.se] = make_float2(acc[i][j].x * a.scale, acc[i][j].y * a.scale);
-        }
-    }
-}
-
 // ------------------------------------------------------------------ 3. accumulation
 // One thread per grid point (x, z), frequencies in order; out [nmx][nz].
 __global__ void __launch_bounds__(256) wem_angles_accum_kernel(const AngleAccumArgs a)
@@ -410,14 +334,6 @@ int launch_angles_fft(const AngleArgs &a, const AngleXArgs &x, int which, cudaSt
     case 2048: return launch_fft_paths<2048>(a, x, which, st);
     default: return -2;
     }
-}
-
-int launch_axis_dft(const AxisDftArgs &a, cudaStream_t st)
-{
-    if (a.nlines <= 0 || a.L <= 0) return 0;
-    dim3 grid((unsigned)((a.nlines + 31) / 32), (unsigned)((a.L + 63) / 64));
-    wem_axis_dft_kernel<<<grid, 256, 0, st>>>(a);
-    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_angles_accum(const AngleAccumArgs &a, cudaStream_t st)

@@ -6,6 +6,7 @@
 // runs on the GPU: trace spectra (wem_spectra_kernel), the fused depth recursion
 // (wem_migrate_kernel) and the image reduction (wem_image_reduce_kernel).
 // There is no CPU fallback: without a CUDA device every entry point fails.
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
@@ -88,6 +89,8 @@ struct wem_ctx {
     DevBuf tcw, tcerr;            // split16: W operands of the tensor-core DFT stages, timeout word
     DevBuf wposb;                 // [nz][WPOS_STRIDE] points taking their wavefield whole (paired form)
     DevBuf plan3;                 // [nz][PLAN3_STRIDE] 3-D paired planes (empty: one plane per reference)
+    cublasHandle_t blas = nullptr;  // the incidence angles' derivative GEMMs
+    int blas_compute = -1;          // their cuBLAS compute type once chosen
     DevBuf dsum3;                 // 3-D direct sums: [item][2][WHOLE_MAX][nky] column sums
     bool plan3_ok = false;
     DevBuf selbp;                 // [nz][nmx rounded up to 16] selection rows (precomputed-table path)
@@ -174,6 +177,7 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->blas) cublasDestroy(c->blas);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (int i = 0; i < 4; i++)
@@ -1026,6 +1030,89 @@ extern "C" int wem_migrate(wem_ctx *c, int nshot, const float *sx, const float *
     return collect_times(c);
 }
 
+
+// ------------------------------------------------------------------ derivative GEMMs
+// The angle computation differentiates its volumes along one axis at a time:
+// IDFT(m(k) i k DFT(u)) * scale with m the whole axis (mode 1, scale 1/L) or its left /
+// right half (modes 2, 3, scale 1; wem.c:900-945). Along the axis this is a circular
+// convolution with w(j) = scale sum_k m(k) i k e^{+2 pi i k j / L}, so for all lines at once
+// it is one complex GEMM against the L x L matrix W(i, k') = w((k' - i) mod L) -- L^2
+// multiply-adds per sample instead of the two direct transforms' 2 L^2. k is the float
+// wavenumber of the direct transforms (axis_k); w is summed in double.
+static void deriv_matrix_host(int L, float dk, int mode, float scale, std::vector<float2> &W)
+{
+    std::vector<double> kx(L);
+    for (int k = 0; k < L; k++) {
+        const float kf = k <= L / 2 ? dk * (float)k : -(dk * (float)L - dk * (float)k);
+        const bool on = mode == 1 || (mode == 2 && k > L / 2) || (mode == 3 && k <= L / 2);
+        kx[k] = on ? (double)kf : 0.0;
+    }
+    std::vector<double> wr(L), wi(L);
+    for (int j = 0; j < L; j++) {
+        double re = 0.0, im = 0.0;
+        for (int k = 0; k < L; k++) {
+            if (kx[k] == 0.0) continue;
+            const double ph = 6.283185307179586476925286766559 * (double)(((long long)k * j) % L) / L;
+            // i k e^{i ph} = k (-sin ph + i cos ph)
+            re -= kx[k] * sin(ph);
+            im += kx[k] * cos(ph);
+        }
+        wr[j] = re * scale;
+        wi[j] = im * scale;
+    }
+    W.resize((size_t)L * L);
+    for (int kp = 0; kp < L; kp++)
+        for (int i = 0; i < L; i++) {
+            const int j = ((kp - i) % L + L) % L;
+            W[(size_t)kp * L + i] = make_float2((float)wr[j], (float)wi[j]);  // column-major (i, k')
+        }
+}
+
+// W of deriv_matrix_host into the device buffer b
+static int deriv_matrix(wem_ctx *c, DevBuf &b, int L, float dk, int mode, float scale)
+{
+    std::vector<float2> W;
+    deriv_matrix_host(L, dk, mode, scale, W);
+    int rc;
+    if ((rc = ensure(b, sizeof(float2) * W.size()))) return rc;
+    CK(cudaMemcpyAsync(b.p, W.data(), sizeof(float2) * W.size(), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));  // W is a local
+    return WEM_OK;
+}
+
+// out = derivative of in along an axis of length L (matrix W from deriv_matrix), for `lines`
+// lines per batch entry and `batch` entries `stride` samples apart. axis_slow: sample i of
+// line l at i * ld + l (the lines contiguous); otherwise at l * ld + i (the axis
+// contiguous). The GEMMs run with cuBLAS's FP32 emulation on the tensor cores (BF16x9)
+// where it accepts complex operands, otherwise in FP32.
+static int deriv_gemm(wem_ctx *c, const DevBuf &W, const float2 *in, float2 *out, int L, bool axis_slow,
+                      long long lines, long long ld, int batch, long long stride)
+{
+    if (!c->blas) {
+        if (cublasCreate(&c->blas) != CUBLAS_STATUS_SUCCESS) return fail(WEM_ERR_CUDA, "cublasCreate failed");
+    }
+    if (cublasSetStream(c->blas, c->st) != CUBLAS_STATUS_SUCCESS) return fail(WEM_ERR_CUDA, "cublasSetStream failed");
+    const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
+    auto run = [&](cublasComputeType_t ct) {
+        if (axis_slow)  // C (lines x L) = A (lines x L, ld) * W
+            return cublasGemmStridedBatchedEx(c->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)lines, L, L, &one, in, CUDA_C_32F,
+                                              (int)ld, stride, W.p, CUDA_C_32F, L, 0, &zero, out, CUDA_C_32F,
+                                              (int)ld, stride, batch, ct, CUBLAS_GEMM_DEFAULT);
+        // C (L x lines) = W^T * A (L x lines, ld)
+        return cublasGemmStridedBatchedEx(c->blas, CUBLAS_OP_T, CUBLAS_OP_N, L, (int)lines, L, &one, W.p, CUDA_C_32F,
+                                          L, 0, in, CUDA_C_32F, (int)ld, stride, &zero, out, CUDA_C_32F, (int)ld,
+                                          stride, batch, ct, CUBLAS_GEMM_DEFAULT);
+    };
+    if (c->blas_compute < 0) {
+        c->blas_compute = (int)CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+        if (run(CUBLAS_COMPUTE_32F_EMULATED_16BFX9) == CUBLAS_STATUS_SUCCESS) return WEM_OK;
+        c->blas_compute = (int)CUBLAS_COMPUTE_32F;
+    }
+    if (run((cublasComputeType_t)c->blas_compute) != CUBLAS_STATUS_SUCCESS)
+        return fail(WEM_ERR_CUDA, "derivative GEMM (L=%d) failed", L);
+    return WEM_OK;
+}
+
 // ---------------------------------------------------------------- incidence angles
 // 3-D (nmy > 1), compute_angles with both lateral axes: per shot and batch of frequencies
 // the source is continued down with the plane passes of wem_3d.cu (mode 3, ssop_source's
@@ -1081,7 +1168,7 @@ static int angles3d(wem_ctx *c, const wem_params &p, const float *vel, const flo
         return w;
     };
     const int lop = (nw - 1) * 2;
-    const std::vector<float2> wt = dft_table(lop), wx = dft_table(nmx), wy = dft_table(nmy), wz = dft_table(nz);
+    const std::vector<float2> wt = dft_table(lop);
     const float dkx = 2 * 3.141592653589793 / ((float)nmx) / p.dmx;
     const float dky = 2 * 3.141592653589793 / ((float)nmy) / p.dmy;
     const float dkz = 2 * 3.141592653589793 / ((float)nz) / p.dz;
@@ -1089,15 +1176,16 @@ static int angles3d(wem_ctx *c, const wem_params &p, const float *vel, const flo
     // frequencies per batch: 9 depth volumes each, within half of the free memory
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
-    const size_t per_f = sizeof(float2) * ((size_t)9 * nn + (size_t)6 * n);
+    const size_t per_f = sizeof(float2) * ((size_t)8 * nn + (size_t)6 * n);
     const int batch = (int)std::max<long long>(1, std::min<long long>(nwf, (long long)(free_b / 2 / per_f)));
     const size_t vol = sizeof(float2) * (size_t)batch * nn;
-    DevBuf bpo, bpd, btx, bty, bfx, bfy, bwt, bwx, bwy, bwz, bsc, bsrc, bbase, bwav, bzf, bitems, bcell, bU, bY, bC, bS,
-        bT, bSX, bLX, bRX, bSY, bLY, bRY, bSZ, bsum, bang;
+    DevBuf bpo, bpd, btx, bty, bfx, bfy, bwt, bsc, bsrc, bbase, bwav, bzf, bitems, bcell, bU, bY, bC, bS,
+        bSX, bLX, bRX, bSY, bLY, bRY, bSZ, bsum, bang;
+    DevBuf bDx, bDlx, bDrx, bDy, bDly, bDry, bDz;  // derivative matrices of the three axes
     auto release = [&]() {
-        DevBuf *bs[] = { &bpo, &bpd, &btx, &bty, &bfx, &bfy, &bwt, &bwx, &bwy, &bwz, &bsc, &bsrc, &bbase, &bwav, &bzf,
-                         &bitems, &bcell, &bU, &bY, &bC, &bS, &bT, &bSX, &bLX, &bRX, &bSY, &bLY, &bRY, &bSZ, &bsum,
-                         &bang };
+        DevBuf *bs[] = { &bpo, &bpd, &btx, &bty, &bfx, &bfy, &bwt, &bsc, &bsrc, &bbase, &bwav, &bzf,
+                         &bitems, &bcell, &bU, &bY, &bC, &bS, &bSX, &bLX, &bRX, &bSY, &bLY, &bRY, &bSZ, &bsum,
+                         &bang, &bDx, &bDlx, &bDrx, &bDy, &bDly, &bDry, &bDz };
         for (DevBuf *b : bs)
             if (b->p) cudaFree(b->p);
     };
@@ -1105,16 +1193,19 @@ static int angles3d(wem_ctx *c, const wem_params &p, const float *vel, const flo
     if ((rc = ensure(bpo, sizeof(float) * nz)) || (rc = ensure(bpd, sizeof(float) * nn)) ||
         (rc = ensure(btx, sizeof(float) * nmx)) || (rc = ensure(bty, sizeof(float) * nmy)) ||
         (rc = ensure(bfx, sizeof(float2) * fx.size())) || (rc = ensure(bfy, sizeof(float2) * fy.size())) ||
-        (rc = ensure(bwt, sizeof(float2) * lop)) || (rc = ensure(bwx, sizeof(float2) * nmx)) ||
-        (rc = ensure(bwy, sizeof(float2) * nmy)) || (rc = ensure(bwz, sizeof(float2) * nz)) ||
+        (rc = ensure(bwt, sizeof(float2) * lop)) ||
         (rc = ensure(bsc, sizeof(float) * nwf)) || (rc = ensure(bsrc, sizeof(float2) * nwf)) ||
         (rc = ensure(bbase, sizeof(int64_t))) || (rc = ensure(bwav, sizeof(float) * p.nt)) || (rc = ensure(bzf, nz)) ||
         (rc = ensure(bitems, sizeof(int) * 2 * (size_t)nwf)) || (rc = ensure(bcell, sizeof(int))) ||
         (rc = ensure(bU, sizeof(float2) * (size_t)batch * 2 * n)) || (rc = ensure(bY, sizeof(float2) * (size_t)batch * 2 * n)) ||
-        (rc = ensure(bC, sizeof(float2) * (size_t)batch * 2 * n)) || (rc = ensure(bS, vol)) || (rc = ensure(bT, vol)) ||
+        (rc = ensure(bC, sizeof(float2) * (size_t)batch * 2 * n)) || (rc = ensure(bS, vol)) ||
         (rc = ensure(bSX, vol)) || (rc = ensure(bLX, vol)) || (rc = ensure(bRX, vol)) || (rc = ensure(bSY, vol)) ||
         (rc = ensure(bLY, vol)) || (rc = ensure(bRY, vol)) || (rc = ensure(bSZ, vol)) ||
-        (rc = ensure(bsum, sizeof(float) * 4 * nn)) || (rc = ensure(bang, sizeof(float) * 2 * nn))) {
+        (rc = ensure(bsum, sizeof(float) * 4 * nn)) || (rc = ensure(bang, sizeof(float) * 2 * nn)) ||
+        (rc = deriv_matrix(c, bDx, nmx, dkx, 1, 1.f / (float)nmx)) || (rc = deriv_matrix(c, bDlx, nmx, dkx, 2, 1.f)) ||
+        (rc = deriv_matrix(c, bDrx, nmx, dkx, 3, 1.f)) || (rc = deriv_matrix(c, bDy, nmy, dky, 1, 1.f / (float)nmy)) ||
+        (rc = deriv_matrix(c, bDly, nmy, dky, 2, 1.f)) || (rc = deriv_matrix(c, bDry, nmy, dky, 3, 1.f)) ||
+        (rc = deriv_matrix(c, bDz, nz, dkz, 1, 1.f / (float)nz))) {
         release();
         return rc;
     }
@@ -1143,9 +1234,6 @@ static int angles3d(wem_ctx *c, const wem_params &p, const float *vel, const flo
     CKR(cudaMemcpyAsync(bfx.p, fx.data(), sizeof(float2) * fx.size(), cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bfy.p, fy.data(), sizeof(float2) * fy.size(), cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bwt.p, wt.data(), sizeof(float2) * lop, cudaMemcpyHostToDevice, st));
-    CKR(cudaMemcpyAsync(bwx.p, wx.data(), sizeof(float2) * nmx, cudaMemcpyHostToDevice, st));
-    CKR(cudaMemcpyAsync(bwy.p, wy.data(), sizeof(float2) * nmy, cudaMemcpyHostToDevice, st));
-    CKR(cudaMemcpyAsync(bwz.p, wz.data(), sizeof(float2) * nz, cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bsc.p, sc.data(), sizeof(float) * nwf, cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bbase.p, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bwav.p, wav, sizeof(float) * p.nt, cudaMemcpyHostToDevice, st));
@@ -1187,31 +1275,19 @@ static int angles3d(wem_ctx *c, const wem_params &p, const float *vel, const flo
                 LCHK(m3d_launch_step(nmx, nmy, 0, 0, a, c->nsm, st), "3-D source step");
             }
             kernels += 1 + 3 * nz;
-            // one-axis transforms of the depth volumes [f][z][x][y]
+            // derivatives of the depth volumes [f][z][x][y] (wem.c:900-992): x lines (nmy of them,
+            // contiguous) with x nmy apart, y contiguous, z lines of n samples nz of them n apart
             const long long nbl = nb;
-            AxisDftArgs ax{};  // x lines: stride nmy
-            ax.nlines = nbl * nz * nmy; ax.nb = nmy; ax.sa = n; ax.sb = 1; ax.se = nmy; ax.L = nmx; ax.dk = dkx;
-            ax.tw = P<float2>(bwx);
-            AxisDftArgs ay{};  // y lines: contiguous
-            ay.nlines = nbl * nz * nmx; ay.nb = 1; ay.sa = nmy; ay.sb = 0; ay.se = 1; ay.L = nmy; ay.dk = dky;
-            ay.tw = P<float2>(bwy);
-            AxisDftArgs az{};  // z lines: stride n
-            az.nlines = nbl * n; az.nb = n; az.sa = (long long)nz * n; az.sb = 1; az.se = n; az.L = nz; az.dk = dkz;
-            az.tw = P<float2>(bwz);
-            struct Step { AxisDftArgs base; const DevBuf *in; DevBuf *out; int sign, mode; float scale; };
-            const Step steps[] = {
-                { ax, &bS, &bT, -1, 0, 1.f }, { ax, &bT, &bSX, +1, 1, 1.f / (float)nmx },
-                { ax, &bT, &bLX, +1, 2, 1.f }, { ax, &bT, &bRX, +1, 3, 1.f },
-                { ay, &bS, &bT, -1, 0, 1.f }, { ay, &bT, &bSY, +1, 1, 1.f / (float)nmy },
-                { ay, &bT, &bLY, +1, 2, 1.f }, { ay, &bT, &bRY, +1, 3, 1.f },
-                { az, &bS, &bT, -1, 0, 1.f }, { az, &bT, &bSZ, +1, 1, 1.f / (float)nz },
-            };
-            for (const Step &sp : steps) {
-                AxisDftArgs d = sp.base;
-                d.in = reinterpret_cast<const float2 *>(sp.in->p);
-                d.out = reinterpret_cast<float2 *>(sp.out->p);
-                d.sign = sp.sign; d.mode = sp.mode; d.scale = sp.scale;
-                LCHK(launch_axis_dft(d, st), "axis transform");
+            const float2 *vs = P<float2>(bS);
+            if ((rc = deriv_gemm(c, bDx, vs, P<float2>(bSX), nmx, true, nmy, nmy, (int)(nbl * nz), n)) ||
+                (rc = deriv_gemm(c, bDlx, vs, P<float2>(bLX), nmx, true, nmy, nmy, (int)(nbl * nz), n)) ||
+                (rc = deriv_gemm(c, bDrx, vs, P<float2>(bRX), nmx, true, nmy, nmy, (int)(nbl * nz), n)) ||
+                (rc = deriv_gemm(c, bDy, vs, P<float2>(bSY), nmy, false, nbl * nz * nmx, nmy, 1, 0)) ||
+                (rc = deriv_gemm(c, bDly, vs, P<float2>(bLY), nmy, false, nbl * nz * nmx, nmy, 1, 0)) ||
+                (rc = deriv_gemm(c, bDry, vs, P<float2>(bRY), nmy, false, nbl * nz * nmx, nmy, 1, 0)) ||
+                (rc = deriv_gemm(c, bDz, vs, P<float2>(bSZ), nz, true, n, n, nb, (long long)nz * n))) {
+                release();
+                return rc;
             }
             AngleAccum3Args ac{};
             ac.n = n; ac.nz = nz; ac.nwf = nb; ac.nw = nw; ac.nfreq_div = ifmax - ifmin + 1;
@@ -1220,7 +1296,7 @@ static int angles3d(wem_ctx *c, const wem_params &p, const float *vel, const flo
             ac.lx = P<float2>(bLX); ac.rx = P<float2>(bRX); ac.ly = P<float2>(bLY); ac.ry = P<float2>(bRY);
             ac.sum = P<float>(bsum); ac.angx = P<float>(bang); ac.angy = P<float>(bang) + nn;
             LCHK(launch_angles_accum3(ac, st), "accumulation");
-            kernels += 11;
+            kernels += 1;  // and the cuBLAS GEMMs of the derivatives
         }
         CKR(cudaMemcpyAsync(angx + (size_t)s * nn, bang.p, sizeof(float) * nn, cudaMemcpyDeviceToHost, st));
         if (angy) CKR(cudaMemcpyAsync(angy + (size_t)s * nn, P<float>(bang) + nn, sizeof(float) * nn, cudaMemcpyDeviceToHost, st));
@@ -1278,7 +1354,7 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     const float dkz = 2 * 3.141592653589793 / ((float)nz) / p.dz;
     // source spectrum: f_op of the wavelet on (nw - 1) * 2 samples, / sqrtf(ntfft)
     const int lop = (nw - 1) * 2;
-    std::vector<float2> wt(lop), twx(nmx), twz(nz);
+    std::vector<float2> wt(lop), twx(nmx);
     for (int k = 0; k < lop; k++) {
         const double a = -6.283185307179586476925286766559 * k / lop;
         wt[k] = make_float2((float)cos(a), (float)sin(a));
@@ -1287,10 +1363,6 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
         const double a = -6.283185307179586476925286766559 * k / nmx;
         twx[k] = make_float2((float)cos(a), (float)sin(a));
     }
-    for (int k = 0; k < nz; k++) {
-        const double a = -6.283185307179586476925286766559 * k / nz;
-        twz[k] = make_float2((float)cos(a), (float)sin(a));
-    }
     std::vector<float> sc(nwf, 1.f / sqrtf((float)ntfft));
     // power-of-two widths: the row FFT's per-pass twiddles instead of the direct table
     const bool fftx = angles_fft_supported(nmx);
@@ -1298,18 +1370,19 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     if (fftx) twiddle_table_host(nmx, twf.data());
     const int64_t zero = 0;
     const size_t plane = sizeof(float2) * (size_t)nwf * n;
-    DevBuf bwt, btwx, btwz, bsc, bsrc, bbase, bU, bT, bX, bL, bR, bZ, bang, bpo, bpd, btap, bwav, btwf;
+    DevBuf bwt, btwx, bsc, bsrc, bbase, bU, bX, bL, bR, bZ, bang, bpo, bpd, btap, bwav, btwf;
+    DevBuf bDz, bDx, bDl, bDr;  // derivative matrices (z; x, left, right where x has no row FFT)
     auto release = [&]() {
-        DevBuf *bs[] = { &bwt, &btwx, &btwz, &bsc, &bsrc, &bbase, &bU, &bT, &bX, &bL, &bR, &bZ, &bang,
-                         &bpo, &bpd, &btap, &bwav, &btwf };
+        DevBuf *bs[] = { &bwt, &btwx, &bsc, &bsrc, &bbase, &bU, &bX, &bL, &bR, &bZ, &bang,
+                         &bpo, &bpd, &btap, &bwav, &btwf, &bDz, &bDx, &bDl, &bDr };
         for (DevBuf *b : bs)
             if (b->p) cudaFree(b->p);
     };
     int rc;
     if ((rc = ensure(bwt, sizeof(float2) * lop)) || (rc = ensure(btwx, sizeof(float2) * nmx)) ||
-        (rc = ensure(btwz, sizeof(float2) * nz)) || (rc = ensure(bsc, sizeof(float) * nwf)) ||
+        (rc = ensure(bsc, sizeof(float) * nwf)) ||
         (rc = ensure(bsrc, sizeof(float2) * nwf)) || (rc = ensure(bbase, sizeof(int64_t))) || (rc = ensure(bU, plane)) ||
-        (rc = ensure(bT, plane)) || (rc = ensure(bX, plane)) || (rc = ensure(bL, plane)) || (rc = ensure(bR, plane)) ||
+        (rc = ensure(bX, plane)) || (rc = ensure(bL, plane)) || (rc = ensure(bR, plane)) ||
         (rc = ensure(bZ, plane)) || (rc = ensure(bang, sizeof(float) * 2 * n)) ||
         (rc = ensure(bpo, sizeof(float) * nz)) || (rc = ensure(bpd, sizeof(float) * n)) ||
         (rc = ensure(btap, sizeof(float) * nmx)) || (rc = ensure(bwav, sizeof(float) * p.nt)) ||
@@ -1327,7 +1400,6 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     } while (0)
     CKR(cudaMemcpyAsync(bwt.p, wt.data(), sizeof(float2) * lop, cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(btwx.p, twx.data(), sizeof(float2) * nmx, cudaMemcpyHostToDevice, st));
-    CKR(cudaMemcpyAsync(btwz.p, twz.data(), sizeof(float2) * nz, cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bsc.p, sc.data(), sizeof(float) * nwf, cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bbase.p, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bpo.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
@@ -1335,6 +1407,12 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     CKR(cudaMemcpyAsync(btap.p, taper.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bwav.p, wav, sizeof(float) * p.nt, cudaMemcpyHostToDevice, st));
     if (fftx) CKR(cudaMemcpyAsync(btwf.p, twf.data(), sizeof(float2) * twf.size(), cudaMemcpyHostToDevice, st));
+    if ((rc = deriv_matrix(c, bDz, nz, dkz, 1, 1.f / (float)nz)) ||
+        (!fftx && ((rc = deriv_matrix(c, bDx, nmx, dkx, 1, 1.f / (float)nmx)) ||
+                   (rc = deriv_matrix(c, bDl, nmx, dkx, 2, 1.f)) || (rc = deriv_matrix(c, bDr, nmx, dkx, 3, 1.f))))) {
+        release();
+        return rc;
+    }
     SpectraArgs sa{};
     sa.d = P<float>(bwav);
     sa.ntr = 1;
@@ -1379,36 +1457,26 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
             release();
             return fail(WEM_ERR_CUDA, "angles: extrapolation launch: %s", cudaGetErrorString(cudaGetLastError()));
         }
-        // one-axis transforms: x lines are contiguous, z lines are nmx apart
-        AxisDftArgs xa{};
-        xa.nlines = (long long)nwf * nz; xa.nb = 1; xa.sa = nmx; xa.sb = 0; xa.se = 1; xa.L = nmx;
-        xa.dk = dkx; xa.tw = P<float2>(btwx);
-        AxisDftArgs za{};
-        za.nlines = (long long)nwf * nmx; za.nb = nmx; za.sa = (long long)nz * nmx; za.sb = 1; za.se = nmx; za.L = nz;
-        za.dk = dkz; za.tw = P<float2>(btwz);
-        struct Step { AxisDftArgs base; const DevBuf *in; DevBuf *out; int sign, mode; float scale; };
-        const Step steps[] = {
-            { xa, &bU, &bT, -1, 0, 1.f },                    // DFT_x(u)
-            { xa, &bT, &bX, +1, 1, 1.f / (float)nmx },       // u_x = IDFT_x(i kx .) / nkx
-            { xa, &bT, &bL, +1, 2, 1.f },                    // u_left  (wem.c:932-945)
-            { xa, &bT, &bR, +1, 3, 1.f },                    // u_right
-            { za, &bU, &bT, -1, 0, 1.f },                    // DFT_z(u)
-            { za, &bT, &bZ, +1, 1, 1.f / (float)nz },        // u_z = IDFT_z(i kz .) / nkz
-        };
-        if (fftx && launch_angles_fft(a, xf, 1, st)) {
-            release();
-            return fail(WEM_ERR_CUDA, "angles: x-derivative launch: %s", cudaGetErrorString(cudaGetLastError()));
-        }
-        for (const Step &sp : steps) {
-            if (fftx && sp.base.se == 1) continue;  // the x transforms ran on the row FFT
-            AxisDftArgs d = sp.base;
-            d.in = reinterpret_cast<const float2 *>(sp.in->p);
-            d.out = reinterpret_cast<float2 *>(sp.out->p);
-            d.sign = sp.sign; d.mode = sp.mode; d.scale = sp.scale;
-            if (launch_axis_dft(d, st)) {
+        // derivatives: u_x, u_left, u_right (wem.c:900-945) along x -- the row FFT for
+        // power-of-two widths, else GEMMs against the derivative matrices (x contiguous) --
+        // and u_z along z (lines of nmx contiguous samples, nz of them nmx apart)
+        if (fftx) {
+            if (launch_angles_fft(a, xf, 1, st)) {
                 release();
-                return fail(WEM_ERR_CUDA, "angles: axis transform launch: %s", cudaGetErrorString(cudaGetLastError()));
+                return fail(WEM_ERR_CUDA, "angles: x-derivative launch: %s", cudaGetErrorString(cudaGetLastError()));
             }
+        } else {
+            const long long xl = (long long)nwf * nz;
+            if ((rc = deriv_gemm(c, bDx, P<float2>(bU), P<float2>(bX), nmx, false, xl, nmx, 1, 0)) ||
+                (rc = deriv_gemm(c, bDl, P<float2>(bU), P<float2>(bL), nmx, false, xl, nmx, 1, 0)) ||
+                (rc = deriv_gemm(c, bDr, P<float2>(bU), P<float2>(bR), nmx, false, xl, nmx, 1, 0))) {
+                release();
+                return rc;
+            }
+        }
+        if ((rc = deriv_gemm(c, bDz, P<float2>(bU), P<float2>(bZ), nz, true, nmx, nmx, nwf, (long long)nz * nmx))) {
+            release();
+            return rc;
         }
         AngleAccumArgs ac{};
         ac.nmx = nmx; ac.nz = nz; ac.nwf = nwf; ac.nw = nw; ac.nfreq_div = ifmax - ifmin + 1;
@@ -1418,7 +1486,7 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
             release();
             return fail(WEM_ERR_CUDA, "angles: accumulation launch: %s", cudaGetErrorString(cudaGetLastError()));
         }
-        kernels += 8;
+        kernels += fftx ? 3 : 2;  // and the cuBLAS GEMMs of the derivatives
         CKR(cudaMemcpyAsync(angx + (size_t)s * n, bang.p, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
         if (angy)
             CKR(cudaMemcpyAsync(angy + (size_t)s * n, P<float>(bang) + n, sizeof(float) * n, cudaMemcpyDeviceToHost, st));

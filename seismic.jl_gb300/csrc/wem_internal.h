@@ -139,14 +139,6 @@ struct AngleArgs {
     const float2 *twx;     // [nmx] e^{-2 pi i k / nmx}
     float2 *u;             // [nwf][nz][nmx] source wavefield
 };
-struct AxisDftArgs {
-    const float2 *in;
-    float2 *out;
-    long long nlines, nb, sa, sb, se;  // line l starts at (l / nb) * sa + (l % nb) * sb, elements se apart
-    int L, sign, mode;                 // mode: 0 none, 1 i k, 2 i k (upper half), 3 i k (lower half)
-    float dk, scale;
-    const float2 *tw;                  // [L] e^{-2 pi i m / L}
-};
 struct AngleAccumArgs {
     int nmx, nz, nwf, nw, nfreq_div;
     const float2 *u, *ux, *uz, *ul, *ur;  // [nwf][nz][nmx]
@@ -171,7 +163,6 @@ int launch_angles_extrap(const AngleArgs &a, cudaStream_t st);
 // power-of-two nmx in [32, 2048]: which = 0 extrapolation, 1 x derivatives on the row FFT
 bool angles_fft_supported(int nmx);
 int launch_angles_fft(const AngleArgs &a, const AngleXArgs &x, int which, cudaStream_t st);
-int launch_axis_dft(const AxisDftArgs &a, cudaStream_t st);
 int launch_angles_accum(const AngleAccumArgs &a, cudaStream_t st);
 
 // Forms of the 2-D depth kernel: FP32; split16 (tensor-core DFT stages, nkx = 2048 only);
