@@ -54,16 +54,17 @@ __global__ void __launch_bounds__(512) wem_angles_extrap_kernel(const AngleArgs 
     float2 *d = sh, *x = sh + nmx;
     const float2 *tw = sh + 2 * nmx;
     float2 *tws = sh + 2 * nmx;
-    const int f = blockIdx.x;
+    const int f = blockIdx.x, shot = blockIdx.y;  // one (frequency, shot of the batch) per CTA
+    const int igx = a.igxs ? a.igxs[shot] : a.igx;
     const float w = __fmul_rn((float)(a.ifmin + f), a.dw);  // w = iw*dw
     const float dzs = -a.dz;                                 // extrapolate_source passes -dz
     for (int i = tid; i < nmx; i += nth) {
         tws[i] = a.twx[i];
-        d[i] = i == a.igx ? a.srcw[f] : make_float2(0.f, 0.f);
+        d[i] = i == igx ? a.srcw[f] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     for (int iz = 0; iz < a.nz; iz++) {
-        float2 *urow = a.u + ((size_t)f * a.nz + iz) * nmx;
+        float2 *urow = a.u + (((size_t)shot * a.nwf + f) * a.nz + iz) * nmx;
         const float z = __fadd_rn(a.oz, __fmul_rn(a.dz, (float)iz));
         if (!(z >= a.sz)) {  // CTA-uniform: nothing above the source
             for (int i = tid; i < nmx; i += nth) urow[i] = make_float2(0.f, 0.f);
@@ -138,14 +139,15 @@ __global__ void __launch_bounds__(N / 16 < 32 ? 32 : N / 16) wem_angles_extrap_f
     const unsigned sync = team_sync_handle<N>(t);
     for (int i = t; i < TW; i += T) s_tw[i] = a.twx[i];
     team_sync<T>(sync);
-    const int f = blockIdx.x;
+    const int f = blockIdx.x, shot = blockIdx.y;  // one (frequency, shot of the batch) per CTA
+    const int igx = a.igxs ? a.igxs[shot] : a.igx;
     const float w = __fmul_rn((float)(a.ifmin + f), a.dw);
     const float dzs = -a.dz;
     float2 v[16];
 #pragma unroll
-    for (int m = 0; m < 16; m++) v[m] = (t + T * m) == a.igx ? a.srcw[f] : make_float2(0.f, 0.f);
+    for (int m = 0; m < 16; m++) v[m] = (t + T * m) == igx ? a.srcw[f] : make_float2(0.f, 0.f);
     for (int iz = 0; iz < a.nz; iz++) {
-        float2 *urow = a.u + ((size_t)f * a.nz + iz) * N;
+        float2 *urow = a.u + (((size_t)shot * a.nwf + f) * a.nz + iz) * N;
         const float z = __fadd_rn(a.oz, __fmul_rn(a.dz, (float)iz));
         if (!(z >= a.sz)) {
 #pragma unroll
@@ -296,7 +298,7 @@ int launch_angles_extrap(const AngleArgs &a, cudaStream_t st)
     if (cudaFuncSetAttribute(wem_angles_extrap_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
         return -1;
-    wem_angles_extrap_kernel<<<a.nwf, 512, smem, st>>>(a);
+    wem_angles_extrap_kernel<<<dim3(a.nwf, a.nshot > 0 ? a.nshot : 1), 512, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -305,7 +307,7 @@ template <int N> static int launch_fft_paths(const AngleArgs &a, const AngleXArg
     constexpr int T = N / 16, TEAMS = 256 / T < 1 ? 1 : 256 / T;
     constexpr int TWP = (fft_tw_size<N>() + 1) & ~1;
     if (which == 0) {
-        wem_angles_extrap_fft_kernel<N><<<a.nwf, T < 32 ? 32 : T, 0, st>>>(a);
+        wem_angles_extrap_fft_kernel<N><<<dim3(a.nwf, a.nshot > 0 ? a.nshot : 1), T < 32 ? 32 : T, 0, st>>>(a);
     } else {
         const size_t smem = sizeof(float2) * ((size_t)TWP + (size_t)TEAMS * pad16(N));
         if (cudaFuncSetAttribute(wem_angles_xderiv_fft_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,

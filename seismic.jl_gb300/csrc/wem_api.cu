@@ -1369,12 +1369,18 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     std::vector<float2> twf(fftx ? twiddle_table_size(nmx) : 0);
     if (fftx) twiddle_table_host(nmx, twf.data());
     const int64_t zero = 0;
-    const size_t plane = sizeof(float2) * (size_t)nwf * n;
+    // shots per batch: all their source volumes and derivatives (5 each) within half the free memory
+    size_t free_b = 0, total_b = 0;
+    CK(cudaMemGetInfo(&free_b, &total_b));
+    const size_t per_shot = sizeof(float2) * (size_t)5 * nwf * n + sizeof(float) * 2 * n;
+    const int nbatch = (int)std::max<long long>(1, std::min<long long>(nshot, (long long)(free_b / 2 / per_shot)));
+    const size_t plane = sizeof(float2) * (size_t)nbatch * nwf * n;
     DevBuf bwt, btwx, bsc, bsrc, bbase, bU, bX, bL, bR, bZ, bang, bpo, bpd, btap, bwav, btwf;
     DevBuf bDz, bDx, bDl, bDr;  // derivative matrices (z; x, left, right where x has no row FFT)
+    DevBuf bigx;                // the batch's source cells
     auto release = [&]() {
         DevBuf *bs[] = { &bwt, &btwx, &bsc, &bsrc, &bbase, &bU, &bX, &bL, &bR, &bZ, &bang,
-                         &bpo, &bpd, &btap, &bwav, &btwf, &bDz, &bDx, &bDl, &bDr };
+                         &bpo, &bpd, &btap, &bwav, &btwf, &bDz, &bDx, &bDl, &bDr, &bigx };
         for (DevBuf *b : bs)
             if (b->p) cudaFree(b->p);
     };
@@ -1383,7 +1389,8 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
         (rc = ensure(bsc, sizeof(float) * nwf)) ||
         (rc = ensure(bsrc, sizeof(float2) * nwf)) || (rc = ensure(bbase, sizeof(int64_t))) || (rc = ensure(bU, plane)) ||
         (rc = ensure(bX, plane)) || (rc = ensure(bL, plane)) || (rc = ensure(bR, plane)) ||
-        (rc = ensure(bZ, plane)) || (rc = ensure(bang, sizeof(float) * 2 * n)) ||
+        (rc = ensure(bZ, plane)) || (rc = ensure(bang, sizeof(float) * 2 * n * nbatch)) ||
+        (rc = ensure(bigx, sizeof(int) * nbatch)) ||
         (rc = ensure(bpo, sizeof(float) * nz)) || (rc = ensure(bpd, sizeof(float) * n)) ||
         (rc = ensure(btap, sizeof(float) * nmx)) || (rc = ensure(bwav, sizeof(float) * p.nt)) ||
         (rc = ensure(btwf, sizeof(float2) * (twf.size() + 1)))) {
@@ -1431,20 +1438,25 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     }
     int kernels = 1;
     CK(cudaEventRecord(c->ev0, st));
+    std::vector<int> igxs(nshot);
     for (int s = 0; s < nshot; s++) {
-        const float xs = sx[s];
-        const int igx = (int)((float)(int)(xs - p.omx) / p.dmx);  // (int) (sx - omx)/dmx, wem.c:654
-        if (igx < 0 || igx >= nmx) {
+        igxs[s] = (int)((float)(int)(sx[s] - p.omx) / p.dmx);  // (int) (sx - omx)/dmx, wem.c:654
+        if (igxs[s] < 0 || igxs[s] >= nmx) {
             release();
-            return fail(WEM_ERR_ARG, "wem_angles: shot %d at sx=%g is outside the grid", s, (double)xs);
+            return fail(WEM_ERR_ARG, "wem_angles: shot %d at sx=%g is outside the grid", s, (double)sx[s]);
         }
+    }
+    const size_t vol = (size_t)nwf * n;  // one shot's volume, samples
+    for (int s0 = 0; s0 < nshot; s0 += nbatch) {
+        const int nb = std::min(nbatch, nshot - s0);
+        CKR(cudaMemcpyAsync(bigx.p, igxs.data() + s0, sizeof(int) * nb, cudaMemcpyHostToDevice, st));
         AngleArgs a{};
-        a.nmx = nmx; a.nz = nz; a.nwf = nwf; a.ifmin = ifmin; a.igx = igx;
+        a.nmx = nmx; a.nz = nz; a.nwf = nwf; a.ifmin = ifmin; a.igx = 0; a.nshot = nb; a.igxs = P<int>(bigx);
         a.dw = dw; a.dz = p.dz; a.oz = p.oz; a.sz = p.sz; a.dkx = dkx; a.inv_sqrt_n = 1.f / sqrtf((float)nmx);
         a.po = P<float>(bpo); a.pd = P<float>(bpd); a.taper = P<float>(btap); a.srcw = P<float2>(bsrc);
         a.twx = P<float2>(btwx); a.u = P<float2>(bU);
         AngleXArgs xf{};
-        xf.nlines = (long long)nwf * nz; xf.dkx = dkx; xf.twx = P<float2>(btwf); xf.u = P<float2>(bU);
+        xf.nlines = (long long)nb * nwf * nz; xf.dkx = dkx; xf.twx = P<float2>(btwf); xf.u = P<float2>(bU);
         xf.ux = P<float2>(bX); xf.ul = P<float2>(bL); xf.ur = P<float2>(bR);
         if (fftx) {
             AngleArgs af = a;
@@ -1457,16 +1469,16 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
             release();
             return fail(WEM_ERR_CUDA, "angles: extrapolation launch: %s", cudaGetErrorString(cudaGetLastError()));
         }
-        // derivatives: u_x, u_left, u_right (wem.c:900-945) along x -- the row FFT for
-        // power-of-two widths, else GEMMs against the derivative matrices (x contiguous) --
-        // and u_z along z (lines of nmx contiguous samples, nz of them nmx apart)
+        // derivatives of all the batch's volumes: u_x, u_left, u_right (wem.c:900-945) along x --
+        // the row FFT for power-of-two widths, else GEMMs against the derivative matrices (x
+        // contiguous) -- and u_z along z (lines of nmx contiguous samples, nz of them nmx apart)
         if (fftx) {
             if (launch_angles_fft(a, xf, 1, st)) {
                 release();
                 return fail(WEM_ERR_CUDA, "angles: x-derivative launch: %s", cudaGetErrorString(cudaGetLastError()));
             }
         } else {
-            const long long xl = (long long)nwf * nz;
+            const long long xl = (long long)nb * nwf * nz;
             if ((rc = deriv_gemm(c, bDx, P<float2>(bU), P<float2>(bX), nmx, false, xl, nmx, 1, 0)) ||
                 (rc = deriv_gemm(c, bDl, P<float2>(bU), P<float2>(bL), nmx, false, xl, nmx, 1, 0)) ||
                 (rc = deriv_gemm(c, bDr, P<float2>(bU), P<float2>(bR), nmx, false, xl, nmx, 1, 0))) {
@@ -1474,23 +1486,31 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
                 return rc;
             }
         }
-        if ((rc = deriv_gemm(c, bDz, P<float2>(bU), P<float2>(bZ), nz, true, nmx, nmx, nwf, (long long)nz * nmx))) {
+        if ((rc = deriv_gemm(c, bDz, P<float2>(bU), P<float2>(bZ), nz, true, nmx, nmx, nb * nwf, (long long)nz * nmx))) {
             release();
             return rc;
         }
-        AngleAccumArgs ac{};
-        ac.nmx = nmx; ac.nz = nz; ac.nwf = nwf; ac.nw = nw; ac.nfreq_div = ifmax - ifmin + 1;
-        ac.u = P<float2>(bU); ac.ux = P<float2>(bX); ac.uz = P<float2>(bZ); ac.ul = P<float2>(bL); ac.ur = P<float2>(bR);
-        ac.angx = P<float>(bang); ac.angy = P<float>(bang) + n;
-        if (launch_angles_accum(ac, st)) {
-            release();
-            return fail(WEM_ERR_CUDA, "angles: accumulation launch: %s", cudaGetErrorString(cudaGetLastError()));
+        for (int j = 0; j < nb; j++) {
+            AngleAccumArgs ac{};
+            ac.nmx = nmx; ac.nz = nz; ac.nwf = nwf; ac.nw = nw; ac.nfreq_div = ifmax - ifmin + 1;
+            ac.u = P<float2>(bU) + j * vol; ac.ux = P<float2>(bX) + j * vol; ac.uz = P<float2>(bZ) + j * vol;
+            ac.ul = P<float2>(bL) + j * vol; ac.ur = P<float2>(bR) + j * vol;
+            ac.angx = P<float>(bang) + (size_t)j * 2 * n; ac.angy = P<float>(bang) + (size_t)j * 2 * n + n;
+            if (launch_angles_accum(ac, st)) {
+                release();
+                return fail(WEM_ERR_CUDA, "angles: accumulation launch: %s", cudaGetErrorString(cudaGetLastError()));
+            }
         }
-        kernels += fftx ? 3 : 2;  // and the cuBLAS GEMMs of the derivatives
-        CKR(cudaMemcpyAsync(angx + (size_t)s * n, bang.p, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
-        if (angy)
-            CKR(cudaMemcpyAsync(angy + (size_t)s * n, P<float>(bang) + n, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
-        CKR(cudaStreamSynchronize(st));  // bang is reused by the next shot
+        kernels += (fftx ? 2 : 1) + nb;  // and the cuBLAS GEMMs of the derivatives
+        for (int j = 0; j < nb; j++) {
+            const int s = s0 + j;
+            CKR(cudaMemcpyAsync(angx + (size_t)s * n, P<float>(bang) + (size_t)j * 2 * n, sizeof(float) * n,
+                                cudaMemcpyDeviceToHost, st));
+            if (angy)
+                CKR(cudaMemcpyAsync(angy + (size_t)s * n, P<float>(bang) + (size_t)j * 2 * n + n, sizeof(float) * n,
+                                    cudaMemcpyDeviceToHost, st));
+        }
+        CKR(cudaStreamSynchronize(st));  // bang is reused by the next batch
     }
     CKR(cudaEventRecord(c->ev1, st));
     CKR(cudaStreamSynchronize(st));

@@ -131,13 +131,15 @@ int m3d_launch_collect(const Mig3dArgs &a, float2 *dg, float scale, cudaStream_t
 // source-side incidence angles (wem_angles.cu), 2-D
 struct AngleArgs {
     int nmx, nz, nwf, ifmin, igx;
+    int nshot;             // shots of the batch (blockIdx.y); igxs[s] their source cells (nullptr: igx)
+    const int *igxs;
     float dw, dz, oz, sz, dkx, inv_sqrt_n;  // inv_sqrt_n = 1/sqrtf(nkx)
     const float *po;       // [nz] mean slowness
     const float *pd;       // [nz][nmx] slowness perturbation
     const float *taper;    // [nmx] boundary_condition weights
     const float2 *srcw;    // [nwf] source spectrum / sqrt(ntfft) over the band
     const float2 *twx;     // [nmx] e^{-2 pi i k / nmx}
-    float2 *u;             // [nwf][nz][nmx] source wavefield
+    float2 *u;             // [shot][nwf][nz][nmx] source wavefield
 };
 struct AngleAccumArgs {
     int nmx, nz, nwf, nw, nfreq_div;
