@@ -244,7 +244,8 @@ __global__ void __launch_bounds__(256) wem_angles_accum_kernel(const AngleAccumA
     float ang = 0.f, sgn = 0.f;
     for (int f = 0; f < a.nwf; f++) {
         const size_t q = (size_t)f * plane + off;
-        const float2 u = a.u[q], sx = a.ux[q], sz = a.uz[q], ul = a.ul[q], ur = a.ur[q];
+        const float2 u = a.u[q], sx = a.ux[q], ul = a.ul[q], ur = a.ur[q];
+        const float2 sz = a.uzp ? make_float2(a.uzp[q + (size_t)f * plane], a.uzp[q + (size_t)f * plane + plane]) : a.uz[q];
         const float au = hypotf(u.x, u.y);
         const float ratio = hypotf(sx.x, sx.y) / (hypotf(sz.x, sz.y) + 1e-10f);
         ang += (float)(57.295779513082323 * (double)atanf(ratio));  // (180/PI)*atanf(...) in double
@@ -336,6 +337,26 @@ int launch_angles_fft(const AngleArgs &a, const AngleXArgs &x, int which, cudaSt
     case 2048: return launch_fft_paths<2048>(a, x, which, st);
     default: return -2;
     }
+}
+
+// interleaved complex -> planar per entry (the layout of the real block GEMMs)
+__global__ void __launch_bounds__(256) wem_planar_kernel(const float2 *in, float *out, long long entry, long long total)
+{
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long b = e / entry, s = e - b * entry;
+        const float2 v = in[e];
+        out[2 * b * entry + s] = v.x;
+        out[2 * b * entry + entry + s] = v.y;
+    }
+}
+
+int launch_planar(const float2 *in, float *out, long long entry, long long nentries, cudaStream_t st)
+{
+    const long long total = entry * nentries;
+    long long blocks = (total + 255) / 256;
+    if (blocks > 152LL * 64) blocks = 152LL * 64;
+    wem_planar_kernel<<<(unsigned)blocks, 256, 0, st>>>(in, out, entry, total);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_angles_accum(const AngleAccumArgs &a, cudaStream_t st)

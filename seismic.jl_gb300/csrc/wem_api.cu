@@ -90,7 +90,8 @@ struct wem_ctx {
     DevBuf wposb;                 // [nz][WPOS_STRIDE] points taking their wavefield whole (paired form)
     DevBuf plan3;                 // [nz][PLAN3_STRIDE] 3-D paired planes (empty: one plane per reference)
     cublasHandle_t blas = nullptr;  // the incidence angles' derivative GEMMs
-    int blas_compute = -1;          // their cuBLAS compute type once chosen
+    int blas_compute = -1;          // their cuBLAS compute type once chosen (complex operands)
+    int blas_real_compute = -1;     // the same for the planar (real) form
     DevBuf dsum3;                 // 3-D direct sums: [item][2][WHOLE_MAX][nky] column sums
     bool plan3_ok = false;
     DevBuf selbp;                 // [nz][nmx rounded up to 16] selection rows (precomputed-table path)
@@ -1080,6 +1081,55 @@ static int deriv_matrix(wem_ctx *c, DevBuf &b, int L, float dk, int mode, float 
     return WEM_OK;
 }
 
+// The same derivative as a real GEMM on planar data: [C_re C_im] = [A_re A_im] Wb with
+// Wb = [[W_re, W_im], [-W_im, W_re]] (2L x 2L), so that cuBLAS can run it with its FP32
+// emulation on the tensor cores (BF16x9), which it does not take for complex operands.
+static int deriv_matrix_block(wem_ctx *c, DevBuf &b, int L, float dk, int mode, float scale)
+{
+    std::vector<float2> W;
+    deriv_matrix_host(L, dk, mode, scale, W);
+    const size_t L2 = 2 * (size_t)L;
+    std::vector<float> Wb(L2 * L2);
+    for (int j = 0; j < L; j++)
+        for (int i = 0; i < L; i++) {
+            const float2 w = W[(size_t)j * L + i];  // (i, j)
+            Wb[(size_t)j * L2 + i] = w.x;
+            Wb[((size_t)j + L) * L2 + i] = w.y;
+            Wb[(size_t)j * L2 + i + L] = -w.y;
+            Wb[((size_t)j + L) * L2 + i + L] = w.x;
+        }
+    int rc;
+    if ((rc = ensure(b, sizeof(float) * Wb.size()))) return rc;
+    CK(cudaMemcpyAsync(b.p, Wb.data(), sizeof(float) * Wb.size(), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));  // Wb is a local
+    return WEM_OK;
+}
+
+// out (planar) = derivative along the slow axis of in (planar): per batch entry `lines`
+// contiguous lines of L samples, [re plane, im plane], entries 2 * lines * L floats apart
+static int deriv_gemm_planar(wem_ctx *c, const DevBuf &Wb, const float *in, float *out, int L, long long lines, int batch)
+{
+    if (!c->blas) {
+        if (cublasCreate(&c->blas) != CUBLAS_STATUS_SUCCESS) return fail(WEM_ERR_CUDA, "cublasCreate failed");
+    }
+    if (cublasSetStream(c->blas, c->st) != CUBLAS_STATUS_SUCCESS) return fail(WEM_ERR_CUDA, "cublasSetStream failed");
+    const float one = 1.f, zero = 0.f;
+    const long long stride = 2 * lines * (long long)L;
+    auto run = [&](cublasComputeType_t ct) {
+        return cublasGemmStridedBatchedEx(c->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)lines, 2 * L, 2 * L, &one, in,
+                                          CUDA_R_32F, (int)lines, stride, Wb.p, CUDA_R_32F, 2 * L, 0, &zero, out,
+                                          CUDA_R_32F, (int)lines, stride, batch, ct, CUBLAS_GEMM_DEFAULT);
+    };
+    if (c->blas_real_compute < 0) {
+        c->blas_real_compute = (int)CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+        if (run(CUBLAS_COMPUTE_32F_EMULATED_16BFX9) == CUBLAS_STATUS_SUCCESS) return WEM_OK;
+        c->blas_real_compute = (int)CUBLAS_COMPUTE_32F;
+    }
+    if (run((cublasComputeType_t)c->blas_real_compute) != CUBLAS_STATUS_SUCCESS)
+        return fail(WEM_ERR_CUDA, "derivative GEMM (planar, L=%d) failed", L);
+    return WEM_OK;
+}
+
 // out = derivative of in along an axis of length L (matrix W from deriv_matrix), for `lines`
 // lines per batch entry and `batch` entries `stride` samples apart. axis_slow: sample i of
 // line l at i * ld + l (the lines contiguous); otherwise at l * ld + i (the axis
@@ -1372,15 +1422,16 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     // shots per batch: all their source volumes and derivatives (5 each) within half the free memory
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
-    const size_t per_shot = sizeof(float2) * (size_t)5 * nwf * n + sizeof(float) * 2 * n;
+    const size_t per_shot = sizeof(float2) * (size_t)6 * nwf * n + sizeof(float) * 2 * n;
     const int nbatch = (int)std::max<long long>(1, std::min<long long>(nshot, (long long)(free_b / 2 / per_shot)));
     const size_t plane = sizeof(float2) * (size_t)nbatch * nwf * n;
     DevBuf bwt, btwx, bsc, bsrc, bbase, bU, bX, bL, bR, bZ, bang, bpo, bpd, btap, bwav, btwf;
     DevBuf bDz, bDx, bDl, bDr;  // derivative matrices (z; x, left, right where x has no row FFT)
     DevBuf bigx;                // the batch's source cells
+    DevBuf bUp;                 // u in planes for the z derivative's real block GEMM
     auto release = [&]() {
         DevBuf *bs[] = { &bwt, &btwx, &bsc, &bsrc, &bbase, &bU, &bX, &bL, &bR, &bZ, &bang,
-                         &bpo, &bpd, &btap, &bwav, &btwf, &bDz, &bDx, &bDl, &bDr, &bigx };
+                         &bpo, &bpd, &btap, &bwav, &btwf, &bDz, &bDx, &bDl, &bDr, &bigx, &bUp };
         for (DevBuf *b : bs)
             if (b->p) cudaFree(b->p);
     };
@@ -1390,7 +1441,7 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
         (rc = ensure(bsrc, sizeof(float2) * nwf)) || (rc = ensure(bbase, sizeof(int64_t))) || (rc = ensure(bU, plane)) ||
         (rc = ensure(bX, plane)) || (rc = ensure(bL, plane)) || (rc = ensure(bR, plane)) ||
         (rc = ensure(bZ, plane)) || (rc = ensure(bang, sizeof(float) * 2 * n * nbatch)) ||
-        (rc = ensure(bigx, sizeof(int) * nbatch)) ||
+        (rc = ensure(bigx, sizeof(int) * nbatch)) || (rc = ensure(bUp, plane)) ||
         (rc = ensure(bpo, sizeof(float) * nz)) || (rc = ensure(bpd, sizeof(float) * n)) ||
         (rc = ensure(btap, sizeof(float) * nmx)) || (rc = ensure(bwav, sizeof(float) * p.nt)) ||
         (rc = ensure(btwf, sizeof(float2) * (twf.size() + 1)))) {
@@ -1414,7 +1465,7 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     CKR(cudaMemcpyAsync(btap.p, taper.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bwav.p, wav, sizeof(float) * p.nt, cudaMemcpyHostToDevice, st));
     if (fftx) CKR(cudaMemcpyAsync(btwf.p, twf.data(), sizeof(float2) * twf.size(), cudaMemcpyHostToDevice, st));
-    if ((rc = deriv_matrix(c, bDz, nz, dkz, 1, 1.f / (float)nz)) ||
+    if ((rc = deriv_matrix_block(c, bDz, nz, dkz, 1, 1.f / (float)nz)) ||
         (!fftx && ((rc = deriv_matrix(c, bDx, nmx, dkx, 1, 1.f / (float)nmx)) ||
                    (rc = deriv_matrix(c, bDl, nmx, dkx, 2, 1.f)) || (rc = deriv_matrix(c, bDr, nmx, dkx, 3, 1.f))))) {
         release();
@@ -1486,14 +1537,20 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
                 return rc;
             }
         }
-        if ((rc = deriv_gemm(c, bDz, P<float2>(bU), P<float2>(bZ), nz, true, nmx, nmx, nb * nwf, (long long)nz * nmx))) {
+        // u_z: u to planes, then the real block GEMM (planes out, read by the accumulation)
+        if (launch_planar(P<float2>(bU), P<float>(bUp), (long long)nz * nmx, (long long)nb * nwf, st)) {
+            release();
+            return fail(WEM_ERR_CUDA, "angles: planar launch: %s", cudaGetErrorString(cudaGetLastError()));
+        }
+        if ((rc = deriv_gemm_planar(c, bDz, P<float>(bUp), P<float>(bZ), nz, nmx, nb * nwf))) {
             release();
             return rc;
         }
         for (int j = 0; j < nb; j++) {
             AngleAccumArgs ac{};
             ac.nmx = nmx; ac.nz = nz; ac.nwf = nwf; ac.nw = nw; ac.nfreq_div = ifmax - ifmin + 1;
-            ac.u = P<float2>(bU) + j * vol; ac.ux = P<float2>(bX) + j * vol; ac.uz = P<float2>(bZ) + j * vol;
+            ac.u = P<float2>(bU) + j * vol; ac.ux = P<float2>(bX) + j * vol; ac.uz = nullptr;
+            ac.uzp = P<float>(bZ) + 2 * j * vol;
             ac.ul = P<float2>(bL) + j * vol; ac.ur = P<float2>(bR) + j * vol;
             ac.angx = P<float>(bang) + (size_t)j * 2 * n; ac.angy = P<float>(bang) + (size_t)j * 2 * n + n;
             if (launch_angles_accum(ac, st)) {
@@ -1501,7 +1558,7 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
                 return fail(WEM_ERR_CUDA, "angles: accumulation launch: %s", cudaGetErrorString(cudaGetLastError()));
             }
         }
-        kernels += (fftx ? 2 : 1) + nb;  // and the cuBLAS GEMMs of the derivatives
+        kernels += (fftx ? 3 : 2) + nb;  // and the cuBLAS GEMMs of the derivatives
         for (int j = 0; j < nb; j++) {
             const int s = s0 + j;
             CKR(cudaMemcpyAsync(angx + (size_t)s * n, P<float>(bang) + (size_t)j * 2 * n, sizeof(float) * n,

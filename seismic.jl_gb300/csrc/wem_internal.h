@@ -144,8 +144,11 @@ struct AngleArgs {
 struct AngleAccumArgs {
     int nmx, nz, nwf, nw, nfreq_div;
     const float2 *u, *ux, *uz, *ul, *ur;  // [nwf][nz][nmx]
+    const float *uzp;                     // u_z in planes instead: [nwf][re, im][nz][nmx] (nullptr: uz)
     float *angx, *angy;                   // [nmx][nz]
 };
+// interleaved complex entries of `entry` samples -> [re plane, im plane] per entry
+int launch_planar(const float2 *in, float *out, long long entry, long long nentries, cudaStream_t st);
 // 3-D: running sums over batches of frequencies, one point per thread
 struct AngleAccum3Args {
     int n, nz, nwf, nw, nfreq_div, last;  // n = nmx*nmy; last: write the angles after this batch
