@@ -121,7 +121,8 @@ WEM_API int wem_migrate_device(wem_ctx *ctx, int nshot, const float *sx, const f
    the half-spectrum weights of its real inverse transform); exact = 1: the exact
    adjoint of wem_migrate with the same parameters, for least-squares migration
    (the two differ only for PSPI in laterally varying velocity and at the Nyquist
-   frequency). On 3-D grids (nmy > 1) exact = 0 only; exact = 1 returns WEM_ERR_SIZE. */
+   frequency). On 3-D grids (nmy > 1) exact = 1 continues the receiver up with the adjoint of
+   the 3-D migration step (PSPI; for split-step the reference's operator already is it). */
 WEM_API int wem_model(wem_ctx *ctx, int nshot, const float *sx, const float *sy,
                       const int64_t *trace_offset, const int32_t *trace_cell,
                       const float *m, float *d, int exact);

@@ -30,7 +30,7 @@ namespace gbwem {
 __device__ __forceinline__ bool m3_active(const Mig3dArgs &a, uint8_t zf, int w)
 {
     if ((a.mode == 1 || a.mode == 3) && w != 0) return false;
-    if (a.mode == 2 && w != 1) return false;
+    if ((a.mode == 2 || a.mode == 4) && w != 1) return false;
     return (zf & (w == 0 ? Z_SRC : Z_REC)) != 0;
 }
 
@@ -425,7 +425,14 @@ __global__ void __launch_bounds__(256, 2) wem3d_rows_inv_kernel(const Mig3dArgs 
                 // planes: one per reference, or (paired planes, a.plan) the real parts of two
                 // references in one plane and one plane per reference taken whole
                 const int *plan = (PSPI && INTERP == 0 && a.plan) ? a.plan + (size_t)iz * PLAN3_STRIDE : nullptr;
-                const int np = plan ? plan[0] : nref;
+                const int np = a.mode == 4 ? 0 : (plan ? plan[0] : nref);
+                if (a.mode == 4) {
+                    // the exact adjoint's receiver (pass B summed the references): one plane in Y
+                    const float2 *yrow = a.Y + (((size_t)item * 2 + w) * nmx + x) * nky;
+#pragma unroll
+                    for (int m = 0; m < 16; m++) acc[m] = yrow[t + TY * m];
+                    fft_row<NY, +1>(acc, xbuf, s_tw, t, sync);
+                }
                 for (int pl = 0; pl < np; pl++) {
                     const float2 *crow = a.C + ((((size_t)item * 2 + w) * nref + pl) * nmx + x) * nky;
                     float2 u[16];
@@ -473,7 +480,7 @@ __global__ void __launch_bounds__(256, 2) wem3d_rows_inv_kernel(const Mig3dArgs 
                 if constexpr (PSPI && INTERP == 0 && TY <= 32) {
                     // points of this row taken whole: Im dref(x0, y0) = Im sum_ky S(ky)
                     // e^{+2 pi i ky y0 / NY} over pass B's column sums (Horner, team sum)
-                    const int *wp = (a.plan && a.wpos) ? a.wpos + (size_t)iz * WPOS_STRIDE : nullptr;
+                    const int *wp = (a.plan && a.wpos && a.mode != 4) ? a.wpos + (size_t)iz * WPOS_STRIDE : nullptr;
                     const int nj = wp ? wp[0] : 0;
                     for (int j = 0; j < nj; j++) {
                         const int cell = wp[1 + j];
@@ -570,6 +577,165 @@ __global__ void __launch_bounds__(256, 2) wem3d_rows_inv_kernel(const Mig3dArgs 
     }
 }
 
+// ---------------------------------------------------------------- exact adjoint (mode 4)
+// The receiver of the exact modelling goes up with the adjoint of the migration step:
+// y = IFFT2( sum_r conj(P_r) FFT2( W_r^T u ) ), W_r the transposed selection / interpolation
+// weights of reference r (the real-part projection where the nearest-lower mode keeps Re).
+// Pass A': m * smig injected, then per reference in use the weighted row's y transform into
+// C plane r; pass B': per column the x transforms of the references' planes times conj(P_r),
+// summed, transformed back into the Y plane; pass C (mode 4) transforms that plane back in y.
+template <int NY, int INTERP>
+__global__ void __launch_bounds__(256) wem3d_rows_fwd_adj_kernel(const Mig3dArgs a)
+{
+    constexpr int TY = NY / 16, TEAMS = 256 / TY;
+    constexpr int TW = fft_tw_size<NY>(), TWP = (TW + 1) & ~1;
+    extern __shared__ float4 smem_raw[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *s_x = s_tw + TWP;
+    const int tid = threadIdx.x, team = tid / TY, t = tid - team * TY;
+    float2 *xbuf = s_x + (size_t)team * pad16(NY);
+    const unsigned sync = team_sync_handle<NY>(tid);
+    for (int i = tid; i < TW; i += 256) s_tw[i] = a.twy[i];
+    __syncthreads();
+    const int iz = a.iz, n = a.nmx * a.nmy, nmy = a.nmy;
+    if (!(a.zflag[iz] & Z_REC)) return;  // the receiver does not step here: nothing to transform
+    const unsigned long long used = a.refmask ? a.refmask[iz] : ~0ull;
+    const long long njobs = (long long)a.nitems * a.nmx;
+    for (long long job = (long long)blockIdx.x * TEAMS + team; job < njobs; job += (long long)gridDim.x * TEAMS) {
+        const int item = (int)(job / a.nmx), x = (int)(job - (long long)item * a.nmx);
+        const size_t zrow = (size_t)iz * n + (size_t)x * nmy;
+        const float2 *urow = a.U + ((size_t)item * 2 + 1) * n + (size_t)x * nmy;
+        const float2 *sm = a.smig + ((size_t)item * a.nz + iz) * n + (size_t)x * nmy;
+        float2 v[16];
+        uint32_t selp[4] = { 0, 0, 0, 0 };
+        float wl[16];
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int y = t + TY * m;
+            float2 q = make_float2(0.f, 0.f);
+            uint32_t b = 0x7fu;
+            wl[m] = 0.f;
+            if (y < nmy) {
+                q = urow[y];
+                const float mv = a.mimg[zrow + y];
+                const float2 s_ = sm[y];
+                q.x += mv * s_.x;  // injection (wem.c:270-272)
+                q.y += mv * s_.y;
+                b = a.selb[zrow + y];
+                if (INTERP == 1) wl[m] = a.wlin[zrow + y];
+            }
+            v[m] = q;
+            selp[m >> 2] |= b << (8 * (m & 3));
+        }
+        for (int r = 0; r < a.nref; r++) {
+            if (!((used >> r) & 1ull)) continue;  // team-uniform
+            float2 u[16];
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                bool re_only;
+                const float g = sel_weight<INTERP>(selp, wl, m, r, re_only);
+                u[m] = make_float2(v[m].x * g, re_only ? 0.f : v[m].y * g);
+            }
+            fft_row<NY, -1>(u, xbuf, s_tw, t, sync);
+            float2 *crow = a.C + ((((size_t)item * 2 + 1) * a.nref + r) * a.nmx + x) * NY;
+#pragma unroll
+            for (int m = 0; m < 16; m++) crow[t + TY * m] = u[m];
+        }
+    }
+}
+
+template <int NX>
+__global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_adj_kernel(const Mig3dArgs a)
+{
+    using CS = ColShape<NX>;
+    constexpr int TX = CS::TX, CW = CS::CW, NT = CS::NT, HALF = CS::HALF;
+    extern __shared__ float4 smem_raw[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *s_ph = s_tw + CS::TWP;                    // [ROWS][HALF] phase table of one reference
+    float2 *s_x = s_ph + (size_t)2 * CS::ROWS * HALF;  // exchange buffers (the layout of pass B)
+    const int pitch = tile_pitch(a.nmx);
+    float2 *s_tile = s_x + (size_t)2 * CW * pad16(NX);  // [2][CW][pitch]: the receiver half is used
+    const int tid = threadIdx.x, team = tid / TX, t = tid - team * TX;
+    const int w = team / CW, c = team - w * CW;
+    float2 *xbuf = s_x + (size_t)team * pad16(NX);
+    const unsigned sync = team_sync_handle<NX>(tid);
+    for (int i = tid; i < CS::TW; i += NT) s_tw[i] = a.twx[i];
+    const int iz = a.iz, nmx = a.nmx, nky = a.nky, nblk = nky / CW;
+    const bool active = w == 1 && (a.zflag[iz] & Z_REC);
+    const bool step = (a.zflag[iz] & Z_REC) != 0;  // CTA-uniform
+    const unsigned long long used = a.refmask ? a.refmask[iz] : ~0ull;
+    constexpr int H = CW / 2;
+    for (int job = blockIdx.x; step && job < a.nitems * nblk; job += gridDim.x) {
+        const int item = job / nblk, blk = job - item * nblk;
+        const int ky_c = col_ky(blk, c, H, nky);
+        const int row_c = c < H ? c : (ky_c == 0 ? H : c - H);
+        const bool zero_col = col_ky(blk, CW - 1, H, nky) == 0;
+        const float wv = __fmul_rn((float)(a.ifmin + a.item_iwi[item]), a.dw);
+        const float w2 = __fmul_rn(wv, wv);
+        float2 acc[16];
+#pragma unroll
+        for (int m = 0; m < 16; m++) acc[m] = make_float2(0.f, 0.f);
+        for (int r = 0; r < a.nref; r++) {
+            if (!((used >> r) & 1ull)) continue;
+            __syncthreads();  // the previous reference's table and tile are no longer read
+            const float2 *src = a.C + (((size_t)item * 2 + 1) * a.nref + r) * nmx * nky;
+            for (int e = tid; e < nmx * CW; e += NT) {
+                const int x = e / CW, cc = e - x * CW;
+                s_tile[((size_t)CW + cc) * pitch + x] = src[(size_t)x * nky + col_ky(blk, cc, H, nky)];
+            }
+            const float slow2 = a.slow2[(size_t)iz * a.nref + r];
+            for (int e = tid; e < (zero_col ? H + 1 : H) * HALF; e += NT) {
+                const int rr = e / HALF, kk = e - rr * HALF;
+                const int kyi = rr < H ? col_ky(blk, rr, H, nky) : 0;
+                const float ky = __fmul_rn(a.dky, (float)kyi);
+                const float kx = __fmul_rn(a.dkx, (float)kk);
+                const float s2 = __fsub_rn(__fsub_rn(__fmul_rn(w2, slow2), __fmul_rn(kx, kx)), __fmul_rn(ky, ky));
+                float2 P;
+                if (s2 >= 0.f) {
+                    float sn, cs;
+                    sincosf(__fmul_rn(__fsqrt_rn(s2), a.dz), &sn, &cs);
+                    P = make_float2(cs, sn);
+                } else {
+                    P = make_float2(expf(-__fmul_rn(__fmul_rn(0.2f, __fsqrt_rn(-s2)), fabsf(a.dz))), 0.f);
+                }
+                s_ph[e] = make_float2(P.x * a.inv_n, P.y * a.inv_n);
+            }
+            __syncthreads();
+            if (active) {
+                float2 v[16];
+#pragma unroll
+                for (int m = 0; m < 16; m++) {
+                    const int x = t + TX * m;
+                    v[m] = x < nmx ? s_tile[((size_t)CW + c) * pitch + x] : make_float2(0.f, 0.f);
+                }
+                fft_row<NX, -1>(v, xbuf, s_tw, t, sync);
+#pragma unroll
+                for (int m = 0; m < 16; m++) {
+                    const int k = t + TX * m;
+                    const float2 q = cmulc(v[m], s_ph[(size_t)row_c * HALF + (k <= NX / 2 ? k : NX - k)]);
+                    acc[m].x += q.x;
+                    acc[m].y += q.y;
+                }
+            }
+        }
+        if (active) fft_row<NX, +1>(acc, xbuf, s_tw, t, sync);
+        __syncthreads();  // every team is past its last tile read
+        if (active) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int x = t + TX * m;
+                if (x < nmx) s_tile[((size_t)CW + c) * pitch + x] = acc[m];
+            }
+        }
+        __syncthreads();
+        float2 *dst = a.Y + ((size_t)item * 2 + 1) * nmx * nky;
+        for (int e = tid; e < nmx * CW; e += NT) {
+            const int x = e / CW, cc = e - x * CW;
+            dst[(size_t)x * nky + col_ky(blk, cc, H, nky)] = s_tile[((size_t)CW + cc) * pitch + x];
+        }
+    }
+}
+
 // initial planes: source spike at (igx, igy), receiver spectra (wem.c:230-233)
 __global__ void wem3d_init_kernel(const Mig3dArgs a)
 {
@@ -649,9 +815,44 @@ int m3d_cols_smem(int nkx, int pspi, const Mig3dArgs &a, size_t *smem)
 #undef CALL
 }
 
+template <int NY, int INTERP> static int rows_fwd_adj(const Mig3dArgs &a, int grid, cudaStream_t st)
+{
+    constexpr int TW = fft_tw_size<NY>(), TWP = (TW + 1) & ~1;
+    const size_t smem = sizeof(float2) * ((size_t)TWP + (size_t)(256 / (NY / 16)) * pad16(NY));
+    auto k = wem3d_rows_fwd_adj_kernel<NY, INTERP>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    k<<<grid, 256, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int NX> static int cols_adj(const Mig3dArgs &a, int grid, cudaStream_t st)
+{
+    using CS = ColShape<NX>;
+    const size_t smem = col_smem_bytes(CS::TWP, CS::HALF, CS::CW, 2 * CS::CW, pad16(NX), a.nmx);
+    auto k = wem3d_cols_adj_kernel<NX>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    k<<<grid, CS::NT, smem, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 int m3d_launch_step(int nkx, int nky, int pspi, int interp, const Mig3dArgs &a, int nsm, cudaStream_t st)
 {
     int rc;
+    if (a.mode == 4) {  // the exact adjoint's receiver step (PSPI)
+        if (!pspi) return -1;
+#define CALL(N) (interp == 0 ? rows_fwd_adj<N, 0>(a, nsm * 4, st) : rows_fwd_adj<N, 1>(a, nsm * 4, st))
+        rc = [&]() { W3_SWITCH(nky, CALL) }();
+#undef CALL
+        if (rc) return rc;
+#define CALL(N) cols_adj<N>(a, nsm * 2, st)
+        rc = [&]() { W3_SWITCH(nkx, CALL) }();
+#undef CALL
+        if (rc) return rc;
+#define CALL(N) (interp == 0 ? rows_inv<N, true, 0>(a, nsm * 4, st) : rows_inv<N, true, 1>(a, nsm * 4, st))
+        rc = [&]() { W3_SWITCH(nky, CALL) }();
+#undef CALL
+        return rc;
+    }
 #define CALL(N) rows_fwd<N>(a, nsm * 4, st)
     rc = [&]() { W3_SWITCH(nky, CALL) }();
 #undef CALL

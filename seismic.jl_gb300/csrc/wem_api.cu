@@ -1595,8 +1595,6 @@ extern "C" int wem_migrate_survey(wem_ctx *c, const wem_params *p, const float *
 static int run_model3d(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, float *d_dev, int exact)
 {
     const wem_params &p = c->p;
-    if (exact) return fail(WEM_ERR_SIZE, "the exact adjoint of the 3-D migration is not built (the reference's "
-                                         "modelling operator is: exact = 0)");
     cudaStream_t st = c->st;
     const int nmx = p.nmx, nmy = p.nmy, nz = p.nz, n = nmx * nmy;
     const int nref = p.pspi ? p.nref : 1;
@@ -1643,6 +1641,7 @@ static int run_model3d(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, f
         a.src_cell = P<int>(c->igx); a.srcw = P<float2>(c->srcw); a.recv = nullptr;
         a.U = P<float2>(c->m3_U); a.Y = P<float2>(c->m3_Y); a.C = P<float2>(c->m3_C); a.img_parts = nullptr;
         a.pspi = p.pspi; a.smig = P<float2>(c->smig); a.mimg = P<float>(c->mimg);
+        a.refmask = P<unsigned long long>(c->refmask);
         a.plan = plan3_for(c, a);
         if (a.plan) {
             a.wpos = P<int>(c->wposb);
@@ -1657,8 +1656,10 @@ static int run_model3d(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, f
                 return fail(WEM_ERR_CUDA, "3-D modelling step launch: %s", cudaGetErrorString(cudaGetLastError()));
             kernels += 3;
         }
-        a.mode = 2;
-        for (int iz = nz - 1; iz >= 0; iz--) {  // receiver up (wem.c:266-276)
+        // receiver up (wem.c:266-276): the reference's operator, or with exact = 1 the exact
+        // adjoint of the migration step (PSPI; for split-step the reference's operator is it)
+        a.mode = exact && p.pspi ? 4 : 2;
+        for (int iz = nz - 1; iz >= 0; iz--) {
             a.iz = iz;
             if (m3d_launch_step(c->nkx, c->nky, p.pspi, p.interp, a, c->nsm, st))
                 return fail(WEM_ERR_CUDA, "3-D modelling step launch: %s", cudaGetErrorString(cudaGetLastError()));

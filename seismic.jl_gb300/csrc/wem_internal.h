@@ -102,6 +102,7 @@ struct Mig3dArgs {
     float2 *img_parts;  // [chunk][nz][nmx*nmy] (sum, 0)
     // modelling (wem.c:252-281): mode 1 continues the source down and keeps it in smig;
     // mode 2 continues the receiver up (-dz, adj=false) with m * smig injected first;
+    // mode 4 continues it up with the exact adjoint of the migration step (PSPI);
     // mode 3 continues the source down as the angle computation does (ssop_source: the
     // split-step correction before the transform) and keeps it in smig
     int mode, pspi;     // mode 0: migration
@@ -116,6 +117,9 @@ struct Mig3dArgs {
     // direct sums: pass B sums each column over kx into dsum, pass C sums over ky)
     const int *wpos;    // [nz][WPOS_STRIDE]
     float2 *dsum;       // [item][2][WHOLE_MAX][nky]
+    // mode 4, the exact adjoint's receiver going up: the references in use per depth (bit r;
+    // nullptr: all)
+    const unsigned long long *refmask;
 };
 constexpr int PLAN3_MAX = 16, PLAN3_STRIDE = 1 + 2 * PLAN3_MAX;
 int m3d_supported(int nkx, int nky);

@@ -105,10 +105,8 @@ def test_3d_modelling_matches_reference_golden(gpu_lib, case):
 @pytest.mark.parametrize("pspi,interp", [(0, "ref"), (1, "ref"), (1, "linear")])
 def test_3d_batched_modelling_matches_port(gpu_lib, oracle_mod, pspi, interp):
     """Several shots with source depth and receiver depth below the surface in one call,
-    against the oracle's port shot by shot at the shots' receiver cells; the exact
-    adjoint is not built in 3-D and says so."""
+    against the oracle's port shot by shot at the shots' receiver cells."""
     from wemgpu import synth
-    from wemgpu._lib import WemError
     c = synth.small_case3d(61, nx=32, ny=32, nz=8, nt=64, nshot=2, pspi=pspi, nref=3, interp=interp)
     p, s = dict(c["params"], sz=15.0, gz=25.0), c["shots"]
     rng = np.random.default_rng(3)
@@ -116,10 +114,29 @@ def test_3d_batched_modelling_matches_port(gpu_lib, oracle_mod, pspi, interp):
     with gpu_lib.Context() as ctx:
         ctx.prepare(p, c["vel"], c["wav"])
         d = ctx.model(s, m, exact=False)
-        with pytest.raises(WemError) as e:
-            ctx.model(s, m, exact=True)
-        assert e.value.code == -2
     for i in range(s.nshot):
         lo, hi = int(s.trace_offset[i]), int(s.trace_offset[i + 1])
         want = oracle_mod.wem_port(dict(p, sx=float(s.sx[i]), sy=float(s.sy[i])), c["vel"], c["wav"], m=m, adj=False)
         assert rel_l2(d[lo:hi], want[s.trace_cell[lo:hi]]) < TOL
+
+
+@pytest.mark.parametrize("pspi,interp,nref", [(1, "linear", 3), (1, "ref", 6), (0, "ref", 1)])
+def test_3d_exact_pair_dot_product(gpu_lib, pspi, interp, nref):
+    """The exact modelling (exact = 1: the receiver goes up with the adjoint of the migration
+    step, W_r^T, FFT2, conj(P_r), sum over r, IFFT2) and the 3-D migration are an adjoint
+    pair: <d, L m> = <L' d, m> to FP32 rounding, with sources and receivers below the
+    surface. Split-step: the reference's modelling operator already is the adjoint."""
+    from wemgpu import synth
+    from wemgpu.api import Shots
+    from wemgpu.cg import dot_test
+    c = synth.small_case3d(91, nx=64, ny=32, nz=8, nt=64, nshot=2, pspi=pspi, nref=nref, interp=interp, fmax=30.0)
+    p, s = dict(c["params"], sz=15.0, gz=25.0), c["shots"]
+    rng = np.random.default_rng(92)
+    m = rng.standard_normal((p["nmx"] * p["nmy"], p["nz"])).astype(np.float32)
+    d = rng.standard_normal(s.data.shape).astype(np.float32)
+    with gpu_lib.Context() as ctx:
+        ctx.prepare(p, c["vel"], c["wav"])
+        geo = lambda r: Shots(s.sx, s.sy, s.trace_offset, s.trace_cell, np.ascontiguousarray(r, np.float32))
+        a, b = dot_test(lambda x: ctx.model(s, np.asarray(x, np.float32), exact=True),
+                        lambda r: ctx.migrate(geo(r)), m, d)
+    assert abs(a - b) / abs(a) < 1e-5, (a, b)
