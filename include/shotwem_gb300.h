@@ -158,6 +158,13 @@ WEM_API int wem_last_timing(wem_ctx *ctx, float *ms, int *kernels);
    recursion, image reduction (CUDA events around each launch). */
 WEM_API int wem_last_kernel_times(wem_ctx *ctx, float *ms_spectra, float *ms_extrapolate, float *ms_reduce);
 
+/* Self-test of the bounded device-side waits (no counterpart in the reference): the
+   tensor-core stages of the split16 form wait on an mbarrier with a time limit (about a
+   second) and report WEM_ERR_TIMEOUT instead of hanging. This launches one such wait that
+   nothing completes on `device` and returns in *timed_out whether it gave up (1), and in
+   *ms how long the launch took; the context of the device stays usable. */
+WEM_API int wem_selftest_wait_timeout(int device, int *timed_out, float *ms);
+
 /* How the last 2-D wem_migrate* call ran its depth recursion (no counterpart in the
    reference): threads per CTA, shots sharing one CTA's phase tables, CTAs launched,
    whether the call replayed a captured CUDA graph of the whole launch sequence (1) or

@@ -205,6 +205,25 @@ extern "C" int wem_last_kernel_times(wem_ctx *c, float *ms_spectra, float *ms_ex
     return WEM_OK;
 }
 
+extern "C" int wem_selftest_wait_timeout(int device, int *timed_out, float *ms)
+{
+    if (!timed_out) return fail(WEM_ERR_ARG, "wem_selftest_wait_timeout: null argument");
+    CK(cudaSetDevice(device));
+    int *d = nullptr;
+    CK(cudaMalloc(&d, sizeof(int)));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = WEM_OK;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess || cudaMemset(d, 0, sizeof(int)) ||
+        cudaEventRecord(e0, 0) || launch_wait_probe(d, 0) || cudaEventRecord(e1, 0) || cudaEventSynchronize(e1) ||
+        cudaMemcpy(timed_out, d, sizeof(int), cudaMemcpyDeviceToHost))
+        rc = fail(WEM_ERR_CUDA, "wem_selftest_wait_timeout: %s", cudaGetErrorString(cudaGetLastError()));
+    if (!rc && ms) cudaEventElapsedTime(ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(d);
+    return rc;
+}
+
 extern "C" int wem_last_launch(wem_ctx *c, int *threads, int *shots_per_cta, int *grid, int *replayed, int *tuned)
 {
     if (!c) return fail(WEM_ERR_ARG, "null context");

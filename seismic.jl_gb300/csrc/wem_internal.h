@@ -183,6 +183,8 @@ int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref,
                      int form = MIG_FORM_FP32);
 int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, int grid, cudaStream_t st,
                    int form = MIG_FORM_FP32);
+// one bounded mbarrier wait that nothing completes; *timed_out (device) = 1 when it gave up
+int launch_wait_probe(int *timed_out, cudaStream_t st);
 // the precomputed phase tables of the paired form (a.ptab layout) into out
 int launch_phase_tables(int nkx, const MigArgs &a, float2 *out, cudaStream_t st);
 // the 10240-byte W operand image of the split16 DFT stages

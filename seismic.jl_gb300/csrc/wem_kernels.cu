@@ -269,6 +269,23 @@ __global__ void __launch_bounds__(256) wem_phase_tables_kernel(const MigArgs a, 
     }
 }
 
+// one bounded mbarrier wait that nothing completes (the waits of the tensor-core stages)
+__global__ void wem_wait_probe_kernel(int *timed_out)
+{
+    __shared__ uint64_t mb;
+    if (threadIdx.x == 0) {
+        mbar_init(smem_u32(&mb), 1);
+        mbar_init_fence();
+        *timed_out = mbar_wait_bounded(smem_u32(&mb), 0) ? 0 : 1;
+    }
+}
+
+int launch_wait_probe(int *timed_out, cudaStream_t st)
+{
+    wem_wait_probe_kernel<<<1, 32, 0, st>>>(timed_out);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
 int launch_phase_tables(int nkx, const MigArgs &a, float2 *out, cudaStream_t st)
 {
     if (a.nz < 1 || a.nwf < 1) return 0;

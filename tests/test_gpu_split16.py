@@ -69,3 +69,19 @@ def test_split16_rejects_other_geometries(gpu_lib):
     with pytest.raises(WemError) as e:
         gpu_lib.migrate(dict(c["params"], precision="split16"), c["vel"], c["wav"], c["shots"])
     assert e.value.code == -2  # WEM_ERR_SIZE
+
+
+def test_bounded_wait_reports_timeout_and_device_stays_usable(gpu_lib):
+    """The tensor-core stages wait on an mbarrier with a time limit (about a second). A wait
+    that nothing completes gives up, reports it, and the context stays usable: a migration
+    on the same device right after it still matches the FP64 operator."""
+    import ctypes as C
+    from wemgpu import synth
+    from wemgpu._lib import lib
+    timed_out, ms = C.c_int(-1), C.c_float(0.0)
+    assert lib().wem_selftest_wait_timeout(0, C.byref(timed_out), C.byref(ms)) == 0
+    assert timed_out.value == 1
+    assert 100.0 < ms.value < 20000.0, ms.value  # the wait ran to its limit, then returned
+    c = synth.small_case(53, nx=64, nz=8, nt=64, nshot=1)
+    m = gpu_lib.migrate(c["params"], c["vel"], c["wav"], c["shots"])
+    assert np.isfinite(m).all() and np.abs(m).max() > 0
