@@ -145,7 +145,9 @@ WEM_API int wem_migrate_survey(wem_ctx *ctx, const wem_params *p, const float *v
    signed by the side the energy arrives from. Uses nt, dt, the grid, sz, fmin and fmax of
    p (padt, padx, pspi, nref, interp are not used; any nmx and nz). vel [nmx][nz], wav [nt];
    angx, angy: host [nshot][nmx][nz] (angy may be NULL; it is 0 in 2-D). Needs a context
-   (wem_ctx_create), not wem_prepare. 2-D: nmx <= 4096. 3-D (nmy > 1): nmx and nmy powers of
+   (wem_ctx_create), not wem_prepare. 2-D: nmx <= 4096; the shots run in batches whose
+   wavefield volumes fit in half the free device memory, and the context keeps those buffers
+   for its next call (wem_ctx_destroy frees them). 3-D (nmy > 1): nmx and nmy powers of
    two in [64, 1024] (WEM_ERR_SIZE otherwise); angy is then the y-axis angle. */
 WEM_API int wem_angles(wem_ctx *ctx, const wem_params *p, const float *vel, const float *wav, int nshot,
                        const float *sx, const float *sy, float *angx, float *angy);

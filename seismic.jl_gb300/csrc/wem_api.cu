@@ -90,6 +90,7 @@ struct wem_ctx {
     DevBuf wposb;                 // [nz][WPOS_STRIDE] points taking their wavefield whole (paired form)
     DevBuf plan3;                 // [nz][PLAN3_STRIDE] 3-D paired planes (empty: one plane per reference)
     cublasHandle_t blas = nullptr;  // the incidence angles' derivative GEMMs
+    DevBuf ang_vol[7];              // 2-D angles: the batch's volumes (u, u_x, u_l, u_r, u_z, u planes) and angles
     int blas_compute = -1;          // their cuBLAS compute type once chosen (complex operands)
     int blas_real_compute = -1;     // the same for the planar (real) form
     DevBuf dsum3;                 // 3-D direct sums: [item][2][WHOLE_MAX][nky] column sums
@@ -177,6 +178,8 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
                        &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb, &c->selbp, &c->wlinp, &c->ptab, &c->plan3, &c->dsum3 };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
+    for (DevBuf &b : c->ang_vol)
+        if (b.p) cudaFree(b.p);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     if (c->blas) cublasDestroy(c->blas);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1067,15 +1070,21 @@ static void deriv_matrix_host(int L, float dk, int mode, float scale, std::vecto
         const bool on = mode == 1 || (mode == 2 && k > L / 2) || (mode == 3 && k <= L / 2);
         kx[k] = on ? (double)kf : 0.0;
     }
+    std::vector<double> cs(L), sn(L);  // e^{2 pi i m / L}
+    for (int m = 0; m < L; m++) {
+        const double ph = 6.283185307179586476925286766559 * (double)m / L;
+        cs[m] = cos(ph);
+        sn[m] = sin(ph);
+    }
     std::vector<double> wr(L), wi(L);
     for (int j = 0; j < L; j++) {
         double re = 0.0, im = 0.0;
         for (int k = 0; k < L; k++) {
             if (kx[k] == 0.0) continue;
-            const double ph = 6.283185307179586476925286766559 * (double)(((long long)k * j) % L) / L;
-            // i k e^{i ph} = k (-sin ph + i cos ph)
-            re -= kx[k] * sin(ph);
-            im += kx[k] * cos(ph);
+            const int m = (int)(((long long)k * j) % L);
+            // i k e^{i ph} = k (-sin ph + i cos ph), ph = 2 pi k j / L
+            re -= kx[k] * sn[m];
+            im += kx[k] * cs[m];
         }
         wr[j] = re * scale;
         wi[j] = im * scale;
@@ -1444,13 +1453,16 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     const size_t per_shot = sizeof(float2) * (size_t)6 * nwf * n + sizeof(float) * 2 * n;
     const int nbatch = (int)std::max<long long>(1, std::min<long long>(nshot, (long long)(free_b / 2 / per_shot)));
     const size_t plane = sizeof(float2) * (size_t)nbatch * nwf * n;
-    DevBuf bwt, btwx, bsc, bsrc, bbase, bU, bX, bL, bR, bZ, bang, bpo, bpd, btap, bwav, btwf;
+    DevBuf bwt, btwx, bsc, bsrc, bbase, bpo, bpd, btap, bwav, btwf;
     DevBuf bDz, bDx, bDl, bDr;  // derivative matrices (z; x, left, right where x has no row FFT)
     DevBuf bigx;                // the batch's source cells
-    DevBuf bUp;                 // u in planes for the z derivative's real block GEMM
+    // the volumes stay with the context for the next call: u, u_x, u_left, u_right, u_z, u in
+    // planes (the z derivative's real block GEMM), the angles
+    DevBuf &bU = c->ang_vol[0], &bX = c->ang_vol[1], &bL = c->ang_vol[2], &bR = c->ang_vol[3],
+           &bZ = c->ang_vol[4], &bUp = c->ang_vol[5], &bang = c->ang_vol[6];
     auto release = [&]() {
-        DevBuf *bs[] = { &bwt, &btwx, &bsc, &bsrc, &bbase, &bU, &bX, &bL, &bR, &bZ, &bang,
-                         &bpo, &bpd, &btap, &bwav, &btwf, &bDz, &bDx, &bDl, &bDr, &bigx, &bUp };
+        DevBuf *bs[] = { &bwt, &btwx, &bsc, &bsrc, &bbase, &bpo, &bpd, &btap, &bwav, &btwf,
+                         &bDz, &bDx, &bDl, &bDr, &bigx };
         for (DevBuf *b : bs)
             if (b->p) cudaFree(b->p);
     };
