@@ -66,6 +66,46 @@ def conjugate_gradients(d, forward: Callable, adjoint: Callable, niter: int = 10
     return m, np.asarray(cost)
 
 
+def least_squares_migration(ctx, shots, niter: int = 10, mu: float = 0.0, tol: float = 1.0e-15,
+                            exact: bool = True, callback: Callable | None = None):
+    """Least-squares migration of host trace data: ConjugateGradients(d, [WEM operator], ...;
+    Niter, mu, tol) (src/Solvers/ConjugateGradients.jl:1-39) over the prepared context's
+    Born modelling / migration pair, with the data, residual, image and search vectors held
+    in device memory for the whole solve. The traces of `shots` (host, [ntrace, nt]) are
+    copied to the device once from pinned memory; the image comes back once. exact=True
+    takes the exact adjoint of migrate() as the forward operator (a symmetric pair for CG);
+    exact=False the reference's Born operator. Returns (m [nmx*nmy, nz] float32, cost)."""
+    import torch
+    p = ctx.params
+    if p is None:
+        raise RuntimeError("prepare() first")
+    dev = torch.device("cuda", torch.cuda.current_device())
+    d_host = torch.from_numpy(np.ascontiguousarray(shots.data, np.float32)).pin_memory()
+    d_obs = d_host.to(dev, non_blocking=True)
+    ntr, nt = d_obs.shape
+    nm = (p.nmx * p.nmy, p.nz)
+    cur = torch.cuda.current_stream(dev)
+
+    def fwd(m_t):
+        d_t = torch.empty((ntr, nt), dtype=torch.float32, device=dev)
+        cur.synchronize()  # the library works on its own stream
+        ctx.model_device(shots, m_t.data_ptr(), d_t.data_ptr(), exact=exact)
+        return d_t
+
+    def adj(r_t):
+        m_t = torch.empty(nm, dtype=torch.float32, device=dev)
+        cur.synchronize()
+        ctx.migrate_device(shots, r_t.data_ptr(), m_t.data_ptr())
+        return m_t
+
+    inner_dev = lambda x, y: float(torch.dot(x.reshape(-1).double(), y.reshape(-1).double()))
+    m_t, cost = conjugate_gradients(d_obs, fwd, adj, niter=niter, mu=mu, tol=tol, callback=callback,
+                                    inner_fn=inner_dev)
+    m_out = torch.empty(nm, dtype=torch.float32).pin_memory()
+    m_out.copy_(m_t)
+    return m_out.numpy(), cost
+
+
 def dot_test(forward, adjoint, m_rand: np.ndarray, d_rand: np.ndarray):
     """<d, L m> and <L' d, m> (src/Tools/DotTest.jl:1-12) in float64."""
     d_fwd = forward(m_rand)
