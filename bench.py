@@ -582,7 +582,8 @@ def main():
     props = torch.cuda.get_device_properties(dev)
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     fp32_nominal = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
-    tr = recorded_traffic(args.workload)
+    prec = p.get("precision", "fp32")
+    tr = recorded_traffic(args.workload if prec == "fp32" else f"{args.workload}_{prec}")
     traffic = tr.get("bytes_per_launch") if tr else None
 
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
