@@ -866,7 +866,7 @@ static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev,
     return WEM_OK;
 }
 
-// The FP32 PSPI kernels read the phase tables of every (frequency, depth) from one array
+// The 2-D PSPI kernels (FP32 and split16) read the phase tables of every (frequency, depth) from one array
 // that wem_phase_tables_kernel fills first, when it fits (at most 32 GiB and half the free
 // device memory); otherwise each CTA builds its own. True when c->ptab holds them.
 static bool alloc_phase_tables(wem_ctx *c)
@@ -973,7 +973,7 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
     if ((rc = ensure(c->recv, sizeof(float2) * recv_elems)) ||
         (rc = ensure(c->slots, sizeof(float2) * (size_t)grid * nz * nmx)))
         return rc;
-    c->ptab_ok = form != MIG_FORM_SPLIT16 && alloc_phase_tables(c);
+    c->ptab_ok = alloc_phase_tables(c);
     c->last_threads = threads;
     c->last_S = S;
     c->last_grid = grid;

@@ -107,16 +107,27 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                 const float2 *srow = slot + (size_t)iz * nmx;
                 for (int x = tid * 16; x < nmx; x += NT * 16) asm volatile("prefetch.global.L2 [%0];" ::"l"(srow + x));
             }
-            if (PSPI && !TC && a.ptab) {
+            if (PSPI && a.ptab) {
                 // precomputed tables: copied while the rows go through their forward
                 // transforms (the barrier first: the previous depth's tables and exchange
                 // buffers are no longer read)
                 __syncthreads();
-                if constexpr (PSPI && !TC) {
+                if constexpr (PSPI) {
                     copy_tables_async<N, INTERP, PAIR>(a, sm, iwi, iz, tid, NT);
+                    float inv_s = 1.f;
                     if (active) {
-                        if constexpr (PAIR) paired_forward<N>(v, xbuf, sacc, sm.tw, t, sync);
-                        else fft_row<N, -1>(v, xbuf, sm.tw, t, sync);
+                        if constexpr (PAIR) {
+                            paired_forward<N>(v, xbuf, sacc, sm.tw, t, sync);
+                        } else if constexpr (TC) {
+                            // split16: the row enters the transform scaled by a power of two
+                            float sc;
+                            row_scale<T>(v, tc.red, t, sync, sc, inv_s);
+#pragma unroll
+                            for (int m = 0; m < 16; m++) v[m] = cscale(v[m], sc);
+                            fft_row<N, -1, TC>(v, xbuf, sm.tw, t, sync, &tc);
+                        } else {
+                            fft_row<N, -1>(v, xbuf, sm.tw, t, sync);
+                        }
                     }
                     cp_async_wait_all();
                     __syncthreads();
@@ -124,7 +135,8 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                         if constexpr (PAIR)
                             paired_inverse<N>(v, is_src, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz), cx_mask(a, iz));
                         else
-                            step_mig_tail<N, PSPI, INTERP>(v, is_src, a, sm, xbuf, sacc, t, sync, nullptr, ref_mask(a, iz), 1.f);
+                            step_mig_tail<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc, ref_mask(a, iz),
+                                                               inv_s);
                     }
                 }
             } else {

@@ -41,6 +41,24 @@ def test_split16_matches_fp64_oracle(gpu_lib, oracle_mod, pspi, interp):
     assert rel_l2(m32, want64) < TOL
 
 
+@pytest.mark.parametrize("interp", ["ref", "linear"])
+def test_split16_precomputed_phase_tables_bit_identical(gpu_lib, monkeypatch, interp):
+    """The split16 kernel reading the phase tables precomputed for every (frequency, depth)
+    gives the image of tables built in each CTA (WEM_PHASE_TABLES=0) bit for bit."""
+    from wemgpu import synth
+    c = synth.small_case(53, nx=1024, nz=24, nt=128, nshot=3, pspi=1, nref=6, interp=interp, fmax=30.0)
+    p = dict(c["params"], precision="split16")
+    images = []
+    for pt in ("1", "0"):
+        monkeypatch.setenv("WEM_PHASE_TABLES", pt)
+        with gpu_lib.Context() as ctx:
+            ctx.prepare(p, c["vel"], c["wav"])
+            images.append(ctx.migrate(c["shots"]))
+            images.append(ctx.migrate(c["shots"]))  # the captured graph replayed
+    assert np.array_equal(images[0], images[1])
+    assert np.array_equal(images[0], images[2]) and np.array_equal(images[2], images[3])
+
+
 def test_split16_survey_geometry_band_subset(gpu_lib, oracle_mod):
     """The PSPI survey's grid (500 x 1024, nref 8) on 2 shots and a narrow band, both
     CTA shapes of the tensor-core kernel."""
