@@ -172,6 +172,11 @@ def accuracy(c: dict, ctx_factory) -> dict:
                       nthreads=os.cpu_count() or 1).astype(np.float64)
     out = {"sample": f"shot {s}, {band(p)} frequencies ({p['fmin']:g}-{p['fmax']:g} Hz) x {p['nz']} depth steps",
            "oracle": "FP64 restatement of wem.c"}
+    # the floor: the reference's own FP32 arithmetic (the port, bit-identical to the compiled
+    # reference) against the same FP64 operator
+    ref32 = O.wem_port(dict(q, sx=float(shots.sx[s])), c["vel"], c["wav"], d=d, adj=True,
+                       nthreads=os.cpu_count() or 1).astype(np.float64)
+    out["rel_l2_reference_fp32"] = float(np.linalg.norm(ref32 - want) / np.linalg.norm(want))
     for prec in sorted({"fp32", p.get("precision", "fp32")}):
         ctx = ctx_factory()
         try:
@@ -359,6 +364,23 @@ def run_angles(args, c, wl, rank, world, local):
                     "h2d_bytes_per_step": int(c["vel"].nbytes + c["wav"].nbytes),
                     "d2h_bytes_per_step": int(ax.nbytes + ay.nbytes)},
             "clocks": clocks}
+    # roofline of the whole angle step: algorithmic FLOPs per unit (one shot, frequency and
+    # depth step) = the z derivative, a complex product against the nz x nz circular-convolution
+    # matrix (8 nz per sample), + the x derivatives on the row FFT (one forward and three
+    # inverse transforms) + the split-step source step (two transforms, 20 per sample)
+    nmx_a, nz_a = int(p["nmx"]), int(p["nz"])
+    fft_a = 5 * nmx_a * math.log2(nmx_a)
+    fl = 8 * nz_a * nmx_a + 6 * fft_a + 20 * nmx_a
+    ach = units * fl / (ms / 1000.0) / 1e12
+    peaks, src = measured_peaks()
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    props = torch.cuda.get_device_properties(torch.device("cuda", local))
+    fp32_nominal = props.multi_processor_count * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    line["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                        "traffic": None, "peak_source": f"bf16 dense, {src}",
+                        "kernel": "wem_angles_* kernels + the z-derivative GEMM (BF16x9 FP32 emulation), whole step",
+                        "ms_per_launch": ms, "flops_per_unit": fl, "fp32_nominal_tflops": fp32_nominal,
+                        "fp32_frac": ach / fp32_nominal}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # the CPU leg: the oracle's FP64 restatement of compute_angles on one shot, 2 Hz of the band
         import angles_np as A
@@ -474,6 +496,25 @@ def run_lsm(args, ctx, c, wl, units, dev, rank, world, dist):
                    "misfit_host_buffers": [float(x) for x in costs_host],
                    "dot_test": [a, b], "dot_rel": abs(a - b) / abs(a), "model_rel_err": err},
             "clocks": clocks}
+    # roofline of the operator pair: the algorithmic FP32 work of every application (the
+    # migration's count per unit; the exact modelling does the same transforms) over the
+    # device-resident solve's time, against the contract's bf16 peak and the nominal FP32 peak
+    fl = flops_per_unit(p)
+    ach = napply * units * fl / el / 1e12
+    peaks, src = measured_peaks()
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    props = torch.cuda.get_device_properties(dev)
+    fp32_nominal = props.multi_processor_count * 128 * 2 * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+    line["roofline"] = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                        "traffic": None, "peak_source": f"bf16 dense, {src}",
+                        "kernel": "wem_migrate_kernel + wem_model_kernel (41 operator applications)",
+                        "ms_per_launch": 1000.0 * el / napply, "flops_per_unit": fl,
+                        "fp32_nominal_tflops": fp32_nominal, "fp32_frac": ach / fp32_nominal}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # the CPU leg: the reference's algorithm for one operator application (the migration
+        # of one shot, every frequency) on the host cores; the Born modelling costs the same
+        # transforms per unit
+        line["cpu_baseline"] = cpu_baseline(c)
     if rank == 0:
         print(json.dumps(line))
     ctx.close()
