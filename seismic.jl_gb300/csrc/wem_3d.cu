@@ -233,10 +233,13 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
             for (int sl = 0; sl < np; sl++) {
                 const int r1 = plan[1 + 2 * sl], r2 = plan[2 + 2 * sl];
                 float2 *s_tile = s_tile0 + (size_t)(sl & 1) * tile_sz;
+                // w^2 / vref^2 of the pair's references, read once per slot
+                const float wsl1 = r1 >= 0 ? __fmul_rn(w2, a.slow2[(size_t)iz * a.nref + r1]) : 0.f;
+                const float wsl2 = r2 >= 0 ? __fmul_rn(w2, a.slow2[(size_t)iz * a.nref + r2]) : 0.f;
+                const int half_e = (zero_col ? H + 1 : H) * HALF;
                 // every thread is past the previous slot's products before its tables change
                 __syncthreads();
-                for (int e = tid; e < 2 * (zero_col ? H + 1 : H) * HALF; e += NT) {
-                    const int half_e = (zero_col ? H + 1 : H) * HALF;
+                for (int e = tid; e < 2 * half_e; e += NT) {
                     const int which = e >= half_e ? 1 : 0, ee = e - which * half_e;
                     const int rr = ee / HALF, kk = ee - rr * HALF;
                     const int r = which ? r2 : r1;
@@ -244,8 +247,7 @@ __global__ void __launch_bounds__(ColShape<NX>::NT) wem3d_cols_kernel(const Mig3
                     const int kyi = rr < H ? col_ky(blk, rr, H, nky) : 0;
                     const float ky = __fmul_rn(a.dky, (float)kyi);
                     const float kx = __fmul_rn(a.dkx, (float)kk);
-                    const float slow2 = a.slow2[(size_t)iz * a.nref + r];
-                    const float s2 = __fsub_rn(__fsub_rn(__fmul_rn(w2, slow2), __fmul_rn(kx, kx)), __fmul_rn(ky, ky));
+                    const float s2 = __fsub_rn(__fsub_rn(which ? wsl2 : wsl1, __fmul_rn(kx, kx)), __fmul_rn(ky, ky));
                     float2 P;
                     if (s2 >= 0.f) {
                         float sn, cs;
