@@ -440,6 +440,13 @@ __global__ void __launch_bounds__(256, 2) wem3d_rows_inv_kernel(const Mig3dArgs 
                     float2 u[16];
 #pragma unroll
                     for (int m = 0; m < 16; m++) u[m] = crow[t + TY * m];
+                    // the next plane's row (or the next item's first) to L2 while this one is
+                    // transformed: 128 bytes per thread cover the row (NY samples, NY/16 threads)
+                    if (pl + 1 < np || item + 1 < it1) {
+                        const float2 *nrow = pl + 1 < np ? crow + (size_t)nmx * nky
+                                                         : a.C + ((((size_t)(item + 1) * 2 + w) * nref) * nmx + x) * nky;
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(nrow + 16 * t));
+                    }
                     fft_row<NY, +1>(u, xbuf, s_tw, t, sync);
                     if (plan) {
                         const int r1 = plan[1 + 2 * pl], r2 = plan[2 + 2 * pl];
