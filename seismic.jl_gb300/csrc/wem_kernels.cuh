@@ -272,30 +272,42 @@ __global__ void __launch_bounds__(S * (N / 16), N <= 1024 ? 2 : 1) wem_model_ker
         // receiver, upward with injection (wem.c:266-276)
 #pragma unroll
         for (int m = 0; m < 16; m++) v[m] = make_float2(0.f, 0.f);
+        // injection of m * smig at depth iz (wem.c:270-272): registers and global memory only
+        auto inject = [&](int iz) {
+            const float2 *row = smig + (size_t)iz * nmx;
+            const float *mr = b.img + (size_t)iz * nmx;
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int x = t + T * m;
+                if (x < nmx) {
+                    const float mv = mr[x];
+                    const float2 s_ = row[x];
+                    v[m].x += mv * s_.x;
+                    v[m].y += mv * s_.y;
+                }
+            }
+        };
         for (int iz = nz - 1; iz >= 0; iz--) {
+            const bool rec = (a.zflag[iz] & Z_REC) != 0;
+            if (iz > 0 && 8 * t < nmx) {
+                // the next depth's source and image rows to L2 (64 bytes of each per thread)
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(smig + (size_t)(iz - 1) * nmx + 8 * t));
+                if (16 * t < nmx) asm volatile("prefetch.global.L2 [%0];" ::"l"(b.img + (size_t)(iz - 1) * nmx + 16 * t));
+            }
             __syncthreads();
             if (PSPI && a.ptab) {
                 if constexpr (PSPI) {
+                    // the tables copied while this depth's injection loads its rows
                     copy_tables_async<N, INTERP, false>(a, sm, iwi, iz, tid, NT);
+                    if (rec) inject(iz);
                     cp_async_wait_all();
                 }
             } else {
                 build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
             }
             __syncthreads();
-            if (a.zflag[iz] & Z_REC) {
-                const float2 *row = smig + (size_t)iz * nmx;
-                const float *mr = b.img + (size_t)iz * nmx;
-#pragma unroll
-                for (int m = 0; m < 16; m++) {
-                    const int x = t + T * m;
-                    if (x < nmx) {
-                        const float mv = mr[x];
-                        const float2 s_ = row[x];
-                        v[m].x += mv * s_.x;
-                        v[m].y += mv * s_.y;
-                    }
-                }
+            if (rec) {
+                if (!(PSPI && a.ptab)) inject(iz);
                 step_model<N, PSPI, INTERP, EXACT>(v, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz));
             }
         }
