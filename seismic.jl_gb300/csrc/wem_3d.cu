@@ -89,6 +89,17 @@ __global__ void __launch_bounds__(256) wem3d_rows_fwd_kernel(const Mig3dArgs a)
                 }
             }
         }
+        {
+            // the team's next row to L2 while this one is transformed (64 bytes per thread)
+            const long long nj = job + (long long)gridDim.x * TEAMS;
+            if (nj < njobs && 8 * t < a.nmy) {
+                const int item_n = (int)(nj / (2 * a.nmx));
+                const int rem_n = (int)(nj - (long long)item_n * 2 * a.nmx);
+                const int w_n = rem_n / a.nmx, x_n = rem_n - w_n * a.nmx;
+                const float2 *nrow = a.U + ((size_t)item_n * 2 + w_n) * n + (size_t)x_n * a.nmy;
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(nrow + 8 * t));
+            }
+        }
         fft_row<NY, -1>(v, xbuf, s_tw, t, sync);
         float2 *yrow = a.Y + (((size_t)item * 2 + w) * a.nmx + x) * NY;
 #pragma unroll
