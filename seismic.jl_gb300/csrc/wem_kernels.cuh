@@ -155,6 +155,12 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
 
             // ---- imaging condition (wem.c:243-247), summed over the group's shots
             if (zf & Z_REC) {
+                // this thread's first two accumulator entries (x = tid, tid + NT), loaded now so
+                // that their latency passes behind the two barriers below; only this thread
+                // touches them
+                float2 *srow = slot + (size_t)iz * nmx;
+                const float2 acc0 = tid < nmx ? srow[tid] : make_float2(0.f, 0.f);
+                const float2 acc1 = tid + NT < nmx ? srow[tid + NT] : make_float2(0.f, 0.f);
                 if (is_src) {
 #pragma unroll
                     for (int m = 0; m < 16; m++) {
@@ -176,12 +182,11 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                     }
                 }
                 __syncthreads();
-                float2 *srow = slot + (size_t)iz * nmx;
-                for (int x = tid; x < nmx; x += NT) {
+                for (int x = tid, k = 0; x < nmx; x += NT, k++) {
                     float c = 0.f;
 #pragma unroll
                     for (int s_ = 0; s_ < S; s_++) c += reinterpret_cast<const float *>(sm.x + (size_t)(S + s_) * PADN)[x];
-                    kahan_add(&srow[x], c);
+                    kahan_add(&srow[x], c, k == 0 ? acc0 : (k == 1 ? acc1 : srow[x]));
                 }
                 tables_free = true;
             } else {

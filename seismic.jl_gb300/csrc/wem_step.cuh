@@ -34,15 +34,15 @@ __device__ __forceinline__ float2 phase_entry(float w2, float slow2, float kx, f
     return make_float2(P.x * inv_n, P.y * inv_n);
 }
 
-__device__ __forceinline__ void kahan_add(float2 *slot, float v)
+__device__ __forceinline__ void kahan_add(float2 *slot, float v, float2 s)
 {
-    float2 s = *slot;
     const float y = __fsub_rn(v, s.y);
     const float t = __fadd_rn(s.x, y);
     s.y = __fsub_rn(__fsub_rn(t, s.x), y);
     s.x = t;
     *slot = s;
 }
+__device__ __forceinline__ void kahan_add(float2 *slot, float v) { kahan_add(slot, v, *slot); }
 
 // ------------------------------------------------------------------ shared pieces
 template <int N> struct MigShape {
