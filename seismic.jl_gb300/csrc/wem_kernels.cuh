@@ -110,10 +110,12 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
             if (PSPI && a.ptab) {
                 // precomputed tables: copied while the rows go through their forward
                 // transforms (the barrier first: the previous depth's tables and exchange
-                // buffers are no longer read)
+                // buffers are no longer read); the depth's reference masks are loaded before
+                // the barrier, which hides their latency
+                const unsigned long long um = ref_mask(a, iz), cm = PAIR ? cx_mask(a, iz) : 0ull;
                 __syncthreads();
                 if constexpr (PSPI) {
-                    copy_tables_async<N, INTERP, PAIR>(a, sm, iwi, iz, tid, NT);
+                    copy_tables_async<N, INTERP, PAIR>(a, sm, iwi, iz, tid, NT, um);
                     float inv_s = 1.f;
                     if (active) {
                         if constexpr (PAIR) {
@@ -133,10 +135,9 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                     __syncthreads();
                     if (active) {
                         if constexpr (PAIR)
-                            paired_inverse<N>(v, is_src, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz), cx_mask(a, iz));
+                            paired_inverse<N>(v, is_src, a, sm, xbuf, sacc, t, sync, um, cm);
                         else
-                            step_mig_tail<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc, ref_mask(a, iz),
-                                                               inv_s);
+                            step_mig_tail<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc, um, inv_s);
                     }
                 }
             } else {

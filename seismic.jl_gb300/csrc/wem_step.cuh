@@ -526,12 +526,12 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 template <int N, int INTERP, bool PAIR>
 __device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N, true> &sm, int iwi, int iz, int tid,
-                                                  int nthreads)
+                                                  int nthreads, unsigned long long used)
 {
     constexpr int PHS = MigShape<N>::PHS, CH = PHS / 2;  // 16-byte chunks per table
     const float4 *src = reinterpret_cast<const float4 *>(a.ptab + ((size_t)iwi * a.nz + iz) * a.nref * PHS);
     float4 *dst = reinterpret_cast<float4 *>(sm.ph);
-    unsigned long long used = ref_mask(a, iz) & (a.nref >= 64 ? ~0ull : ((1ull << a.nref) - 1ull));
+    used &= (a.nref >= 64 ? ~0ull : ((1ull << a.nref) - 1ull));
     while (used) {
         const int r = __ffsll((long long)used) - 1;
         used &= used - 1ull;
@@ -548,6 +548,12 @@ __device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N
     if (PAIR && tid < 2)
         cp_async16(reinterpret_cast<float4 *>(sm.wpos) + tid, reinterpret_cast<const float4 *>(a.wpos + (size_t)iz * WPOS_STRIDE) + tid);
     cp_async_commit();
+}
+template <int N, int INTERP, bool PAIR>
+__device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N, true> &sm, int iwi, int iz, int tid,
+                                                  int nthreads)
+{
+    copy_tables_async<N, INTERP, PAIR>(a, sm, iwi, iz, tid, nthreads, ref_mask(a, iz));
 }
 
 // One upward step of the modelling recursion (wem.c:273-274, -dz, adj=false), in
