@@ -167,6 +167,11 @@ WEM_API int wem_last_kernel_times(wem_ctx *ctx, float *ms_spectra, float *ms_ext
    *ms how long the launch took; the context of the device stays usable. */
 WEM_API int wem_selftest_wait_timeout(int device, int *timed_out, float *ms);
 
+/* Measured FP32 FMA throughput of `device` in TFLOP/s (no counterpart in the reference):
+   the best of three ~40 ms launches of a kernel of independent FMA chains, 2 FLOPs per
+   FMA. The denominator of the CUDA-core roofline of the depth kernels. */
+WEM_API int wem_measure_fp32_peak(int device, double *tflops);
+
 /* How the last 2-D wem_migrate* call ran its depth recursion (no counterpart in the
    reference): threads per CTA, shots sharing one CTA's phase tables, CTAs launched,
    whether the call replayed a captured CUDA graph of the whole launch sequence (1) or
@@ -181,19 +186,24 @@ WEM_API int wem_ctx_stream(wem_ctx *ctx, void **stream);
    For callers that cannot call cudaMalloc/cudaFree while they run (an application that
    gives all device memory to its own pool at start-up, or a loop with a fixed memory
    budget): the caller passes device buffers for every input and the output, and all
-   working memory comes from one fixed 24 MiB device array inside the library, which
-   every GPU that loads shotwem.so holds until the process exits.
+   working memory comes from one fixed 24 MiB device array inside the library. CUDA
+   loads that array (and the code of the kernels the call launches) on a device when
+   the library's module is first used there (lazy module loading, CUDA's default), and
+   the device keeps it until the process exits: make one small call on each device
+   before handing the rest of its memory to a pool of your own, or run with
+   CUDA_MODULE_LOADING=EAGER.
    vel_dev [nmx][nz], wav_dev [nt], d_dev [nshot][nmx][nt] (every shot on the full
    grid), m_dev [nmx][nz] (overwritten); sx, sy: host arrays of nshot source
    positions (sy may be NULL); stream: a cudaStream_t or NULL; the call returns when
    the result is in m_dev. 2-D only; padx*nmx in {256, 512, 1024, 2048}; nmx, nz <= 1024;
    nref <= 16; nshot <= 64; and the tables (12*nz*nmx bytes), trace spectra
    (8*nshot*nfreq*nmx bytes) and image (4*nz*nmx bytes) must fit the 24 MiB together --
-   larger surveys return WEM_ERR_SIZE. The first call on a device (made current by the
-   caller) looks up the array's device address; make that first call before any stream
-   capture. Calls share the array: calls that overlap on the GPU (other streams, other
-   host threads) race and corrupt each other. The image is summed with atomic additions,
-   so its last bits can vary from run to run. */
+   larger surveys return WEM_ERR_SIZE. Every call looks up the array's device address on
+   the current device (the first call on a device also loads it there); make that first
+   call before any stream capture. Each call waits for its stream (cudaStreamSynchronize)
+   before it returns. Calls share the array: calls that overlap on the GPU (other
+   streams, other host threads) race and corrupt each other. The image is summed with
+   atomic additions, so its last bits can vary from run to run. */
 WEM_API int wem_migrate_noalloc(const wem_params *p, const float *vel_dev, const float *wav_dev, int nshot,
                                 const float *sx, const float *sy, const float *d_dev, float *m_dev, void *stream);
 

@@ -50,20 +50,24 @@ def build(force: bool = False) -> str:
     return LIB_PATH
 
 
-# where the reference's sources lie in the build container (the recipe reads them there)
-REF_ROOT = os.environ.get("WEM_REFERENCE_ROOT", "/root/reference")
+_ref_present = None
 
 
 def ref_sources_available() -> bool:
-    return os.path.exists(os.path.join(REF_ROOT, "src", "Imaging", "c", "wem.c"))
+    """Whether the reference's sources exist on this machine; the recipe (oracle/Makefile,
+    REF= or WEM_REFERENCE_ROOT) is the one place that knows where they lie."""
+    global _ref_present
+    if _ref_present is None:
+        _ref_present = subprocess.run(["make", "-s", "-C", HERE, "ref-present"],
+                                      stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL).returncode == 0
+    return _ref_present
 
 
 def build_ref() -> str | None:
     """Compile the reference C core into oracle/_ref when its sources exist."""
-    ref_root = REF_ROOT
     if not ref_sources_available():
         return None
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
     return REF_LIB_PATH
 
 

@@ -233,6 +233,169 @@ __global__ void __launch_bounds__(256) wem_angles_xderiv_fft_kernel(const AngleX
     }
 }
 
+// ------------------------------------------------------------------ 2'. derivative convolutions
+// A derivative along an axis of L samples (any L <= 2048) is the circular convolution of
+// each line with w = IDFT_L(i k mask) * scale (the reference's 3-D transform is separable
+// and i k acts on one axis). It runs on M-point rows, M the power of two >= 2L - 1: the line
+// zero-padded to M, FFT_M, times H = FFT_M(g) / M with g = w placed at j and M - j (the
+// M-point circular convolution then equals the L-point one on the first L outputs), inverse
+// FFT_M. Up to three transfer functions (u_x, u_left, u_right) share one forward transform.
+template <int M>
+__device__ __forceinline__ void conv_line(const float2 (&X)[16], const float2 *H, float2 (&u)[16], float2 *xbuf,
+                                          const float2 *tw, int t, unsigned sync)
+{
+    constexpr int T = M / 16;
+#pragma unroll
+    for (int m = 0; m < 16; m++) u[m] = c_mul(X[m], __ldg(H + t + T * m));
+    fft_row<M, +1>(u, xbuf, tw, t, sync);
+}
+
+// Lines of L contiguous samples ([line][L]); one team of M/16 threads per line, 256 threads.
+template <int M>
+__global__ void __launch_bounds__(256) wem_angles_conv_rows_kernel(const AngleConvArgs a)
+{
+    constexpr int T = M / 16, TEAMS = 256 / T < 1 ? 1 : 256 / T, NT = TEAMS * T;
+    constexpr int TW = fft_tw_size<M>(), TWP = (TW + 1) & ~1;
+    extern __shared__ float4 smem_raw[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
+    const int tid = threadIdx.x, team = tid / T, t = tid - team * T;
+    float2 *xbuf = s_tw + TWP + (size_t)team * pad16(M);
+    const unsigned sync = team_sync_handle<M>(tid);
+    for (int i = tid; i < TW; i += NT) s_tw[i] = a.tw[i];
+    __syncthreads();
+    const int L = a.L;
+    for (long long l = (long long)blockIdx.x * TEAMS + team; l < a.nlines; l += (long long)gridDim.x * TEAMS) {
+        const float2 *in = a.u + (size_t)l * L;
+        float2 X[16];
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            X[m] = x < L ? in[x] : make_float2(0.f, 0.f);
+        }
+        fft_row<M, -1>(X, xbuf, s_tw, t, sync);
+#pragma unroll 1
+        for (int o = 0; o < a.nout; o++) {
+            float2 u[16];
+            conv_line<M>(X, a.H + (size_t)o * M, u, xbuf, s_tw, t, sync);
+            float2 *out = a.out[o] + (size_t)l * L;
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int x = t + T * m;
+                if (x < L) out[x] = u[m];
+            }
+        }
+    }
+}
+
+// Lines strided across planes: plane p holds L rows of `cols` samples ([p][L][cols]), line
+// (p, c) is column c of plane p. A CTA stages a tile of TX adjacent columns of one plane in
+// shared memory with coalesced loads along the rows (row pitch TX + 1: conflict-free
+// column reads), each of its TX teams transforms one column, and the results leave the
+// same way. 512 threads.
+template <int M>
+__global__ void __launch_bounds__(512) wem_angles_conv_cols_kernel(const AngleConvArgs a)
+{
+    constexpr int T = M / 16, TX = 512 / T < 1 ? 1 : 512 / T, NT = TX * T, P = TX + 1;
+    constexpr int TW = fft_tw_size<M>(), TWP = (TW + 1) & ~1;
+    extern __shared__ float4 smem_raw[];
+    float2 *s_tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *s_x = s_tw + TWP;
+    float2 *tile = s_x + (size_t)TX * pad16(M);
+    const int tid = threadIdx.x, team = tid / T, t = tid - team * T;
+    float2 *xbuf = s_x + (size_t)team * pad16(M);
+    const unsigned sync = team_sync_handle<M>(tid);
+    for (int i = tid; i < TW; i += NT) s_tw[i] = a.tw[i];
+    const int L = a.L, cols = a.cols;
+    const int ntile = (cols + TX - 1) / TX;
+    const long long nplanes = a.nlines / cols;
+    for (long long b = blockIdx.x; b < nplanes * ntile; b += gridDim.x) {
+        const long long pl = b / ntile;
+        const int c0 = (int)(b - pl * ntile) * TX;
+        const size_t base = (size_t)pl * L * cols;
+        __syncthreads();  // the previous tile is written out
+        for (int e = tid; e < L * TX; e += NT) {
+            const int z = e / TX, j = e - z * TX;
+            tile[z * P + j] = c0 + j < cols ? a.u[base + (size_t)z * cols + c0 + j] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        float2 X[16];
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int z = t + T * m;
+            X[m] = z < L ? tile[z * P + team] : make_float2(0.f, 0.f);
+        }
+        fft_row<M, -1>(X, xbuf, s_tw, t, sync);
+#pragma unroll 1
+        for (int o = 0; o < a.nout; o++) {
+            float2 u[16];
+            conv_line<M>(X, a.H + (size_t)o * M, u, xbuf, s_tw, t, sync);
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int z = t + T * m;
+                if (z < L) tile[z * P + team] = u[m];  // only this team touches its column
+            }
+            __syncthreads();
+            float2 *out = a.out[o];
+            for (int e = tid; e < L * TX; e += NT) {
+                const int z = e / TX, j = e - z * TX;
+                if (c0 + j < cols) out[base + (size_t)z * cols + c0 + j] = tile[z * P + j];
+            }
+            __syncthreads();  // the tile is read out before the next output overwrites it
+        }
+    }
+}
+
+template <int M> static int launch_conv(const AngleConvArgs &a, int nsm, cudaStream_t st)
+{
+    constexpr int T = M / 16;
+    constexpr int TWP = (fft_tw_size<M>() + 1) & ~1;
+    if (a.cols > 1) {
+        constexpr int TX = 512 / T < 1 ? 1 : 512 / T;
+        const size_t smem = sizeof(float2) * ((size_t)TWP + (size_t)TX * pad16(M) + (size_t)a.L * (TX + 1));
+        if (cudaFuncSetAttribute(wem_angles_conv_cols_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return -1;
+        const long long tiles = a.nlines / a.cols * ((a.cols + TX - 1) / TX);
+        const long long grid = tiles < (long long)nsm * 8 ? tiles : (long long)nsm * 8;
+        wem_angles_conv_cols_kernel<M><<<(unsigned)(grid > 0 ? grid : 1), TX * T, smem, st>>>(a);
+    } else {
+        constexpr int TEAMS = 256 / T < 1 ? 1 : 256 / T;
+        const size_t smem = sizeof(float2) * ((size_t)TWP + (size_t)TEAMS * pad16(M));
+        if (cudaFuncSetAttribute(wem_angles_conv_rows_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return -1;
+        long long blocks = (a.nlines + TEAMS - 1) / TEAMS;
+        if (blocks > (long long)nsm * 16) blocks = (long long)nsm * 16;
+        wem_angles_conv_rows_kernel<M><<<(unsigned)(blocks > 0 ? blocks : 1), 256, smem, st>>>(a);
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int angles_conv_length(int L)
+{
+    if (L < 1 || L > 2048) return 0;
+    int m = 32;
+    while (m < 2 * L - 1) m *= 2;
+    return m;
+}
+
+int launch_angles_conv(const AngleConvArgs &a, int nsm, cudaStream_t st)
+{
+    if (a.nlines <= 0) return 0;
+    if (a.cols > 1 && a.nlines % a.cols) return -2;
+    switch (angles_conv_length(a.L)) {
+    case 32: return launch_conv<32>(a, nsm, st);
+    case 64: return launch_conv<64>(a, nsm, st);
+    case 128: return launch_conv<128>(a, nsm, st);
+    case 256: return launch_conv<256>(a, nsm, st);
+    case 512: return launch_conv<512>(a, nsm, st);
+    case 1024: return launch_conv<1024>(a, nsm, st);
+    case 2048: return launch_conv<2048>(a, nsm, st);
+    case 4096: return launch_conv<4096>(a, nsm, st);
+    default: return -2;
+    }
+}
+
 // ------------------------------------------------------------------ 3. accumulation
 // One thread per grid point (x, z), frequencies in order; out [nmx][nz].
 __global__ void __launch_bounds__(256) wem_angles_accum_kernel(const AngleAccumArgs a)

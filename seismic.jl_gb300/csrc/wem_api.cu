@@ -6,7 +6,6 @@
 // runs on the GPU: trace spectra (wem_spectra_kernel), the fused depth recursion
 // (wem_migrate_kernel) and the image reduction (wem_image_reduce_kernel).
 // There is no CPU fallback: without a CUDA device every entry point fails.
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdarg.h>
@@ -81,18 +80,22 @@ struct wem_ctx {
     wem_params p{};
     int ntfft = 0, nw = 0, nf = 0, ifmin = 0, ifmax = 0, nwf = 0, nkx = 0, nky = 0;
     float dw = 0.f, dkx = 0.f, dky = 0.f;
+    // 2-D rows: the depth kernels' row length nfft (= nkx, or for an nkx that is not a power
+    // of two the power of two >= 2 nkx - 1 that carries it in Bluestein's chirp form, blu)
+    int nfft = 0;
+    bool blu = false;
+    int chirp_off = 0, bfft_off = 0;  // offsets of the chirp and G/N tables in twid (blu)
 
     // per-velocity tables
     DevBuf vref, slow2, po, pd, sel, wlin, taper, zflag, twid, wtab, scale_recv, scale_src, srcw, wav, wav_base;
+    DevBuf vref64;                // [nz][nref] reference velocities in double (split16 FP64 phase tables)
+    double dkx64 = 0.0;
     DevBuf ssyn_ref, ssyn_exact;  // synthesis weights w^2 * (half-spectrum | image) factor
     DevBuf tapery, twy;           // 3-D: y taper and y-FFT twiddles
     DevBuf tcw, tcerr;            // split16: W operands of the tensor-core DFT stages, timeout word
     DevBuf wposb;                 // [nz][WPOS_STRIDE] points taking their wavefield whole (paired form)
     DevBuf plan3;                 // [nz][PLAN3_STRIDE] 3-D paired planes (empty: one plane per reference)
-    cublasHandle_t blas = nullptr;  // the incidence angles' derivative GEMMs
     DevBuf ang_vol[7];              // 2-D angles: the batch's volumes (u, u_x, u_l, u_r, u_z, u planes) and angles
-    int blas_compute = -1;          // their cuBLAS compute type once chosen (complex operands)
-    int blas_real_compute = -1;     // the same for the planar (real) form
     DevBuf dsum3;                 // 3-D direct sums: [item][2][WHOLE_MAX][nky] column sums
     bool plan3_ok = false;
     DevBuf selbp;                 // [nz][nmx rounded up to 16] selection rows (precomputed-table path)
@@ -181,7 +184,6 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
     for (DevBuf &b : c->ang_vol)
         if (b.p) cudaFree(b.p);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
-    if (c->blas) cublasDestroy(c->blas);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     for (int i = 0; i < 4; i++)
@@ -221,6 +223,34 @@ extern "C" int wem_selftest_wait_timeout(int device, int *timed_out, float *ms)
         cudaMemcpy(timed_out, d, sizeof(int), cudaMemcpyDeviceToHost))
         rc = fail(WEM_ERR_CUDA, "wem_selftest_wait_timeout: %s", cudaGetErrorString(cudaGetLastError()));
     if (!rc && ms) cudaEventElapsedTime(ms, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(d);
+    return rc;
+}
+
+extern "C" int wem_measure_fp32_peak(int device, double *tflops)
+{
+    if (!tflops) return fail(WEM_ERR_ARG, "wem_measure_fp32_peak: null argument");
+    CK(cudaSetDevice(device));
+    int nsm = 0;
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+    const int grid = 2 * nsm, iters = 20000;  // 2 CTAs of 512 threads per SM, ~40 ms
+    float *d = nullptr;
+    CK(cudaMalloc(&d, sizeof(float) * (size_t)grid * 512));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = WEM_OK;
+    float best = 0.f;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = fail(WEM_ERR_CUDA, "event");
+    for (int rep = 0; rep < 4 && !rc; rep++) {  // the first launch warms up; the best of the rest counts
+        float ms = 0.f;
+        if (cudaEventRecord(e0, 0) || launch_fma_probe(d, iters, grid, 0) || cudaEventRecord(e1, 0) ||
+            cudaEventSynchronize(e1) || cudaEventElapsedTime(&ms, e0, e1))
+            rc = fail(WEM_ERR_CUDA, "wem_measure_fp32_peak: %s", cudaGetErrorString(cudaGetLastError()));
+        else if (rep > 0 && ms > 0.f && (best == 0.f || ms < best))
+            best = ms;
+    }
+    if (!rc) *tflops = 2.0 * 64.0 * iters * (double)grid * 512.0 / (best * 1e-3) / 1e12;
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     cudaFree(d);
@@ -281,6 +311,73 @@ static void freq_grid(const wem_params &p, int *ntfft, int *nw, int *ifmin, int 
 
 static int is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
+// In-place radix-2 FFT of n = re.size() (a power of two) complex doubles, sign -1 forward.
+static void fft_pow2_double(std::vector<double> &re, std::vector<double> &im, int sign)
+{
+    const int n = (int)re.size();
+    for (int i = 1, j = 0; i < n; i++) {
+        int bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) {
+            std::swap(re[i], re[j]);
+            std::swap(im[i], im[j]);
+        }
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+        const double ang = sign * 6.283185307179586476925286766559 / len;
+        for (int k = 0; k < len / 2; k++) {
+            const double wr = cos(ang * k), wi = sin(ang * k);
+            for (int i = k; i < n; i += len) {
+                const int j = i + len / 2;
+                const double xr = re[j] * wr - im[j] * wi, xi = re[j] * wi + im[j] * wr;
+                re[j] = re[i] - xr;
+                im[j] = im[i] - xi;
+                re[i] += xr;
+                im[i] += xi;
+            }
+        }
+    }
+}
+
+// Tables of a length-L transform on N-point rows in Bluestein's chirp form (xform in
+// wem_step.cuh): chirp[n] = e^{i pi n^2 / L}, n < L (n^2 reduced mod 2L in integers, then
+// the angle in double), and gq = G / N with G the forward N-point FFT (double precision) of
+// the chirp placed at n and N - n (N >= 2L - 1, so the two copies do not overlap).
+static void bluestein_tables(int L, int N, float2 *chirp, float2 *gq)
+{
+    std::vector<double> gr(N, 0.0), gi(N, 0.0);
+    for (int n = 0; n < L; n++) {
+        const long long r = ((long long)n * n) % (2LL * L);
+        const double ang = 3.14159265358979323846264338327950288 * (double)r / (double)L;
+        const double cr = cos(ang), ci = sin(ang);
+        chirp[n] = make_float2((float)cr, (float)ci);
+        gr[n] = cr;
+        gi[n] = ci;
+        if (n > 0) {
+            gr[N - n] = cr;
+            gi[N - n] = ci;
+        }
+    }
+    fft_pow2_double(gr, gi, -1);
+    for (int q = 0; q < N; q++) gq[q] = make_float2((float)(gr[q] / N), (float)(gi[q] / N));
+}
+
+// The 2-D row length of the depth kernels for a transform of length nkx: nkx itself when it
+// is a power of two in [32, 4096]; otherwise (Bluestein) the smallest power of two >= 2 nkx - 1,
+// when that is at most 4096; 0 when neither fits.
+static int row_length_2d(int nkx, bool *blu)
+{
+    *blu = false;
+    if (is_pow2(nkx)) return (nkx >= 32 && nkx <= 4096) ? nkx : 0;
+    if (nkx < 9) return 0;
+    int n = 32;
+    while (n < 2 * nkx - 1) n *= 2;
+    if (n > 4096) return 0;
+    *blu = true;
+    return n;
+}
+
 // boundary_condition weights along one axis (wem.c:546-564), in the reference's float
 // expressions (lm = 30 points from each edge when the axis has more than 100)
 static std::vector<float> taper_of(int nm)
@@ -315,9 +412,14 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     if (p.precision == WEM_PREC_SPLIT16 && (p.nmy != 1 || nkx != 2048))
         return fail(WEM_ERR_SIZE, "split16 (tensor-core) migration is built for 2-D rows of nkx = padx*nmx = 2048 "
                                   "(have nmy=%d, nkx=%d)", p.nmy, nkx);
+    bool blu = false;
+    const int nfft = p.nmy == 1 ? row_length_2d(nkx, &blu) : nkx;
     if (p.nmy == 1) {
-        if (!is_pow2(nkx) || nkx < 32 || nkx > 4096)
-            return fail(WEM_ERR_SIZE, "nkx = padx*nmx = %d must be a power of two in [32, 4096]", nkx);
+        if (!nfft)
+            return fail(WEM_ERR_SIZE, "nkx = padx*nmx = %d: 2-D rows take a power of two in [32, 4096] or any other "
+                                      "length in [9, 2048]", nkx);
+        if (blu && p.precision != WEM_PREC_FP32)
+            return fail(WEM_ERR_SIZE, "nkx = %d is not a power of two: FP32 precision only", nkx);
     } else if (!m3d_supported(nkx, nky)) {
         return fail(WEM_ERR_SIZE, "3-D: padx*nmx = %d and padx*nmy = %d must be powers of two in [64, 1024]", nkx, nky);
     } else if (!(p.dmy > 0)) {
@@ -336,6 +438,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     // Device layouts are depth-major ([iz][ix]) so that a depth step reads a row.
     std::vector<float> po(nz), pd((size_t)nz * n), vref((size_t)nz * nref), wl((size_t)nz * n, 0.f);
     std::vector<float> slow2((size_t)nz * nref);
+    std::vector<double> vref64((size_t)nz * nref);
     std::vector<uint8_t> sel((size_t)nz * n);
     // points taking their wavefield whole, listed where a depth has at most WHOLE_MAX (their
     // references then pair like the others, and the imaginary parts come from direct sums)
@@ -361,6 +464,8 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
             const float vr = nref > 1 ? vmin + (float)ir * (vmax - vmin) / ((float)nref - 1) : vmin;
             vref[(size_t)iz * nref + ir] = vr;
             slow2[(size_t)iz * nref + ir] = 1 / (vr * vr);  // the float expression of wem.c:434
+            vref64[(size_t)iz * nref + ir] =
+                nref > 1 ? (double)vmin + (double)ir * ((double)vmax - (double)vmin) / (double)(nref - 1) : (double)vmin;
         }
         for (int ix = 0; ix < n; ix++) {
             const float v = vel[(size_t)ix * nz + iz];
@@ -408,15 +513,23 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         const float z = p.oz + p.dz * iz;
         zf[iz] = (uint8_t)((z >= p.sz ? Z_SRC : 0) | (z >= p.gz ? Z_REC : 0));
     }
-    const int ntw = twiddle_table_size(nkx);
+    const int ntw = twiddle_table_size(nfft);
     std::vector<float2> tw(ntw > 0 ? ntw : 1);
-    twiddle_table_host(nkx, tw.data());
+    twiddle_table_host(nfft, tw.data());
     // then e^{+2 pi i e / nkx}, e = 0 .. nkx/2 (FP64-built): the direct sums of the paired form
     c->wdot_off = (int)tw.size();
     tw.resize(tw.size() + nkx / 2 + 1);
     for (int e = 0; e <= nkx / 2; e++) {
         const double ang = 6.283185307179586476925 * (double)e / (double)nkx;
         tw[(size_t)c->wdot_off + e] = make_float2((float)cos(ang), (float)sin(ang));
+    }
+    // then, for a row length that is not a power of two, the chirp (nkx entries, padded to an
+    // even count) and G/N (nfft entries) of Bluestein's form
+    if (blu) {
+        c->chirp_off = (int)tw.size();
+        c->bfft_off = c->chirp_off + ((nkx + 1) & ~1);
+        tw.resize((size_t)c->bfft_off + nfft);
+        bluestein_tables(nkx, nfft, &tw[c->chirp_off], &tw[c->bfft_off]);
     }
     const int ntwy = p.nmy > 1 ? twiddle_table_size(nky) : 1;
     std::vector<float2> twy(ntwy > 0 ? ntwy : 1);
@@ -448,7 +561,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
 
     int rc;
     if ((rc = ensure(c->po, sizeof(float) * nz)) || (rc = ensure(c->pd, sizeof(float) * pd.size())) ||
-        (rc = ensure(c->vref, sizeof(float) * vref.size())) ||
+        (rc = ensure(c->vref, sizeof(float) * vref.size())) || (rc = ensure(c->vref64, sizeof(double) * vref64.size())) ||
         (rc = ensure(c->slow2, sizeof(float) * slow2.size())) || (rc = ensure(c->sel, sel.size())) ||
         (rc = ensure(c->wlin, sizeof(float) * wl.size())) || (rc = ensure(c->taper, sizeof(float) * nmx)) ||
         (rc = ensure(c->zflag, nz)) || (rc = ensure(c->twid, sizeof(float2) * tw.size())) ||
@@ -516,6 +629,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     CK(cudaMemcpyAsync(c->po.p, po.data(), sizeof(float) * nz, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->pd.p, pd.data(), sizeof(float) * pd.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->vref.p, vref.data(), sizeof(float) * vref.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->vref64.p, vref64.data(), sizeof(double) * vref64.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->slow2.p, slow2.data(), sizeof(float) * slow2.size(), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(c->sel.p, sel.data(), sel.size(), cudaMemcpyHostToDevice, st));
     if (p.nmy == 1) {  // selection rows and weights padded to 16 bytes (asynchronous table copies)
@@ -571,8 +685,11 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     c->nwf = nwf;
     c->nkx = nkx;
     c->nky = nky;
+    c->nfft = nfft;
+    c->blu = blu;
     c->dw = dw;
     c->dkx = 2 * 3.141592653589793 / ((float)nkx) / p.dmx;
+    c->dkx64 = 2 * 3.141592653589793 / ((double)nkx * (double)p.dmx);
     c->dky = 2 * 3.141592653589793 / ((float)nky) / p.dmy;
     c->prepared = true;
     c->prep_gen++;
@@ -646,11 +763,12 @@ static int tcmode(const wem_ctx *c) { return c->p.precision == WEM_PREC_SPLIT16 
 static int mig_form(const wem_ctx *c, int wide)
 {
     const wem_params &p = c->p;
+    if (c->blu) return MIG_FORM_BLU;
     if (tcmode(c)) return MIG_FORM_SPLIT16;
     if (c->paired && p.pspi && p.interp == WEM_INTERP_REF) {
         int S, th;
         size_t smem;
-        if (!migrate_config(c->nkx, wide, p.pspi, p.interp, p.nmx, p.nref, &S, &th, &smem, MIG_FORM_PAIRED) &&
+        if (!migrate_config(c->nfft, wide, p.pspi, p.interp, p.nmx, p.nref, &S, &th, &smem, MIG_FORM_PAIRED) &&
             (int)smem <= c->max_smem)
             return MIG_FORM_PAIRED;
     }
@@ -696,6 +814,13 @@ static MigArgs mig_args(wem_ctx *c, int nshot, int ngroups)
     a.selbp = P<uint8_t>(c->selbp);
     a.wlinp = P<float>(c->wlinp);
     a.ptab = nullptr;
+    a.nlog = c->nkx;
+    if (c->blu) {
+        a.chirp = P<float2>(c->twid) + c->chirp_off;
+        a.bfft = P<float2>(c->twid) + c->bfft_off;
+    }
+    a.vref64 = P<double>(c->vref64);
+    a.dkx64 = c->dkx64;
     return a;
 }
 
@@ -708,10 +833,10 @@ static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
     int S, threads, bps = 0;
     size_t smem;
     const int form = mig_form(c, wide);
-    if (migrate_config(c->nkx, wide, p.pspi, p.interp, p.nmx, p.nref, &S, &threads, &smem, form) ||
+    if (migrate_config(c->nfft, wide, p.pspi, p.interp, p.nmx, p.nref, &S, &threads, &smem, form) ||
         (int)smem > c->max_smem)
         return WEM_OK;
-    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, p.nmx, p.nref, &bps, form) || bps < 1) {
+    if (migrate_max_grid(c->nfft, wide, p.pspi, p.interp, p.nmx, p.nref, &bps, form) || bps < 1) {
         cudaGetLastError();
         return WEM_OK;
     }
@@ -726,10 +851,10 @@ static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
     a.nz = std::min(p.nz, 48);
     if ((rc = ensure(c->slots, sizeof(float2) * (size_t)items * a.nz * p.nmx))) return rc;
     a.slots = P<float2>(c->slots);
-    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st, form))
+    if (launch_migrate(c->nfft, wide, p.pspi, p.interp, a, items, c->st, form))
         return fail(WEM_ERR_CUDA, "migrate launch (tuning): %s", cudaGetErrorString(cudaGetLastError()));
     CK(cudaEventRecord(c->ev0, c->st));
-    if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, items, c->st, form))
+    if (launch_migrate(c->nfft, wide, p.pspi, p.interp, a, items, c->st, form))
         return fail(WEM_ERR_CUDA, "migrate launch (tuning): %s", cudaGetErrorString(cudaGetLastError()));
     CK(cudaEventRecord(c->ev1, c->st));
     CK(cudaEventSynchronize(c->ev1));
@@ -746,7 +871,7 @@ static int choose_shape(wem_ctx *c, int nshot, int *wide)
     const char *e = getenv("WEM_CTA_SHAPE");
     int S, th;
     size_t smem;
-    const bool wide_fits = !migrate_config(c->nkx, 1, p.pspi, p.interp, p.nmx, p.nref, &S, &th, &smem, mig_form(c, 1)) &&
+    const bool wide_fits = !migrate_config(c->nfft, 1, p.pspi, p.interp, p.nmx, p.nref, &S, &th, &smem, mig_form(c, 1)) &&
                            (int)smem <= c->max_smem;
     c->last_tuned = 0;
     if (e && !strcmp(e, "narrow")) return *wide = 0, WEM_OK;
@@ -866,6 +991,11 @@ static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev,
     return WEM_OK;
 }
 
+// entries of a precomputed phase table (|k| = 0 .. nkx/2) and their stride (float2) in c->ptab:
+// the layout the depth kernels' shared memory takes (ph_stride in wem_step.cuh)
+static int ph_half_of(const wem_ctx *c) { return c->nkx / 2 + 1; }
+static int ph_stride_of(const wem_ctx *c) { return c->blu ? c->nfft / 4 + 2 : c->nkx / 2 + 2; }
+
 // The 2-D PSPI kernels (FP32 and split16) read the phase tables of every (frequency, depth) from one array
 // that wem_phase_tables_kernel fills first, when it fits (at most 32 GiB and half the free
 // device memory); otherwise each CTA builds its own. True when c->ptab holds them.
@@ -873,7 +1003,7 @@ static bool alloc_phase_tables(wem_ctx *c)
 {
     const wem_params &p = c->p;
     if (!c->use_ptab || c->nwf < 1 || !p.pspi || p.nmy > 1) return false;
-    const size_t bytes = sizeof(float2) * (size_t)c->nwf * p.nz * p.nref * (size_t)(c->nkx / 2 + 2);
+    const size_t bytes = sizeof(float2) * (size_t)c->nwf * p.nz * p.nref * (size_t)ph_stride_of(c);
     if (c->ptab.n >= bytes) return true;
     size_t fr = 0, tot = 0;
     bool ok = false;
@@ -925,11 +1055,11 @@ static int enqueue_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_de
         MigArgs a = mig_args(c, nshot, ngroups);
         if (c->ptab_ok) {
             a.ptab = P<float2>(c->ptab);
-            if (launch_phase_tables(c->nkx, a, P<float2>(c->ptab), st))
+            if (launch_phase_tables(ph_half_of(c), ph_stride_of(c), a, P<float2>(c->ptab), st, tcmode(c)))
                 return fail(WEM_ERR_CUDA, "phase-table launch: %s", cudaGetErrorString(cudaGetLastError()));
             kernels++;
         }
-        if (launch_migrate(c->nkx, wide, p.pspi, p.interp, a, grid, st, mig_form(c, wide)))
+        if (launch_migrate(c->nfft, wide, p.pspi, p.interp, a, grid, st, mig_form(c, wide)))
             return fail(WEM_ERR_CUDA, "migrate launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;
     }
@@ -957,12 +1087,12 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
     int rc;
     if ((rc = choose_shape(c, nshot, &wide))) return rc;
     const int form = mig_form(c, wide);
-    if (migrate_config(c->nkx, wide, p.pspi, p.interp, nmx, p.nref, &S, &threads, &smem, form))
+    if (migrate_config(c->nfft, wide, p.pspi, p.interp, nmx, p.nref, &S, &threads, &smem, form))
         return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
     if ((int)smem > c->max_smem)
         return fail(WEM_ERR_SIZE, "nref=%d needs %zu B of shared memory per CTA (device limit %d B)", p.nref, smem,
                     c->max_smem);
-    if (migrate_max_grid(c->nkx, wide, p.pspi, p.interp, nmx, p.nref, &bps, form) || bps < 1)
+    if (migrate_max_grid(c->nfft, wide, p.pspi, p.interp, nmx, p.nref, &bps, form) || bps < 1)
         return fail(WEM_ERR_CUDA, "kernel does not fit on the device (smem %zu B, %d threads): %s", smem, threads,
                     cudaGetErrorString(cudaGetLastError()));
     const int ngroups = (nshot + S - 1) / S;
@@ -1054,15 +1184,13 @@ extern "C" int wem_migrate(wem_ctx *c, int nshot, const float *sx, const float *
 }
 
 
-// ------------------------------------------------------------------ derivative GEMMs
+// ------------------------------------------------------------------ derivative convolutions
 // The angle computation differentiates its volumes along one axis at a time:
 // IDFT(m(k) i k DFT(u)) * scale with m the whole axis (mode 1, scale 1/L) or its left /
 // right half (modes 2, 3, scale 1; wem.c:900-945). Along the axis this is a circular
-// convolution with w(j) = scale sum_k m(k) i k e^{+2 pi i k j / L}, so for all lines at once
-// it is one complex GEMM against the L x L matrix W(i, k') = w((k' - i) mod L) -- L^2
-// multiply-adds per sample instead of the two direct transforms' 2 L^2. k is the float
-// wavenumber of the direct transforms (axis_k); w is summed in double.
-static void deriv_matrix_host(int L, float dk, int mode, float scale, std::vector<float2> &W)
+// convolution with w(j) = scale sum_k m(k) i k e^{+2 pi i k j / L}; k is the float
+// wavenumber of the reference (axis_k), w is summed in double.
+static void deriv_kernel_host(int L, float dk, int mode, float scale, std::vector<double> &wr, std::vector<double> &wi)
 {
     std::vector<double> kx(L);
     for (int k = 0; k < L; k++) {
@@ -1076,7 +1204,8 @@ static void deriv_matrix_host(int L, float dk, int mode, float scale, std::vecto
         cs[m] = cos(ph);
         sn[m] = sin(ph);
     }
-    std::vector<double> wr(L), wi(L);
+    wr.assign(L, 0.0);
+    wi.assign(L, 0.0);
     for (int j = 0; j < L; j++) {
         double re = 0.0, im = 0.0;
         for (int k = 0; k < L; k++) {
@@ -1089,109 +1218,64 @@ static void deriv_matrix_host(int L, float dk, int mode, float scale, std::vecto
         wr[j] = re * scale;
         wi[j] = im * scale;
     }
-    W.resize((size_t)L * L);
-    for (int kp = 0; kp < L; kp++)
-        for (int i = 0; i < L; i++) {
-            const int j = ((kp - i) % L + L) % L;
-            W[(size_t)kp * L + i] = make_float2((float)wr[j], (float)wi[j]);  // column-major (i, k')
+}
+
+// The derivative kernels of `modes` (nout of them) along an axis of L samples as transfer
+// functions of the M-point rows of launch_angles_conv (M = angles_conv_length(L)):
+// H_o = FFT_M(g_o) / M, g_o = w_o at j and at M - j for w_o(-j) = w_o(L - j), in double; H
+// holds [nout][M] and tw the row FFT's twiddles.
+static int deriv_conv_tables(wem_ctx *c, DevBuf &H, DevBuf &tw, int L, float dk, const int *modes, int nout)
+{
+    const int M = angles_conv_length(L);
+    if (!M) return fail(WEM_ERR_SIZE, "wem_angles: an axis of %d samples (the derivatives take at most 2048)", L);
+    std::vector<float2> h((size_t)nout * M), t(twiddle_table_size(M) + 1);
+    std::vector<double> wr, wi;
+    for (int o = 0; o < nout; o++) {
+        deriv_kernel_host(L, dk, modes[o], modes[o] == 1 ? 1.f / (float)L : 1.f, wr, wi);
+        std::vector<double> gr(M, 0.0), gi(M, 0.0);
+        for (int j = 0; j < L; j++) {
+            gr[j] = wr[j];
+            gi[j] = wi[j];
+            if (j > 0) {
+                gr[M - j] = wr[L - j];
+                gi[M - j] = wi[L - j];
+            }
         }
-}
-
-// W of deriv_matrix_host into the device buffer b
-static int deriv_matrix(wem_ctx *c, DevBuf &b, int L, float dk, int mode, float scale)
-{
-    std::vector<float2> W;
-    deriv_matrix_host(L, dk, mode, scale, W);
+        fft_pow2_double(gr, gi, -1);
+        for (int q = 0; q < M; q++) h[(size_t)o * M + q] = make_float2((float)(gr[q] / M), (float)(gi[q] / M));
+    }
+    twiddle_table_host(M, t.data());
     int rc;
-    if ((rc = ensure(b, sizeof(float2) * W.size()))) return rc;
-    CK(cudaMemcpyAsync(b.p, W.data(), sizeof(float2) * W.size(), cudaMemcpyHostToDevice, c->st));
-    CK(cudaStreamSynchronize(c->st));  // W is a local
+    if ((rc = ensure(H, sizeof(float2) * h.size())) || (rc = ensure(tw, sizeof(float2) * t.size()))) return rc;
+    CK(cudaMemcpyAsync(H.p, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(tw.p, t.data(), sizeof(float2) * t.size(), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));  // h and t are locals
     return WEM_OK;
 }
 
-// The same derivative as a real GEMM on planar data: [C_re C_im] = [A_re A_im] Wb with
-// Wb = [[W_re, W_im], [-W_im, W_re]] (2L x 2L), so that cuBLAS can run it with its FP32
-// emulation on the tensor cores (BF16x9), which it does not take for complex operands.
-static int deriv_matrix_block(wem_ctx *c, DevBuf &b, int L, float dk, int mode, float scale)
+// out[o] = derivative o of u along an axis of L samples (tables of deriv_conv_tables):
+// cols == 1 lines of L contiguous samples; cols > 1 column c of planes [L][cols]
+static int deriv_conv(wem_ctx *c, const DevBuf &H, const DevBuf &tw, const float2 *u, float2 *const *out, int nout,
+                      int L, int cols, long long nlines)
 {
-    std::vector<float2> W;
-    deriv_matrix_host(L, dk, mode, scale, W);
-    const size_t L2 = 2 * (size_t)L;
-    std::vector<float> Wb(L2 * L2);
-    for (int j = 0; j < L; j++)
-        for (int i = 0; i < L; i++) {
-            const float2 w = W[(size_t)j * L + i];  // (i, j)
-            Wb[(size_t)j * L2 + i] = w.x;
-            Wb[((size_t)j + L) * L2 + i] = w.y;
-            Wb[(size_t)j * L2 + i + L] = -w.y;
-            Wb[((size_t)j + L) * L2 + i + L] = w.x;
-        }
-    int rc;
-    if ((rc = ensure(b, sizeof(float) * Wb.size()))) return rc;
-    CK(cudaMemcpyAsync(b.p, Wb.data(), sizeof(float) * Wb.size(), cudaMemcpyHostToDevice, c->st));
-    CK(cudaStreamSynchronize(c->st));  // Wb is a local
-    return WEM_OK;
-}
-
-// out (planar) = derivative along the slow axis of in (planar): per batch entry `lines`
-// contiguous lines of L samples, [re plane, im plane], entries 2 * lines * L floats apart
-static int deriv_gemm_planar(wem_ctx *c, const DevBuf &Wb, const float *in, float *out, int L, long long lines, int batch)
-{
-    if (!c->blas) {
-        if (cublasCreate(&c->blas) != CUBLAS_STATUS_SUCCESS) return fail(WEM_ERR_CUDA, "cublasCreate failed");
-    }
-    if (cublasSetStream(c->blas, c->st) != CUBLAS_STATUS_SUCCESS) return fail(WEM_ERR_CUDA, "cublasSetStream failed");
-    const float one = 1.f, zero = 0.f;
-    const long long stride = 2 * lines * (long long)L;
-    auto run = [&](cublasComputeType_t ct) {
-        return cublasGemmStridedBatchedEx(c->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)lines, 2 * L, 2 * L, &one, in,
-                                          CUDA_R_32F, (int)lines, stride, Wb.p, CUDA_R_32F, 2 * L, 0, &zero, out,
-                                          CUDA_R_32F, (int)lines, stride, batch, ct, CUBLAS_GEMM_DEFAULT);
-    };
-    if (c->blas_real_compute < 0) {
-        c->blas_real_compute = (int)CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
-        if (run(CUBLAS_COMPUTE_32F_EMULATED_16BFX9) == CUBLAS_STATUS_SUCCESS) return WEM_OK;
-        c->blas_real_compute = (int)CUBLAS_COMPUTE_32F;
-    }
-    if (run((cublasComputeType_t)c->blas_real_compute) != CUBLAS_STATUS_SUCCESS)
-        return fail(WEM_ERR_CUDA, "derivative GEMM (planar, L=%d) failed", L);
-    return WEM_OK;
-}
-
-// out = derivative of in along an axis of length L (matrix W from deriv_matrix), for `lines`
-// lines per batch entry and `batch` entries `stride` samples apart. axis_slow: sample i of
-// line l at i * ld + l (the lines contiguous); otherwise at l * ld + i (the axis
-// contiguous). The GEMMs run with cuBLAS's FP32 emulation on the tensor cores (BF16x9)
-// where it accepts complex operands, otherwise in FP32.
-static int deriv_gemm(wem_ctx *c, const DevBuf &W, const float2 *in, float2 *out, int L, bool axis_slow,
-                      long long lines, long long ld, int batch, long long stride)
-{
-    if (!c->blas) {
-        if (cublasCreate(&c->blas) != CUBLAS_STATUS_SUCCESS) return fail(WEM_ERR_CUDA, "cublasCreate failed");
-    }
-    if (cublasSetStream(c->blas, c->st) != CUBLAS_STATUS_SUCCESS) return fail(WEM_ERR_CUDA, "cublasSetStream failed");
-    const cuComplex one = make_cuComplex(1.f, 0.f), zero = make_cuComplex(0.f, 0.f);
-    auto run = [&](cublasComputeType_t ct) {
-        if (axis_slow)  // C (lines x L) = A (lines x L, ld) * W
-            return cublasGemmStridedBatchedEx(c->blas, CUBLAS_OP_N, CUBLAS_OP_N, (int)lines, L, L, &one, in, CUDA_C_32F,
-                                              (int)ld, stride, W.p, CUDA_C_32F, L, 0, &zero, out, CUDA_C_32F,
-                                              (int)ld, stride, batch, ct, CUBLAS_GEMM_DEFAULT);
-        // C (L x lines) = W^T * A (L x lines, ld)
-        return cublasGemmStridedBatchedEx(c->blas, CUBLAS_OP_T, CUBLAS_OP_N, L, (int)lines, L, &one, W.p, CUDA_C_32F,
-                                          L, 0, in, CUDA_C_32F, (int)ld, stride, &zero, out, CUDA_C_32F, (int)ld,
-                                          stride, batch, ct, CUBLAS_GEMM_DEFAULT);
-    };
-    if (c->blas_compute < 0) {
-        c->blas_compute = (int)CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
-        if (run(CUBLAS_COMPUTE_32F_EMULATED_16BFX9) == CUBLAS_STATUS_SUCCESS) return WEM_OK;
-        c->blas_compute = (int)CUBLAS_COMPUTE_32F;
-    }
-    if (run((cublasComputeType_t)c->blas_compute) != CUBLAS_STATUS_SUCCESS)
-        return fail(WEM_ERR_CUDA, "derivative GEMM (L=%d) failed", L);
+    AngleConvArgs a{};
+    a.L = L;
+    a.cols = cols;
+    a.nout = nout;
+    a.nlines = nlines;
+    a.tw = P<float2>(const_cast<DevBuf &>(tw));
+    a.H = P<float2>(const_cast<DevBuf &>(H));
+    a.u = u;
+    for (int o = 0; o < nout; o++) a.out[o] = out[o];
+    if (launch_angles_conv(a, c->nsm, c->st))
+        return fail(WEM_ERR_CUDA, "angles: derivative launch (L=%d): %s", L, cudaGetErrorString(cudaGetLastError()));
     return WEM_OK;
 }
 
 // ---------------------------------------------------------------- incidence angles
+// u_x (whole axis), u_left, u_right: the derivative modes of deriv_kernel_host
+static const int kDerivModes[3] = { 1, 2, 3 };
+
 // 3-D (nmy > 1), compute_angles with both lateral axes: per shot and batch of frequencies
 // the source is continued down with the plane passes of wem_3d.cu (mode 3, ssop_source's
 // split-step step on the unpadded plane, every depth kept), then one-axis transforms
@@ -1259,11 +1343,11 @@ static int angles3d(wem_ctx *c, const wem_params &p, const float *vel, const flo
     const size_t vol = sizeof(float2) * (size_t)batch * nn;
     DevBuf bpo, bpd, btx, bty, bfx, bfy, bwt, bsc, bsrc, bbase, bwav, bzf, bitems, bcell, bU, bY, bC, bS,
         bSX, bLX, bRX, bSY, bLY, bRY, bSZ, bsum, bang;
-    DevBuf bDx, bDlx, bDrx, bDy, bDly, bDry, bDz;  // derivative matrices of the three axes
+    DevBuf bHx, bHy, bHz, bTx, bTy, bTz;  // derivative transfer functions and row twiddles of the three axes
     auto release = [&]() {
         DevBuf *bs[] = { &bpo, &bpd, &btx, &bty, &bfx, &bfy, &bwt, &bsc, &bsrc, &bbase, &bwav, &bzf,
                          &bitems, &bcell, &bU, &bY, &bC, &bS, &bSX, &bLX, &bRX, &bSY, &bLY, &bRY, &bSZ, &bsum,
-                         &bang, &bDx, &bDlx, &bDrx, &bDy, &bDly, &bDry, &bDz };
+                         &bang, &bHx, &bHy, &bHz, &bTx, &bTy, &bTz };
         for (DevBuf *b : bs)
             if (b->p) cudaFree(b->p);
     };
@@ -1280,10 +1364,9 @@ static int angles3d(wem_ctx *c, const wem_params &p, const float *vel, const flo
         (rc = ensure(bSX, vol)) || (rc = ensure(bLX, vol)) || (rc = ensure(bRX, vol)) || (rc = ensure(bSY, vol)) ||
         (rc = ensure(bLY, vol)) || (rc = ensure(bRY, vol)) || (rc = ensure(bSZ, vol)) ||
         (rc = ensure(bsum, sizeof(float) * 4 * nn)) || (rc = ensure(bang, sizeof(float) * 2 * nn)) ||
-        (rc = deriv_matrix(c, bDx, nmx, dkx, 1, 1.f / (float)nmx)) || (rc = deriv_matrix(c, bDlx, nmx, dkx, 2, 1.f)) ||
-        (rc = deriv_matrix(c, bDrx, nmx, dkx, 3, 1.f)) || (rc = deriv_matrix(c, bDy, nmy, dky, 1, 1.f / (float)nmy)) ||
-        (rc = deriv_matrix(c, bDly, nmy, dky, 2, 1.f)) || (rc = deriv_matrix(c, bDry, nmy, dky, 3, 1.f)) ||
-        (rc = deriv_matrix(c, bDz, nz, dkz, 1, 1.f / (float)nz))) {
+        (rc = deriv_conv_tables(c, bHx, bTx, nmx, dkx, kDerivModes, 3)) ||
+        (rc = deriv_conv_tables(c, bHy, bTy, nmy, dky, kDerivModes, 3)) ||
+        (rc = deriv_conv_tables(c, bHz, bTz, nz, dkz, kDerivModes, 1))) {
         release();
         return rc;
     }
@@ -1353,17 +1436,17 @@ static int angles3d(wem_ctx *c, const wem_params &p, const float *vel, const flo
                 LCHK(m3d_launch_step(nmx, nmy, 0, 0, a, c->nsm, st), "3-D source step");
             }
             kernels += 1 + 3 * nz;
-            // derivatives of the depth volumes [f][z][x][y] (wem.c:900-992): x lines (nmy of them,
-            // contiguous) with x nmy apart, y contiguous, z lines of n samples nz of them n apart
+            // derivatives of the depth volumes [f][z][x][y] (wem.c:900-992): x along the columns
+            // of the [x][y] planes, y along their rows, z along the columns of the [z][x y]
+            // volumes of each frequency
             const long long nbl = nb;
             const float2 *vs = P<float2>(bS);
-            if ((rc = deriv_gemm(c, bDx, vs, P<float2>(bSX), nmx, true, nmy, nmy, (int)(nbl * nz), n)) ||
-                (rc = deriv_gemm(c, bDlx, vs, P<float2>(bLX), nmx, true, nmy, nmy, (int)(nbl * nz), n)) ||
-                (rc = deriv_gemm(c, bDrx, vs, P<float2>(bRX), nmx, true, nmy, nmy, (int)(nbl * nz), n)) ||
-                (rc = deriv_gemm(c, bDy, vs, P<float2>(bSY), nmy, false, nbl * nz * nmx, nmy, 1, 0)) ||
-                (rc = deriv_gemm(c, bDly, vs, P<float2>(bLY), nmy, false, nbl * nz * nmx, nmy, 1, 0)) ||
-                (rc = deriv_gemm(c, bDry, vs, P<float2>(bRY), nmy, false, nbl * nz * nmx, nmy, 1, 0)) ||
-                (rc = deriv_gemm(c, bDz, vs, P<float2>(bSZ), nz, true, n, n, nb, (long long)nz * n))) {
+            float2 *ox[3] = { P<float2>(bSX), P<float2>(bLX), P<float2>(bRX) };
+            float2 *oy[3] = { P<float2>(bSY), P<float2>(bLY), P<float2>(bRY) };
+            float2 *oz[1] = { P<float2>(bSZ) };
+            if ((rc = deriv_conv(c, bHx, bTx, vs, ox, 3, nmx, nmy, nbl * nz * nmy)) ||
+                (rc = deriv_conv(c, bHy, bTy, vs, oy, 3, nmy, 1, nbl * nz * nmx)) ||
+                (rc = deriv_conv(c, bHz, bTz, vs, oz, 1, nz, n, nbl * n))) {
                 release();
                 return rc;
             }
@@ -1374,7 +1457,7 @@ static int angles3d(wem_ctx *c, const wem_params &p, const float *vel, const flo
             ac.lx = P<float2>(bLX); ac.rx = P<float2>(bRX); ac.ly = P<float2>(bLY); ac.ry = P<float2>(bRY);
             ac.sum = P<float>(bsum); ac.angx = P<float>(bang); ac.angy = P<float>(bang) + nn;
             LCHK(launch_angles_accum3(ac, st), "accumulation");
-            kernels += 1;  // and the cuBLAS GEMMs of the derivatives
+            kernels += 4;
         }
         CKR(cudaMemcpyAsync(angx + (size_t)s * nn, bang.p, sizeof(float) * nn, cudaMemcpyDeviceToHost, st));
         if (angy) CKR(cudaMemcpyAsync(angy + (size_t)s * nn, P<float>(bang) + nn, sizeof(float) * nn, cudaMemcpyDeviceToHost, st));
@@ -1402,7 +1485,8 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
         return fail(WEM_ERR_ARG, "wem_angles: invalid grid (nt=%d nmx=%d nz=%d)", p.nt, p.nmx, p.nz);
     if (p.nmy != 1) return angles3d(c, p, vel, wav, nshot, sx, sy, angx, angy);
     const int nmx = p.nmx, nz = p.nz;
-    if (nmx > 4096) return fail(WEM_ERR_SIZE, "wem_angles: nmx = %d above 4096", nmx);
+    if (nmx > 2048 || nz > 2048)
+        return fail(WEM_ERR_SIZE, "wem_angles: nmx = %d and nz = %d must be at most 2048 (the derivatives' rows)", nmx, nz);
     CK(cudaSetDevice(c->device));
     cudaStream_t st = c->st;
     // slowness split of compute_angles (wem.c:609-618), depth-major on the device
@@ -1450,19 +1534,19 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     // shots per batch: all their source volumes and derivatives (5 each) within half the free memory
     size_t free_b = 0, total_b = 0;
     CK(cudaMemGetInfo(&free_b, &total_b));
-    const size_t per_shot = sizeof(float2) * (size_t)6 * nwf * n + sizeof(float) * 2 * n;
+    const size_t per_shot = sizeof(float2) * (size_t)5 * nwf * n + sizeof(float) * 2 * n;
     const int nbatch = (int)std::max<long long>(1, std::min<long long>(nshot, (long long)(free_b / 2 / per_shot)));
     const size_t plane = sizeof(float2) * (size_t)nbatch * nwf * n;
     DevBuf bwt, btwx, bsc, bsrc, bbase, bpo, bpd, btap, bwav, btwf;
-    DevBuf bDz, bDx, bDl, bDr;  // derivative matrices (z; x, left, right where x has no row FFT)
+    DevBuf bHz, bTz, bHx, bTx;  // derivative transfer functions and row twiddles (z; x where x has no row FFT)
     DevBuf bigx;                // the batch's source cells
-    // the volumes stay with the context for the next call: u, u_x, u_left, u_right, u_z, u in
-    // planes (the z derivative's real block GEMM), the angles
+    // the volumes stay with the context for the next call: u, u_x, u_left, u_right, u_z, the
+    // angles
     DevBuf &bU = c->ang_vol[0], &bX = c->ang_vol[1], &bL = c->ang_vol[2], &bR = c->ang_vol[3],
-           &bZ = c->ang_vol[4], &bUp = c->ang_vol[5], &bang = c->ang_vol[6];
+           &bZ = c->ang_vol[4], &bang = c->ang_vol[6];
     auto release = [&]() {
         DevBuf *bs[] = { &bwt, &btwx, &bsc, &bsrc, &bbase, &bpo, &bpd, &btap, &bwav, &btwf,
-                         &bDz, &bDx, &bDl, &bDr, &bigx };
+                         &bHz, &bTz, &bHx, &bTx, &bigx };
         for (DevBuf *b : bs)
             if (b->p) cudaFree(b->p);
     };
@@ -1472,7 +1556,7 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
         (rc = ensure(bsrc, sizeof(float2) * nwf)) || (rc = ensure(bbase, sizeof(int64_t))) || (rc = ensure(bU, plane)) ||
         (rc = ensure(bX, plane)) || (rc = ensure(bL, plane)) || (rc = ensure(bR, plane)) ||
         (rc = ensure(bZ, plane)) || (rc = ensure(bang, sizeof(float) * 2 * n * nbatch)) ||
-        (rc = ensure(bigx, sizeof(int) * nbatch)) || (rc = ensure(bUp, plane)) ||
+        (rc = ensure(bigx, sizeof(int) * nbatch)) ||
         (rc = ensure(bpo, sizeof(float) * nz)) || (rc = ensure(bpd, sizeof(float) * n)) ||
         (rc = ensure(btap, sizeof(float) * nmx)) || (rc = ensure(bwav, sizeof(float) * p.nt)) ||
         (rc = ensure(btwf, sizeof(float2) * (twf.size() + 1)))) {
@@ -1496,9 +1580,8 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
     CKR(cudaMemcpyAsync(btap.p, taper.data(), sizeof(float) * nmx, cudaMemcpyHostToDevice, st));
     CKR(cudaMemcpyAsync(bwav.p, wav, sizeof(float) * p.nt, cudaMemcpyHostToDevice, st));
     if (fftx) CKR(cudaMemcpyAsync(btwf.p, twf.data(), sizeof(float2) * twf.size(), cudaMemcpyHostToDevice, st));
-    if ((rc = deriv_matrix_block(c, bDz, nz, dkz, 1, 1.f / (float)nz)) ||
-        (!fftx && ((rc = deriv_matrix(c, bDx, nmx, dkx, 1, 1.f / (float)nmx)) ||
-                   (rc = deriv_matrix(c, bDl, nmx, dkx, 2, 1.f)) || (rc = deriv_matrix(c, bDr, nmx, dkx, 3, 1.f))))) {
+    if ((rc = deriv_conv_tables(c, bHz, bTz, nz, dkz, kDerivModes, 1)) ||
+        (!fftx && (rc = deriv_conv_tables(c, bHx, bTx, nmx, dkx, kDerivModes, 3)))) {
         release();
         return rc;
     }
@@ -1552,36 +1635,32 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
             return fail(WEM_ERR_CUDA, "angles: extrapolation launch: %s", cudaGetErrorString(cudaGetLastError()));
         }
         // derivatives of all the batch's volumes: u_x, u_left, u_right (wem.c:900-945) along x --
-        // the row FFT for power-of-two widths, else GEMMs against the derivative matrices (x
-        // contiguous) -- and u_z along z (lines of nmx contiguous samples, nz of them nmx apart)
+        // the row FFT for power-of-two widths, else circular convolutions on the rows -- and u_z
+        // along z (the columns of every [z][x] plane)
         if (fftx) {
             if (launch_angles_fft(a, xf, 1, st)) {
                 release();
                 return fail(WEM_ERR_CUDA, "angles: x-derivative launch: %s", cudaGetErrorString(cudaGetLastError()));
             }
         } else {
-            const long long xl = (long long)nb * nwf * nz;
-            if ((rc = deriv_gemm(c, bDx, P<float2>(bU), P<float2>(bX), nmx, false, xl, nmx, 1, 0)) ||
-                (rc = deriv_gemm(c, bDl, P<float2>(bU), P<float2>(bL), nmx, false, xl, nmx, 1, 0)) ||
-                (rc = deriv_gemm(c, bDr, P<float2>(bU), P<float2>(bR), nmx, false, xl, nmx, 1, 0))) {
+            float2 *ox[3] = { P<float2>(bX), P<float2>(bL), P<float2>(bR) };
+            if ((rc = deriv_conv(c, bHx, bTx, P<float2>(bU), ox, 3, nmx, 1, (long long)nb * nwf * nz))) {
                 release();
                 return rc;
             }
         }
-        // u_z: u to planes, then the real block GEMM (planes out, read by the accumulation)
-        if (launch_planar(P<float2>(bU), P<float>(bUp), (long long)nz * nmx, (long long)nb * nwf, st)) {
-            release();
-            return fail(WEM_ERR_CUDA, "angles: planar launch: %s", cudaGetErrorString(cudaGetLastError()));
-        }
-        if ((rc = deriv_gemm_planar(c, bDz, P<float>(bUp), P<float>(bZ), nz, nmx, nb * nwf))) {
-            release();
-            return rc;
+        {
+            float2 *oz[1] = { P<float2>(bZ) };
+            if ((rc = deriv_conv(c, bHz, bTz, P<float2>(bU), oz, 1, nz, nmx, (long long)nb * nwf * nmx))) {
+                release();
+                return rc;
+            }
         }
         for (int j = 0; j < nb; j++) {
             AngleAccumArgs ac{};
             ac.nmx = nmx; ac.nz = nz; ac.nwf = nwf; ac.nw = nw; ac.nfreq_div = ifmax - ifmin + 1;
-            ac.u = P<float2>(bU) + j * vol; ac.ux = P<float2>(bX) + j * vol; ac.uz = nullptr;
-            ac.uzp = P<float>(bZ) + 2 * j * vol;
+            ac.u = P<float2>(bU) + j * vol; ac.ux = P<float2>(bX) + j * vol; ac.uz = P<float2>(bZ) + j * vol;
+            ac.uzp = nullptr;
             ac.ul = P<float2>(bL) + j * vol; ac.ur = P<float2>(bR) + j * vol;
             ac.angx = P<float>(bang) + (size_t)j * 2 * n; ac.angy = P<float>(bang) + (size_t)j * 2 * n + n;
             if (launch_angles_accum(ac, st)) {
@@ -1589,7 +1668,7 @@ extern "C" int wem_angles(wem_ctx *c, const wem_params *pp, const float *vel, co
                 return fail(WEM_ERR_CUDA, "angles: accumulation launch: %s", cudaGetErrorString(cudaGetLastError()));
             }
         }
-        kernels += (fftx ? 3 : 2) + nb;  // and the cuBLAS GEMMs of the derivatives
+        kernels += 3 + nb;
         for (int j = 0; j < nb; j++) {
             const int s = s0 + j;
             CKR(cudaMemcpyAsync(angx + (size_t)s * n, P<float>(bang) + (size_t)j * 2 * n, sizeof(float) * n,
@@ -1725,11 +1804,12 @@ static int run_model(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, flo
     const int nmx = p.nmx, nz = p.nz;
     int S, threads, bps = 0;
     size_t smem;
-    if (model_config(c->nkx, p.pspi, nmx, p.nref, &S, &threads, &smem)) return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
+    if (model_config(c->nfft, p.pspi, nmx, p.nref, &S, &threads, &smem, c->blu))
+        return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
     if ((int)smem > c->max_smem)
         return fail(WEM_ERR_SIZE, "nref=%d needs %zu B of shared memory per CTA (device limit %d B)", p.nref, smem,
                     c->max_smem);
-    if (model_max_grid(c->nkx, p.pspi, p.interp, exact, nmx, p.nref, &bps) || bps < 1)
+    if (model_max_grid(c->nfft, p.pspi, p.interp, exact, nmx, p.nref, &bps, c->blu) || bps < 1)
         return fail(WEM_ERR_CUDA, "modelling kernel does not fit on the device: %s", cudaGetErrorString(cudaGetLastError()));
     const int ngroups = (nshot + S - 1) / S;
     const long long nitems = (long long)ngroups * c->nwf;
@@ -1760,9 +1840,14 @@ static int run_model(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, flo
         a.refmask = P<unsigned long long>(c->refmask);
         a.selbp = P<uint8_t>(c->selbp);
         a.wlinp = P<float>(c->wlinp);
+        a.nlog = c->nkx;
+        if (c->blu) {
+            a.chirp = P<float2>(c->twid) + c->chirp_off;
+            a.bfft = P<float2>(c->twid) + c->bfft_off;
+        }
         if (alloc_phase_tables(c)) {
             a.ptab = P<float2>(c->ptab);
-            if (launch_phase_tables(c->nkx, a, P<float2>(c->ptab), st))
+            if (launch_phase_tables(ph_half_of(c), ph_stride_of(c), a, P<float2>(c->ptab), st))
                 return fail(WEM_ERR_CUDA, "phase-table launch: %s", cudaGetErrorString(cudaGetLastError()));
             kernels++;
         }
@@ -1771,7 +1856,7 @@ static int run_model(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, flo
         b.smig = P<float2>(c->smig);
         b.dg = P<float2>(c->recv);
         b.inv_sqt = (float)(1.0 / (double)sqrtf((float)c->ntfft));
-        if (launch_model(c->nkx, p.pspi, p.interp, exact, a, b, grid, st))
+        if (launch_model(c->nfft, p.pspi, p.interp, exact, a, b, grid, st, c->blu))
             return fail(WEM_ERR_CUDA, "modelling launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;
     }

@@ -53,6 +53,18 @@ struct MigArgs {
     const float2 *ptab;
     const uint8_t *selbp;  // [nz][(nmx + 15) / 16 * 16]
     const float *wlinp;    // [nz][(nmx + 3) / 4 * 4] linear weights, rows padded to 16 bytes
+    // rows whose transform length nkx is not a power of two (Bluestein's chirp form): the
+    // transform length L = nkx (the kernels' row length N is a power of two >= 2L - 1), the
+    // chirp b[n] = e^{i pi n^2 / L} (n < L) and G/N, G the N-point FFT of b placed at n and
+    // N - n (see xform in wem_step.cuh)
+    int nlog;
+    const float2 *chirp;
+    const float2 *bfft;
+    // split16 PSPI: phase tables built in FP64 -- the reference velocities in double
+    // ([nz][nref], vmin + r (vmax - vmin)/(nref - 1) from the float extremes) and the
+    // wavenumber step 2 pi / (nkx dmx) in double
+    const double *vref64;
+    double dkx64;
 };
 // points per depth whose imaginary part the paired form takes from a direct sum
 constexpr int WHOLE_MAX = 4;
@@ -168,6 +180,21 @@ struct AngleXArgs {
     const float2 *u;                   // [nlines][nmx]
     float2 *ux, *ul, *ur;              // [nlines][nmx]
 };
+// Derivatives along one axis as circular convolutions on power-of-two rows (wem_angles.cu):
+// nlines lines of L samples; cols == 1: contiguous lines ([line][L]); cols > 1: column c of
+// plane p ([p][L][cols], nlines = planes * cols). H: nout transfer functions of the row
+// length M = angles_conv_length(L) (G/M of the convolution kernel), out[o] like u.
+struct AngleConvArgs {
+    int L, cols, nout;
+    long long nlines;
+    const float2 *tw;   // FFT twiddle table of M
+    const float2 *H;    // [nout][M]
+    const float2 *u;
+    float2 *out[3];
+};
+// M for an axis of L samples: the power of two >= max(32, 2L - 1); 0 above L = 2048
+int angles_conv_length(int L);
+int launch_angles_conv(const AngleConvArgs &a, int nsm, cudaStream_t st);
 int launch_angles_extrap(const AngleArgs &a, cudaStream_t st);
 // power-of-two nmx in [32, 2048]: which = 0 extrapolation, 1 x derivatives on the row FFT
 bool angles_fft_supported(int nmx);
@@ -175,8 +202,10 @@ int launch_angles_fft(const AngleArgs &a, const AngleXArgs &x, int which, cudaSt
 int launch_angles_accum(const AngleAccumArgs &a, cudaStream_t st);
 
 // Forms of the 2-D depth kernel: FP32; split16 (tensor-core DFT stages, nkx = 2048 only);
-// paired (FP32, PSPI nearest-lower mode: two references' real parts per inverse transform).
-constexpr int MIG_FORM_FP32 = 0, MIG_FORM_SPLIT16 = 1, MIG_FORM_PAIRED = 2;
+// paired (FP32, PSPI nearest-lower mode: two references' real parts per inverse transform);
+// Bluestein (FP32, transform length nkx not a power of two, on rows of the power of two
+// N >= 2 nkx - 1; the nkx argument of the dispatch functions below is that N).
+constexpr int MIG_FORM_FP32 = 0, MIG_FORM_SPLIT16 = 1, MIG_FORM_PAIRED = 2, MIG_FORM_BLU = 3;
 int migrate_config(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *shots_per_cta, int *threads,
                    size_t *smem, int form = MIG_FORM_FP32);
 int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *blocks_per_sm,
@@ -185,14 +214,18 @@ int launch_migrate(int nkx, int wide, int pspi, int interp, const MigArgs &a, in
                    int form = MIG_FORM_FP32);
 // one bounded mbarrier wait that nothing completes; *timed_out (device) = 1 when it gave up
 int launch_wait_probe(int *timed_out, cudaStream_t st);
-// the precomputed phase tables of the paired form (a.ptab layout) into out
-int launch_phase_tables(int nkx, const MigArgs &a, float2 *out, cudaStream_t st);
+// FP32 FMA probe: grid CTAs of 512 threads, each thread 64 x iters FMAs
+int launch_fma_probe(float *out, int iters, int grid, cudaStream_t st);
+// the precomputed phase tables (a.ptab layout: `half` entries of every reference in use at a
+// stride of `phs` float2) into out
+int launch_phase_tables(int half, int phs, const MigArgs &a, float2 *out, cudaStream_t st, int f64 = 0);
 // the 10240-byte W operand image of the split16 DFT stages
 void tc_w_table_host(uint16_t *out);
-int model_config(int nkx, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem);
-int model_max_grid(int nkx, int pspi, int interp, int exact, int nmx, int nref, int *blocks_per_sm);
+// blu = 1: the Bluestein rows (MIG_FORM_BLU), nkx the row length N
+int model_config(int nkx, int pspi, int nmx, int nref, int *shots_per_cta, int *threads, size_t *smem, int blu = 0);
+int model_max_grid(int nkx, int pspi, int interp, int exact, int nmx, int nref, int *blocks_per_sm, int blu = 0);
 int launch_model(int nkx, int pspi, int interp, int exact, const MigArgs &a, const BornArgs &b, int grid,
-                 cudaStream_t st);
+                 cudaStream_t st, int blu = 0);
 int launch_spectra(const SpectraArgs &a, cudaStream_t st);
 int launch_image_reduce(const float2 *slots, int nslots, int nz, int nmx, float *m, cudaStream_t st);
 int launch_synth(const SynthArgs &a, cudaStream_t st);

@@ -253,7 +253,8 @@ void twiddle_table_host(int nkx, float2 *out)
 // The phase tables of the paired form for every (frequency, depth): one CTA per (depth,
 // frequency), entries as build_tables makes them (phase_entry, the same FP32 operations),
 // references some point of the depth takes only. out: [nwf][nz][nref][phs].
-__global__ void __launch_bounds__(256) wem_phase_tables_kernel(const MigArgs a, int half, int phs, float2 *out)
+// f64 = 1 (the split16 form): the entries in FP64 (phase_entry_fp64, as build_tables<F64>).
+__global__ void __launch_bounds__(256) wem_phase_tables_kernel(const MigArgs a, int half, int phs, float2 *out, int f64)
 {
     const int iz = blockIdx.x, iwi = blockIdx.y;
     const float w = __fmul_rn((float)(a.ifmin + iwi), a.dw);
@@ -264,8 +265,14 @@ __global__ void __launch_bounds__(256) wem_phase_tables_kernel(const MigArgs a, 
         if (!((used >> r) & 1ull)) continue;
         const float slow2 = sl[r];
         float2 *o = out + (((size_t)iwi * a.nz + iz) * a.nref + r) * phs;
-        for (int kk = threadIdx.x; kk < half; kk += blockDim.x)
-            o[kk] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
+        if (f64) {
+            const double vr = a.vref64[(size_t)iz * a.nref + r], inv_n = 1.0 / (double)a.nlog;
+            for (int kk = threadIdx.x; kk < half; kk += blockDim.x)
+                o[kk] = phase_entry_fp64((double)w, vr, __dmul_rn((double)kk, a.dkx64), (double)a.dz, inv_n);
+        } else {
+            for (int kk = threadIdx.x; kk < half; kk += blockDim.x)
+                o[kk] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
+        }
     }
 }
 
@@ -286,10 +293,37 @@ int launch_wait_probe(int *timed_out, cudaStream_t st)
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_phase_tables(int nkx, const MigArgs &a, float2 *out, cudaStream_t st)
+// FP32 FMA throughput probe: 8 independent multiply-add chains per thread, 32 warps per
+// SM, `iters` x 64 FMAs per thread. The result is stored only under a condition that the
+// chains never meet, so that the compiler keeps every FMA.
+__global__ void __launch_bounds__(512) wem_fma_probe_kernel(float *out, int iters)
+{
+    float a[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) a[j] = 1e-3f * (float)(threadIdx.x + j);
+    const float b = 0.9999999f, c = 1e-7f;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) a[j] = fmaf(a[j], b, c);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; j++) s += a[j];
+    if (s == -1.f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+int launch_fma_probe(float *out, int iters, int grid, cudaStream_t st)
+{
+    wem_fma_probe_kernel<<<grid, 512, 0, st>>>(out, iters);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_phase_tables(int half, int phs, const MigArgs &a, float2 *out, cudaStream_t st, int f64)
 {
     if (a.nz < 1 || a.nwf < 1) return 0;
-    wem_phase_tables_kernel<<<dim3(a.nz, a.nwf), 256, 0, st>>>(a, nkx / 2 + 1, nkx / 2 + 2, out);
+    wem_phase_tables_kernel<<<dim3(a.nz, a.nwf), 256, 0, st>>>(a, half, phs, out, f64);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -378,28 +412,28 @@ void tc_w_table_host(uint16_t *out)
     }
 }
 
-int model_config(int nkx, int pspi, int nmx, int nref, int *S, int *threads, size_t *smem)
+int model_config(int nkx, int pspi, int nmx, int nref, int *S, int *threads, size_t *smem, int blu)
 {
-#define CALL(N) model_launch<N>(pspi, 0, 0, nref, nmx, nullptr, nullptr, 0, 0, S, threads, smem, nullptr)
+#define CALL(N) model_launch<N>(pspi, 0, 0, nref, nmx, nullptr, nullptr, 0, 0, S, threads, smem, nullptr, blu)
     WEM_SWITCH_N(nkx, CALL)
 #undef CALL
 }
 
-int model_max_grid(int nkx, int pspi, int interp, int exact, int nmx, int nref, int *bps)
+int model_max_grid(int nkx, int pspi, int interp, int exact, int nmx, int nref, int *bps, int blu)
 {
     int S, th;
     size_t smem;
-#define CALL(N) model_launch<N>(pspi, interp, exact, nref, nmx, nullptr, nullptr, 0, 0, &S, &th, &smem, bps)
+#define CALL(N) model_launch<N>(pspi, interp, exact, nref, nmx, nullptr, nullptr, 0, 0, &S, &th, &smem, bps, blu)
     WEM_SWITCH_N(nkx, CALL)
 #undef CALL
 }
 
 int launch_model(int nkx, int pspi, int interp, int exact, const MigArgs &a, const BornArgs &b, int grid,
-                 cudaStream_t st)
+                 cudaStream_t st, int blu)
 {
     int S, th;
     size_t smem;
-#define CALL(N) model_launch<N>(pspi, interp, exact, a.nref, a.nmx, &a, &b, grid, st, &S, &th, &smem, nullptr)
+#define CALL(N) model_launch<N>(pspi, interp, exact, a.nref, a.nmx, &a, &b, grid, st, &S, &th, &smem, nullptr, blu)
     WEM_SWITCH_N(nkx, CALL)
 #undef CALL
 }

@@ -17,15 +17,18 @@ namespace gbwem {
 // team gets 32 TMEM columns for its accumulators and an mbarrier.
 // PAIR (PSPI nearest-lower mode, FP32): the step of step_mig_paired, with an N-sample
 // spectrum buffer per team in place of the selection accumulator.
-template <int N, bool PSPI, int INTERP, int S, bool TC = false, bool PAIR = false>
+// BLU (FP32): transforms of length a.nlog (not a power of two) on rows of N samples,
+// N >= 2 a.nlog - 1, in Bluestein's chirp form (xform in wem_step.cuh).
+template <int N, bool PSPI, int INTERP, int S, bool TC = false, bool PAIR = false, bool BLU = false>
 __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const MigArgs a)
 {
     static_assert(!PAIR || (PSPI && INTERP == 0 && !TC), "paired transforms: PSPI nearest-lower mode, FP32");
+    static_assert(!BLU || (!PAIR && !TC), "Bluestein rows: FP32, one transform per reference");
     using SH = MigShape<N>;
     constexpr int T = SH::T, PADN = SH::PADN;
     constexpr int NT = 2 * S * T;
     extern __shared__ float4 smem_raw[];
-    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx, 2 * S, PAIR);
+    const Smem<N, PSPI, BLU> sm(smem_raw, a.nref, a.nmx, 2 * S, PAIR);
 
     const int tid = threadIdx.x;
     const int team = tid / T, t = tid - team * T;
@@ -128,7 +131,7 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                             for (int m = 0; m < 16; m++) v[m] = cscale(v[m], sc);
                             fft_row<N, -1, TC>(v, xbuf, sm.tw, t, sync, &tc);
                         } else {
-                            fft_row<N, -1>(v, xbuf, sm.tw, t, sync);
+                            xform<N, -1, false, BLU>(v, xbuf, sm.tw, t, sync, nullptr, a);
                         }
                     }
                     cp_async_wait_all();
@@ -142,7 +145,7 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                 }
             } else {
                 if (!tables_free) __syncthreads();
-                build_tables<N, PSPI, INTERP>(a, sm, w, w2, iz, tid, NT);
+                build_tables<N, PSPI, INTERP, BLU, TC>(a, sm, w, w2, iz, tid, NT);
                 if constexpr (PAIR)
                     if (tid < WPOS_STRIDE) sm.wpos[tid] = a.wpos ? a.wpos[(size_t)iz * WPOS_STRIDE + tid] : 0;
                 __syncthreads();
@@ -216,14 +219,14 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
 // sqrt(ntfft) (wem.c:277-279), is the shot's spectrum at this frequency.
 // Rows of up to 1024 samples: two CTAs per SM (their shared memory fits twice), so the
 // registers are capped at 128 per thread.
-template <int N, bool PSPI, int INTERP, int S, bool EXACT>
+template <int N, bool PSPI, int INTERP, int S, bool EXACT, bool BLU = false>
 __global__ void __launch_bounds__(S * (N / 16), N <= 1024 ? 2 : 1) wem_model_kernel(const MigArgs a, const BornArgs b)
 {
     using SH = MigShape<N>;
     constexpr int T = SH::T, PADN = SH::PADN;
     constexpr int NT = S * T;
     extern __shared__ float4 smem_raw[];
-    const Smem<N, PSPI> sm(smem_raw, a.nref, a.nmx, S);
+    const Smem<N, PSPI, BLU> sm(smem_raw, a.nref, a.nmx, S);
     const int tid = threadIdx.x;
     const int team = tid / T, t = tid - team * T;
     float2 *xbuf = sm.x + (size_t)team * PADN;
@@ -258,7 +261,7 @@ __global__ void __launch_bounds__(S * (N / 16), N <= 1024 ? 2 : 1) wem_model_ker
                 // precomputed tables, copied behind the forward transform
                 if constexpr (PSPI) {
                     copy_tables_async<N, INTERP, false>(a, sm, iwi, iz, tid, NT);
-                    if (act) fft_row<N, -1>(v, xbuf, sm.tw, t, sync);
+                    if (act) xform<N, -1, false, BLU>(v, xbuf, sm.tw, t, sync, nullptr, a);
                     cp_async_wait_all();
                     __syncthreads();
                     if (act) step_mig_tail<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync, nullptr, ref_mask(a, iz), 1.f);
@@ -314,7 +317,7 @@ __global__ void __launch_bounds__(S * (N / 16), N <= 1024 ? 2 : 1) wem_model_ker
             __syncthreads();
             if (rec) {
                 if (!(PSPI && a.ptab)) inject(iz);
-                step_model<N, PSPI, INTERP, EXACT>(v, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz));
+                step_model<N, PSPI, INTERP, EXACT, BLU>(v, a, sm, xbuf, sacc, t, sync, ref_mask(a, iz));
             }
         }
         if (shot_ok) {
@@ -339,29 +342,30 @@ template <int N> struct Shapes {
     static constexpr int S_MODEL = (T >= 256) ? 1 : (256 / T > 16 ? 16 : 256 / T);
 };
 
-template <int N, bool PSPI, int INTERP, int S, bool TC, bool PAIR = false>
+template <int N, bool PSPI, int INTERP, int S, bool TC, bool PAIR = false, bool BLU = false>
 int mig_run(const MigArgs *a, int grid, size_t smem, cudaStream_t st, int *bps)
 {
-    auto k = wem_migrate_kernel<N, PSPI, INTERP, S, TC, PAIR>;
+    auto k = wem_migrate_kernel<N, PSPI, INTERP, S, TC, PAIR, BLU>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
     if (bps) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, 2 * S * (N / 16), smem) == cudaSuccess ? 0 : -1;
     k<<<grid, 2 * S * (N / 16), smem, st>>>(*a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <int N, int S, bool TC>
+template <int N, int S, bool TC, bool BLU = false>
 int mig_sel(int pspi, int interp, const MigArgs *a, int grid, size_t smem, cudaStream_t st, int *bps)
 {
-    if (!pspi) return mig_run<N, false, 0, S, TC>(a, grid, smem, st, bps);
-    if (interp == 0) return mig_run<N, true, 0, S, TC>(a, grid, smem, st, bps);
-    return mig_run<N, true, 1, S, TC>(a, grid, smem, st, bps);
+    if (!pspi) return mig_run<N, false, 0, S, TC, false, BLU>(a, grid, smem, st, bps);
+    if (interp == 0) return mig_run<N, true, 0, S, TC, false, BLU>(a, grid, smem, st, bps);
+    return mig_run<N, true, 1, S, TC, false, BLU>(a, grid, smem, st, bps);
 }
 
 // wide = 1 selects the 512-thread shape. form: MIG_FORM_FP32; MIG_FORM_SPLIT16, the
 // tensor-core form, built for N = 2048 only (-2 otherwise); MIG_FORM_PAIRED, the paired
-// inverse transforms of the PSPI nearest-lower mode (-2 for other modes). Fills
-// *S/*threads/*smem; launches when a != nullptr and bps == nullptr, queries occupancy
-// when bps != nullptr.
+// inverse transforms of the PSPI nearest-lower mode (-2 for other modes); MIG_FORM_BLU,
+// transforms of a length that is not a power of two on N-sample rows (wide shape only).
+// Fills *S/*threads/*smem; launches when a != nullptr and bps == nullptr, queries
+// occupancy when bps != nullptr.
 template <int N>
 int mig_launch(int wide, int pspi, int interp, int nref, int nmx, const MigArgs *a, int grid, cudaStream_t st,
                int *S, int *threads, size_t *smem, int *bps, int form)
@@ -371,7 +375,12 @@ int mig_launch(int wide, int pspi, int interp, int nref, int nmx, const MigArgs 
     const int tc = form == MIG_FORM_SPLIT16;
     *S = s_;
     *threads = 2 * s_ * SH::T;
-    *smem = mig_smem_bytes<N>(pspi != 0, nref, nmx, 2 * s_, tc != 0, form == MIG_FORM_PAIRED);
+    *smem = mig_smem_bytes<N>(pspi != 0, nref, nmx, 2 * s_, tc != 0, form == MIG_FORM_PAIRED, form == MIG_FORM_BLU);
+    if (form == MIG_FORM_BLU) {
+        if (!wide) return -2;
+        if (!a && !bps) return 0;
+        return mig_sel<N, SH::S_WIDE, false, true>(pspi, interp, a, grid, *smem, st, bps);
+    }
     if (form == MIG_FORM_PAIRED) {
         if (!pspi || interp != 0) return -2;
         if (!a && !bps) return 0;
@@ -392,33 +401,42 @@ int mig_launch(int wide, int pspi, int interp, int nref, int nmx, const MigArgs 
     return mig_sel<N, SH::S_NARROW, false>(pspi, interp, a, grid, *smem, st, bps);
 }
 
-template <int N, bool PSPI, int INTERP, bool EXACT>
+template <int N, bool PSPI, int INTERP, bool EXACT, bool BLU = false>
 int model_run(const MigArgs *a, const BornArgs *b, int grid, size_t smem, cudaStream_t st, int *bps)
 {
     constexpr int S = Shapes<N>::S_MODEL;
-    auto k = wem_model_kernel<N, PSPI, INTERP, S, EXACT>;
+    auto k = wem_model_kernel<N, PSPI, INTERP, S, EXACT, BLU>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
     if (bps) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, S * (N / 16), smem) == cudaSuccess ? 0 : -1;
     k<<<grid, S * (N / 16), smem, st>>>(*a, *b);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
+template <int N, bool BLU>
+int model_sel(int pspi, int interp, int exact, const MigArgs *a, const BornArgs *b, int grid, size_t smem,
+              cudaStream_t st, int *bps)
+{
+    if (!pspi) return model_run<N, false, 0, false, BLU>(a, b, grid, smem, st, bps);
+    if (exact) {
+        if (interp == 0) return model_run<N, true, 0, true, BLU>(a, b, grid, smem, st, bps);
+        return model_run<N, true, 1, true, BLU>(a, b, grid, smem, st, bps);
+    }
+    if (interp == 0) return model_run<N, true, 0, false, BLU>(a, b, grid, smem, st, bps);
+    return model_run<N, true, 1, false, BLU>(a, b, grid, smem, st, bps);
+}
+
+// blu = 1: transforms of a length that is not a power of two on N-sample rows
 template <int N>
 int model_launch(int pspi, int interp, int exact, int nref, int nmx, const MigArgs *a, const BornArgs *b, int grid,
-                 cudaStream_t st, int *S, int *threads, size_t *smem, int *bps)
+                 cudaStream_t st, int *S, int *threads, size_t *smem, int *bps, int blu)
 {
     using SH = Shapes<N>;
     *S = SH::S_MODEL;
     *threads = SH::S_MODEL * SH::T;
-    *smem = mig_smem_bytes<N>(pspi != 0, nref, nmx, SH::S_MODEL);
+    *smem = mig_smem_bytes<N>(pspi != 0, nref, nmx, SH::S_MODEL, false, false, blu != 0);
     if (!a && !bps) return 0;
-    if (!pspi) return model_run<N, false, 0, false>(a, b, grid, *smem, st, bps);
-    if (exact) {
-        if (interp == 0) return model_run<N, true, 0, true>(a, b, grid, *smem, st, bps);
-        return model_run<N, true, 1, true>(a, b, grid, *smem, st, bps);
-    }
-    if (interp == 0) return model_run<N, true, 0, false>(a, b, grid, *smem, st, bps);
-    return model_run<N, true, 1, false>(a, b, grid, *smem, st, bps);
+    if (blu) return model_sel<N, true>(pspi, interp, exact, a, b, grid, *smem, st, bps);
+    return model_sel<N, false>(pspi, interp, exact, a, b, grid, *smem, st, bps);
 }
 
 // defined in wem_n<N>.cu
@@ -426,7 +444,7 @@ int model_launch(int pspi, int interp, int exact, int nref, int nmx, const MigAr
     extern template int mig_launch<N>(int, int, int, int, int, const MigArgs *, int, cudaStream_t, int *, int *, \
                                       size_t *, int *, int);                                                      \
     extern template int model_launch<N>(int, int, int, int, int, const MigArgs *, const BornArgs *, int,         \
-                                        cudaStream_t, int *, int *, size_t *, int *);
+                                        cudaStream_t, int *, int *, size_t *, int *, int);
 WEM_DECLARE_N(32)
 WEM_DECLARE_N(64)
 WEM_DECLARE_N(128)

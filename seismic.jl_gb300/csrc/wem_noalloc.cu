@@ -6,8 +6,13 @@
 // not stall on the allocator or fail halfway through a survey. They pass their own
 // device buffers for the inputs and the output; everything the migration needs
 // besides those (the per-velocity tables, the trace spectra, the image
-// accumulator) lives in one file-scope device array of fixed size, g_wem_scratch,
-// which every GPU that loads shotwem.so holds until the process exits.
+// accumulator) lives in one file-scope device array of fixed size, g_wem_scratch.
+// CUDA loads a module's device memory when the module is first used on a device
+// (lazy loading, the default since CUDA 12.2), so the array -- and the code of the
+// kernels this path launches -- takes its device memory at the first call on each
+// device, and keeps it until the process exits. A caller that is about to give all
+// free device memory to its own pool therefore makes one small call first (or runs
+// with CUDA_MODULE_LOADING=EAGER, which loads everything when the context is made).
 //
 // The path is the same computation as wem_migrate (wem.c:3-204 semantics) with two
 // differences: the tables are derived on the GPU from the caller's velocity instead
@@ -18,8 +23,6 @@
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
-
-#include <mutex>
 
 #include "../../include/shotwem_gb300.h"
 #include "wem_fft.cuh"
@@ -72,27 +75,20 @@ Layout noalloc_layout(int nmx, int nz, int nref, int ntw, int nf, int nwf, int n
     return L;
 }
 
-// One device pointer to g_wem_scratch per CUDA ordinal, looked up once with that
-// device current. A host-side reference to g_wem_scratch names a host shadow, not
-// device memory, so the address must come from cudaGetSymbolAddress.
-std::mutex g_mu;
-void *g_scratch_ptr[256];
-
+// The device address of g_wem_scratch on the current device. A host-side reference to
+// g_wem_scratch names a host shadow, not device memory, so the address must come from
+// cudaGetSymbolAddress with the device current. It is looked up on every call (a cheap
+// query once the module is loaded): after a cudaDeviceReset the module is loaded again
+// and the array may sit at another address.
 int scratch_for_current_device(void **out)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return set_error(WEM_ERR_CUDA, cudaGetErrorString(e));
-    if (dev < 0 || dev >= 256) return set_error(WEM_ERR_ARG, "device ordinal out of range");
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_wem_scratch);
-        if (e != cudaSuccess || !p)
-            return set_error(WEM_ERR_CUDA, "cudaGetSymbolAddress(g_wem_scratch) failed");
-        g_scratch_ptr[dev] = p;
-    }
-    *out = g_scratch_ptr[dev];
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_wem_scratch);
+    if (e != cudaSuccess || !p) return set_error(WEM_ERR_CUDA, "cudaGetSymbolAddress(g_wem_scratch) failed");
+    *out = p;
     return WEM_OK;
 }
 
@@ -110,8 +106,11 @@ struct TableArgs {
 };
 
 // The host setup of wem_prepare (wem.c:28-70 and the grids of wem.c:79-89) on the
-// GPU, same float operation order: block iz < nz builds depth iz; the extra blocks
-// fill the depth-independent tables.
+// GPU: block iz < nz builds depth iz; the extra blocks fill the depth-independent
+// tables. The integer decisions and their float arithmetic (po, pd, the reference
+// velocities, the selection bytes and the linear weights) follow the host's operation
+// order exactly. The taper (device expf) and the FFT and DFT twiddles (device sincos in
+// double) can differ from the host tables by one unit in the last place.
 __global__ void __launch_bounds__(256) noalloc_tables_kernel(const TableArgs a)
 {
     __shared__ float s_po, s_vmin, s_vmax;

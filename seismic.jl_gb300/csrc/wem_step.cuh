@@ -34,6 +34,23 @@ __device__ __forceinline__ float2 phase_entry(float w2, float slow2, float kx, f
     return make_float2(P.x * inv_n, P.y * inv_n);
 }
 
+// The same entry built in FP64 (the split16 form's tables): s = w^2 / vref^2 - kx^2 with
+// w the FP32 frequency of the kernels, vref and kx in double, the square root and the
+// sine/cosine (or the evanescent exponential) in double, rounded to FP32 once at the end.
+// Explicit roundings keep the table kernel and the in-CTA builder bit-identical.
+__device__ __forceinline__ float2 phase_entry_fp64(double wd, double vr, double kx, double dz, double inv_n)
+{
+    const double s = __dsub_rn(__ddiv_rn(__dmul_rn(wd, wd), __dmul_rn(vr, vr)), __dmul_rn(kx, kx));
+    double re, im;
+    if (s >= 0.0) {
+        sincos(__dmul_rn(__dsqrt_rn(s), dz), &im, &re);
+    } else {
+        re = exp(-__dmul_rn(__dmul_rn(0.2, __dsqrt_rn(-s)), fabs(dz)));
+        im = 0.0;
+    }
+    return make_float2(__double2float_rn(__dmul_rn(re, inv_n)), __double2float_rn(__dmul_rn(im, inv_n)));
+}
+
 __device__ __forceinline__ void kahan_add(float2 *slot, float v, float2 s)
 {
     const float y = __fsub_rn(v, s.y);
@@ -65,10 +82,16 @@ template <int N> __host__ __device__ constexpr int sel_entries(int nmx)
     return (nmx + N / 16 - 1) / (N / 16) * (N / 16);
 }
 
+// Phase-table stride (float2, even: 16-byte aligned tables). Rows of N = nkx samples hold
+// N/2 + 1 entries; rows whose transform length L = nkx is not a power of two run on
+// N-point transforms with N >= 2L - 1 (Bluestein's chirp form, BLU) and hold L/2 + 1 <=
+// N/4 + 1 entries.
+template <int N, bool BLU> __host__ __device__ constexpr int ph_stride() { return BLU ? N / 4 + 2 : MigShape<N>::PHS; }
+
 // float2 entries of the phase tables, kept even so that what follows stays 16-byte aligned
-template <int N> __host__ __device__ constexpr int ph_entries(bool pspi, int nref)
+template <int N, bool BLU = false> __host__ __device__ constexpr int ph_entries(bool pspi, int nref)
 {
-    return (pspi ? nref : 1) * MigShape<N>::PHS;
+    return (pspi ? nref : 1) * ph_stride<N, BLU>();
 }
 
 // bytes after the selection rows that the tensor-core stages use (split16 mode):
@@ -81,7 +104,8 @@ __host__ __device__ constexpr int tc_extra_bytes(int teams) { return 10240 + 8 *
 // of points taken whole follow the selection bytes.
 template <int N> __host__ __device__ constexpr int wdot_entries() { return (N / 2 + 2) & ~1; }
 
-template <int N, bool PSPI> struct Smem {
+template <int N, bool PSPI, bool BLU = false> struct Smem {
+    static constexpr int PHS = ph_stride<N, BLU>();
     float2 *tw, *ph, *corr, *x, *acc;
     uint8_t *selb;
     float *wl;
@@ -94,7 +118,7 @@ template <int N, bool PSPI> struct Smem {
         using SH = MigShape<N>;
         tw = reinterpret_cast<float2 *>(raw);
         ph = tw + SH::TWP;
-        corr = ph + ph_entries<N>(PSPI, nref);
+        corr = ph + ph_entries<N, BLU>(PSPI, nref);
         x = corr + (PSPI ? 0 : ((nmx + 1) & ~1));
         acc = x + (size_t)teams * SH::PADN;
         acc_stride = PSPI ? (paired ? N + 2 : sel_entries<N>(nmx)) : 0;
@@ -110,11 +134,11 @@ template <int N, bool PSPI> struct Smem {
 // shared-memory footprint (bytes) of one CTA with `teams` row teams
 template <int N>
 __host__ __device__ constexpr size_t mig_smem_bytes(bool pspi, int nref, int nmx, int teams, bool tc = false,
-                                                    bool paired = false)
+                                                    bool paired = false, bool blu = false)
 {
     using SH = MigShape<N>;
     const size_t base =
-        sizeof(float2) * ((size_t)SH::TWP + (size_t)ph_entries<N>(pspi, nref) + (size_t)(pspi ? 0 : ((nmx + 1) & ~1)) +
+        sizeof(float2) * ((size_t)SH::TWP + (size_t)(blu ? ph_entries<N, true>(pspi, nref) : ph_entries<N>(pspi, nref)) + (size_t)(pspi ? 0 : ((nmx + 1) & ~1)) +
                           (size_t)teams * SH::PADN +
                           (pspi ? (size_t)teams * (paired ? (size_t)N + 2 : (size_t)sel_entries<N>(nmx)) : 0)) +
         (pspi ? sizeof(float) * (size_t)((nmx + 3) & ~3) + (size_t)((nmx + 15) & ~15) : 0);
@@ -139,20 +163,27 @@ __device__ __forceinline__ unsigned long long cx_mask(const MigArgs &a, int iz)
 // PSPI: one phase table per reference velocity and the depth's selection row;
 // split-step: the phase table of the mean slowness and the correction
 // exp(i w pd dz) * taper (wem.c:326, 353-359).
-template <int N, bool PSPI, int INTERP>
-__device__ __forceinline__ void build_tables(const MigArgs &a, const Smem<N, PSPI> &sm, float w, float w2, int iz,
+// F64 (split16 PSPI): the phase tables in FP64 (phase_entry_fp64).
+template <int N, bool PSPI, int INTERP, bool BLU = false, bool F64 = false>
+__device__ __forceinline__ void build_tables(const MigArgs &a, const Smem<N, PSPI, BLU> &sm, float w, float w2, int iz,
                                              int tid, int nthreads)
 {
-    constexpr int HALF = MigShape<N>::HALF;
+    const int HALF = BLU ? a.nlog / 2 + 1 : MigShape<N>::HALF;
     if (PSPI) {
         const float *sl = a.slow2 + (size_t)iz * a.nref;
         const unsigned long long used = ref_mask(a, iz);
         for (int r = 0; r < a.nref; r++) {
             if (!((used >> r) & 1ull)) continue;  // no grid point takes this reference
             const float slow2 = sl[r];
-            float2 *ph = sm.ph + (size_t)r * MigShape<N>::PHS;
-            for (int kk = tid; kk < HALF; kk += nthreads)
-                ph[kk] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
+            float2 *ph = sm.ph + (size_t)r * sm.PHS;
+            if constexpr (F64) {
+                const double vr = a.vref64[(size_t)iz * a.nref + r], inv_n = 1.0 / (double)a.nlog;
+                for (int kk = tid; kk < HALF; kk += nthreads)
+                    ph[kk] = phase_entry_fp64((double)w, vr, __dmul_rn((double)kk, a.dkx64), (double)a.dz, inv_n);
+            } else {
+                for (int kk = tid; kk < HALF; kk += nthreads)
+                    ph[kk] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
+            }
         }
         const uint8_t *sr = a.selb + (size_t)iz * a.nmx;
         for (int x = tid; x < a.nmx; x += nthreads) sm.selb[x] = sr[x];
@@ -184,12 +215,68 @@ template <int N> __device__ __forceinline__ int kfold(int t, int m)
     return m < 8 ? t + T * m : T * (16 - m) - t;
 }
 
+// |k| (phase-table index) of position m of thread t for a transform of length L: k for
+// k <= L/2, L - k above (the reference's kx of wem.c:340-341, 430-431); positions k >= L
+// of an N-point row carrying a shorter transform (BLU) hold zeros and read entry 0.
+template <int N, bool BLU> __device__ __forceinline__ int kidx(int t, int m, int L)
+{
+    if constexpr (!BLU) {
+        return kfold<N>(t, m);
+    } else {
+        const int k = t + (N / 16) * m;
+        return k < L ? (2 * k <= L ? k : L - k) : 0;
+    }
+}
+
+// The row transform of the depth step. Rows of N = nkx samples: the N-point FFT, the
+// spectrum at k = t + T*m. BLU: a transform of length L = a.nlog (not a power of two) as
+// circular convolutions of length N >= 2L - 1 (Bluestein, IEEE Trans. Audio Electroacoust.
+// 18 (1970); chirp b[n] = e^{i pi n^2 / L}, nk = (n^2 + k^2 - (k - n)^2) / 2):
+//   forward  Z[k] = sum_n (x[n] conj b[n]) b[k - n] = X[k] b[k]   (k < L; zero above),
+//   inverse  x[n] = b[n] sum_k W[k] conj b[n - k],  W[k] = U[k] b[k].
+// The spectrum is kept as Z = X b: a pointwise multiplier P[|k|] maps Z to U b, so the
+// chirps between the two transforms cancel and each one is two N-point FFTs around a
+// multiply by G/N (a.bfft, G = FFT_N of b placed at j and N - j) or its conjugate.
+// a.chirp holds b[n] for n < L (built in FP64 on the host). Unnormalised like the FFT:
+// the 1/L of the pair is in the phase tables.
+template <int N, int DIR, bool TC, bool BLU>
+__device__ __forceinline__ void xform(float2 (&v)[16], float2 *xbuf, const float2 *tw, int t, unsigned sync,
+                                      TcTeam *tc, const MigArgs &a)
+{
+    if constexpr (!BLU) {
+        fft_row<N, DIR, TC>(v, xbuf, tw, t, sync, tc);
+    } else {
+        constexpr int T = N / 16;
+        const int L = a.nlog;
+        if constexpr (DIR < 0) {
+#pragma unroll
+            for (int m = 0; m < 16; m++) {
+                const int x = t + T * m;
+                v[m] = x < L ? cmulc(v[m], __ldg(a.chirp + x)) : make_float2(0.f, 0.f);
+            }
+        }
+        fft_row<N, -1>(v, xbuf, tw, t, sync);
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const float2 G = __ldg(a.bfft + t + T * m);
+            v[m] = DIR < 0 ? cmul(v[m], G) : cmulc(v[m], G);
+        }
+        fft_row<N, +1>(v, xbuf, tw, t, sync);
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int k = t + T * m;
+            if (k >= L) v[m] = make_float2(0.f, 0.f);
+            else if (DIR > 0) v[m] = cmul(v[m], __ldg(a.chirp + k));
+        }
+    }
+}
+
 // The thread's selection bytes of the current depth (from shared memory), four per
 // register: bits 0-6 iref1, bit 7 set where the reference interpolates
 // (vref2 - vref1 > 10, wem.c:454); positions beyond nmx get 0x7f, which matches no
 // reference. Linear mode also loads the weight of iref2 (= iref1 + 1 there).
-template <int N, int INTERP, bool PSPI>
-__device__ __forceinline__ void load_sel(const Smem<N, PSPI> &sm, int nmx, int t, uint32_t (&selp)[4], float (&wl)[16])
+template <int N, int INTERP, bool PSPI, bool BLU = false>
+__device__ __forceinline__ void load_sel(const Smem<N, PSPI, BLU> &sm, int nmx, int t, uint32_t (&selp)[4], float (&wl)[16])
 {
     constexpr int T = N / 16;
 #pragma unroll
@@ -226,8 +313,8 @@ __device__ __forceinline__ float sel_weight(const uint32_t (&selp)[4], const flo
 // used: the references in use at this depth (ref_mask); the others are skipped.
 // step_mig_tail is everything after the forward transform (v holds the spectrum at
 // k = t + T*m; inv_s undoes the split16 row scaling), step_mig the whole step.
-template <int N, bool PSPI, int INTERP, bool TC = false>
-__device__ __forceinline__ void step_mig_tail(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, PSPI> &sm,
+template <int N, bool PSPI, int INTERP, bool TC = false, bool BLU = false>
+__device__ __forceinline__ void step_mig_tail(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, PSPI, BLU> &sm,
                                               float2 *xbuf, float2 *sacc, int t, unsigned sync, TcTeam *tc,
                                               unsigned long long used, float inv_s)
 {
@@ -247,14 +334,14 @@ __device__ __forceinline__ void step_mig_tail(float2 (&v)[16], bool conj, const 
         for (int q = 0; q < 4; q++) i1p[q] = selp[q] & 0x7f7f7f7fu;
         for (int r = 0; r < a.nref; r++) {
             if (!((used >> r) & 1ull)) continue;  // CTA-uniform
-            const float2 *ph = sm.ph + (size_t)r * MigShape<N>::PHS;
+            const float2 *ph = sm.ph + (size_t)r * sm.PHS;
             float2 u[16];
 #pragma unroll
             for (int m = 0; m < 16; m++) {
-                const float2 P = ph[kfold<N>(t, m)];
+                const float2 P = ph[kidx<N, BLU>(t, m, a.nlog)];
                 u[m] = conj ? cmulc(v[m], P) : cmul(v[m], P);
             }
-            fft_row<N, +1, TC>(u, xbuf, sm.tw, t, sync, tc);
+            xform<N, +1, TC, BLU>(u, xbuf, sm.tw, t, sync, tc, a);
             if constexpr (INTERP == 0) {
                 // the nearest-lower wavefield, whole or its real part (wem.c:454-459, 477):
                 // the positions that take reference r, found four at a time
@@ -301,10 +388,10 @@ __device__ __forceinline__ void step_mig_tail(float2 (&v)[16], bool conj, const 
         float2 acc[16];
 #pragma unroll
         for (int m = 0; m < 16; m++) {
-            const float2 P = sm.ph[kfold<N>(t, m)];
+            const float2 P = sm.ph[kidx<N, BLU>(t, m, a.nlog)];
             acc[m] = conj ? cmulc(v[m], P) : cmul(v[m], P);
         }
-        fft_row<N, +1, TC>(acc, xbuf, sm.tw, t, sync, tc);
+        xform<N, +1, TC, BLU>(acc, xbuf, sm.tw, t, sync, tc, a);
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             const int x = t + T * m;
@@ -314,8 +401,8 @@ __device__ __forceinline__ void step_mig_tail(float2 (&v)[16], bool conj, const 
     }
 }
 
-template <int N, bool PSPI, int INTERP, bool TC = false>
-__device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, PSPI> &sm,
+template <int N, bool PSPI, int INTERP, bool TC = false, bool BLU = false>
+__device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigArgs &a, const Smem<N, PSPI, BLU> &sm,
                                          float2 *xbuf, float2 *sacc, int t, unsigned sync, TcTeam *tc = nullptr,
                                          unsigned long long used = ~0ull)
 {
@@ -327,8 +414,8 @@ __device__ __forceinline__ void step_mig(float2 (&v)[16], bool conj, const MigAr
 #pragma unroll
         for (int m = 0; m < 16; m++) v[m] = cscale(v[m], s);
     }
-    fft_row<N, -1, TC>(v, xbuf, sm.tw, t, sync, tc);  // v now holds the spectrum at k = t + T*m
-    step_mig_tail<N, PSPI, INTERP, TC>(v, conj, a, sm, xbuf, sacc, t, sync, tc, used, inv_s);
+    xform<N, -1, TC, BLU>(v, xbuf, sm.tw, t, sync, tc, a);  // v now holds the spectrum at k = t + T*m
+    step_mig_tail<N, PSPI, INTERP, TC, BLU>(v, conj, a, sm, xbuf, sacc, t, sync, tc, used, inv_s);
 }
 
 // e^{+2 pi i e / N}, e in [0, N), from the table of e in [0, N/2]
@@ -524,11 +611,11 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src)
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-template <int N, int INTERP, bool PAIR>
-__device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N, true> &sm, int iwi, int iz, int tid,
+template <int N, int INTERP, bool PAIR, bool BLU = false>
+__device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N, true, BLU> &sm, int iwi, int iz, int tid,
                                                   int nthreads, unsigned long long used)
 {
-    constexpr int PHS = MigShape<N>::PHS, CH = PHS / 2;  // 16-byte chunks per table
+    constexpr int PHS = Smem<N, true, BLU>::PHS, CH = PHS / 2;  // 16-byte chunks per table
     const float4 *src = reinterpret_cast<const float4 *>(a.ptab + ((size_t)iwi * a.nz + iz) * a.nref * PHS);
     float4 *dst = reinterpret_cast<float4 *>(sm.ph);
     used &= (a.nref >= 64 ? ~0ull : ((1ull << a.nref) - 1ull));
@@ -549,11 +636,11 @@ __device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N
         cp_async16(reinterpret_cast<float4 *>(sm.wpos) + tid, reinterpret_cast<const float4 *>(a.wpos + (size_t)iz * WPOS_STRIDE) + tid);
     cp_async_commit();
 }
-template <int N, int INTERP, bool PAIR>
-__device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N, true> &sm, int iwi, int iz, int tid,
+template <int N, int INTERP, bool PAIR, bool BLU = false>
+__device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N, true, BLU> &sm, int iwi, int iz, int tid,
                                                   int nthreads)
 {
-    copy_tables_async<N, INTERP, PAIR>(a, sm, iwi, iz, tid, nthreads, ref_mask(a, iz));
+    copy_tables_async<N, INTERP, PAIR, BLU>(a, sm, iwi, iz, tid, nthreads, ref_mask(a, iz));
 }
 
 // One upward step of the modelling recursion (wem.c:273-274, -dz, adj=false), in
@@ -565,13 +652,13 @@ __device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N
 // PSPI scatters the row into the reference wavefields with the transposed
 // interpolation weights before transforming, y = sum_r F^-1 conj(P_r) F (W_r^T v);
 // for split-step the reference's operator already is that adjoint.
-template <int N, bool PSPI, int INTERP, bool EXACT>
-__device__ __forceinline__ void step_model(float2 (&v)[16], const MigArgs &a, const Smem<N, PSPI> &sm, float2 *xbuf,
+template <int N, bool PSPI, int INTERP, bool EXACT, bool BLU = false>
+__device__ __forceinline__ void step_model(float2 (&v)[16], const MigArgs &a, const Smem<N, PSPI, BLU> &sm, float2 *xbuf,
                                            float2 *sacc, int t, unsigned sync, unsigned long long used = ~0ull)
 {
     constexpr int T = N / 16;
     if (PSPI && !EXACT) {
-        step_mig<N, PSPI, INTERP>(v, true, a, sm, xbuf, sacc, t, sync, nullptr, used);
+        step_mig<N, PSPI, INTERP, false, BLU>(v, true, a, sm, xbuf, sacc, t, sync, nullptr, used);
         return;
     }
     float2 acc[16];
@@ -581,9 +668,9 @@ __device__ __forceinline__ void step_model(float2 (&v)[16], const MigArgs &a, co
             const int x = t + T * m;
             acc[m] = x < a.nmx ? cmulc(v[m], sm.corr[x]) : make_float2(0.f, 0.f);
         }
-        fft_row<N, -1>(acc, xbuf, sm.tw, t, sync);
+        xform<N, -1, false, BLU>(acc, xbuf, sm.tw, t, sync, nullptr, a);
 #pragma unroll
-        for (int m = 0; m < 16; m++) acc[m] = cmulc(acc[m], sm.ph[kfold<N>(t, m)]);
+        for (int m = 0; m < 16; m++) acc[m] = cmulc(acc[m], sm.ph[kidx<N, BLU>(t, m, a.nlog)]);
     } else {
         uint32_t selp[4];
         float wl[16];
@@ -599,17 +686,17 @@ __device__ __forceinline__ void step_model(float2 (&v)[16], const MigArgs &a, co
                 const float wgt = sel_weight<INTERP>(selp, wl, m, r, re_only);
                 u[m] = make_float2(v[m].x * wgt, re_only ? 0.f : v[m].y * wgt);
             }
-            fft_row<N, -1>(u, xbuf, sm.tw, t, sync);
-            const float2 *ph = sm.ph + (size_t)r * MigShape<N>::PHS;
+            xform<N, -1, false, BLU>(u, xbuf, sm.tw, t, sync, nullptr, a);
+            const float2 *ph = sm.ph + (size_t)r * sm.PHS;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
-                const float2 q = cmulc(u[m], ph[kfold<N>(t, m)]);
+                const float2 q = cmulc(u[m], ph[kidx<N, BLU>(t, m, a.nlog)]);
                 acc[m].x += q.x;
                 acc[m].y += q.y;
             }
         }
     }
-    fft_row<N, +1>(acc, xbuf, sm.tw, t, sync);
+    xform<N, +1, false, BLU>(acc, xbuf, sm.tw, t, sync, nullptr, a);
 #pragma unroll
     for (int m = 0; m < 16; m++) {
         const int x = t + T * m;

@@ -28,7 +28,7 @@ PRECISION = {"fp32": 0, "split16": 1}
 EXPORTS = ["wem_last_error", "wem_version", "wem_ctx_create", "wem_ctx_destroy", "wem_prepare",
            "wem_migrate", "wem_migrate_device", "wem_migrate_survey", "wem_last_timing",
            "wem_last_kernel_times", "wem_last_launch", "wem_ctx_stream", "wem_migrate_noalloc", "wem_model",
-           "wem_model_device", "wem_angles", "wem", "wem_selftest_wait_timeout",
+           "wem_model_device", "wem_angles", "wem", "wem_selftest_wait_timeout", "wem_measure_fp32_peak",
            "shotwem_main", "main"]
 
 
@@ -88,6 +88,7 @@ def lib():
         ip = C.POINTER(C.c_int)
         L.wem_last_launch.argtypes = [vp, ip, ip, ip, ip, ip]
         L.wem_selftest_wait_timeout.argtypes = [C.c_int, ip, C.POINTER(C.c_float)]
+        L.wem_measure_fp32_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
         L.wem_angles.argtypes = [vp, C.POINTER(Params), fp, fp, C.c_int, fp, fp, fp, fp]
         L.wem_ctx_stream.argtypes = [vp, C.POINTER(vp)]
         L.wem_migrate_noalloc.argtypes = [C.POINTER(Params), vp, vp, C.c_int, fp, fp, vp, vp, vp]
@@ -101,6 +102,13 @@ def lib():
                           C.c_int, C.c_bool, C.c_bool, C.c_bool]
         _lib = L
     return _lib
+
+
+def measure_fp32_peak(device: int = 0) -> float:
+    """Measured FP32 FMA throughput of the device in TFLOP/s (wem_measure_fp32_peak)."""
+    v = C.c_double()
+    check(lib().wem_measure_fp32_peak(device, C.byref(v)))
+    return float(v.value)
 
 
 def check(rc: int):

@@ -147,6 +147,40 @@ def config1(seed: int = 1001, nshot: int = 64, nx: int = 1024, nz: int = 500, nt
                 shots=shots)
 
 
+def random_reflectivity(seed: int, nx: int, nz: int, density: float = 0.01) -> np.ndarray:
+    """Seeded reflectivity [nx, nz]: `density` of the cells nonzero, N(0, 1) amplitudes."""
+    rng = np.random.default_rng(seed)
+    m = np.zeros((nx, nz), np.float32)
+    k = int(round(density * m.size))
+    m.flat[rng.choice(m.size, k, replace=False)] = rng.standard_normal(k).astype(np.float32)
+    return m
+
+
+def with_born_data(c: dict, ctx=None, seed: int | None = None, density: float = 0.01) -> dict:
+    """The survey c with its traces replaced by Born data of a seeded random reflectivity
+    (1 % of the cells, N(0, 1)): the reference's forward operator (wem.c:252-281, adj=false)
+    run by the GPU library on every shot's receivers (wem_model, exact=0). The traces keep
+    each shot's aperture. c["reflectivity"] holds the model."""
+    from .api import Context
+    p = c["params"]
+    seed = (int(p["nmx"]) * 7919 + int(p["nz"])) if seed is None else seed
+    m = random_reflectivity(seed, int(p["nmx"]) * int(p.get("nmy", 1)), int(p["nz"]), density)
+    own = ctx is None
+    ctx = Context() if own else ctx
+    try:
+        ctx.prepare(p, c["vel"], c["wav"])
+        d = ctx.model(c["shots"], m, exact=False)
+    finally:
+        if own:
+            ctx.close()
+    s = c["shots"]
+    out = dict(c)
+    out["shots"] = Shots(s.sx, s.sy, s.trace_offset, s.trace_cell, np.ascontiguousarray(d, np.float32))
+    out["reflectivity"] = m
+    out["name"] = c["name"] + ", Born data of a 1 % random reflectivity"
+    return out
+
+
 def dipping_layers(rng, nx, nz, dx, dz, nlayer, vlo, vhi):
     x = np.arange(nx) * dx
     depths = np.sort(rng.uniform(0.1, 0.95, nlayer)) * nz * dz

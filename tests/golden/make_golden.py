@@ -32,6 +32,12 @@ CASES = {
     "pspi_64": (13, 64, 24, 128, 1, 4, 40.0, 2, 2),
     "pspi_128_r8": (14, 128, 16, 96, 1, 8, 30.0, 2, 1),
     "pspi_64_padx1": (15, 64, 12, 64, 1, 3, 40.0, 1, 2),
+    # row lengths nkx = padx*nmx that are not powers of two (FFTW plans any length, wem.c:103-104)
+    "pspi_500_padx2": (16, 500, 12, 256, 1, 4, 30.0, 2, 2),   # nkx 1000 = 2^3 5^3
+    "ss_300_padx2": (17, 300, 12, 96, 0, 2, 30.0, 2, 2),      # nkx 600, taper on
+    "pspi_768_padx2": (18, 768, 8, 64, 1, 3, 25.0, 2, 2),     # nkx 1536 = 2^9 3
+    "pspi_97_padx1": (19, 97, 16, 96, 1, 4, 40.0, 1, 2),      # nkx 97, a prime
+    "ss_50_padx1": (20, 50, 16, 96, 0, 2, 40.0, 1, 2),        # nkx 50
 }
 
 
@@ -46,12 +52,14 @@ def case_inputs(seed, nx, nz, nt, pspi, nref, fmax, padx, padt):
     return p, c["vel"], c["wav"], d, m_in
 
 
-def main():
+def main(only=None):
     O.build()
     if O.build_ref() is None:
         sys.exit("reference sources not found: golden vectors come from the reference itself")
     os.environ.setdefault("OMP_NUM_THREADS", "4")
     for name, args in CASES.items():
+        if only and name not in only:
+            continue
         p, vel, wav, d, m_in = case_inputs(*args)
         m_ref = O.wem_ref(p, vel, wav, d=d, adj=True)
         d_ref = O.wem_ref(p, vel, wav, m=m_in, adj=False)
@@ -59,6 +67,8 @@ def main():
                             m_ref=m_ref, d_ref=d_ref,
                             params=np.array(repr({k: v for k, v in p.items()})))
         print(name, "image norm", float(np.linalg.norm(m_ref)), "data norm", float(np.linalg.norm(d_ref)))
+    if only:
+        return
 
     # 3-D (nmy > 1): rank-2 transforms over (nkx, nky), wem.c:100-104
     for name, (seed, pspi) in {"ss3d_32": (21, 0), "pspi3d_32": (22, 1)}.items():
@@ -122,6 +132,9 @@ def angles_main():
 if __name__ == "__main__":
     if sys.argv[1:] == ["angles"]:
         angles_main()
+    elif sys.argv[1:2] == ["--only"]:
+        # python tests/golden/make_golden.py --only name[,name...]: those 2-D cases only
+        main(set(sys.argv[2].split(",")))
     else:
         main()
         subprocess.run([sys.executable, os.path.abspath(__file__), "angles"], check=True,

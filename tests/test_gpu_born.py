@@ -12,7 +12,7 @@ from conftest import load_golden, rel_l2
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-4
-GOLDEN_CASES = ["ss_64", "ss_128_taper", "pspi_64", "pspi_128_r8", "pspi_64_padx1"]
+GOLDEN_CASES = ["ss_64", "ss_128_taper", "pspi_64", "pspi_128_r8", "pspi_64_padx1", "pspi_500_padx2", "ss_300_padx2", "pspi_768_padx2", "pspi_97_padx1", "ss_50_padx1"]
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
@@ -22,10 +22,13 @@ def test_wem_dropin_modelling_matches_reference_golden(gpu_lib, case):
     assert rel_l2(d, g["d_ref"]) < TOL
 
 
-@pytest.mark.parametrize("pspi,interp", [(0, "ref"), (1, "ref"), (1, "linear")])
-def test_batched_modelling_matches_port(gpu_lib, oracle_mod, pspi, interp):
+@pytest.mark.parametrize("pspi,interp,nx", [(0, "ref", 64), (1, "ref", 64), (1, "linear", 64), (0, "ref", 300),
+                                             (1, "ref", 500), (1, "linear", 97)])
+def test_batched_modelling_matches_port(gpu_lib, oracle_mod, pspi, interp, nx):
+    """Born modelling of several shots in one call vs the port shot by shot; nx 300, 500 and 97
+    give rows of nkx 600, 1000 and 194 (Bluestein's form)."""
     from wemgpu import synth
-    c = synth.small_case(81, nx=64, nz=20, nt=128, nshot=3, pspi=pspi, nref=4, interp=interp)
+    c = synth.small_case(81, nx=nx, nz=20, nt=128, nshot=3, pspi=pspi, nref=4, interp=interp)
     p, shots = c["params"], c["shots"]
     rng = np.random.default_rng(3)
     m = rng.standard_normal((p["nmx"], p["nz"])).astype(np.float32)
@@ -51,7 +54,8 @@ def _pair(gpu_lib, c):
     return ctx, fwd, adj
 
 
-@pytest.mark.parametrize("pspi,interp,nx", [(0, "ref", 128), (1, "ref", 64), (1, "linear", 64), (1, "linear", 512)])
+@pytest.mark.parametrize("pspi,interp,nx", [(0, "ref", 128), (1, "ref", 64), (1, "linear", 64), (1, "linear", 512),
+                                             (1, "linear", 300), (0, "ref", 150)])
 def test_dot_product_of_exact_pair(gpu_lib, pspi, interp, nx):
     """<d, L m> = <L' d, m> to 1e-5 (src/Tools/DotTest.jl), L = wem_model(exact), L' = wem_migrate."""
     from wemgpu import synth

@@ -16,7 +16,7 @@ from conftest import load_golden, rel_l2
 pytestmark = pytest.mark.gpu
 TOL = 1e-4
 
-GOLDEN_CASES = ["ss_64", "ss_128_taper", "pspi_64", "pspi_128_r8", "pspi_64_padx1"]
+GOLDEN_CASES = ["ss_64", "ss_128_taper", "pspi_64", "pspi_128_r8", "pspi_64_padx1", "pspi_500_padx2", "ss_300_padx2", "pspi_768_padx2", "pspi_97_padx1", "ss_50_padx1"]
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)
@@ -60,6 +60,41 @@ def test_row_lengths(gpu_lib, oracle_mod, nx, padx):
     m = gpu_lib.migrate(c["params"], c["vel"], c["wav"], c["shots"])
     want = _port_stack(oracle_mod, c["params"], c["vel"], c["wav"], c["shots"])
     assert rel_l2(m, want) < TOL
+
+
+@pytest.mark.parametrize("nx,padx,pspi,interp", [
+    (500, 2, 1, "ref"), (500, 2, 1, "linear"), (300, 2, 0, "ref"), (768, 2, 1, "ref"), (1023, 2, 1, "linear"),
+    (97, 1, 1, "ref"), (50, 1, 0, "ref"), (1000, 1, 1, "ref"), (9, 1, 1, "linear")])
+def test_row_lengths_not_power_of_two(gpu_lib, oracle_mod, nx, padx, pspi, interp):
+    """nkx = padx*nmx of any length in [9, 2048] (the reference plans FFTW transforms of any
+    length, wem.c:103-104): nkx 1000, 600, 1536, 2046, 97 (prime), 50, 1000, 9. The depth
+    kernels run them on power-of-two rows in Bluestein's chirp form; several shots against
+    the port and the FP64 operator."""
+    from wemgpu import synth
+    c = synth.small_case(61 + nx + padx, nx=nx, nz=8, nt=128, nshot=3, pspi=pspi, nref=4, interp=interp,
+                         fmax=30.0, padx=padx)
+    m = gpu_lib.migrate(c["params"], c["vel"], c["wav"], c["shots"])
+    want = _port_stack(oracle_mod, c["params"], c["vel"], c["wav"], c["shots"])
+    want64 = _port_stack(oracle_mod, c["params"], c["vel"], c["wav"], c["shots"], fp64=True)
+    assert rel_l2(want, want64) < TOL  # the reference's own FP32 floor on this case
+    assert rel_l2(m, want64) < TOL
+    assert rel_l2(m, want) < TOL
+
+
+def test_row_length_limits(gpu_lib):
+    """Lengths with no kernel are refused with WEM_ERR_SIZE instead of running anything:
+    below 9, non-powers of two above 2048 (their chirp rows would exceed 4096 samples),
+    and the split16 form off its 2048-point rows."""
+    from wemgpu import synth
+    from wemgpu._lib import WemError, WEM_ERR_SIZE
+    c = synth.small_case(5, nx=64, nz=4, nt=64, nshot=1)
+    for nmx, padx, prec in ((4, 2, "fp32"), (2049, 1, "fp32"), (500, 2, "split16")):
+        p = dict(c["params"], nmx=nmx, padx=padx, precision=prec)
+        vel = np.full((nmx, 4), 2000.0, np.float32)
+        with gpu_lib.Context() as ctx:
+            with pytest.raises(WemError) as e:
+                ctx.prepare(p, vel, c["wav"])
+            assert e.value.code == WEM_ERR_SIZE
 
 
 def test_deterministic(gpu_lib):
@@ -246,3 +281,11 @@ def test_source_and_receiver_depth(gpu_lib, oracle_mod):
     want = _port_stack(oracle_mod, p, c["vel"], c["wav"], c["shots"])
     assert rel_l2(m, want) < TOL
     assert not np.any(m[:, :10])
+
+
+def test_measured_fp32_peak_is_plausible(gpu_lib):
+    """wem_measure_fp32_peak (the denominator of the depth kernels' CUDA-core roofline):
+    152 SMs x 128 FP32 lanes x 2 FLOPs at up to 2.07 GHz is 80.5 TFLOP/s nominal."""
+    from wemgpu._lib import measure_fp32_peak
+    v = measure_fp32_peak(0)
+    assert 20.0 < v < 100.0, v
