@@ -78,10 +78,16 @@ def survey(workload: str, rank: int, born: str = "gpu"):
     return c, wl
 
 
+def cpu_sample_shots(nshot: int, k: int = 4) -> list[int]:
+    """The shots the CPU legs time: k evenly spaced ones."""
+    k = min(k, nshot)
+    return [int((2 * i + 1) * nshot // (2 * k)) for i in range(k)]
+
+
 def born_data_port_shot(c: dict) -> dict:
-    """The CPU sample's shot (the middle one) with Born data of the same seeded reflectivity
-    as synth.with_born_data, modelled by the oracle's port of the reference's forward
-    operator (wem.c:252-281) on the host cores; the other shots keep their traces."""
+    """The CPU sample's shots (cpu_sample_shots) with Born data of the same seeded
+    reflectivity as synth.with_born_data, modelled by the oracle's port of the reference's
+    forward operator (wem.c:252-281) on the host cores; the other shots keep their traces."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from wemgpu import Shots, synth
@@ -89,12 +95,12 @@ def born_data_port_shot(c: dict) -> dict:
     p, shots = c["params"], c["shots"]
     nmx, nz = int(p["nmx"]), int(p["nz"])
     m = synth.random_reflectivity(nmx * 7919 + nz, nmx, nz)
-    s = shots.nshot // 2
-    full = O.wem_port(dict(p, sx=float(shots.sx[s])), c["vel"], c["wav"], m=m, adj=False,
-                      nthreads=os.cpu_count() or 1)
-    lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
     data = shots.data.copy()
-    data[lo:hi] = full[shots.trace_cell[lo:hi]]
+    for s in cpu_sample_shots(shots.nshot):
+        full = O.wem_port(dict(p, sx=float(shots.sx[s])), c["vel"], c["wav"], m=m, adj=False,
+                          nthreads=os.cpu_count() or 1)
+        lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
+        data[lo:hi] = full[shots.trace_cell[lo:hi]]
     out = dict(c)
     out["shots"] = Shots(shots.sx, shots.sy, shots.trace_offset, shots.trace_cell, data)
     return out
@@ -192,8 +198,7 @@ def accuracy(c: dict, ctx_factory, nsample: int = 4) -> dict:
     O.build()
     p = dict(c["params"])
     shots = c["shots"]
-    k = min(nsample, shots.nshot)
-    which = [int((2 * i + 1) * shots.nshot // (2 * k)) for i in range(k)]
+    which = cpu_sample_shots(shots.nshot, nsample)
     offs, cells, data = [0], [], []
     for s in which:
         lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
@@ -359,19 +364,19 @@ def executed_flops_per_unit(p: dict, vel, paired: bool) -> tuple[float, float, f
     return 2 * F + 3 * nmx, x, r_used
 
 
-def cpu_baseline(c, seconds_hint: float = 20.0):
-    """The reference's CPU algorithm on one shot of the survey (every frequency), all
-    host cores. oracle/_ref (the reference's own C core) when it was built on this
-    machine, else the oracle port of it."""
+def cpu_baseline(c, nsample: int = 4, which=None):
+    """The reference's CPU algorithm on `nsample` evenly spaced shots of the survey (every
+    frequency; about 20-25 s on the GPU host's cores), all host cores, one shot at a time as
+    the Julia wrapper calls it. oracle/_ref (the reference's own C core) when it was built
+    on this machine, else the oracle port of it. `which` picks the shots instead."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from wemgpu import synth
     O.build()
     p = dict(c["params"])
     shots = c["shots"]
-    s = shots.nshot // 2
-    p["sx"] = float(shots.sx[s])
-    d = synth.shot_gather_full(shots, s, int(p["nmx"]) * int(p.get("nmy", 1)))
+    if which is None:
+        which = cpu_sample_shots(shots.nshot, nsample)
     cores = os.cpu_count() or 1
     kind = "reference" if O.ref_available() else "port"
     nf_all = band(p)
@@ -379,16 +384,20 @@ def cpu_baseline(c, seconds_hint: float = 20.0):
         # a 3-D depth step costs ~1000x a 2-D one: the sample is the lowest 17 frequencies
         # (the band edge is (int)fmax, wem.c:86), about one per host core
         p["fmax"] = float(p["fmin"]) + 2.0
-    t0 = time.perf_counter()
-    if kind == "reference":
-        O.wem_ref(p, c["vel"], c["wav"], d=d, adj=True)
-        cores = O.omp_threads()
-    else:
-        O.wem_port(p, c["vel"], c["wav"], d=d, adj=True, nthreads=cores)
-    dt = time.perf_counter() - t0
-    units = band(p) * int(p["nz"])
+    dt = 0.0
+    for s in which:
+        q = dict(p, sx=float(shots.sx[s]))
+        d = synth.shot_gather_full(shots, s, int(p["nmx"]) * int(p.get("nmy", 1)))
+        t0 = time.perf_counter()
+        if kind == "reference":
+            O.wem_ref(q, c["vel"], c["wav"], d=d, adj=True)
+            cores = O.omp_threads()
+        else:
+            O.wem_port(q, c["vel"], c["wav"], d=d, adj=True, nthreads=cores)
+        dt += time.perf_counter() - t0
+    units = len(which) * band(p) * int(p["nz"])
     return {"value": units / dt, "unit": "shot*omega*depth-steps/s", "cores": cores, "kind": kind,
-            "sample": f"1 of {shots.nshot} shots, {band(p)} of {nf_all} frequencies x {p['nz']} depth steps "
+            "sample": f"shots {which} of {shots.nshot}, {band(p)} of {nf_all} frequencies x {p['nz']} depth steps "
                       f"({units} units) in {dt:.1f} s"}
 
 
@@ -402,7 +411,9 @@ def run_reference_arm(args):
     vals = []
     info = None
     for i in range(args.warmup + args.steps):
-        info = cpu_baseline(c)
+        # one shot per step, cycling over the CPU sample's shots (their apertures differ)
+        sample = cpu_sample_shots(c["shots"].nshot)
+        info = cpu_baseline(c, which=[sample[i % len(sample)]])
         if i >= args.warmup:
             vals.append(info["value"])
     v = statistics.mean(vals)
@@ -411,7 +422,8 @@ def run_reference_arm(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * (nf * int(p["nz"])) / v, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": wl, "step": "one shot of the survey on the host cores"},
+            "config": {"workload": wl, "step": "one shot of the survey on the host cores, cycling over 4 evenly "
+                                                "spaced shots"},
             "cpu_baseline": info,
             "e2e": {"value": v, "unit": "shot*omega*depth-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -621,6 +633,8 @@ def main():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split16"],
                     help="split16: the FFTs' DFT stages on the tensor cores (split fp16 operands)")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the image-error check against the FP64 oracle")
+    ap.add_argument("--fmax", type=float, default=None,
+                    help="upper band edge in Hz instead of the workload's (smaller cases for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -642,6 +656,9 @@ def main():
     if not os.path.exists(wemgpu.LIB_PATH):
         raise SystemExit("shotwem.so is not built: python -c 'import __graft_entry__ as g; g.build()'")
     c, wl = survey(args.workload, rank)
+    if args.fmax is not None:
+        c["params"] = dict(c["params"], fmax=float(args.fmax))
+        wl += f" [band cut to {c['params']['fmin']:g}-{args.fmax:g} Hz]"
     if args.workload == "angles8":
         return run_angles(args, c, wl, rank, world, local)
     if args.precision != "fp32":
@@ -686,15 +703,24 @@ def main():
     elapsed = float(t.item())
     value = world * units * args.steps / elapsed
 
-    # end to end through the public API with host buffers
-    e2e_t = []
+    # end to end through the public API with host buffers: the traces in pinned host memory
+    # (the contract's e2e), and beside it from ordinary pageable memory (what a caller that
+    # does not pin gets: the library stages the copy through its own pinned slots)
+    from wemgpu import Shots
+    pinned = torch.from_numpy(np.ascontiguousarray(shots.data)).pin_memory()
+    shots_pinned = Shots(shots.sx, shots.sy, shots.trace_offset, shots.trace_cell, pinned.numpy())
     img = np.zeros((int(p["nmx"]) * int(p.get("nmy", 1)), nz), np.float32)
-    for _ in range(max(1, args.e2e_steps)):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        img = ctx.migrate(shots)
-        e2e_t.append(time.perf_counter() - t0)
-    e2e_s = statistics.mean(e2e_t)
+
+    def e2e_time(sv):
+        ts = []
+        for _ in range(max(1, args.e2e_steps)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = ctx.migrate(sv)
+            ts.append(time.perf_counter() - t0)
+        return statistics.mean(ts), out
+    e2e_s, img = e2e_time(shots_pinned)
+    e2e_page_s, _ = e2e_time(shots)
     te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
     if dist:
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
@@ -725,8 +751,7 @@ def main():
     if tr and tr["stale"]:
         roof["traffic_note"] = "the recorded ncu capture is of older kernel sources; not reported"
     if int(p.get("pspi", 1)) and int(p.get("nmy", 1)) == 1:
-        paired = p.get("interp", "ref") == "ref" and os.environ.get("WEM_PAIRED", "1") != "0" and \
-            p.get("precision", "fp32") == "fp32"
+        paired = (launch or {}).get("form") == "fp32-paired"
         fe, xinv, rused = executed_flops_per_unit(p, c["vel"], paired)
         roof.update({"inverse_transforms_per_wavefield_step": xinv, "references_used_per_depth_step": rused,
                      "flops_per_unit_executed": fe, "achieved_executed": units * fe / (mig_ms / 1000.0) / 1e12,
@@ -773,7 +798,8 @@ def main():
                    "parallelism": f"replicas x{world}, shots sharded by rank",
                    "depth_kernel_launch": launch},
         "e2e": {"value": world * units / e2e_s, "unit": "shot*omega*depth-steps/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+                "d2h_bytes_per_step": d2h, "host_buffers": "traces in pinned host memory",
+                "pageable_value": world * units / e2e_page_s},
         "gpu_launches": kernels_per_step * args.steps,
         "roofline": roof,
         "kernel_ms": {"spectra": statistics.mean(k[0] for k in kms), "extrapolate": mig_ms,

@@ -179,6 +179,15 @@ WEM_API int wem_measure_fp32_peak(int device, double *tflops);
 WEM_API int wem_last_launch(wem_ctx *ctx, int *threads, int *shots_per_cta, int *grid, int *replayed,
                             int *tuned);
 
+/* The form of the depth kernel the last 2-D wem_migrate* call ran (no counterpart in the
+   reference; the autotuner's choice): *form 0 FP32 with one inverse transform per
+   reference velocity, 1 split16 (tensor-core DFT stages), 2 FP32 paired (two references'
+   real parts per inverse transform, PSPI nearest-lower mode), 3 FP32 on power-of-two rows
+   carrying a transform length that is not a power of two (Bluestein); *bulk_tables 1 when
+   the precomputed phase tables reached shared memory by bulk copies (TMA engine), 0 by
+   per-thread asynchronous copies or built in each CTA. */
+WEM_API int wem_last_launch_form(wem_ctx *ctx, int *form, int *bulk_tables);
+
 /* The cudaStream_t (as void*) on which ctx orders all its work. */
 WEM_API int wem_ctx_stream(wem_ctx *ctx, void **stream);
 

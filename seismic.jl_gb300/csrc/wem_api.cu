@@ -70,6 +70,9 @@ struct wem_ctx {
     int device = 0;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // pinned staging ring for host buffers that are not pinned (copy_h2d)
+    void *stage[2] = { nullptr, nullptr };
+    cudaEvent_t stage_ev[2] = { nullptr, nullptr };
     cudaEvent_t evk[4] = { nullptr, nullptr, nullptr, nullptr };  // around spectra / migrate / reduce
     int nsm = 0;
     float last_ms = 0.f;
@@ -102,7 +105,9 @@ struct wem_ctx {
     DevBuf wlinp;                 // [nz][nmx rounded up to 4] linear weights (precomputed-table path)
     DevBuf ptab;                  // [nwf][nz][nref][nkx/2 + 2] phase tables (paired form)
     bool use_ptab = true;         // WEM_PHASE_TABLES=0: every CTA builds its own tables
+    bool use_tma = true;          // WEM_TMA=0: the precomputed tables by per-thread cp.async, not bulk copies
     bool ptab_ok = false;         // the current migration uses ptab
+    int ptab_nc = 0;              // frequencies per sub-band of ptab (alloc_phase_tables)
     int wdot_off = 0;             // offset of the direct-sum table in twid
     DevBuf refmask;               // [2][nz] bit r: some grid point takes its wavefield from reference r
                                   // (all of it, in the second row)
@@ -119,7 +124,9 @@ struct wem_ctx {
     // the launch sequence of the last 2-D migration, captured as a CUDA graph and
     // replayed while nothing it depends on has changed
     bool use_graph = true;
-    bool paired = true;  // PSPI nearest-lower mode: the paired inverse transforms (WEM_PAIRED=0: off)
+    bool paired = true;  // PSPI nearest-lower mode: the paired inverse transforms (the tuner's choice)
+    bool paired_env = true;  // WEM_PAIRED=0: never paired
+    bool tma_env = true;     // WEM_TMA=0: never bulk copies
     cudaGraphExec_t gexec = nullptr;
     struct GraphKey {
         int nshot, wide, grid;
@@ -135,6 +142,7 @@ struct wem_ctx {
     } gkey{};
     // what the last migration launched
     int last_threads = 0, last_S = 0, last_grid = 0, last_replayed = 0, last_tuned = 0;
+    int last_form = 0, last_tma = 0;  // the depth kernel's form (MIG_FORM_*) and table copies of the last 2-D call
 };
 
 namespace gbwem {
@@ -178,9 +186,13 @@ extern "C" int wem_ctx_destroy(wem_ctx *c)
                        &c->wtab, &c->scale_recv, &c->scale_src, &c->srcw, &c->wav, &c->wav_base,
                        &c->ssyn_ref, &c->ssyn_exact, &c->recv, &c->slots, &c->image, &c->data,
                        &c->tbase, &c->igx, &c->smig, &c->mimg, &c->tapery, &c->twy, &c->m3_items,
-                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb, &c->selbp, &c->wlinp, &c->ptab, &c->plan3, &c->dsum3 };
+                       &c->m3_U, &c->m3_Y, &c->m3_C, &c->m3_parts, &c->tcw, &c->tcerr, &c->refmask, &c->wposb, &c->selbp, &c->wlinp, &c->ptab, &c->plan3, &c->dsum3, &c->vref64 };
     for (DevBuf *b : bufs)
         if (b->p) cudaFree(b->p);
+    for (int i = 0; i < 2; i++) {
+        if (c->stage[i]) cudaFreeHost(c->stage[i]);
+        if (c->stage_ev[i]) cudaEventDestroy(c->stage_ev[i]);
+    }
     for (DevBuf &b : c->ang_vol)
         if (b.p) cudaFree(b.p);
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
@@ -268,6 +280,14 @@ extern "C" int wem_last_launch(wem_ctx *c, int *threads, int *shots_per_cta, int
     return WEM_OK;
 }
 
+extern "C" int wem_last_launch_form(wem_ctx *c, int *form, int *bulk_tables)
+{
+    if (!c) return fail(WEM_ERR_ARG, "null context");
+    if (form) *form = c->last_form;
+    if (bulk_tables) *bulk_tables = c->last_tma;
+    return WEM_OK;
+}
+
 extern "C" int wem_ctx_stream(wem_ctx *c, void **stream)
 {
     if (!c || !stream) return fail(WEM_ERR_ARG, "null argument");
@@ -279,9 +299,10 @@ extern "C" int wem_ctx_stream(wem_ctx *c, void **stream)
 // the tensor-core timeout word of the depth kernel
 static int collect_times(wem_ctx *c)
 {
-    if (c->prepared && c->p.precision == WEM_PREC_SPLIT16 && c->p.nmy == 1 && c->tcerr.p) {
+    if (c->prepared && c->p.nmy == 1 && c->tcerr.p) {
         int e = 0;
         CK(cudaMemcpy(&e, c->tcerr.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e == 2) return fail(WEM_ERR_TIMEOUT, "a wait for the depth kernel's bulk table copies ran out");
         if (e) return fail(WEM_ERR_TIMEOUT, "a tensor-core wait of the depth kernel ran out (split16 mode)");
     }
     CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
@@ -695,9 +716,13 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
     c->prep_gen++;
     {
         const char *e = getenv("WEM_PAIRED");
-        c->paired = !(e && !strcmp(e, "0"));
+        c->paired_env = !(e && !strcmp(e, "0"));
+        c->paired = c->paired_env;
         const char *pt = getenv("WEM_PHASE_TABLES");
         c->use_ptab = !(pt && !strcmp(pt, "0"));
+        const char *tm = getenv("WEM_TMA");
+        c->tma_env = !(tm && !strcmp(tm, "0"));
+        c->use_tma = c->tma_env;
     }
     c->last_nshot = -1;
     return WEM_OK;
@@ -744,16 +769,22 @@ static int set_shots(wem_ctx *c, int nshot, const float *sx, const float *sy, co
     return WEM_OK;
 }
 
-// ---------------------------------------------------------------- CTA shape autotuner
-// The depth-recursion kernel comes in two shapes: "wide" (512 threads; S shots of an item
-// share one set of per-depth phase tables) and "narrow" (256 threads; S = 1, more CTAs per
-// SM where the shared memory allows). Which one is faster depends on nkx, nref, nmx and the
-// device, so the first migration of a geometry times both on a slice of its own work (one
-// wave of items over the first 48 depth steps, after a warm-up launch) and the process
-// keeps the faster one for that geometry. WEM_CTA_SHAPE=wide|narrow forces a shape;
-// WEM_AUTOTUNE=0 takes the wide shape whenever its shared memory fits.
+// ---------------------------------------------------------------- launch autotuner
+// The 2-D depth kernel has choices whose best setting depends on nkx, nref, nmx, the
+// velocity model and the device: the CTA shape -- "wide" (512 threads; S shots of an item
+// share one set of per-depth phase tables) or "narrow" (256 threads, more CTAs per SM where
+// the shared memory allows) --, in the PSPI nearest-lower mode (FP32) the paired inverse
+// transforms or one transform per reference, and how the precomputed tables reach shared
+// memory (bulk copies on the TMA engine or per-thread cp.async). The first migration of a
+// geometry times the candidates on a slice of its own work (one wave of items over the
+// first 48 depth steps, with that slice's precomputed tables, after a warm-up launch):
+// shape x transforms first, then the table copies for the winner. The process keeps the
+// choice per geometry. WEM_CTA_SHAPE=wide|narrow, WEM_PAIRED=0 and WEM_TMA=0 pin a choice;
+// WEM_AUTOTUNE=0 takes the wide shape, the paired transforms and bulk copies wherever they
+// apply.
 struct TuneEntry {
-    int device, nkx, pspi, interp, nmx, nref, prec, paired, wide;
+    int device, nkx, pspi, interp, nmx, nref, prec, paired_ok, tma_ok, shape_env;
+    int wide, paired, tma;
 };
 
 static int tcmode(const wem_ctx *c) { return c->p.precision == WEM_PREC_SPLIT16 ? 1 : 0; }
@@ -821,11 +852,18 @@ static MigArgs mig_args(wem_ctx *c, int nshot, int ngroups)
     }
     a.vref64 = P<double>(c->vref64);
     a.dkx64 = c->dkx64;
+    a.tma = c->use_tma ? 1 : 0;
     return a;
 }
 
-// shots*frequencies per ms of one shape on a slice of the survey; 0 when the shape
-// does not fit. c->recv must hold nshot*nwf rows (contents do not matter for timing).
+static int ph_half_of(const wem_ctx *c);
+static int ph_stride_of(const wem_ctx *c);
+static bool alloc_phase_tables(wem_ctx *c);
+
+// shots*frequencies per ms of one launch setting (c->paired, c->use_tma, `wide`) on a slice
+// of the survey; 0 when it does not fit. c->recv must hold nshot*nwf rows (their contents do
+// not matter for timing). With precomputed tables the slice's tables are built first, so the
+// trial runs the path the migration takes.
 static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
 {
     const wem_params &p = c->p;
@@ -843,7 +881,8 @@ static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
     const int cap = c->nsm * bps;
     const int ngroups = (nshot + S - 1) / S;
     const int ngroups_t = std::min(ngroups, cap);
-    const int nwf_t = std::max(1, std::min(c->nwf, cap / ngroups_t));
+    const bool tables = alloc_phase_tables(c);
+    const int nwf_t = std::max(1, std::min(tables ? c->ptab_nc : c->nwf, cap / ngroups_t));
     const int items = ngroups_t * nwf_t;  // <= cap: one wave
     int rc;
     MigArgs a = mig_args(c, nshot, ngroups_t);
@@ -851,6 +890,12 @@ static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
     a.nz = std::min(p.nz, 48);
     if ((rc = ensure(c->slots, sizeof(float2) * (size_t)items * a.nz * p.nmx))) return rc;
     a.slots = P<float2>(c->slots);
+    if (tables) {  // the slice's tables, laid out for a.nwf x a.nz
+        a.ptab = P<float2>(c->ptab);
+        if (launch_phase_tables(ph_half_of(c), ph_stride_of(c), a, P<float2>(c->ptab), c->st, tcmode(c)))
+            return fail(WEM_ERR_CUDA, "phase-table launch (tuning): %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    CK(cudaMemsetAsync(c->tcerr.p, 0, sizeof(int), c->st));
     if (launch_migrate(c->nfft, wide, p.pspi, p.interp, a, items, c->st, form))
         return fail(WEM_ERR_CUDA, "migrate launch (tuning): %s", cudaGetErrorString(cudaGetLastError()));
     CK(cudaEventRecord(c->ev0, c->st));
@@ -858,6 +903,9 @@ static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
         return fail(WEM_ERR_CUDA, "migrate launch (tuning): %s", cudaGetErrorString(cudaGetLastError()));
     CK(cudaEventRecord(c->ev1, c->st));
     CK(cudaEventSynchronize(c->ev1));
+    int terr = 0;
+    CK(cudaMemcpy(&terr, c->tcerr.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (terr) return fail(WEM_ERR_TIMEOUT, "a bounded wait of the depth kernel ran out (tuning)");
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     const int shots = std::min(nshot, ngroups_t * S);
@@ -865,34 +913,72 @@ static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
     return WEM_OK;
 }
 
-static int choose_shape(wem_ctx *c, int nshot, int *wide)
+// Sets *wide, c->paired and c->use_tma for this migration (see the autotuner note above).
+static int choose_launch(wem_ctx *c, int nshot, int *wide)
 {
     const wem_params &p = c->p;
     const char *e = getenv("WEM_CTA_SHAPE");
-    int S, th;
-    size_t smem;
-    const bool wide_fits = !migrate_config(c->nfft, 1, p.pspi, p.interp, p.nmx, p.nref, &S, &th, &smem, mig_form(c, 1)) &&
-                           (int)smem <= c->max_smem;
+    const int shape_env = e && !strcmp(e, "narrow") ? 1 : (e && !strcmp(e, "wide") ? 2 : 0);
+    const bool paired_ok = c->paired_env && p.pspi && p.interp == WEM_INTERP_REF && !tcmode(c) && !c->blu;
+    const bool tma_ok = c->tma_env && p.pspi && c->use_ptab;
+    c->paired = paired_ok;
+    c->use_tma = tma_ok;
+    auto fits = [&](int w) {
+        int S, th;
+        size_t smem;
+        return !migrate_config(c->nfft, w, p.pspi, p.interp, p.nmx, p.nref, &S, &th, &smem, mig_form(c, w)) &&
+               (int)smem <= c->max_smem;
+    };
+    const bool wide_fits = fits(1);
     c->last_tuned = 0;
-    if (e && !strcmp(e, "narrow")) return *wide = 0, WEM_OK;
-    if (e && !strcmp(e, "wide")) return *wide = wide_fits ? 1 : 0, WEM_OK;
+    *wide = shape_env == 1 ? 0 : (wide_fits ? 1 : 0);
     const char *t = getenv("WEM_AUTOTUNE");
-    if (!wide_fits || (t && !strcmp(t, "0")) || c->nwf < 1) return *wide = wide_fits ? 1 : 0, WEM_OK;
+    if ((t && !strcmp(t, "0")) || c->nwf < 1) return WEM_OK;
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
         for (const TuneEntry &te : g_tune)
             if (te.device == c->device && te.nkx == c->nkx && te.pspi == p.pspi && te.interp == p.interp &&
-                te.nmx == p.nmx && te.nref == p.nref && te.prec == p.precision && te.paired == (int)c->paired)
-                return *wide = te.wide, WEM_OK;
+                te.nmx == p.nmx && te.nref == p.nref && te.prec == p.precision && te.paired_ok == (int)paired_ok &&
+                te.tma_ok == (int)tma_ok && te.shape_env == shape_env) {
+                *wide = te.wide;
+                c->paired = te.paired != 0;
+                c->use_tma = te.tma != 0;
+                return WEM_OK;
+            }
     }
     int rc;
     if ((rc = ensure(c->recv, sizeof(float2) * (size_t)nshot * std::max(c->nwf, 1) * p.nmx))) return rc;
-    double rw = 0.0, rn = 0.0;
-    if ((rc = trial_rate(c, nshot, 1, &rw)) || (rc = trial_rate(c, nshot, 0, &rn))) return rc;
-    *wide = rw >= rn ? 1 : 0;
+    // shape x transforms
+    double best = -1.0;
+    int bw = *wide, bp = c->paired ? 1 : 0;
+    for (int w = 1; w >= 0; w--) {
+        if ((shape_env == 1 && w) || (shape_env == 2 && !w && wide_fits)) continue;
+        for (int pr = paired_ok ? 1 : 0; pr >= 0; pr--) {
+            c->paired = pr != 0;
+            double r = 0.0;
+            if ((rc = trial_rate(c, nshot, w, &r))) return rc;
+            if (r > best) {
+                best = r;
+                bw = w;
+                bp = pr;
+            }
+        }
+    }
+    *wide = bw;
+    c->paired = bp != 0;
+    // table copies
+    if (tma_ok) {
+        double r_bulk = 0.0, r_async = 0.0;
+        c->use_tma = true;
+        if ((rc = trial_rate(c, nshot, bw, &r_bulk))) return rc;
+        c->use_tma = false;
+        if ((rc = trial_rate(c, nshot, bw, &r_async))) return rc;
+        c->use_tma = r_bulk >= r_async;
+    }
     c->last_tuned = 1;
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune.push_back({ c->device, c->nkx, p.pspi, p.interp, p.nmx, p.nref, p.precision, (int)c->paired, *wide });
+    g_tune.push_back({ c->device, c->nkx, p.pspi, p.interp, p.nmx, p.nref, p.precision, (int)paired_ok, (int)tma_ok,
+                       shape_env, *wide, (int)c->paired, (int)c->use_tma });
     return WEM_OK;
 }
 
@@ -996,21 +1082,54 @@ static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev,
 static int ph_half_of(const wem_ctx *c) { return c->nkx / 2 + 1; }
 static int ph_stride_of(const wem_ctx *c) { return c->blu ? c->nfft / 4 + 2 : c->nkx / 2 + 2; }
 
-// The 2-D PSPI kernels (FP32 and split16) read the phase tables of every (frequency, depth) from one array
-// that wem_phase_tables_kernel fills first, when it fits (at most 32 GiB and half the free
-// device memory); otherwise each CTA builds its own. True when c->ptab holds them.
+// The 2-D PSPI kernels read the phase tables of every (frequency, depth) from an array that
+// wem_phase_tables_kernel fills first. The whole band's tables when they fit (at most 32 GiB
+// and half the free device memory, counting the array already held); otherwise the band is
+// cut into equal sub-bands whose tables fit, and each sub-band is one table launch followed by
+// the depth kernel on that sub-band's items (WEM_PTAB_CHUNK=n caps a sub-band at n
+// frequencies). Only where not even one frequency's tables fit does each CTA build its own.
+// Sets c->ptab_nc (frequencies per sub-band; 0: no precomputed tables); true when c->ptab
+// holds them.
 static bool alloc_phase_tables(wem_ctx *c)
 {
     const wem_params &p = c->p;
+    c->ptab_nc = 0;
     if (!c->use_ptab || c->nwf < 1 || !p.pspi || p.nmy > 1) return false;
-    const size_t bytes = sizeof(float2) * (size_t)c->nwf * p.nz * p.nref * (size_t)ph_stride_of(c);
-    if (c->ptab.n >= bytes) return true;
+    const size_t per_f = sizeof(float2) * (size_t)p.nz * p.nref * (size_t)ph_stride_of(c);
+    int cap = c->nwf;
+    if (const char *e = getenv("WEM_PTAB_CHUNK")) {
+        const int v = atoi(e);
+        if (v > 0 && v < cap) cap = v;
+    }
     size_t fr = 0, tot = 0;
-    bool ok = false;
-    if (bytes <= (32ull << 30) && cudaMemGetInfo(&fr, &tot) == cudaSuccess && bytes <= fr / 2)
-        ok = ensure(c->ptab, bytes) == WEM_OK;
-    cudaGetLastError();
-    return ok;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    const size_t budget = std::min<size_t>(32ull << 30, (fr + c->ptab.n) / 2);
+    const long long fit = (long long)(budget / per_f);
+    if (fit < 1) return false;
+    int nc = (int)std::min<long long>(cap, fit);
+    const int nchunk = (c->nwf + nc - 1) / nc;
+    nc = (c->nwf + nchunk - 1) / nchunk;  // equal sub-bands
+    if (c->ptab.n < per_f * nc && ensure(c->ptab, per_f * nc) != WEM_OK) {
+        cudaGetLastError();
+        return false;
+    }
+    c->ptab_nc = nc;
+    return true;
+}
+
+// The depth kernel's arguments for the sub-band [f0, f0 + nf) of the frequency band: the
+// band offsets of the wavelet spectrum and the receiver rows, the row stride of the full band.
+static MigArgs band_args(MigArgs a, const wem_ctx *c, int f0, int nf)
+{
+    a.ifmin = c->ifmin + f0;
+    a.nwf = nf;
+    a.recv_nwf = c->nwf;
+    a.srcw += f0;
+    if (a.recv) a.recv += (size_t)f0 * c->p.nmx;
+    return a;
 }
 
 // record an event on c->st; inside a stream capture as a graph node (so that the
@@ -1032,7 +1151,7 @@ static int enqueue_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_de
     CK(rec(c->ev0, st, capture));
     CK(cudaMemsetAsync(c->recv.p, 0, sizeof(float2) * recv_elems, st));
     CK(cudaMemsetAsync(c->slots.p, 0, sizeof(float2) * (size_t)grid * nz * nmx, st));
-    if (tcmode(c)) CK(cudaMemsetAsync(c->tcerr.p, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(c->tcerr.p, 0, sizeof(int), st));  // the depth kernel's timeout word
     CK(rec(c->evk[0], st, capture));
     if (c->nwf > 0 && ntr > 0) {
         SpectraArgs sa{};
@@ -1051,15 +1170,19 @@ static int enqueue_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_de
         kernels++;
     }
     CK(rec(c->evk[1], st, capture));
-    if (c->nwf > 0) {
-        MigArgs a = mig_args(c, nshot, ngroups);
+    // the band at once, or sub-band by sub-band when only a part of its tables fits
+    const int nc = c->ptab_ok ? c->ptab_nc : c->nwf;
+    for (int f0 = 0; f0 < c->nwf; f0 += nc) {
+        const int nf = std::min(nc, c->nwf - f0);
+        MigArgs a = band_args(mig_args(c, nshot, ngroups), c, f0, nf);
         if (c->ptab_ok) {
             a.ptab = P<float2>(c->ptab);
             if (launch_phase_tables(ph_half_of(c), ph_stride_of(c), a, P<float2>(c->ptab), st, tcmode(c)))
                 return fail(WEM_ERR_CUDA, "phase-table launch: %s", cudaGetErrorString(cudaGetLastError()));
             kernels++;
         }
-        if (launch_migrate(c->nfft, wide, p.pspi, p.interp, a, grid, st, mig_form(c, wide)))
+        const int g = (int)std::min<long long>(grid, (long long)ngroups * nf);
+        if (launch_migrate(c->nfft, wide, p.pspi, p.interp, a, g, st, mig_form(c, wide)))
             return fail(WEM_ERR_CUDA, "migrate launch: %s", cudaGetErrorString(cudaGetLastError()));
         kernels++;
     }
@@ -1085,7 +1208,7 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
     int S, threads, bps = 0, wide = 0;
     size_t smem;
     int rc;
-    if ((rc = choose_shape(c, nshot, &wide))) return rc;
+    if ((rc = choose_launch(c, nshot, &wide))) return rc;
     const int form = mig_form(c, wide);
     if (migrate_config(c->nfft, wide, p.pspi, p.interp, nmx, p.nref, &S, &threads, &smem, form))
         return fail(WEM_ERR_SIZE, "no kernel for nkx=%d", c->nkx);
@@ -1104,6 +1227,8 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
         (rc = ensure(c->slots, sizeof(float2) * (size_t)grid * nz * nmx)))
         return rc;
     c->ptab_ok = alloc_phase_tables(c);
+    c->last_form = form;
+    c->last_tma = c->ptab_ok && c->use_tma && p.pspi ? 1 : 0;
     c->last_threads = threads;
     c->last_S = S;
     c->last_grid = grid;
@@ -1162,6 +1287,71 @@ extern "C" int wem_migrate_device(wem_ctx *c, int nshot, const float *sx, const 
     return WEM_OK;
 }
 
+// Host -> device copy on c->st. Pinned (or managed) sources go straight to the copy engine.
+// A pageable source of more than a few MB goes through two pinned 16 MiB slots: the host
+// copies chunk k into one slot while the copy engine moves chunk k - 1 out of the other, so
+// the transfer runs at the copy engine's pinned rate instead of the driver's pageable path.
+static int copy_h2d(wem_ctx *c, void *dst, const void *src, size_t bytes)
+{
+    constexpr size_t SLOT = 16u << 20;
+    cudaPointerAttributes at{};
+    const bool pinned = cudaPointerGetAttributes(&at, src) == cudaSuccess &&
+                        (at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    if (pinned || bytes <= 2 * SLOT) {
+        CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->st));
+        return WEM_OK;
+    }
+    for (int i = 0; i < 2; i++) {
+        if (!c->stage[i]) CK(cudaHostAlloc(&c->stage[i], SLOT, cudaHostAllocDefault));
+        if (!c->stage_ev[i]) CK(cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming));
+    }
+    int k = 0;
+    for (size_t off = 0; off < bytes; off += SLOT, k ^= 1) {
+        const size_t n = std::min(SLOT, bytes - off);
+        CK(cudaEventSynchronize(c->stage_ev[k]));  // the slot's previous chunk has left
+        memcpy(c->stage[k], (const char *)src + off, n);
+        CK(cudaMemcpyAsync((char *)dst + off, c->stage[k], n, cudaMemcpyHostToDevice, c->st));
+        CK(cudaEventRecord(c->stage_ev[k], c->st));
+    }
+    return WEM_OK;
+}
+
+// Device -> host copy on c->st that has completed when it returns (the stream is synchronised).
+// A pageable destination of more than a few MB comes through the two pinned slots: the copy
+// engine fills one while the host empties the other.
+static int copy_d2h_sync(wem_ctx *c, void *dst, const void *src, size_t bytes)
+{
+    constexpr size_t SLOT = 16u << 20;
+    cudaPointerAttributes at{};
+    const bool pinned = cudaPointerGetAttributes(&at, dst) == cudaSuccess &&
+                        (at.type == cudaMemoryTypeHost || at.type == cudaMemoryTypeManaged);
+    cudaGetLastError();
+    if (pinned || bytes <= 2 * SLOT) {
+        CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        return WEM_OK;
+    }
+    for (int i = 0; i < 2; i++) {
+        if (!c->stage[i]) CK(cudaHostAlloc(&c->stage[i], SLOT, cudaHostAllocDefault));
+        if (!c->stage_ev[i]) CK(cudaEventCreateWithFlags(&c->stage_ev[i], cudaEventDisableTiming));
+    }
+    const size_t nchunk = (bytes + SLOT - 1) / SLOT;
+    auto issue = [&](size_t k) -> cudaError_t {
+        const size_t off = k * SLOT, n = std::min(SLOT, bytes - off);
+        cudaError_t e = cudaMemcpyAsync(c->stage[k & 1], (const char *)src + off, n, cudaMemcpyDeviceToHost, c->st);
+        return e != cudaSuccess ? e : cudaEventRecord(c->stage_ev[k & 1], c->st);
+    };
+    CK(issue(0));
+    for (size_t k = 0; k < nchunk; k++) {
+        CK(cudaEventSynchronize(c->stage_ev[k & 1]));  // chunk k is in its slot
+        if (k + 1 < nchunk) CK(issue(k + 1));           // the other slot was emptied in step k - 1
+        const size_t off = k * SLOT, n = std::min(SLOT, bytes - off);
+        memcpy((char *)dst + off, c->stage[k & 1], n);
+    }
+    return WEM_OK;
+}
+
 extern "C" int wem_migrate(wem_ctx *c, int nshot, const float *sx, const float *sy, const int64_t *toff,
                            const int32_t *tcell, const float *d, float *m)
 {
@@ -1176,7 +1366,7 @@ extern "C" int wem_migrate(wem_ctx *c, int nshot, const float *sx, const float *
     const size_t dbytes = sizeof(float) * (size_t)ntr * p.nt;
     const size_t mbytes = sizeof(float) * (size_t)p.nmx * p.nmy * p.nz;
     if ((rc = ensure(c->data, dbytes)) || (rc = ensure(c->image, mbytes))) return rc;
-    if (dbytes) CK(cudaMemcpyAsync(c->data.p, d, dbytes, cudaMemcpyHostToDevice, c->st));
+    if (dbytes && (rc = copy_h2d(c, c->data.p, d, dbytes))) return rc;
     if ((rc = run_migrate(c, nshot, ntr, P<float>(c->data), P<float>(c->image)))) return rc;
     CK(cudaMemcpyAsync(m, c->image.p, mbytes, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
@@ -1823,6 +2013,7 @@ static int run_model(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, flo
         return rc;
     int kernels = 0;
     CK(cudaEventRecord(c->ev0, st));
+    CK(cudaMemsetAsync(c->tcerr.p, 0, sizeof(int), st));  // no timeout word from an earlier migration
     CK(cudaMemsetAsync(c->recv.p, 0, sizeof(float2) * dg_elems, st));
     if (launch_transpose(m_dev, nmx, nz, P<float>(c->mimg), st))
         return fail(WEM_ERR_CUDA, "transpose launch: %s", cudaGetErrorString(cudaGetLastError()));
@@ -1845,20 +2036,28 @@ static int run_model(wem_ctx *c, int nshot, int64_t ntr, const float *m_dev, flo
             a.chirp = P<float2>(c->twid) + c->chirp_off;
             a.bfft = P<float2>(c->twid) + c->bfft_off;
         }
-        if (alloc_phase_tables(c)) {
-            a.ptab = P<float2>(c->ptab);
-            if (launch_phase_tables(ph_half_of(c), ph_stride_of(c), a, P<float2>(c->ptab), st))
-                return fail(WEM_ERR_CUDA, "phase-table launch: %s", cudaGetErrorString(cudaGetLastError()));
-            kernels++;
-        }
         BornArgs b{};
         b.img = P<float>(c->mimg);
         b.smig = P<float2>(c->smig);
-        b.dg = P<float2>(c->recv);
         b.inv_sqt = (float)(1.0 / (double)sqrtf((float)c->ntfft));
-        if (launch_model(c->nfft, p.pspi, p.interp, exact, a, b, grid, st, c->blu))
-            return fail(WEM_ERR_CUDA, "modelling launch: %s", cudaGetErrorString(cudaGetLastError()));
-        kernels++;
+        // the band at once, or sub-band by sub-band when only a part of its tables fits
+        const bool tables = alloc_phase_tables(c);
+        const int nc = tables ? c->ptab_nc : c->nwf;
+        for (int f0 = 0; f0 < c->nwf; f0 += nc) {
+            const int nf = std::min(nc, c->nwf - f0);
+            MigArgs ab = band_args(a, c, f0, nf);
+            b.dg = P<float2>(c->recv) + (size_t)f0 * nmx;
+            if (tables) {
+                ab.ptab = P<float2>(c->ptab);
+                if (launch_phase_tables(ph_half_of(c), ph_stride_of(c), ab, P<float2>(c->ptab), st))
+                    return fail(WEM_ERR_CUDA, "phase-table launch: %s", cudaGetErrorString(cudaGetLastError()));
+                kernels++;
+            }
+            const int g = (int)std::min<long long>(grid, (long long)ngroups * nf);
+            if (launch_model(c->nfft, p.pspi, p.interp, exact, ab, b, g, st, c->blu))
+                return fail(WEM_ERR_CUDA, "modelling launch: %s", cudaGetErrorString(cudaGetLastError()));
+            kernels++;
+        }
     }
     CK(cudaEventRecord(c->evk[2], st));
     if (ntr > 0) {
@@ -1911,8 +2110,11 @@ extern "C" int wem_model(wem_ctx *c, int nshot, const float *sx, const float *sy
     if ((rc = ensure(c->data, dbytes)) || (rc = ensure(c->image, mbytes))) return rc;
     CK(cudaMemcpyAsync(c->image.p, m, mbytes, cudaMemcpyHostToDevice, c->st));
     if ((rc = run_model(c, nshot, ntr, P<float>(c->image), P<float>(c->data), exact ? 1 : 0))) return rc;
-    if (dbytes) CK(cudaMemcpyAsync(d, c->data.p, dbytes, cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
+    if (dbytes) {
+        if ((rc = copy_d2h_sync(c, d, c->data.p, dbytes))) return rc;
+    } else {
+        CK(cudaStreamSynchronize(c->st));
+    }
     return collect_times(c);
 }
 

@@ -65,6 +65,12 @@ struct MigArgs {
     // wavenumber step 2 pi / (nkx dmx) in double
     const double *vref64;
     double dkx64;
+    // 1: the precomputed tables reach shared memory by bulk copies (TMA engine) completing on
+    // an mbarrier; 0: per-thread 16-byte cp.async
+    int tma;
+    // frequencies between the rows of one shot in recv (migration) and dg (modelling) when a
+    // launch covers a band [ifmin, ifmin + nwf) of a longer spectrum; 0: nwf
+    int recv_nwf;
 };
 // points per depth whose imaginary part the paired form takes from a direct sum
 constexpr int WHOLE_MAX = 4;

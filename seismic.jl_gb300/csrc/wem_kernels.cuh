@@ -73,6 +73,21 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
         tc.err = a.err;
     }
 
+    // the bulk-copy path of the precomputed tables: the CTA's mbarrier, its phase, the
+    // abort flag of a wait that ran out
+    __shared__ __align__(8) uint64_t s_tbar;
+    __shared__ int s_tabort;
+    const bool tma = PSPI && a.ptab && a.tma;
+    uint32_t tphase = 0;
+    if (tma) {
+        if (tid == 0) {
+            mbar_init(smem_u32(&s_tbar), 1);
+            s_tabort = 0;
+            mbar_init_fence();
+        }
+        __syncthreads();
+    }
+
     float2 *slot = a.slots + (size_t)blockIdx.x * a.nz * a.nmx;
     const int nitems = a.ngroups * a.nwf;
     const int nmx = a.nmx;
@@ -92,7 +107,7 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
         float2 v[16];
         const int igx = shot_ok ? a.igx[shot] : -1;
         const float2 sw = a.srcw[iwi];
-        const float2 *rrow = a.recv + ((size_t)(shot_ok ? shot : 0) * a.nwf + iwi) * nmx;
+        const float2 *rrow = a.recv + ((size_t)(shot_ok ? shot : 0) * (a.recv_nwf ? a.recv_nwf : a.nwf) + iwi) * nmx;
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             const int x = t + T * m;
@@ -118,7 +133,11 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                 const unsigned long long um = ref_mask(a, iz), cm = PAIR ? cx_mask(a, iz) : 0ull;
                 __syncthreads();
                 if constexpr (PSPI) {
-                    copy_tables_async<N, INTERP, PAIR>(a, sm, iwi, iz, tid, NT, um);
+                    if (tma) {
+                        if (tid == 0 && !s_tabort) copy_tables_bulk<N, INTERP, PAIR>(a, sm, iwi, iz, um, smem_u32(&s_tbar));
+                    } else {
+                        copy_tables_async<N, INTERP, PAIR>(a, sm, iwi, iz, tid, NT, um);
+                    }
                     float inv_s = 1.f;
                     if (active) {
                         if constexpr (PAIR) {
@@ -134,7 +153,8 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                             xform<N, -1, false, BLU>(v, xbuf, sm.tw, t, sync, nullptr, a);
                         }
                     }
-                    cp_async_wait_all();
+                    if (tma) tables_bulk_wait(smem_u32(&s_tbar), tphase, &s_tabort, a.err);
+                    else cp_async_wait_all();
                     __syncthreads();
                     if (active) {
                         if constexpr (PAIR)
@@ -198,6 +218,7 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
             }
         }
     }
+    if (tma && s_tabort && tid == 0) mbar_wait_bounded(smem_u32(&s_tbar), tphase ^ 1u);  // copies still in flight
     if constexpr (TC) {
         // every MMA was waited for, unless a wait ran out: then drain before freeing TMEM
         if (t == 0 && *tc.abort) {
@@ -321,7 +342,7 @@ __global__ void __launch_bounds__(S * (N / 16), N <= 1024 ? 2 : 1) wem_model_ker
             }
         }
         if (shot_ok) {
-            float2 *out = b.dg + ((size_t)shot * a.nwf + iwi) * nmx;
+            float2 *out = b.dg + ((size_t)shot * (a.recv_nwf ? a.recv_nwf : a.nwf) + iwi) * nmx;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const int x = t + T * m;

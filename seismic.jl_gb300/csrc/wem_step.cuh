@@ -51,6 +51,15 @@ __device__ __forceinline__ float2 phase_entry_fp64(double wd, double vr, double 
     return make_float2(__double2float_rn(__dmul_rn(re, inv_n)), __double2float_rn(__dmul_rn(im, inv_n)));
 }
 
+// One reference's FP64-built table (entries kk = tid, tid + nth, ... < half), out of line so
+// that its double-precision code does not weigh on the registers of the kernels' hot loops
+// (it runs only where a CTA builds its own split16 tables).
+static __device__ __noinline__ void phase_table_fp64(float2 *ph, int half, double wd, double vr, double dkx, double dz,
+                                              double inv_n, int tid, int nth)
+{
+    for (int kk = tid; kk < half; kk += nth) ph[kk] = phase_entry_fp64(wd, vr, __dmul_rn((double)kk, dkx), dz, inv_n);
+}
+
 __device__ __forceinline__ void kahan_add(float2 *slot, float v, float2 s)
 {
     const float y = __fsub_rn(v, s.y);
@@ -177,9 +186,8 @@ __device__ __forceinline__ void build_tables(const MigArgs &a, const Smem<N, PSP
             const float slow2 = sl[r];
             float2 *ph = sm.ph + (size_t)r * sm.PHS;
             if constexpr (F64) {
-                const double vr = a.vref64[(size_t)iz * a.nref + r], inv_n = 1.0 / (double)a.nlog;
-                for (int kk = tid; kk < HALF; kk += nthreads)
-                    ph[kk] = phase_entry_fp64((double)w, vr, __dmul_rn((double)kk, a.dkx64), (double)a.dz, inv_n);
+                phase_table_fp64(ph, HALF, (double)w, a.vref64[(size_t)iz * a.nref + r], a.dkx64, (double)a.dz,
+                                 1.0 / (double)a.nlog, tid, nthreads);
             } else {
                 for (int kk = tid; kk < HALF; kk += nthreads)
                     ph[kk] = phase_entry(w2, slow2, __fmul_rn(a.dkx, (float)kk), a.dz, a.inv_n);
@@ -641,6 +649,60 @@ __device__ __forceinline__ void copy_tables_async(const MigArgs &a, const Smem<N
                                                   int nthreads)
 {
     copy_tables_async<N, INTERP, PAIR, BLU>(a, sm, iwi, iz, tid, nthreads, ref_mask(a, iz));
+}
+
+// The same tables with the bulk-copy (TMA) engine: one thread issues one cp.async.bulk per
+// contiguous piece (each used reference's phase table, the selection row, the linear
+// weights, the list of points taken whole) -- this GPU's own global memory into this CTA's
+// shared memory, no multicast -- and they complete on the CTA's mbarrier `mbar` with the
+// byte count armed first. Every piece starts 16-byte aligned on both sides and is a
+// multiple of 16 bytes long (the table stride, the padded selection and weight rows). The
+// generic-proxy reads of the previous depth's tables are ordered before the asynchronous
+// writes by the caller's barrier and the proxy fence here. Call from one thread; every
+// thread then waits on the mbarrier's phase (tables_bulk_wait).
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint32_t mbar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+template <int N, int INTERP, bool PAIR, bool BLU = false>
+__device__ __forceinline__ void copy_tables_bulk(const MigArgs &a, const Smem<N, true, BLU> &sm, int iwi, int iz,
+                                                 unsigned long long used, uint32_t mbar)
+{
+    constexpr int PHS = Smem<N, true, BLU>::PHS;
+    constexpr uint32_t TB = PHS * sizeof(float2);
+    used &= (a.nref >= 64 ? ~0ull : ((1ull << a.nref) - 1ull));
+    const uint32_t nsel = (uint32_t)((a.nmx + 15) / 16) * 16, nwl = (uint32_t)((a.nmx + 3) / 4) * 16;
+    const uint32_t total = (uint32_t)__popcll(used) * TB + nsel + (INTERP == 1 ? nwl : 0u) + (PAIR ? 32u : 0u);
+    fence_async_smem();
+    mbar_expect_tx(mbar, total);
+    const float2 *src = a.ptab + ((size_t)iwi * a.nz + iz) * a.nref * PHS;
+    while (used) {
+        const int r = __ffsll((long long)used) - 1;
+        used &= used - 1ull;
+        bulk_g2s(sm.ph + (size_t)r * PHS, src + (size_t)r * PHS, TB, mbar);
+    }
+    bulk_g2s(sm.selb, a.selbp + (size_t)iz * nsel, nsel, mbar);
+    if (INTERP == 1) bulk_g2s(sm.wl, a.wlinp + (size_t)iz * (nwl / 4), nwl, mbar);
+    if (PAIR) bulk_g2s(sm.wpos, a.wpos + (size_t)iz * WPOS_STRIDE, 32u, mbar);
+}
+
+// Wait for the depth's bulk copies (all threads): bounded; on a timeout the error word is
+// set, *abort records it (later depths stop waiting) and the kernel's end waits once more.
+__device__ __forceinline__ void tables_bulk_wait(uint32_t mbar, uint32_t &phase, int *abort, int *err)
+{
+    if (!*abort && !mbar_wait_bounded(mbar, phase)) {
+        *abort = 1;
+        atomicExch(err, 2);
+    }
+    phase ^= 1u;
 }
 
 // One upward step of the modelling recursion (wem.c:273-274, -dz, adj=false), in

@@ -27,7 +27,7 @@ PRECISION = {"fp32": 0, "split16": 1}
 # every symbol the public header declares
 EXPORTS = ["wem_last_error", "wem_version", "wem_ctx_create", "wem_ctx_destroy", "wem_prepare",
            "wem_migrate", "wem_migrate_device", "wem_migrate_survey", "wem_last_timing",
-           "wem_last_kernel_times", "wem_last_launch", "wem_ctx_stream", "wem_migrate_noalloc", "wem_model",
+           "wem_last_kernel_times", "wem_last_launch", "wem_last_launch_form", "wem_ctx_stream", "wem_migrate_noalloc", "wem_model",
            "wem_model_device", "wem_angles", "wem", "wem_selftest_wait_timeout", "wem_measure_fp32_peak",
            "shotwem_main", "main"]
 
@@ -87,6 +87,7 @@ def lib():
         L.wem_last_kernel_times.argtypes = [vp, f_p, f_p, f_p]
         ip = C.POINTER(C.c_int)
         L.wem_last_launch.argtypes = [vp, ip, ip, ip, ip, ip]
+        L.wem_last_launch_form.argtypes = [vp, ip, ip]
         L.wem_selftest_wait_timeout.argtypes = [C.c_int, ip, C.POINTER(C.c_float)]
         L.wem_measure_fp32_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
         L.wem_angles.argtypes = [vp, C.POINTER(Params), fp, fp, C.c_int, fp, fp, fp, fp]

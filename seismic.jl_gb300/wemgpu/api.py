@@ -190,7 +190,12 @@ class Context:
         it replayed the captured CUDA graph and whether it timed the CTA shapes first."""
         v = [C.c_int() for _ in range(5)]
         L.check(L.lib().wem_last_launch(self._h, *[C.byref(x) for x in v]))
-        return dict(zip(["threads", "shots_per_cta", "grid", "graph_replayed", "tuned"], [x.value for x in v]))
+        out = dict(zip(["threads", "shots_per_cta", "grid", "graph_replayed", "tuned"], [x.value for x in v]))
+        f, b = C.c_int(), C.c_int()
+        L.check(L.lib().wem_last_launch_form(self._h, C.byref(f), C.byref(b)))
+        out["form"] = {0: "fp32", 1: "split16", 2: "fp32-paired", 3: "fp32-bluestein"}.get(f.value, str(f.value))
+        out["bulk_table_copies"] = b.value
+        return out
 
     def stream(self) -> int:
         """cudaStream_t of this context, as an integer handle."""

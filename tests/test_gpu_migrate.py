@@ -177,8 +177,10 @@ def test_paired_inverse_transforms(gpu_lib, oracle_mod, monkeypatch, nref):
     reference keeps a transform of its own). Against the port and against one transform
     per reference (WEM_PAIRED=0); the phase tables precomputed for every (frequency,
     depth) give the image bit for bit that tables built in each CTA give
-    (WEM_PHASE_TABLES=0)."""
+    (WEM_PHASE_TABLES=0). The autotuner is off so that each run takes the form its switches
+    name, in the same CTA shape."""
     from wemgpu import synth
+    monkeypatch.setenv("WEM_AUTOTUNE", "0")  # the forms the switches name, not the tuner's pick
     c = synth.small_case(47, nx=256, nz=18, nt=96, nshot=3, pspi=1, nref=nref, interp="ref")
     rng = np.random.default_rng(48)
     vel = c["vel"].copy()
@@ -263,9 +265,10 @@ def test_edge_cases(gpu_lib):
         # zero data gives a zero image
         zero = gpu_lib.Shots(shots.sx, shots.sy, shots.trace_offset, shots.trace_cell, np.zeros_like(shots.data))
         assert not np.any(ctx.migrate(zero))
-        # unsupported FFT length and a single reference velocity are rejected
+        # a row length with no kernel (a non-power of two above 2048) and a single reference
+        # velocity are rejected
         with pytest.raises(WemError) as e:
-            ctx.prepare(dict(p, nmx=48), np.ones((48, p["nz"]), np.float32) * 2000, wav)
+            ctx.prepare(dict(p, nmx=1100, padx=2), np.ones((1100, p["nz"]), np.float32) * 2000, wav)
         assert e.value.code == -2
         with pytest.raises(WemError) as e:
             ctx.prepare(dict(p, nref=1), vel, wav)
@@ -289,3 +292,28 @@ def test_measured_fp32_peak_is_plausible(gpu_lib):
     from wemgpu._lib import measure_fp32_peak
     v = measure_fp32_peak(0)
     assert 20.0 < v < 100.0, v
+
+
+@pytest.mark.parametrize("interp", ["ref", "linear"])
+def test_phase_tables_in_sub_bands(gpu_lib, oracle_mod, monkeypatch, interp):
+    """When the whole band's phase tables do not fit the device, the migration and the
+    modelling run sub-band by sub-band (one table launch, then the depth kernel on that
+    sub-band's items); WEM_PTAB_CHUNK caps a sub-band so that this small case takes the
+    path. The images and data agree with the single-band run to FP32 rounding (the CTAs see
+    the items in another order) and with the port."""
+    from wemgpu import synth
+    c = synth.small_case(47, nx=128, nz=16, nt=128, nshot=3, pspi=1, nref=4, interp=interp)
+    p, shots = c["params"], c["shots"]
+    rng = np.random.default_rng(5)
+    m_in = rng.standard_normal((p["nmx"], p["nz"])).astype(np.float32)
+    out = []
+    for chunk in (None, "3"):
+        if chunk:
+            monkeypatch.setenv("WEM_PTAB_CHUNK", chunk)
+        with gpu_lib.Context() as ctx:
+            ctx.prepare(p, c["vel"], c["wav"])
+            out.append((ctx.migrate(shots), ctx.migrate(shots), ctx.model(shots, m_in, exact=True)))
+    (m1, m1b, d1), (m2, m2b, d2) = out
+    assert np.array_equal(m2, m2b)  # the captured graph of the sub-band launches replays
+    assert rel_l2(m2, m1) < 1e-5 and rel_l2(d2, d1) < 1e-5
+    assert rel_l2(m2, _port_stack(oracle_mod, p, c["vel"], c["wav"], shots)) < TOL

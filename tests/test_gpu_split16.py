@@ -49,6 +49,7 @@ def test_split16_precomputed_phase_tables_bit_identical(gpu_lib, monkeypatch, in
     c = synth.small_case(53, nx=1024, nz=24, nt=128, nshot=3, pspi=1, nref=6, interp=interp, fmax=30.0)
     p = dict(c["params"], precision="split16")
     images = []
+    monkeypatch.setenv("WEM_AUTOTUNE", "0")  # the same CTA shape for both runs
     for pt in ("1", "0"):
         monkeypatch.setenv("WEM_PHASE_TABLES", pt)
         with gpu_lib.Context() as ctx:
