@@ -635,8 +635,6 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the image-error check against the FP64 oracle")
     ap.add_argument("--fmax", type=float, default=None,
                     help="upper band edge in Hz instead of the workload's (smaller cases for profiling)")
-    ap.add_argument("--fmax", type=float, default=None,
-                    help="upper band edge in Hz instead of the workload's (smaller cases for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -658,9 +656,6 @@ def main():
     if not os.path.exists(wemgpu.LIB_PATH):
         raise SystemExit("shotwem.so is not built: python -c 'import __graft_entry__ as g; g.build()'")
     c, wl = survey(args.workload, rank)
-    if args.fmax is not None:
-        c["params"] = dict(c["params"], fmax=float(args.fmax))
-        wl += f" [band cut to {c['params']['fmin']:g}-{args.fmax:g} Hz]"
     if args.fmax is not None:
         c["params"] = dict(c["params"], fmax=float(args.fmax))
         wl += f" [band cut to {c['params']['fmin']:g}-{args.fmax:g} Hz]"
