@@ -71,6 +71,11 @@ def survey(workload: str, rank: int, born: str = "gpu"):
     elif workload == "split1":
         c = synth.config0(seed=1000 + rank)
         wl = "2-D split-step: 1 shot, 200x256 grid @10 m, 3 layers, 5-60 Hz, nt=1000, padx=padt=2"
+    elif workload == "elastic8":
+        c = synth.config4(seed=1004 + rank, nshot=8)
+        c["params"] = dict(c["params"], fmax=30.0)
+        wl = ("2-D elastic migration (ewem): 8 shots, 300x512 grid @10 m, vs = vp/1.8 with a 5% seeded wobble, "
+              "5-30 Hz, nt=1500, padx=padt=2, x and z components on every cell")
     else:
         raise SystemExit(f"unknown workload {workload}")
     if workload in ("survey64", "survey8", "angles8"):
@@ -115,6 +120,20 @@ def band(p: dict):
     fmax, fmin = f32(p["fmax"]), f32(p["fmin"])
     ifmax = int(f32(int(fmax)) * dt * f32(ntfft) + f32(1)) if fmax * dt * f32(ntfft) + f32(1) < nw else nw
     ifmin = int(f32(int(fmin)) * dt * f32(ntfft)) if fmin * dt * f32(ntfft) + f32(1) < ifmax else 0
+    return ifmax - ifmin
+
+
+def band_elastic(p: dict):
+    """Frequencies of the reference's elastic migration (ewem.c:44-57: ntfft = 2 truncf(padt nt/2),
+    ifmax = trunc(fmax dt ntfft) + 1, float products)."""
+    f32 = np.float32
+    nt, padt, dt = int(p["nt"]), int(p["padt"]), f32(p["dt"])
+    ntfft = 2 * int(math.trunc(float(f32(f32(padt) * f32(nt)) / f32(2))))
+    nw = ntfft // 2 + 1
+    prod = f32(f32(p["fmax"]) * dt * f32(ntfft))
+    ifmax = int(math.trunc(float(prod))) + 1 if prod + f32(1) < nw else nw
+    prodn = f32(f32(p["fmin"]) * dt * f32(ntfft))
+    ifmin = int(math.trunc(float(prodn))) if prodn + f32(1) < ifmax else 0
     return ifmax - ifmin
 
 
@@ -430,6 +449,81 @@ def run_reference_arm(args):
     return 0
 
 
+def run_elastic(args, c, wl, rank, world, local):
+    """Elastic migration of every shot (wem_elastic; the reference's ewem, src/Imaging/c/ewem.c).
+    A unit is one shot * frequency * depth step (the source step and the receiver's
+    separation, two potential continuations and recombination). One step = all shots."""
+    import torch
+    import wemgpu
+    from wemgpu import synth
+    p, shots = c["params"], c["shots"]
+    nmx, nz, nt = int(p["nmx"]), int(p["nz"]), int(p["nt"])
+    rng = np.random.default_rng(2005 + rank)
+    vp = c["vel"]
+    vs = (vp / 1.8 * (1.0 + 0.05 * rng.standard_normal(vp.shape))).astype(np.float32)
+    uz = np.stack([synth.shot_gather_full(shots, s, nmx) for s in range(shots.nshot)])
+    ux = (0.5 * np.roll(uz, 3, axis=2)).astype(np.float32)
+    sx = np.asarray(shots.sx, np.float32)
+    nf = band_elastic(p)
+    units = len(sx) * nf * nz
+    for _ in range(args.warmup):
+        wemgpu.elastic(p, vp, vs, c["wav"], sx, ux=ux, uz=uz, adj=True, device=local)
+    sampler = ClockSampler(local)
+    torch.cuda.synchronize()
+    sampler.start()
+    dev_ms, wall = [], []
+    L = wemgpu.lib()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        wemgpu.elastic(p, vp, vs, c["wav"], sx, ux=ux, uz=uz, adj=True, device=local)
+        wall.append(time.perf_counter() - t0)
+        dev_ms.append(float(L.wem_elastic_last_ms()))
+    clocks = sampler.stop()
+    ms = statistics.mean(dev_ms)
+    nkx = int(p["padx"]) * nmx
+    lg = math.log2(nkx)
+    # algorithmic FLOPs per unit: the source step (2 transforms) and the receiver's separation,
+    # two continuations and recombination (10 transforms), 5 N log2 N each, plus ~60 per sample
+    fl = 12 * 5 * nkx * lg + 60 * nkx
+    ach = units * fl / (ms / 1000.0) / 1e12
+    fp32_meas = fp32_peak(local)
+    line = {"metric": "shot*omega*depth-steps/s", "value": world * units / (ms / 1000.0),
+            "unit": "shot*omega*depth-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)", "gpu_launches": args.steps * 4,
+            "config": {"workload": wl, "units_per_step_per_gpu": units, "shots": len(sx), "frequencies": nf,
+                       "depth_steps": nz, "nkx": nkx, "l2": "inputs larger than L2"},
+            "e2e": {"value": world * units / statistics.mean(wall), "unit": "shot*omega*depth-steps/s",
+                    "h2d_bytes_per_step": int(ux.nbytes + uz.nbytes), "d2h_bytes_per_step": int(2 * nmx * nz * 4)},
+            "roofline": {"bound": "fp32", "achieved": ach, "peak": fp32_meas, "unit": "TFLOP/s",
+                         "frac": ach / fp32_meas, "traffic": None,
+                         "peak_source": "FP32 FMA probe (wem_measure_fp32_peak), measured in this run",
+                         "kernel": "wem_ewem_kernel + spectra + reductions, whole step", "ms_per_launch": ms,
+                         "flops_per_unit": fl},
+            "clocks": clocks}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # the CPU leg: the oracle's FP64 restatement (NumPy, one thread) on one shot, 2 Hz of the band
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import ewem_np as E
+        q = dict(p, sx=float(sx[len(sx) // 2]), fmax=float(p["fmin"]) + 2.0)
+        nq = band_elastic(q)
+        s0 = len(sx) // 2
+        t0 = time.perf_counter()
+        want = E.ewem(q, vp, vs, c["wav"], ux=ux[s0], uz=uz[s0], adj=True)
+        el = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": nq * nz / el, "unit": "shot*omega*depth-steps/s", "cores": 1, "kind": "port",
+                                "sample": f"1 shot, {nq} frequencies x {nz} depth steps in {el:.1f} s "
+                                          "(NumPy FP64 restatement, one thread)"}
+        got = wemgpu.elastic(q, vp, vs, c["wav"], [q["sx"]], ux=ux[s0:s0 + 1], uz=uz[s0:s0 + 1], adj=True,
+                             device=local)
+        line["accuracy"] = {"rel_l2_p_vs_fp64": float(np.linalg.norm(got[0] - want[0]) / np.linalg.norm(want[0])),
+                            "rel_l2_s_vs_fp64": float(np.linalg.norm(got[1] - want[2]) / np.linalg.norm(want[2])),
+                            "sample": "the CPU leg's shot and band"}
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
 def run_angles(args, c, wl, rank, world, local):
     """Source-side incidence angles of every shot (wem_angles; the reference's
     compute_angles, wem.c:566-992). A unit is one shot * frequency * depth step of the
@@ -627,7 +721,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="survey64",
-                    choices=["survey64", "survey8", "survey3d", "survey3d_band", "split1", "lsm32", "angles8"])
+                    choices=["survey64", "survey8", "survey3d", "survey3d_band", "split1", "lsm32", "angles8",
+                             "elastic8"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split16"],
@@ -661,6 +756,8 @@ def main():
         wl += f" [band cut to {c['params']['fmin']:g}-{args.fmax:g} Hz]"
     if args.workload == "angles8":
         return run_angles(args, c, wl, rank, world, local)
+    if args.workload == "elastic8":
+        return run_elastic(args, c, wl, rank, world, local)
     if args.precision != "fp32":
         c["params"] = dict(c["params"], precision=args.precision)
         wl += f" [{args.precision}: DFT stages on the tensor cores, split fp16 hi+lo operands, fp32 accumulation]"

@@ -216,6 +216,29 @@ WEM_API int wem_ctx_stream(wem_ctx *ctx, void **stream);
 WEM_API int wem_migrate_noalloc(const wem_params *p, const float *vel_dev, const float *wav_dev, int nshot,
                                 const float *sx, const float *sy, const float *d_dev, float *m_dev, void *stream);
 
+/* Elastic shot-profile migration (adj = 1) or its forward operator (adj = 0) on `device`:
+   the reference's ewem() (ewem.c:3-253, ewem.h:3-16) for nshot shots at once, 2-D (nmy = 1).
+   vp, vs [nmx][nz]; wav [nt]; ux, uz [nshot][nmx][nt], the x and z components recorded on
+   every grid cell (adj: read; forward: written); mpp, mps2 [nmx][nz], the P and S images
+   (adj: written, stacked over the shots; forward: read). The y component and the S1 image
+   take no part, as in the reference's separation (ewem.c:553-741). padx*nmx a power of two
+   in [64, 2048] or another length in [33, 1024]. Allocates its device memory per call. */
+WEM_API int wem_elastic(int device, const wem_params *p, const float *vp, const float *vs, const float *wav,
+                        int nshot, const float *sx, const float *sy, float *ux, float *uz, float *mpp,
+                        float *mps2, int adj);
+
+/* Device time in ms of the last wem_elastic call (spectra, depth kernel, reduction or
+   synthesis; CUDA events), no counterpart in the reference. */
+WEM_API float wem_elastic_last_ms(void);
+
+/* Drop-in for the reference's ewem() (ewem.h:3-16): the same arguments, float** rows as
+   alloc2float builds them (seismic.c:92-106), one shot; adj: (ux, uz) -> (mpp, mps2), mps1
+   zeroed; forward: (mpp, mps2) -> (ux, uz), uy zeroed. Returns a status instead of void. */
+WEM_API int ewem(float **ux, float **uy, float **uz, float **mpp, float **mps1, float **mps2, float **wav, int nt,
+                 float ot, float dt, int nmx, float omx, float dmx, int nmy, float omy, float dmy, float sx, float sy,
+                 int nz, float oz, float dz, float gz, float sz, float **vp, float **vs, float fmin, float fmax,
+                 int padt, int padx, bool adj, bool verbose);
+
 /* Drop-in for the reference's wem() (wem.h:3-11). Same arguments, float** rows as
    alloc2float builds them (seismic.c:92-106). Returns a status instead of void.
    adj=true: d -> m (m overwritten); adj=false: m -> d (d overwritten). */

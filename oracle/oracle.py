@@ -27,9 +27,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "libshotwem_ref.so")
 REF_EXE_PATH = os.path.join(HERE, "_ref", "shotwem_ref")
+EWEM_REF_PATH = os.path.join(HERE, "_ref", "libewem_ref.so")
 
 _lib = None
 _ref = None
+_ewem = None
 
 _f = C.c_float
 _i = C.c_int
@@ -116,6 +118,40 @@ def ref_lib():
                                      fpp, _f, _f, C.c_bool]
         _ref = L
     return _ref
+
+
+def ewem_ref(p: dict, vp: np.ndarray, vs: np.ndarray, wav: np.ndarray, ux=None, uz=None, mpp=None, mps2=None,
+             adj: bool = True):
+    """The reference's own elastic migration ewem() (oracle/_ref/libewem_ref.so,
+    src/Imaging/c/ewem.c:3-253), one shot, via float** rows. adj=True: (ux, uz) data
+    [nx*ny, nt] -> (mpp, mps1, mps2) images [nx*ny, nz]; adj=False: (mpp, mps2) -> (ux, uy,
+    uz). The y component and mps1 take no part in the reference's 2-D separation
+    (ewem.c:553-741), so they are zero in and out here."""
+    global _ewem
+    if _ewem is None:
+        if not os.path.exists(EWEM_REF_PATH):
+            build_ref()
+        if not os.path.exists(EWEM_REF_PATH):
+            raise RuntimeError("the reference's elastic core is not built (oracle/_ref missing)")
+        L = C.CDLL(EWEM_REF_PATH)
+        fpp = C.POINTER(_fp)
+        L.ewem.restype = None
+        L.ewem.argtypes = [fpp] * 7 + _WEM_ARGS_TAIL + [fpp, fpp, _f, _f, _i, _i, C.c_bool, C.c_bool]
+        _ewem = L
+    n = int(p["nmx"]) * int(p.get("nmy", 1))
+    nt, nz = int(p["nt"]), int(p["nz"])
+
+    def arr(a, cols):
+        return np.zeros((n, cols), np.float32) if a is None else np.ascontiguousarray(a, np.float32).copy()
+    dx, dy, dz_ = arr(ux, nt), np.zeros((n, nt), np.float32), arr(uz, nt)
+    m1, m2, m3 = arr(mpp, nz), np.zeros((n, nz), np.float32), arr(mps2, nz)
+    wav2 = np.ascontiguousarray(np.asarray(wav, np.float32).reshape(1, -1)).copy()
+    vpa = np.ascontiguousarray(vp, np.float32).copy()
+    vsa = np.ascontiguousarray(vs, np.float32).copy()
+    _ewem.ewem(_rows(dx), _rows(dy), _rows(dz_), _rows(m1), _rows(m2), _rows(m3), _rows(wav2), *_common(p),
+               _rows(vpa), _rows(vsa), float(p.get("fmin", 0.0)), float(p.get("fmax", 80.0)),
+               int(p.get("padt", 1)), int(p.get("padx", 1)), bool(adj), False)
+    return (m1, m2, m3) if adj else (dx, dy, dz_)
 
 
 def angles_ref(p: dict, vel: np.ndarray, wav: np.ndarray):

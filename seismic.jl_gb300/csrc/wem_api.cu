@@ -333,7 +333,7 @@ static void freq_grid(const wem_params &p, int *ntfft, int *nw, int *ifmin, int 
 static int is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
 // In-place radix-2 FFT of n = re.size() (a power of two) complex doubles, sign -1 forward.
-static void fft_pow2_double(std::vector<double> &re, std::vector<double> &im, int sign)
+void fft_pow2_double(std::vector<double> &re, std::vector<double> &im, int sign)
 {
     const int n = (int)re.size();
     for (int i = 1, j = 0; i < n; i++) {
@@ -365,7 +365,7 @@ static void fft_pow2_double(std::vector<double> &re, std::vector<double> &im, in
 // wem_step.cuh): chirp[n] = e^{i pi n^2 / L}, n < L (n^2 reduced mod 2L in integers, then
 // the angle in double), and gq = G / N with G the forward N-point FFT (double precision) of
 // the chirp placed at n and N - n (N >= 2L - 1, so the two copies do not overlap).
-static void bluestein_tables(int L, int N, float2 *chirp, float2 *gq)
+void bluestein_tables(int L, int N, float2 *chirp, float2 *gq)
 {
     std::vector<double> gr(N, 0.0), gi(N, 0.0);
     for (int n = 0; n < L; n++) {
@@ -387,7 +387,7 @@ static void bluestein_tables(int L, int N, float2 *chirp, float2 *gq)
 // The 2-D row length of the depth kernels for a transform of length nkx: nkx itself when it
 // is a power of two in [32, 4096]; otherwise (Bluestein) the smallest power of two >= 2 nkx - 1,
 // when that is at most 4096; 0 when neither fits.
-static int row_length_2d(int nkx, bool *blu)
+int row_length_2d(int nkx, bool *blu)
 {
     *blu = false;
     if (is_pow2(nkx)) return (nkx >= 32 && nkx <= 4096) ? nkx : 0;

@@ -1,0 +1,395 @@
+// wem_elastic.cuh -- the elastic depth kernels (see wem_elastic.cu) as templates over the row
+// length N, instantiated one N per translation unit (wem_elastic_n<N>.cu) so that the build
+// compiles them in parallel.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "wem_fft.cuh"
+#include "wem_internal.h"
+#include "wem_step.cuh"
+
+namespace gbwem {
+
+struct EwemArgs {
+    MigArgs m;           // nmx, nz, nwf, ifmin, nshot, dw, dz, dkx, inv_n; nlog/chirp/bfft for Bluestein rows
+    int nkx;             // transform length L (the row length N, or shorter on Bluestein rows)
+    float gz, sz, oz;
+    float inv_max_source;  // 1 / max_t |wav| / sqrtf(ntfft) (ewem.c:145)
+    float inv_sqt;         // 1 / sqrtf(ntfft)
+    const float *po_p, *po_s;   // [nz] layer slownesses
+    const float *pd_p, *pd_s;   // [nz][nmx] slowness perturbations
+    const float *vp_mean, *vs_mean;  // [nz] 1/po (the separation's velocities, ewem.c:314)
+    const float *taper;         // [nmx] boundary_condition (ewem.c:533-551)
+    const float2 *twid;         // FFT twiddles of N
+    const float2 *srcw;         // [nwf] wavelet spectrum / sqrtf(ntfft)
+    const int *igx;             // [nshot]
+    const float2 *recv_x, *recv_z;  // [nshot][nwf][nmx] receiver spectra / sqrtf(ntfft) (adj)
+    float2 *slots;              // adj: [2][grid][nz][nmx] (sum, compensation) of the P and S2 images
+    float2 *smig;               // forward: [grid][nz][nmx] source wavefield of every depth
+    const float *img_p, *img_s;  // forward: [nz][nmx] images (depth-major)
+    float2 *dg_x, *dg_z;        // forward: [nshot][nwf][nmx] modelled spectra / sqrtf(ntfft)
+};
+
+// signed wavenumber of position k of a transform of length L: ikx < L/2. ? dkx ikx :
+// -(dkx L - dkx ikx), float operations of ewem.c:414, 614
+__device__ __forceinline__ float kx_signed(int k, int L, float dkx)
+{
+    return 2 * k < L ? __fmul_rn(dkx, (float)k) : -__fsub_rn(__fmul_rn(dkx, (float)L), __fmul_rn(dkx, (float)k));
+}
+
+// The separation coefficients of ewem.c:598-611 at wavenumber kx; `on` where the potentials
+// are separated (norm >= 0.1 and w >= 20; NaN compares false, as in the reference).
+struct SepCoef {
+    float kxp, kzp, kxs, kzs, norm;
+    bool on;
+};
+__device__ __forceinline__ SepCoef sep_coef(float kx, float w, float vp, float vs)
+{
+    SepCoef c;
+    const float w2 = __fmul_rn(w, w), kx2 = __fmul_rn(kx, kx);
+    const float sp = __fsub_rn(__fdiv_rn(w2, __fmul_rn(vp, vp)), kx2);
+    const float ss = __fsub_rn(__fdiv_rn(w2, __fmul_rn(vs, vs)), kx2);
+    float kzp = sp > 0.f ? __fsqrt_rn(sp) : 0.f;
+    float kzs = ss > 0.f ? __fsqrt_rn(ss) : 0.f;
+    const float np_ = __fsqrt_rn(__fadd_rn(kx2, __fmul_rn(kzp, kzp)));
+    const float ns_ = __fsqrt_rn(__fadd_rn(kx2, __fmul_rn(kzs, kzs)));
+    c.kxp = __fdiv_rn(kx, np_);
+    c.kxs = __fdiv_rn(kx, ns_);
+    c.kzp = __fdiv_rn(kzp, np_);
+    c.kzs = __fdiv_rn(kzs, ns_);
+    c.norm = __fadd_rn(__fmul_rn(c.kxp, c.kxs), __fmul_rn(c.kzp, c.kzs));
+    c.on = (double)c.norm >= 0.1 && (double)w >= 20.0;
+    return c;
+}
+
+__device__ __forceinline__ float2 c_axpy(float a, float2 x, float b, float2 y)
+{
+    return make_float2(a * x.x + b * y.x, a * x.y + b * y.y);
+}
+
+// ssop of ewem.c:368-456 on a team's row (x-domain in v, zero at x >= nmx), both directions:
+// adj (migration and the source): transform, phase, inverse, then exp(i w pd dz) and the taper;
+// forward (modelling, -dz): the taper and exp(i w pd dz) first. ph: the phase table of the
+// layer slowness (entries / L folded, +dz), corr: exp(i w pd dz) of the row (+dz); conj selects
+// -dz.
+template <int N, bool BLU>
+__device__ __forceinline__ void ssop_row(float2 (&v)[16], bool adj, bool conj, const float2 *ph, const float2 *corr,
+                                         const float *taper, float2 *xbuf, const float2 *tw, int t, unsigned sync,
+                                         const MigArgs &m)
+{
+    constexpr int T = N / 16;
+    const int nmx = m.nmx;
+    if (!adj) {
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int x = t + T * q;
+            if (x < nmx) {
+                const float2 c = corr[x];
+                const float tp = taper[x];
+                const float2 u = make_float2(v[q].x * tp, v[q].y * tp);
+                v[q] = conj ? cmulc(u, c) : cmul(u, c);
+            } else {
+                v[q] = make_float2(0.f, 0.f);
+            }
+        }
+    }
+    xform<N, -1, false, BLU>(v, xbuf, tw, t, sync, nullptr, m);
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const float2 P = ph[kidx<N, BLU>(t, q, m.nlog)];
+        v[q] = conj ? cmulc(v[q], P) : cmul(v[q], P);
+    }
+    xform<N, +1, false, BLU>(v, xbuf, tw, t, sync, nullptr, m);
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const int x = t + T * q;
+        if (x < nmx) {
+            if (adj) {
+                const float2 c = corr[x];
+                const float tp = taper[x];
+                const float2 u = conj ? cmulc(v[q], c) : cmul(v[q], c);
+                v[q] = make_float2(u.x * tp, u.y * tp);
+            }
+        } else {
+            v[q] = make_float2(0.f, 0.f);
+        }
+    }
+}
+
+// The mixing of elastic_separate_3d at the team's wavenumbers: the team's own spectrum is in
+// v (Z form on Bluestein rows, which the per-wavenumber mixing keeps), the two spectra in
+// sa (x or P) and sb (z or S2). role 0 computes the first output (P, or ux), role 1 the second
+// (S2, or uz). sep: components -> potentials; otherwise potentials -> components. adj picks
+// the reference's two variants. The 1/L of the transform pair is applied here.
+template <int N, bool BLU>
+__device__ __forceinline__ void mix_row(float2 (&v)[16], int role, bool sep, bool adj, const float2 *sa,
+                                        const float2 *sb, float w, float vp, float vs, int t, const MigArgs &m)
+{
+    constexpr int T = N / 16;
+    const int L = BLU ? m.nlog : N;
+    const float s = m.inv_n;
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+        const int k = t + T * q;
+        if (BLU && k >= L) {
+            v[q] = make_float2(0.f, 0.f);
+            continue;
+        }
+        const float2 A = sa[k], B = sb[k];
+        const SepCoef c = sep_coef(kx_signed(k, L, m.dkx), w, vp, vs);
+        float2 r;
+        if (sep) {
+            if (!c.on) {
+                r = role == 0 ? B : A;                                   // up = uz, us2 = ux
+            } else if (adj) {
+                r = role == 0 ? c_axpy(c.kxp, A, c.kzp, B) : c_axpy(-c.kzs, A, c.kxs, B);
+            } else {
+                const float2 q0 = role == 0 ? c_axpy(c.kxs, A, c.kzs, B) : c_axpy(-c.kzp, A, c.kxp, B);
+                r = make_float2(__fdiv_rn(q0.x, c.norm), __fdiv_rn(q0.y, c.norm));
+            }
+        } else {
+            if (!c.on) {
+                r = role == 0 ? B : A;                                   // ux = us2, uz = up
+            } else if (!adj) {
+                r = role == 0 ? c_axpy(c.kxp, A, -c.kzs, B) : c_axpy(c.kzp, A, c.kxs, B);
+            } else {
+                const float2 q0 = role == 0 ? c_axpy(c.kxs, A, -c.kzp, B) : c_axpy(c.kzs, A, c.kxp, B);
+                r = make_float2(__fdiv_rn(q0.x, c.norm), __fdiv_rn(q0.y, c.norm));
+            }
+        }
+        v[q] = make_float2(r.x * s, r.y * s);
+    }
+}
+
+template <int N> struct EwemShape {
+    static constexpr int T = N / 16, NT = 3 * T, PADN = pad16(N);
+    static constexpr int TW = fft_tw_size<N>(), TWP = (TW + 1) & ~1;
+    static constexpr int HM = N / 2 + 2;  // phase-table stride (entries <= L/2 + 1)
+};
+
+__host__ __device__ inline size_t ewem_smem_floats2(int N, int TWP, int PADN, int nmx)
+{
+    const int nmxp = (nmx + 1) & ~1;
+    return (size_t)TWP + 2 * (size_t)(N / 2 + 2) + 2 * (size_t)nmxp + 3 * (size_t)N + 3 * (size_t)PADN;
+}
+
+// The depth recursion of every (shot, frequency) item: ADJ migration, otherwise modelling.
+template <int N, bool BLU, bool ADJ>
+__global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArgs a)
+{
+    using SH = EwemShape<N>;
+    constexpr int T = SH::T, NT = SH::NT, PADN = SH::PADN;
+    const MigArgs &m = a.m;
+    const int nmx = m.nmx, nz = m.nz;
+    const int nmxp = (nmx + 1) & ~1;
+    extern __shared__ float4 smem_raw[];
+    float2 *tw = reinterpret_cast<float2 *>(smem_raw);
+    float2 *php = tw + SH::TWP, *phs = php + SH::HM;
+    float2 *cp = phs + SH::HM, *cs = cp + nmxp;
+    float2 *specA = cs + nmxp, *specB = specA + N, *srow = specB + N;
+    float2 *xb = srow + N;
+    const int tid = threadIdx.x, team = tid / T, t = tid - team * T;
+    float2 *xbuf = xb + (size_t)team * PADN;
+    const unsigned sync = team_sync_handle<N>(tid);
+    for (int i = tid; i < SH::TW; i += NT) tw[i] = a.twid[i];
+    const int HALF = (BLU ? m.nlog : N) / 2 + 1;
+    const int nitems = m.nshot * m.nwf;
+
+    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
+        const int shot = item % m.nshot, iwi = item / m.nshot;
+        const int iw = m.ifmin + iwi;
+        const float w = __fmul_rn((float)iw, m.dw);
+        const float w2 = __fmul_rn(w, w);
+        const float factor = iw == 0 ? 1.f : 2.f;
+        const int igx = a.igx[shot];
+        float2 v[16];
+        // the row this team carries: the source spike, or the receiver's ux / uz spectra
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int x = t + T * q;
+            float2 u = make_float2(0.f, 0.f);
+            if (x < nmx) {
+                if (team == 0) u = x == igx ? a.srcw[iwi] : u;
+                else if (ADJ) u = (team == 1 ? a.recv_x : a.recv_z)[((size_t)shot * m.nwf + iwi) * nmx + x];
+            }
+            v[q] = u;
+        }
+        // tables of depth iz for the layer slownesses (all threads)
+        auto tables = [&](int iz) {
+            const float pp = a.po_p[iz], ps = a.po_s[iz];
+            const float sp2 = __fmul_rn(pp, pp), ss2 = __fmul_rn(ps, ps);
+            for (int k = tid; k < HALF; k += NT) {
+                const float kx = __fmul_rn(m.dkx, (float)k);
+                php[k] = phase_entry(w2, sp2, kx, m.dz, m.inv_n);
+                phs[k] = phase_entry(w2, ss2, kx, m.dz, m.inv_n);
+            }
+            const float *dp = a.pd_p + (size_t)iz * nmx, *ds = a.pd_s + (size_t)iz * nmx;
+            for (int x = tid; x < nmx; x += NT) {
+                float sn, c;
+                sincosf(__fmul_rn(__fmul_rn(w, dp[x]), m.dz), &sn, &c);
+                cp[x] = make_float2(c, sn);
+                sincosf(__fmul_rn(__fmul_rn(w, ds[x]), m.dz), &sn, &c);
+                cs[x] = make_float2(c, sn);
+            }
+        };
+        // the receiver teams' separation or recombination: forward transforms, spectra to
+        // shared memory, mixing at each wavenumber, inverse transforms
+        auto mix = [&](bool sep, float vp, float vs) {
+            if (team > 0) {
+                xform<N, -1, false, BLU>(v, xbuf, tw, t, sync, nullptr, m);
+                float2 *dst = team == 1 ? specA : specB;
+#pragma unroll
+                for (int q = 0; q < 16; q++) dst[t + T * q] = v[q];
+            }
+            __syncthreads();
+            if (team > 0) {
+                mix_row<N, BLU>(v, team - 1, sep, ADJ, specA, specB, w, vp, vs, t, m);
+                xform<N, +1, false, BLU>(v, xbuf, tw, t, sync, nullptr, m);
+#pragma unroll
+                for (int q = 0; q < 16; q++)
+                    if (t + T * q >= nmx) v[q] = make_float2(0.f, 0.f);
+            }
+        };
+
+        if (ADJ) {
+            float2 *slot_p = a.slots + (size_t)blockIdx.x * nz * nmx;
+            float2 *slot_s = a.slots + ((size_t)gridDim.x + blockIdx.x) * nz * nmx;
+            for (int iz = 0; iz < nz; iz++) {
+                const float z = __fadd_rn(a.oz, __fmul_rn(m.dz, (float)iz));
+                const bool src_on = z >= a.sz, rec_on = z >= a.gz;
+                __syncthreads();  // the previous depth's tables, spectra and source row are read
+                tables(iz);
+                __syncthreads();
+                if (team == 0) {
+                    if (src_on) {
+                        ssop_row<N, BLU>(v, true, true, php, cp, a.taper, xbuf, tw, t, sync, m);
+#pragma unroll
+                        for (int q = 0; q < 16; q++)
+                            srow[t + T * q] = make_float2(v[q].x * a.inv_max_source, v[q].y * a.inv_max_source);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < 16; q++) srow[t + T * q] = make_float2(0.f, 0.f);
+                    }
+                }
+                if (!rec_on) continue;  // CTA-uniform
+                const float vp = a.vp_mean[iz], vs = a.vs_mean[iz];
+                mix(true, vp, vs);  // components -> potentials
+                if (team > 0)
+                    ssop_row<N, BLU>(v, true, false, team == 1 ? php : phs, team == 1 ? cp : cs, a.taper, xbuf, tw, t,
+                                     sync, m);
+                __syncthreads();  // the source row is in srow; the spectra were read
+                if (team > 0) {
+                    float2 *slot = (team == 1 ? slot_p : slot_s) + (size_t)iz * nmx;
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const int x = t + T * q;
+                        if (x < nmx) {
+                            const float2 s_ = srow[x];
+                            kahan_add(&slot[x], factor * (s_.x * v[q].x + s_.y * v[q].y));  // Re(conj(smig) u)
+                        }
+                    }
+                }
+                mix(false, vp, vs);  // potentials -> components
+            }
+        } else {
+            float2 *smig = a.smig + (size_t)blockIdx.x * nz * nmx;
+            // source, downward, every depth kept
+            for (int iz = 0; iz < nz; iz++) {
+                const float z = __fadd_rn(a.oz, __fmul_rn(m.dz, (float)iz));
+                __syncthreads();
+                tables(iz);
+                __syncthreads();
+                if (team == 0) {
+                    float2 *row = smig + (size_t)iz * nmx;
+                    if (z >= a.sz) ssop_row<N, BLU>(v, true, true, php, cp, a.taper, xbuf, tw, t, sync, m);
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const int x = t + T * q;
+                        if (x < nmx)
+                            row[x] = z >= a.sz ? make_float2(v[q].x * a.inv_max_source, v[q].y * a.inv_max_source)
+                                               : make_float2(0.f, 0.f);
+                    }
+                }
+            }
+            __syncthreads();  // smig written by team 0 is read by the receiver teams below
+            // receiver, upward with the images injected
+            for (int iz = nz - 1; iz >= 0; iz--) {
+                const float z = __fadd_rn(a.oz, __fmul_rn(m.dz, (float)iz));
+                if (!(z >= a.gz)) continue;  // CTA-uniform
+                __syncthreads();
+                tables(iz);
+                __syncthreads();
+                const float vp = a.vp_mean[iz], vs = a.vs_mean[iz];
+                mix(true, vp, vs);
+                if (team > 0) {
+                    const float2 *row = smig + (size_t)iz * nmx;
+                    const float *img = (team == 1 ? a.img_p : a.img_s) + (size_t)iz * nmx;
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const int x = t + T * q;
+                        if (x < nmx) {
+                            const float2 s_ = row[x];
+                            const float mv = img[x];
+                            v[q].x += s_.x * mv;
+                            v[q].y += s_.y * mv;
+                        }
+                    }
+                    ssop_row<N, BLU>(v, false, true, team == 1 ? php : phs, team == 1 ? cp : cs, a.taper, xbuf, tw, t,
+                                     sync, m);
+                }
+                __syncthreads();  // the spectra of the separation were read
+                mix(false, vp, vs);
+            }
+            if (team > 0) {  // ux_g_wx, uz_g_wx = u / sqrtf(ntfft) (ewem.c:357-361)
+                float2 *out = (team == 1 ? a.dg_x : a.dg_z) + ((size_t)shot * m.nwf + iwi) * nmx;
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const int x = t + T * q;
+                    if (x < nmx) out[x] = make_float2(v[q].x * a.inv_sqt, v[q].y * a.inv_sqt);
+                }
+            }
+        }
+    }
+}
+
+template <int N, bool BLU, bool ADJ>
+int ewem_launch_t(const EwemArgs *a, int nsm, int nitems, cudaStream_t st, int *grid_out, size_t *smem_out)
+{
+    using SH = EwemShape<N>;
+    const size_t smem = sizeof(float2) * ewem_smem_floats2(N, SH::TWP, SH::PADN, a ? a->m.nmx : 0);
+    *smem_out = smem;
+    auto k = wem_ewem_kernel<N, BLU, ADJ>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, SH::NT, smem) != cudaSuccess || bps < 1) return -1;
+    const long long cap = (long long)nsm * bps;
+    const int grid = (int)std::max<long long>(1, std::min<long long>(cap, nitems));
+    *grid_out = grid;
+    if (!a->slots && !a->smig) return 0;  // sizing only
+    k<<<grid, SH::NT, smem, st>>>(*a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N>
+int ewem_launch_n(int blu, int adj, const EwemArgs *a, int nsm, int nitems, cudaStream_t st, int *grid, size_t *smem)
+{
+    if (blu) return adj ? ewem_launch_t<N, true, true>(a, nsm, nitems, st, grid, smem)
+                        : ewem_launch_t<N, true, false>(a, nsm, nitems, st, grid, smem);
+    return adj ? ewem_launch_t<N, false, true>(a, nsm, nitems, st, grid, smem)
+               : ewem_launch_t<N, false, false>(a, nsm, nitems, st, grid, smem);
+}
+
+#define WEM_EWEM_DECLARE_N(N)                                                                            \
+    extern template int ewem_launch_n<N>(int, int, const EwemArgs *, int, int, cudaStream_t, int *, size_t *);
+WEM_EWEM_DECLARE_N(64)
+WEM_EWEM_DECLARE_N(128)
+WEM_EWEM_DECLARE_N(256)
+WEM_EWEM_DECLARE_N(512)
+WEM_EWEM_DECLARE_N(1024)
+WEM_EWEM_DECLARE_N(2048)
+#undef WEM_EWEM_DECLARE_N
+
+}  // namespace gbwem

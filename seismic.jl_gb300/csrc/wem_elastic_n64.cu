@@ -1,0 +1,6 @@
+// wem_elastic_n64.cu -- instantiates the elastic depth kernels for rows of 64 samples.
+#include "wem_elastic.cuh"
+
+namespace gbwem {
+template int ewem_launch_n<64>(int, int, const EwemArgs *, int, int, cudaStream_t, int *, size_t *);
+}  // namespace gbwem

@@ -7,4 +7,4 @@ Arrays follow the reference's layouts: vel [nmx*nmy, nz], image [nmx*nmy, nz],
 traces [ntrace, nt].
 """
 from ._lib import WemError, build, lib, LIB_PATH, EXPORTS  # noqa: F401
-from .api import Context, Shots, make_params, migrate, wem_dropin  # noqa: F401
+from .api import Context, Shots, elastic, make_params, migrate, wem_dropin  # noqa: F401

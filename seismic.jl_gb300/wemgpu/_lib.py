@@ -29,6 +29,7 @@ EXPORTS = ["wem_last_error", "wem_version", "wem_ctx_create", "wem_ctx_destroy",
            "wem_migrate", "wem_migrate_device", "wem_migrate_survey", "wem_last_timing",
            "wem_last_kernel_times", "wem_last_launch", "wem_last_launch_form", "wem_ctx_stream", "wem_migrate_noalloc", "wem_model",
            "wem_model_device", "wem_angles", "wem", "wem_selftest_wait_timeout", "wem_measure_fp32_peak",
+           "wem_elastic", "wem_elastic_last_ms", "ewem",
            "shotwem_main", "main"]
 
 
@@ -90,6 +91,8 @@ def lib():
         L.wem_last_launch_form.argtypes = [vp, ip, ip]
         L.wem_selftest_wait_timeout.argtypes = [C.c_int, ip, C.POINTER(C.c_float)]
         L.wem_measure_fp32_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+        L.wem_elastic.argtypes = [C.c_int, C.POINTER(Params), fp, fp, fp, C.c_int, fp, fp, fp, fp, fp, fp, C.c_int]
+        L.wem_elastic_last_ms.restype = C.c_float
         L.wem_angles.argtypes = [vp, C.POINTER(Params), fp, fp, C.c_int, fp, fp, fp, fp]
         L.wem_ctx_stream.argtypes = [vp, C.POINTER(vp)]
         L.wem_migrate_noalloc.argtypes = [C.POINTER(Params), vp, vp, C.c_int, fp, fp, vp, vp, vp]

@@ -236,3 +236,33 @@ def wem_dropin(p: dict, vel, wav, d=None, m=None, adj=True) -> np.ndarray:
                      int(p.get("padx", 1)), bool(adj), bool(p.get("pspi", True)), False)
     L.check(rc)
     return mm if adj else dd
+
+
+def elastic(params: dict, vp, vs, wav, sx, sy=None, ux=None, uz=None, mpp=None, mps2=None, adj: bool = True,
+            device: int = 0):
+    """Elastic shot-profile migration (adj=True: the x and z components ux, uz [nshot, nmx, nt]
+    recorded on every grid cell -> the P and S images mpp, mps2 [nmx, nz], stacked over the
+    shots) or its forward operator (adj=False: mpp, mps2 -> ux, uz), wem_elastic (the
+    reference's ewem, src/Imaging/c/ewem.c, 2-D). Returns (mpp, mps2) or (ux, uz)."""
+    p = make_params(**params)
+    sx = np.ascontiguousarray(np.atleast_1d(sx), dtype=np.float32)
+    sy = np.ascontiguousarray(np.zeros(len(sx)) if sy is None else np.atleast_1d(sy), dtype=np.float32)
+    nshot, nmx, nz, nt = len(sx), p.nmx, p.nz, p.nt
+    vp = np.ascontiguousarray(vp, dtype=np.float32)
+    vs = np.ascontiguousarray(vs, dtype=np.float32)
+    wav = np.ascontiguousarray(wav, dtype=np.float32)
+    if adj:
+        ux = np.ascontiguousarray(ux, dtype=np.float32).reshape(nshot, nmx, nt)
+        uz = np.ascontiguousarray(uz, dtype=np.float32).reshape(nshot, nmx, nt)
+        mpp = np.empty((nmx, nz), np.float32)
+        mps2 = np.empty((nmx, nz), np.float32)
+    else:
+        mpp = np.ascontiguousarray(mpp, dtype=np.float32).reshape(nmx, nz)
+        mps2 = np.ascontiguousarray(mps2, dtype=np.float32).reshape(nmx, nz)
+        ux = np.empty((nshot, nmx, nt), np.float32)
+        uz = np.empty((nshot, nmx, nt), np.float32)
+    L.check(L.lib().wem_elastic(device, C.byref(p), vp.ctypes.data_as(_f32p), vs.ctypes.data_as(_f32p),
+                                wav.ctypes.data_as(_f32p), nshot, sx.ctypes.data_as(_f32p), sy.ctypes.data_as(_f32p),
+                                ux.ctypes.data_as(_f32p), uz.ctypes.data_as(_f32p), mpp.ctypes.data_as(_f32p),
+                                mps2.ctypes.data_as(_f32p), int(bool(adj))))
+    return (mpp, mps2) if adj else (ux, uz)

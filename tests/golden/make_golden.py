@@ -102,6 +102,37 @@ def main(only=None):
         print("main() image norm", float(np.linalg.norm(m_main)))
 
 
+EWEM_CASES = {
+    # name: (seed, nx, nz, nt, fmax, padx); the S velocity is vp / 1.8 with a seeded wobble
+    "ewem_64": (41, 64, 16, 128, 40.0, 2),        # nkx 128
+    "ewem_150_padx1": (42, 150, 12, 128, 35.0, 1),  # nkx 150 (taper on)
+}
+
+
+def ewem_main():
+    """The reference's elastic ewem() (oracle/_ref/libewem_ref.so, src/Imaging/c/ewem.c),
+    one shot per case, migration and forward."""
+    os.environ.setdefault("OMP_NUM_THREADS", "4")
+    for name, (seed, nx, nz, nt, fmax, padx) in EWEM_CASES.items():
+        c = synth.small_case(seed, nx=nx, nz=nz, nt=nt, nshot=1, pspi=0, fmax=fmax, padx=padx)
+        rng = np.random.default_rng(seed + 200)
+        vp = c["vel"]
+        vs = (vp / 1.8 * (1.0 + 0.05 * rng.standard_normal(vp.shape))).astype(np.float32)
+        p = dict(c["params"], sx=float(c["shots"].sx[0]), fmin=3.0)
+        d = synth.shot_gather_full(c["shots"], 0, nx)
+        ux_in = (0.4 * d + 0.1 * np.roll(d, 3, axis=1)).astype(np.float32)
+        uz_in = d
+        m_pp, m_s1, m_s2 = O.ewem_ref(p, vp, vs, c["wav"], ux=ux_in, uz=uz_in, adj=True)
+        mpp_in = rng.standard_normal((nx, nz)).astype(np.float32)
+        mps2_in = rng.standard_normal((nx, nz)).astype(np.float32)
+        ux_ref, uy_ref, uz_ref = O.ewem_ref(p, vp, vs, c["wav"], mpp=mpp_in, mps2=mps2_in, adj=False)
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), vp=vp, vs=vs, wav=c["wav"], ux=ux_in, uz=uz_in,
+                            mpp_ref=m_pp, mps2_ref=m_s2, mpp_in=mpp_in, mps2_in=mps2_in, ux_ref=ux_ref,
+                            uz_ref=uz_ref, params=np.array(repr(p)))
+        print(name, "images", float(np.linalg.norm(m_pp)), float(np.linalg.norm(m_s2)), "data",
+              float(np.linalg.norm(ux_ref)), float(np.linalg.norm(uz_ref)))
+
+
 ANGLE_CASES = {
     # name: (seed, nx, nz, nt, fmax); nx > 100 switches the reference's taper on
     "angles_64": (31, 64, 24, 64, 40.0),
@@ -132,6 +163,11 @@ def angles_main():
 if __name__ == "__main__":
     if sys.argv[1:] == ["angles"]:
         angles_main()
+    elif sys.argv[1:] == ["ewem"]:
+        O.build()
+        if O.build_ref() is None:
+            sys.exit("reference sources not found")
+        ewem_main()
     elif sys.argv[1:2] == ["--only"]:
         # python tests/golden/make_golden.py --only name[,name...]: those 2-D cases only
         main(set(sys.argv[2].split(",")))
@@ -139,3 +175,4 @@ if __name__ == "__main__":
         main()
         subprocess.run([sys.executable, os.path.abspath(__file__), "angles"], check=True,
                        env=dict(os.environ, OMP_NUM_THREADS="1"))
+        ewem_main()

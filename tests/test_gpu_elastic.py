@@ -1,0 +1,85 @@
+"""Elastic shot-profile migration and its forward operator on the GPU (wem_elastic and the
+ewem() drop-in; the reference's src/Imaging/c/ewem.c, 2-D) against the reference's own output
+(golden vectors) and the oracle's FP64 restatement (oracle/ewem_np.py).
+
+Tolerance: relative L2 <= 1e-4 on each image (P, S2) and each data component (x, z)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+
+
+@pytest.mark.parametrize("case", ["ewem_64", "ewem_150_padx1"])
+def test_elastic_matches_reference_golden(gpu_lib, case):
+    g = load_golden(f"{case}.npz")
+    p = g["params"]
+    mpp, mps2 = gpu_lib.elastic(p, g["vp"], g["vs"], g["wav"], [p["sx"]], ux=g["ux"][None], uz=g["uz"][None], adj=True)
+    assert rel_l2(mpp, g["mpp_ref"]) < TOL, rel_l2(mpp, g["mpp_ref"])
+    assert rel_l2(mps2, g["mps2_ref"]) < TOL, rel_l2(mps2, g["mps2_ref"])
+    ux, uz = gpu_lib.elastic(p, g["vp"], g["vs"], g["wav"], [p["sx"]], mpp=g["mpp_in"], mps2=g["mps2_in"], adj=False)
+    assert rel_l2(ux[0], g["ux_ref"]) < TOL, rel_l2(ux[0], g["ux_ref"])
+    assert rel_l2(uz[0], g["uz_ref"]) < TOL, rel_l2(uz[0], g["uz_ref"])
+
+
+def _rows(a):
+    fp = C.POINTER(C.c_float)
+    rows = (fp * a.shape[0])()
+    for i in range(a.shape[0]):
+        rows[i] = C.cast(a.ctypes.data + i * a.strides[0], fp)
+    return rows
+
+
+def test_ewem_dropin_matches_reference_golden(gpu_lib):
+    """ewem() with the reference's argument list and float** rows (ewem.h:3-16)."""
+    g = load_golden("ewem_64.npz")
+    p = g["params"]
+    L = gpu_lib.lib()
+    fpp = C.POINTER(C.POINTER(C.c_float))
+    L.ewem.restype = C.c_int
+    L.ewem.argtypes = [fpp] * 7 + [C.c_int, C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_int, C.c_float,
+                                   C.c_float, C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                                   fpp, fpp, C.c_float, C.c_float, C.c_int, C.c_int, C.c_bool, C.c_bool]
+    n, nt, nz = p["nmx"], p["nt"], p["nz"]
+    ux, uz = np.ascontiguousarray(g["ux"], np.float32), np.ascontiguousarray(g["uz"], np.float32)
+    uy = np.full((n, nt), 7.0, np.float32)
+    mpp, mps1, mps2 = (np.full((n, nz), 7.0, np.float32) for _ in range(3))
+    wav = np.ascontiguousarray(g["wav"], np.float32).reshape(1, -1)
+    vp, vs = np.ascontiguousarray(g["vp"], np.float32), np.ascontiguousarray(g["vs"], np.float32)
+    args = [p["nt"], 0.0, p["dt"], n, p["omx"], p["dmx"], 1, 0.0, p["dmx"], p["sx"], 0.0, nz, p["oz"], p["dz"], 0.0,
+            0.0, _rows(vp), _rows(vs), p["fmin"], p["fmax"], p["padt"], p["padx"]]
+    rc = L.ewem(_rows(ux), _rows(uy), _rows(uz), _rows(mpp), _rows(mps1), _rows(mps2), _rows(wav), *args, True, False)
+    assert rc == 0
+    assert rel_l2(mpp, g["mpp_ref"]) < TOL and rel_l2(mps2, g["mps2_ref"]) < TOL and not np.any(mps1)
+
+
+@pytest.mark.parametrize("nx,padx", [(128, 2), (500, 2), (256, 1)])
+def test_elastic_shots_stacked_match_fp64_oracle(gpu_lib, nx, padx):
+    """Several shots in one call (the images stacked over the shots) against the FP64
+    restatement shot by shot; nx 500 with padx 2 runs rows of nkx 1000 (Bluestein's form)."""
+    import ewem_np as E
+    from wemgpu import synth
+    c = synth.small_case(70 + nx, nx=nx, nz=10, nt=128, nshot=3, pspi=0, fmax=30.0, padx=padx)
+    rng = np.random.default_rng(nx)
+    vp = c["vel"]
+    vs = (vp / 1.7 * (1.0 + 0.05 * rng.standard_normal(vp.shape))).astype(np.float32)
+    p = dict(c["params"], fmin=3.0)
+    shots = c["shots"]
+    uz = np.stack([synth.shot_gather_full(shots, s, nx) for s in range(shots.nshot)])
+    ux = (0.5 * np.roll(uz, 2, axis=2)).astype(np.float32)
+    mpp, mps2 = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, ux=ux, uz=uz, adj=True)
+    want_p = want_s = 0.0
+    for s in range(shots.nshot):
+        a, _, b = E.ewem(dict(p, sx=float(shots.sx[s])), vp, vs, c["wav"], ux=ux[s], uz=uz[s], adj=True)
+        want_p, want_s = want_p + a, want_s + b
+    assert rel_l2(mpp, want_p) < TOL and rel_l2(mps2, want_s) < TOL
+    m1 = rng.standard_normal((nx, 10)).astype(np.float32)
+    m2 = rng.standard_normal((nx, 10)).astype(np.float32)
+    dx, dz = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, mpp=m1, mps2=m2, adj=False)
+    for s in range(shots.nshot):
+        wx, _, wz = E.ewem(dict(p, sx=float(shots.sx[s])), vp, vs, c["wav"], mpp=m1, mps2=m2, adj=False)
+        assert rel_l2(dx[s], wx) < TOL and rel_l2(dz[s], wz) < TOL

@@ -151,3 +151,17 @@ def test_angle_oracle_matches_reference_golden_3d():
         live = np.abs(ref) > 1e-3
         assert np.count_nonzero(np.sign(got[live]) != np.sign(ref[live])) == 0
         assert np.abs(ref).max() > 30.0
+
+
+@pytest.mark.parametrize("case", ["ewem_64", "ewem_150_padx1"])
+def test_elastic_fp64_restatement_matches_reference_golden(case):
+    """oracle/ewem_np.py (FP64 restatement of src/Imaging/c/ewem.c) vs the reference's own
+    ewem() output: migration (P and S2 images) and the forward operator (x and z data). The
+    reference computes in FP32, so the bar is its rounding level."""
+    import ewem_np as E
+    g = load_golden(f"{case}.npz")
+    p = g["params"]
+    m_pp, _, m_s2 = E.ewem(p, g["vp"], g["vs"], g["wav"], ux=g["ux"], uz=g["uz"], adj=True)
+    assert rel_l2(m_pp, g["mpp_ref"]) < 1e-5 and rel_l2(m_s2, g["mps2_ref"]) < 1e-5
+    ux, _, uz = E.ewem(p, g["vp"], g["vs"], g["wav"], mpp=g["mpp_in"], mps2=g["mps2_in"], adj=False)
+    assert rel_l2(ux, g["ux_ref"]) < 1e-5 and rel_l2(uz, g["uz_ref"]) < 1e-5
