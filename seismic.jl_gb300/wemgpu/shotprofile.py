@@ -295,3 +295,109 @@ def ShotProfileWEM(m: str, d: str, adj: bool = True, *, pspi=True, nref=5, dampi
     finally:
         if own:
             ctx.close()
+
+
+# --------------------------------------------------------------------------- elastic
+
+def _signs(ax, ay):
+    """signf(angx) * signf(angy) of ShotProfileEWEM.jl:434-438 (-1 below zero, else +1),
+    the factor the S images carry into and out of the angle gathers."""
+    return np.where(np.asarray(ax) < 0, -1.0, 1.0) * np.where(np.asarray(ay) < 0, -1.0, 1.0)
+
+
+def _full_grid(data: np.ndarray, hd: np.ndarray, sx, sy, g: dict) -> np.ndarray:
+    """Every shot's traces placed on the full receiver grid [nshot, n, nt] by (gx, gy)
+    (SeisWindow by sx, sy: ShotProfileEWEM.jl:91-95), zeros where a cell has no trace."""
+    n = g["nmx"] * g["nmy"]
+    shots = window_shots(data, hd, sx, sy, g)
+    out = np.zeros((len(sx), n, data.shape[1]), np.float32)
+    for s in range(len(sx)):
+        lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
+        out[s, shots.trace_cell[lo:hi]] = shots.data[lo:hi]
+    return out
+
+
+def ShotProfileEWEM(m, d, adj: bool = True, *, damping=1000.0, vp="vp.seis", vs="vs.seis", angx="angx.seis",
+                    angy="angy.seis", wav="wav.seis", sz=0.0, gz=0.0, nangx=1, oangx=0, dangx=1, nangy=1, oangy=0,
+                    dangy=1, fmin=0, fmax=80, padt=1, padx=1, verbose=False, sx=(0.0,), sy=(0.0,), device=0):
+    """Elastic migration (adj=True: data files d = [ux, uy, uz] -> image files m = [mpp, mps1,
+    mps2]) or demigration (adj=False: m -> d) of the shots at (sx[i], sy[i]): the interface of
+    Seismic.jl's ShotProfileEWEM (src/Imaging/ShotProfileEWEM.jl:38), keyword names and
+    defaults included (`damping` is accepted and unused, as there). All shots go to the GPU in
+    one wem_elastic call (per shot where angle gathers need each shot's image); with
+    nangx, nangy > 1 the shot images are binned by the shot's incidence angles (the angx/angy
+    files of ComputeAngles), the S images with the sign of the angles (ShotProfileEWEM.jl:
+    155-230, 290-350). 2-D grids; mps1 and uy are written as zeros (the separation has no S1
+    potential, ewem.c:553-741)."""
+    from .api import elastic
+    gathers = nangx != 1 or nangy != 1
+    abin = (nangx, float(oangx), float(dangx), nangy, float(oangy), float(dangy))
+    vpv, hv, g = grid_from_velocity(vp)
+    vsv, _, _ = seis.read(vs)
+    w, hw, ew = seis.read(wav)
+    nt, dt, ot = int(hw[0]["n1"]), float(hw[0]["d1"]), float(hw[0]["o1"])
+    sx = [float(v) for v in np.atleast_1d(sx)]
+    sy = [float(v) for v in np.atleast_1d(sy)]
+    if len(sy) == 1 and len(sx) > 1:
+        sy = sy * len(sx)
+    n, nz, nb = g["nmx"] * g["nmy"], g["nz"], nangx * nangy
+    params = dict(nt=nt, ot=ot, dt=dt, nmx=g["nmx"], omx=g["omx"], dmx=g["dmx"], nmy=g["nmy"], omy=g["omy"],
+                  dmy=g["dmy"], nz=nz, oz=g["oz"], dz=g["dz"], gz=gz, sz=sz, fmin=fmin, fmax=fmax, padt=padt,
+                  padx=padx, verbose=int(bool(verbose)))
+    vpv, vsv = vpv[:n], vsv[:n]
+    ext = ([nz, g["nmx"], g["nmy"], nangx, nangy], [g["oz"], g["omx"], g["omy"], oangx, oangy],
+           [g["dz"], g["dmx"], g["dmy"], dangx, dangy])
+    labels = dict(labels=["Depth", "mx", "my", "angx", "angy"], units=["m", "m", "m", "degrees", "degrees"])
+    if adj:
+        (ux, hx, _), (uz, hz, _) = seis.read(d[0]), seis.read(d[2])
+        ux, uz = _full_grid(ux, hx, sx, sy, g), _full_grid(uz, hz, sx, sy, g)
+        if not gathers:
+            mpp, mps2 = elastic(params, vpv, vsv, w[0], sx, sy, ux=ux, uz=uz, adj=True, device=device)
+            out = [mpp.astype(np.float64)[:, None], np.zeros((n, 1, nz)), mps2.astype(np.float64)[:, None]]
+        else:
+            out = [np.zeros((n, nb, nz)) for _ in range(3)]
+            for i, (x0, y0) in enumerate(zip(sx, sy)):
+                mpp, mps2 = elastic(params, vpv, vsv, w[0], [x0], [y0], ux=ux[i:i + 1], uz=uz[i:i + 1], adj=True,
+                                    device=device)
+                ax = _shot_angles(angx, x0, y0, n, nz)
+                ay = _shot_angles(angy, x0, y0, n, nz)
+                sg = _signs(ax, ay)
+                bin_shot(mpp.astype(np.float64), ax, ay, out[0], *abin)
+                bin_shot(sg * mps2, ax, ay, out[2], *abin)
+        h = gather_headers(g, g["dz"], *abin)
+        for name, a in zip(m, out):
+            seis.write(name, a.reshape(n * nb, nz).astype(np.float32), h, *ext, **labels)
+        return tuple(a.reshape(n, nb, nz) if gathers else a.reshape(n, nz) for a in out)
+    # demigration: every shot recorded on every grid cell
+    imgs = [seis.read(name)[0] for name in (m[0], m[2])]
+    if not gathers:
+        ux, uz = elastic(params, vpv, vsv, w[0], sx, sy, mpp=imgs[0][:n], mps2=imgs[1][:n], adj=False, device=device)
+    else:
+        gp, gs = (a.reshape(n, nb, nz).astype(np.float64) for a in imgs)
+        ux, uz = np.zeros((len(sx), n, nt), np.float32), np.zeros((len(sx), n, nt), np.float32)
+        for i, (x0, y0) in enumerate(zip(sx, sy)):
+            ax = _shot_angles(angx, x0, y0, n, nz)
+            ay = _shot_angles(angy, x0, y0, n, nz)
+            ip = unbin_shot(gp, ax, ay, *abin).astype(np.float32)
+            is2 = (_signs(ax, ay) * unbin_shot(gs, ax, ay, *abin)).astype(np.float32)
+            a, b = elastic(params, vpv, vsv, w[0], [x0], [y0], mpp=ip, mps2=is2, adj=False, device=device)
+            ux[i], uz[i] = a[0], b[0]
+    hd = seis.empty_headers(len(sx) * n)
+    mx = g["omx"] + g["dmx"] * np.repeat(np.arange(g["nmx"]), g["nmy"])
+    my = g["omy"] + g["dmy"] * np.tile(np.arange(g["nmy"]), g["nmx"])
+    for i, (x0, y0) in enumerate(zip(sx, sy)):
+        q = hd[i * n:(i + 1) * n]
+        q["tracenum"] = np.arange(1, n + 1) + i * n
+        q["n1"], q["d1"], q["o1"] = nt, dt, ot
+        q["sx"], q["sy"] = x0, y0
+        q["gx"], q["gy"], q["mx"], q["my"] = mx, my, mx, my
+        q["hx"], q["hy"] = mx - x0, my - y0
+        q["imx"] = np.repeat(np.arange(g["nmx"]), g["nmy"])
+        q["imy"] = np.tile(np.arange(g["nmy"]), g["nmx"])
+    nsx = len(sx)
+    dext = ([nt, g["nmx"], g["nmy"], nsx, 1], [ot, g["omx"], g["omy"], sx[0], sy[0]],
+            [dt, g["dmx"], g["dmy"], (sx[1] - sx[0]) if nsx > 1 else 1.0, 1.0])
+    comps = (ux.reshape(-1, nt), np.zeros((nsx * n, nt), np.float32), uz.reshape(-1, nt))
+    for name, a in zip(d, comps):
+        seis.write(name, a, hd, *dext, labels=["Time", "gx", "gy", "sx", "sy"], units=["s", "m", "m", "m", "m"])
+    return ux, uz

@@ -51,6 +51,21 @@ def test_compute_angles_library_exports_its_entry_points(gpu_lib):
     assert lib.main(2, argv) == gpu_lib._lib.WEM_ERR_ARG
 
 
+def test_shotewem_library_exports_its_entry_points(gpu_lib):
+    """shotewem.so (the drop-in for the reference's shotewem library) exports main and what
+    include/shotewem_gb300.h declares, and reports a missing key as a status
+    (shotewem.c:37-45 calls exit(1))."""
+    path = os.path.join(os.path.dirname(gpu_lib.LIB_PATH), "shotewem.so")
+    lib = C.CDLL(path)
+    names = declared_functions(os.path.join(ROOT, "include", "shotewem_gb300.h"))
+    assert names == ["shotewem_main"]
+    for name in names + ["main"]:
+        assert hasattr(lib, name)
+    lib.main.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+    argv = (C.c_char_p * 4)(b"0", b"ux=a", b"uy=b", b"uz=c")
+    assert lib.main(4, argv) == gpu_lib._lib.WEM_ERR_ARG
+
+
 def _has_gpu():
     lib = C.CDLL(__import__("wemgpu").LIB_PATH)
     h = C.c_void_p()

@@ -83,3 +83,49 @@ def test_elastic_shots_stacked_match_fp64_oracle(gpu_lib, nx, padx):
     for s in range(shots.nshot):
         wx, _, wz = E.ewem(dict(p, sx=float(shots.sx[s])), vp, vs, c["wav"], mpp=m1, mps2=m2, adj=False)
         assert rel_l2(dx[s], wx) < TOL and rel_l2(dz[s], wz) < TOL
+
+
+def test_shotewem_main_on_seis_files(gpu_lib, tmp_path):
+    """main of shotewem.so (shotewem.c:13-222) on seis files, migration and the forward
+    operator, against the reference's ewem() output; headers as shotewem.c writes them."""
+    import os
+    from wemgpu import seis
+    g = load_golden("ewem_64.npz")
+    p = g["params"]
+    t = str(tmp_path)
+    lib = C.CDLL(os.path.join(os.path.dirname(gpu_lib.LIB_PATH), "shotewem.so"))
+    lib.main.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+    seis.write_grid(t + "/vp", g["vp"], o1=p["oz"], d1=p["dz"], ox=p["omx"], dx=p["dmx"])
+    seis.write_grid(t + "/vs", g["vs"], o1=p["oz"], d1=p["dz"], ox=p["omx"], dx=p["dmx"])
+    seis.write_wavelet(t + "/wav", g["wav"], dt=p["dt"])
+    for k in ("ux", "uz"):
+        seis.write_shot(f"{t}/{k}", g[k], sx=p["sx"], dt=p["dt"], ox=p["omx"], dx=p["dmx"])
+    seis.write_shot(t + "/uy", np.zeros_like(g["ux"]), sx=p["sx"], dt=p["dt"], ox=p["omx"], dx=p["dmx"])
+    common = [f"{k}={t}/{k}" for k in ("ux", "uy", "uz", "mpp", "mps1", "mps2", "vp", "vs", "wav")] + [
+        f"sx={p['sx']}", "sy=0", "sz=0", "gz=0", f"fmin={p['fmin']}", f"fmax={p['fmax']}", f"padt={p['padt']}",
+        f"padx={p['padx']}"]
+
+    def run(adj):
+        args = ["0", "adj=" + ("y" if adj else "n")] + common
+        argv = (C.c_char_p * len(args))(*[a.encode() for a in args])
+        return lib.main(len(args), argv)
+
+    assert run(True) == 0
+    mpp, hp, ext = seis.read(t + "/mpp")
+    mps1, _, _ = seis.read(t + "/mps1")
+    mps2, hs, _ = seis.read(t + "/mps2")
+    assert rel_l2(mpp, g["mpp_ref"]) < TOL and rel_l2(mps2, g["mps2_ref"]) < TOL and not np.any(mps1)
+    assert np.all(hp["trid"] == 1) and np.all(hs["trid"] == 2)
+    assert np.array_equal(hp["imx"], np.arange(p["nmx"])) and ext["n"][:2] == [p["nz"], p["nmx"]]
+
+    seis.write_grid(t + "/mpp", g["mpp_in"], o1=p["oz"], d1=p["dz"], ox=p["omx"], dx=p["dmx"])
+    seis.write_grid(t + "/mps1", np.zeros_like(g["mpp_in"]), o1=p["oz"], d1=p["dz"], ox=p["omx"], dx=p["dmx"])
+    seis.write_grid(t + "/mps2", g["mps2_in"], o1=p["oz"], d1=p["dz"], ox=p["omx"], dx=p["dmx"])
+    assert run(False) == 0
+    ux, hx, ext = seis.read(t + "/ux")
+    uy, _, _ = seis.read(t + "/uy")
+    uz, _, _ = seis.read(t + "/uz")
+    assert rel_l2(ux, g["ux_ref"]) < TOL and rel_l2(uz, g["uz_ref"]) < TOL and not np.any(uy)
+    gx = p["omx"] + p["dmx"] * np.arange(p["nmx"])
+    assert np.allclose(hx["gx"], gx) and np.allclose(hx["hx"], gx - p["sx"]) and np.all(hx["n1"] == p["nt"])
+    assert ext["n"][:2] == [p["nt"], p["nmx"]]
