@@ -33,6 +33,53 @@ int row_length_2d(int nkx, bool *blu);                           // wem_api.cu
 
 using namespace gbwem;
 
+namespace gbwem {
+// The tables of one (frequency, depth) record per block: the phase entries and the slowness
+// corrections of the P and S layers, and the separation coefficients of elastic_separate_3d
+// (ewem.c:598-611) at every wavenumber; the float operations of the in-kernel forms they
+// replace (bit-identical), shared by every shot of the frequency.
+__global__ void __launch_bounds__(256) wem_ewem_tables_kernel(const EwemArgs a)
+{
+    const MigArgs &m = a.m;
+    const int rec = blockIdx.x, iz = rec % m.nz, iwc = rec / m.nz;
+    const int L = a.nkx, nmx = m.nmx;
+    const EwemRec R(L, nmx);
+    float *out = a.tabs + (size_t)rec * R.floats();
+    float2 *php = reinterpret_cast<float2 *>(out + R.php()), *phs = reinterpret_cast<float2 *>(out + R.phs());
+    float2 *cp = reinterpret_cast<float2 *>(out + R.cp()), *cs = reinterpret_cast<float2 *>(out + R.cs());
+    float *sep = out + R.sep();
+    const int iw = m.ifmin + a.wbase + iwc;
+    const float w = __fmul_rn((float)iw, m.dw);
+    const float w2 = __fmul_rn(w, w);
+    const float pp = a.po_p[iz], ps = a.po_s[iz];
+    const float sp2 = __fmul_rn(pp, pp), ss2 = __fmul_rn(ps, ps);
+    for (int k = threadIdx.x; k < R.rh; k += blockDim.x) {
+        const float kx = __fmul_rn(m.dkx, (float)k);
+        php[k] = k < L / 2 + 1 ? phase_entry(w2, sp2, kx, m.dz, m.inv_n) : make_float2(0.f, 0.f);
+        phs[k] = k < L / 2 + 1 ? phase_entry(w2, ss2, kx, m.dz, m.inv_n) : make_float2(0.f, 0.f);
+    }
+    const float *dp = a.pd_p + (size_t)iz * nmx, *ds = a.pd_s + (size_t)iz * nmx;
+    for (int x = threadIdx.x; x < R.nmxp; x += blockDim.x) {
+        float sn = 0.f, c = 0.f;
+        if (x < nmx) sincosf(__fmul_rn(__fmul_rn(w, dp[x]), m.dz), &sn, &c);
+        cp[x] = make_float2(c, sn);
+        sn = c = 0.f;
+        if (x < nmx) sincosf(__fmul_rn(__fmul_rn(w, ds[x]), m.dz), &sn, &c);
+        cs[x] = make_float2(c, sn);
+    }
+    const float vp = a.vp_mean[iz], vs = a.vs_mean[iz];
+    for (int k = threadIdx.x; k < R.lp; k += blockDim.x) {
+        SepCoef c{};
+        if (k < L) c = sep_coef(kx_signed(k, L, m.dkx), w, vp, vs);
+        sep[k] = c.kxp;
+        sep[R.lp + k] = c.kzp;
+        sep[2 * R.lp + k] = c.kxs;
+        sep[3 * R.lp + k] = c.kzs;
+        sep[4 * R.lp + k] = c.norm;
+    }
+}
+}  // namespace gbwem
+
 // ------------------------------------------------------------------ host side
 namespace {
 
@@ -258,13 +305,24 @@ extern "C" WEM_API int wem_elastic(int device, const wem_params *pp, const float
     a.po_p = d_po_p; a.po_s = d_po_s; a.pd_p = d_pd_p; a.pd_s = d_pd_s; a.vp_mean = d_vpm; a.vs_mean = d_vsm;
     a.taper = d_tap; a.twid = d_tw; a.srcw = d_srcw; a.igx = d_igx; a.recv_x = d_sx; a.recv_z = d_sz;
     a.img_p = d_mp; a.img_s = d_ms; a.dg_x = d_sx; a.dg_z = d_sz;
-    const int nitems = nshot * nwf;
+    // the per-(frequency, depth) tables, in sub-bands of at most `chunk` frequencies when the
+    // whole band's tables would take more than 4 GiB or a quarter of the free device memory
+    const size_t rec_bytes = sizeof(float) * (size_t)EwemRec(nkx, nmx).floats() * nz;
+    size_t free_b = 0, total_b = 0;
+    ECK(cudaMemGetInfo(&free_b, &total_b));
+    const size_t budget = std::min<size_t>((size_t)4 << 30, free_b / 4);
+    const int chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(nwf, 1), budget / rec_bytes));
+    a.wbase = 0;
+    a.nwc = std::min(nwf, chunk);
+    const int nitems = nshot * a.nwc;  // the largest sub-band's items size the grid and the scratch
     int grid = 0;
     size_t smem = 0;
     if (nitems > 0) {
         EwemArgs probe = a;  // sizing: no scratch yet
         if (ewem_launch(nfft, blu, adj, &probe, nsm, nitems, st, &grid, &smem))
             return set_error(WEM_ERR_SIZE, "wem_elastic: no kernel fits this row length and grid");
+        a.tabs = B.get<float>(rec_bytes / sizeof(float) * a.nwc);
+        if (!a.tabs) return set_error(WEM_ERR_NOMEM, "wem_elastic: out of device memory");
         if (adj) {
             a.slots = B.get<float2>(2 * (size_t)grid * nzx);
             if (!a.slots) return set_error(WEM_ERR_NOMEM, "wem_elastic: out of device memory");
@@ -275,8 +333,15 @@ extern "C" WEM_API int wem_elastic(int device, const wem_params *pp, const float
             ECK(cudaMemsetAsync(d_sx, 0, sizeof(float2) * ntr * nwf, st));
             ECK(cudaMemsetAsync(d_sz, 0, sizeof(float2) * ntr * nwf, st));
         }
-        if (ewem_launch(nfft, blu, adj, &a, nsm, nitems, st, &grid, &smem))
-            return set_error(WEM_ERR_CUDA, "wem_elastic: depth kernel launch");
+        for (int w0 = 0; w0 < nwf; w0 += chunk) {
+            a.wbase = w0;
+            a.nwc = std::min(chunk, nwf - w0);
+            wem_ewem_tables_kernel<<<a.nwc * nz, 256, 0, st>>>(a);
+            ECK(cudaGetLastError());
+            int g = 0;
+            if (ewem_launch(nfft, blu, adj, &a, nsm, nshot * a.nwc, st, &g, &smem))
+                return set_error(WEM_ERR_CUDA, "wem_elastic: depth kernel launch");
+        }
     }
     if (adj) {
         if (nitems > 0) {

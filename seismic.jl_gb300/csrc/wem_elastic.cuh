@@ -31,6 +31,25 @@ struct EwemArgs {
     float2 *smig;               // forward: [grid][nz][nmx] source wavefield of every depth
     const float *img_p, *img_s;  // forward: [nz][nmx] images (depth-major)
     float2 *dg_x, *dg_z;        // forward: [nshot][nwf][nmx] modelled spectra / sqrtf(ntfft)
+    // per-(frequency, depth) tables of the frequencies [wbase, wbase + nwc) (wem_ewem_tables_kernel),
+    // one record of EwemRec::floats floats per (frequency - wbase, depth), frequency-major
+    float *tabs;
+    int wbase, nwc;
+};
+
+// Layout of one table record, in floats, every part a multiple of 16 bytes:
+//   php[rh], phs[rh]   float2 phase entries of the P and S layer slownesses, k < L/2 + 1
+//   cp[nmxp], cs[nmxp] float2 exp(i w pd dz) of the P and S slowness perturbations
+//   kxp, kzp, kxs, kzs, norm [lp] each: the separation coefficients at every k < L
+struct EwemRec {
+    int rh, nmxp, lp;
+    __host__ __device__ EwemRec(int L, int nmx) : rh(((L / 2 + 1) + 1) & ~1), nmxp((nmx + 1) & ~1), lp((L + 3) & ~3) {}
+    __host__ __device__ int php() const { return 0; }
+    __host__ __device__ int phs() const { return 2 * rh; }
+    __host__ __device__ int cp() const { return 4 * rh; }
+    __host__ __device__ int cs() const { return 4 * rh + 2 * nmxp; }
+    __host__ __device__ int sep() const { return 4 * rh + 4 * nmxp; }
+    __host__ __device__ int floats() const { return 4 * rh + 4 * nmxp + 5 * lp; }
 };
 
 // signed wavenumber of position k of a transform of length L: ikx < L/2. ? dkx ikx :
@@ -126,7 +145,8 @@ __device__ __forceinline__ void ssop_row(float2 (&v)[16], bool adj, bool conj, c
 // the reference's two variants. The 1/L of the transform pair is applied here.
 template <int N, bool BLU>
 __device__ __forceinline__ void mix_row(float2 (&v)[16], int role, bool sep, bool adj, const float2 *sa,
-                                        const float2 *sb, float w, float vp, float vs, int t, const MigArgs &m)
+                                        const float2 *sb, bool w_on, const float *tab, int lp, int t,
+                                        const MigArgs &m)
 {
     constexpr int T = N / 16;
     const int L = BLU ? m.nlog : N;
@@ -139,7 +159,13 @@ __device__ __forceinline__ void mix_row(float2 (&v)[16], int role, bool sep, boo
             continue;
         }
         const float2 A = sa[k], B = sb[k];
-        const SepCoef c = sep_coef(kx_signed(k, L, m.dkx), w, vp, vs);
+        SepCoef c;
+        c.kxp = tab[k];
+        c.kzp = tab[lp + k];
+        c.kxs = tab[2 * lp + k];
+        c.kzs = tab[3 * lp + k];
+        c.norm = tab[4 * lp + k];
+        c.on = (double)c.norm >= 0.1 && w_on;
         float2 r;
         if (sep) {
             if (!c.on) {
@@ -167,13 +193,11 @@ __device__ __forceinline__ void mix_row(float2 (&v)[16], int role, bool sep, boo
 template <int N> struct EwemShape {
     static constexpr int T = N / 16, NT = 3 * T, PADN = pad16(N);
     static constexpr int TW = fft_tw_size<N>(), TWP = (TW + 1) & ~1;
-    static constexpr int HM = N / 2 + 2;  // phase-table stride (entries <= L/2 + 1)
 };
 
-__host__ __device__ inline size_t ewem_smem_floats2(int N, int TWP, int PADN, int nmx)
+__host__ __device__ inline size_t ewem_smem_floats2(int N, int TWP, int PADN, int L, int nmx)
 {
-    const int nmxp = (nmx + 1) & ~1;
-    return (size_t)TWP + 2 * (size_t)(N / 2 + 2) + 2 * (size_t)nmxp + 3 * (size_t)N + 3 * (size_t)PADN;
+    return (size_t)TWP + (size_t)EwemRec(L, nmx).floats() / 2 + 3 * (size_t)N + 3 * (size_t)PADN;
 }
 
 // The depth recursion of every (shot, frequency) item: ADJ migration, otherwise modelling.
@@ -184,25 +208,29 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
     constexpr int T = SH::T, NT = SH::NT, PADN = SH::PADN;
     const MigArgs &m = a.m;
     const int nmx = m.nmx, nz = m.nz;
-    const int nmxp = (nmx + 1) & ~1;
+    const EwemRec R(a.nkx, nmx);
     extern __shared__ float4 smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
-    float2 *php = tw + SH::TWP, *phs = php + SH::HM;
-    float2 *cp = phs + SH::HM, *cs = cp + nmxp;
-    float2 *specA = cs + nmxp, *specB = specA + N, *srow = specB + N;
+    float *rec = reinterpret_cast<float *>(tw + SH::TWP);
+    const float2 *php = reinterpret_cast<const float2 *>(rec + R.php());
+    const float2 *phs = reinterpret_cast<const float2 *>(rec + R.phs());
+    const float2 *cp = reinterpret_cast<const float2 *>(rec + R.cp());
+    const float2 *cs = reinterpret_cast<const float2 *>(rec + R.cs());
+    const float *sept = rec + R.sep();
+    float2 *specA = reinterpret_cast<float2 *>(rec + R.floats()), *specB = specA + N, *srow = specB + N;
     float2 *xb = srow + N;
     const int tid = threadIdx.x, team = tid / T, t = tid - team * T;
     float2 *xbuf = xb + (size_t)team * PADN;
     const unsigned sync = team_sync_handle<N>(tid);
     for (int i = tid; i < SH::TW; i += NT) tw[i] = a.twid[i];
-    const int HALF = (BLU ? m.nlog : N) / 2 + 1;
-    const int nitems = m.nshot * m.nwf;
+    const int nitems = m.nshot * a.nwc;
+    const int recf4 = R.floats() / 4;
 
     for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int shot = item % m.nshot, iwi = item / m.nshot;
+        const int shot = item % m.nshot, iwc = item / m.nshot, iwi = a.wbase + iwc;
         const int iw = m.ifmin + iwi;
         const float w = __fmul_rn((float)iw, m.dw);
-        const float w2 = __fmul_rn(w, w);
+        const bool w_on = (double)w >= 20.0;
         const float factor = iw == 0 ? 1.f : 2.f;
         const int igx = a.igx[shot];
         float2 v[16];
@@ -217,27 +245,21 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
             }
             v[q] = u;
         }
-        // tables of depth iz for the layer slownesses (all threads)
+        // the record of depth iz (wem_ewem_tables_kernel) into shared memory (all threads)
         auto tables = [&](int iz) {
-            const float pp = a.po_p[iz], ps = a.po_s[iz];
-            const float sp2 = __fmul_rn(pp, pp), ss2 = __fmul_rn(ps, ps);
-            for (int k = tid; k < HALF; k += NT) {
-                const float kx = __fmul_rn(m.dkx, (float)k);
-                php[k] = phase_entry(w2, sp2, kx, m.dz, m.inv_n);
-                phs[k] = phase_entry(w2, ss2, kx, m.dz, m.inv_n);
-            }
-            const float *dp = a.pd_p + (size_t)iz * nmx, *ds = a.pd_s + (size_t)iz * nmx;
-            for (int x = tid; x < nmx; x += NT) {
-                float sn, c;
-                sincosf(__fmul_rn(__fmul_rn(w, dp[x]), m.dz), &sn, &c);
-                cp[x] = make_float2(c, sn);
-                sincosf(__fmul_rn(__fmul_rn(w, ds[x]), m.dz), &sn, &c);
-                cs[x] = make_float2(c, sn);
-            }
+            const float4 *src = reinterpret_cast<const float4 *>(a.tabs + ((size_t)iwc * nz + iz) * R.floats());
+            float4 *dst = reinterpret_cast<float4 *>(rec);
+            for (int i = tid; i < recf4; i += NT) dst[i] = __ldg(src + i);
+        };
+        // the record of the depth after this one towards L2, so that its copy does not wait on DRAM
+        auto prefetch = [&](int iz) {
+            if (iz < 0 || iz >= nz) return;
+            const char *src = reinterpret_cast<const char *>(a.tabs + ((size_t)iwc * nz + iz) * R.floats());
+            for (int o = tid * 128; o < recf4 * 16; o += NT * 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(src + o));
         };
         // the receiver teams' separation or recombination: forward transforms, spectra to
         // shared memory, mixing at each wavenumber, inverse transforms
-        auto mix = [&](bool sep, float vp, float vs) {
+        auto mix = [&](bool sep) {
             if (team > 0) {
                 xform<N, -1, false, BLU>(v, xbuf, tw, t, sync, nullptr, m);
                 float2 *dst = team == 1 ? specA : specB;
@@ -246,7 +268,7 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
             }
             __syncthreads();
             if (team > 0) {
-                mix_row<N, BLU>(v, team - 1, sep, ADJ, specA, specB, w, vp, vs, t, m);
+                mix_row<N, BLU>(v, team - 1, sep, ADJ, specA, specB, w_on, sept, R.lp, t, m);
                 xform<N, +1, false, BLU>(v, xbuf, tw, t, sync, nullptr, m);
 #pragma unroll
                 for (int q = 0; q < 16; q++)
@@ -262,6 +284,7 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
                 const bool src_on = z >= a.sz, rec_on = z >= a.gz;
                 __syncthreads();  // the previous depth's tables, spectra and source row are read
                 tables(iz);
+                prefetch(iz + 1);
                 __syncthreads();
                 if (team == 0) {
                     if (src_on) {
@@ -275,8 +298,7 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
                     }
                 }
                 if (!rec_on) continue;  // CTA-uniform
-                const float vp = a.vp_mean[iz], vs = a.vs_mean[iz];
-                mix(true, vp, vs);  // components -> potentials
+                mix(true);  // components -> potentials
                 if (team > 0)
                     ssop_row<N, BLU>(v, true, false, team == 1 ? php : phs, team == 1 ? cp : cs, a.taper, xbuf, tw, t,
                                      sync, m);
@@ -292,7 +314,7 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
                         }
                     }
                 }
-                mix(false, vp, vs);  // potentials -> components
+                mix(false);  // potentials -> components
             }
         } else {
             float2 *smig = a.smig + (size_t)blockIdx.x * nz * nmx;
@@ -301,6 +323,7 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
                 const float z = __fadd_rn(a.oz, __fmul_rn(m.dz, (float)iz));
                 __syncthreads();
                 tables(iz);
+                prefetch(iz + 1);
                 __syncthreads();
                 if (team == 0) {
                     float2 *row = smig + (size_t)iz * nmx;
@@ -321,9 +344,9 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
                 if (!(z >= a.gz)) continue;  // CTA-uniform
                 __syncthreads();
                 tables(iz);
+                prefetch(iz - 1);
                 __syncthreads();
-                const float vp = a.vp_mean[iz], vs = a.vs_mean[iz];
-                mix(true, vp, vs);
+                mix(true);
                 if (team > 0) {
                     const float2 *row = smig + (size_t)iz * nmx;
                     const float *img = (team == 1 ? a.img_p : a.img_s) + (size_t)iz * nmx;
@@ -341,7 +364,7 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
                                      sync, m);
                 }
                 __syncthreads();  // the spectra of the separation were read
-                mix(false, vp, vs);
+                mix(false);
             }
             if (team > 0) {  // ux_g_wx, uz_g_wx = u / sqrtf(ntfft) (ewem.c:357-361)
                 float2 *out = (team == 1 ? a.dg_x : a.dg_z) + ((size_t)shot * m.nwf + iwi) * nmx;
@@ -359,7 +382,7 @@ template <int N, bool BLU, bool ADJ>
 int ewem_launch_t(const EwemArgs *a, int nsm, int nitems, cudaStream_t st, int *grid_out, size_t *smem_out)
 {
     using SH = EwemShape<N>;
-    const size_t smem = sizeof(float2) * ewem_smem_floats2(N, SH::TWP, SH::PADN, a ? a->m.nmx : 0);
+    const size_t smem = sizeof(float2) * ewem_smem_floats2(N, SH::TWP, SH::PADN, a->nkx, a->m.nmx);
     *smem_out = smem;
     auto k = wem_ewem_kernel<N, BLU, ADJ>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;

@@ -168,36 +168,35 @@ __global__ void __launch_bounds__(256) wem_transpose_kernel(const float *in, int
 }
 
 // ------------------------------------------------------------------ image reduce
-// m[x][iz] = sum over slots of (sum - compensation), compensated, fixed order;
-// 32x32 tiles so that both the [iz][x] reads and the [x][iz] writes coalesce.
+// m[x][iz] = sum over slots of (sum - compensation), compensated, fixed order; one output
+// per thread on tiles of 32 x by 8 z, so that the [iz][x] reads coalesce and enough loads are in
+// flight (16 slots ahead per thread, the additions still in slot order), and the [x][iz] writes
+// go through a transposed shared tile.
 __global__ void __launch_bounds__(256) wem_image_reduce_kernel(const float2 *slots, int nslots, int nz, int nmx,
                                                                float *m)
 {
-    __shared__ float tile[32][33];
-    const int x0 = blockIdx.x * 32, z0 = blockIdx.y * 32;
+    __shared__ float tile[8][33];
+    const int x0 = blockIdx.x * 32, z0 = blockIdx.y * 8;
     const int lx = threadIdx.x & 31, ly = threadIdx.x >> 5;  // 32 x 8
     const size_t plane = (size_t)nz * nmx;
-    for (int j = ly; j < 32; j += 8) {
-        const int iz = z0 + j, x = x0 + lx;
-        float s = 0.f, c = 0.f;
-        if (iz < nz && x < nmx) {
-            const float2 *p = slots + (size_t)iz * nmx + x;
-            for (int q = 0; q < nslots; q++) {
-                const float2 e = p[(size_t)q * plane];
-                const float val = __fsub_rn(e.x, e.y);
-                const float y = __fsub_rn(val, c);
-                const float tt = __fadd_rn(s, y);
-                c = __fsub_rn(__fsub_rn(tt, s), y);
-                s = tt;
-            }
+    const int iz = z0 + ly, x = x0 + lx;
+    float s = 0.f, c = 0.f;
+    if (iz < nz && x < nmx) {
+        const float2 *p = slots + (size_t)iz * nmx + x;
+#pragma unroll 16
+        for (int q = 0; q < nslots; q++) {
+            const float2 e = p[(size_t)q * plane];
+            const float val = __fsub_rn(e.x, e.y);
+            const float y = __fsub_rn(val, c);
+            const float tt = __fadd_rn(s, y);
+            c = __fsub_rn(__fsub_rn(tt, s), y);
+            s = tt;
         }
-        tile[j][lx] = s;
     }
+    tile[ly][lx] = s;
     __syncthreads();
-    for (int j = ly; j < 32; j += 8) {
-        const int x = x0 + j, iz = z0 + lx;
-        if (x < nmx && iz < nz) m[(size_t)x * nz + iz] = tile[lx][j];
-    }
+    const int wx = x0 + (threadIdx.x >> 3), wz = z0 + (threadIdx.x & 7);
+    if (wx < nmx && wz < nz) m[(size_t)wx * nz + wz] = tile[threadIdx.x & 7][threadIdx.x >> 3];
 }
 
 // ------------------------------------------------------------------ host side
@@ -448,7 +447,7 @@ int launch_spectra(const SpectraArgs &a, cudaStream_t st)
 
 int launch_image_reduce(const float2 *slots, int nslots, int nz, int nmx, float *m, cudaStream_t st)
 {
-    dim3 grid((nmx + 31) / 32, (nz + 31) / 32);
+    dim3 grid((nmx + 31) / 32, (nz + 7) / 8);
     wem_image_reduce_kernel<<<grid, 256, 0, st>>>(slots, nslots, nz, nmx, m);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
