@@ -315,6 +315,7 @@ extern "C" WEM_API int wem_elastic(int device, const wem_params *pp, const float
     a.wbase = 0;
     a.nwc = std::min(nwf, chunk);
     const int nitems = nshot * a.nwc;  // the largest sub-band's items size the grid and the scratch
+    const int per_cta = ewem_group(nfft, blu);  // shots per CTA: accumulator and source slots per CTA
     int grid = 0;
     size_t smem = 0;
     if (nitems > 0) {
@@ -324,11 +325,11 @@ extern "C" WEM_API int wem_elastic(int device, const wem_params *pp, const float
         a.tabs = B.get<float>(rec_bytes / sizeof(float) * a.nwc);
         if (!a.tabs) return set_error(WEM_ERR_NOMEM, "wem_elastic: out of device memory");
         if (adj) {
-            a.slots = B.get<float2>(2 * (size_t)grid * nzx);
+            a.slots = B.get<float2>(2 * (size_t)grid * per_cta * nzx);
             if (!a.slots) return set_error(WEM_ERR_NOMEM, "wem_elastic: out of device memory");
-            ECK(cudaMemsetAsync(a.slots, 0, sizeof(float2) * 2 * (size_t)grid * nzx, st));
+            ECK(cudaMemsetAsync(a.slots, 0, sizeof(float2) * 2 * (size_t)grid * per_cta * nzx, st));
         } else {
-            a.smig = B.get<float2>((size_t)grid * nzx);
+            a.smig = B.get<float2>((size_t)grid * per_cta * nzx);
             if (!a.smig) return set_error(WEM_ERR_NOMEM, "wem_elastic: out of device memory");
             ECK(cudaMemsetAsync(d_sx, 0, sizeof(float2) * ntr * nwf, st));
             ECK(cudaMemsetAsync(d_sz, 0, sizeof(float2) * ntr * nwf, st));
@@ -345,8 +346,8 @@ extern "C" WEM_API int wem_elastic(int device, const wem_params *pp, const float
     }
     if (adj) {
         if (nitems > 0) {
-            if (launch_image_reduce(a.slots, grid, nz, nmx, d_mp, st) ||
-                launch_image_reduce(a.slots + (size_t)grid * nzx, grid, nz, nmx, d_ms, st))
+            if (launch_image_reduce(a.slots, grid * per_cta, nz, nmx, d_mp, st) ||
+                launch_image_reduce(a.slots + (size_t)grid * per_cta * nzx, grid * per_cta, nz, nmx, d_ms, st))
                 return set_error(WEM_ERR_CUDA, "wem_elastic: reduce launch");
         } else {
             ECK(cudaMemsetAsync(d_mp, 0, sizeof(float) * nzx, st));

@@ -190,22 +190,36 @@ __device__ __forceinline__ void mix_row(float2 (&v)[16], int role, bool sep, boo
     }
 }
 
-template <int N> struct EwemShape {
-    static constexpr int T = N / 16, NT = 3 * T, PADN = pad16(N);
+// Shots per CTA: three for power-of-two rows up to 1024 points (one source team then advances
+// three source rows while three receiver pairs continue theirs, six transforms each per depth
+// step), else one (the register budget of longer rows and of the chirp form).
+__host__ __device__ constexpr int ewem_group(int N, bool blu) { return (!blu && N <= 1024) ? 3 : 1; }
+
+template <int N, bool BLU> struct EwemShape {
+    static constexpr int T = N / 16, EG = ewem_group(N, BLU), NTEAM = 2 * EG + 1, NT = NTEAM * T;
+    static constexpr int PADN = pad16(N);
     static constexpr int TW = fft_tw_size<N>(), TWP = (TW + 1) & ~1;
+    static constexpr int MINB = (!BLU && NT <= 224) ? 2 : 1;  // CTAs per SM the register budget aims at
 };
 
-__host__ __device__ inline size_t ewem_smem_floats2(int N, int TWP, int PADN, int L, int nmx)
+__host__ __device__ inline size_t ewem_smem_floats2(int N, int EG, int TWP, int PADN, int L, int nmx)
 {
-    return (size_t)TWP + (size_t)EwemRec(L, nmx).floats() / 2 + 3 * (size_t)N + 3 * (size_t)PADN;
+    return (size_t)TWP + (size_t)EwemRec(L, nmx).floats() / 2 + 3 * (size_t)EG * N + (2 * (size_t)EG + 1) * PADN;
 }
 
-// The depth recursion of every (shot, frequency) item: ADJ migration, otherwise modelling.
+// The depth recursion of EG shots of one frequency per CTA: ADJ migration, otherwise modelling.
+// Teams 0..2EG-1 are the receiver pairs (pair j = teams 2j, 2j+1: the x / P and z / S2 rows of
+// shot j of the group; warp-aligned, so a pair synchronises on its own), team 2EG the source.
+// In migration the source team keeps the EG source rows in shared memory (srow_j) and continues
+// them one after the other at every depth step, while each receiver pair separates, continues and
+// recombines its rows; the images of shot j go to accumulator slot (CTA, j). In modelling the
+// first EG teams take one source row each down through every depth (smig of slot (CTA, j)), then
+// the receiver pairs go up.
 template <int N, bool BLU, bool ADJ>
-__global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArgs a)
+__global__ void __launch_bounds__(EwemShape<N, BLU>::NT, EwemShape<N, BLU>::MINB) wem_ewem_kernel(const EwemArgs a)
 {
-    using SH = EwemShape<N>;
-    constexpr int T = SH::T, NT = SH::NT, PADN = SH::PADN;
+    using SH = EwemShape<N, BLU>;
+    constexpr int T = SH::T, NT = SH::NT, PADN = SH::PADN, EG = SH::EG, SRC = 2 * EG;
     const MigArgs &m = a.m;
     const int nmx = m.nmx, nz = m.nz;
     const EwemRec R(a.nkx, nmx);
@@ -217,115 +231,140 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
     const float2 *cp = reinterpret_cast<const float2 *>(rec + R.cp());
     const float2 *cs = reinterpret_cast<const float2 *>(rec + R.cs());
     const float *sept = rec + R.sep();
-    float2 *specA = reinterpret_cast<float2 *>(rec + R.floats()), *specB = specA + N, *srow = specB + N;
-    float2 *xb = srow + N;
+    float2 *rows = reinterpret_cast<float2 *>(rec + R.floats());  // per shot j: specA, specB, srow
+    float2 *xb = rows + 3 * EG * N;
     const int tid = threadIdx.x, team = tid / T, t = tid - team * T;
+    const int pair = team >> 1, role = team & 1;  // receiver teams
     float2 *xbuf = xb + (size_t)team * PADN;
     const unsigned sync = team_sync_handle<N>(tid);
     for (int i = tid; i < SH::TW; i += NT) tw[i] = a.twid[i];
-    const int nitems = m.nshot * a.nwc;
+    const int nsb = (m.nshot + EG - 1) / EG;  // shot blocks per frequency
+    const int ngroups = nsb * a.nwc;
     const int recf4 = R.floats() / 4;
 
-    for (int item = blockIdx.x; item < nitems; item += gridDim.x) {
-        const int shot = item % m.nshot, iwc = item / m.nshot, iwi = a.wbase + iwc;
+    for (int g = blockIdx.x; g < ngroups; g += gridDim.x) {
+        const int iwc = g / nsb, sb = g % nsb, iwi = a.wbase + iwc;
         const int iw = m.ifmin + iwi;
         const float w = __fmul_rn((float)iw, m.dw);
         const bool w_on = (double)w >= 20.0;
         const float factor = iw == 0 ? 1.f : 2.f;
-        const int igx = a.igx[shot];
-        float2 v[16];
-        // the row this team carries: the source spike, or the receiver's ux / uz spectra
-#pragma unroll
-        for (int q = 0; q < 16; q++) {
-            const int x = t + T * q;
-            float2 u = make_float2(0.f, 0.f);
-            if (x < nmx) {
-                if (team == 0) u = x == igx ? a.srcw[iwi] : u;
-                else if (ADJ) u = (team == 1 ? a.recv_x : a.recv_z)[((size_t)shot * m.nwf + iwi) * nmx + x];
-            }
-            v[q] = u;
-        }
-        // the record of depth iz (wem_ewem_tables_kernel) into shared memory (all threads)
-        auto tables = [&](int iz) {
+        // the receiver pair's shot (teams below SRC)
+        const int jj = team < SRC ? pair : 0;
+        const int shot = sb * EG + jj;
+        const bool valid = team < SRC && shot < m.nshot;
+        float2 *specA = rows + (size_t)3 * jj * N, *specB = specA + N, *srow = specB + N;
+
+        auto tables = [&](int iz) {  // the record of depth iz into shared memory (all threads)
             const float4 *src = reinterpret_cast<const float4 *>(a.tabs + ((size_t)iwc * nz + iz) * R.floats());
             float4 *dst = reinterpret_cast<float4 *>(rec);
             for (int i = tid; i < recf4; i += NT) dst[i] = __ldg(src + i);
         };
-        // the record of the depth after this one towards L2, so that its copy does not wait on DRAM
+        // the record of the next depth towards L2, so that its copy does not wait on DRAM
         auto prefetch = [&](int iz) {
             if (iz < 0 || iz >= nz) return;
             const char *src = reinterpret_cast<const char *>(a.tabs + ((size_t)iwc * nz + iz) * R.floats());
             for (int o = tid * 128; o < recf4 * 16; o += NT * 128) asm volatile("prefetch.global.L2 [%0];" ::"l"(src + o));
         };
-        // the receiver teams' separation or recombination: forward transforms, spectra to
-        // shared memory, mixing at each wavenumber, inverse transforms
-        auto mix = [&](bool sep) {
-            if (team > 0) {
-                xform<N, -1, false, BLU>(v, xbuf, tw, t, sync, nullptr, m);
-                float2 *dst = team == 1 ? specA : specB;
+        // a receiver pair's separation or recombination: forward transforms, spectra to shared
+        // memory, mixing at each wavenumber, inverse transforms
+        auto mix = [&](float2 (&v)[16], bool sep) {
+            xform<N, -1, false, BLU>(v, xbuf, tw, t, sync, nullptr, m);
+            float2 *dst = role == 0 ? specA : specB;
 #pragma unroll
-                for (int q = 0; q < 16; q++) dst[t + T * q] = v[q];
-            }
-            __syncthreads();
-            if (team > 0) {
-                mix_row<N, BLU>(v, team - 1, sep, ADJ, specA, specB, w_on, sept, R.lp, t, m);
-                xform<N, +1, false, BLU>(v, xbuf, tw, t, sync, nullptr, m);
+            for (int q = 0; q < 16; q++) dst[t + T * q] = v[q];
+            team_pair_sync<N>(pair, tid);
+            mix_row<N, BLU>(v, role, sep, ADJ, specA, specB, w_on, sept, R.lp, t, m);
+            xform<N, +1, false, BLU>(v, xbuf, tw, t, sync, nullptr, m);
 #pragma unroll
-                for (int q = 0; q < 16; q++)
-                    if (t + T * q >= nmx) v[q] = make_float2(0.f, 0.f);
-            }
+            for (int q = 0; q < 16; q++)
+                if (t + T * q >= nmx) v[q] = make_float2(0.f, 0.f);
         };
 
+        __syncthreads();  // the previous group's rows and spectra are read
+        float2 v[16];
         if (ADJ) {
-            float2 *slot_p = a.slots + (size_t)blockIdx.x * nz * nmx;
-            float2 *slot_s = a.slots + ((size_t)gridDim.x + blockIdx.x) * nz * nmx;
+            if (team == SRC) {  // the source spikes of the group's shots
+                for (int j = 0; j < EG; j++) {
+                    const int sj = sb * EG + j;
+                    if (sj >= m.nshot) break;
+                    const int igx = a.igx[sj];
+                    float2 *sr = rows + (size_t)(3 * j + 2) * N;
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {
+                        const int x = t + T * q;
+                        sr[x] = (x == igx && x < nmx) ? a.srcw[iwi] : make_float2(0.f, 0.f);
+                    }
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+                const int x = t + T * q;
+                v[q] = (valid && x < nmx) ? (role == 0 ? a.recv_x : a.recv_z)[((size_t)shot * m.nwf + iwi) * nmx + x]
+                                          : make_float2(0.f, 0.f);
+            }
+            const size_t nzx = (size_t)nz * nmx;
+            float2 *slot = a.slots + ((size_t)role * gridDim.x * EG + (size_t)blockIdx.x * EG + jj) * nzx;
             for (int iz = 0; iz < nz; iz++) {
                 const float z = __fadd_rn(a.oz, __fmul_rn(m.dz, (float)iz));
                 const bool src_on = z >= a.sz, rec_on = z >= a.gz;
-                __syncthreads();  // the previous depth's tables, spectra and source row are read
+                __syncthreads();  // the previous depth's tables, spectra and source rows are read
                 tables(iz);
                 prefetch(iz + 1);
                 __syncthreads();
-                if (team == 0) {
+                if (team == SRC) {
                     if (src_on) {
-                        ssop_row<N, BLU>(v, true, true, php, cp, a.taper, xbuf, tw, t, sync, m);
+                        for (int j = 0; j < EG; j++) {
+                            if (sb * EG + j >= m.nshot) break;
+                            float2 *sr = rows + (size_t)(3 * j + 2) * N;
 #pragma unroll
-                        for (int q = 0; q < 16; q++)
-                            srow[t + T * q] = make_float2(v[q].x * a.inv_max_source, v[q].y * a.inv_max_source);
-                    } else {
+                            for (int q = 0; q < 16; q++) v[q] = sr[t + T * q];
+                            ssop_row<N, BLU>(v, true, true, php, cp, a.taper, xbuf, tw, t, sync, m);
 #pragma unroll
-                        for (int q = 0; q < 16; q++) srow[t + T * q] = make_float2(0.f, 0.f);
+                            for (int q = 0; q < 16; q++) sr[t + T * q] = v[q];
+                        }
                     }
+                } else if (valid && rec_on) {
+                    mix(v, true);  // components -> potentials
+                    ssop_row<N, BLU>(v, true, false, role == 0 ? php : phs, role == 0 ? cp : cs, a.taper, xbuf, tw, t,
+                                     sync, m);
                 }
                 if (!rec_on) continue;  // CTA-uniform
-                mix(true);  // components -> potentials
-                if (team > 0)
-                    ssop_row<N, BLU>(v, true, false, team == 1 ? php : phs, team == 1 ? cp : cs, a.taper, xbuf, tw, t,
-                                     sync, m);
-                __syncthreads();  // the source row is in srow; the spectra were read
-                if (team > 0) {
-                    float2 *slot = (team == 1 ? slot_p : slot_s) + (size_t)iz * nmx;
+                __syncthreads();  // the source rows are continued; the spectra were read
+                if (valid) {
+                    float2 *acc = slot + (size_t)iz * nmx;
 #pragma unroll
                     for (int q = 0; q < 16; q++) {
                         const int x = t + T * q;
                         if (x < nmx) {
-                            const float2 s_ = srow[x];
-                            kahan_add(&slot[x], factor * (s_.x * v[q].x + s_.y * v[q].y));  // Re(conj(smig) u)
+                            const float2 s0 = srow[x];
+                            const float2 s_ = src_on ? make_float2(s0.x * a.inv_max_source, s0.y * a.inv_max_source)
+                                                     : make_float2(0.f, 0.f);
+                            kahan_add(&acc[x], factor * (s_.x * v[q].x + s_.y * v[q].y));  // Re(conj(smig) u)
                         }
                     }
+                    mix(v, false);  // potentials -> components
                 }
-                mix(false);  // potentials -> components
             }
         } else {
-            float2 *smig = a.smig + (size_t)blockIdx.x * nz * nmx;
-            // source, downward, every depth kept
+            // source, downward, every depth kept: team j < EG takes the group's shot j
+            const int sj = sb * EG + team;
+            const bool sv = team < EG && sj < m.nshot;
+            float2 *smig = a.smig + ((size_t)blockIdx.x * EG + (team < EG ? team : 0)) * nz * nmx;
+            {
+                const int igx = sv ? a.igx[sj] : -1;
+#pragma unroll
+                for (int q = 0; q < 16; q++) {
+                    const int x = t + T * q;
+                    v[q] = (x == igx && x < nmx) ? a.srcw[iwi] : make_float2(0.f, 0.f);
+                }
+            }
             for (int iz = 0; iz < nz; iz++) {
                 const float z = __fadd_rn(a.oz, __fmul_rn(m.dz, (float)iz));
                 __syncthreads();
                 tables(iz);
                 prefetch(iz + 1);
                 __syncthreads();
-                if (team == 0) {
+                if (sv) {
                     float2 *row = smig + (size_t)iz * nmx;
                     if (z >= a.sz) ssop_row<N, BLU>(v, true, true, php, cp, a.taper, xbuf, tw, t, sync, m);
 #pragma unroll
@@ -337,8 +376,11 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
                     }
                 }
             }
-            __syncthreads();  // smig written by team 0 is read by the receiver teams below
+            __syncthreads();  // smig written by the source teams is read by the receiver pairs below
             // receiver, upward with the images injected
+            const float2 *smr = a.smig + ((size_t)blockIdx.x * EG + jj) * nz * nmx;
+#pragma unroll
+            for (int q = 0; q < 16; q++) v[q] = make_float2(0.f, 0.f);
             for (int iz = nz - 1; iz >= 0; iz--) {
                 const float z = __fadd_rn(a.oz, __fmul_rn(m.dz, (float)iz));
                 if (!(z >= a.gz)) continue;  // CTA-uniform
@@ -346,10 +388,10 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
                 tables(iz);
                 prefetch(iz - 1);
                 __syncthreads();
-                mix(true);
-                if (team > 0) {
-                    const float2 *row = smig + (size_t)iz * nmx;
-                    const float *img = (team == 1 ? a.img_p : a.img_s) + (size_t)iz * nmx;
+                if (valid) {
+                    mix(v, true);
+                    const float2 *row = smr + (size_t)iz * nmx;
+                    const float *img = (role == 0 ? a.img_p : a.img_s) + (size_t)iz * nmx;
 #pragma unroll
                     for (int q = 0; q < 16; q++) {
                         const int x = t + T * q;
@@ -360,14 +402,14 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
                             v[q].y += s_.y * mv;
                         }
                     }
-                    ssop_row<N, BLU>(v, false, true, team == 1 ? php : phs, team == 1 ? cp : cs, a.taper, xbuf, tw, t,
+                    ssop_row<N, BLU>(v, false, true, role == 0 ? php : phs, role == 0 ? cp : cs, a.taper, xbuf, tw, t,
                                      sync, m);
+                    team_pair_sync<N>(pair, tid);  // the spectra of the separation were read
+                    mix(v, false);
                 }
-                __syncthreads();  // the spectra of the separation were read
-                mix(false);
             }
-            if (team > 0) {  // ux_g_wx, uz_g_wx = u / sqrtf(ntfft) (ewem.c:357-361)
-                float2 *out = (team == 1 ? a.dg_x : a.dg_z) + ((size_t)shot * m.nwf + iwi) * nmx;
+            if (valid) {  // ux_g_wx, uz_g_wx = u / sqrtf(ntfft) (ewem.c:357-361)
+                float2 *out = (role == 0 ? a.dg_x : a.dg_z) + ((size_t)shot * m.nwf + iwi) * nmx;
 #pragma unroll
                 for (int q = 0; q < 16; q++) {
                     const int x = t + T * q;
@@ -381,15 +423,17 @@ __global__ void __launch_bounds__(3 * (N / 16), 1) wem_ewem_kernel(const EwemArg
 template <int N, bool BLU, bool ADJ>
 int ewem_launch_t(const EwemArgs *a, int nsm, int nitems, cudaStream_t st, int *grid_out, size_t *smem_out)
 {
-    using SH = EwemShape<N>;
-    const size_t smem = sizeof(float2) * ewem_smem_floats2(N, SH::TWP, SH::PADN, a->nkx, a->m.nmx);
+    using SH = EwemShape<N, BLU>;
+    const size_t smem = sizeof(float2) * ewem_smem_floats2(N, SH::EG, SH::TWP, SH::PADN, a->nkx, a->m.nmx);
     *smem_out = smem;
     auto k = wem_ewem_kernel<N, BLU, ADJ>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
     int bps = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, SH::NT, smem) != cudaSuccess || bps < 1) return -1;
     const long long cap = (long long)nsm * bps;
-    const int grid = (int)std::max<long long>(1, std::min<long long>(cap, nitems));
+    const long long ngroups = (long long)a->nwc * ((a->m.nshot + SH::EG - 1) / SH::EG);
+    (void)nitems;
+    const int grid = (int)std::max<long long>(1, std::min<long long>(cap, ngroups));
     *grid_out = grid;
     if (!a->slots && !a->smig) return 0;  // sizing only
     k<<<grid, SH::NT, smem, st>>>(*a);
