@@ -383,11 +383,39 @@ def executed_flops_per_unit(p: dict, vel, paired: bool) -> tuple[float, float, f
     return 2 * F + 3 * nmx, x, r_used
 
 
-def cpu_baseline(c, nsample: int = 4, which=None):
+def accuracy_sample(c: dict, kept: dict, ctx_factory) -> dict:
+    """Relative L2 image error of the GPU migration against the CPU leg's own image (the
+    reference's FP32 arithmetic, the port bit-identical to the compiled reference) on the
+    CPU leg's shots and band: for the 3-D survey, whose FP64 oracle would take minutes more."""
+    from wemgpu.api import Shots
+    shots, which = c["shots"], kept["which"]
+    offs, cells, data = [0], [], []
+    for s in which:
+        lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
+        cells.append(shots.trace_cell[lo:hi])
+        data.append(shots.data[lo:hi])
+        offs.append(offs[-1] + hi - lo)
+    sub = Shots(shots.sx[which], shots.sy[which], np.asarray(offs, np.int64), np.concatenate(cells),
+                np.concatenate(data))
+    q = {k_: v for k_, v in kept["params"].items() if k_ != "precision"}
+    ctx = ctx_factory()
+    try:
+        m = ctx.prepare(q, c["vel"], c["wav"]).migrate(sub).astype(np.float64)
+    finally:
+        ctx.close()
+    ref = kept["image"]
+    return {"sample": f"the CPU leg's shots {which}, {band(q)} frequencies ({q['fmin']:g}-{q['fmax']:g} Hz) x "
+                      f"{q['nz']} depth steps",
+            "oracle": "the port of the reference's C (its FP32 arithmetic)",
+            "rel_l2_fp32_vs_reference_fp32": float(np.linalg.norm(m - ref) / np.linalg.norm(ref))}
+
+
+def cpu_baseline(c, nsample: int = 4, which=None, keep=None):
     """The reference's CPU algorithm on `nsample` evenly spaced shots of the survey (every
     frequency; about 20-25 s on the GPU host's cores), all host cores, one shot at a time as
     the Julia wrapper calls it. oracle/_ref (the reference's own C core) when it was built
-    on this machine, else the oracle port of it. `which` picks the shots instead."""
+    on this machine, else the oracle port of it. `which` picks the shots instead. `keep`, a
+    dict, receives the stacked CPU image, the parameters and the shots it was made with."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from wemgpu import synth
@@ -404,16 +432,21 @@ def cpu_baseline(c, nsample: int = 4, which=None):
         # (the band edge is (int)fmax, wem.c:86), about one per host core
         p["fmax"] = float(p["fmin"]) + 2.0
     dt = 0.0
+    img = None
     for s in which:
         q = dict(p, sx=float(shots.sx[s]))
         d = synth.shot_gather_full(shots, s, int(p["nmx"]) * int(p.get("nmy", 1)))
         t0 = time.perf_counter()
         if kind == "reference":
-            O.wem_ref(q, c["vel"], c["wav"], d=d, adj=True)
+            m = O.wem_ref(q, c["vel"], c["wav"], d=d, adj=True)
             cores = O.omp_threads()
         else:
-            O.wem_port(q, c["vel"], c["wav"], d=d, adj=True, nthreads=cores)
+            m = O.wem_port(q, c["vel"], c["wav"], d=d, adj=True, nthreads=cores)
         dt += time.perf_counter() - t0
+        if keep is not None:
+            img = np.asarray(m, np.float64) if img is None else img + m
+    if keep is not None:
+        keep.update(image=img, params=p, which=list(which))
     units = len(which) * band(p) * int(p["nz"])
     return {"value": units / dt, "unit": "shot*omega*depth-steps/s", "cores": cores, "kind": kind,
             "sample": f"shots {which} of {shots.nshot}, {band(p)} of {nf_all} frequencies x {p['nz']} depth steps "
@@ -907,9 +940,13 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # the CPU leg: the reference's algorithm timed on the host cores, and the FP64
         # oracle as the checker of the image error
-        line["cpu_baseline"] = cpu_baseline(c)
-        if not args.no_accuracy and int(p.get("nmy", 1)) == 1:
-            line["accuracy"] = accuracy(c, lambda: wemgpu.Context(local))
+        kept = {}
+        line["cpu_baseline"] = cpu_baseline(c, keep=kept)
+        if not args.no_accuracy:
+            if int(p.get("nmy", 1)) == 1:
+                line["accuracy"] = accuracy(c, lambda: wemgpu.Context(local))
+            else:
+                line["accuracy"] = accuracy_sample(c, kept, lambda: wemgpu.Context(local))
     if rank == 0:
         print(json.dumps(line))
     ctx.close()
