@@ -102,7 +102,7 @@ def born_data_port_shot(c: dict) -> dict:
     m = synth.random_reflectivity(nmx * 7919 + nz, nmx, nz)
     data = shots.data.copy()
     for s in cpu_sample_shots(shots.nshot):
-        full = O.wem_port(dict(p, sx=float(shots.sx[s])), c["vel"], c["wav"], m=m, adj=False,
+        full = O.wem_port(dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s])), c["vel"], c["wav"], m=m, adj=False,
                           nthreads=os.cpu_count() or 1)
         lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
         data[lo:hi] = full[shots.trace_cell[lo:hi]]
@@ -233,7 +233,7 @@ def accuracy(c: dict, ctx_factory, nsample: int = 4) -> dict:
     t0 = time.perf_counter()
     for s in which:
         d = synth.shot_gather_full(shots, s, ncell)
-        qs = dict(q, sx=float(shots.sx[s]))
+        qs = dict(q, sx=float(shots.sx[s]), sy=float(shots.sy[s]))
         w = O.wem_fp64(qs, c["vel"], c["wav"], d=d, adj=True, nthreads=cores).astype(np.float64)
         r = O.wem_port(qs, c["vel"], c["wav"], d=d, adj=True, nthreads=cores).astype(np.float64)
         want = w if want is None else want + w
@@ -434,7 +434,7 @@ def cpu_baseline(c, nsample: int = 4, which=None, keep=None):
     dt = 0.0
     img = None
     for s in which:
-        q = dict(p, sx=float(shots.sx[s]))
+        q = dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s]))
         d = synth.shot_gather_full(shots, s, int(p["nmx"]) * int(p.get("nmy", 1)))
         t0 = time.perf_counter()
         if kind == "reference":

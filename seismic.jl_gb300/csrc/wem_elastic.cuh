@@ -35,6 +35,7 @@ struct EwemArgs {
     // one record of EwemRec::floats floats per (frequency - wbase, depth), frequency-major
     float *tabs;
     int wbase, nwc;
+    int dbuf;  // two record buffers in shared memory: the next depth's copy overlaps this depth
 };
 
 // Layout of one table record, in floats, every part a multiple of 16 bytes:
@@ -202,9 +203,15 @@ template <int N, bool BLU> struct EwemShape {
     static constexpr int MINB = (!BLU && NT <= 224) ? 2 : 1;  // CTAs per SM the register budget aims at
 };
 
-__host__ __device__ inline size_t ewem_smem_floats2(int N, int EG, int TWP, int PADN, int L, int nmx)
+__host__ __device__ inline size_t ewem_smem_floats2(int N, int EG, int TWP, int PADN, int L, int nmx, int dbuf)
 {
-    return (size_t)TWP + (size_t)EwemRec(L, nmx).floats() / 2 + 3 * (size_t)EG * N + (2 * (size_t)EG + 1) * PADN;
+    return (size_t)TWP + (size_t)(dbuf ? 2 : 1) * EwemRec(L, nmx).floats() / 2 + 3 * (size_t)EG * N +
+           (2 * (size_t)EG + 1) * PADN;
+}
+
+__device__ __forceinline__ void cp_async_wait_newest_pending()
+{
+    asm volatile("cp.async.wait_group 1;" ::: "memory");
 }
 
 // The depth recursion of EG shots of one frequency per CTA: ADJ migration, otherwise modelling.
@@ -225,13 +232,18 @@ __global__ void __launch_bounds__(EwemShape<N, BLU>::NT, EwemShape<N, BLU>::MINB
     const EwemRec R(a.nkx, nmx);
     extern __shared__ float4 smem_raw[];
     float2 *tw = reinterpret_cast<float2 *>(smem_raw);
-    float *rec = reinterpret_cast<float *>(tw + SH::TWP);
-    const float2 *php = reinterpret_cast<const float2 *>(rec + R.php());
-    const float2 *phs = reinterpret_cast<const float2 *>(rec + R.phs());
-    const float2 *cp = reinterpret_cast<const float2 *>(rec + R.cp());
-    const float2 *cs = reinterpret_cast<const float2 *>(rec + R.cs());
-    const float *sept = rec + R.sep();
-    float2 *rows = reinterpret_cast<float2 *>(rec + R.floats());  // per shot j: specA, specB, srow
+    float *rec0 = reinterpret_cast<float *>(tw + SH::TWP);  // record buffer(s): depth iz in buffer iz & 1
+    const float2 *php, *phs, *cp, *cs;
+    const float *sept;
+    auto use_record = [&](int iz) {
+        const float *rec = rec0 + (a.dbuf ? (iz & 1) * R.floats() : 0);
+        php = reinterpret_cast<const float2 *>(rec + R.php());
+        phs = reinterpret_cast<const float2 *>(rec + R.phs());
+        cp = reinterpret_cast<const float2 *>(rec + R.cp());
+        cs = reinterpret_cast<const float2 *>(rec + R.cs());
+        sept = rec + R.sep();
+    };
+    float2 *rows = reinterpret_cast<float2 *>(rec0 + (a.dbuf ? 2 : 1) * R.floats());  // per shot j: specA, specB, srow
     float2 *xb = rows + 3 * EG * N;
     const int tid = threadIdx.x, team = tid / T, t = tid - team * T;
     const int pair = team >> 1, role = team & 1;  // receiver teams
@@ -254,10 +266,30 @@ __global__ void __launch_bounds__(EwemShape<N, BLU>::NT, EwemShape<N, BLU>::MINB
         const bool valid = team < SRC && shot < m.nshot;
         float2 *specA = rows + (size_t)3 * jj * N, *specB = specA + N, *srow = specB + N;
 
-        auto tables = [&](int iz) {  // the record of depth iz into shared memory (all threads)
-            const float4 *src = reinterpret_cast<const float4 *>(a.tabs + ((size_t)iwc * nz + iz) * R.floats());
-            float4 *dst = reinterpret_cast<float4 *>(rec);
-            for (int i = tid; i < recf4; i += NT) dst[i] = __ldg(src + i);
+        // The record of depth iz into shared memory (all threads). Double-buffered: issue(next)
+        // starts the asynchronous copy of the next depth's record into the other buffer (a
+        // commit group per call, empty when there is none), ready(iz) waits for every group
+        // but that newest one; the callers' barriers before and after order the buffers.
+        // Single buffer: ready(iz) copies synchronously.
+        auto issue = [&](int iz) {
+            if (a.dbuf) {
+                if (iz >= 0 && iz < nz) {
+                    const float4 *src = reinterpret_cast<const float4 *>(a.tabs + ((size_t)iwc * nz + iz) * R.floats());
+                    float4 *dst = reinterpret_cast<float4 *>(rec0 + (iz & 1) * R.floats());
+                    for (int i = tid; i < recf4; i += NT) cp_async16(dst + i, src + i);
+                }
+                cp_async_commit();
+            }
+        };
+        auto ready = [&](int iz) {
+            if (a.dbuf) {
+                cp_async_wait_newest_pending();
+            } else {
+                const float4 *src = reinterpret_cast<const float4 *>(a.tabs + ((size_t)iwc * nz + iz) * R.floats());
+                float4 *dst = reinterpret_cast<float4 *>(rec0);
+                for (int i = tid; i < recf4; i += NT) dst[i] = __ldg(src + i);
+            }
+            use_record(iz);
         };
         // the record of the next depth towards L2, so that its copy does not wait on DRAM
         auto prefetch = [&](int iz) {
@@ -304,12 +336,14 @@ __global__ void __launch_bounds__(EwemShape<N, BLU>::NT, EwemShape<N, BLU>::MINB
             }
             const size_t nzx = (size_t)nz * nmx;
             float2 *slot = a.slots + ((size_t)role * gridDim.x * EG + (size_t)blockIdx.x * EG + jj) * nzx;
+            issue(0);
             for (int iz = 0; iz < nz; iz++) {
                 const float z = __fadd_rn(a.oz, __fmul_rn(m.dz, (float)iz));
                 const bool src_on = z >= a.sz, rec_on = z >= a.gz;
                 __syncthreads();  // the previous depth's tables, spectra and source rows are read
-                tables(iz);
-                prefetch(iz + 1);
+                issue(iz + 1);
+                ready(iz);
+                prefetch(iz + 2);
                 __syncthreads();
                 if (team == SRC) {
                     if (src_on) {
@@ -358,11 +392,13 @@ __global__ void __launch_bounds__(EwemShape<N, BLU>::NT, EwemShape<N, BLU>::MINB
                     v[q] = (x == igx && x < nmx) ? a.srcw[iwi] : make_float2(0.f, 0.f);
                 }
             }
+            issue(0);
             for (int iz = 0; iz < nz; iz++) {
                 const float z = __fadd_rn(a.oz, __fmul_rn(m.dz, (float)iz));
                 __syncthreads();
-                tables(iz);
-                prefetch(iz + 1);
+                issue(iz + 1);
+                ready(iz);
+                prefetch(iz + 2);
                 __syncthreads();
                 if (sv) {
                     float2 *row = smig + (size_t)iz * nmx;
@@ -381,12 +417,16 @@ __global__ void __launch_bounds__(EwemShape<N, BLU>::NT, EwemShape<N, BLU>::MINB
             const float2 *smr = a.smig + ((size_t)blockIdx.x * EG + jj) * nz * nmx;
 #pragma unroll
             for (int q = 0; q < 16; q++) v[q] = make_float2(0.f, 0.f);
-            for (int iz = nz - 1; iz >= 0; iz--) {
-                const float z = __fadd_rn(a.oz, __fmul_rn(m.dz, (float)iz));
-                if (!(z >= a.gz)) continue;  // CTA-uniform
+            // the receiver's depths: z >= gz, the deepest ones (z grows with iz)
+            int iz_lo = nz;
+            while (iz_lo > 0 && __fadd_rn(a.oz, __fmul_rn(m.dz, (float)(iz_lo - 1))) >= a.gz) iz_lo--;
+            if (a.dbuf) cp_async_wait_all();  // the source pass's last (empty) group
+            issue(nz - 1 >= iz_lo ? nz - 1 : -1);
+            for (int iz = nz - 1; iz >= iz_lo; iz--) {
                 __syncthreads();
-                tables(iz);
-                prefetch(iz - 1);
+                issue(iz - 1 >= iz_lo ? iz - 1 : -1);
+                ready(iz);
+                prefetch(iz - 2 >= iz_lo ? iz - 2 : -1);
                 __syncthreads();
                 if (valid) {
                     mix(v, true);
@@ -424,19 +464,40 @@ template <int N, bool BLU, bool ADJ>
 int ewem_launch_t(const EwemArgs *a, int nsm, int nitems, cudaStream_t st, int *grid_out, size_t *smem_out)
 {
     using SH = EwemShape<N, BLU>;
-    const size_t smem = sizeof(float2) * ewem_smem_floats2(N, SH::EG, SH::TWP, SH::PADN, a->nkx, a->m.nmx);
-    *smem_out = smem;
     auto k = wem_ewem_kernel<N, BLU, ADJ>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
-    int bps = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, SH::NT, smem) != cudaSuccess || bps < 1) return -1;
+    // double-buffered records where the second buffer keeps the CTAs per SM of a single one
+    int bps = 0, dbuf = 0;
+    size_t smem = 0;
+    for (int db = 1; db >= 0; db--) {
+        const size_t sz = sizeof(float2) * ewem_smem_floats2(N, SH::EG, SH::TWP, SH::PADN, a->nkx, a->m.nmx, db);
+        int b = 0;
+        if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sz) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, SH::NT, sz) != cudaSuccess) {
+            b = 0;
+            (void)cudaGetLastError();  // a size above the opt-in limit: not an error of the launch
+        }
+        if (db == 1) {
+            bps = b;
+            smem = sz;
+            dbuf = 1;
+        } else if (b > bps || bps < 1) {
+            bps = b;
+            smem = sz;
+            dbuf = 0;
+        }
+    }
+    if (bps < 1 || cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return -1;
+    *smem_out = smem;
     const long long cap = (long long)nsm * bps;
     const long long ngroups = (long long)a->nwc * ((a->m.nshot + SH::EG - 1) / SH::EG);
     (void)nitems;
     const int grid = (int)std::max<long long>(1, std::min<long long>(cap, ngroups));
     *grid_out = grid;
     if (!a->slots && !a->smig) return 0;  // sizing only
-    k<<<grid, SH::NT, smem, st>>>(*a);
+    EwemArgs b = *a;
+    b.dbuf = dbuf;
+    k<<<grid, SH::NT, smem, st>>>(b);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -36,7 +36,7 @@ def test_batched_modelling_matches_port(gpu_lib, oracle_mod, pspi, interp, nx):
         d = ctx.prepare(p, c["vel"], c["wav"]).model(shots, m, exact=False)
     for s in range(shots.nshot):
         lo, hi = shots.trace_offset[s], shots.trace_offset[s + 1]
-        want = oracle_mod.wem_port(dict(p, sx=float(shots.sx[s])), c["vel"], c["wav"], m=m, adj=False)
+        want = oracle_mod.wem_port(dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s])), c["vel"], c["wav"], m=m, adj=False)
         assert rel_l2(d[lo:hi], want[shots.trace_cell[lo:hi]]) < TOL
 
 
@@ -129,7 +129,7 @@ def test_misfit_curve_matches_reference_operator_pair(gpu_lib, oracle_mod):
         out = []
         for s in range(shots.nshot):
             lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
-            full = oracle_mod.wem_port(dict(p, sx=float(shots.sx[s])), c["vel"], c["wav"], m=m, adj=False)
+            full = oracle_mod.wem_port(dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s])), c["vel"], c["wav"], m=m, adj=False)
             out.append(full[shots.trace_cell[lo:hi]])
         return np.concatenate(out).astype(np.float64)
 
@@ -139,7 +139,7 @@ def test_misfit_curve_matches_reference_operator_pair(gpu_lib, oracle_mod):
             lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
             g = np.zeros((p["nmx"], p["nt"]), np.float32)
             g[shots.trace_cell[lo:hi]] = d[lo:hi]
-            img += oracle_mod.wem_port(dict(p, sx=float(shots.sx[s])), c["vel"], c["wav"], d=g, adj=True)
+            img += oracle_mod.wem_port(dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s])), c["vel"], c["wav"], d=g, adj=True)
         return img
 
     rng = np.random.default_rng(14)

@@ -57,13 +57,15 @@ def test_ewem_dropin_matches_reference_golden(gpu_lib):
     assert rel_l2(mpp, g["mpp_ref"]) < TOL and rel_l2(mps2, g["mps2_ref"]) < TOL and not np.any(mps1)
 
 
-@pytest.mark.parametrize("nx,padx", [(128, 2), (500, 2), (256, 1)])
-def test_elastic_shots_stacked_match_fp64_oracle(gpu_lib, nx, padx):
+@pytest.mark.parametrize("nx,padx,nshot", [(128, 2, 3), (500, 2, 3), (256, 1, 3), (512, 2, 4), (64, 1, 5)])
+def test_elastic_shots_stacked_match_fp64_oracle(gpu_lib, nx, padx, nshot):
     """Several shots in one call (the images stacked over the shots) against the FP64
-    restatement shot by shot; nx 500 with padx 2 runs rows of nkx 1000 (Bluestein's form)."""
+    restatement shot by shot. nx 500 with padx 2 runs rows of nkx 1000 (Bluestein's form, one
+    shot per CTA); the power-of-two rows carry three shots of a frequency per CTA, so 4 and 5
+    shots leave a group part-filled (1024-point rows; 64-point rows with teams of 4 threads)."""
     import ewem_np as E
     from wemgpu import synth
-    c = synth.small_case(70 + nx, nx=nx, nz=10, nt=128, nshot=3, pspi=0, fmax=30.0, padx=padx)
+    c = synth.small_case(70 + nx, nx=nx, nz=10, nt=128, nshot=nshot, pspi=0, fmax=30.0, padx=padx)
     rng = np.random.default_rng(nx)
     vp = c["vel"]
     vs = (vp / 1.7 * (1.0 + 0.05 * rng.standard_normal(vp.shape))).astype(np.float32)

@@ -32,7 +32,7 @@ def _port_stack(oracle_mod, p, vel, wav, shots, fp64=False):
     op = oracle_mod.wem_fp64 if fp64 else oracle_mod.wem_port
     img = None
     for s in range(shots.nshot):
-        q = dict(p, sx=float(shots.sx[s]))
+        q = dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s]))
         d = synth.shot_gather_full(shots, s, p["nmx"])
         m = op(q, vel, wav, d=d, adj=True).astype(np.float64)
         img = m if img is None else img + m

@@ -119,7 +119,7 @@ def test_least_squares_geometry_misfit_curve_vs_port_pair(gpu_lib, oracle_mod):
         out = []
         for s in range(shots.nshot):
             lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
-            full = oracle_mod.wem_port(dict(p, sx=float(shots.sx[s])), c["vel"], c["wav"],
+            full = oracle_mod.wem_port(dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s])), c["vel"], c["wav"],
                                        m=np.asarray(m, np.float32), adj=False, nthreads=CORES)
             out.append(full[shots.trace_cell[lo:hi]])
         return np.concatenate(out).astype(np.float64)
@@ -130,7 +130,7 @@ def test_least_squares_geometry_misfit_curve_vs_port_pair(gpu_lib, oracle_mod):
             lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
             g = np.zeros((p["nmx"], p["nt"]), np.float32)
             g[shots.trace_cell[lo:hi]] = d[lo:hi]
-            img += oracle_mod.wem_port(dict(p, sx=float(shots.sx[s])), c["vel"], c["wav"], d=g, adj=True,
+            img += oracle_mod.wem_port(dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s])), c["vel"], c["wav"], d=g, adj=True,
                                        nthreads=CORES)
         return img
 

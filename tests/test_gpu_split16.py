@@ -20,7 +20,7 @@ def _stack(oracle_mod, p, vel, wav, shots, fp64):
     img = None
     for s in range(shots.nshot):
         d = synth.shot_gather_full(shots, s, p["nmx"])
-        m = op(dict(p, sx=float(shots.sx[s])), vel, wav, d=d, adj=True).astype(np.float64)
+        m = op(dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s])), vel, wav, d=d, adj=True).astype(np.float64)
         img = m if img is None else img + m
     return img
 

@@ -42,7 +42,7 @@ def _port_stack(oracle_mod, c):
     p, shots = c["params"], c["shots"]
     out = None
     for s in range(shots.nshot):
-        q = dict(p, sx=float(shots.sx[s]))
+        q = dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s]))
         m = oracle_mod.wem_port(q, c["vel"], c["wav"], d=synth.shot_gather_full(shots, s, p["nmx"]), adj=True)
         out = m.astype(np.float64) if out is None else out + m
     return out
