@@ -358,14 +358,6 @@ __global__ void __launch_bounds__(EwemShape<N, BLU>::NT, EwemShape<N, BLU>::MINB
                         }
                     }
                 } else if (valid && rec_on) {
-                    // the accumulator row of this depth towards L2: its read-modify-write below
-                    // then does not wait on DRAM (one prefetch per 16 threads and 128-byte line)
-                    if ((t & 15) == 0) {
-#pragma unroll
-                        for (int q = 0; q < 16; q++)
-                            if (t + T * q < nmx)
-                                asm volatile("prefetch.global.L2 [%0];" ::"l"(slot + (size_t)iz * nmx + t + T * q));
-                    }
                     mix(v, true);  // components -> potentials
                     ssop_row<N, BLU>(v, true, false, role == 0 ? php : phs, role == 0 ? cp : cs, a.taper, xbuf, tw, t,
                                      sync, m);
