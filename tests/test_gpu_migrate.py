@@ -97,6 +97,25 @@ def test_row_length_limits(gpu_lib):
             assert e.value.code == WEM_ERR_SIZE
 
 
+@pytest.mark.parametrize("interp", ["ref", "linear"])
+def test_many_reference_velocities_at_2048(gpu_lib, oracle_mod, interp):
+    """2048-point rows keep the phase tables of every reference velocity in shared memory:
+    16 references fit (one shot per CTA) and match the port; 40 do not, and the call is
+    refused with WEM_ERR_SIZE instead of running anything."""
+    from wemgpu import synth
+    from wemgpu._lib import WemError, WEM_ERR_SIZE
+    c = synth.small_case(83, nx=1024, nz=6, nt=64, nshot=2, pspi=1, nref=16, interp=interp, fmax=20.0)
+    p = c["params"]
+    assert p["nmx"] * p["padx"] == 2048 and p["nref"] == 16
+    m = gpu_lib.migrate(p, c["vel"], c["wav"], c["shots"])
+    want = _port_stack(oracle_mod, p, c["vel"], c["wav"], c["shots"])
+    assert rel_l2(m, want) < TOL
+    with gpu_lib.Context() as ctx:
+        with pytest.raises(WemError) as e:
+            ctx.prepare(dict(p, nref=40), c["vel"], c["wav"]).migrate(c["shots"])
+        assert e.value.code == WEM_ERR_SIZE
+
+
 def test_deterministic(gpu_lib):
     from wemgpu import synth
     c = synth.small_case(41, nx=128, nz=16, nt=96, nshot=4)
