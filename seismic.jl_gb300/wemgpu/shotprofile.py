@@ -330,7 +330,7 @@ def ShotProfileEWEM(m, d, adj: bool = True, *, damping=1000.0, vp="vp.seis", vs=
     155-230, 290-350). 2-D grids; mps1 and uy are written as zeros (the separation has no S1
     potential, ewem.c:553-741). Differences, where the reference is ill-defined: traces are
     placed on the grid by their gx/gy headers, and the modelled traces carry gx = ox + dx*imx
-    (the reference's per-shot images carry mx = dx*imx, ShotProfileEWEM.jl:267-268, which
+    (the reference's per-shot images carry mx = dx*imx, ShotProfileEWEM.jl:274, which
     shotewem.c copies into gx: the same unless the grid starts at ox = 0)."""
     from .api import elastic
     gathers = nangx != 1 or nangy != 1
