@@ -281,12 +281,19 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
+        self.first = ""
 
     def start(self):
+        """Starts the sampler and waits (at most 2 s) for its first sample, so that a timed
+        region shorter than the 200 ms period still has the sample taken as it begins."""
+        import select
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                                           "-i", str(self.device), "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            ready, _, _ = select.select([self.proc.stdout], [], [], 2.0)
+            if ready:
+                self.first = self.proc.stdout.readline()
         except Exception:
             self.proc = None
 
@@ -299,6 +306,7 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
             out, _ = self.proc.communicate()
+        out = self.first + (out or "")
         sm, mx, reasons = [], 0.0, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in out.strip().splitlines():
