@@ -118,7 +118,10 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
 
         for (int iz = 0; iz < a.nz; iz++) {
             const uint8_t zf = a.zflag[iz];
-            const bool active = is_src ? (zf & Z_SRC) : (zf & Z_REC);
+            // split-step: a slot of a part-filled shot group has zero rows and its team skips
+            // the arithmetic (a one-shot survey leaves most slots empty; the PSPI forms keep
+            // the registers of the full-group code)
+            const bool active = (PSPI || shot_ok) && (is_src ? (zf & Z_SRC) : (zf & Z_REC));
             if (zf & Z_REC) {
                 // the CTA's image row of this depth to L2 now; it is read and rewritten at the
                 // end of the step
@@ -276,7 +279,7 @@ __global__ void __launch_bounds__(S * (N / 16), N <= 1024 ? 2 : 1) wem_model_ker
         }
         // source, downward (wem.c:255-265)
         for (int iz = 0; iz < nz; iz++) {
-            const bool act = (a.zflag[iz] & Z_SRC) != 0;
+            const bool act = (PSPI || shot_ok) && (a.zflag[iz] & Z_SRC) != 0;  // split-step: empty slots skip
             __syncthreads();
             if (PSPI && a.ptab) {
                 // precomputed tables, copied behind the forward transform
@@ -318,7 +321,7 @@ __global__ void __launch_bounds__(S * (N / 16), N <= 1024 ? 2 : 1) wem_model_ker
             }
         };
         for (int iz = nz - 1; iz >= 0; iz--) {
-            const bool rec = (a.zflag[iz] & Z_REC) != 0;
+            const bool rec = (PSPI || shot_ok) && (a.zflag[iz] & Z_REC) != 0;
             if (iz > 0 && 8 * t < nmx) {
                 // the next depth's source and image rows to L2 (64 bytes of each per thread)
                 asm volatile("prefetch.global.L2 [%0];" ::"l"(smig + (size_t)(iz - 1) * nmx + 8 * t));
