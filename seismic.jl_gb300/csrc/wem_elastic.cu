@@ -2,18 +2,21 @@
 // the reference's ewem / elastic_extrap1f / elastic_separate_3d (src/Imaging/c/ewem.c:3-741),
 // 2-D (nmy = 1, the case its separation handles: it uses kx only, ewem.c:596-611).
 //
-// Per (shot, frequency) one CTA of three row teams (N/16 threads each, a row of N samples in
-// registers as in the acoustic depth kernels): the source row, and the receiver's two rows --
-// the components (ux, uz), separated at every depth into the P and S2 potentials
-// (elastic_separate_3d), continued with the split-step operator of their own velocity
-// (ssop with vp or vs), and recombined into components. The two receiver teams meet in two
-// shared spectrum buffers for the separation and the recombination, which mix the two rows at
-// each wavenumber. Migration (adj): the source goes down beside the receiver and each depth adds
-// Re(conj(smig) P) into the P image and Re(conj(smig) S2) into the S image (compensated per-CTA
-// accumulators, reduced in a fixed order). Modelling: the source pass stores smig for every
-// depth, then the receiver goes up with smig * image injected into P and S2. The y component
-// and the S1 image stay zero, as in the reference (its S1 separation is commented out,
-// ewem.c:579-587).
+// Everything that depends only on (frequency, depth) -- the phase rows of the P and S layer
+// slownesses, the slowness corrections and the separation coefficients of every wavenumber -- is
+// built once per frequency band by wem_ewem_tables_kernel, one record per (frequency, depth),
+// and shared by every shot. The depth kernel carries several shots of one frequency per CTA,
+// each as a receiver pair of row teams (N/16 threads each, a row of N samples in registers as in
+// the acoustic depth kernels): the components (ux, uz), separated at every depth into the P and
+// S2 potentials (elastic_separate_3d), continued with the split-step operator of their own
+// velocity (ssop with vp or vs), and recombined into components. A pair meets in two shared
+// spectrum buffers for the separation and the recombination, which mix its two rows at each
+// wavenumber. One source team advances the group's source rows. Migration (adj): the sources go
+// down beside the receivers and each depth adds Re(conj(smig) P) into the P image and
+// Re(conj(smig) S2) into the S image (compensated accumulators per CTA and shot slot, reduced in
+// a fixed order). Modelling: the source pass stores smig for every depth, then the receivers go
+// up with smig * image injected into P and S2. The y component and the S1 image stay zero, as
+// in the reference (its S1 separation is commented out, ewem.c:579-587).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
