@@ -227,8 +227,8 @@ WEM_API int wem_elastic(int device, const wem_params *p, const float *vp, const 
                         int nshot, const float *sx, const float *sy, float *ux, float *uz, float *mpp,
                         float *mps2, int adj);
 
-/* Device time in ms of the last wem_elastic call (spectra, depth kernel, reduction or
-   synthesis; CUDA events), no counterpart in the reference. */
+/* Device time in ms of the calling thread's last wem_elastic call (spectra, tables, depth
+   kernel, reduction or synthesis; CUDA events), no counterpart in the reference. */
 WEM_API float wem_elastic_last_ms(void);
 
 /* Drop-in for the reference's ewem() (ewem.h:3-16): the same arguments, float** rows as

@@ -116,7 +116,7 @@ struct Bufs {
     }
 };
 
-float g_last_ms = 0.f;
+thread_local float g_last_ms = 0.f;  // per calling thread
 
 }  // namespace
 
