@@ -103,22 +103,28 @@ def main(only=None):
 
 
 EWEM_CASES = {
-    # name: (seed, nx, nz, nt, fmax, padx); the S velocity is vp / 1.8 with a seeded wobble
+    # name: (seed, nx, nz, nt, fmax, padx[, sz, gz]); the S velocity is vp / 1.8 with a seeded
+    # wobble; sz, gz (m) put the source and the receivers below the surface
     "ewem_64": (41, 64, 16, 128, 40.0, 2),        # nkx 128
     "ewem_150_padx1": (42, 150, 12, 128, 35.0, 1),  # nkx 150 (taper on)
+    "ewem_64_buried": (43, 64, 16, 128, 40.0, 2, 35.0, 25.0),  # source from z = 40 m, receivers from 30 m
 }
 
 
-def ewem_main():
+def ewem_main(only=None):
     """The reference's elastic ewem() (oracle/_ref/libewem_ref.so, src/Imaging/c/ewem.c),
-    one shot per case, migration and forward."""
+    one shot per case, migration and forward; `only` limits it to the named cases."""
     os.environ.setdefault("OMP_NUM_THREADS", "4")
-    for name, (seed, nx, nz, nt, fmax, padx) in EWEM_CASES.items():
+    for name, case in EWEM_CASES.items():
+        if only and name not in only:
+            continue
+        seed, nx, nz, nt, fmax, padx = case[:6]
+        sz, gz = case[6:8] if len(case) > 6 else (0.0, 0.0)
         c = synth.small_case(seed, nx=nx, nz=nz, nt=nt, nshot=1, pspi=0, fmax=fmax, padx=padx)
         rng = np.random.default_rng(seed + 200)
         vp = c["vel"]
         vs = (vp / 1.8 * (1.0 + 0.05 * rng.standard_normal(vp.shape))).astype(np.float32)
-        p = dict(c["params"], sx=float(c["shots"].sx[0]), fmin=3.0)
+        p = dict(c["params"], sx=float(c["shots"].sx[0]), fmin=3.0, sz=sz, gz=gz)
         d = synth.shot_gather_full(c["shots"], 0, nx)
         ux_in = (0.4 * d + 0.1 * np.roll(d, 3, axis=1)).astype(np.float32)
         uz_in = d
@@ -163,11 +169,12 @@ def angles_main():
 if __name__ == "__main__":
     if sys.argv[1:] == ["angles"]:
         angles_main()
-    elif sys.argv[1:] == ["ewem"]:
+    elif sys.argv[1:2] == ["ewem"]:
+        # python tests/golden/make_golden.py ewem [name,name...]: the elastic cases (or those named)
         O.build()
         if O.build_ref() is None:
             sys.exit("reference sources not found")
-        ewem_main()
+        ewem_main(set(sys.argv[2].split(",")) if len(sys.argv) > 2 else None)
     elif sys.argv[1:2] == ["--only"]:
         # python tests/golden/make_golden.py --only name[,name...]: those 2-D cases only
         main(set(sys.argv[2].split(",")))

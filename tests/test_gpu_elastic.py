@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 TOL = 1e-4
 
 
-@pytest.mark.parametrize("case", ["ewem_64", "ewem_150_padx1"])
+@pytest.mark.parametrize("case", ["ewem_64", "ewem_150_padx1", "ewem_64_buried"])
 def test_elastic_matches_reference_golden(gpu_lib, case):
     g = load_golden(f"{case}.npz")
     p = g["params"]

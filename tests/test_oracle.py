@@ -153,7 +153,7 @@ def test_angle_oracle_matches_reference_golden_3d():
         assert np.abs(ref).max() > 30.0
 
 
-@pytest.mark.parametrize("case", ["ewem_64", "ewem_150_padx1"])
+@pytest.mark.parametrize("case", ["ewem_64", "ewem_150_padx1", "ewem_64_buried"])
 def test_elastic_fp64_restatement_matches_reference_golden(case):
     """oracle/ewem_np.py (FP64 restatement of src/Imaging/c/ewem.c) vs the reference's own
     ewem() output: migration (P and S2 images) and the forward operator (x and z data). The
