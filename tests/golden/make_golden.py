@@ -38,14 +38,19 @@ CASES = {
     "pspi_768_padx2": (18, 768, 8, 64, 1, 3, 25.0, 2, 2),     # nkx 1536 = 2^9 3
     "pspi_97_padx1": (19, 97, 16, 96, 1, 4, 40.0, 1, 2),      # nkx 97, a prime
     "ss_50_padx1": (20, 50, 16, 96, 0, 2, 40.0, 1, 2),        # nkx 50
+    # the source and the receivers below the surface (sz, gz in m; wem.c:213-224)
+    "ss_64_buried": (23, 64, 24, 128, 0, 2, 40.0, 2, 2, 45.0, 95.0),
+    "pspi_64_buried": (24, 64, 24, 128, 1, 4, 40.0, 2, 2, 95.0, 45.0),
 }
 
 
-def case_inputs(seed, nx, nz, nt, pspi, nref, fmax, padx, padt):
+def case_inputs(seed, nx, nz, nt, pspi, nref, fmax, padx, padt, sz=0.0, gz=0.0):
     c = synth.small_case(seed, nx=nx, nz=nz, nt=nt, nshot=1, pspi=pspi, nref=nref, fmax=fmax, padx=padx,
                          padt=padt)
     p = dict(c["params"])
     p["sx"] = float(c["shots"].sx[0])
+    if sz or gz:
+        p["sz"], p["gz"] = float(sz), float(gz)
     d = synth.shot_gather_full(c["shots"], 0, nx)
     rng = np.random.default_rng(seed + 100)
     m_in = rng.standard_normal((nx, nz)).astype(np.float32)

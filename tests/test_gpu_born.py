@@ -12,7 +12,7 @@ from conftest import load_golden, rel_l2
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-4
-GOLDEN_CASES = ["ss_64", "ss_128_taper", "pspi_64", "pspi_128_r8", "pspi_64_padx1", "pspi_500_padx2", "ss_300_padx2", "pspi_768_padx2", "pspi_97_padx1", "ss_50_padx1"]
+GOLDEN_CASES = ["ss_64", "ss_128_taper", "pspi_64", "pspi_128_r8", "pspi_64_padx1", "pspi_500_padx2", "ss_300_padx2", "pspi_768_padx2", "pspi_97_padx1", "ss_50_padx1", "ss_64_buried", "pspi_64_buried"]
 
 
 @pytest.mark.parametrize("case", GOLDEN_CASES)

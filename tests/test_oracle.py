@@ -14,7 +14,7 @@ import pytest
 
 from conftest import load_golden, rel_l2
 
-GOLDEN_CASES = ["ss_64", "ss_128_taper", "pspi_64", "pspi_128_r8", "pspi_64_padx1", "ss3d_32", "pspi3d_32", "pspi_500_padx2", "ss_300_padx2", "pspi_768_padx2", "pspi_97_padx1", "ss_50_padx1"]
+GOLDEN_CASES = ["ss_64", "ss_128_taper", "pspi_64", "pspi_128_r8", "pspi_64_padx1", "ss3d_32", "pspi3d_32", "pspi_500_padx2", "ss_300_padx2", "pspi_768_padx2", "pspi_97_padx1", "ss_50_padx1", "ss_64_buried", "pspi_64_buried"]
 
 
 @pytest.mark.parametrize("n", [1, 2, 3, 5, 7, 12, 16, 17, 30, 64, 125, 256, 512, 1000, 1024, 2000, 2048, 3000, 4096])
