@@ -17,27 +17,8 @@
 #include <string.h>
 
 #include "../../include/shotwem_gb300.h"
+#include "cli_args.h"
 #include "seis_io.h"
-
-static const char *arg_value(int argc, char **argv, const char *key)
-{
-    const size_t n = strlen(key);
-    for (int i = 1; i < argc; i++) {
-        if (!argv[i]) continue;
-        if (!strncmp(argv[i], key, n) && argv[i][n] == '=') return argv[i] + n + 1;
-    }
-    return NULL;
-}
-static void arg_bool(int argc, char **argv, const char *k, bool *v)
-{
-    const char *s = arg_value(argc, argv, k);
-    if (s) *v = (s[0] == 'y'); /* par_read_bool, seismic.c:50 */
-}
-static void arg_float(int argc, char **argv, const char *k, float *v)
-{
-    const char *s = arg_value(argc, argv, k);
-    if (s) *v = (float)atof(s);
-}
 
 static int run(int argc, char **argv)
 {

@@ -76,6 +76,30 @@ def image_headers(g: dict, dz: float):
     return h
 
 
+def data_layout(g: dict, sx, sy, nt: int, dt: float, ot: float):
+    """Trace headers and extent of modelled data: every shot recorded on every grid cell,
+    shot after shot, receiver (gx, gy) = cell position, offsets hx, hy, keyed by sx, sy (the
+    data files of ShotProfileWEM.jl:291-302, ShotProfileEWEM.jl:366-377). Returns the
+    arguments of seis.write after the data."""
+    n = g["nmx"] * g["nmy"]
+    hd = seis.empty_headers(len(sx) * n)
+    imx = np.repeat(np.arange(g["nmx"]), g["nmy"])
+    imy = np.tile(np.arange(g["nmy"]), g["nmx"])
+    mx, my = g["omx"] + g["dmx"] * imx, g["omy"] + g["dmy"] * imy
+    for i, (x0, y0) in enumerate(zip(sx, sy)):
+        q = hd[i * n:(i + 1) * n]
+        q["tracenum"] = np.arange(1, n + 1) + i * n
+        q["n1"], q["d1"], q["o1"] = nt, dt, ot
+        q["sx"], q["sy"] = x0, y0
+        q["gx"], q["gy"], q["mx"], q["my"] = mx, my, mx, my
+        q["hx"], q["hy"] = mx - x0, my - y0
+        q["imx"], q["imy"] = imx, imy
+    nsx = len(sx)
+    return (hd, [nt, g["nmx"], g["nmy"], nsx, 1], [ot, g["omx"], g["omy"], sx[0], sy[0]],
+            [dt, g["dmx"], g["dmy"], (sx[1] - sx[0]) if nsx > 1 else 1.0, 1.0],
+            ["Time", "gx", "gy", "sx", "sy"], ["s", "m", "m", "m", "m"])
+
+
 # --------------------------------------------------------------------------- angles
 
 def ComputeAngles(angx: str, angy: str, dip_flag=False, vel="vel", wav="wav", sz=0.0, fmin=0, fmax=80,
@@ -275,22 +299,7 @@ def ShotProfileWEM(m: str, d: str, adj: bool = True, *, pspi=True, nref=5, dampi
             data = np.concatenate(parts)
         else:
             data = ctx.model(shots, img[:n], exact=False)
-        hd = seis.empty_headers(len(sx) * n)
-        mx = g["omx"] + g["dmx"] * np.repeat(np.arange(g["nmx"]), g["nmy"])
-        my = g["omy"] + g["dmy"] * np.tile(np.arange(g["nmy"]), g["nmx"])
-        for i, (x0, y0) in enumerate(zip(sx, sy)):
-            q = hd[i * n:(i + 1) * n]
-            q["tracenum"] = np.arange(1, n + 1) + i * n
-            q["n1"], q["d1"], q["o1"] = nt, dt, ot
-            q["sx"], q["sy"] = x0, y0
-            q["gx"], q["gy"], q["mx"], q["my"] = mx, my, mx, my
-            q["hx"], q["hy"] = mx - x0, my - y0
-            q["imx"] = np.repeat(np.arange(g["nmx"]), g["nmy"])
-            q["imy"] = np.tile(np.arange(g["nmy"]), g["nmx"])
-        nsx = len(sx)
-        seis.write(d, data, hd, [nt, g["nmx"], g["nmy"], nsx, 1], [ot, g["omx"], g["omy"], sx[0], sy[0]],
-                   [dt, g["dmx"], g["dmy"], (sx[1] - sx[0]) if nsx > 1 else 1.0, 1.0],
-                   labels=["Time", "gx", "gy", "sx", "sy"], units=["s", "m", "m", "m", "m"])
+        seis.write(d, data, *data_layout(g, sx, sy, nt, dt, ot))
         return data
     finally:
         if own:
@@ -385,22 +394,8 @@ def ShotProfileEWEM(m, d, adj: bool = True, *, damping=1000.0, vp="vp.seis", vs=
             is2 = (_signs(ax, ay) * unbin_shot(gs, ax, ay, *abin)).astype(np.float32)
             a, b = elastic(params, vpv, vsv, w[0], [x0], [y0], mpp=ip, mps2=is2, adj=False, device=device)
             ux[i], uz[i] = a[0], b[0]
-    hd = seis.empty_headers(len(sx) * n)
-    mx = g["omx"] + g["dmx"] * np.repeat(np.arange(g["nmx"]), g["nmy"])
-    my = g["omy"] + g["dmy"] * np.tile(np.arange(g["nmy"]), g["nmx"])
-    for i, (x0, y0) in enumerate(zip(sx, sy)):
-        q = hd[i * n:(i + 1) * n]
-        q["tracenum"] = np.arange(1, n + 1) + i * n
-        q["n1"], q["d1"], q["o1"] = nt, dt, ot
-        q["sx"], q["sy"] = x0, y0
-        q["gx"], q["gy"], q["mx"], q["my"] = mx, my, mx, my
-        q["hx"], q["hy"] = mx - x0, my - y0
-        q["imx"] = np.repeat(np.arange(g["nmx"]), g["nmy"])
-        q["imy"] = np.tile(np.arange(g["nmy"]), g["nmx"])
-    nsx = len(sx)
-    dext = ([nt, g["nmx"], g["nmy"], nsx, 1], [ot, g["omx"], g["omy"], sx[0], sy[0]],
-            [dt, g["dmx"], g["dmy"], (sx[1] - sx[0]) if nsx > 1 else 1.0, 1.0])
-    comps = (ux.reshape(-1, nt), np.zeros((nsx * n, nt), np.float32), uz.reshape(-1, nt))
+    layout = data_layout(g, sx, sy, nt, dt, ot)
+    comps = (ux.reshape(-1, nt), np.zeros((len(sx) * n, nt), np.float32), uz.reshape(-1, nt))
     for name, a in zip(d, comps):
-        seis.write(name, a, hd, *dext, labels=["Time", "gx", "gy", "sx", "sy"], units=["s", "m", "m", "m", "m"])
+        seis.write(name, a, *layout)
     return ux, uz
