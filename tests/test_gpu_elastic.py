@@ -131,3 +131,21 @@ def test_shotewem_main_on_seis_files(gpu_lib, tmp_path):
     gx = p["omx"] + p["dmx"] * np.arange(p["nmx"])
     assert np.allclose(hx["gx"], gx) and np.allclose(hx["hx"], gx - p["sx"]) and np.all(hx["n1"] == p["nt"])
     assert ext["n"][:2] == [p["nt"], p["nmx"]]
+
+
+def test_elastic_edge_cases(gpu_lib):
+    """A source off the grid, a 3-D grid and a row length with no kernel are refused with a
+    status before anything runs. (ewem.c's band arithmetic always leaves at least one
+    frequency, ewem.c:49-57, so there is no empty band to test.)"""
+    from wemgpu import synth
+    from wemgpu._lib import WemError, WEM_ERR_ARG, WEM_ERR_SIZE
+    c = synth.small_case(91, nx=64, nz=8, nt=64, nshot=2, pspi=0, fmax=30.0)
+    p, shots = c["params"], c["shots"]
+    for q, sx, code in ((p, [1e6, 0.0], WEM_ERR_ARG), (dict(p, nmy=2), shots.sx, WEM_ERR_SIZE),
+                        (dict(p, nmx=16, padx=2), shots.sx, WEM_ERR_SIZE)):
+        n = int(q["nmx"])
+        vp = c["vel"][:n]
+        zeros = np.zeros((2, n, int(q["nt"])), np.float32)
+        with pytest.raises(WemError) as e:
+            gpu_lib.elastic(q, vp, vp / 1.8, c["wav"], sx, ux=zeros, uz=zeros, adj=True)
+        assert e.value.code == code
