@@ -82,7 +82,7 @@ def test_survey_four_shots_full_band_vs_fp64(gpu_lib, oracle_mod, survey64, prec
 
 
 def test_3d_512_plane_matches_port_and_fp64(gpu_lib, oracle_mod):
-    """configs' 3-D geometry: 256 x 256 cells at 12.5 m, padx 2 (512 x 512 planes), 6
+    """The 3-D survey's geometry: 256 x 256 cells at 12.5 m, padx 2 (512 x 512 planes), 6
     reference velocities, the full receiver grid; 12 depth steps of the smooth random
     field and 3-5 Hz (17 frequencies) so that the CPU finishes in about a minute."""
     from wemgpu import synth
