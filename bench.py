@@ -338,11 +338,15 @@ KERNEL_SOURCES = ("wem_fft.cuh", "wem_step.cuh", "wem_kernels.cuh", "wem_kernels
                   "wem_internal.h")
 
 
-def kernel_source_sha() -> str:
+ELASTIC_SOURCES = KERNEL_SOURCES + ("wem_elastic.cuh", "wem_elastic.cu")
+TRAFFIC_SOURCES = {"elastic8": ELASTIC_SOURCES}  # workloads whose kernels have sources of their own
+
+
+def kernel_source_sha(names=KERNEL_SOURCES) -> str:
     """sha256 (first 16 hex digits) of the device-code sources the depth kernels are built from."""
     import hashlib
     h = hashlib.sha256()
-    for name in KERNEL_SOURCES:
+    for name in names:
         with open(os.path.join(ROOT, "seismic.jl_gb300", "csrc", name), "rb") as f:
             h.update(f.read())
     return h.hexdigest()[:16]
@@ -361,7 +365,7 @@ def recorded_traffic(workload: str):
     if rec is None:
         return None
     rec = dict(rec)
-    rec["stale"] = rec.get("kernel_source_sha") != kernel_source_sha()
+    rec["stale"] = rec.get("kernel_source_sha") != kernel_source_sha(TRAFFIC_SOURCES.get(workload, KERNEL_SOURCES))
     return rec
 
 
@@ -529,6 +533,8 @@ def run_elastic(args, c, wl, rank, world, local):
     fl = 12 * 5 * nkx * lg + 60 * nkx
     ach = units * fl / (ms / 1000.0) / 1e12
     fp32_meas = fp32_peak(local)
+    tr = recorded_traffic("elastic8") if args.fmax is None else None
+    traffic = tr.get("bytes_per_launch") if tr and not tr["stale"] else None
     line = {"metric": "shot*omega*depth-steps/s", "value": world * units / (ms / 1000.0),
             "unit": "shot*omega*depth-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -538,10 +544,10 @@ def run_elastic(args, c, wl, rank, world, local):
             "e2e": {"value": world * units / statistics.mean(wall), "unit": "shot*omega*depth-steps/s",
                     "h2d_bytes_per_step": int(ux.nbytes + uz.nbytes), "d2h_bytes_per_step": int(2 * nmx * nz * 4)},
             "roofline": {"bound": "fp32", "achieved": ach, "peak": fp32_meas, "unit": "TFLOP/s",
-                         "frac": ach / fp32_meas, "traffic": None,
+                         "frac": ach / fp32_meas, "traffic": traffic,
                          "peak_source": "FP32 FMA probe (wem_measure_fp32_peak), measured in this run",
                          "kernel": "wem_ewem_kernel + tables + spectra + reductions, whole step", "ms_per_launch": ms,
-                         "flops_per_unit": fl},
+                         "flops_per_unit": fl, "traffic_kernel": "wem_ewem_kernel (DRAM bytes of one launch)"},
             "clocks": clocks}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # the CPU leg: the oracle's FP64 restatement (NumPy, one thread) on one shot, 2 Hz of the band
@@ -614,6 +620,8 @@ def run_angles(args, c, wl, rank, world, local):
     fl = 10 * nmx_a * math.log2(nmx_a) + 20 * nmx_a + 25 * nmx_a * math.log2(nmx_a * nz_a)
     ach = units * fl / (ms / 1000.0) / 1e12
     fp32_meas = fp32_peak(local)
+    tr = recorded_traffic("elastic8") if args.fmax is None else None
+    traffic = tr.get("bytes_per_launch") if tr and not tr["stale"] else None
     line["roofline"] = {"bound": "fp32", "achieved": ach, "peak": fp32_meas, "unit": "TFLOP/s",
                         "frac": ach / fp32_meas, "traffic": None,
                         "peak_source": "FP32 FMA probe (wem_measure_fp32_peak), measured in this run",
