@@ -205,3 +205,127 @@ def test_shotprofile_ewem_on_files_with_and_without_angle_gathers(gpu_lib, tmp_p
     gdx = shotprofile.ShotProfileEWEM([t + "/gpp", t + "/gps1", t + "/gps2"], [t + "/ex", t + "/ey", t + "/ez"],
                                       False, **kw, **spec)
     assert np.all(np.isfinite(gdx[0])) and np.any(gdx[0]) and np.any(gdx[1])
+
+
+def test_shotprofile_ewem_file_plumbing_with_a_fake_operator(tmp_path, monkeypatch):
+    """The host side of ShotProfileEWEM (ShotProfileEWEM.jl:38-411) on CPU: the GPU call is
+    replaced by a deterministic fake (each shot's P image = sx * column sums of its ux traces,
+    S image = -the same of uz; modelling = the images broadcast over time), so the test checks
+    what the operator itself does with files: windowing by sx, placing traces by gx, stacking,
+    angle binning with the S images signed by the angles, unbinning, and the data headers."""
+    from wemgpu import seis, synth, shotprofile, api
+    c = synth.small_case(131, nx=32, nz=6, nt=16, nshot=2, pspi=0, fmax=30.0)
+    p, shots, nx, nz, nt = c["params"], c["shots"], 32, 6, 16
+    rng = np.random.default_rng(9)
+    uz = rng.standard_normal((shots.nshot, nx, nt)).astype(np.float32)
+    ux = rng.standard_normal((shots.nshot, nx, nt)).astype(np.float32)
+    calls = []
+
+    def fake_elastic(params, vp, vs, wav, sx, sy=None, ux=None, uz=None, mpp=None, mps2=None, adj=True, device=0):
+        sx = np.atleast_1d(sx).astype(np.float64)
+        calls.append((adj, len(sx)))
+        if adj:
+            a = sum(x * np.repeat(u.sum(axis=1, keepdims=True), nz, 1) for x, u in zip(sx, ux))
+            b = sum(-x * np.repeat(u.sum(axis=1, keepdims=True), nz, 1) for x, u in zip(sx, uz))
+            return a.astype(np.float32), b.astype(np.float32)
+        return (np.stack([np.repeat(mpp[:, :1], nt, 1) * x for x in sx]).astype(np.float32),
+                np.stack([np.repeat(mps2[:, :1], nt, 1) * x for x in sx]).astype(np.float32))
+
+    monkeypatch.setattr(api, "elastic", fake_elastic)
+    t = str(tmp_path)
+    _write_elastic_survey(t, c, (c["vel"] / 1.7).astype(np.float32), ux, uz)
+    sx = [float(v) for v in shots.sx]
+    kw = dict(vp=t + "/vp", vs=t + "/vs", wav=t + "/wav", sx=sx, sy=[0.0] * 2, angx=t + "/angx", angy=t + "/angy")
+    m = [t + "/mpp", t + "/mps1", t + "/mps2"]
+    d = [t + "/ux", t + "/uy", t + "/uz"]
+    mpp, mps1, mps2 = shotprofile.ShotProfileEWEM(m, d, True, **kw)
+    want_p, want_s = fake_elastic(p, None, None, None, sx, ux=ux, uz=uz)
+    assert np.allclose(mpp, want_p) and np.allclose(mps2, want_s) and not np.any(mps1) and calls[-1] == (True, 2)
+    got, h, e = seis.read(t + "/mpp")
+    assert e["n"][:2] == [nz, nx] and np.allclose(got, want_p)
+
+    ang = rng.uniform(-50.0, 50.0, (2, nx, nz))
+    _write_shot_angles(t + "/angx", ang, sx, p)
+    _write_shot_angles(t + "/angy", np.zeros_like(ang), sx, p)
+    spec = dict(nangx=7, oangx=-60.0, dangx=20.0)
+    gp, _, gs = shotprofile.ShotProfileEWEM([t + "/gpp", t + "/gps1", t + "/gps2"], d, True, **kw, **spec)
+    per = [fake_elastic(p, None, None, None, [sx[i]], ux=ux[i:i + 1], uz=uz[i:i + 1]) for i in range(2)]
+    assert np.allclose(gp.sum(axis=1), mpp, rtol=1e-5, atol=1e-3)
+    signed = sum(np.where(ang[i] < 0, -1.0, 1.0) * per[i][1] for i in range(2))
+    assert np.allclose(gs.sum(axis=1), signed, rtol=1e-5, atol=1e-3)
+    _, hg, eg = seis.read(t + "/gpp")
+    assert eg["n"][:4] == [nz, nx, 1, 7] and list(hg["ang"][:7]) == [-60, -40, -20, 0, 20, 40, 60]
+
+    ux2, uz2 = shotprofile.ShotProfileEWEM(m, [t + "/dx", t + "/dy", t + "/dz"], False, **kw)
+    assert np.allclose(ux2[1], np.repeat(mpp[:, :1], nt, 1) * sx[1]) and calls[-1] == (False, 2)
+    dx_, hdx, edx = seis.read(t + "/dx")
+    dy_, _, _ = seis.read(t + "/dy")
+    gx = p["omx"] + p["dmx"] * np.arange(nx)
+    assert dx_.shape == (2 * nx, nt) and not np.any(dy_) and edx["n"][:4] == [nt, nx, 1, 2]
+    assert np.allclose(hdx["sx"][nx:], sx[1]) and np.allclose(hdx["gx"][:nx], gx) and np.allclose(hdx["hx"][:nx], gx - sx[0])
+
+
+class _FakeContext:
+    """Stands in for wemgpu.Context in a CPU test of the file plumbing: a shot's image is
+    sx * the sum of its traces over time at each cell (nz copies); modelling puts the image's
+    first depth sample times sx on every time sample."""
+
+    def __init__(self, nz, nt):
+        self.nz, self.nt, self.calls = nz, nt, []
+
+    def prepare(self, params, vel, wav):
+        self.params = params
+        return self
+
+    def migrate(self, shots):
+        n = self.params["nmx"] * self.params["nmy"]
+        img = np.zeros((n, self.nz))
+        for s in range(shots.nshot):
+            lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
+            for cell, tr in zip(shots.trace_cell[lo:hi], shots.data[lo:hi]):
+                img[cell] += float(shots.sx[s]) * tr.sum()
+        self.calls.append(("migrate", shots.nshot))
+        return img.astype(np.float32)
+
+    def model(self, shots, m, exact=False):
+        out = []
+        for s in range(shots.nshot):
+            lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
+            out.append(np.repeat(m[shots.trace_cell[lo:hi], :1], self.nt, 1) * float(shots.sx[s]))
+        self.calls.append(("model", shots.nshot))
+        return np.concatenate(out).astype(np.float32)
+
+
+def test_shotprofile_wem_file_plumbing_with_a_fake_context(tmp_path):
+    """The host side of ShotProfileWEM (ShotProfileWEM.jl:39-310) on CPU with a fake context:
+    the survey file windowed by sx and placed by gx, one batched call for the stack, one call
+    per shot for angle gathers (their sum over the bins is the stack), and the modelled data's
+    layout and headers."""
+    from wemgpu import seis, synth, shotprofile
+    c = synth.small_case(141, nx=32, nz=6, nt=16, nshot=3, pspi=1, nref=3)
+    p, shots = c["params"], c["shots"]
+    t = str(tmp_path)
+    _write_survey(t, c)
+    sx = [float(v) for v in shots.sx]
+    fake = _FakeContext(p["nz"], p["nt"])
+    kw = dict(vel=t + "/vel", wav=t + "/wav", sx=sx, sy=[0.0] * 3, ctx=fake, angx=t + "/angx", angy=t + "/angy")
+    img = shotprofile.ShotProfileWEM(t + "/m", t + "/d", True, **kw)
+    want = sum(s * np.repeat(synth.shot_gather_full(shots, i, 32).sum(axis=1, keepdims=True), p["nz"], 1)
+               for i, s in enumerate(sx))
+    assert np.allclose(img, want, rtol=1e-5) and fake.calls == [("migrate", 3)]
+    got, h, e = seis.read(t + "/m")
+    assert np.allclose(got, want, rtol=1e-5) and e["n"][:2] == [p["nz"], 32]
+
+    ang = np.random.default_rng(2).uniform(-50.0, 50.0, (3, 32, p["nz"]))
+    _write_shot_angles(t + "/angx", ang, sx, p)
+    _write_shot_angles(t + "/angy", np.zeros_like(ang), sx, p)
+    gath = shotprofile.ShotProfileWEM(t + "/mg", t + "/d", True, **kw, nangx=7, oangx=-60.0, dangx=20.0)
+    assert gath.shape == (32, 7, p["nz"]) and np.allclose(gath.sum(axis=1), want, rtol=1e-5)
+    assert fake.calls[1:] == [("migrate", 1)] * 3
+
+    data = shotprofile.ShotProfileWEM(t + "/m", t + "/dm", False, **kw)
+    assert data.shape == (3 * 32, p["nt"]) and fake.calls[-1] == ("model", 3)
+    assert np.allclose(data[32:64], np.repeat(got[:, :1], p["nt"], 1) * sx[1], rtol=1e-5)
+    _, hd, ed = seis.read(t + "/dm")
+    assert ed["n"][:4] == [p["nt"], 32, 1, 3] and np.allclose(hd["sx"][64:], sx[2])
+    assert np.allclose(hd["gx"][:32], p["omx"] + p["dmx"] * np.arange(32))
