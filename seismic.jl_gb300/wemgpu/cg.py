@@ -29,12 +29,21 @@ def _copy(x):
     return x.clone() if hasattr(x, "clone") else np.array(x, copy=True)
 
 
-def conjugate_gradients(d, forward: Callable, adjoint: Callable, niter: int = 10, mu: float = 0.0,
+def conjugate_gradients(d, forward: Callable, adjoint: Callable, niter: int = 10, mu=0.0,
                         tol: float = 1.0e-15, callback: Callable | None = None, inner_fn: Callable = inner):
     """Returns (m, cost) with cost[0] = 1 and cost[i] = (||r||^2 + mu ||m||^2)/||d||^2.
     d, and what forward/adjoint return, are NumPy arrays, or device tensors with inner_fn a
-    float64 inner product of them."""
+    float64 inner product of them. mu is one weight, or (NumPy models) one per component along
+    the model's first axis, as the multi-component ConjugateGradients of
+    src/Solvers/ConjugateGradients.jl:95-150 takes [mu1; mu2]."""
     inner_ = inner_fn
+    mus = np.atleast_1d(np.asarray(mu, dtype=np.float64))
+    if mus.size == 1:
+        mu_dot = lambda x: float(mus[0]) * inner_(x, x)  # noqa: E731
+        mu_times = lambda x: float(mus[0]) * x  # noqa: E731
+    else:
+        mu_dot = lambda x: sum(float(mk) * inner_(x[k], x[k]) for k, mk in enumerate(mus))  # noqa: E731
+        mu_times = lambda x: x * mus.reshape((-1,) + (1,) * (np.ndim(x) - 1)).astype(x.dtype)  # noqa: E731
     cost = [1.0]
     r = _copy(d)
     g = adjoint(r)
@@ -45,17 +54,17 @@ def conjugate_gradients(d, forward: Callable, adjoint: Callable, niter: int = 10
     cost0 = inner_(r, r)
     for it in range(1, niter + 1):
         t = forward(s)
-        delta = inner_(t, t) + mu * inner_(s, s)
+        delta = inner_(t, t) + mu_dot(s)
         if delta <= tol:
             break
         alpha = gamma / delta
         m = m + alpha * s
         r = r - alpha * t
         g = adjoint(r)
-        g = g - mu * m
+        g = g - mu_times(m)
         gamma0 = gamma
         gamma = inner_(g, g)
-        cost1 = inner_(r, r) + mu * inner_(m, m)
+        cost1 = inner_(r, r) + mu_dot(m)
         cost.append(cost1 / cost0 if cost0 > 0 else 0.0)
         beta = gamma / gamma0
         s = beta * s + g
@@ -111,3 +120,37 @@ def dot_test(forward, adjoint, m_rand: np.ndarray, d_rand: np.ndarray):
     d_fwd = forward(m_rand)
     m_adj = adjoint(d_rand)
     return inner(d_rand, d_fwd), inner(m_rand, m_adj)
+
+
+def trace_weights(d: np.ndarray, cutoff: float = 1e-10) -> np.ndarray:
+    """1 for every trace (last axis = time) whose energy exceeds `cutoff`, else 0: the data
+    weights of CalculateSampling (src/Tools/CalculateSampling.jl:1-18)."""
+    d = np.asarray(d, np.float64)
+    return (np.sum(d * d, axis=-1) > cutoff).astype(np.float32)
+
+
+def least_squares_elastic(params: dict, vp, vs, wav, sx, ux, uz, niter: int = 10, mu=(0.0, 0.0),
+                          tol: float = 1.0e-15, sy=None, device: int = 0, callback: Callable | None = None):
+    """Elastic least-squares migration: ConjugateGradients over [ApplyDataWeights, SeisMute,
+    ShotProfileEWEM] as ShotProfileLSEWEM builds it (src/Imaging/ShotProfileLSEWEM.jl:1-19; its
+    mute has tmute = 0, vmute = 999999, so it keeps every sample). The model is (mpp, mps2)
+    [2, nmx, nz], the data (ux, uz) [2, nshot, nmx, nt] on every grid cell, weighted by the
+    sampling of the x component (CalculateSampling of d[1]); the operators are wem_elastic's
+    migration and forward operator, the reference's pair. mu: one weight per image (the
+    multi-component CG, ConjugateGradients.jl:95-150). Returns (mpp, mps2, cost)."""
+    from .api import elastic
+    ux = np.asarray(ux, np.float32)
+    uz = np.asarray(uz, np.float32)
+    w = trace_weights(ux)[..., None]  # [nshot, nmx, 1]
+    d = np.stack([ux * w, uz * w])
+
+    def fwd(m):
+        a, b = elastic(params, vp, vs, wav, sx, sy, mpp=m[0], mps2=m[1], adj=False, device=device)
+        return np.stack([a * w, b * w])
+
+    def adj(r):
+        a, b = elastic(params, vp, vs, wav, sx, sy, ux=r[0] * w, uz=r[1] * w, adj=True, device=device)
+        return np.stack([a, b])
+
+    m, cost = conjugate_gradients(d, fwd, adj, niter=niter, mu=mu, tol=tol, callback=callback)
+    return m[0], m[1], cost

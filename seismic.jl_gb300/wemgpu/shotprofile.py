@@ -399,3 +399,116 @@ def ShotProfileEWEM(m, d, adj: bool = True, *, damping=1000.0, vp="vp.seis", vs=
     for name, a in zip(d, comps):
         seis.write(name, a, *layout)
     return ux, uz
+
+
+# --------------------------------------------------------------------------- least squares
+
+def _cost_writer(name: str):
+    """The cost file of the file-level ConjugateGradients (src/Solvers/ConjugateGradients.jl:
+    41-80): a first line with the start time, then cost[0] = 1 and one normalised cost per
+    iteration, one number per line. Returns the per-iteration callback."""
+    import time
+    with open(name, "w") as f:
+        f.write("began execution at: " + time.strftime("%a %b %d %H:%M:%S %Y") + "\n")
+        f.write("1.0\n")
+
+    def cb(it, m, cost):
+        with open(name, "a") as f:
+            f.write(repr(float(cost)) + "\n")
+    return cb
+
+
+def _live_traces(shots: Shots) -> Shots:
+    """The traces CalculateSampling keeps (energy above 1e-10, CalculateSampling.jl:1-18): the
+    others have weight 0, i.e. they take no part in the least-squares problem."""
+    from .cg import trace_weights
+    keep = trace_weights(shots.data) > 0
+    offs = [0]
+    for s in range(shots.nshot):
+        lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
+        offs.append(offs[-1] + int(keep[lo:hi].sum()))
+    return Shots(shots.sx, shots.sy, np.asarray(offs, np.int64), shots.trace_cell[keep], shots.data[keep])
+
+
+def ShotProfileLSWEM(m: str, m0: str, d: str, param=None, ctx: Context | None = None):
+    """Least-squares shot-profile migration over seis files: the interface of Seismic.jl's
+    ShotProfileLSWEM(m, m0, d, param) (src/Imaging/ShotProfileLSWEM.jl:1-20): ConjugateGradients
+    over [ApplyDataWeights, SeisMute, ShotProfileWEM] with the sampling of the data as weights and
+    the mute off (tmute = 0, vmute = 999999). param holds ShotProfileWEM's keywords (vel, wav,
+    sx, sy, nref, pspi, fmin, fmax, padt, padx, sz, gz, interp) and the solver's Niter (10), mu
+    (0), tol (1e-15) and cost (the cost file, "cost"); exact=True takes the exact adjoint of the
+    migration as the forward operator instead of the reference's Born operator. m0 is accepted
+    and unused, as there (the file-level CG starts from m = 0, ConjugateGradients.jl:55-57). The
+    traces go to the GPU once per operator application (one batched call each way). Writes the
+    image file m and returns (image, cost)."""
+    from .cg import conjugate_gradients
+    q = dict(param or {})
+    vel, wav = q.get("vel", "vel"), q.get("wav", "wav")
+    velv, hv, g = grid_from_velocity(vel)
+    w, hw, ew = seis.read(wav)
+    nt, dt, ot = int(hw[0]["n1"]), float(hw[0]["d1"]), float(hw[0]["o1"])
+    sx = [float(v) for v in np.atleast_1d(q.get("sx", [0.0]))]
+    sy = [float(v) for v in np.atleast_1d(q.get("sy", [0.0]))]
+    if len(sy) == 1 and len(sx) > 1:
+        sy = sy * len(sx)
+    params = dict(nt=nt, ot=ot, dt=dt, nmx=g["nmx"], omx=g["omx"], dmx=g["dmx"], nmy=g["nmy"], omy=g["omy"],
+                  dmy=g["dmy"], nz=g["nz"], oz=g["oz"], dz=g["dz"], gz=q.get("gz", 0.0), sz=q.get("sz", 0.0),
+                  nref=q.get("nref", 5), fmin=q.get("fmin", 0), fmax=q.get("fmax", 80), padt=q.get("padt", 2),
+                  padx=q.get("padx", 2), pspi=int(bool(q.get("pspi", True))), interp=q.get("interp", "ref"))
+    data, hd, ed = seis.read(d)
+    shots = _live_traces(window_shots(data, hd, sx, sy, g))
+    own = ctx is None
+    ctx = ctx or Context(q.get("device", 0))
+    try:
+        ctx.prepare(params, velv, w[0])
+        exact = bool(q.get("exact", False))
+        fwd = lambda mm: ctx.model(shots, np.asarray(mm, np.float32), exact=exact)  # noqa: E731
+        adj = lambda r: ctx.migrate(Shots(shots.sx, shots.sy, shots.trace_offset, shots.trace_cell,  # noqa: E731
+                                          np.ascontiguousarray(r, np.float32)))
+        img, cost = conjugate_gradients(shots.data, fwd, adj, niter=int(q.get("Niter", 10)), mu=q.get("mu", 0.0),
+                                        tol=float(q.get("tol", 1.0e-15)), callback=_cost_writer(q.get("cost", "cost")))
+    finally:
+        if own:
+            ctx.close()
+    img = np.asarray(img, np.float32)
+    seis.write(m, img, image_headers(g, g["dz"]), [g["nz"], g["nmx"], g["nmy"], 1, 1],
+               [g["oz"], g["omx"], g["omy"], 0.0, 0.0], [g["dz"], g["dmx"], g["dmy"], 1.0, 1.0],
+               labels=["Depth", "mx", "my", "angx", "angy"], units=["m", "m", "m", "degrees", "degrees"])
+    return img, cost
+
+
+def ShotProfileLSEWEM(m, m0, d, param=None):
+    """Elastic least-squares migration over seis files: the interface of Seismic.jl's
+    ShotProfileLSEWEM(m, m0, d, param) (src/Imaging/ShotProfileLSEWEM.jl:1-19), m = [mpp, mps1,
+    mps2] and d = [ux, uy, uz]: ConjugateGradients over [ApplyDataWeights, SeisMute,
+    ShotProfileEWEM] (cg.least_squares_elastic). param holds ShotProfileEWEM's keywords (vp, vs,
+    wav, sx, sy, sz, gz, fmin, fmax, padt, padx) and the solver's Niter (10), mu (one weight or
+    one per image, 0), tol (1e-15) and cost ("cost.txt"). m0 is accepted and unused, as there.
+    2-D grids; mps1 is written as zeros. Returns (mpp, mps2, cost)."""
+    from .cg import least_squares_elastic
+    q = dict(param or {})
+    vpv, hv, g = grid_from_velocity(q.get("vp", "vp.seis"))
+    vsv, _, _ = seis.read(q.get("vs", "vs.seis"))
+    w, hw, ew = seis.read(q.get("wav", "wav.seis"))
+    nt, dt, ot = int(hw[0]["n1"]), float(hw[0]["d1"]), float(hw[0]["o1"])
+    sx = [float(v) for v in np.atleast_1d(q.get("sx", [0.0]))]
+    sy = [float(v) for v in np.atleast_1d(q.get("sy", [0.0]))]
+    if len(sy) == 1 and len(sx) > 1:
+        sy = sy * len(sx)
+    n, nz = g["nmx"] * g["nmy"], g["nz"]
+    params = dict(nt=nt, ot=ot, dt=dt, nmx=g["nmx"], omx=g["omx"], dmx=g["dmx"], nmy=g["nmy"], omy=g["omy"],
+                  dmy=g["dmy"], nz=nz, oz=g["oz"], dz=g["dz"], gz=q.get("gz", 0.0), sz=q.get("sz", 0.0),
+                  fmin=q.get("fmin", 0), fmax=q.get("fmax", 80), padt=q.get("padt", 1), padx=q.get("padx", 1))
+    (ux, hx, _), (uz, hz, _) = seis.read(d[0]), seis.read(d[2])
+    ux, uz = _full_grid(ux, hx, sx, sy, g), _full_grid(uz, hz, sx, sy, g)
+    mu = q.get("mu", 0.0)
+    mpp, mps2, cost = least_squares_elastic(params, vpv[:n], vsv[:n], w[0], sx, ux, uz, niter=int(q.get("Niter", 10)),
+                                            mu=mu if np.ndim(mu) else (mu, mu), tol=float(q.get("tol", 1.0e-15)),
+                                            sy=sy, device=q.get("device", 0),
+                                            callback=_cost_writer(q.get("cost", "cost.txt")))
+    h = gather_headers(g, g["dz"], 1, 0.0, 1.0, 1, 0.0, 1.0)
+    ext = ([nz, g["nmx"], g["nmy"], 1, 1], [g["oz"], g["omx"], g["omy"], 0.0, 0.0], [g["dz"], g["dmx"], g["dmy"], 1.0, 1.0])
+    for name, a in zip(m, (mpp, np.zeros_like(mpp), mps2)):
+        seis.write(name, np.asarray(a, np.float32), h, *ext, labels=["Depth", "mx", "my", "angx", "angy"],
+                   units=["m", "m", "m", "degrees", "degrees"])
+    return mpp, mps2, cost

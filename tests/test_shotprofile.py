@@ -329,3 +329,103 @@ def test_shotprofile_wem_file_plumbing_with_a_fake_context(tmp_path):
     _, hd, ed = seis.read(t + "/dm")
     assert ed["n"][:4] == [p["nt"], 32, 1, 3] and np.allclose(hd["sx"][64:], sx[2])
     assert np.allclose(hd["gx"][:32], p["omx"] + p["dmx"] * np.arange(32))
+
+
+class _LinearContext:
+    """A stand-in context whose model/migrate are an exact adjoint pair: every trace of shot s
+    at cell c is (1 + s) K m[c], K a fixed random (nt x nz) matrix."""
+
+    def __init__(self, nz, nt, seed=3):
+        self.K = np.random.default_rng(seed).standard_normal((nt, nz)).astype(np.float64)
+
+    def prepare(self, params, vel, wav):
+        self.params = params
+        return self
+
+    def _each(self, shots):
+        for s in range(shots.nshot):
+            lo, hi = int(shots.trace_offset[s]), int(shots.trace_offset[s + 1])
+            yield s, lo, hi
+
+    def model(self, shots, m, exact=False):
+        out = np.zeros((int(shots.trace_offset[-1]), self.K.shape[0]))
+        for s, lo, hi in self._each(shots):
+            out[lo:hi] = (1 + s) * m[shots.trace_cell[lo:hi]].astype(np.float64) @ self.K.T
+        return out.astype(np.float32)
+
+    def migrate(self, shots):
+        img = np.zeros((self.params["nmx"] * self.params["nmy"], self.K.shape[1]))
+        for s, lo, hi in self._each(shots):
+            np.add.at(img, shots.trace_cell[lo:hi], (1 + s) * shots.data[lo:hi].astype(np.float64) @ self.K)
+        return img.astype(np.float32)
+
+
+def test_shotprofile_lswem_on_files_with_a_linear_stand_in(tmp_path):
+    """ShotProfileLSWEM(m, m0, d, param) (ShotProfileLSWEM.jl:1-20) on CPU: the cost file of the
+    file-level ConjugateGradients (start line, 1.0, one cost per iteration), a decreasing misfit,
+    dead traces left out (CalculateSampling's weights), and the same result as conjugate_gradients
+    on the same operator pair and live traces."""
+    from wemgpu import seis, synth, shotprofile, cg
+    c = synth.small_case(151, nx=24, nz=5, nt=12, nshot=2, pspi=1, nref=3)
+    t = str(tmp_path)
+    _write_survey(t, c)
+    data, hd, ed = seis.read(t + "/d")
+    data[3] = 0.0  # a dead trace: weight 0
+    seis.write(t + "/d", data, hd, ed["n"], ed["o"], ed["d"])
+    sx = [float(v) for v in c["shots"].sx]
+    fake = _LinearContext(5, 12)
+    param = dict(vel=t + "/vel", wav=t + "/wav", sx=sx, sy=[0.0, 0.0], Niter=6, cost=t + "/cost")
+    img, cost = shotprofile.ShotProfileLSWEM(t + "/m", t + "/m0", t + "/d", param, ctx=fake)
+    lines = open(t + "/cost").read().splitlines()
+    assert lines[0].startswith("began execution at: ") and len(lines) == 2 + 6
+    assert np.allclose([float(v) for v in lines[1:]], cost) and cost[0] == 1.0
+    assert np.all(np.diff(cost) <= 1e-12) and cost[-1] < cost[1]  # CG on an exact pair: the misfit never grows
+    g = shotprofile.grid_from_velocity(t + "/vel")[2]
+    shots = shotprofile._live_traces(shotprofile.window_shots(data, hd, sx, [0.0, 0.0], g))
+    live = int(np.sum(np.sum(data.astype(np.float64) ** 2, axis=1) > 1e-10))
+    assert int(shots.trace_offset[-1]) == live < len(data)
+    fake.prepare(dict(nmx=24, nmy=1), None, None)
+    want, wcost = cg.conjugate_gradients(shots.data, lambda m: fake.model(shots, m),
+                                         lambda r: fake.migrate(shotprofile.Shots(shots.sx, shots.sy, shots.trace_offset,
+                                                                                  shots.trace_cell, r)), niter=6)
+    assert np.allclose(img, want, rtol=1e-5, atol=1e-6) and np.allclose(cost, wcost)
+    m_file, hm, em = seis.read(t + "/m")
+    assert np.allclose(m_file, img) and em["n"][:2] == [5, 24]
+
+
+def test_shotprofile_lsewem_on_files_with_a_linear_stand_in(tmp_path, monkeypatch):
+    """ShotProfileLSEWEM(m, m0, d, param) (ShotProfileLSEWEM.jl:1-19) on CPU with a linear stand-in
+    for wem_elastic (an exact adjoint pair): the two-image CG with one mu per image, its cost file,
+    the three image files (mps1 zero)."""
+    from wemgpu import seis, synth, shotprofile, api, cg
+    c = synth.small_case(161, nx=16, nz=4, nt=10, nshot=2, pspi=0, fmax=30.0)
+    p, shots = c["params"], c["shots"]
+    rng = np.random.default_rng(4)
+    Ka, Kb = rng.standard_normal((10, 4)), rng.standard_normal((10, 4))
+
+    def fake_elastic(params, vp, vs, wav, sx, sy=None, ux=None, uz=None, mpp=None, mps2=None, adj=True, device=0):
+        ns = len(np.atleast_1d(sx))
+        if adj:
+            a = sum((1 + s) * ux[s].astype(np.float64) @ Ka for s in range(ns))
+            b = sum((1 + s) * uz[s].astype(np.float64) @ Kb for s in range(ns))
+            return a.astype(np.float32), b.astype(np.float32)
+        return (np.stack([(1 + s) * mpp.astype(np.float64) @ Ka.T for s in range(ns)]).astype(np.float32),
+                np.stack([(1 + s) * mps2.astype(np.float64) @ Kb.T for s in range(ns)]).astype(np.float32))
+
+    monkeypatch.setattr(api, "elastic", fake_elastic)
+    ux = rng.standard_normal((2, 16, 10)).astype(np.float32)
+    uz = rng.standard_normal((2, 16, 10)).astype(np.float32)
+    t = str(tmp_path)
+    _write_elastic_survey(t, c, (c["vel"] / 1.7).astype(np.float32), ux, uz)
+    sx = [float(v) for v in shots.sx]
+    param = dict(vp=t + "/vp", vs=t + "/vs", wav=t + "/wav", sx=sx, sy=[0.0, 0.0], Niter=5, mu=[0.1, 0.2],
+                 cost=t + "/cost.txt")
+    mpp, mps2, cost = shotprofile.ShotProfileLSEWEM([t + "/mpp", t + "/mps1", t + "/mps2"], None,
+                                                   [t + "/ux", t + "/uy", t + "/uz"], param)
+    a, b, wcost = cg.least_squares_elastic(p, None, None, None, sx, ux, uz, niter=5, mu=(0.1, 0.2))
+    assert np.allclose(mpp, a, rtol=1e-5, atol=1e-6) and np.allclose(mps2, b, rtol=1e-5, atol=1e-6)
+    assert np.allclose(cost, wcost) and cost[-1] < cost[1]
+    lines = open(t + "/cost.txt").read().splitlines()
+    assert lines[0].startswith("began execution at: ") and len(lines) == 2 + 5
+    f1, _, e1 = seis.read(t + "/mps1")
+    assert not np.any(f1) and e1["n"][:2] == [4, 16]
