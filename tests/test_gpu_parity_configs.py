@@ -143,3 +143,57 @@ def test_least_squares_geometry_misfit_curve_vs_port_pair(gpu_lib, oracle_mod):
     cost_gpu, cost_ref = np.array(cost_gpu), np.array(cost_ref)
     print("misfit GPU", cost_gpu, "port", cost_ref)
     assert np.all(np.abs(cost_gpu - cost_ref) <= 1e-3 * np.maximum(cost_ref, 1e-3)), (cost_gpu, cost_ref)
+
+
+def test_elastic_workload_two_shots_full_band_vs_fp64(gpu_lib):
+    """The elastic workload's geometry (300 x 512 grid, padx 2: 1024-point rows, vs = vp/1.8 with a
+    5 % wobble) over its whole 5-30 Hz band (151 frequencies x 300 depth steps): two shots
+    stacked, P and S images against the FP64 restatement of ewem.c (oracle/ewem_np.py), at
+    1e-4. The reference's own FP32 arithmetic sits at 2.6e-5 / 3.0e-5 on one shot of this
+    geometry over 5-7 Hz."""
+    import ewem_np as E
+    from wemgpu import synth
+    c = synth.config4(seed=1004, nshot=8)
+    p = dict(c["params"], fmax=30.0)
+    assert p["nmx"] == 512 and p["nz"] == 300
+    rng = np.random.default_rng(2005)
+    vp = c["vel"]
+    vs = (vp / 1.8 * (1.0 + 0.05 * rng.standard_normal(vp.shape))).astype(np.float32)
+    shots = c["shots"]
+    which = [2, 5]
+    uz = np.stack([synth.shot_gather_full(shots, s, 512) for s in which])
+    ux = (0.5 * np.roll(uz, 3, axis=2)).astype(np.float32)
+    sx = [float(shots.sx[s]) for s in which]
+    mpp, mps2 = gpu_lib.elastic(p, vp, vs, c["wav"], sx, ux=ux, uz=uz, adj=True)
+    want_p = want_s = 0.0
+    for i, s in enumerate(sx):
+        a, _, b = E.ewem(dict(p, sx=s), vp, vs, c["wav"], ux=ux[i], uz=uz[i], adj=True)
+        want_p, want_s = want_p + a, want_s + b
+    ep, es = rel_l2(mpp, want_p), rel_l2(mps2, want_s)
+    print(f"elastic, 2 shots, 151 frequencies x 300 depth steps: rel L2 vs FP64 P {ep:.3e} S {es:.3e}")
+    assert ep < TOL and es < TOL
+
+
+def test_angles_workload_two_shots_full_band_vs_fp64(gpu_lib):
+    """The incidence-angle workload's geometry (the 64-shot survey's 500 x 1024 grid, 5-50 Hz of
+    the unpadded 1500-sample axis: 136 frequencies x 500 depth steps), two shots, against the
+    FP64 restatement of compute_angles (oracle/angles_np.py): the angle magnitudes at 1e-4, and
+    the side of arrival (the sign) at all but a few points per 100,000 (where both sides carry
+    equal energy the side is ill-conditioned: the reference's own FP32 result flips the same
+    way there)."""
+    import angles_np as A
+    from wemgpu import synth
+    c = synth.config1(seed=1001, nshot=8)
+    p = c["params"]
+    assert p["nmx"] == 1024 and p["nz"] == 500
+    sxs = [float(c["shots"].sx[2]), float(c["shots"].sx[5])]
+    with gpu_lib.Context() as ctx:
+        ax, _ = ctx.angles(p, c["vel"], c["wav"], sxs)
+    for i, s in enumerate(sxs):
+        want, _ = A.compute_angles(dict(p, sx=s), c["vel"], c["wav"])
+        em = rel_l2(np.abs(ax[i]), np.abs(want))
+        live = np.abs(want) > 1e-6
+        flips = int(np.count_nonzero(np.sign(ax[i][live]) != np.sign(want[live])))
+        print(f"angles, shot at {s:g} m, 136 frequencies x 500 depth steps: magnitudes {em:.3e}, "
+              f"{flips} sign flips of {int(live.sum())} points")
+        assert em < TOL and flips <= 1e-4 * live.sum()
