@@ -149,8 +149,9 @@ def test_elastic_workload_two_shots_full_band_vs_fp64(gpu_lib):
     """The elastic workload's geometry (300 x 512 grid, padx 2: 1024-point rows, vs = vp/1.8 with a
     5 % wobble) over its whole 5-30 Hz band (151 frequencies x 300 depth steps): two shots
     stacked, P and S images against the FP64 restatement of ewem.c (oracle/ewem_np.py), at
-    1e-4. The reference's own FP32 arithmetic sits at 2.6e-5 / 3.0e-5 on one shot of this
-    geometry over 5-7 Hz."""
+    1e-4. The reference's own FP32 arithmetic (ewem.c compiled in the build container) on the
+    same two shots and band: 5.3e-5 (P) and 4.7e-5 (S) against the same FP64 images; this
+    operator's 2 x 2 separation divides by norms down to 0.1 at every depth step."""
     import ewem_np as E
     from wemgpu import synth
     c = synth.config4(seed=1004, nshot=8)
