@@ -198,3 +198,17 @@ def test_angles_workload_two_shots_full_band_vs_fp64(gpu_lib):
         print(f"angles, shot at {s:g} m, 136 frequencies x 500 depth steps: magnitudes {em:.3e}, "
               f"{flips} sign flips of {int(live.sum())} points")
         assert em < TOL and flips <= 1e-4 * live.sum()
+
+
+def test_3d_survey_top_of_the_band_matches_port(gpu_lib, oracle_mod):
+    """The 3-D survey (300 x 256 x 256, 512 x 512 planes, 6 reference velocities) over all 300
+    depth steps at the top of its band, 58-60 Hz (17 frequencies, where most wavenumbers
+    propagate), against the port of the reference's C at 1e-4."""
+    from wemgpu import synth
+    c = synth.config3(seed=1003)
+    p = dict(c["params"], fmin=58.0, fmax=60.0)
+    m = gpu_lib.migrate(p, c["vel"], c["wav"], c["shots"])
+    want = _stack(oracle_mod, p, c["vel"], c["wav"], c["shots"], [0])
+    err = rel_l2(m, want)
+    print(f"3-D survey, 58-60 Hz x 300 depth steps: rel L2 vs the port {err:.3e}")
+    assert err < TOL
