@@ -308,7 +308,9 @@ static void ORC(f_op)(double _Complex *mw, IMG_T *d, int nw, int nt, int adj, FF
         buf[0].im = 0;
         if (n % 2 == 0) buf[n / 2].im = 0;
         FFT_EXEC(pt, +1, buf, work);
-        for (int it = 0; it < nt; it++) d[it] = (IMG_T)buf[it].re;
+        /* nt > n (padt = 1, odd nt): the reference reads one float past its c2r output there
+           (wem.c:505-507); the periodic continuation of the transform stands in */
+        for (int it = 0; it < nt; it++) d[it] = (IMG_T)buf[it < n ? it : it - n].re;
     }
 }
 

@@ -684,7 +684,7 @@ extern "C" int wem_prepare(wem_ctx *c, const wem_params *pp, const float *vel, c
         SpectraArgs sa{};
         sa.d = P<float>(c->wav);
         sa.ntr = 1;
-        sa.nt = p.nt;
+        sa.nt = std::min(p.nt, nf);  // padt = 1 and an odd nt: f_op transforms nt - 1 samples
         sa.ntfft = nf;
         sa.ifmin = ifmin;
         sa.nwf = nwf;
@@ -1032,7 +1032,8 @@ static int run_migrate3d(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev,
     CK(cudaEventRecord(c->evk[0], st));
     if (c->nwf > 0 && ntr > 0) {
         SpectraArgs sa{};
-        sa.d = d_dev; sa.ntr = (int)ntr; sa.nt = p.nt; sa.ntfft = c->nf; sa.ifmin = c->ifmin; sa.nwf = c->nwf;
+        sa.d = d_dev; sa.ntr = (int)ntr; sa.nt = std::min(p.nt, c->nf); sa.ld = p.nt; sa.ntfft = c->nf;
+        sa.ifmin = c->ifmin; sa.nwf = c->nwf;
         sa.out_base = P<int64_t>(c->tbase); sa.out_fstride = n; sa.wtab = P<float2>(c->wtab);
         sa.scale = P<float>(c->scale_recv); sa.out = P<float2>(c->recv);
         if (launch_spectra(sa, st)) return fail(WEM_ERR_CUDA, "spectra launch: %s", cudaGetErrorString(cudaGetLastError()));
@@ -1157,7 +1158,8 @@ static int enqueue_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_de
         SpectraArgs sa{};
         sa.d = d_dev;
         sa.ntr = (int)ntr;
-        sa.nt = p.nt;
+        sa.nt = std::min(p.nt, c->nf);  // the samples f_op transforms (wem.c:490-493)
+        sa.ld = p.nt;
         sa.ntfft = c->nf;
         sa.ifmin = c->ifmin;
         sa.nwf = c->nwf;

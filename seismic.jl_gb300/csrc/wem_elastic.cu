@@ -284,7 +284,7 @@ extern "C" WEM_API int wem_elastic(int device, const wem_params *pp, const float
         SpectraArgs sa{};
         // f_op's r2c of length (nw - 1) * 2 (ewem.c:465-471); with padt = 1 and an odd nt that is
         // one sample short of nt, and the reference writes past its buffer: the last sample is left out
-        sa.d = d_wav; sa.ntr = 1; sa.nt = std::min(nt, nf); sa.ntfft = nf; sa.ifmin = ifmin; sa.nwf = nwf;
+        sa.d = d_wav; sa.ntr = 1; sa.nt = std::min(nt, nf); sa.ld = nt; sa.ntfft = nf; sa.ifmin = ifmin; sa.nwf = nwf;
         sa.out_base = d_zero; sa.out_fstride = 1; sa.wtab = d_wtab; sa.scale = d_scin; sa.out = d_srcw;
         if (launch_spectra(sa, st)) return set_error(WEM_ERR_CUDA, "wem_elastic: wavelet spectrum launch");
         if (adj) {

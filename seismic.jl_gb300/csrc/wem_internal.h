@@ -77,8 +77,9 @@ constexpr int WHOLE_MAX = 4;
 constexpr int WPOS_STRIDE = 8;  // ints per depth in wpos (count, positions, padding to 32 bytes)
 
 struct SpectraArgs {
-    const float *d;        // [ntr][nt]
-    int ntr, nt, ntfft;
+    const float *d;        // [ntr][ld] (ld = 0: nt)
+    int ntr, nt, ntfft;    // nt: samples transformed, at most ntfft (f_op's r2c reads ntfft samples, wem.c:490-493)
+    int ld;                // row stride of d in samples
     int ifmin, nwf;
     const int64_t *out_base;  // [ntr] element offset of (row, iwi = 0) in out
     int64_t out_fstride;      // element stride between consecutive frequencies

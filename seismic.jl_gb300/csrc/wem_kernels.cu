@@ -46,7 +46,7 @@ __global__ void __launch_bounds__(256) wem_spectra_kernel(const SpectraArgs a)
         for (int e = tid; e < TR * KC; e += 256) {
             const int i = e / KC, k = e - i * KC;
             const int tr = tr0 + i, ts = k0 + k;
-            s_d[i][k] = (tr < a.ntr && ts < a.nt) ? a.d[(size_t)tr * a.nt + ts] : 0.f;
+            s_d[i][k] = (tr < a.ntr && ts < a.nt) ? a.d[(size_t)tr * (a.ld ? a.ld : a.nt) + ts] : 0.f;
         }
         for (int e = tid; e < KC * FQ; e += 256) {
             const int k = e / FQ, f = e - k * FQ;

@@ -412,7 +412,8 @@ extern "C" WEM_API int wem_migrate_noalloc(const wem_params *pp, const float *ve
     if (cudaGetLastError() != cudaSuccess) return set_error(WEM_ERR_CUDA, "table kernel launch failed");
     if (nwf > 0) {
         SpectraArgs sa{};
-        sa.d = wav_dev; sa.ntr = 1; sa.nt = p.nt; sa.ntfft = nf; sa.ifmin = ifmin; sa.nwf = nwf;
+        sa.d = wav_dev; sa.ntr = 1; sa.nt = p.nt < nf ? p.nt : nf; sa.ld = p.nt; sa.ntfft = nf; sa.ifmin = ifmin;
+        sa.nwf = nwf;
         sa.out_base = NA(int64_t, wbase); sa.out_fstride = 1; sa.wtab = NA(float2, wtab);
         sa.scale = NA(float, ssrc); sa.out = NA(float2, srcw);
         if (launch_spectra(sa, st)) return set_error(WEM_ERR_CUDA, "wavelet spectrum launch failed");

@@ -27,6 +27,20 @@ def test_wem_dropin_matches_reference_golden(gpu_lib, case):
     assert rel_l2(m, g["m_ref"]) < TOL
 
 
+@pytest.mark.parametrize("case", ["pspi_64_nt97_padt1", "ss_64_nt97_padt1"])
+def test_odd_trace_length_with_padt1_matches_reference_golden(gpu_lib, case):
+    """padt = 1 with an odd nt: the transform is one sample shorter than the trace, so the last
+    sample takes no part in migration (wem.c:490-493); modelled traces match the reference on
+    every sample but the last (the reference reads past its buffer there, wem.c:505-507)."""
+    g = load_golden(f"wem_{case}.npz")
+    p = g["params"]
+    assert p["nt"] % 2 == 1 and p["padt"] == 1
+    m = gpu_lib.wem_dropin(p, g["vel"], g["wav"], d=g["d"], adj=True)
+    assert rel_l2(m, g["m_ref"]) < TOL
+    d = gpu_lib.wem_dropin(p, g["vel"], g["wav"], m=g["m_in"], adj=False)
+    assert rel_l2(d[:, :-1], g["d_ref"][:, :-1]) < TOL
+
+
 def _port_stack(oracle_mod, p, vel, wav, shots, fp64=False):
     from wemgpu import synth
     op = oracle_mod.wem_fp64 if fp64 else oracle_mod.wem_port

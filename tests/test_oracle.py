@@ -84,6 +84,36 @@ def test_port_bitwise_vs_compiled_reference(oracle_mod, case):
     assert np.array_equal(d, d_ref)
 
 
+# padt = 1 with an odd nt (ntfft = nt - 1): the reference's modelling reads one float past its
+# c2r output for the last sample (wem.c:505-507), so these compare every sample but that one
+ODD_NT_CASES = ["pspi_64_nt97_padt1", "ss_64_nt97_padt1"]
+
+
+@pytest.mark.parametrize("case", ODD_NT_CASES)
+def test_port_odd_trace_length_with_padt1(oracle_mod, case):
+    """The last sample of the trace takes no part in migration (f_op's r2c reads ntfft = nt - 1
+    samples, wem.c:490-493): the port's image equals the reference's golden image, and its
+    modelled traces equal the reference's on every sample but the last."""
+    g = load_golden(f"wem_{case}.npz")
+    p = g["params"]
+    assert p["nt"] % 2 == 1 and p["padt"] == 1
+    m = oracle_mod.wem_port(p, g["vel"], g["wav"], d=g["d"], adj=True, nthreads=4)
+    assert rel_l2(m, g["m_ref"]) < 1e-5
+    d = oracle_mod.wem_port(p, g["vel"], g["wav"], m=g["m_in"], adj=False, nthreads=4)
+    assert rel_l2(d[:, :-1], g["d_ref"][:, :-1]) < 1e-5
+
+
+@pytest.mark.skipif(not __import__("oracle").ref_sources_available(), reason="reference sources absent")
+@pytest.mark.parametrize("case", ODD_NT_CASES)
+def test_port_bitwise_vs_compiled_reference_odd_nt(oracle_mod, case):
+    oracle_mod.build_ref()
+    nthr = oracle_mod.omp_threads()
+    g = load_golden(f"wem_{case}.npz")
+    p = g["params"]
+    m_ref = oracle_mod.wem_ref(p, g["vel"], g["wav"], d=g["d"], adj=True)
+    assert np.array_equal(oracle_mod.wem_port(p, g["vel"], g["wav"], d=g["d"], adj=True, nthreads=nthr), m_ref)
+
+
 @pytest.mark.parametrize("case", ["ss_64", "pspi_64", "pspi_64_padx1"])
 @pytest.mark.parametrize("interp", [0, 1])
 def test_fp64_oracles_agree(oracle_mod, case, interp):
