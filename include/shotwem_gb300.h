@@ -183,7 +183,9 @@ WEM_API int wem_last_launch(wem_ctx *ctx, int *threads, int *shots_per_cta, int 
    reference; the autotuner's choice): *form 0 FP32 with one inverse transform per
    reference velocity, 1 split16 (tensor-core DFT stages), 2 FP32 paired (two references'
    real parts per inverse transform, PSPI nearest-lower mode), 3 FP32 on power-of-two rows
-   carrying a transform length that is not a power of two (Bluestein); *bulk_tables 1 when
+   carrying a transform length that is not a power of two (Bluestein), 4 FP32 PSPI with the
+   phase tables read from device memory (rows of 1024 points and up, chosen only when the
+   reference velocities' tables do not fit in shared memory); *bulk_tables 1 when
    the precomputed phase tables reached shared memory by bulk copies (TMA engine), 0 by
    per-thread asynchronous copies or built in each CTA. */
 WEM_API int wem_last_launch_form(wem_ctx *ctx, int *form, int *bulk_tables);

@@ -803,6 +803,15 @@ static int mig_form(const wem_ctx *c, int wide)
             (int)smem <= c->max_smem)
             return MIG_FORM_PAIRED;
     }
+    if (p.pspi && c->use_ptab && c->nfft >= 1024) {
+        // reference counts whose phase tables do not fit in shared memory beside the rows:
+        // the tables are read from the precomputed ones in device memory
+        int S, th;
+        size_t smem;
+        if (migrate_config(c->nfft, wide, p.pspi, p.interp, p.nmx, p.nref, &S, &th, &smem, MIG_FORM_FP32) ||
+            (int)smem > c->max_smem)
+            return MIG_FORM_GT;
+    }
     return MIG_FORM_FP32;
 }
 static std::mutex g_tune_mu;
@@ -882,6 +891,7 @@ static int trial_rate(wem_ctx *c, int nshot, int wide, double *rate)
     const int ngroups = (nshot + S - 1) / S;
     const int ngroups_t = std::min(ngroups, cap);
     const bool tables = alloc_phase_tables(c);
+    if (form == MIG_FORM_GT && !tables) return WEM_OK;  // that form reads the precomputed tables
     const int nwf_t = std::max(1, std::min(tables ? c->ptab_nc : c->nwf, cap / ngroups_t));
     const int items = ngroups_t * nwf_t;  // <= cap: one wave
     int rc;
@@ -923,15 +933,19 @@ static int choose_launch(wem_ctx *c, int nshot, int *wide)
     const bool tma_ok = c->tma_env && p.pspi && c->use_ptab;
     c->paired = paired_ok;
     c->use_tma = tma_ok;
-    auto fits = [&](int w) {
+    // fits(w, 0): the shape runs with the phase tables in shared memory; fits(w, 1): in any form
+    auto fits = [&](int w, bool any) {
         int S, th;
         size_t smem;
-        return !migrate_config(c->nfft, w, p.pspi, p.interp, p.nmx, p.nref, &S, &th, &smem, mig_form(c, w)) &&
+        const int form = mig_form(c, w);
+        if (form == MIG_FORM_GT && !any) return false;
+        return !migrate_config(c->nfft, w, p.pspi, p.interp, p.nmx, p.nref, &S, &th, &smem, form) &&
                (int)smem <= c->max_smem;
     };
-    const bool wide_fits = fits(1);
+    const bool wide_fits = fits(1, true);
     c->last_tuned = 0;
-    *wide = shape_env == 1 ? 0 : (wide_fits ? 1 : 0);
+    // untuned: the wide shape, unless only the narrow one keeps the tables in shared memory
+    *wide = shape_env == 1 ? 0 : (wide_fits && (fits(1, false) || !fits(0, false)) ? 1 : 0);
     const char *t = getenv("WEM_AUTOTUNE");
     if ((t && !strcmp(t, "0")) || c->nwf < 1) return WEM_OK;
     {
@@ -1229,6 +1243,9 @@ static int run_migrate(wem_ctx *c, int nshot, int64_t ntr, const float *d_dev, f
         (rc = ensure(c->slots, sizeof(float2) * (size_t)grid * nz * nmx)))
         return rc;
     c->ptab_ok = alloc_phase_tables(c);
+    if (form == MIG_FORM_GT && !c->ptab_ok)
+        return fail(WEM_ERR_SIZE, "nref=%d: the phase tables fit neither in shared memory (%zu B per CTA, device "
+                    "limit %d B) nor in device memory", p.nref, smem, c->max_smem);
     c->last_form = form;
     c->last_tma = c->ptab_ok && c->use_tma && p.pspi ? 1 : 0;
     c->last_threads = threads;

@@ -212,7 +212,9 @@ int launch_angles_accum(const AngleAccumArgs &a, cudaStream_t st);
 // paired (FP32, PSPI nearest-lower mode: two references' real parts per inverse transform);
 // Bluestein (FP32, transform length nkx not a power of two, on rows of the power of two
 // N >= 2 nkx - 1; the nkx argument of the dispatch functions below is that N).
-constexpr int MIG_FORM_FP32 = 0, MIG_FORM_SPLIT16 = 1, MIG_FORM_PAIRED = 2, MIG_FORM_BLU = 3;
+// MIG_FORM_GT: PSPI FP32 with the phase tables read from device memory (nkx >= 1024), for
+// reference counts whose tables do not fit in shared memory
+constexpr int MIG_FORM_FP32 = 0, MIG_FORM_SPLIT16 = 1, MIG_FORM_PAIRED = 2, MIG_FORM_BLU = 3, MIG_FORM_GT = 4;
 int migrate_config(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *shots_per_cta, int *threads,
                    size_t *smem, int form = MIG_FORM_FP32);
 int migrate_max_grid(int nkx, int wide, int pspi, int interp, int nmx, int nref, int *blocks_per_sm,

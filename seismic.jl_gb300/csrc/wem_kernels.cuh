@@ -19,16 +19,21 @@ namespace gbwem {
 // spectrum buffer per team in place of the selection accumulator.
 // BLU (FP32): transforms of length a.nlog (not a power of two) on rows of N samples,
 // N >= 2 a.nlog - 1, in Bluestein's chirp form (xform in wem_step.cuh).
-template <int N, bool PSPI, int INTERP, int S, bool TC = false, bool PAIR = false, bool BLU = false>
+// GT (PSPI FP32, one transform per reference): the depth's phase tables are read from the
+// precomputed tables in device memory (through L2) instead of being copied into shared
+// memory, for reference counts whose tables do not fit there (a.ptab required).
+template <int N, bool PSPI, int INTERP, int S, bool TC = false, bool PAIR = false, bool BLU = false, bool GT = false>
 __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const MigArgs a)
 {
     static_assert(!PAIR || (PSPI && INTERP == 0 && !TC), "paired transforms: PSPI nearest-lower mode, FP32");
     static_assert(!BLU || (!PAIR && !TC), "Bluestein rows: FP32, one transform per reference");
+    static_assert(!GT || (PSPI && !PAIR && !TC && !BLU), "tables in device memory: PSPI FP32, one transform per reference");
     using SH = MigShape<N>;
     constexpr int T = SH::T, PADN = SH::PADN;
     constexpr int NT = 2 * S * T;
     extern __shared__ float4 smem_raw[];
-    const Smem<N, PSPI, BLU> sm(smem_raw, a.nref, a.nmx, 2 * S, PAIR);
+    const Smem<N, PSPI, BLU> sm(smem_raw, GT ? 0 : a.nref, a.nmx, 2 * S, PAIR);
+    if (GT && !a.ptab) return;  // the host launches this form only with the tables in place
 
     const int tid = threadIdx.x;
     const int team = tid / T, t = tid - team * T;
@@ -134,12 +139,13 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                 // buffers are no longer read); the depth's reference masks are loaded before
                 // the barrier, which hides their latency
                 const unsigned long long um = ref_mask(a, iz), cm = PAIR ? cx_mask(a, iz) : 0ull;
+                const unsigned long long cu = GT ? 0ull : um;  // the phase tables copied (GT: none)
                 __syncthreads();
                 if constexpr (PSPI) {
                     if (tma) {
-                        if (tid == 0 && !s_tabort) copy_tables_bulk<N, INTERP, PAIR>(a, sm, iwi, iz, um, smem_u32(&s_tbar));
+                        if (tid == 0 && !s_tabort) copy_tables_bulk<N, INTERP, PAIR>(a, sm, iwi, iz, cu, smem_u32(&s_tbar));
                     } else {
-                        copy_tables_async<N, INTERP, PAIR>(a, sm, iwi, iz, tid, NT, um);
+                        copy_tables_async<N, INTERP, PAIR>(a, sm, iwi, iz, tid, NT, cu);
                     }
                     float inv_s = 1.f;
                     if (active) {
@@ -160,10 +166,15 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                     else cp_async_wait_all();
                     __syncthreads();
                     if (active) {
-                        if constexpr (PAIR)
+                        if constexpr (PAIR) {
                             paired_inverse<N>(v, is_src, a, sm, xbuf, sacc, t, sync, um, cm);
-                        else
+                        } else if constexpr (GT) {
+                            Smem<N, PSPI, BLU> smg = sm;  // the depth's tables where they lie in device memory
+                            smg.ph = const_cast<float2 *>(a.ptab) + ((size_t)iwi * a.nz + iz) * a.nref * SH::PHS;
+                            step_mig_tail<N, PSPI, INTERP, TC>(v, is_src, a, smg, xbuf, sacc, t, sync, &tc, um, inv_s);
+                        } else {
                             step_mig_tail<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc, um, inv_s);
+                        }
                     }
                 }
             } else {
@@ -366,10 +377,10 @@ template <int N> struct Shapes {
     static constexpr int S_MODEL = (T >= 256) ? 1 : (256 / T > 16 ? 16 : 256 / T);
 };
 
-template <int N, bool PSPI, int INTERP, int S, bool TC, bool PAIR = false, bool BLU = false>
+template <int N, bool PSPI, int INTERP, int S, bool TC, bool PAIR = false, bool BLU = false, bool GT = false>
 int mig_run(const MigArgs *a, int grid, size_t smem, cudaStream_t st, int *bps)
 {
-    auto k = wem_migrate_kernel<N, PSPI, INTERP, S, TC, PAIR, BLU>;
+    auto k = wem_migrate_kernel<N, PSPI, INTERP, S, TC, PAIR, BLU, GT>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
     if (bps) return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bps, k, 2 * S * (N / 16), smem) == cudaSuccess ? 0 : -1;
     k<<<grid, 2 * S * (N / 16), smem, st>>>(*a);
@@ -404,6 +415,21 @@ int mig_launch(int wide, int pspi, int interp, int nref, int nmx, const MigArgs 
         if (!wide) return -2;
         if (!a && !bps) return 0;
         return mig_sel<N, SH::S_WIDE, false, true>(pspi, interp, a, grid, *smem, st, bps);
+    }
+    if (form == MIG_FORM_GT) {
+        if constexpr (N >= 1024) {
+            if (!pspi) return -2;
+            *smem = mig_smem_bytes<N>(true, 0, nmx, 2 * s_);  // no phase tables in shared memory
+            if (!a && !bps) return 0;
+            if (interp == 0) {
+                if (wide) return mig_run<N, true, 0, SH::S_WIDE, false, false, false, true>(a, grid, *smem, st, bps);
+                return mig_run<N, true, 0, SH::S_NARROW, false, false, false, true>(a, grid, *smem, st, bps);
+            }
+            if (wide) return mig_run<N, true, 1, SH::S_WIDE, false, false, false, true>(a, grid, *smem, st, bps);
+            return mig_run<N, true, 1, SH::S_NARROW, false, false, false, true>(a, grid, *smem, st, bps);
+        } else {
+            return -2;
+        }
     }
     if (form == MIG_FORM_PAIRED) {
         if (!pspi || interp != 0) return -2;

@@ -193,7 +193,7 @@ class Context:
         out = dict(zip(["threads", "shots_per_cta", "grid", "graph_replayed", "tuned"], [x.value for x in v]))
         f, b = C.c_int(), C.c_int()
         L.check(L.lib().wem_last_launch_form(self._h, C.byref(f), C.byref(b)))
-        out["form"] = {0: "fp32", 1: "split16", 2: "fp32-paired", 3: "fp32-bluestein"}.get(f.value, str(f.value))
+        out["form"] = {0: "fp32", 1: "split16", 2: "fp32-paired", 3: "fp32-bluestein", 4: "fp32-device-tables"}.get(f.value, str(f.value))
         out["bulk_table_copies"] = b.value
         return out
 

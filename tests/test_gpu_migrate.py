@@ -111,22 +111,56 @@ def test_row_length_limits(gpu_lib):
             assert e.value.code == WEM_ERR_SIZE
 
 
+# (nmx, nref, whether the tables leave shared memory: True when neither CTA shape holds them,
+# False when both do, None when only the narrow one does and the autotuner decides); padx = 2,
+# so rows of 2 nmx points. Shared memory holds up to 41 / 29 references (narrow / wide shape)
+# at 1024 points, 19 / 13 at 2048, 5 at 4096.
+MANY_REF_CASES = [(512, 24, False), (512, 64, True), (1024, 12, False), (1024, 16, None), (1024, 40, True),
+                  (1024, 64, True), (2048, 5, False), (2048, 24, True), (2048, 64, True)]
+
+
 @pytest.mark.parametrize("interp", ["ref", "linear"])
-def test_many_reference_velocities_at_2048(gpu_lib, oracle_mod, interp):
-    """2048-point rows keep the phase tables of every reference velocity in shared memory:
-    16 references fit (one shot per CTA) and match the port; 40 do not, and the call is
-    refused with WEM_ERR_SIZE instead of running anything."""
+@pytest.mark.parametrize("nmx,nref,device_tables", MANY_REF_CASES)
+def test_many_reference_velocities(gpu_lib, oracle_mod, interp, nmx, nref, device_tables):
+    """Rows of 1024, 2048 and 4096 points: reference counts whose phase tables fit in shared
+    memory beside the rows keep them there; larger counts (up to the reference's 64) read the
+    precomputed tables in device memory instead. Every count matches the port."""
+    from wemgpu import synth
+    c = synth.small_case(83, nx=nmx, nz=6, nt=64, nshot=2, pspi=1, nref=nref, interp=interp, fmax=20.0)
+    p = c["params"]
+    assert p["nmx"] * p["padx"] == 2 * nmx and p["nref"] == nref
+    with gpu_lib.Context() as ctx:
+        m = ctx.prepare(p, c["vel"], c["wav"]).migrate(c["shots"])
+        form = ctx.last_launch().get("form")
+    want = _port_stack(oracle_mod, p, c["vel"], c["wav"], c["shots"])
+    assert rel_l2(m, want) < TOL, (nref, form, rel_l2(m, want))
+    if device_tables is not None:
+        assert (form == "fp32-device-tables") == device_tables, (nref, form)
+
+
+def test_untuned_shape_keeps_tables_in_shared_memory(gpu_lib, monkeypatch):
+    """Without the autotuner the launch takes the wide CTA shape unless only the narrow one
+    holds the phase tables in shared memory: 16 references at 2048 points run narrow."""
+    from wemgpu import synth
+    monkeypatch.setenv("WEM_AUTOTUNE", "0")
+    c = synth.small_case(83, nx=1024, nz=6, nt=64, nshot=2, pspi=1, nref=16, interp="ref", fmax=20.0)
+    with gpu_lib.Context() as ctx:
+        ctx.prepare(c["params"], c["vel"], c["wav"]).migrate(c["shots"])
+        ll = ctx.last_launch()
+    assert ll["threads"] == 256 and ll["form"] != "fp32-device-tables", ll
+
+
+def test_many_reference_velocities_without_tables(gpu_lib, monkeypatch):
+    """With the precomputed tables switched off (WEM_PHASE_TABLES=0) the depth kernel builds
+    each depth's tables in shared memory, so 40 references at 2048 points do not fit and the
+    call is refused with WEM_ERR_SIZE instead of running."""
     from wemgpu import synth
     from wemgpu._lib import WemError, WEM_ERR_SIZE
-    c = synth.small_case(83, nx=1024, nz=6, nt=64, nshot=2, pspi=1, nref=16, interp=interp, fmax=20.0)
-    p = c["params"]
-    assert p["nmx"] * p["padx"] == 2048 and p["nref"] == 16
-    m = gpu_lib.migrate(p, c["vel"], c["wav"], c["shots"])
-    want = _port_stack(oracle_mod, p, c["vel"], c["wav"], c["shots"])
-    assert rel_l2(m, want) < TOL
+    monkeypatch.setenv("WEM_PHASE_TABLES", "0")
+    c = synth.small_case(83, nx=1024, nz=6, nt=64, nshot=2, pspi=1, nref=40, interp="ref", fmax=20.0)
     with gpu_lib.Context() as ctx:
         with pytest.raises(WemError) as e:
-            ctx.prepare(dict(p, nref=40), c["vel"], c["wav"]).migrate(c["shots"])
+            ctx.prepare(c["params"], c["vel"], c["wav"]).migrate(c["shots"])
         assert e.value.code == WEM_ERR_SIZE
 
 
