@@ -212,7 +212,7 @@ WEM_API int wem_ctx_stream(wem_ctx *ctx, void **stream);
    larger surveys return WEM_ERR_SIZE. Every call looks up the array's device address on
    the current device (the first call on a device also loads it there); make that first
    call before any stream capture. Each call waits for its stream (cudaStreamSynchronize)
-   before it returns, so a call cannot itself be captured into a CUDA graph. Calls share the array: calls that overlap on the GPU (other
+   before it returns. Calls share the array: calls that overlap on the GPU (other
    streams, other host threads) race and corrupt each other. The image is summed with
    atomic additions, so its last bits can vary from run to run. */
 WEM_API int wem_migrate_noalloc(const wem_params *p, const float *vel_dev, const float *wav_dev, int nshot,
