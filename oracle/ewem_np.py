@@ -224,3 +224,144 @@ def ewem(p: dict, vp, vs, wav, ux=None, uz=None, mpp=None, mps2=None, adj: bool 
         full[:, :nw] = U
         return np.fft.irfft(full, nf, axis=1)[:, :nt] * nf
     return synth(UXo), np.zeros((nmx, nt)), synth(UZo)
+
+
+# ------------------------------------------------------------------ 3-D grids (nmy > 1)
+# The same operator on (x, y) planes with the reference's rank-2 transforms (ewem.c:84-96):
+# the separation and recombination use kx alone, broadcast over ky (ewem.c:596-611, 680-695);
+# ssop's phase uses kx and ky (ewem.c:412-421); boundary_condition tapers both axes.
+
+def _pad2(d, nkx, nky):
+    a = np.zeros((nkx, nky), complex)
+    a[:d.shape[0], :d.shape[1]] = d
+    return a
+
+
+def ssop3(d, w, kx, ky, nkx, nky, po, pd, dz, tap, adj):
+    """ewem.c:368-456 on one plane [nmx, nmy] of depth iz."""
+    nmx, nmy = d.shape
+    s_ = math.sqrt(nkx * nky)
+    if adj:
+        a = _pad2(d, nkx, nky)
+    else:
+        d = d * tap
+        a = _pad2(d * np.exp(1j * w * pd * dz), nkx, nky)
+    A = np.fft.fft2(a)
+    s = (w * w) * (po * po) - kx[:, None] ** 2 - ky[None, :] ** 2
+    L = np.where(s >= 0, np.exp(1j * np.sqrt(np.abs(s)) * dz), np.exp(-0.2 * np.sqrt(np.abs(s)) * abs(dz)))
+    b = np.fft.ifft2(A * L / s_) * (nkx * nky)
+    if adj:
+        return b[:nmx, :nmy] * np.exp(1j * w * pd * dz) / s_ * tap
+    return b[:nmx, :nmy] / s_
+
+
+def _mix3(a0, a1, w, kx, nkx, nky, vp, vs, adj, sep):
+    nmx, nmy = a0.shape
+    s_ = math.sqrt(nkx * nky)
+    k0 = np.fft.fft2(_pad2(a0, nkx, nky)) / s_
+    k1 = np.fft.fft2(_pad2(a1, nkx, nky)) / s_
+    kxp, kzp, kxs, kzs, norm, on = (q[:, None] for q in separation(w, kx, vp, vs))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        if sep:
+            if adj:
+                o0, o1 = kxp * k0 + kzp * k1, -kzs * k0 + kxs * k1
+            else:
+                o0, o1 = (kxs * k0 + kzs * k1) / norm, (-kzp * k0 + kxp * k1) / norm
+        else:
+            if not adj:
+                o0, o1 = kxp * k0 - kzs * k1, kzp * k0 + kxs * k1
+            else:
+                o0, o1 = (kxs * k0 - kzp * k1) / norm, (kzs * k0 + kxp * k1) / norm
+    o0 = np.where(on, o0, k1)
+    o1 = np.where(on, o1, k0)
+    b0 = np.fft.ifft2(o0) * (nkx * nky) / s_
+    b1 = np.fft.ifft2(o1) * (nkx * nky) / s_
+    return b0[:nmx, :nmy], b1[:nmx, :nmy]
+
+
+def ewem3d(p: dict, vp, vs, wav, ux=None, uz=None, mpp=None, mps2=None, adj: bool = True):
+    """One shot on a 3-D grid. vp, vs [nmx*nmy, nz] (cell = imx*nmy + imy); ux, uz [nmx*nmy, nt]
+    (adj) or mpp, mps2 [nmx*nmy, nz] (forward). Returns (mpp, mps1, mps2) or (ux, uy, uz) in
+    float64 (mps1, uy zero)."""
+    nmx, nmy, nz, nt = int(p["nmx"]), int(p["nmy"]), int(p["nz"]), int(p["nt"])
+    nn = nmx * nmy
+    ntfft, nw, ifmin, ifmax, nkx = grids(p)
+    nky = int(p.get("padx", 1)) * nmy
+    dmx, dmy, dz, dt = float(p["dmx"]), float(p["dmy"]), float(p["dz"]), float(p["dt"])
+    dkx = float(f32(2 * math.pi / f32(nkx) / f32(dmx)))
+    dky = float(f32(2 * math.pi / f32(nky) / f32(dmy)))
+    dw = float(f32(2 * math.pi / f32(ntfft) / f32(dt)))
+    kx, ky = kx_signed(nkx, dkx), kx_signed(nky, dky)
+    vp = np.asarray(vp, np.float64).reshape(nn, nz)
+    vs = np.asarray(vs, np.float64).reshape(nn, nz)
+    po_p = 1.0 / vp.mean(axis=0)
+    po_s = 1.0 / vs.mean(axis=0)
+    pd_p = (1.0 / vp - po_p[None, :]).reshape(nmx, nmy, nz)
+    pd_s = (1.0 / vs - po_s[None, :]).reshape(nmx, nmy, nz)
+    tap = taper(nmx)[:, None] * taper(nmy)[None, :]
+    igx = int(math.trunc(float(f32((f32(p["sx"]) - f32(p.get("omx", 0.0))) / f32(dmx)))))
+    igy = int(math.trunc(float(f32((f32(p["sy"]) - f32(p.get("omy", 0.0))) / f32(dmy)))))
+    w0 = np.zeros(ntfft)
+    w0[:nt] = np.asarray(wav, np.float64)[:nt]
+    W = np.fft.rfft(w0)[:nw]
+    max_source = np.max(np.abs(np.asarray(wav, np.float64)[:nt])) / math.sqrt(ntfft)
+    oz, sz, gz = float(p.get("oz", 0.0)), float(p.get("sz", 0.0)), float(p.get("gz", 0.0))
+    zs = [oz + dz * iz for iz in range(nz)]
+    if adj:
+        def spec(u):
+            d = np.zeros((nn, ntfft))
+            d[:, :nt] = np.asarray(u, np.float64)
+            return np.fft.rfft(d, axis=1)[:, :nw].reshape(nmx, nmy, nw)
+        UX, UZ = spec(ux), spec(uz)
+        m_pp = np.zeros((nmx, nmy, nz))
+        m_s2 = np.zeros((nmx, nmy, nz))
+    else:
+        UXo = np.zeros((nmx, nmy, nw), complex)
+        UZo = np.zeros((nmx, nmy, nw), complex)
+        mpp = np.asarray(mpp, np.float64).reshape(nmx, nmy, nz)
+        mps2 = np.asarray(mps2, np.float64).reshape(nmx, nmy, nz)
+    for iw in range(ifmin, ifmax):
+        factor = 1.0 if iw == 0 else 2.0
+        w = iw * dw
+        src = np.zeros((nmx, nmy), complex)
+        src[igx, igy] = W[iw] / math.sqrt(ntfft)
+        smig = np.zeros((nmx, nmy, nz), complex)
+        for iz in range(nz):
+            if zs[iz] >= sz:
+                src = ssop3(src, w, kx, ky, nkx, nky, po_p[iz], pd_p[:, :, iz], -dz, tap, True)
+                smig[:, :, iz] = src / max_source
+        if adj:
+            gx = UX[:, :, iw] / math.sqrt(ntfft)
+            gzr = UZ[:, :, iw] / math.sqrt(ntfft)
+            for iz in range(nz):
+                if zs[iz] >= gz:
+                    vpi, vsi = 1.0 / po_p[iz], 1.0 / po_s[iz]
+                    up, us = _mix3(gx, gzr, w, kx, nkx, nky, vpi, vsi, True, True)
+                    up = ssop3(up, w, kx, ky, nkx, nky, po_p[iz], pd_p[:, :, iz], dz, tap, True)
+                    us = ssop3(us, w, kx, ky, nkx, nky, po_s[iz], pd_s[:, :, iz], dz, tap, True)
+                    gx, gzr = _mix3(up, us, w, kx, nkx, nky, vpi, vsi, True, False)
+                    m_pp[:, :, iz] += factor * np.real(np.conj(smig[:, :, iz]) * up)
+                    m_s2[:, :, iz] += factor * np.real(np.conj(smig[:, :, iz]) * us)
+        else:
+            gx = np.zeros((nmx, nmy), complex)
+            gzr = np.zeros((nmx, nmy), complex)
+            for iz in range(nz - 1, -1, -1):
+                if zs[iz] >= gz:
+                    vpi, vsi = 1.0 / po_p[iz], 1.0 / po_s[iz]
+                    up, us = _mix3(gx, gzr, w, kx, nkx, nky, vpi, vsi, False, True)
+                    up = up + smig[:, :, iz] * mpp[:, :, iz]
+                    us = us + smig[:, :, iz] * mps2[:, :, iz]
+                    up = ssop3(up, w, kx, ky, nkx, nky, po_p[iz], pd_p[:, :, iz], -dz, tap, False)
+                    us = ssop3(us, w, kx, ky, nkx, nky, po_s[iz], pd_s[:, :, iz], -dz, tap, False)
+                    gx, gzr = _mix3(up, us, w, kx, nkx, nky, vpi, vsi, False, False)
+            UXo[:, :, iw] = gx / math.sqrt(ntfft)
+            UZo[:, :, iw] = gzr / math.sqrt(ntfft)
+    if adj:
+        return m_pp.reshape(nn, nz), np.zeros((nn, nz)), m_s2.reshape(nn, nz)
+    nf = (nw - 1) * 2
+
+    def synth(U):
+        full = np.zeros((nn, nf // 2 + 1), complex)
+        full[:, :nw] = U.reshape(nn, nw)
+        return np.fft.irfft(full, nf, axis=1)[:, :nt] * nf
+    return synth(UXo), np.zeros((nn, nt)), synth(UZo)

@@ -149,6 +149,47 @@ def ewem_main(only=None):
               float(np.linalg.norm(ux_ref)), float(np.linalg.norm(uz_ref)))
 
 
+# 3-D grids (nmy > 1): (seed, nx, ny, nz, nt, fmax, padx[, sz, gz]); planes of padx*nx x padx*ny
+EWEM3D_CASES = {
+    "ewem3d_32": (51, 32, 32, 8, 64, 40.0, 2),                    # 64 x 64 planes
+    "ewem3d_64x32_buried": (53, 64, 32, 6, 32, 35.0, 2, 15.0, 25.0),  # 128 x 64 planes, source and receivers below the surface
+    "ewem3d_128x32_taper": (54, 128, 32, 4, 32, 30.0, 2),          # 256 x 64 planes, the taper on along x
+}
+# the x component fed to the migration: a mix of the z component and its time shift
+
+
+def ewem3d_ux(uz):
+    return (0.4 * uz + 0.1 * np.roll(uz, 3, axis=1)).astype(np.float32)
+
+
+def ewem3d_main(only=None):
+    """The reference's elastic ewem() on 3-D grids (rank-2 transforms over the x-y planes,
+    ewem.c:84-96), one shot per case, migration and forward."""
+    os.environ.setdefault("OMP_NUM_THREADS", "4")
+    for name, case in EWEM3D_CASES.items():
+        if only and name not in only:
+            continue
+        seed, nx, ny, nz, nt, fmax, padx = case[:7]
+        sz, gz = case[7:9] if len(case) > 7 else (0.0, 0.0)
+        c = synth.small_case3d(seed, nx=nx, ny=ny, nz=nz, nt=nt, nshot=1, pspi=0, fmax=fmax, padx=padx)
+        rng = np.random.default_rng(seed + 200)
+        vp = c["vel"]
+        vs = (vp / 1.8 * (1.0 + 0.05 * rng.standard_normal(vp.shape))).astype(np.float32)
+        p = dict(c["params"], sx=float(c["shots"].sx[0]), sy=float(c["shots"].sy[0]), fmin=3.0, sz=sz, gz=gz)
+        d = synth.shot_gather_full(c["shots"], 0, nx * ny)
+        uz_in = d
+        m_pp, m_s1, m_s2 = O.ewem_ref(p, vp, vs, c["wav"], ux=ewem3d_ux(uz_in), uz=uz_in, adj=True)
+        mpp_in = rng.standard_normal((nx * ny, nz)).astype(np.float32)
+        mps2_in = rng.standard_normal((nx * ny, nz)).astype(np.float32)
+        ux_ref, uy_ref, uz_ref = O.ewem_ref(p, vp, vs, c["wav"], mpp=mpp_in, mps2=mps2_in, adj=False)
+        # ux is not stored: ewem3d_ux(uz) rebuilds it
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), vp=vp, vs=vs, wav=c["wav"], uz=uz_in,
+                            mpp_ref=m_pp, mps2_ref=m_s2, mpp_in=mpp_in, mps2_in=mps2_in, ux_ref=ux_ref,
+                            uz_ref=uz_ref, params=np.array(repr(p)))
+        print(name, "images", float(np.linalg.norm(m_pp)), float(np.linalg.norm(m_s2)), "data",
+              float(np.linalg.norm(ux_ref)), float(np.linalg.norm(uz_ref)))
+
+
 ANGLE_CASES = {
     # name: (seed, nx, nz, nt, fmax); nx > 100 switches the reference's taper on
     "angles_64": (31, 64, 24, 64, 40.0),
@@ -185,6 +226,12 @@ if __name__ == "__main__":
         if O.build_ref() is None:
             sys.exit("reference sources not found")
         ewem_main(set(sys.argv[2].split(",")) if len(sys.argv) > 2 else None)
+    elif sys.argv[1:2] == ["ewem3d"]:
+        # python tests/golden/make_golden.py ewem3d [name,name...]: the 3-D elastic cases
+        O.build()
+        if O.build_ref() is None:
+            sys.exit("reference sources not found")
+        ewem3d_main(set(sys.argv[2].split(",")) if len(sys.argv) > 2 else None)
     elif sys.argv[1:2] == ["--only"]:
         # python tests/golden/make_golden.py --only name[,name...]: those 2-D cases only
         main(set(sys.argv[2].split(",")))
@@ -193,3 +240,4 @@ if __name__ == "__main__":
         subprocess.run([sys.executable, os.path.abspath(__file__), "angles"], check=True,
                        env=dict(os.environ, OMP_NUM_THREADS="1"))
         ewem_main()
+        ewem3d_main()

@@ -195,3 +195,21 @@ def test_elastic_fp64_restatement_matches_reference_golden(case):
     assert rel_l2(m_pp, g["mpp_ref"]) < 1e-5 and rel_l2(m_s2, g["mps2_ref"]) < 1e-5
     ux, _, uz = E.ewem(p, g["vp"], g["vs"], g["wav"], mpp=g["mpp_in"], mps2=g["mps2_in"], adj=False)
     assert rel_l2(ux, g["ux_ref"]) < 1e-5 and rel_l2(uz, g["uz_ref"]) < 1e-5
+
+
+@pytest.mark.parametrize("case", ["ewem3d_32", "ewem3d_64x32_buried", "ewem3d_128x32_taper"])
+def test_elastic3d_fp64_restatement_matches_reference_golden(case):
+    """oracle/ewem_np.py's 3-D form (ewem3d: rank-2 transforms over the x-y planes) vs the
+    reference's own ewem() on 3-D grids, migration and forward operator, at the reference's
+    FP32 rounding level."""
+    import ewem_np as E
+    g = load_golden(f"{case}.npz")
+    p = g["params"]
+    uz = g["uz"]
+    ux = (0.4 * uz + 0.1 * np.roll(uz, 3, axis=1)).astype(np.float32)  # make_golden.py's ewem3d_ux
+    m_pp, _, m_s2 = E.ewem3d(p, g["vp"], g["vs"], g["wav"], ux=ux, uz=uz, adj=True)
+    assert rel_l2(m_pp, g["mpp_ref"]) < 2e-5 and rel_l2(m_s2, g["mps2_ref"]) < 2e-5, (rel_l2(m_pp, g["mpp_ref"]),
+                                                                                   rel_l2(m_s2, g["mps2_ref"]))
+    ux, _, uz = E.ewem3d(p, g["vp"], g["vs"], g["wav"], mpp=g["mpp_in"], mps2=g["mps2_in"], adj=False)
+    assert rel_l2(ux, g["ux_ref"]) < 1e-5 and rel_l2(uz, g["uz_ref"]) < 1e-5, (rel_l2(ux, g["ux_ref"]),
+                                                                             rel_l2(uz, g["uz_ref"]))
