@@ -76,6 +76,11 @@ def survey(workload: str, rank: int, born: str = "gpu"):
         c["params"] = dict(c["params"], fmax=30.0)
         wl = ("2-D elastic migration (ewem): 8 shots, 300x512 grid @10 m, vs = vp/1.8 with a 5% seeded wobble, "
               "5-30 Hz, nt=1500, padx=padt=2, x and z components on every cell")
+    elif workload == "elastic3d":
+        c = synth.small_case3d(1006 + rank, nx=128, ny=128, nz=60, nt=500, nshot=2, pspi=0, fmax=25.0, padx=2)
+        c["params"] = dict(c["params"], fmin=5.0)
+        wl = ("3-D elastic migration (ewem, nmy > 1): 2 shots, 60x128x128 grid @10 m, vs = vp/1.8 with a 5% "
+              "seeded wobble, 5-25 Hz, nt=500, padx=padt=2 (256x256 planes), x and z components on every cell")
     else:
         raise SystemExit(f"unknown workload {workload}")
     if workload in ("survey64", "survey8", "angles8"):
@@ -502,17 +507,19 @@ def run_elastic(args, c, wl, rank, world, local):
     import wemgpu
     from wemgpu import synth
     p, shots = c["params"], c["shots"]
-    nmx, nz, nt = int(p["nmx"]), int(p["nz"]), int(p["nt"])
+    nmx, nmy, nz, nt = int(p["nmx"]), int(p.get("nmy", 1)), int(p["nz"]), int(p["nt"])
+    ncell = nmx * nmy
     rng = np.random.default_rng(2005 + rank)
     vp = c["vel"]
     vs = (vp / 1.8 * (1.0 + 0.05 * rng.standard_normal(vp.shape))).astype(np.float32)
-    uz = np.stack([synth.shot_gather_full(shots, s, nmx) for s in range(shots.nshot)])
+    uz = np.stack([synth.shot_gather_full(shots, s, ncell) for s in range(shots.nshot)])
     ux = (0.5 * np.roll(uz, 3, axis=2)).astype(np.float32)
     sx = np.asarray(shots.sx, np.float32)
+    sy = np.asarray(shots.sy, np.float32)
     nf = band_elastic(p)
     units = len(sx) * nf * nz
     for _ in range(args.warmup):
-        wemgpu.elastic(p, vp, vs, c["wav"], sx, ux=ux, uz=uz, adj=True, device=local)
+        wemgpu.elastic(p, vp, vs, c["wav"], sx, sy, ux=ux, uz=uz, adj=True, device=local)
     sampler = ClockSampler(local)
     torch.cuda.synchronize()
     sampler.start()
@@ -520,49 +527,57 @@ def run_elastic(args, c, wl, rank, world, local):
     L = wemgpu.lib()
     for _ in range(args.steps):
         t0 = time.perf_counter()
-        wemgpu.elastic(p, vp, vs, c["wav"], sx, ux=ux, uz=uz, adj=True, device=local)
+        wemgpu.elastic(p, vp, vs, c["wav"], sx, sy, ux=ux, uz=uz, adj=True, device=local)
         wall.append(time.perf_counter() - t0)
         dev_ms.append(float(L.wem_elastic_last_ms()))
     clocks = sampler.stop()
     ms = statistics.mean(dev_ms)
     nkx = int(p["padx"]) * nmx
-    lg = math.log2(nkx)
-    # launches per step: 3 spectra (wavelet, x, z), the tables, the depth kernel, 2 image reductions
+    npl = nkx * (int(p["padx"]) * nmy if nmy > 1 else 1)  # samples of a padded row (2-D) or plane (3-D)
+    lg = math.log2(npl)
     # algorithmic FLOPs per unit: the source step (2 transforms) and the receiver's separation,
     # two continuations and recombination (10 transforms), 5 N log2 N each, plus ~60 per sample
-    fl = 12 * 5 * nkx * lg + 60 * nkx
+    fl = 12 * 5 * npl * lg + 60 * npl
     ach = units * fl / (ms / 1000.0) / 1e12
     fp32_meas = fp32_peak(local)
-    tr = recorded_traffic("elastic8") if args.fmax is None else None
+    tr = recorded_traffic("elastic8") if args.fmax is None and nmy == 1 else None
     traffic = tr.get("bytes_per_launch") if tr and not tr["stale"] else None
+    if nmy > 1:
+        # per depth step: 3 spectra once, then 6 plane passes (3 row, 3 column) per step and 2 reductions
+        launches = 3 + 6 * nz + 2 + 2
+        kern = "3-D plane passes (wem_e3_rows_kernel, wem_e3_cols_kernel) + spectra + reductions, whole step"
+    else:
+        # 3 spectra (wavelet, x, z), the tables, the depth kernel, 2 image reductions
+        launches = 7
+        kern = "wem_ewem_kernel + tables + spectra + reductions, whole step"
     line = {"metric": "shot*omega*depth-steps/s", "value": world * units / (ms / 1000.0),
             "unit": "shot*omega*depth-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (seeded)", "gpu_launches": args.steps * 7,
+            "data": "synthetic (seeded)", "gpu_launches": args.steps * launches,
             "config": {"workload": wl, "units_per_step_per_gpu": units, "shots": len(sx), "frequencies": nf,
-                       "depth_steps": nz, "nkx": nkx, "l2": "inputs larger than L2"},
+                       "depth_steps": nz, "nkx": nkx, "plane": npl, "l2": "inputs larger than L2"},
             "e2e": {"value": world * units / statistics.mean(wall), "unit": "shot*omega*depth-steps/s",
-                    "h2d_bytes_per_step": int(ux.nbytes + uz.nbytes), "d2h_bytes_per_step": int(2 * nmx * nz * 4)},
+                    "h2d_bytes_per_step": int(ux.nbytes + uz.nbytes), "d2h_bytes_per_step": int(2 * ncell * nz * 4)},
             "roofline": {"bound": "fp32", "achieved": ach, "peak": fp32_meas, "unit": "TFLOP/s",
                          "frac": ach / fp32_meas, "traffic": traffic,
                          "peak_source": "FP32 FMA probe (wem_measure_fp32_peak), measured in this run",
-                         "kernel": "wem_ewem_kernel + tables + spectra + reductions, whole step", "ms_per_launch": ms,
+                         "kernel": kern, "ms_per_launch": ms,
                          "flops_per_unit": fl, "traffic_kernel": "wem_ewem_kernel (DRAM bytes of one launch)"},
             "clocks": clocks}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         # the CPU leg: the oracle's FP64 restatement (NumPy, one thread) on one shot, 2 Hz of the band
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import ewem_np as E
-        q = dict(p, sx=float(sx[len(sx) // 2]), fmax=float(p["fmin"]) + 2.0)
+        q = dict(p, sx=float(sx[len(sx) // 2]), sy=float(sy[len(sx) // 2]), fmax=float(p["fmin"]) + 2.0)
         nq = band_elastic(q)
         s0 = len(sx) // 2
         t0 = time.perf_counter()
-        want = E.ewem(q, vp, vs, c["wav"], ux=ux[s0], uz=uz[s0], adj=True)
+        want = (E.ewem3d if nmy > 1 else E.ewem)(q, vp, vs, c["wav"], ux=ux[s0], uz=uz[s0], adj=True)
         el = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": nq * nz / el, "unit": "shot*omega*depth-steps/s", "cores": 1, "kind": "port",
                                 "sample": f"1 shot, {nq} frequencies x {nz} depth steps in {el:.1f} s "
                                           "(NumPy FP64 restatement, one thread)"}
-        got = wemgpu.elastic(q, vp, vs, c["wav"], [q["sx"]], ux=ux[s0:s0 + 1], uz=uz[s0:s0 + 1], adj=True,
+        got = wemgpu.elastic(q, vp, vs, c["wav"], [q["sx"]], [q["sy"]], ux=ux[s0:s0 + 1], uz=uz[s0:s0 + 1], adj=True,
                              device=local)
         line["accuracy"] = {"rel_l2_p_vs_fp64": float(np.linalg.norm(got[0] - want[0]) / np.linalg.norm(want[0])),
                             "rel_l2_s_vs_fp64": float(np.linalg.norm(got[1] - want[2]) / np.linalg.norm(want[2])),
@@ -772,7 +787,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="survey64",
                     choices=["survey64", "survey8", "survey3d", "survey3d_band", "split1", "lsm32", "angles8",
-                             "elastic8"])
+                             "elastic8", "elastic3d"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "split16"],
@@ -806,7 +821,7 @@ def main():
         wl += f" [band cut to {c['params']['fmin']:g}-{args.fmax:g} Hz]"
     if args.workload == "angles8":
         return run_angles(args, c, wl, rank, world, local)
-    if args.workload == "elastic8":
+    if args.workload in ("elastic8", "elastic3d"):
         return run_elastic(args, c, wl, rank, world, local)
     if args.precision != "fp32":
         c["params"] = dict(c["params"], precision=args.precision)

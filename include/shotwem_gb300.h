@@ -219,12 +219,15 @@ WEM_API int wem_migrate_noalloc(const wem_params *p, const float *vel_dev, const
                                 const float *sx, const float *sy, const float *d_dev, float *m_dev, void *stream);
 
 /* Elastic shot-profile migration (adj = 1) or its forward operator (adj = 0) on `device`:
-   the reference's ewem() (ewem.c:3-253, ewem.h:3-16) for nshot shots at once, 2-D (nmy = 1).
-   vp, vs [nmx][nz]; wav [nt]; ux, uz [nshot][nmx][nt], the x and z components recorded on
-   every grid cell (adj: read; forward: written); mpp, mps2 [nmx][nz], the P and S images
-   (adj: written, stacked over the shots; forward: read). The y component and the S1 image
-   take no part, as in the reference's separation (ewem.c:553-741). padx*nmx a power of two
-   in [64, 2048] or another length in [33, 1024]. Allocates its device memory per call. */
+   the reference's ewem() (ewem.c:3-253, ewem.h:3-16) for nshot shots at once, on 2-D
+   (nmy = 1) and 3-D (nmy > 1) grids. With n = nmx*nmy cells (cell = imx*nmy + imy):
+   vp, vs [n][nz]; wav [nt]; ux, uz [nshot][n][nt], the x and z components recorded on every
+   grid cell (adj: read; forward: written); mpp, mps2 [n][nz], the P and S images (adj:
+   written, stacked over the shots; forward: read); sy is read on 3-D grids (it may be NULL
+   in 2-D). The y component and the S1 image take no part, as in the reference's separation
+   (ewem.c:553-741). 2-D: padx*nmx a power of two in [64, 2048] or another length in
+   [33, 1024]; 3-D: padx*nmx and padx*nmy powers of two in [64, 1024]. Allocates its device
+   memory per call. */
 WEM_API int wem_elastic(int device, const wem_params *p, const float *vp, const float *vs, const float *wav,
                         int nshot, const float *sx, const float *sy, float *ux, float *uz, float *mpp,
                         float *mps2, int adj);

@@ -14,7 +14,8 @@
  * mpp's headers, n1/o1/d1 of the wavelet, gx/gy = mx/my and hx/hy the offsets (shotewem.c:
  * 120-150); uy is zero. Differences, on error paths only: a missing key returns WEM_ERR_ARG
  * instead of exit(1), an unreadable file WEM_ERR_IO, a data file with more traces than the
- * grid is read only up to the grid size, and a 3-D grid (ny > 1) returns WEM_ERR_SIZE.
+ * grid is read only up to the grid size. 3-D grids (ny > 1) run on the x-y plane passes when
+ * padx*nx and padx*ny are powers of two in [64, 1024], and return WEM_ERR_SIZE otherwise.
  */
 #include <math.h>
 #include <stdbool.h>

@@ -1,6 +1,6 @@
 // wem_elastic.cu -- elastic shot-profile migration and its forward operator on the GPU:
 // the reference's ewem / elastic_extrap1f / elastic_separate_3d (src/Imaging/c/ewem.c:3-741),
-// 2-D (nmy = 1, the case its separation handles: it uses kx only, ewem.c:596-611).
+// 2-D grids (nmy = 1) here; 3-D grids (nmy > 1) go to wem_elastic3d.cu.
 //
 // Everything that depends only on (frequency, depth) -- the phase rows of the P and S layer
 // slownesses, the slowness corrections and the separation coefficients of every wavenumber -- is
@@ -30,6 +30,9 @@
 
 namespace gbwem {
 int set_error(int code, const char *msg);  // wem_api.cu: records wem_last_error()
+// wem_elastic3d.cu: the same operator on 3-D grids (nmy > 1)
+int wem_elastic3d(int device, const wem_params &p, const float *vp, const float *vs, const float *wav, int nshot,
+                  const float *sx, const float *sy, float *ux, float *uz, float *mpp, float *mps2, int adj, float *ms);
 }
 void bluestein_tables(int L, int N, float2 *chirp, float2 *gq);  // wem_api.cu
 int row_length_2d(int nkx, bool *blu);                           // wem_api.cu
@@ -133,7 +136,8 @@ extern "C" WEM_API int wem_elastic(int device, const wem_params *pp, const float
     if (!pp || !vp || !vs || !wav || !sx || !ux || !uz || !mpp || !mps2 || nshot < 1)
         return set_error(WEM_ERR_ARG, "wem_elastic: null argument or no shot");
     const wem_params p = *pp;
-    if (p.nmy != 1) return set_error(WEM_ERR_SIZE, "wem_elastic: 2-D grids only (nmy = 1)");
+    if (p.nmy > 1) return wem_elastic3d(device, p, vp, vs, wav, nshot, sx, sy, ux, uz, mpp, mps2, adj, &g_last_ms);
+    if (p.nmy != 1) return set_error(WEM_ERR_ARG, "wem_elastic: nmy must be at least 1");
     if (p.nt < 2 || p.nmx < 2 || p.nz < 1 || p.padt < 1 || p.padx < 1 || !(p.dt > 0) || !(p.dmx > 0))
         return set_error(WEM_ERR_ARG, "wem_elastic: invalid grid");
     const int nmx = p.nmx, nz = p.nz, nt = p.nt;
@@ -386,7 +390,8 @@ extern "C" WEM_API float wem_elastic_last_ms(void) { return g_last_ms; }
 
 // The reference's ewem() (ewem.h:3-16), one shot, float** rows as alloc2float builds them
 // (seismic.c:92-106): adj = true, (ux, uz) -> (mpp, mps2) with mps1 = 0; adj = false, (mpp,
-// mps2) -> (ux, uz) with uy = 0. The y component takes no part (2-D, ewem.c:553-741).
+// mps2) -> (ux, uz) with uy = 0. The y component takes no part (ewem.c:553-741); nmy > 1
+// runs the 3-D form.
 extern "C" WEM_API int ewem(float **ux, float **uy, float **uz, float **mpp, float **mps1, float **mps2, float **wav,
                             int nt, float ot, float dt, int nmx, float omx, float dmx, int nmy, float omy, float dmy,
                             float sx, float sy, int nz, float oz, float dz, float gz, float sz, float **vp, float **vs,

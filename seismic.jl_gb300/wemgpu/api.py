@@ -240,14 +240,15 @@ def wem_dropin(p: dict, vel, wav, d=None, m=None, adj=True) -> np.ndarray:
 
 def elastic(params: dict, vp, vs, wav, sx, sy=None, ux=None, uz=None, mpp=None, mps2=None, adj: bool = True,
             device: int = 0):
-    """Elastic shot-profile migration (adj=True: the x and z components ux, uz [nshot, nmx, nt]
-    recorded on every grid cell -> the P and S images mpp, mps2 [nmx, nz], stacked over the
+    """Elastic shot-profile migration (adj=True: the x and z components ux, uz [nshot, ncell, nt]
+    recorded on every grid cell -> the P and S images mpp, mps2 [ncell, nz], stacked over the
     shots) or its forward operator (adj=False: mpp, mps2 -> ux, uz), wem_elastic (the
-    reference's ewem, src/Imaging/c/ewem.c, 2-D). Returns (mpp, mps2) or (ux, uz)."""
+    reference's ewem, src/Imaging/c/ewem.c). ncell = nmx * nmy, cell = imx * nmy + imy (3-D
+    grids when nmy > 1). Returns (mpp, mps2) or (ux, uz)."""
     p = make_params(**params)
     sx = np.ascontiguousarray(np.atleast_1d(sx), dtype=np.float32)
     sy = np.ascontiguousarray(np.zeros(len(sx)) if sy is None else np.atleast_1d(sy), dtype=np.float32)
-    nshot, nmx, nz, nt = len(sx), p.nmx, p.nz, p.nt
+    nshot, nmx, nz, nt = len(sx), p.nmx * max(p.nmy, 1), p.nz, p.nt
     vp = np.ascontiguousarray(vp, dtype=np.float32)
     vs = np.ascontiguousarray(vs, dtype=np.float32)
     wav = np.ascontiguousarray(wav, dtype=np.float32)

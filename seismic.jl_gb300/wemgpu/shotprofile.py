@@ -336,7 +336,7 @@ def ShotProfileEWEM(m, d, adj: bool = True, *, damping=1000.0, vp="vp.seis", vs=
     one wem_elastic call (per shot where angle gathers need each shot's image); with
     nangx, nangy > 1 the shot images are binned by the shot's incidence angles (the angx/angy
     files of ComputeAngles), the S images with the sign of the angles (ShotProfileEWEM.jl:
-    155-230, 290-350). 2-D grids; mps1 and uy are written as zeros (the separation has no S1
+    155-230, 290-350). 2-D and 3-D grids; mps1 and uy are written as zeros (the separation has no S1
     potential, ewem.c:553-741). Differences, where the reference is ill-defined: traces are
     placed on the grid by their gx/gy headers, and the modelled traces carry gx = ox + dx*imx
     (the reference's per-shot images carry mx = dx*imx, ShotProfileEWEM.jl:274, which

@@ -134,20 +134,23 @@ def test_shotewem_main_on_seis_files(gpu_lib, tmp_path):
 
 
 def test_elastic_edge_cases(gpu_lib):
-    """A source off the grid, a 3-D grid and a row length with no kernel are refused with a
-    status before anything runs. (ewem.c's band arithmetic always leaves at least one
-    frequency, ewem.c:49-57, so there is no empty band to test.)"""
+    """A source off the grid (in x, and in y on a 3-D grid), a row length with no kernel and
+    a 3-D plane whose sides are not powers of two in [64, 1024] are refused with a status
+    before anything runs. (ewem.c's band arithmetic always leaves at least one frequency,
+    ewem.c:49-57, so there is no empty band to test.)"""
     from wemgpu import synth
     from wemgpu._lib import WemError, WEM_ERR_ARG, WEM_ERR_SIZE
     c = synth.small_case(91, nx=64, nz=8, nt=64, nshot=2, pspi=0, fmax=30.0)
     p, shots = c["params"], c["shots"]
-    for q, sx, code in ((p, [1e6, 0.0], WEM_ERR_ARG), (dict(p, nmy=2), shots.sx, WEM_ERR_SIZE),
-                        (dict(p, nmx=16, padx=2), shots.sx, WEM_ERR_SIZE)):
-        n = int(q["nmx"])
-        vp = c["vel"][:n]
+    p3 = dict(p, nmx=32, nmy=32, omy=0.0, dmy=p["dmx"])
+    for q, sx, sy, code in ((p, [1e6, 0.0], None, WEM_ERR_ARG), (dict(p, nmx=16, padx=2), shots.sx, None, WEM_ERR_SIZE),
+                            (dict(p, nmx=40, nmy=4), shots.sx, [0.0, 0.0], WEM_ERR_SIZE),
+                            (p3, [100.0, 100.0], [100.0, 1e6], WEM_ERR_ARG)):
+        n = int(q["nmx"]) * int(q.get("nmy", 1))
+        vp = np.resize(c["vel"], (n, c["vel"].shape[1]))
         zeros = np.zeros((2, n, int(q["nt"])), np.float32)
         with pytest.raises(WemError) as e:
-            gpu_lib.elastic(q, vp, vp / 1.8, c["wav"], sx, ux=zeros, uz=zeros, adj=True)
+            gpu_lib.elastic(q, vp, vp / 1.8, c["wav"], sx, sy=sy, ux=zeros, uz=zeros, adj=True)
         assert e.value.code == code
 
 
@@ -190,3 +193,106 @@ def test_elastic_least_squares_misfit_curve_vs_fp64_pair(gpu_lib):
     print("misfit GPU", cost_gpu, "FP64", cost_cpu)
     assert len(cost_gpu) == len(cost_cpu) == 5
     assert np.all(np.abs(np.asarray(cost_gpu) - cost_cpu) <= 1e-3 * np.maximum(cost_cpu, 1e-3))
+
+
+# ------------------------------------------------------------------ 3-D grids (nmy > 1)
+def _ewem3d_ux(uz):
+    """The x component the 3-D golden cases migrate (tests/golden/make_golden.py, ewem3d_ux)."""
+    return (0.4 * uz + 0.1 * np.roll(uz, 3, axis=1)).astype(np.float32)
+
+
+@pytest.mark.parametrize("case", ["ewem3d_32", "ewem3d_64x32_buried", "ewem3d_128x32_taper"])
+def test_elastic3d_matches_reference_golden(gpu_lib, case):
+    """3-D grids: the reference's ewem() with its rank-2 transforms over the x-y planes
+    (64 x 64, 128 x 64 with the source and receivers below the surface, 256 x 64 with the
+    taper on along x), migration and forward operator."""
+    g = load_golden(f"{case}.npz")
+    p = g["params"]
+    ux = _ewem3d_ux(g["uz"])
+    mpp, mps2 = gpu_lib.elastic(p, g["vp"], g["vs"], g["wav"], [p["sx"]], sy=[p["sy"]], ux=ux[None], uz=g["uz"][None],
+                                adj=True)
+    assert rel_l2(mpp, g["mpp_ref"]) < TOL, rel_l2(mpp, g["mpp_ref"])
+    assert rel_l2(mps2, g["mps2_ref"]) < TOL, rel_l2(mps2, g["mps2_ref"])
+    ux, uz = gpu_lib.elastic(p, g["vp"], g["vs"], g["wav"], [p["sx"]], sy=[p["sy"]], mpp=g["mpp_in"],
+                             mps2=g["mps2_in"], adj=False)
+    assert rel_l2(ux[0], g["ux_ref"]) < TOL, rel_l2(ux[0], g["ux_ref"])
+    assert rel_l2(uz[0], g["uz_ref"]) < TOL, rel_l2(uz[0], g["uz_ref"])
+
+
+def test_ewem_dropin_3d_matches_reference_golden(gpu_lib):
+    """ewem() with the reference's argument list on a 3-D grid (nmy > 1, float** rows of the
+    nmx * nmy cells)."""
+    g = load_golden("ewem3d_32.npz")
+    p = g["params"]
+    L = gpu_lib.lib()
+    fpp = C.POINTER(C.POINTER(C.c_float))
+    L.ewem.restype = C.c_int
+    L.ewem.argtypes = [fpp] * 7 + [C.c_int, C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_int, C.c_float,
+                                   C.c_float, C.c_float, C.c_float, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                                   fpp, fpp, C.c_float, C.c_float, C.c_int, C.c_int, C.c_bool, C.c_bool]
+    n, nt, nz = p["nmx"] * p["nmy"], p["nt"], p["nz"]
+    uz = np.ascontiguousarray(g["uz"], np.float32)
+    ux = _ewem3d_ux(uz)
+    uy = np.full((n, nt), 7.0, np.float32)
+    mpp, mps1, mps2 = (np.full((n, nz), 7.0, np.float32) for _ in range(3))
+    wav = np.ascontiguousarray(g["wav"], np.float32).reshape(1, -1)
+    vp, vs = np.ascontiguousarray(g["vp"], np.float32), np.ascontiguousarray(g["vs"], np.float32)
+    args = [p["nt"], 0.0, p["dt"], p["nmx"], p["omx"], p["dmx"], p["nmy"], p["omy"], p["dmy"], p["sx"], p["sy"], nz,
+            p["oz"], p["dz"], p["gz"], p["sz"], _rows(vp), _rows(vs), p["fmin"], p["fmax"], p["padt"], p["padx"]]
+    rc = L.ewem(_rows(ux), _rows(uy), _rows(uz), _rows(mpp), _rows(mps1), _rows(mps2), _rows(wav), *args, True, False)
+    assert rc == 0
+    assert rel_l2(mpp, g["mpp_ref"]) < TOL and rel_l2(mps2, g["mps2_ref"]) < TOL and not np.any(mps1)
+
+
+@pytest.mark.parametrize("nx,ny,padx,nshot", [(64, 32, 2, 3), (512, 32, 2, 2), (32, 512, 2, 2), (128, 64, 1, 3)])
+def test_elastic3d_shots_stacked_match_fp64_oracle(gpu_lib, nx, ny, padx, nshot):
+    """Several shots in one 3-D call against the FP64 restatement (oracle/ewem_np.py,
+    ewem3d) shot by shot, migration and forward: planes of 128 x 64, 1024 x 64 (the column
+    pass's widest transform), 64 x 1024 (the row pass's) and 128 x 64 without padding."""
+    import ewem_np as E
+    from wemgpu import synth
+    nz = 5  # small_case3d places its scatterers between 3 dz and (nz - 1) dz
+    c = synth.small_case3d(90 + nx + ny, nx=nx, ny=ny, nz=nz, nt=32, nshot=nshot, pspi=0, fmax=30.0, padx=padx)
+    rng = np.random.default_rng(nx + 7 * ny)
+    vp = c["vel"]
+    vs = (vp / 1.7 * (1.0 + 0.05 * rng.standard_normal(vp.shape))).astype(np.float32)
+    p = dict(c["params"], fmin=3.0)
+    shots = c["shots"]
+    uz = np.stack([synth.shot_gather_full(shots, s, nx * ny) for s in range(shots.nshot)])
+    ux = (0.5 * np.roll(uz, 2, axis=2)).astype(np.float32)
+    mpp, mps2 = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, ux=ux, uz=uz, adj=True)
+    want_p = want_s = 0.0
+    for s in range(shots.nshot):
+        q = dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s]))
+        a, _, b = E.ewem3d(q, vp, vs, c["wav"], ux=ux[s], uz=uz[s], adj=True)
+        want_p, want_s = want_p + a, want_s + b
+    assert rel_l2(mpp, want_p) < TOL, rel_l2(mpp, want_p)
+    assert rel_l2(mps2, want_s) < TOL, rel_l2(mps2, want_s)
+    m_in = [rng.standard_normal((nx * ny, nz)).astype(np.float32) for _ in range(2)]
+    gx, gz = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, mpp=m_in[0], mps2=m_in[1], adj=False)
+    for s in range(shots.nshot):
+        q = dict(p, sx=float(shots.sx[s]), sy=float(shots.sy[s]))
+        a, _, b = E.ewem3d(q, vp, vs, c["wav"], mpp=m_in[0], mps2=m_in[1], adj=False)
+        assert rel_l2(gx[s], a) < TOL, (s, rel_l2(gx[s], a))
+        assert rel_l2(gz[s], b) < TOL, (s, rel_l2(gz[s], b))
+
+
+def test_elastic3d_linearity(gpu_lib):
+    """The 3-D migration is linear in the data: twice the data gives exactly twice the images
+    (a power-of-two scale passes every FP32 operation exactly), and the images of the x and z
+    components migrated apart add up to the images of both at once."""
+    from wemgpu import synth
+    c = synth.small_case3d(97, nx=32, ny=32, nz=5, nt=32, nshot=2, pspi=0, fmax=25.0, padx=2)
+    vp = c["vel"]
+    vs = (vp / 1.8).astype(np.float32)
+    p = dict(c["params"], fmin=3.0)
+    shots = c["shots"]
+    uz = np.stack([synth.shot_gather_full(shots, s, 32 * 32) for s in range(shots.nshot)])
+    ux = (0.3 * np.roll(uz, 1, axis=2)).astype(np.float32)
+    a = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, ux=ux, uz=uz, adj=True)
+    b = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, ux=2 * ux, uz=2 * uz, adj=True)
+    assert np.array_equal(2 * a[0], b[0]) and np.array_equal(2 * a[1], b[1])
+    z = np.zeros_like(ux)
+    ax = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, ux=ux, uz=z, adj=True)
+    az = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, ux=z, uz=uz, adj=True)
+    assert rel_l2(ax[0] + az[0], a[0]) < 1e-5 and rel_l2(ax[1] + az[1], a[1]) < 1e-5
