@@ -9,11 +9,10 @@
 //     transform sit the x-domain operations: the crop to the grid (y >= nmy zeroed), the
 //     1/sqrt(nkx nky) scales, the slowness correction exp(i w pd dz) and the boundary taper of
 //     ssop, the imaging condition, and the image injection of the forward operator;
-//   * column passes: transforms along x on tiles of adjacent ky columns staged in shared memory
-//     (coalesced loads and stores), one team of nkx/16 threads per column. Between the forward
-//     and the inverse transform sit the k-domain operations: the separation and recombination
-//     mixes of elastic_separate_3d (per kx, the same for every ky, as in the reference), and the
-//     split-step phase of ssop at (kx, ky).
+//   * column passes: transforms along x, one team of nkx/16 threads per ky column, the teams of
+//     a CTA on adjacent columns. Between the forward and the inverse transform sit the k-domain
+//     operations: the separation and recombination mixes of elastic_separate_3d (per kx, the
+//     same for every ky, as in the reference), and the split-step phase of ssop at (kx, ky).
 // Between passes a plane stays in the (x, ky) form of the y transform, K[item][plane][x][ky] for
 // x < nmx: the rows the reference pads with zeros (x >= nmx) are zero-filled by the column pass,
 // whose inverse transform keeps x < nmx only -- the reference's crop in x.
@@ -92,19 +91,25 @@ __device__ __forceinline__ float2 e3_phase(float w, float po, float kx, float ky
 }
 
 // ------------------------------------------------------------------ row passes (along y)
+// twiddles, one exchange buffer per team, and per team the depth's source row (imaging form)
 template <int NY> __host__ __device__ constexpr size_t e3_rows_smem()
 {
-    return sizeof(float2) * ((size_t)((fft_tw_size<NY>() + 1) & ~1) + (size_t)(E3_THREADS / (NY / 16)) * pad16(NY));
+    return sizeof(float2) *
+           ((size_t)((fft_tw_size<NY>() + 1) & ~1) + (size_t)(E3_THREADS / (NY / 16)) * (pad16(NY) + NY));
 }
 
-template <int NY>
-__global__ void __launch_bounds__(E3_THREADS) wem_e3_rows_kernel(const E3Args a)
+// OP: the row operation (E3R_*), a template parameter so that each form gets its own register
+// budget; two CTAs per SM.
+template <int NY, int OP>
+__global__ void __launch_bounds__(E3_THREADS, 2) wem_e3_rows_kernel(const E3Args a)
 {
     constexpr int T = NY / 16, TEAMS = E3_THREADS / T, TW = fft_tw_size<NY>();
     extern __shared__ float4 e3r_smem[];
     float2 *s_tw = reinterpret_cast<float2 *>(e3r_smem);
     const int tid = threadIdx.x, team = tid / T, t = tid - team * T;
     float2 *xbuf = s_tw + ((TW + 1) & ~1) + (size_t)team * pad16(NY);
+    // the team's source row of the depth (smig / max_source at y = t + T m, entry m T + t)
+    float2 *sm = s_tw + ((TW + 1) & ~1) + (size_t)TEAMS * pad16(NY) + (size_t)team * NY;
     const unsigned sync = team_sync_handle<NY>(tid);
     for (int i = tid; i < TW; i += E3_THREADS) s_tw[i] = a.twy[i];
     __syncthreads();
@@ -130,9 +135,9 @@ __global__ void __launch_bounds__(E3_THREADS) wem_e3_rows_kernel(const E3Args a)
         const float w = __fmul_rn((float)iw, a.dw);
         float2 *Kx = a.K + (size_t)li * 3 * plane + (size_t)x * nky;  // row x of plane 0
         float2 v[16];
-        if (a.op == E3R_LOAD_REC || a.op == E3R_LOAD_SRC) {
+        if (OP == E3R_LOAD_REC || OP == E3R_LOAD_SRC) {
             // the initial planes (ewem.c:109, 295-300): the component spectra, the source spike
-            const int p0 = a.op == E3R_LOAD_REC ? 0 : 2, p1 = a.op == E3R_LOAD_REC ? 1 : 2;
+            const int p0 = OP == E3R_LOAD_REC ? 0 : 2, p1 = OP == E3R_LOAD_REC ? 1 : 2;
             for (int p = p0; p <= p1; p++) {
 #pragma unroll
                 for (int m = 0; m < 16; m++) {
@@ -153,10 +158,9 @@ __global__ void __launch_bounds__(E3_THREADS) wem_e3_rows_kernel(const E3Args a)
             continue;
         }
         // the source at this depth (E3R_IMG, E3R_SRC_STORE): smig = ssop(source) / max_source
-        float2 sm[16];
 #pragma unroll
-        for (int m = 0; m < 16; m++) sm[m] = make_float2(0.f, 0.f);
-        if ((a.op == E3R_IMG || a.op == E3R_SRC_STORE) && (a.mask & 4)) {
+        for (int m = 0; m < 16; m++) sm[T * m + t] = make_float2(0.f, 0.f);
+        if ((OP == E3R_IMG || OP == E3R_SRC_STORE) && (a.mask & 4)) {
             float2 *row = Kx + 2 * plane;
 #pragma unroll
             for (int m = 0; m < 16; m++) v[m] = row[t + T * m];
@@ -171,24 +175,24 @@ __global__ void __launch_bounds__(E3_THREADS) wem_e3_rows_kernel(const E3Args a)
                     const float tp = __fmul_rn(tx, a.tapy[y]);
                     u = make_float2(u.x * a.inv_s * tp, u.y * a.inv_s * tp);
                     v[m] = u;
-                    sm[m] = make_float2(u.x * a.inv_max_source, u.y * a.inv_max_source);
+                    sm[T * m + t] = make_float2(u.x * a.inv_max_source, u.y * a.inv_max_source);
                 } else {
                     v[m] = make_float2(0.f, 0.f);
                 }
             }
-            if (a.op == E3R_SRC_STORE) {
+            if (OP == E3R_SRC_STORE) {
                 float2 *sg = a.smig + ((size_t)li * a.nz) * nn + zc;
 #pragma unroll
                 for (int m = 0; m < 16; m++) {
                     const int y = t + T * m;
-                    if (y < nmy) sg[y] = sm[m];
+                    if (y < nmy) sg[y] = sm[T * m + t];
                 }
             }
             fft_row<NY, -1>(v, xbuf, s_tw, t, sync);
 #pragma unroll
             for (int m = 0; m < 16; m++) row[t + T * m] = v[m];
         }
-        if (a.op == E3R_SRC_STORE) continue;
+        if (OP == E3R_SRC_STORE) continue;
         const float factor = iw == 0 ? 1.f : 2.f;  // ewem.c:290-291
         for (int p = 0; p < 2; p++) {
             if (!((a.mask >> p) & 1)) continue;
@@ -197,7 +201,7 @@ __global__ void __launch_bounds__(E3_THREADS) wem_e3_rows_kernel(const E3Args a)
             for (int m = 0; m < 16; m++) v[m] = row[t + T * m];
             fft_row<NY, +1>(v, xbuf, s_tw, t, sync);
             const float *pd = p == 0 ? a.pd_p : a.pd_s;
-            float2 *out = a.op == E3R_OUT ? (p == 0 ? a.out_x : a.out_z) + ((size_t)shot * a.nwf + iwi) * nn + (size_t)x * nmy
+            float2 *out = OP == E3R_OUT ? (p == 0 ? a.out_x : a.out_z) + ((size_t)shot * a.nwf + iwi) * nn + (size_t)x * nmy
                                           : nullptr;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
@@ -207,18 +211,19 @@ __global__ void __launch_bounds__(E3_THREADS) wem_e3_rows_kernel(const E3Args a)
                     continue;
                 }
                 float2 u = v[m];
-                if (a.op == E3R_IMG) {
+                if (OP == E3R_IMG) {
                     // ssop with +dz, adj: b exp(i w pd dz) / sqrt(nkx nky), the taper, then the
                     // imaging condition (ewem.c:313-323)
                     u = cmul(u, e3_corr(w, pd[zc + y], a.dz));
                     const float tp = __fmul_rn(tx, a.tapy[y]);
                     u = make_float2(u.x * a.inv_s * tp, u.y * a.inv_s * tp);
-                    const float r = __fmul_rn(factor, __fadd_rn(__fmul_rn(sm[m].x, u.x), __fmul_rn(sm[m].y, u.y)));
+                    const float2 q = sm[T * m + t];
+                    const float r = __fmul_rn(factor, __fadd_rn(__fmul_rn(q.x, u.x), __fmul_rn(q.y, u.y)));
                     if (p == 0) imp[m] = __fadd_rn(imp[m], r);
                     else ims[m] = __fadd_rn(ims[m], r);
                 } else {
                     u = make_float2(u.x * a.inv_s, u.y * a.inv_s);  // the inverse transform's 1/sqrt(nkx nky)
-                    if (a.op == E3R_INJ) {
+                    if (OP == E3R_INJ) {
                         // the forward operator (ewem.c:331-339): the potential plus smig * image,
                         // then ssop with -dz, adj = false: the taper, exp(-i w pd dz)
                         const float mv = (p == 0 ? a.mpp : a.mps2)[zc + y];
@@ -227,19 +232,19 @@ __global__ void __launch_bounds__(E3_THREADS) wem_e3_rows_kernel(const E3Args a)
                         const float tp = __fmul_rn(tx, a.tapy[y]);
                         u = make_float2(u.x * tp, u.y * tp);
                         u = cmulc(u, e3_corr(w, pd[zc + y], a.dz));
-                    } else if (a.op == E3R_OUT) {
+                    } else if (OP == E3R_OUT) {
                         out[y] = make_float2(u.x * a.inv_sqt, u.y * a.inv_sqt);  // ewem.c:345-349
                     }
                 }
                 v[m] = u;
             }
-            if (a.op == E3R_OUT) continue;
+            if (OP == E3R_OUT) continue;
             fft_row<NY, -1>(v, xbuf, s_tw, t, sync);
 #pragma unroll
             for (int m = 0; m < 16; m++) row[t + T * m] = v[m];
         }
     }
-    if (a.op == E3R_IMG && (a.mask & 3)) {
+    if (OP == E3R_IMG && (a.mask & 3)) {
         float2 *ap = a.acc_p + (size_t)chunk * a.nz * nn + zc, *as = a.acc_s + (size_t)chunk * a.nz * nn + zc;
 #pragma unroll
         for (int m = 0; m < 16; m++) {
@@ -253,192 +258,200 @@ __global__ void __launch_bounds__(E3_THREADS) wem_e3_rows_kernel(const E3Args a)
 }
 
 // ------------------------------------------------------------------ column passes (along x)
-// CTA: CW adjacent ky columns of one item, one team of NX/16 threads per column.
+// CTA: CW = 4096/NX adjacent ky columns of one item (at most nky), one team of NX/16 threads per
+// column. A team reads and writes its column straight from device memory (x = t + T m, stride
+// nky): the CTA's teams cover adjacent columns, so the sectors one team touches are the ones its
+// neighbours read at the same time through L1. No CTA-wide barrier but the one after the mix
+// coefficients; one CTA per (item, block of columns), so that the loads of one CTA overlap the
+// transforms of the others on the SM.
 template <int NX> __host__ __device__ constexpr int e3_cols_cw_max() { return E3_THREADS / (NX / 16); }
-__host__ __device__ inline int e3_pitch(int nmx) { return nmx | 1; }
-template <int NX> __host__ __device__ inline size_t e3_cols_smem(int cw, int nmx)
+template <int NX> __host__ __device__ inline size_t e3_cols_smem(int cw)
 {
-    return sizeof(float2) * ((size_t)((fft_tw_size<NX>() + 1) & ~1) + (size_t)cw * pad16(NX) +
-                             (size_t)3 * cw * e3_pitch(nmx) + 1) +
+    return sizeof(float2) * ((size_t)((fft_tw_size<NX>() + 1) & ~1) + (size_t)cw * pad16(NX)) +
            sizeof(float) * 5 * (size_t)NX + (size_t)NX;
 }
 
-template <int NX>
-__global__ void __launch_bounds__(E3_THREADS) wem_e3_cols_kernel(const E3Args a)
+template <int NX, int OP>
+__global__ void __launch_bounds__(E3_THREADS, 2) wem_e3_cols_kernel(const E3Args a)
 {
     constexpr int T = NX / 16, TW = fft_tw_size<NX>();
+    constexpr bool MIX = OP != E3C_SSOP;
     extern __shared__ float4 e3c_smem[];
     const int nt = blockDim.x, cw = nt / T;
-    const int nmx = a.nmx, nky = a.nky, iz = a.iz, pitch = e3_pitch(nmx);
+    const int nmx = a.nmx, nky = a.nky, iz = a.iz;
     float2 *s_tw = reinterpret_cast<float2 *>(e3c_smem);
     float2 *s_x = s_tw + ((TW + 1) & ~1);
-    float2 *s_tile = s_x + (size_t)cw * pad16(NX);  // [3][cw][pitch]
-    float *s_cf = reinterpret_cast<float *>(s_tile + (size_t)3 * cw * pitch + 1);  // [5][NX]
+    float *s_cf = reinterpret_cast<float *>(s_x + (size_t)cw * pad16(NX));  // [5][NX]
     uint8_t *s_on = reinterpret_cast<uint8_t *>(s_cf + 5 * NX);
     const int tid = threadIdx.x, c = tid / T, t = tid - c * T;
     float2 *xbuf = s_x + (size_t)c * pad16(NX);
     const unsigned sync = team_sync_handle<NX>(tid);
-    for (int i = tid; i < TW; i += nt) s_tw[i] = a.twx[i];
-    const size_t plane = (size_t)nmx * nky;
     const int nblk = nky / cw;
-    const bool mix = a.op != E3C_SSOP;
-    for (int job = blockIdx.x; job < a.nitems * nblk; job += gridDim.x) {
-        const int li = job / nblk, blk = job - li * nblk, ky0 = blk * cw;
-        const int item = a.item0 + li;
-        const int iw = a.ifmin + a.item_iwi[item];
-        const float w = __fmul_rn((float)iw, a.dw);
-        const float2 *Kin = a.K + (size_t)li * 3 * plane;
-        __syncthreads();  // the previous job's tile is stored, its coefficients read
+    const int li = blockIdx.x / nblk, ky = (blockIdx.x - li * nblk) * cw + c;
+    const int item = a.item0 + li;
+    const int iw = a.ifmin + a.item_iwi[item];
+    const float w = __fmul_rn((float)iw, a.dw);
+    for (int i = tid; i < TW; i += nt) s_tw[i] = a.twx[i];
+    if constexpr (MIX) {
+        // elastic_separate_3d's coefficients of every kx (ewem.c:596-611): the layer's vp, vs
+        const float vp = a.vpm[iz], vs = a.vsm[iz];
+        for (int k = tid; k < NX; k += nt) {
+            const SepCoef cf = sep_coef(kx_signed(k, NX, a.dkx), w, vp, vs);
+            s_cf[k] = cf.kxp;
+            s_cf[NX + k] = cf.kzp;
+            s_cf[2 * NX + k] = cf.kxs;
+            s_cf[3 * NX + k] = cf.kzs;
+            s_cf[4 * NX + k] = cf.norm;
+            s_on[k] = cf.on ? 1 : 0;
+        }
+    }
+    __syncthreads();
+    const size_t plane = (size_t)nmx * nky;
+    // column ky of plane 0 from this thread's first sample x = t: sample x = t + T m at K[m * sT]
+    float2 *K = a.K + (size_t)li * 3 * plane + (size_t)t * nky + ky;
+    const size_t sT = (size_t)T * nky;
+    float2 v[16];
+    if constexpr (!MIX) {
+        const float kyv = kx_signed(ky, nky, a.dky);
         for (int p = 0; p < 3; p++) {
             if (!((a.mask >> p) & 1)) continue;
-            for (int e = tid; e < nmx * cw; e += nt) {
-                const int x = e / cw, cc = e - x * cw;
-                s_tile[((size_t)p * cw + cc) * pitch + x] = Kin[(size_t)p * plane + (size_t)x * nky + ky0 + cc];
-            }
-        }
-        if (mix) {
-            // elastic_separate_3d's coefficients of every kx (ewem.c:596-611): the layer's vp, vs
-            const float vp = a.vpm[iz], vs = a.vsm[iz];
-            for (int k = tid; k < NX; k += nt) {
-                const SepCoef cf = sep_coef(kx_signed(k, NX, a.dkx), w, vp, vs);
-                s_cf[k] = cf.kxp;
-                s_cf[NX + k] = cf.kzp;
-                s_cf[2 * NX + k] = cf.kxs;
-                s_cf[3 * NX + k] = cf.kzs;
-                s_cf[4 * NX + k] = cf.norm;
-                s_on[k] = cf.on ? 1 : 0;
-            }
-        }
-        __syncthreads();
-        const float ky = kx_signed(ky0 + c, nky, a.dky);
-        float2 v[16];
-        if (!mix) {
-            for (int p = 0; p < 3; p++) {
-                if (!((a.mask >> p) & 1)) continue;
-                float2 *col = s_tile + ((size_t)p * cw + c) * pitch;
-#pragma unroll
-                for (int m = 0; m < 16; m++) {
-                    const int x = t + T * m;
-                    v[m] = x < nmx ? col[x] : make_float2(0.f, 0.f);
-                }
-                fft_row<NX, -1>(v, xbuf, s_tw, t, sync);
-                // the source goes down with -dz; the forward operator's receivers go up with -dz
-                const bool neg = p == 2 || !a.adj;
-                const float po = p == 1 ? a.po_s[iz] : a.po_p[iz];
-#pragma unroll
-                for (int m = 0; m < 16; m++) {
-                    const float kx = kx_signed(t + T * m, NX, a.dkx);
-                    float2 L = e3_phase(w, po, kx, ky, a.dz);
-                    if (neg) L.y = -L.y;  // sqrtf(s) * (-dz) = -(sqrtf(s) * dz)
-                    const float2 u = cmul(v[m], L);
-                    v[m] = make_float2(u.x * a.inv_s, u.y * a.inv_s);
-                }
-                fft_row<NX, +1>(v, xbuf, s_tw, t, sync);
-#pragma unroll
-                for (int m = 0; m < 16; m++) {
-                    const int x = t + T * m;
-                    if (x < nmx) col[x] = v[m];
-                }
-            }
-        } else {
-            float2 u[16];
-            float2 *c0 = s_tile + (size_t)c * pitch, *c1 = s_tile + ((size_t)cw + c) * pitch;
+            float2 *col = K + (size_t)p * plane;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const int x = t + T * m;
-                v[m] = x < nmx ? c0[x] : make_float2(0.f, 0.f);
-                u[m] = x < nmx ? c1[x] : make_float2(0.f, 0.f);
+                v[m] = x < nmx ? col[m * sT] : make_float2(0.f, 0.f);
             }
             fft_row<NX, -1>(v, xbuf, s_tw, t, sync);
-            fft_row<NX, -1>(u, xbuf, s_tw, t, sync);
+            // the source goes down with -dz; the forward operator's receivers go up with -dz
+            const bool neg = p == 2 || !a.adj;
+            const float po = p == 1 ? a.po_s[iz] : a.po_p[iz];
 #pragma unroll
             for (int m = 0; m < 16; m++) {
-                const int k = t + T * m;
-                const float2 A = make_float2(v[m].x * a.inv_s, v[m].y * a.inv_s);  // first plane / sqrt(nkx nky)
-                const float2 B = make_float2(u[m].x * a.inv_s, u[m].y * a.inv_s);
-                float2 o0, o1;
-                if (s_on[k]) {
-                    const float kxp = s_cf[k], kzp = s_cf[NX + k], kxs = s_cf[2 * NX + k], kzs = s_cf[3 * NX + k],
-                                nrm = s_cf[4 * NX + k];
-                    if (a.op == E3C_SEP) {
-                        // (ux, uz) -> (P, S2), ewem.c:612-620
-                        if (a.adj) {
-                            o0 = c_axpy(kxp, A, kzp, B);
-                            o1 = c_axpy(-kzs, A, kxs, B);
-                        } else {
-                            o0 = c_axpy(kxs, A, kzs, B);
-                            o1 = c_axpy(-kzp, A, kxp, B);
-                            o0 = make_float2(__fdiv_rn(o0.x, nrm), __fdiv_rn(o0.y, nrm));
-                            o1 = make_float2(__fdiv_rn(o1.x, nrm), __fdiv_rn(o1.y, nrm));
-                        }
-                    } else {
-                        // (P, S2) -> (ux, uz), ewem.c:696-704
-                        if (a.adj) {
-                            o0 = c_axpy(kxs, A, -kzp, B);
-                            o1 = c_axpy(kzs, A, kxp, B);
-                            o0 = make_float2(__fdiv_rn(o0.x, nrm), __fdiv_rn(o0.y, nrm));
-                            o1 = make_float2(__fdiv_rn(o1.x, nrm), __fdiv_rn(o1.y, nrm));
-                        } else {
-                            o0 = c_axpy(kxp, A, -kzs, B);
-                            o1 = c_axpy(kzp, A, kxs, B);
-                        }
-                    }
-                } else {
-                    // the swap where the potentials are not separated (ewem.c:622-625, 706-709)
-                    o0 = B;
-                    o1 = A;
-                }
-                v[m] = o0;
-                u[m] = o1;
+                const float kx = kx_signed(t + T * m, NX, a.dkx);
+                float2 L = e3_phase(w, po, kx, kyv, a.dz);
+                if (neg) L.y = -L.y;  // sqrtf(s) * (-dz) = -(sqrtf(s) * dz)
+                const float2 u = cmul(v[m], L);
+                v[m] = make_float2(u.x * a.inv_s, u.y * a.inv_s);
             }
             fft_row<NX, +1>(v, xbuf, s_tw, t, sync);
-            fft_row<NX, +1>(u, xbuf, s_tw, t, sync);
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const int x = t + T * m;
-                if (x < nmx) {
-                    c0[x] = v[m];
-                    c1[x] = u[m];
-                }
+                if (x < nmx) col[m * sT] = v[m];
             }
         }
-        __syncthreads();
-        float2 *Kout = a.K + (size_t)li * 3 * plane;
-        for (int p = 0; p < 3; p++) {
-            if (!((a.mask >> p) & 1)) continue;
-            for (int e = tid; e < nmx * cw; e += nt) {
-                const int x = e / cw, cc = e - x * cw;
-                Kout[(size_t)p * plane + (size_t)x * nky + ky0 + cc] = s_tile[((size_t)p * cw + cc) * pitch + x];
+    } else {
+        float2 u[16];
+        float2 *c0 = K, *c1 = K + plane;
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            v[m] = x < nmx ? c0[m * sT] : make_float2(0.f, 0.f);
+            u[m] = x < nmx ? c1[m * sT] : make_float2(0.f, 0.f);
+        }
+        fft_row<NX, -1>(v, xbuf, s_tw, t, sync);
+        fft_row<NX, -1>(u, xbuf, s_tw, t, sync);
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int k = t + T * m;
+            const float2 A = make_float2(v[m].x * a.inv_s, v[m].y * a.inv_s);  // first plane / sqrt(nkx nky)
+            const float2 B = make_float2(u[m].x * a.inv_s, u[m].y * a.inv_s);
+            float2 o0, o1;
+            if (s_on[k]) {
+                const float kxp = s_cf[k], kzp = s_cf[NX + k], kxs = s_cf[2 * NX + k], kzs = s_cf[3 * NX + k],
+                            nrm = s_cf[4 * NX + k];
+                if (OP == E3C_SEP) {
+                    // (ux, uz) -> (P, S2), ewem.c:612-620
+                    if (a.adj) {
+                        o0 = c_axpy(kxp, A, kzp, B);
+                        o1 = c_axpy(-kzs, A, kxs, B);
+                    } else {
+                        o0 = c_axpy(kxs, A, kzs, B);
+                        o1 = c_axpy(-kzp, A, kxp, B);
+                        o0 = make_float2(__fdiv_rn(o0.x, nrm), __fdiv_rn(o0.y, nrm));
+                        o1 = make_float2(__fdiv_rn(o1.x, nrm), __fdiv_rn(o1.y, nrm));
+                    }
+                } else {
+                    // (P, S2) -> (ux, uz), ewem.c:696-704
+                    if (a.adj) {
+                        o0 = c_axpy(kxs, A, -kzp, B);
+                        o1 = c_axpy(kzs, A, kxp, B);
+                        o0 = make_float2(__fdiv_rn(o0.x, nrm), __fdiv_rn(o0.y, nrm));
+                        o1 = make_float2(__fdiv_rn(o1.x, nrm), __fdiv_rn(o1.y, nrm));
+                    } else {
+                        o0 = c_axpy(kxp, A, -kzs, B);
+                        o1 = c_axpy(kzp, A, kxs, B);
+                    }
+                }
+            } else {
+                // the swap where the potentials are not separated (ewem.c:622-625, 706-709)
+                o0 = B;
+                o1 = A;
+            }
+            v[m] = o0;
+            u[m] = o1;
+        }
+        fft_row<NX, +1>(v, xbuf, s_tw, t, sync);
+        fft_row<NX, +1>(u, xbuf, s_tw, t, sync);
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int x = t + T * m;
+            if (x < nmx) {
+                c0[m * sT] = v[m];
+                c1[m * sT] = u[m];
             }
         }
     }
 }
 
-template <int NY> int e3_rows_launch(const E3Args &a, cudaStream_t st)
+template <int NY, int OP> int e3_rows_launch_op(const E3Args &a, cudaStream_t st)
 {
     constexpr int TEAMS = E3_THREADS / (NY / 16);
     const size_t smem = e3_rows_smem<NY>();
-    if (cudaFuncSetAttribute(wem_e3_rows_kernel<NY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    if (cudaFuncSetAttribute(wem_e3_rows_kernel<NY, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
         return -1;
     const long long units = (long long)((a.nitems + a.ipc - 1) / a.ipc) * a.nmx;
     if (units <= 0) return 0;
-    wem_e3_rows_kernel<NY><<<(unsigned)((units + TEAMS - 1) / TEAMS), E3_THREADS, smem, st>>>(a);
+    wem_e3_rows_kernel<NY, OP><<<(unsigned)((units + TEAMS - 1) / TEAMS), E3_THREADS, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <int NX> int e3_cols_launch(const E3Args &a, int nsm, cudaStream_t st)
+template <int NY> int e3_rows_launch(const E3Args &a, cudaStream_t st)
+{
+    switch (a.op) {
+    case E3R_LOAD_REC: return e3_rows_launch_op<NY, E3R_LOAD_REC>(a, st);
+    case E3R_LOAD_SRC: return e3_rows_launch_op<NY, E3R_LOAD_SRC>(a, st);
+    case E3R_MID: return e3_rows_launch_op<NY, E3R_MID>(a, st);
+    case E3R_IMG: return e3_rows_launch_op<NY, E3R_IMG>(a, st);
+    case E3R_SRC_STORE: return e3_rows_launch_op<NY, E3R_SRC_STORE>(a, st);
+    case E3R_INJ: return e3_rows_launch_op<NY, E3R_INJ>(a, st);
+    case E3R_OUT: return e3_rows_launch_op<NY, E3R_OUT>(a, st);
+    default: return -2;
+    }
+}
+
+template <int NX, int OP> int e3_cols_launch_op(const E3Args &a, cudaStream_t st)
 {
     const int cw = std::min(e3_cols_cw_max<NX>(), a.nky);
-    const size_t smem = e3_cols_smem<NX>(cw, a.nmx);
-    if (smem > 227 * 1024) return -2;
-    if (cudaFuncSetAttribute(wem_e3_cols_kernel<NX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    const size_t smem = e3_cols_smem<NX>(cw);
+    if (cudaFuncSetAttribute(wem_e3_cols_kernel<NX, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
         return -1;
     const long long jobs = (long long)a.nitems * (a.nky / cw);
     if (jobs <= 0) return 0;
-    const int per_sm = std::max(1, (int)((227 * 1024) / (smem + 1024)));
-    const long long grid = std::min<long long>(jobs, (long long)nsm * std::min(per_sm, 8));
-    wem_e3_cols_kernel<NX><<<(unsigned)grid, cw * (NX / 16), smem, st>>>(a);
+    wem_e3_cols_kernel<NX, OP><<<(unsigned)jobs, cw * (NX / 16), smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int NX> int e3_cols_launch(const E3Args &a, cudaStream_t st)
+{
+    switch (a.op) {
+    case E3C_SEP: return e3_cols_launch_op<NX, E3C_SEP>(a, st);
+    case E3C_SSOP: return e3_cols_launch_op<NX, E3C_SSOP>(a, st);
+    case E3C_RECOMB: return e3_cols_launch_op<NX, E3C_RECOMB>(a, st);
+    default: return -2;
+    }
 }
 
 int e3_rows(int nky, const E3Args &a, cudaStream_t st)
@@ -453,14 +466,14 @@ int e3_rows(int nky, const E3Args &a, cudaStream_t st)
     }
 }
 
-int e3_cols(int nkx, const E3Args &a, int nsm, cudaStream_t st)
+int e3_cols(int nkx, const E3Args &a, cudaStream_t st)
 {
     switch (nkx) {
-    case 64: return e3_cols_launch<64>(a, nsm, st);
-    case 128: return e3_cols_launch<128>(a, nsm, st);
-    case 256: return e3_cols_launch<256>(a, nsm, st);
-    case 512: return e3_cols_launch<512>(a, nsm, st);
-    case 1024: return e3_cols_launch<1024>(a, nsm, st);
+    case 64: return e3_cols_launch<64>(a, st);
+    case 128: return e3_cols_launch<128>(a, st);
+    case 256: return e3_cols_launch<256>(a, st);
+    case 512: return e3_cols_launch<512>(a, st);
+    case 1024: return e3_cols_launch<1024>(a, st);
     default: return -2;
     }
 }
@@ -732,7 +745,7 @@ int wem_elastic3d(int device, const wem_params &p, const float *vp, const float 
     };
     auto cols = [&](int op, int mask, int iz) {
         a.op = op; a.mask = mask; a.iz = iz;
-        return e3_cols(nkx, a, nsm, st);
+        return e3_cols(nkx, a, st);
     };
     for (int i0 = 0; i0 < nall; i0 += batch) {
         a.item0 = i0;
