@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -135,7 +136,7 @@ __global__ void __launch_bounds__(E3_THREADS, 2) wem_e3_rows_kernel(const E3Args
         const float w = __fmul_rn((float)iw, a.dw);
         float2 *Kx = a.K + (size_t)li * 3 * plane + (size_t)x * nky;  // row x of plane 0
         float2 v[16];
-        if (OP == E3R_LOAD_REC || OP == E3R_LOAD_SRC) {
+        if constexpr (OP == E3R_LOAD_REC || OP == E3R_LOAD_SRC) {
             // the initial planes (ewem.c:109, 295-300): the component spectra, the source spike
             const int p0 = OP == E3R_LOAD_REC ? 0 : 2, p1 = OP == E3R_LOAD_REC ? 1 : 2;
             for (int p = p0; p <= p1; p++) {
@@ -156,92 +157,95 @@ __global__ void __launch_bounds__(E3_THREADS, 2) wem_e3_rows_kernel(const E3Args
                 for (int m = 0; m < 16; m++) row[t + T * m] = v[m];
             }
             continue;
-        }
-        // the source at this depth (E3R_IMG, E3R_SRC_STORE): smig = ssop(source) / max_source
+        } else {
+            // the source at this depth (E3R_IMG, E3R_SRC_STORE): smig = ssop(source) / max_source
+            if constexpr (OP == E3R_IMG || OP == E3R_SRC_STORE) {
 #pragma unroll
-        for (int m = 0; m < 16; m++) sm[T * m + t] = make_float2(0.f, 0.f);
-        if ((OP == E3R_IMG || OP == E3R_SRC_STORE) && (a.mask & 4)) {
-            float2 *row = Kx + 2 * plane;
-#pragma unroll
-            for (int m = 0; m < 16; m++) v[m] = row[t + T * m];
-            fft_row<NY, +1>(v, xbuf, s_tw, t, sync);
-#pragma unroll
-            for (int m = 0; m < 16; m++) {
-                const int y = t + T * m;
-                if (y < nmy) {
-                    // ssop with -dz, adj (ewem.c:427-437): b exp(-i w pd dz) / sqrt(nkx nky), then the taper
-                    const float2 c = e3_corr(w, a.pd_p[zc + y], a.dz);
-                    float2 u = cmulc(v[m], c);
-                    const float tp = __fmul_rn(tx, a.tapy[y]);
-                    u = make_float2(u.x * a.inv_s * tp, u.y * a.inv_s * tp);
-                    v[m] = u;
-                    sm[T * m + t] = make_float2(u.x * a.inv_max_source, u.y * a.inv_max_source);
-                } else {
-                    v[m] = make_float2(0.f, 0.f);
-                }
+                for (int m = 0; m < 16; m++) sm[T * m + t] = make_float2(0.f, 0.f);
             }
-            if (OP == E3R_SRC_STORE) {
-                float2 *sg = a.smig + ((size_t)li * a.nz) * nn + zc;
+            if ((OP == E3R_IMG || OP == E3R_SRC_STORE) && (a.mask & 4)) {
+                float2 *row = Kx + 2 * plane;
+#pragma unroll
+                for (int m = 0; m < 16; m++) v[m] = row[t + T * m];
+                fft_row<NY, +1>(v, xbuf, s_tw, t, sync);
 #pragma unroll
                 for (int m = 0; m < 16; m++) {
                     const int y = t + T * m;
-                    if (y < nmy) sg[y] = sm[T * m + t];
-                }
-            }
-            fft_row<NY, -1>(v, xbuf, s_tw, t, sync);
-#pragma unroll
-            for (int m = 0; m < 16; m++) row[t + T * m] = v[m];
-        }
-        if (OP == E3R_SRC_STORE) continue;
-        const float factor = iw == 0 ? 1.f : 2.f;  // ewem.c:290-291
-        for (int p = 0; p < 2; p++) {
-            if (!((a.mask >> p) & 1)) continue;
-            float2 *row = Kx + (size_t)p * plane;
-#pragma unroll
-            for (int m = 0; m < 16; m++) v[m] = row[t + T * m];
-            fft_row<NY, +1>(v, xbuf, s_tw, t, sync);
-            const float *pd = p == 0 ? a.pd_p : a.pd_s;
-            float2 *out = OP == E3R_OUT ? (p == 0 ? a.out_x : a.out_z) + ((size_t)shot * a.nwf + iwi) * nn + (size_t)x * nmy
-                                          : nullptr;
-#pragma unroll
-            for (int m = 0; m < 16; m++) {
-                const int y = t + T * m;
-                if (y >= nmy) {
-                    v[m] = make_float2(0.f, 0.f);
-                    continue;
-                }
-                float2 u = v[m];
-                if (OP == E3R_IMG) {
-                    // ssop with +dz, adj: b exp(i w pd dz) / sqrt(nkx nky), the taper, then the
-                    // imaging condition (ewem.c:313-323)
-                    u = cmul(u, e3_corr(w, pd[zc + y], a.dz));
-                    const float tp = __fmul_rn(tx, a.tapy[y]);
-                    u = make_float2(u.x * a.inv_s * tp, u.y * a.inv_s * tp);
-                    const float2 q = sm[T * m + t];
-                    const float r = __fmul_rn(factor, __fadd_rn(__fmul_rn(q.x, u.x), __fmul_rn(q.y, u.y)));
-                    if (p == 0) imp[m] = __fadd_rn(imp[m], r);
-                    else ims[m] = __fadd_rn(ims[m], r);
-                } else {
-                    u = make_float2(u.x * a.inv_s, u.y * a.inv_s);  // the inverse transform's 1/sqrt(nkx nky)
-                    if (OP == E3R_INJ) {
-                        // the forward operator (ewem.c:331-339): the potential plus smig * image,
-                        // then ssop with -dz, adj = false: the taper, exp(-i w pd dz)
-                        const float mv = (p == 0 ? a.mpp : a.mps2)[zc + y];
-                        const float2 s = a.smig[((size_t)li * a.nz) * nn + zc + y];
-                        u = make_float2(__fadd_rn(u.x, __fmul_rn(s.x, mv)), __fadd_rn(u.y, __fmul_rn(s.y, mv)));
+                    if (y < nmy) {
+                        // ssop with -dz, adj (ewem.c:427-437): b exp(-i w pd dz) / sqrt(nkx nky), then the taper
+                        const float2 c = e3_corr(w, a.pd_p[zc + y], a.dz);
+                        float2 u = cmulc(v[m], c);
                         const float tp = __fmul_rn(tx, a.tapy[y]);
-                        u = make_float2(u.x * tp, u.y * tp);
-                        u = cmulc(u, e3_corr(w, pd[zc + y], a.dz));
-                    } else if (OP == E3R_OUT) {
-                        out[y] = make_float2(u.x * a.inv_sqt, u.y * a.inv_sqt);  // ewem.c:345-349
+                        u = make_float2(u.x * a.inv_s * tp, u.y * a.inv_s * tp);
+                        v[m] = u;
+                        sm[T * m + t] = make_float2(u.x * a.inv_max_source, u.y * a.inv_max_source);
+                    } else {
+                        v[m] = make_float2(0.f, 0.f);
                     }
                 }
-                v[m] = u;
-            }
-            if (OP == E3R_OUT) continue;
-            fft_row<NY, -1>(v, xbuf, s_tw, t, sync);
+                if (OP == E3R_SRC_STORE) {
+                    float2 *sg = a.smig + ((size_t)li * a.nz) * nn + zc;
 #pragma unroll
-            for (int m = 0; m < 16; m++) row[t + T * m] = v[m];
+                    for (int m = 0; m < 16; m++) {
+                        const int y = t + T * m;
+                        if (y < nmy) sg[y] = sm[T * m + t];
+                    }
+                }
+                fft_row<NY, -1>(v, xbuf, s_tw, t, sync);
+#pragma unroll
+                for (int m = 0; m < 16; m++) row[t + T * m] = v[m];
+            }
+            if (OP == E3R_SRC_STORE) continue;
+            const float factor = iw == 0 ? 1.f : 2.f;  // ewem.c:290-291
+            for (int p = 0; p < 2; p++) {
+                if (!((a.mask >> p) & 1)) continue;
+                float2 *row = Kx + (size_t)p * plane;
+#pragma unroll
+                for (int m = 0; m < 16; m++) v[m] = row[t + T * m];
+                fft_row<NY, +1>(v, xbuf, s_tw, t, sync);
+                const float *pd = p == 0 ? a.pd_p : a.pd_s;
+                float2 *out = OP == E3R_OUT ? (p == 0 ? a.out_x : a.out_z) + ((size_t)shot * a.nwf + iwi) * nn + (size_t)x * nmy
+                                              : nullptr;
+#pragma unroll
+                for (int m = 0; m < 16; m++) {
+                    const int y = t + T * m;
+                    if (y >= nmy) {
+                        v[m] = make_float2(0.f, 0.f);
+                        continue;
+                    }
+                    float2 u = v[m];
+                    if (OP == E3R_IMG) {
+                        // ssop with +dz, adj: b exp(i w pd dz) / sqrt(nkx nky), the taper, then the
+                        // imaging condition (ewem.c:313-323)
+                        u = cmul(u, e3_corr(w, pd[zc + y], a.dz));
+                        const float tp = __fmul_rn(tx, a.tapy[y]);
+                        u = make_float2(u.x * a.inv_s * tp, u.y * a.inv_s * tp);
+                        const float2 q = sm[T * m + t];
+                        const float r = __fmul_rn(factor, __fadd_rn(__fmul_rn(q.x, u.x), __fmul_rn(q.y, u.y)));
+                        if (p == 0) imp[m] = __fadd_rn(imp[m], r);
+                        else ims[m] = __fadd_rn(ims[m], r);
+                    } else {
+                        u = make_float2(u.x * a.inv_s, u.y * a.inv_s);  // the inverse transform's 1/sqrt(nkx nky)
+                        if (OP == E3R_INJ) {
+                            // the forward operator (ewem.c:331-339): the potential plus smig * image,
+                            // then ssop with -dz, adj = false: the taper, exp(-i w pd dz)
+                            const float mv = (p == 0 ? a.mpp : a.mps2)[zc + y];
+                            const float2 s = a.smig[((size_t)li * a.nz) * nn + zc + y];
+                            u = make_float2(__fadd_rn(u.x, __fmul_rn(s.x, mv)), __fadd_rn(u.y, __fmul_rn(s.y, mv)));
+                            const float tp = __fmul_rn(tx, a.tapy[y]);
+                            u = make_float2(u.x * tp, u.y * tp);
+                            u = cmulc(u, e3_corr(w, pd[zc + y], a.dz));
+                        } else if (OP == E3R_OUT) {
+                            out[y] = make_float2(u.x * a.inv_sqt, u.y * a.inv_sqt);  // ewem.c:345-349
+                        }
+                    }
+                    v[m] = u;
+                }
+                if (OP == E3R_OUT) continue;
+                fft_row<NY, -1>(v, xbuf, s_tw, t, sync);
+#pragma unroll
+                for (int m = 0; m < 16; m++) row[t + T * m] = v[m];
+            }
         }
     }
     if (OP == E3R_IMG && (a.mask & 3)) {
@@ -720,7 +724,11 @@ int wem_elastic3d(int device, const wem_params &p, const float *vp, const float 
     E3CK(cudaMemGetInfo(&free_b, &total_b));
     const size_t per_item = sizeof(float2) * ((size_t)3 * nmx * nky + (adj ? 0 : nzn));
     const size_t budget = std::min<size_t>((size_t)8 << 30, free_b / 4);
-    const int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(nall, 1), budget / per_item));
+    int batch = (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(nall, 1), budget / per_item));
+    if (const char *e = getenv("WEM_E3_BATCH")) {  // a smaller batch (tests of the batch loop)
+        const int b = atoi(e);
+        if (b > 0 && b < batch) batch = b;
+    }
     const int rows_teams = E3_THREADS / (nky / 16);
     int nchunk = std::max(1, std::min(batch, (nsm * 8 * rows_teams + nmx - 1) / nmx));
     const size_t acc_bytes = sizeof(float2) * nzn;  // per chunk and image

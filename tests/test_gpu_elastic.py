@@ -296,3 +296,26 @@ def test_elastic3d_linearity(gpu_lib):
     ax = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, ux=ux, uz=z, adj=True)
     az = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, ux=z, uz=uz, adj=True)
     assert rel_l2(ax[0] + az[0], a[0]) < 1e-5 and rel_l2(ax[1] + az[1], a[1]) < 1e-5
+
+
+def test_elastic3d_batches_agree(gpu_lib, monkeypatch):
+    """The 3-D items (shot, frequency) run in batches when their planes exceed the memory
+    budget; forcing batches of 5 items (WEM_E3_BATCH) gives the images and data of one batch to
+    FP32 rounding (the imaging chunks sum the items in another grouping)."""
+    from wemgpu import synth
+    c = synth.small_case3d(98, nx=32, ny=32, nz=5, nt=32, nshot=3, pspi=0, fmax=25.0, padx=2)
+    vp = c["vel"]
+    vs = (vp / 1.8).astype(np.float32)
+    p = dict(c["params"], fmin=3.0)
+    shots = c["shots"]
+    uz = np.stack([synth.shot_gather_full(shots, s, 32 * 32) for s in range(shots.nshot)])
+    ux = (0.3 * np.roll(uz, 1, axis=2)).astype(np.float32)
+    rng = np.random.default_rng(99)
+    m_in = [rng.standard_normal((32 * 32, 5)).astype(np.float32) for _ in range(2)]
+    one = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, ux=ux, uz=uz, adj=True)
+    d_one = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, mpp=m_in[0], mps2=m_in[1], adj=False)
+    monkeypatch.setenv("WEM_E3_BATCH", "5")
+    many = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, ux=ux, uz=uz, adj=True)
+    d_many = gpu_lib.elastic(p, vp, vs, c["wav"], shots.sx, sy=shots.sy, mpp=m_in[0], mps2=m_in[1], adj=False)
+    assert rel_l2(many[0], one[0]) < 1e-6 and rel_l2(many[1], one[1]) < 1e-6
+    assert np.array_equal(d_many[0], d_one[0]) and np.array_equal(d_many[1], d_one[1])
