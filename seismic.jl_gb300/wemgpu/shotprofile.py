@@ -484,7 +484,7 @@ def ShotProfileLSEWEM(m, m0, d, param=None):
     ShotProfileEWEM] (cg.least_squares_elastic). param holds ShotProfileEWEM's keywords (vp, vs,
     wav, sx, sy, sz, gz, fmin, fmax, padt, padx) and the solver's Niter (10), mu (one weight or
     one per image, 0), tol (1e-15) and cost ("cost.txt"). m0 is accepted and unused, as there.
-    2-D grids; mps1 is written as zeros. Returns (mpp, mps2, cost)."""
+    2-D and 3-D grids; mps1 is written as zeros. Returns (mpp, mps2, cost)."""
     from .cg import least_squares_elastic
     q = dict(param or {})
     vpv, hv, g = grid_from_velocity(q.get("vp", "vp.seis"))
