@@ -263,16 +263,25 @@ __global__ void __launch_bounds__(E3_THREADS, 2) wem_e3_rows_kernel(const E3Args
 
 // ------------------------------------------------------------------ column passes (along x)
 // CTA: CW = 4096/NX adjacent ky columns of one item (at most nky), one team of NX/16 threads per
-// column. A team reads and writes its column straight from device memory (x = t + T m, stride
-// nky): the CTA's teams cover adjacent columns, so the sectors one team touches are the ones its
-// neighbours read at the same time through L1. No CTA-wide barrier but the one after the mix
-// coefficients; one CTA per (item, block of columns), so that the loads of one CTA overlap the
-// transforms of the others on the SM.
+// column. The block's columns of every plane the operation touches reach a shared-memory tile by
+// asynchronous copies of row segments (a warp copies 2 .. 8 rows of 128 .. 32 bytes, each line
+// once), the teams transform their columns from and back into the tile, and the CTA writes the
+// tile back row segment by row segment. One CTA per (item, block of columns), so that the copies
+// of one CTA overlap the transforms of the others on the SM.
 template <int NX> __host__ __device__ constexpr int e3_cols_cw_max() { return E3_THREADS / (NX / 16); }
-template <int NX> __host__ __device__ inline size_t e3_cols_smem(int cw)
+// twiddles, exchange buffers, the tile of the CTA's columns (one [nmx][cw + 1] block per plane of
+// the operation), the mix coefficients
+template <int NX> __host__ __device__ inline size_t e3_cols_smem(int cw, int nmx, int nplanes)
 {
-    return sizeof(float2) * ((size_t)((fft_tw_size<NX>() + 1) & ~1) + (size_t)cw * pad16(NX)) +
+    return sizeof(float2) * ((size_t)((fft_tw_size<NX>() + 1) & ~1) + (size_t)cw * pad16(NX) +
+                             (size_t)nplanes * nmx * (cw + 1)) +
            sizeof(float) * 5 * (size_t)NX + (size_t)NX;
+}
+
+__device__ __forceinline__ void cp_async8(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
 }
 
 template <int NX, int OP>
@@ -283,18 +292,34 @@ __global__ void __launch_bounds__(E3_THREADS, 2) wem_e3_cols_kernel(const E3Args
     extern __shared__ float4 e3c_smem[];
     const int nt = blockDim.x, cw = nt / T;
     const int nmx = a.nmx, nky = a.nky, iz = a.iz;
+    const int RS = cw + 1;  // tile row stride (odd: the teams' column reads spread over the banks)
     float2 *s_tw = reinterpret_cast<float2 *>(e3c_smem);
     float2 *s_x = s_tw + ((TW + 1) & ~1);
-    float *s_cf = reinterpret_cast<float *>(s_x + (size_t)cw * pad16(NX));  // [5][NX]
+    float2 *s_tile = s_x + (size_t)cw * pad16(NX);                              // [planes][nmx][RS]
+    float *s_cf = reinterpret_cast<float *>(s_tile + (size_t)__popc(a.mask & 7) * nmx * RS);  // [5][NX]
     uint8_t *s_on = reinterpret_cast<uint8_t *>(s_cf + 5 * NX);
     const int tid = threadIdx.x, c = tid / T, t = tid - c * T;
     float2 *xbuf = s_x + (size_t)c * pad16(NX);
     const unsigned sync = team_sync_handle<NX>(tid);
     const int nblk = nky / cw;
-    const int li = blockIdx.x / nblk, ky = (blockIdx.x - li * nblk) * cw + c;
+    const int li = blockIdx.x / nblk, ky0 = (blockIdx.x - li * nblk) * cw, ky = ky0 + c;
     const int item = a.item0 + li;
     const int iw = a.ifmin + a.item_iwi[item];
     const float w = __fmul_rn((float)iw, a.dw);
+    const size_t plane = (size_t)nmx * nky;
+    float2 *Kg = a.K + (size_t)li * 3 * plane + ky0;  // the block's first column, plane 0
+    const int lcw = __ffs(cw) - 1;                     // cw is a power of two
+    // the block's columns of every plane of the operation into the tile: 8-byte asynchronous
+    // copies, consecutive threads on consecutive columns of a row (a 32 .. 128-byte segment)
+    for (int p = 0, q = 0; p < 3; p++) {
+        if (!((a.mask >> p) & 1)) continue;
+        for (int e = tid; e < nmx * cw; e += nt) {
+            const int x = e >> lcw, j = e & (cw - 1);
+            cp_async8(s_tile + ((size_t)q * nmx + x) * RS + j, Kg + (size_t)p * plane + (size_t)x * nky + j);
+        }
+        q++;
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
     for (int i = tid; i < TW; i += nt) s_tw[i] = a.twx[i];
     if constexpr (MIX) {
         // elastic_separate_3d's coefficients of every kx (ewem.c:596-611): the layer's vp, vs
@@ -309,17 +334,19 @@ __global__ void __launch_bounds__(E3_THREADS, 2) wem_e3_cols_kernel(const E3Args
             s_on[k] = cf.on ? 1 : 0;
         }
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
-    const size_t plane = (size_t)nmx * nky;
-    // column ky of plane 0 from this thread's first sample x = t: sample x = t + T m at K[m * sT]
-    float2 *K = a.K + (size_t)li * 3 * plane + (size_t)t * nky + ky;
-    const size_t sT = (size_t)T * nky;
+    // the team's column in the tile's first plane from this thread's first sample x = t: sample
+    // x = t + T m at K[m * sT]; tile planes nmx * RS apart, in the order of the operation's planes
+    float2 *K = s_tile + (size_t)t * RS + c;
+    const size_t sT = (size_t)T * RS;
+    const size_t tplane = (size_t)nmx * RS;
     float2 v[16];
     if constexpr (!MIX) {
         const float kyv = kx_signed(ky, nky, a.dky);
         for (int p = 0; p < 3; p++) {
             if (!((a.mask >> p) & 1)) continue;
-            float2 *col = K + (size_t)p * plane;
+            float2 *col = K + (size_t)__popc(a.mask & ((1 << p) - 1)) * tplane;
 #pragma unroll
             for (int m = 0; m < 16; m++) {
                 const int x = t + T * m;
@@ -346,7 +373,7 @@ __global__ void __launch_bounds__(E3_THREADS, 2) wem_e3_cols_kernel(const E3Args
         }
     } else {
         float2 u[16];
-        float2 *c0 = K, *c1 = K + plane;
+        float2 *c0 = K, *c1 = K + tplane;  // planes 0 and 1 (mask 3)
 #pragma unroll
         for (int m = 0; m < 16; m++) {
             const int x = t + T * m;
@@ -406,6 +433,15 @@ __global__ void __launch_bounds__(E3_THREADS, 2) wem_e3_cols_kernel(const E3Args
             }
         }
     }
+    __syncthreads();  // the tile holds every team's results
+    for (int p = 0, q = 0; p < 3; p++) {
+        if (!((a.mask >> p) & 1)) continue;
+        for (int e = tid; e < nmx * cw; e += nt) {
+            const int x = e >> lcw, j = e & (cw - 1);
+            Kg[(size_t)p * plane + (size_t)x * nky + j] = s_tile[((size_t)q * nmx + x) * RS + j];
+        }
+        q++;
+    }
 }
 
 template <int NY, int OP> int e3_rows_launch_op(const E3Args &a, cudaStream_t st)
@@ -438,7 +474,8 @@ template <int NY> int e3_rows_launch(const E3Args &a, cudaStream_t st)
 template <int NX, int OP> int e3_cols_launch_op(const E3Args &a, cudaStream_t st)
 {
     const int cw = std::min(e3_cols_cw_max<NX>(), a.nky);
-    const size_t smem = e3_cols_smem<NX>(cw);
+    const size_t smem = e3_cols_smem<NX>(cw, a.nmx, __builtin_popcount(a.mask & 7));
+    if (smem > 227 * 1024) return -2;
     if (cudaFuncSetAttribute(wem_e3_cols_kernel<NX, OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
         return -1;
