@@ -133,3 +133,35 @@ def test_ricker_matches_reference_definition():
     from wemgpu import synth
     w = synth.ricker(20.0, 0.002)
     assert len(w) == 51 and np.argmax(w) == 25 and abs(w[25] - 1.0) < 1e-7
+
+
+def test_shotewem_main_3d_grid_spacing_from_first_two_traces(gpu_lib, tmp_path):
+    """shotewem.c:78 takes dx from the first two velocity traces' mx. A 3-D grid stored as the
+    computation indexes it (cell = imx * ny + imy, y fastest) has the same mx on those two traces,
+    so dx = 0: the reference goes on with a zero spacing, the drop-in refuses with WEM_ERR_ARG
+    before any device work (no GPU is needed to see it)."""
+    import numpy as np
+    from wemgpu import seis
+    nx, ny, nz, nt = 4, 4, 3, 8
+    t = str(tmp_path)
+    n = nx * ny
+    h = seis.empty_headers(n)
+    cell = np.arange(n)
+    h["tracenum"] = cell + 1
+    h["imx"], h["imy"] = cell // ny, cell % ny
+    h["mx"], h["my"] = 10.0 * (cell // ny), 10.0 * (cell % ny)
+    h["n1"], h["d1"] = nz, 10.0
+    v = np.full((n, nz), 2000.0, np.float32)
+    seis.write(t + "/vp", v, h, [nz, nx, ny], [0.0, 0.0, 0.0], [10.0, 10.0, 10.0])
+    seis.write(t + "/vs", v / 1.8, h, [nz, nx, ny], [0.0, 0.0, 0.0], [10.0, 10.0, 10.0])
+    seis.write_wavelet(t + "/wav", np.ones(nt, np.float32), dt=0.004)
+    hd = seis.empty_headers(n)
+    hd["n1"], hd["d1"], hd["gx"], hd["gy"] = nt, 0.004, h["mx"], h["my"]
+    for k in ("ux", "uy", "uz"):
+        seis.write(f"{t}/{k}", np.zeros((n, nt), np.float32), hd, [nt, nx, ny], [0.0] * 3, [0.004, 10.0, 10.0])
+    lib = C.CDLL(os.path.join(os.path.dirname(gpu_lib.LIB_PATH), "shotewem.so"))
+    lib.main.argtypes = [C.c_int, C.POINTER(C.c_char_p)]
+    args = ["0", "adj=y"] + [f"{k}={t}/{k}" for k in ("ux", "uy", "uz", "mpp", "mps1", "mps2", "vp", "vs", "wav")]
+    argv = (C.c_char_p * len(args))(*[a.encode() for a in args])
+    assert lib.main(len(args), argv) == gpu_lib._lib.WEM_ERR_ARG
+    assert "invalid grid" in gpu_lib.lib().wem_last_error().decode()
