@@ -165,3 +165,26 @@ def test_shotewem_main_3d_grid_spacing_from_first_two_traces(gpu_lib, tmp_path):
     argv = (C.c_char_p * len(args))(*[a.encode() for a in args])
     assert lib.main(len(args), argv) == gpu_lib._lib.WEM_ERR_ARG
     assert "invalid grid" in gpu_lib.lib().wem_last_error().decode()
+
+
+def test_elastic_3d_argument_checks_need_no_device(gpu_lib):
+    """wem_elastic on a 3-D grid checks its sizes and source positions before any device
+    work: planes whose sides are not powers of two in [64, 1024] give WEM_ERR_SIZE, and a
+    source off the grid in y gives WEM_ERR_ARG."""
+    import numpy as np
+    from wemgpu._lib import WemError, WEM_ERR_ARG, WEM_ERR_SIZE
+    p = dict(nt=16, dt=0.004, nmx=32, omx=0.0, dmx=10.0, nmy=32, omy=0.0, dmy=10.0, nz=4, oz=0.0, dz=10.0,
+             fmin=3.0, fmax=30.0, padt=2, padx=2)
+    wav = np.ones(16, np.float32)
+
+    def call(q, sx, sy):
+        n = q["nmx"] * q["nmy"]
+        v = np.full((n, q["nz"]), 2000.0, np.float32)
+        z = np.zeros((len(sx), n, q["nt"]), np.float32)
+        with pytest.raises(WemError) as e:
+            gpu_lib.elastic(q, v, v / 1.8, wav, sx, sy=sy, ux=z, uz=z, adj=True)
+        return e.value.code
+
+    assert call(dict(p, nmx=40, nmy=24), [100.0], [100.0]) == WEM_ERR_SIZE  # 80 x 48 planes
+    assert call(dict(p, nmx=1024, nmy=32), [100.0], [100.0]) == WEM_ERR_SIZE  # 2048 x 64 planes
+    assert call(p, [100.0], [1e6]) == WEM_ERR_ARG
