@@ -360,7 +360,7 @@ def kernel_source_sha(names=KERNEL_SOURCES) -> str:
 def recorded_traffic(workload: str):
     """Per-launch DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of the depth
     kernel for a workload, from the committed ncu summary (profiles/dram_traffic.json).
-    A record whose kernel-source hash differs from the sources of this build is returned
+    A record whose kernel-source hash differs from the current kernel sources is returned
     with "stale": True (its bytes describe an older kernel)."""
     try:
         with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
@@ -969,8 +969,8 @@ def main():
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        # the CPU leg: the reference's algorithm timed on the host cores, and the FP64
-        # oracle as the checker of the image error
+        # the CPU leg: the reference's algorithm timed on the host cores, and the image
+        # error measured against the FP64 oracle
         kept = {}
         line["cpu_baseline"] = cpu_baseline(c, keep=kept)
         if not args.no_accuracy:

@@ -37,7 +37,7 @@ extern "C" {
    printf on I/O failure (seismic.c:277-289, 323-337). */
 #define WEM_OK 0
 #define WEM_ERR_ARG (-1)      /* invalid or missing argument */
-#define WEM_ERR_SIZE (-2)     /* size this build does not support (e.g. nkx not a power of two) */
+#define WEM_ERR_SIZE (-2)     /* size the library does not support (e.g. a 3-D plane side not a power of two) */
 #define WEM_ERR_CUDA (-3)     /* a CUDA runtime call failed */
 #define WEM_ERR_TIMEOUT (-4)  /* a bounded device-side wait ran out */
 #define WEM_ERR_IO (-5)       /* seis file could not be read or written */

@@ -1,7 +1,7 @@
 """oracle/oracle.py -- TEST INFRASTRUCTURE (CPU oracle), never the product path.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
-module, and only as the checker or the timed CPU baseline.
+module, and only to check results or as the timed CPU baseline.
 
 ctypes access to
   * oracle/liboracle.so   -- the C restatements of the reference operator
