@@ -95,6 +95,16 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
 
     float2 *slot = a.slots + (size_t)blockIdx.x * a.nz * a.nmx;
     const int nitems = a.ngroups * a.nwf;
+    // split-step: a second set of depth tables after the shared-memory layout. Where a shot group
+    // is part-filled (a one-shot survey leaves all but one slot empty), the empty slots' teams
+    // build the next depth's tables into the other set while the live teams run the current
+    // depth, so that the table build leaves the depth chain's critical path.
+    Smem<N, PSPI, BLU> sm1 = sm;
+    if constexpr (!PSPI && !TC) {
+        sm1.ph = reinterpret_cast<float2 *>(reinterpret_cast<char *>(smem_raw) +
+                                            mig_smem_bytes<N>(false, a.nref, a.nmx, 2 * S, false, false, BLU));
+        sm1.corr = sm1.ph + ph_entries<N, BLU>(false, a.nref);
+    }
     const int nmx = a.nmx;
     bool tables_free = true;  // no thread still reads the tables of the previous step
 
@@ -107,6 +117,20 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
         const float w = __fmul_rn((float)iw, a.dw);        // w = iw*dw, wem.c:228
         const float w2 = __fmul_rn(w, w);
         const float factor = iw == 0 ? 1.f : 2.f;          // wem.c:226-227
+
+        // split-step, part-filled group: the tables of depth 0 by every thread, the later ones by
+        // the empty slots' teams (helper index hid of nhelp) one depth ahead
+        const int nlive = a.nshot - g * S;  // live slots of the group (CTA-uniform)
+        const bool helped = !PSPI && !TC && nlive < S;
+        const int nhelp = 2 * (S - nlive) * T;
+        const int hid = ((is_src ? 0 : S - nlive) + (sg - nlive)) * T + t;
+        if constexpr (!PSPI && !TC) {
+            if (helped) {
+                if (!tables_free) __syncthreads();
+                build_tables<N, PSPI, INTERP, BLU, TC>(a, sm, w, w2, 0, tid, NT);
+                __syncthreads();
+            }
+        }
 
         // initial rows (wem.c:230-233): source spike at igx, receiver spectra
         float2 v[16];
@@ -176,6 +200,17 @@ __global__ void __launch_bounds__(2 * S * (N / 16), 1) wem_migrate_kernel(const 
                             step_mig_tail<N, PSPI, INTERP, TC>(v, is_src, a, sm, xbuf, sacc, t, sync, &tc, um, inv_s);
                         }
                     }
+                }
+            } else if (!PSPI && !TC && helped) {
+                if constexpr (!PSPI && !TC) {
+                    // this depth's tables are complete (built one depth ahead), the previous
+                    // depth's set and every exchange buffer are free (the image sum of the
+                    // previous depth reads the receivers' buffers)
+                    __syncthreads();
+                    const Smem<N, PSPI, BLU> &cur = (iz & 1) ? sm1 : sm;
+                    if (!shot_ok && iz + 1 < a.nz)
+                        build_tables<N, PSPI, INTERP, BLU, TC>(a, (iz & 1) ? sm : sm1, w, w2, iz + 1, hid, nhelp);
+                    if (active) step_mig<N, PSPI, INTERP, TC>(v, is_src, a, cur, xbuf, sacc, t, sync, &tc, ref_mask(a, iz));
                 }
             } else {
                 if (!tables_free) __syncthreads();
@@ -411,6 +446,9 @@ int mig_launch(int wide, int pspi, int interp, int nref, int nmx, const MigArgs 
     *S = s_;
     *threads = 2 * s_ * SH::T;
     *smem = mig_smem_bytes<N>(pspi != 0, nref, nmx, 2 * s_, tc != 0, form == MIG_FORM_PAIRED, form == MIG_FORM_BLU);
+    if (!pspi && !tc)  // split-step: the second set of depth tables (wem_migrate_kernel)
+        *smem += sizeof(float2) * ((size_t)(form == MIG_FORM_BLU ? ph_entries<N, true>(false, nref) : ph_entries<N>(false, nref)) +
+                                   (size_t)((nmx + 1) & ~1));
     if (form == MIG_FORM_BLU) {
         if (!wide) return -2;
         if (!a && !bps) return 0;
